@@ -1,0 +1,206 @@
+/*
+ * gpat_engine.h -- C ABI of the GB300 particle-mover engine for GPAT
+ * (stochastic integration of Parker's transport equation).
+ *
+ * The entry points replace, one for one, the Fortran module procedures the
+ * reference driver calls on its hot path (paths are relative to the
+ * xiaocanli/stochastic-parker project root).  The Fortran driver reaches them
+ * through an ISO_C_BINDING interface module; every argument is a plain
+ * pointer, integer or double, and no call retains a caller pointer.
+ *
+ * Conventions
+ *  - Every call returns GPAT_OK (0) or a negative GPAT_ERR_* code;
+ *    gpat_last_error() gives a message.  Nothing throws across the ABI.
+ *  - Host buffers stay owned by the caller; device memory is owned by the
+ *    handle.  Calls are synchronous on return.
+ *  - One host thread per handle; a handle is bound to one CUDA device.
+ *  - Frame indices (ct_mhd, mhd_tframe) are 1-based as in the reference.
+ *
+ * Reference differences that are part of the contract
+ *  - Random increments come from Philox-4x32-10 keyed by (seed, particle
+ *    tags, push counter) instead of per-thread MT19937 streams, so results
+ *    are reproducible for any launch shape.
+ *  - remove_particles keeps the survivors in their original order; the
+ *    reference swaps removed particles to the end.  Particle sets, counters
+ *    and histograms are unaffected.
+ *  - leak, leak_negp and all histogram weights are accumulated as exact
+ *    128-bit fixed point (64 fraction bits), so sums do not depend on order.
+ */
+#ifndef GPAT_ENGINE_H
+#define GPAT_ENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPAT_OK 0
+#define GPAT_ERR_ARG (-1)          /* invalid argument or NULL pointer          */
+#define GPAT_ERR_OOM (-2)          /* device or host allocation failed          */
+#define GPAT_ERR_CAPACITY (-3)     /* nptl_max reached (data kept up to the cap) */
+#define GPAT_ERR_TIMEOUT (-4)      /* a bounded device wait gave up              */
+#define GPAT_ERR_CUDA (-5)         /* CUDA runtime error                         */
+#define GPAT_ERR_UNSUPPORTED (-6)  /* option outside the engine's scope          */
+#define GPAT_ERR_IO (-7)           /* file missing, short or malformed           */
+#define GPAT_ERR_STATE (-8)        /* call out of order (e.g. no fields yet)     */
+#define GPAT_ERR_DEVICE (-9)       /* device status word set (NaN / index guard) */
+
+#define GPAT_PREC_FP64 0    /* FP64 everywhere, reference operation order      */
+#define GPAT_PREC_MIXED 1   /* FP32 fields/kappa/drift, FP64 accumulators      */
+
+#define GPAT_NOISE_UNIFORM 0  /* (2u-1)*sqrt(3), the reference's increment    */
+#define GPAT_NOISE_GAUSS 1    /* Box-Muller Gaussian increments               */
+
+#define GPAT_COUNT_FLAG_INBOX 1
+#define GPAT_COUNT_FLAG_OTHERS 0
+
+/* mhd_configuration: same fields, order and binary layout (13 doubles then
+ * 13 int32, 156 bytes) as mhd_config.dat; src/modules/mhd_config.f90:16-27. */
+typedef struct gpat_mhd_config {
+    double dx, dy, dz, xmin, ymin, zmin, xmax, ymax, zmax, lx, ly, lz, dt_out;
+    int32_t nx, ny, nz, nxs, nys, nzs, topox, topoy, topoz, nvar, bcx, bcy, bcz;
+} gpat_mhd_config_t;
+
+/* Run parameters on the mover path.  The first block mirrors conf.dat as read
+ * by read_particle_params (particle_module.f90:2778-2878) plus the drift,
+ * boundary and diagnostics settings (set_drift_parameters :318-328,
+ * read_particle_boundary_conditions simulation_setup.f90:104-150,
+ * read_diagnostics_params diagnostics.f90:2049-2100). */
+typedef struct gpat_params {
+    double b0, p0, pmin, pmax;
+    double gamma_turb, pindex, kpara0, kret, dt_min_rel, dt_max_rel;
+    double acc_region[6];
+    double drift1, drift2;
+    int32_t momentum_dependency, mag_dependency, acc_region_flag, charge;
+    int32_t check_drift_2d, ndim, pbcx, pbcy, pbcz, npp_global;
+    uint64_t seed;
+    int32_t noise;              /* GPAT_NOISE_*                                */
+    int32_t precision;          /* GPAT_PREC_*                                 */
+    int64_t nptl_max;           /* particle capacity (init_particles)          */
+    int32_t time_interp;        /* 1: two field frames, linear in time         */
+    /* Options of the reference that this engine rejects with
+     * GPAT_ERR_UNSUPPORTED when non-zero: dpp_wave, dpp_shear, deltab_flag,
+     * correlation_flag, include_3rd_dim, spherical_coord, nonuniform_grid. */
+    int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
+    int32_t spherical_coord, nonuniform_grid;
+} gpat_params_t;
+
+/* particle_type (particle_module.f90:38-50) as structure-of-arrays.  rng_ctr
+ * is the per-particle Philox push counter that replaces the MT19937 state. */
+typedef struct gpat_particles {
+    double *x, *y, *z, *p, *v, *mu, *weight, *t, *dt;
+    int8_t *split_times, *count_flag;
+    int32_t *origin, *nsteps_tracked, *nsteps_pushed, *tag_injected, *tag_splitted;
+    uint32_t *rng_ctr;
+} gpat_particles_t;
+
+/* Module-level state of particle_module (:65-79) plus engine statistics. */
+typedef struct gpat_counters {
+    int64_t nptl_current, nptl_split, nptl_escaped, tag_max;
+    double leak, leak_negp;                     /* exact sums, rounded once   */
+    uint64_t leak_hi, leak_lo, leak_negp_hi, leak_negp_lo;  /* raw fixed point */
+    uint64_t steps;                             /* particle pushes, cumulative */
+    double last_mover_ms;                       /* device time of last mover  */
+    uint64_t last_mover_steps;
+} gpat_counters_t;
+
+typedef struct gpat_handle gpat_handle_t;
+
+const char *gpat_version(void);
+
+/* conf.dat reader.  Replaces read_particle_params (particle_module.f90:
+ * 2778-2878) + read_config.f90:20-44: keys are searched forward from the
+ * previous match without rewinding, by substring; a key that is not found
+ * reads as -1.  pindex = 3 - gamma_turb.  Also reads pbcx/pbcy/pbcz
+ * (simulation_setup.f90:104-150, from the start of the file) and
+ * npp_global (diagnostics.f90:2049-2100).  Fields it does not read keep
+ * the values already in *params. */
+int gpat_read_particle_params(const char *conf_path, gpat_params_t *params);
+/* get_variable (read_config.f90:20-44) for a single key from the file start. */
+int gpat_get_variable(const char *conf_path, const char *key, double *value);
+/* load_mhd_config (mhd_config.f90:139-148): 156-byte raw record. */
+int gpat_load_mhd_config(const char *path, gpat_mhd_config_t *cfg);
+
+/* init_particles + init_field_data + init_particle_distributions
+ * (particle_module.f90:177-258, mhd_data_parallel.f90:66-105,
+ * diagnostics.f90:178-226): allocates all device state on `device`. */
+int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int device,
+                gpat_handle_t **out);
+/* free_particles + free_field_data. */
+int gpat_destroy(gpat_handle_t *h);
+const char *gpat_last_error(const gpat_handle_t *h);
+
+/* tstamps_mhd: load_tstamps_mhd / calc_tstamps_mhd (mhd_config.f90:218-271).
+ * tstamps[0] is the reference's tstamps_mhd(1). */
+int gpat_set_tstamps(gpat_handle_t *h, const double *tstamps, int n);
+int gpat_calc_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end);
+
+/* read_field_data_parallel (mhd_data_parallel.f90:224-300) from memory:
+ * farray is the Fortran-order (nvar, nxg, nyg, nzg) single-precision array,
+ * nvar = 8 (raw file layout vx vy vz rho bx by bz |B|) or 32 (with the 24
+ * gradients).  var_flag 0 fills farray1, otherwise farray2. */
+int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nvar);
+/* read_field_data_parallel from a raw mhd_data_XXXX file (8 vars). */
+int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag);
+/* calc_fields_gradients (mhd_data_parallel.f90:504-610) on the device. */
+int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag);
+/* copy_fields (mhd_data_parallel.f90:1920-1926): farray1 = farray2. */
+int gpat_copy_fields(gpat_handle_t *h);
+/* Copies a device field array (32 vars per cell, Fortran order) to the host. */
+int gpat_get_fields(gpat_handle_t *h, int var_flag, float *farray);
+
+/* inject_particles_spatial_uniform + inject_one_particle
+ * (particle_module.f90:385-530), one rank: part_box = {xmin, ymin, zmin,
+ * xmax, ymax, zmax}; t = tstamps(ct_mhd) + U * (tstamps(ct_mhd+1) -
+ * tstamps(ct_mhd)).  Adds min(nptl, nptl_max - nptl_current) particles and
+ * returns GPAT_ERR_CAPACITY when it had to stop at the cap. */
+int gpat_inject_particles_spatial_uniform(gpat_handle_t *h, int64_t nptl, double dt,
+                                          int dist_flag, double particle_v0, int ct_mhd,
+                                          const double part_box[6], double power_index);
+/* Injection on the plane x = xpos at t = tstamps(ct_mhd), with the draw order
+ * of inject_particles_at_shock (particle_module.f90:542-633).  It replaces
+ * the reference's shock locator (interp_shock_location), whose weights use
+ * dpy for both ry and rz (:580-581). */
+int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, double dt,
+                               int dist_flag, double particle_v0, int ct_mhd,
+                               double power_index);
+
+/* Particle exchange with the host (e.g. restart files, the Fortran ptls
+ * array).  put replaces the whole particle set. */
+int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n);
+int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity,
+                       int64_t *n);
+
+/* particle_mover (particle_module.f90:1846-1974) on one rank:
+ * mover cycle (:1481-1833), remove_particles, boundary pass on the exact
+ * box, remove_particles.  focused_transport and nlgc must be 0.
+ * mhd_tframe indexes tstamps (t0 = tstamps(mhd_tframe)). */
+int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc,
+                        double kperp_kpara, int nsteps_interval, int mhd_tframe,
+                        int num_fine_steps, int dump_escaped_dist);
+/* split_particle (particle_module.f90:5430-5480): children appended in
+ * parent order; stops at nptl_max like the reference. */
+int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
+                        int nsteps_interval);
+/* Global f(p) of calc_particle_distributions (diagnostics.f90:738-780):
+ * fglobal[npp_global] weighted counts (may be NULL) and counts[npp_global]
+ * particle numbers (may be NULL).  Bins are exact. */
+int gpat_calc_particle_distributions(gpat_handle_t *h, double *fglobal, uint64_t *counts);
+/* pbins_edges_global (diagnostics.f90:194-204): npp_global + 1 values. */
+int gpat_pbins_edges(gpat_handle_t *h, double *edges);
+/* quick_check (diagnostics.f90:116-170) for one rank: out = {nptl_current,
+ * nptl_split, sum of weights, leak, leak_negp, pdt_min, pdt_max, pdt_avg}. */
+int gpat_quick_check(gpat_handle_t *h, double out[8]);
+int gpat_get_counters(gpat_handle_t *h, gpat_counters_t *out);
+/* Restores module state after a restart (save/read_particle_module_state). */
+int gpat_set_counters(gpat_handle_t *h, const gpat_counters_t *in);
+
+/* The handle's CUDA stream (a cudaStream_t) for callers that time or
+ * order work around the engine. */
+void *gpat_stream(gpat_handle_t *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,994 @@
+/*
+ * gpat_oracle.c -- CPU FP64 restatement of the reference's Parker mover.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline; see
+ * gpat_oracle.h).  Parity is unpinned by reference tests: the reference has
+ * none and cannot be built here.
+ *
+ * Every routine cites the Fortran routine it restates (paths relative to the
+ * reference project root).  Expressions keep Fortran's left-to-right order;
+ * build with -ffp-contract=off.
+ */
+#include "gpat_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Counter-based RNG: Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).    */
+/* ------------------------------------------------------------------------ */
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t m0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t m1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(m0 >> 32), lo0 = (uint32_t)m0;
+        uint32_t hi1 = (uint32_t)(m1 >> 32), lo1 = (uint32_t)m1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* 53-bit uniform on [0,1) from two 32-bit words. The reference draws
+ * genrand_double1 (closed [0,1]); random_number_generator.f90:97-101. */
+double orc_u01(uint32_t a, uint32_t b)
+{
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Exact weight sums: unsigned 128-bit fixed point, 64 fraction bits.       */
+/* ------------------------------------------------------------------------ */
+static void fixed_split(double w, uint64_t *h, uint64_t *l)
+{
+    double fl = floor(w);
+    *h = (uint64_t)fl;
+    *l = (uint64_t)((w - fl) * 18446744073709551616.0);
+}
+
+void orc_fixed_add(uint64_t *hi, uint64_t *lo, double w)
+{
+    uint64_t h, l;
+    if (w >= 0.0) {
+        fixed_split(w, &h, &l);
+        uint64_t old = *lo;
+        *lo = old + l;
+        *hi += h + (*lo < old ? 1u : 0u);
+    } else {
+        fixed_split(-w, &h, &l);
+        uint64_t old = *lo;
+        *lo = old - l;
+        *hi -= h + (old < l ? 1u : 0u);
+    }
+}
+
+double orc_fixed_to_double(uint64_t hi, uint64_t lo)
+{
+    return (double)hi + (double)lo * (1.0 / 18446744073709551616.0);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Field gradients: mhd_data_parallel.f90:504-610 (calc_fields_gradients).   */
+/* farray is (32, nxg, nyg, nzg) with the variable index fastest; the first  */
+/* 8 variables are vx vy vz rho bx by bz |B|; variable v's d/dx, d/dy, d/dz  */
+/* go to 8+3v, 8+3v+1, 8+3v+2.  Differences are single precision, scaled by */
+/* the double 0.5/dx and rounded back to single.                            */
+/* ------------------------------------------------------------------------ */
+#define FA(a, v, i, j, k) (a)[(size_t)(v) + 32u * ((size_t)(i) + (size_t)nxg * ((size_t)(j) + (size_t)nyg * (size_t)(k)))]
+
+void orc_calc_fields_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
+                               double dx, double dy, double dz)
+{
+    const double idxh = 0.5 / dx, idyh = 0.5 / dy, idzh = 0.5 / dz;
+    for (int k = 0; k < nzg; ++k)
+        for (int j = 0; j < nyg; ++j)
+            for (int i = 0; i < nxg; ++i)
+                for (int v = 0; v < 8; ++v) {
+                    float d;
+                    if (i == 0) {
+                        float t = -(3.0f * FA(a, v, 0, j, k));
+                        t = t + 4.0f * FA(a, v, 1, j, k);
+                        t = t - FA(a, v, 2, j, k);
+                        d = (float)((double)t * idxh);
+                    } else if (i == nxg - 1) {
+                        float t = 3.0f * FA(a, v, nxg - 1, j, k);
+                        t = t - 4.0f * FA(a, v, nxg - 2, j, k);
+                        t = t + FA(a, v, nxg - 3, j, k);
+                        d = (float)((double)t * idxh);
+                    } else {
+                        float t = FA(a, v, i + 1, j, k) - FA(a, v, i - 1, j, k);
+                        d = (float)((double)t * idxh);
+                    }
+                    FA(a, 8 + 3 * v, i, j, k) = d;
+                    if (nyg > 1) {
+                        if (j == 0) {
+                            float t = -(3.0f * FA(a, v, i, 0, k));
+                            t = t + 4.0f * FA(a, v, i, 1, k);
+                            t = t - FA(a, v, i, 2, k);
+                            d = (float)((double)t * idyh);
+                        } else if (j == nyg - 1) {
+                            float t = 3.0f * FA(a, v, i, nyg - 1, k);
+                            t = t - 4.0f * FA(a, v, i, nyg - 2, k);
+                            t = t + FA(a, v, i, nyg - 3, k);
+                            d = (float)((double)t * idyh);
+                        } else {
+                            float t = FA(a, v, i, j + 1, k) - FA(a, v, i, j - 1, k);
+                            d = (float)((double)t * idyh);
+                        }
+                        FA(a, 8 + 3 * v + 1, i, j, k) = d;
+                    }
+                    if (nzg > 1 && ndim == 3) {
+                        if (k == 0) {
+                            float t = -(3.0f * FA(a, v, i, j, 0));
+                            t = t + 4.0f * FA(a, v, i, j, 1);
+                            t = t - FA(a, v, i, j, 2);
+                            d = (float)((double)t * idzh);
+                        } else if (k == nzg - 1) {
+                            float t = 3.0f * FA(a, v, i, j, nzg - 1);
+                            t = t - 4.0f * FA(a, v, i, j, nzg - 2);
+                            t = t + FA(a, v, i, j, nzg - 3);
+                            d = (float)((double)t * idzh);
+                        } else {
+                            float t = FA(a, v, i, j, k + 1) - FA(a, v, i, j, k - 1);
+                            d = (float)((double)t * idzh);
+                        }
+                        FA(a, 8 + 3 * v + 2, i, j, k) = d;
+                    }
+                }
+}
+
+/* ------------------------------------------------------------------------ */
+/* get_interp_paramters: particle_module.f90:642-674.  pos is returned as   */
+/* the reference's 1-based Fortran index (ghost cells start at -1).         */
+/* ------------------------------------------------------------------------ */
+void orc_get_interp_paramters(int ndim, double px, double py, double pz,
+                              int32_t pos[3], double w[8])
+{
+    double rx, ry, rz;
+    pos[0] = (int32_t)floor(px) + 1;
+    if (ndim == 2) {
+        pos[1] = (int32_t)floor(py) + 1;
+        pos[2] = 1;
+        ry = (py - (double)pos[1]) + 1.0;
+        rz = 0.0;
+    } else {
+        pos[1] = (int32_t)floor(py) + 1;
+        pos[2] = (int32_t)floor(pz) + 1;
+        ry = (py - (double)pos[1]) + 1.0;
+        rz = (pz - (double)pos[2]) + 1.0;
+    }
+    rx = (px - (double)pos[0]) + 1.0;
+    double rx1 = 1.0 - rx, ry1 = 1.0 - ry, rz1 = 1.0 - rz;
+    w[0] = rx1 * ry1 * rz1;
+    w[1] = rx * ry1 * rz1;
+    w[2] = rx1 * ry * rz1;
+    w[3] = rx * ry * rz1;
+    w[4] = rx1 * ry1 * rz;
+    w[5] = rx * ry1 * rz;
+    w[6] = rx1 * ry * rz;
+    w[7] = rx * ry * rz;
+}
+
+/* ------------------------------------------------------------------------ */
+/* interp_fields: mhd_data_parallel.f90:1751-1804.  Fortran index i maps to */
+/* C index i+1 in x and y; z is i+1 in 3D and 0 in 2D (declared 1:1).       */
+/* ------------------------------------------------------------------------ */
+void orc_interp_fields(const float *f1, const float *f2, int time_interp, int ndim,
+                       int nxg, int nyg, const int32_t pos[3], const double w[8],
+                       double rt, double fields[32])
+{
+    const int ix = pos[0] + 1, iy = pos[1] + 1;
+    const int iz = (ndim == 3) ? pos[2] + 1 : 0;
+    const int ze = (ndim == 3) ? 1 : 0;
+    double fields2[32];
+    for (int v = 0; v < 32; ++v) { fields[v] = 0.0; fields2[v] = 0.0; }
+    for (int k = 0; k <= ze; ++k)
+        for (int j = 0; j <= 1; ++j)
+            for (int i = 0; i <= 1; ++i) {
+                const int idx = k * 4 + j * 2 + i;
+                const size_t c = 32u * ((size_t)(ix + i) + (size_t)nxg * ((size_t)(iy + j) + (size_t)nyg * (size_t)(iz + k)));
+                for (int v = 0; v < 32; ++v) fields[v] = fields[v] + (double)f1[c + v] * w[idx];
+                if (time_interp)
+                    for (int v = 0; v < 32; ++v) fields2[v] = fields2[v] + (double)f2[c + v] * w[idx];
+            }
+    if (time_interp)
+        for (int v = 0; v < 32; ++v) fields[v] = fields[v] * (1.0 - rt) + fields2[v] * rt;
+}
+
+/* ------------------------------------------------------------------------ */
+/* calc_spatial_diffusion_coefficients: particle_module.f90:2208-2450 for   */
+/* Parker transport without delta-B or correlation-length inputs.  kappa    */
+/* follows kappa_type (:93-104): knorm_para knorm_perp kpara kperp skpara   */
+/* skperp skpara_perp kxx kyy kzz kxy kxz kyz dkxx_dx dkyy_dy dkzz_dz       */
+/* dkxy_dx dkxy_dy dkxz_dx dkxz_dz dkyz_dy dkyz_dz.                         */
+/* ------------------------------------------------------------------------ */
+enum { K_KNORM_PARA, K_KNORM_PERP, K_KPARA, K_KPERP, K_SKPARA, K_SKPERP, K_SKPARA_PERP,
+       K_KXX, K_KYY, K_KZZ, K_KXY, K_KXZ, K_KYZ, K_DKXX_DX, K_DKYY_DY, K_DKZZ_DZ,
+       K_DKXY_DX, K_DKXY_DY, K_DKXZ_DX, K_DKXZ_DZ, K_DKYZ_DY, K_DKYZ_DZ };
+
+void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p,
+                                             const double f[32], double kap[22])
+{
+    const double bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
+    const double ib2 = ib1 * ib1;
+    const double ib3 = ib1 * ib2;
+    double knorm_para = 1.0, knorm;
+    if (pr->mag_dependency == 1) knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
+    if (pr->momentum_dependency == 1) knorm = knorm_para * pow(p / pr->p0, pr->pindex);
+    else knorm = knorm_para;
+    const double kpara = pr->kpara0 * knorm;
+    const double kperp = kpara * pr->kret;
+    kap[K_KNORM_PARA] = knorm_para;
+    kap[K_KNORM_PERP] = knorm_para;
+    kap[K_KPARA] = kpara;
+    kap[K_KPERP] = kperp;
+    kap[K_SKPARA] = sqrt(2.0 * kpara);
+    kap[K_SKPERP] = sqrt(2.0 * kperp);
+    kap[K_SKPARA_PERP] = sqrt(2.0 * (kpara - kperp));
+    const double kpp = kpara - kperp;
+    if (pr->ndim == 2) {
+        const double dbx_dx = f[20], dbx_dy = f[21], dby_dx = f[23], dby_dy = f[24];
+        const double db_dx = f[29], db_dy = f[30];
+        double dkdx = 0.0, dkdy = 0.0;
+        if (pr->mag_dependency == 1) {
+            dkdx = db_dx * ib1 * (pr->gamma_turb - 2.0);
+            dkdy = db_dy * ib1 * (pr->gamma_turb - 2.0);
+        }
+        kap[K_DKXX_DX] = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2 +
+                         2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
+        kap[K_DKYY_DY] = kperp * dkdy + kpp * dkdy * (by * by) * ib2 +
+                         2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3;
+        kap[K_DKXY_DX] = kpp * dkdx * bx * by * ib2 +
+                         kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0 * bx * by * db_dx * ib3);
+        kap[K_DKXY_DY] = kpp * dkdy * bx * by * ib2 +
+                         kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0 * bx * by * db_dy * ib3);
+        kap[K_KXX] = kperp + kpp * bx * bx * ib2;
+        kap[K_KYY] = kperp + kpp * by * by * ib2;
+        kap[K_KXY] = kpp * bx * by * ib2;
+        kap[K_KZZ] = 0.0; kap[K_KXZ] = 0.0; kap[K_KYZ] = 0.0;
+        kap[K_DKZZ_DZ] = 0.0; kap[K_DKXZ_DX] = 0.0; kap[K_DKXZ_DZ] = 0.0;
+        kap[K_DKYZ_DY] = 0.0; kap[K_DKYZ_DZ] = 0.0;
+    } else {
+        const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
+        const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
+        const double dbz_dx = f[26], dbz_dy = f[27], dbz_dz = f[28];
+        const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
+        double dkdx = 0.0, dkdy = 0.0, dkdz = 0.0;
+        if (pr->mag_dependency == 1) {
+            /* 3D branch has no 1/B factor here (reference :2406-2408). */
+            dkdx = db_dx * (pr->gamma_turb - 2.0);
+            dkdy = db_dy * (pr->gamma_turb - 2.0);
+            dkdz = db_dz * (pr->gamma_turb - 2.0);
+        }
+        kap[K_DKXX_DX] = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2 +
+                         2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
+        kap[K_DKYY_DY] = kperp * dkdy + kpp * dkdy * (by * by) * ib2 +
+                         2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3;
+        kap[K_DKZZ_DZ] = kperp * dkdz + kpp * dkdz * (bz * bz) * ib2 +
+                         2.0 * kpp * bz * (dbz_dz * b - bz * db_dz) * ib3;
+        kap[K_DKXY_DX] = kpp * dkdx * bx * by * ib2 +
+                         kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0 * bx * by * db_dx * ib3);
+        kap[K_DKXY_DY] = kpp * dkdy * bx * by * ib2 +
+                         kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0 * bx * by * db_dy * ib3);
+        kap[K_DKXZ_DX] = kpp * dkdx * bx * bz * ib2 +
+                         kpp * ((dbx_dx * bz + bx * dbz_dx) * ib2 - 2.0 * bx * bz * db_dx * ib3);
+        kap[K_DKXZ_DZ] = kpp * dkdz * bx * bz * ib2 +
+                         kpp * ((dbx_dz * bz + bx * dbz_dz) * ib2 - 2.0 * bx * bz * db_dz * ib3);
+        kap[K_DKYZ_DY] = kpp * dkdy * by * bz * ib2 +
+                         kpp * ((dby_dy * bz + by * dbz_dy) * ib2 - 2.0 * by * bz * db_dy * ib3);
+        kap[K_DKYZ_DZ] = kpp * dkdz * by * bz * ib2 +
+                         kpp * ((dby_dz * bz + by * dbz_dz) * ib2 - 2.0 * by * bz * db_dz * ib3);
+        kap[K_KXX] = kperp + kpp * bx * bx * ib2;
+        kap[K_KYY] = kperp + kpp * by * by * ib2;
+        kap[K_KZZ] = kperp + kpp * bz * bz * ib2;
+        kap[K_KXY] = kpp * bx * by * ib2;
+        kap[K_KXZ] = kpp * bx * bz * ib2;
+        kap[K_KYZ] = kpp * by * bz * ib2;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Mover.                                                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct mover_ctx {
+    const orc_params *pr;
+    const float *f1, *f2;
+    int time_interp, ndim, nxg, nyg;
+    double dx, dy, dz;
+    double xmin, ymin, zmin;                   /* fconfig box (exact)      */
+    double xmin1, xmax1, ymin1, ymax1, zmin1, zmax1;  /* half-cell-extended */
+    double cfg_xmin, cfg_ymin, cfg_zmin, cfg_lx, cfg_ly, cfg_lz;
+    double dt_min, dt_max, t0, dtf;
+    uint32_t key[2];
+} mover_ctx;
+
+typedef struct ptl_state {
+    double x, y, z, p, t, dt, weight;
+    int flag;
+    int32_t nsteps_pushed, tag_injected, tag_splitted;
+    uint32_t rng_ctr;
+} ptl_state;
+
+typedef struct thread_acc {
+    uint64_t leak_hi, leak_lo, negp_hi, negp_lo, steps;
+} thread_acc;
+
+/* Four unit-variance increments for one push, drawn in the reference's order
+ * ran1, ran2, ran3 (position) then ran1 again (momentum); :3546-3590. */
+static void push_noise(const mover_ctx *c, ptl_state *s, double r[4])
+{
+    uint32_t w[8];
+    uint32_t ctr[4] = {s->rng_ctr, 0u, (uint32_t)s->tag_injected, (uint32_t)s->tag_splitted};
+    orc_philox4x32_10(ctr, c->key, w);
+    ctr[1] = 1u;
+    orc_philox4x32_10(ctr, c->key, w + 4);
+    s->rng_ctr += 1u;
+    const double u0 = orc_u01(w[0], w[1]), u1 = orc_u01(w[2], w[3]);
+    const double u2 = orc_u01(w[4], w[5]), u3 = orc_u01(w[6], w[7]);
+    if (c->pr->noise == 0) {
+        const double sqrt3 = sqrt(3.0);
+        r[0] = (2.0 * u0 - 1.0) * sqrt3;
+        r[1] = (2.0 * u1 - 1.0) * sqrt3;
+        r[2] = (2.0 * u2 - 1.0) * sqrt3;
+        r[3] = (2.0 * u3 - 1.0) * sqrt3;
+    } else {
+        const double twopi = 6.283185307179586;
+        const double ra = sqrt(-2.0 * log(1.0 - u0)), rb = sqrt(-2.0 * log(1.0 - u2));
+        r[0] = ra * cos(twopi * u1);
+        r[1] = ra * sin(twopi * u1);
+        r[2] = rb * cos(twopi * u3);
+        r[3] = rb * sin(twopi * u3);
+    }
+}
+
+/* particle_in_acceleration_region: particle_module.f90:2885-2906. */
+static int in_acc_region(const mover_ctx *c, const ptl_state *s)
+{
+    const double *a = c->pr->acc_region;
+    const double xn = (s->x - c->cfg_xmin) / c->cfg_lx;
+    int in = (xn >= a[0]) && (xn <= a[1]);
+    if (c->ndim > 1) {
+        const double yn = (s->y - c->cfg_ymin) / c->cfg_ly;
+        in = in && (yn >= a[2]) && (yn <= a[3]);
+    }
+    if (c->ndim == 3) {
+        const double zn = (s->z - c->cfg_zmin) / c->cfg_lz;
+        in = in && (zn >= a[4]) && (zn <= a[5]);
+    }
+    return in;
+}
+
+static double vdrift_prefactor(const orc_params *pr, double p)
+{
+    /* 1.0 / (3 * pcharge) is single precision in the reference. */
+    const float q = 1.0f / (float)(3 * pr->charge);
+    const double t1 = pr->drift1 * pr->p0 / p;
+    const double t2 = pr->drift2 * (pr->p0 * pr->p0) / (p * p);
+    return (double)q / sqrt(t1 * t1 + t2 * t2);
+}
+
+/* Momentum update, acceleration-region mask and the 0.25 p0 floor, shared
+ * by the 2D and 3D pushes (:3591-3605, :4885-4906). */
+static void push_momentum(const mover_ctx *c, ptl_state *s, double dp_dt, double sdt,
+                          double ranp, double *deltap)
+{
+    const double dpp = 0.0;
+    double dP = dp_dt * s->dt + ranp * sqrt(2.0 * dpp) * sdt;
+    if (c->pr->acc_region_flag == 1) {
+        if (in_acc_region(c, s)) s->p = s->p + dP;
+        else dP = 0.0;
+    } else {
+        s->p = s->p + dP;
+    }
+    const double pfloor = (double)0.25f * c->pr->p0;
+    if (s->p < pfloor) {
+        s->p = s->p - dP;
+        dP = pfloor - s->p;
+        s->p = pfloor;
+    }
+    *deltap = dP;
+}
+
+/* push_particle_2d, Cartesian uniform grid: particle_module.f90:3358-3606. */
+static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
+                    int fixed_dt, double *deltax, double *deltay, double *deltaz, double *deltap)
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double dvx_dx = f[8], dvy_dy = f[12];
+    const double dxm = c->dx, dym = c->dy;
+    const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    const double dbz_dx = f[26], dbz_dy = f[27], db_dx = f[29], db_dy = f[30];
+    const double ib2 = ib * ib;
+    const double ib3 = ib * ib2;
+    const double vdp = vdrift_prefactor(pr, s->p);
+    const double vdx = vdp * (dbz_dy * ib2 - 2.0 * bz * db_dy * ib3);
+    const double vdy = vdp * (-(dbz_dx * ib2) + 2.0 * bz * db_dx * ib3);
+    double vdz = 0.0;
+    if (pr->check_drift_2d) {
+        const double dbx_dy = f[21], dby_dx = f[23];
+        vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
+    }
+    const double dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
+    const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY];
+    const double dz_dt = vdz;
+    const double divv = dvx_dx + dvy_dy;
+    const double dp_dt = -(s->p * divv / 3.0);
+    const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double a = 0.5 * dxm / skpara, m = a * a;
+            a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = sk / dy_dt; if (a * a < m) m = a * a;
+            a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
+            s->dt = m;
+        } else {
+            s->dt = c->dt_min;
+        }
+        if (s->dt < c->dt_min) s->dt = c->dt_min;
+        if (s->dt > c->dt_max) s->dt = c->dt_max;
+    }
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double skpp = kap[K_SKPARA_PERP];
+    const double dX = dx_dt * s->dt + r[0] * skperp * sdt + r[2] * skpp * sdt * bx * ib;
+    const double dY = dy_dt * s->dt + r[1] * skperp * sdt + r[2] * skpp * sdt * by * ib;
+    const double dZ = dz_dt * s->dt;
+    s->x = s->x + dX;
+    s->y = s->y + dY;
+    s->z = s->z + dZ;
+    s->t = s->t + s->dt;
+    *deltax = dX; *deltay = dY; *deltaz = dZ;
+    push_momentum(c, s, dp_dt, sdt, r[3], deltap);
+}
+
+/* push_particle_3d, Cartesian uniform grid: particle_module.f90:4625-4907. */
+static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
+                    int fixed_dt, double *deltax, double *deltay, double *deltaz, double *deltap)
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+    const double bxyn = sqrt(bxn * bxn + byn * byn);
+    const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
+    const double dvx_dx = f[8], dvy_dy = f[12], dvz_dz = f[16];
+    const double dxm = c->dx, dym = c->dy, dzm = c->dz;
+    const double dbx_dy = f[21], dbx_dz = f[22], dby_dx = f[23], dby_dz = f[25];
+    const double dbz_dx = f[26], dbz_dy = f[27];
+    const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
+    const double ib2 = ib * ib;
+    const double ib3 = ib * ib2;
+    const double vdp = vdrift_prefactor(pr, s->p);
+    const double vdx = vdp * ((dbz_dy - dby_dz) * ib2 - 2.0 * (bz * db_dy - by * db_dz) * ib3);
+    const double vdy = vdp * ((dbx_dz - dbz_dx) * ib2 - 2.0 * (bx * db_dz - bz * db_dx) * ib3);
+    const double vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
+    const double dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
+    const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
+    const double dz_dt = vz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
+    const double divv = dvx_dx + dvy_dy + dvz_dz;
+    const double dp_dt = -(s->p * divv / 3.0);
+    const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double a = 0.5 * dxm / skpara, m = a * a;
+            a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
+            a = 0.5 * dzm / skpara; if (a * a < m) m = a * a;
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = sk / dy_dt; if (a * a < m) m = a * a;
+            a = sk / dz_dt; if (a * a < m) m = a * a;
+            a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
+            s->dt = m;
+        } else {
+            s->dt = c->dt_min;
+        }
+        if (s->dt < c->dt_min) s->dt = c->dt_min;
+        if (s->dt > c->dt_max) s->dt = c->dt_max;
+    }
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double dX = dx_dt * s->dt +
+        (bxn * skpara * r[0] - bxn * bzn * skperp * ibxyn * r[1] - byn * skperp * ibxyn * r[2]) * sdt;
+    const double dY = dy_dt * s->dt +
+        (byn * skpara * r[0] - byn * bzn * skperp * ibxyn * r[1] + bxn * skperp * ibxyn * r[2]) * sdt;
+    const double dZ = dz_dt * s->dt + (bzn * skpara * r[0] + bxyn * skperp * r[1]) * sdt;
+    s->x = s->x + dX;
+    s->y = s->y + dY;
+    s->z = s->z + dZ;
+    s->t = s->t + s->dt;
+    *deltax = dX; *deltay = dY; *deltaz = dZ;
+    push_momentum(c, s, dp_dt, sdt, r[3], deltap);
+}
+
+/* particle_boundary_condition on a single rank: particle_module.f90:1984-2129.
+ * A periodic direction has itself as neighbour and wraps by the box passed
+ * in; an open direction escapes with count_flag -1..-6 and adds to leak. */
+static void boundary(const mover_ctx *c, ptl_state *s, double xlo, double xhi, double ylo,
+                     double yhi, double zlo, double zhi, thread_acc *acc)
+{
+    const orc_params *pr = c->pr;
+    if (s->x < xlo && s->flag == 1) {
+        if (pr->pbcx) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -1; }
+        else s->x = s->x - xlo + xhi;
+    } else if (s->x > xhi && s->flag == 1) {
+        if (pr->pbcx) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -2; }
+        else s->x = s->x - xhi + xlo;
+    }
+    if (c->ndim > 1) {
+        if (s->y < ylo && s->flag == 1) {
+            if (pr->pbcy) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -3; }
+            else s->y = s->y - ylo + yhi;
+        } else if (s->y > yhi && s->flag == 1) {
+            if (pr->pbcy) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -4; }
+            else s->y = s->y - yhi + ylo;
+        }
+    }
+    if (c->ndim == 3) {
+        if (s->z < zlo && s->flag == 1) {
+            if (pr->pbcz) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -5; }
+            else s->z = s->z - zlo + zhi;
+        } else if (s->z > zhi && s->flag == 1) {
+            if (pr->pbcz) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -6; }
+            else s->z = s->z - zhi + zlo;
+        }
+    }
+}
+
+static void check_negp_or_boundary(const mover_ctx *c, ptl_state *s, thread_acc *acc)
+{
+    if (s->p < 0.0) {
+        s->flag = 0;
+        orc_fixed_add(&acc->negp_hi, &acc->negp_lo, s->weight);
+    } else {
+        boundary(c, s, c->xmin1, c->xmax1, c->ymin1, c->ymax1, c->zmin1, c->zmax1, acc);
+    }
+}
+
+/* One push at the particle's current state: interpolation parameters,
+ * interp_fields, kappa, push (the body at particle_module.f90:1615-1703). */
+static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double *dX, double *dY,
+                    double *dZ, double *dP)
+{
+    const double px = (s->x - c->xmin) / c->dx;
+    const double py = (s->y - c->ymin) / c->dy;
+    const double pz = (s->z - c->zmin) / c->dz;
+    const double rt = (s->t - c->t0) / c->dtf;
+    int32_t pos[3];
+    double w[8], f[32], kap[22];
+    orc_get_interp_paramters(c->ndim, px, py, pz, pos, w);
+    orc_interp_fields(c->f1, c->f2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, f);
+    orc_calc_spatial_diffusion_coefficients(c->pr, s->p, f, kap);
+    if (c->ndim == 2) push_2d(c, s, f, kap, fixed_dt, dX, dY, dZ, dP);
+    else push_3d(c, s, f, kap, fixed_dt, dX, dY, dZ, dP);
+}
+
+/* The per-particle body of particle_mover_one_cycle: :1560-1830. */
+static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
+                     int num_fine_steps, thread_acc *acc)
+{
+    const double t0 = c->t0, dtf = c->dtf;
+    const double dt_fine = dtf / num_fine_steps;
+    double deltax = 0.0, deltay = 0.0, deltaz = 0.0, deltap = 0.0;
+    const double step = ceil((s->t - t0) / dt_fine);
+    double dt_target = (step <= 0.0) ? dt_fine : step * dt_fine;
+    if (dt_target > dtf) dt_target = dtf;
+
+    if (s->p < 0.0 && s->flag == 1) {
+        s->flag = 0;
+        orc_fixed_add(&acc->negp_hi, &acc->negp_lo, s->weight);
+    } else {
+        boundary(c, s, c->xmin1, c->xmax1, c->ymin1, c->ymax1, c->zmin1, c->zmax1, acc);
+    }
+    if (s->flag != 1) return;
+
+    const double limit = dtf + dt_fine * (double)0.1f;
+    while (dt_target < limit) {
+        if (s->flag != 1) break;
+        while ((s->t - t0) < dt_target && s->flag == 1) {
+            check_negp_or_boundary(c, s, acc);
+            if (s->flag != 1) break;
+            do_push(c, s, 0, &deltax, &deltay, &deltaz, &deltap);
+            acc->steps += 1;
+            s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
+        }
+        if ((s->t - t0) > dt_target && s->flag == 1) {
+            s->x = s->x - deltax;
+            s->y = s->y - deltay;
+            s->z = s->z - deltaz;
+            s->p = s->p - deltap;
+            s->t = s->t - s->dt;
+            const double dt_old = s->dt;
+            s->dt = t0 + dt_target - s->t;
+            if (s->dt > 0.0) {
+                s->nsteps_pushed = s->nsteps_pushed - 1;
+                do_push(c, s, 1, &deltax, &deltay, &deltaz, &deltap);
+                acc->steps += 1;
+                s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
+            }
+            s->dt = dt_old;
+            check_negp_or_boundary(c, s, acc);
+        }
+        dt_target = dt_target + dt_fine;
+    }
+}
+
+static void load_state(const orc_particles *P, int64_t i, ptl_state *s)
+{
+    s->x = P->x[i]; s->y = P->y[i]; s->z = P->z[i]; s->p = P->p[i];
+    s->t = P->t[i]; s->dt = P->dt[i]; s->weight = P->weight[i];
+    s->flag = P->count_flag[i];
+    s->nsteps_pushed = P->nsteps_pushed[i];
+    s->tag_injected = P->tag_injected[i];
+    s->tag_splitted = P->tag_splitted[i];
+    s->rng_ctr = P->rng_ctr[i];
+}
+
+static void store_state(orc_particles *P, int64_t i, const ptl_state *s)
+{
+    P->x[i] = s->x; P->y[i] = s->y; P->z[i] = s->z; P->p[i] = s->p;
+    P->t[i] = s->t; P->dt[i] = s->dt;
+    P->count_flag[i] = (int8_t)s->flag;
+    P->nsteps_pushed[i] = s->nsteps_pushed;
+    P->rng_ctr[i] = s->rng_ctr;
+}
+
+static void swap_particles(orc_particles *P, int64_t a, int64_t b)
+{
+#define SWP(arr, T) do { T t_ = P->arr[a]; P->arr[a] = P->arr[b]; P->arr[b] = t_; } while (0)
+    SWP(x, double); SWP(y, double); SWP(z, double); SWP(p, double); SWP(v, double);
+    SWP(mu, double); SWP(weight, double); SWP(t, double); SWP(dt, double);
+    SWP(split_times, int8_t); SWP(count_flag, int8_t); SWP(origin, int32_t);
+    SWP(nsteps_tracked, int32_t); SWP(nsteps_pushed, int32_t);
+    SWP(tag_injected, int32_t); SWP(tag_splitted, int32_t); SWP(rng_ctr, uint32_t);
+#undef SWP
+}
+
+/* remove_particles: particle_module.f90:5365-5403 (same swap order). */
+int64_t orc_remove_particles(orc_particles *P, int64_t n, orc_counters *cnt)
+{
+    if (n <= 0) return n;
+    int64_t nremoved = 0, i = 0;   /* i is 0-based; Fortran i = i0 + 1 */
+    while (i < n) {
+        if ((n - (i + 1)) == (nremoved - 1)) break;
+        if (P->count_flag[i] == 1) {
+            i += 1;
+        } else {
+            if (P->count_flag[i] < 0) cnt->nptl_escaped += 1;
+            swap_particles(P, n - nremoved - 1, i);
+            nremoved += 1;
+        }
+    }
+    return n - nremoved;
+}
+
+static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *cfg,
+                      const float *f1, const float *f2, int time_interp, double t0, double dtf)
+{
+    memset(c, 0, sizeof(*c));
+    c->pr = pr; c->f1 = f1; c->f2 = f2; c->time_interp = time_interp;
+    c->ndim = pr->ndim;
+    c->nxg = cfg->nx + 4;
+    c->nyg = cfg->ny + 4;
+    c->dx = cfg->dx; c->dy = cfg->dy; c->dz = cfg->dz;
+    /* set_field_configuration on one rank: simulation_setup.f90:171-253. */
+    c->xmin = cfg->xmin;
+    const double xmax = c->xmin + (double)cfg->nx * cfg->dx;
+    c->ymin = cfg->ymin;
+    const double ymax = c->ymin + (double)cfg->ny * cfg->dy;
+    double zmax;
+    if (pr->ndim == 3) {
+        c->zmin = cfg->zmin;
+        zmax = c->zmin + (double)cfg->nz * cfg->dz;
+    } else {
+        c->zmin = cfg->zmin;
+        zmax = cfg->zmax;
+    }
+    c->xmin1 = c->xmin - c->dx * 0.5; c->xmax1 = xmax + c->dx * 0.5;
+    c->ymin1 = c->ymin - c->dy * 0.5; c->ymax1 = ymax + c->dy * 0.5;
+    c->zmin1 = c->zmin - c->dz * 0.5; c->zmax1 = zmax + c->dz * 0.5;
+    c->cfg_xmin = cfg->xmin; c->cfg_ymin = cfg->ymin; c->cfg_zmin = cfg->zmin;
+    c->cfg_lx = cfg->lx; c->cfg_ly = cfg->ly; c->cfg_lz = cfg->lz;
+    /* set_dt_min_max: particle_module.f90:5519-5524. */
+    c->dt_min = pr->dt_min_rel * dtf;
+    c->dt_max = pr->dt_max_rel * dtf;
+    c->t0 = t0; c->dtf = dtf;
+    c->key[0] = (uint32_t)pr->seed;
+    c->key[1] = (uint32_t)(pr->seed >> 32);
+}
+
+/* particle_mover on a single rank: particle_module.f90:1846-1974.  One
+ * mover cycle, remove_particles, then the boundary pass on the exact box
+ * and a second remove_particles.  Returns the new particle count. */
+int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,
+                           const float *f1, const float *f2, int time_interp,
+                           orc_particles *P, int64_t n, double t0, double dtf,
+                           int nsteps_interval, int num_fine_steps, int nthreads,
+                           orc_counters *cnt)
+{
+    mover_ctx c;
+    setup_ctx(&c, pr, cfg, f1, f2, time_interp, t0, dtf);
+    for (int64_t i = 0; i < n; ++i) P->nsteps_tracked[i] = 1;
+    uint64_t lh = 0, ll = 0, nh = 0, nl = 0, steps = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+        thread_acc acc = {0, 0, 0, 0, 0};
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t i = 0; i < n; ++i) {
+            ptl_state s;
+            load_state(P, i, &s);
+            move_one(&c, &s, nsteps_interval, num_fine_steps, &acc);
+            store_state(P, i, &s);
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        {
+            uint64_t o = ll; ll += acc.leak_lo; lh += acc.leak_hi + (ll < o);
+            o = nl; nl += acc.negp_lo; nh += acc.negp_hi + (nl < o);
+            steps += acc.steps;
+        }
+    }
+    (void)nthreads;
+    {
+        uint64_t o = cnt->leak_lo; cnt->leak_lo += ll; cnt->leak_hi += lh + (cnt->leak_lo < o);
+        o = cnt->leak_negp_lo; cnt->leak_negp_lo += nl; cnt->leak_negp_hi += nh + (cnt->leak_negp_lo < o);
+        cnt->steps += steps;
+    }
+    n = orc_remove_particles(P, n, cnt);
+    /* Final pass on the exact box (:1959-1973). */
+    thread_acc acc = {0, 0, 0, 0, 0};
+    const double xmax = c.xmin + (double)cfg->nx * cfg->dx;
+    const double ymax = c.ymin + (double)cfg->ny * cfg->dy;
+    const double zmax = (pr->ndim == 3) ? c.zmin + (double)cfg->nz * cfg->dz : cfg->zmax;
+    for (int64_t i = 0; i < n; ++i) {
+        ptl_state s;
+        load_state(P, i, &s);
+        if (s.p < 0.0 && s.flag != 1) {
+            s.flag = 0;
+            orc_fixed_add(&acc.negp_hi, &acc.negp_lo, s.weight);
+        } else {
+            boundary(&c, &s, c.xmin, xmax, c.ymin, ymax, c.zmin, zmax, &acc);
+        }
+        store_state(P, i, &s);
+    }
+    {
+        uint64_t o = cnt->leak_lo; cnt->leak_lo += acc.leak_lo; cnt->leak_hi += acc.leak_hi + (cnt->leak_lo < o);
+        o = cnt->leak_negp_lo; cnt->leak_negp_lo += acc.negp_lo; cnt->leak_negp_hi += acc.negp_hi + (cnt->leak_negp_lo < o);
+    }
+    return orc_remove_particles(P, n, cnt);
+}
+
+/* split_particle: particle_module.f90:5430-5480 (no tracking).  The
+ * threshold uses split_ratio**split_times by repeated multiplication, the
+ * new weight is 0.5**(1+split_times) (exact in single precision). */
+int64_t orc_split_particle(const orc_params *pr, orc_particles *P, int64_t n,
+                           int64_t nptl_max, double split_ratio, double pmin_split,
+                           orc_counters *cnt)
+{
+    const int64_t nptl = n;
+    for (int64_t i = 0; i < nptl; ++i) {
+        const int k = P->split_times[i];
+        double rk = 1.0;
+        for (int j = 0; j < k; ++j) rk = rk * split_ratio;
+        const double p_threshold = pmin_split * pr->p0 * rk;
+        if (P->p[i] > p_threshold && P->p[i] <= pr->pmax) {
+            if (n + 1 > nptl_max) return n;
+            cnt->nptl_split += 1;
+            P->weight[i] = ldexp(1.0, -(k + 1));
+            P->split_times[i] = (int8_t)(k + 1);
+            const int64_t c = n;
+            n += 1;
+            P->x[c] = P->x[i]; P->y[c] = P->y[i]; P->z[c] = P->z[i]; P->p[c] = P->p[i];
+            P->v[c] = P->v[i]; P->mu[c] = P->mu[i]; P->weight[c] = P->weight[i];
+            P->t[c] = P->t[i]; P->dt[c] = P->dt[i];
+            P->split_times[c] = P->split_times[i]; P->count_flag[c] = P->count_flag[i];
+            P->origin[c] = P->origin[i]; P->nsteps_tracked[c] = P->nsteps_tracked[i];
+            P->nsteps_pushed[c] = P->nsteps_pushed[i];
+            P->tag_injected[c] = P->tag_injected[i];
+            P->tag_splitted[c] = (int32_t)((uint32_t)P->tag_splitted[i] + (1u << k));
+            P->rng_ctr[c] = P->rng_ctr[i];
+        }
+    }
+    return n;
+}
+
+/* Bin edges: init_particle_distributions, diagnostics.f90:194-204. */
+void orc_pbins_edges(const orc_params *pr, double *edges)
+{
+    const double lo = log10(pr->pmin), hi = log10(pr->pmax);
+    const double d = (hi - lo) / pr->npp_global;
+    for (int i = 0; i <= pr->npp_global; ++i) edges[i] = pow(10.0, lo + i * d);
+}
+
+/* Global f(p): calc_particle_distributions, diagnostics.f90:738-780 (Parker,
+ * one mu bin).  Counts and exact fixed-point weight sums per bin. */
+void orc_calc_particle_distributions(const orc_params *pr, const orc_particles *P,
+                                     int64_t n, uint64_t *counts, uint64_t *whi,
+                                     uint64_t *wlo, double *fglobal)
+{
+    const int npp = pr->npp_global;
+    const double pmin_log = log10(pr->pmin), pmax_log = log10(pr->pmax);
+    const double dp_log = (pmax_log - pmin_log) / npp;
+    for (int b = 0; b < npp; ++b) { counts[b] = 0; whi[b] = 0; wlo[b] = 0; }
+    for (int64_t i = 0; i < n; ++i) {
+        const double p = P->p[i], mu = P->mu[i];
+        if (p > pr->pmin && p <= pr->pmax && mu >= -1.0 && mu <= 1.0) {
+            int ip = (int)floor((log10(p) - pmin_log) / dp_log);
+            if (ip < 0 || ip >= npp) continue;   /* unreachable for p in range */
+            counts[ip] += 1;
+            orc_fixed_add(&whi[ip], &wlo[ip], P->weight[i]);
+        }
+    }
+    for (int b = 0; b < npp; ++b) fglobal[b] = orc_fixed_to_double(whi[b], wlo[b]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Injection.  Draw order follows the reference; the draws come from a     */
+/* Philox stream keyed (seed_lo, seed_hi + 1) with counter (tag, call,      */
+/* 0x494E4A43, 0), two uniforms per call.                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct inj_stream {
+    uint32_t key[2], tag, call;
+    double buf[2];
+    int avail;
+} inj_stream;
+
+static double inj_u01(inj_stream *s)
+{
+    if (s->avail == 0) {
+        uint32_t ctr[4] = {s->tag, s->call, 0x494E4A43u, 0u}, w[4];
+        orc_philox4x32_10(ctr, s->key, w);
+        s->call += 1;
+        s->buf[0] = orc_u01(w[0], w[1]);
+        s->buf[1] = orc_u01(w[2], w[3]);
+        s->avail = 2;
+    }
+    double u = s->buf[2 - s->avail];
+    s->avail -= 1;
+    return u;
+}
+
+static void inj_stream_init(inj_stream *s, const orc_params *pr, uint32_t tag)
+{
+    s->key[0] = (uint32_t)pr->seed;
+    s->key[1] = (uint32_t)(pr->seed >> 32) + 1u;
+    s->tag = tag; s->call = 0; s->avail = 0;
+}
+
+static void set_new_particle(orc_particles *P, int64_t c, double x, double y, double z, double p,
+                             double v, double mu, double t, double dt, int32_t tag)
+{
+    P->x[c] = x; P->y[c] = y; P->z[c] = z; P->p[c] = p; P->v[c] = v; P->mu[c] = mu;
+    P->weight[c] = 1.0; P->t[c] = t; P->dt[c] = dt;
+    P->split_times[c] = 0; P->count_flag[c] = 1; P->origin[c] = 0;
+    P->nsteps_tracked[c] = 0; P->nsteps_pushed[c] = 0;
+    P->tag_injected[c] = tag; P->tag_splitted[c] = 1; P->rng_ctr[c] = 0;
+}
+
+/* inject_one_particle momentum draw: particle_module.f90:398-418. */
+static double draw_p_one(const orc_params *pr, inj_stream *s, int dist_flag, double power_index)
+{
+    if (dist_flag == 0) {
+        double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
+        while (ftest > fxp) {
+            ptmp = (inj_u01(s) * (pr->pmax - pr->pmin) + pr->pmin) / pr->p0;
+            fxp = ptmp * ptmp * exp(-(ptmp * ptmp));
+            ftest = inj_u01(s) * (double)0.37f;
+        }
+        return ptmp * pr->p0;
+    } else if (dist_flag == 2) {
+        const double r01 = inj_u01(s);
+        if ((int)power_index == 1) return pow(pr->pmax / pr->p0, r01) * pr->p0;
+        const double norm = pow(pr->pmax, -power_index + 1.0) - pow(pr->p0, -power_index + 1.0);
+        return pow(r01 * norm + pow(pr->p0, -power_index + 1.0), 1.0 / (-power_index + 1.0));
+    }
+    return pr->p0;
+}
+
+/* inject_particles_spatial_uniform + inject_one_particle, single rank:
+ * particle_module.f90:385-530.  Returns the new particle count; at most
+ * nptl_max - n particles are added. */
+int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *P, int64_t n,
+                                   int64_t nptl_max, int64_t nptl, double dt,
+                                   int dist_flag, double particle_v0, double t_frame,
+                                   double dt_mhd, const double box[6],
+                                   double power_index, orc_counters *cnt)
+{
+    for (int64_t i = 0; i < nptl && n < nptl_max; ++i) {
+        const int32_t tag = (int32_t)cnt->tag_max;
+        cnt->tag_max += 1;
+        inj_stream s;
+        inj_stream_init(&s, pr, (uint32_t)tag);
+        const double x = inj_u01(&s) * (box[3] - box[0]) + box[0];
+        const double y = inj_u01(&s) * (box[4] - box[1]) + box[1];
+        const double z = inj_u01(&s) * (box[5] - box[2]) + box[2];
+        const double mu = (double)0.99f * (2.0 * inj_u01(&s) - 1.0);
+        const double p = draw_p_one(pr, &s, dist_flag, power_index);
+        const double v = particle_v0 * p / pr->p0;
+        const double t = t_frame + inj_u01(&s) * dt_mhd;
+        set_new_particle(P, n, x, y, z, p, v, mu, t, dt, tag);
+        n += 1;
+    }
+    return n;
+}
+
+/* Injection on the plane x = xpos at the frame start, following the draw
+ * order of inject_particles_at_shock (particle_module.f90:542-633) with the
+ * shock locator replaced by the given x. */
+int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
+                        orc_particles *P, int64_t n, int64_t nptl_max,
+                        int64_t nptl, double xpos, double dt, int dist_flag,
+                        double particle_v0, double t_frame, double power_index,
+                        orc_counters *cnt)
+{
+    const double ymin = cfg->ymin, ymax = cfg->ymin + (double)cfg->ny * cfg->dy;
+    double zmin = cfg->zmin, zmax = cfg->zmax;
+    if (pr->ndim == 3) zmax = cfg->zmin + (double)cfg->nz * cfg->dz;
+    for (int64_t i = 0; i < nptl && n < nptl_max; ++i) {
+        const int32_t tag = (int32_t)cnt->tag_max;
+        cnt->tag_max += 1;
+        inj_stream s;
+        inj_stream_init(&s, pr, (uint32_t)tag);
+        const double y = inj_u01(&s) * (ymax - ymin) + ymin;
+        const double z = inj_u01(&s) * (zmax - zmin) + zmin;
+        double p = pr->p0;
+        if (dist_flag == 0) {
+            double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
+            while (ftest > fxp) {
+                ptmp = (inj_u01(&s) * (pr->pmax - pr->pmin) + pr->pmin) / pr->p0;
+                fxp = ptmp * ptmp * exp((double)(-0.5f) * (ptmp * ptmp));
+                ftest = inj_u01(&s) * (double)0.75f;
+            }
+            p = ptmp * pr->p0;
+        } else if (dist_flag == 2) {
+            p = draw_p_one(pr, &s, 2, power_index);
+        }
+        const double v = particle_v0 * p / pr->p0;
+        const double mu = (double)0.99f * (2.0 * inj_u01(&s) - 1.0);
+        set_new_particle(P, n, xpos, y, z, p, v, mu, t_frame, dt, tag);
+        n += 1;
+    }
+    return n;
+}
+
+/* quick_check sums for one rank: diagnostics.f90:116-170.  out = {sum of
+ * weights, pdt_min, pdt_max, sum of dt}. */
+void orc_quick_check(const orc_particles *P, int64_t n, double out[4])
+{
+    double w = 0.0, mn = 1.0, mx = 0.0, s = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        w = w + P->weight[i];
+        if (P->dt[i] < mn) mn = P->dt[i];
+        if (P->dt[i] > mx) mx = P->dt[i];
+        s = s + P->dt[i];
+    }
+    out[0] = w; out[1] = mn; out[2] = mx; out[3] = s;
+}

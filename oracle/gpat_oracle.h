@@ -1,0 +1,122 @@
+/*
+ * gpat_oracle.h -- CPU oracle for the GPAT Parker-transport particle mover.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C FP64 restatement of the
+ * reference's CPU algorithm (xiaocanli/stochastic-parker, Fortran), used as
+ * the checker for the CUDA engine and as the timed CPU baseline.  Nothing in
+ * the product links or calls it; only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py load it.
+ *
+ * Parity status: UNPINNED by the reference's own tests.  The reference ships
+ * no tests, golden vectors or fixtures, and it cannot be built here (Fortran +
+ * MPI + HDF5 + FLAP + mt_stream; no gfortran).  The restatement is pinned
+ * instead by analytic known answers (drift-only advection, pure-diffusion
+ * variance, DSA spectral index) in tests/test_oracle_*.py and by the golden
+ * vectors it generated (tests/golden/make_golden.py).
+ *
+ * Arithmetic follows the Fortran evaluation order of each cited routine,
+ * left to right, with single-precision literals (0.1, 1.0/(3*charge)) kept
+ * single, and is compiled with -ffp-contract=off so every +,-,*,/,sqrt is one
+ * IEEE-rounded operation.  pow/log10/exp come from the host libm.
+ *
+ * The reference's MT19937 streams are replaced by Philox-4x32-10 (Salmon et
+ * al., SC'11) keyed per particle, so results do not depend on the thread
+ * count or schedule.
+ */
+#ifndef GPAT_ORACLE_H
+#define GPAT_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* mhd_configuration record, same field order and binary layout as the
+ * reference's mhd_config.dat (src/modules/mhd_config.f90:16-27). */
+typedef struct orc_mhd_config {
+    double dx, dy, dz, xmin, ymin, zmin, xmax, ymax, zmax, lx, ly, lz, dt_out;
+    int32_t nx, ny, nz, nxs, nys, nzs, topox, topoy, topoz, nvar, bcx, bcy, bcz;
+} orc_mhd_config;
+
+/* Parameters on the path: conf.dat keys read by read_particle_params
+ * (particle_module.f90:2778-2878), the drift / flag setters (:269-328) and
+ * the boundary flags (simulation_setup.f90:104-150). */
+typedef struct orc_params {
+    double b0, p0, pmin, pmax;
+    double gamma_turb, pindex, kpara0, kret, dt_min_rel, dt_max_rel;
+    double acc_region[6];
+    double drift1, drift2;
+    int32_t momentum_dependency, mag_dependency, acc_region_flag, charge;
+    int32_t check_drift_2d, ndim, pbcx, pbcy, pbcz, npp_global;
+    uint64_t seed;
+    int32_t noise;      /* 0: (2u-1)*sqrt(3) as the reference; 1: Gaussian */
+    int32_t reserved;
+} orc_params;
+
+/* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the
+ * per-particle Philox push counter that replaces the MT19937 state. */
+typedef struct orc_particles {
+    double *x, *y, *z, *p, *v, *mu, *weight, *t, *dt;
+    int8_t *split_times, *count_flag;
+    int32_t *origin, *nsteps_tracked, *nsteps_pushed, *tag_injected, *tag_splitted;
+    uint32_t *rng_ctr;
+} orc_particles;
+
+/* Module-level counters (particle_module.f90:65-79).  leak and leak_negp are
+ * kept as unsigned 128-bit fixed point with 64 fraction bits so the sums are
+ * exact for dyadic weights and independent of summation order. */
+typedef struct orc_counters {
+    uint64_t leak_hi, leak_lo, leak_negp_hi, leak_negp_lo;
+    uint64_t steps;          /* pushes, landing redo pushes included */
+    int64_t nptl_escaped;    /* removed with count_flag < 0 */
+    int64_t nptl_split;
+    int64_t tag_max;
+} orc_counters;
+
+#define ORC_COUNT_FLAG_INBOX 1
+#define ORC_COUNT_FLAG_OTHERS 0
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double orc_u01(uint32_t a, uint32_t b);
+void orc_fixed_add(uint64_t *hi, uint64_t *lo, double w);
+double orc_fixed_to_double(uint64_t hi, uint64_t lo);
+
+void orc_calc_fields_gradients(float *farray, int ndim, int nxg, int nyg, int nzg,
+                               double dx, double dy, double dz);
+void orc_get_interp_paramters(int ndim, double px, double py, double pz,
+                              int32_t pos[3], double weights[8]);
+void orc_interp_fields(const float *f1, const float *f2, int time_interp, int ndim,
+                       int nxg, int nyg, const int32_t pos[3], const double weights[8],
+                       double rt, double fields[32]);
+void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p,
+                                             const double fields[32], double kappa[22]);
+
+int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,
+                           const float *f1, const float *f2, int time_interp,
+                           orc_particles *ptl, int64_t n, double t0, double dtf,
+                           int nsteps_interval, int num_fine_steps, int nthreads,
+                           orc_counters *cnt);
+int64_t orc_remove_particles(orc_particles *ptl, int64_t n, orc_counters *cnt);
+int64_t orc_split_particle(const orc_params *pr, orc_particles *ptl, int64_t n,
+                           int64_t nptl_max, double split_ratio, double pmin_split,
+                           orc_counters *cnt);
+void orc_pbins_edges(const orc_params *pr, double *edges);
+void orc_calc_particle_distributions(const orc_params *pr, const orc_particles *ptl,
+                                     int64_t n, uint64_t *counts, uint64_t *whi,
+                                     uint64_t *wlo, double *fglobal);
+int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *ptl, int64_t n,
+                                   int64_t nptl_max, int64_t nptl, double dt,
+                                   int dist_flag, double particle_v0, double t_frame,
+                                   double dt_mhd, const double part_box[6],
+                                   double power_index, orc_counters *cnt);
+int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
+                        orc_particles *ptl, int64_t n, int64_t nptl_max,
+                        int64_t nptl, double xpos, double dt, int dist_flag,
+                        double particle_v0, double t_frame, double power_index,
+                        orc_counters *cnt);
+void orc_quick_check(const orc_particles *ptl, int64_t n, double out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

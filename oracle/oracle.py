@@ -1,0 +1,241 @@
+"""ctypes binding of the CPU oracle (oracle/gpat_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+the CPU-baseline leg of bench.py as the checker.  The product never loads it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB_PATH = ORACLE_DIR / "_build" / "libgpat_oracle.so"
+
+d, i32, i64, u32, u64 = C.c_double, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64
+P = C.POINTER
+
+
+class OrcMhdConfig(C.Structure):
+    _fields_ = [(n, d) for n in ("dx", "dy", "dz", "xmin", "ymin", "zmin", "xmax", "ymax", "zmax",
+                                 "lx", "ly", "lz", "dt_out")] + \
+               [(n, i32) for n in ("nx", "ny", "nz", "nxs", "nys", "nzs", "topox", "topoy", "topoz",
+                                   "nvar", "bcx", "bcy", "bcz")]
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("b0", d), ("p0", d), ("pmin", d), ("pmax", d),
+        ("gamma_turb", d), ("pindex", d), ("kpara0", d), ("kret", d),
+        ("dt_min_rel", d), ("dt_max_rel", d),
+        ("acc_region", d * 6),
+        ("drift1", d), ("drift2", d),
+        ("momentum_dependency", i32), ("mag_dependency", i32), ("acc_region_flag", i32),
+        ("charge", i32),
+        ("check_drift_2d", i32), ("ndim", i32), ("pbcx", i32), ("pbcy", i32), ("pbcz", i32),
+        ("npp_global", i32),
+        ("seed", u64),
+        ("noise", i32), ("reserved", i32),
+    ]
+
+
+FIELDS = [
+    ("x", "f8"), ("y", "f8"), ("z", "f8"), ("p", "f8"), ("v", "f8"), ("mu", "f8"),
+    ("weight", "f8"), ("t", "f8"), ("dt", "f8"),
+    ("split_times", "i1"), ("count_flag", "i1"),
+    ("origin", "i4"), ("nsteps_tracked", "i4"), ("nsteps_pushed", "i4"),
+    ("tag_injected", "i4"), ("tag_splitted", "i4"), ("rng_ctr", "u4"),
+]
+_CT = {"f8": C.c_double, "i1": C.c_int8, "i4": C.c_int32, "u4": C.c_uint32}
+
+
+class OrcParticles(C.Structure):
+    _fields_ = [(n, P(_CT[t])) for n, t in FIELDS]
+
+
+class OrcCounters(C.Structure):
+    _fields_ = [("leak_hi", u64), ("leak_lo", u64), ("leak_negp_hi", u64), ("leak_negp_lo", u64),
+                ("steps", u64), ("nptl_escaped", i64), ("nptl_split", i64), ("tag_max", i64)]
+
+    def leak(self) -> float:
+        return fixed_to_double(self.leak_hi, self.leak_lo)
+
+    def leak_negp(self) -> float:
+        return fixed_to_double(self.leak_negp_hi, self.leak_negp_lo)
+
+
+def fixed_to_double(hi: int, lo: int) -> float:
+    return float(hi) + float(lo) * (1.0 / 18446744073709551616.0)
+
+
+_lib = None
+
+
+def build() -> Path:
+    """Compiles the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    src = ORACLE_DIR / "gpat_oracle.c"
+    if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-C", str(ORACLE_DIR), "-B", "_build/libgpat_oracle.so"],
+                       check=True, capture_output=True)
+    return LIB_PATH
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB_PATH))
+        lib.orc_philox4x32_10.argtypes = [P(u32), P(u32), P(u32)]
+        lib.orc_u01.restype = d
+        lib.orc_u01.argtypes = [u32, u32]
+        lib.orc_calc_fields_gradients.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int,
+                                                  d, d, d]
+        lib.orc_get_interp_paramters.argtypes = [C.c_int, d, d, d, P(i32), P(d)]
+        lib.orc_interp_fields.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_int,
+                                          C.c_int, P(i32), P(d), d, P(d)]
+        lib.orc_calc_spatial_diffusion_coefficients.argtypes = [P(OrcParams), d, P(d), P(d)]
+        lib.orc_particle_mover.restype = i64
+        lib.orc_particle_mover.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
+                                           P(C.c_float), C.c_int, P(OrcParticles), i64, d, d,
+                                           C.c_int, C.c_int, C.c_int, P(OrcCounters)]
+        lib.orc_remove_particles.restype = i64
+        lib.orc_remove_particles.argtypes = [P(OrcParticles), i64, P(OrcCounters)]
+        lib.orc_split_particle.restype = i64
+        lib.orc_split_particle.argtypes = [P(OrcParams), P(OrcParticles), i64, i64, d, d,
+                                           P(OrcCounters)]
+        lib.orc_pbins_edges.argtypes = [P(OrcParams), P(d)]
+        lib.orc_calc_particle_distributions.argtypes = [P(OrcParams), P(OrcParticles), i64,
+                                                        P(u64), P(u64), P(u64), P(d)]
+        lib.orc_inject_spatial_uniform.restype = i64
+        lib.orc_inject_spatial_uniform.argtypes = [P(OrcParams), P(OrcParticles), i64, i64, i64, d,
+                                                   C.c_int, d, d, d, P(d), d, P(OrcCounters)]
+        lib.orc_inject_at_x.restype = i64
+        lib.orc_inject_at_x.argtypes = [P(OrcParams), P(OrcMhdConfig), P(OrcParticles), i64, i64,
+                                        i64, d, d, C.c_int, d, d, d, P(OrcCounters)]
+        lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
+        _lib = lib
+    return _lib
+
+
+def params_from(p) -> OrcParams:
+    """Copies the shared fields of an engine gpat_params_t (or a dict)."""
+    o = OrcParams()
+    get = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
+    for name, _ in OrcParams._fields_:
+        if name == "reserved":
+            continue
+        v = get(name)
+        if name == "acc_region":
+            o.acc_region = (C.c_double * 6)(*tuple(v))
+        else:
+            setattr(o, name, v)
+    return o
+
+
+def config_from(c) -> OrcMhdConfig:
+    o = OrcMhdConfig()
+    for name, _ in OrcMhdConfig._fields_:
+        setattr(o, name, getattr(c, name))
+    return o
+
+
+class Particles:
+    """Oracle particle storage (numpy SoA with spare capacity)."""
+
+    def __init__(self, capacity: int, arrays: dict | None = None):
+        self.cap = capacity
+        self.a = {k: np.zeros(capacity, dtype=t) for k, t in FIELDS}
+        self.n = 0
+        if arrays is not None:
+            n = len(arrays["x"])
+            assert n <= capacity
+            for k, _ in FIELDS:
+                self.a[k][:n] = arrays[k]
+            self.n = n
+        self.c = OrcParticles()
+        for k, t in FIELDS:
+            setattr(self.c, k, self.a[k].ctypes.data_as(P(_CT[t])))
+
+    def view(self) -> dict:
+        return {k: v[:self.n].copy() for k, v in self.a.items()}
+
+
+def full_fields(frame8: np.ndarray, ndim: int, cfg) -> np.ndarray:
+    """32-variable array with the reference's gradients from an 8-var frame."""
+    nzg, nyg, nxg, _ = frame8.shape
+    full = np.zeros((nzg, nyg, nxg, 32), dtype=np.float32)
+    full[..., :8] = frame8
+    lib = load()
+    lib.orc_calc_fields_gradients(full.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
+                                  cfg.dx, cfg.dy, cfg.dz)
+    return full
+
+
+def philox(ctr, key):
+    lib = load()
+    c = (u32 * 4)(*ctr)
+    k = (u32 * 2)(*key)
+    o = (u32 * 4)()
+    lib.orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def mover(params: OrcParams, cfg: OrcMhdConfig, f1: np.ndarray, parts: Particles, t0: float,
+          dtf: float, nsteps_interval: int = 10, num_fine_steps: int = 1, nthreads: int = 0,
+          counters: OrcCounters | None = None, f2: np.ndarray | None = None) -> OrcCounters:
+    lib = load()
+    cnt = counters if counters is not None else OrcCounters()
+    fp1 = f1.ctypes.data_as(P(C.c_float))
+    fp2 = (f2 if f2 is not None else f1).ctypes.data_as(P(C.c_float))
+    parts.n = lib.orc_particle_mover(C.byref(params), C.byref(cfg), fp1, fp2,
+                                     1 if f2 is not None else 0, C.byref(parts.c), parts.n, t0,
+                                     dtf, nsteps_interval, num_fine_steps, nthreads, C.byref(cnt))
+    return cnt
+
+
+def split(params: OrcParams, parts: Particles, split_ratio: float, pmin_split: float,
+          counters: OrcCounters) -> None:
+    lib = load()
+    parts.n = lib.orc_split_particle(C.byref(params), C.byref(parts.c), parts.n, parts.cap,
+                                     split_ratio, pmin_split, C.byref(counters))
+
+
+def histogram(params: OrcParams, parts: Particles):
+    lib = load()
+    npp = params.npp_global
+    counts = np.zeros(npp, np.uint64)
+    whi = np.zeros(npp, np.uint64)
+    wlo = np.zeros(npp, np.uint64)
+    f = np.zeros(npp, np.float64)
+    lib.orc_calc_particle_distributions(
+        C.byref(params), C.byref(parts.c), parts.n, counts.ctypes.data_as(P(u64)),
+        whi.ctypes.data_as(P(u64)), wlo.ctypes.data_as(P(u64)), f.ctypes.data_as(P(d)))
+    return f, counts
+
+
+def inject_at_x(params: OrcParams, cfg: OrcMhdConfig, parts: Particles, nptl: int, xpos: float,
+                dt: float, dist_flag: int, particle_v0: float, t_frame: float,
+                counters: OrcCounters, power_index: float = 7.0):
+    lib = load()
+    parts.n = lib.orc_inject_at_x(C.byref(params), C.byref(cfg), C.byref(parts.c), parts.n,
+                                  parts.cap, nptl, xpos, dt, dist_flag, particle_v0, t_frame,
+                                  power_index, C.byref(counters))
+
+
+def inject_spatial_uniform(params: OrcParams, parts: Particles, nptl: int, dt: float,
+                           dist_flag: int, particle_v0: float, t_frame: float, dt_mhd: float,
+                           box, counters: OrcCounters, power_index: float = 7.0):
+    lib = load()
+    b = (d * 6)(*box)
+    parts.n = lib.orc_inject_spatial_uniform(C.byref(params), C.byref(parts.c), parts.n,
+                                             parts.cap, nptl, dt, dist_flag, particle_v0,
+                                             t_frame, dt_mhd, b, power_index, C.byref(counters))
+
+
+def quick_check(parts: Particles):
+    lib = load()
+    out = (d * 4)()
+    lib.orc_quick_check(C.byref(parts.c), parts.n, out)
+    return list(out)

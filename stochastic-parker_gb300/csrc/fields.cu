@@ -1,0 +1,120 @@
+// Field preparation kernels: raw 8-variable frames -> 32-variable arrays
+// with gradients (mhd_data_parallel.f90:504-610) -> packed mover records.
+#include "device_common.cuh"
+
+namespace gpat {
+
+// Slot order of the packed records, as indices into the 32-variable cell
+// (vars 0-7: vx vy vz rho bx by bz |B|; gradient of var v along d at 8+3v+d).
+__constant__ int kPack2D[kRec2D] = {0, 1, 4, 5, 6, 8, 12, 20, 21, 23, 24, 26, 27, 29, 30, 3};
+__constant__ int kPack3D[kRec3D] = {0, 1, 2, 4, 5, 6, 8, 12, 16, 20, 21, 22,
+                                    23, 24, 25, 26, 27, 28, 29, 30, 31, 3, 7, -1};
+
+__global__ void scatter_raw_kernel(const float *__restrict__ raw, int nvar,
+                                   float *__restrict__ full, size_t ncells) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride) {
+        float *dst = full + 32 * c;
+        const float *src = raw + (size_t)nvar * c;
+#pragma unroll 8
+        for (int v = 0; v < 32; ++v) dst[v] = (v < nvar) ? src[v] : 0.0f;
+    }
+}
+
+cudaError_t launch_scatter_raw_fields(const float *raw, int nvar, float *full, size_t ncells,
+                                      cudaStream_t s) {
+    const int threads = 256;
+    const size_t blocks = (ncells + threads - 1) / threads;
+    scatter_raw_kernel<<<(unsigned)(blocks < 65535 * 16 ? blocks : 65535 * 16), threads, 0, s>>>(
+        raw, nvar, full, ncells);
+    return cudaGetLastError();
+}
+
+// One-sided / centred difference exactly as the reference evaluates it:
+// single-precision differences, scaled by the double 0.5/d, rounded to float.
+__device__ __forceinline__ float grad_lo(float a0, float a1, float a2, double ih) {
+    float t = -__fmul_rn(3.0f, a0);
+    t = __fadd_rn(t, __fmul_rn(4.0f, a1));
+    t = __fsub_rn(t, a2);
+    return (float)__dmul_rn((double)t, ih);
+}
+__device__ __forceinline__ float grad_hi(float an, float an1, float an2, double ih) {
+    float t = __fmul_rn(3.0f, an);
+    t = __fsub_rn(t, __fmul_rn(4.0f, an1));
+    t = __fadd_rn(t, an2);
+    return (float)__dmul_rn((double)t, ih);
+}
+__device__ __forceinline__ float grad_c(float ap, float am, double ih) {
+    return (float)__dmul_rn((double)__fsub_rn(ap, am), ih);
+}
+
+__global__ void gradients_kernel(float *__restrict__ a, int ndim, int nxg, int nyg, int nzg,
+                                 double idxh, double idyh, double idzh) {
+    const size_t ncells = (size_t)nxg * nyg * nzg;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t sx = 32, sy = 32 * (size_t)nxg, sz = 32 * (size_t)nxg * nyg;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride) {
+        const int i = (int)(c % nxg);
+        const int j = (int)((c / nxg) % nyg);
+        const int k = (int)(c / ((size_t)nxg * nyg));
+        float *cell = a + 32 * c;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            float d;
+            if (i == 0) d = grad_lo(cell[v], cell[v + sx], cell[v + 2 * sx], idxh);
+            else if (i == nxg - 1) d = grad_hi(cell[v], cell[v - sx], cell[v - 2 * sx], idxh);
+            else d = grad_c(cell[v + sx], cell[v - sx], idxh);
+            cell[8 + 3 * v] = d;
+            if (nyg > 1) {
+                if (j == 0) d = grad_lo(cell[v], cell[v + sy], cell[v + 2 * sy], idyh);
+                else if (j == nyg - 1) d = grad_hi(cell[v], cell[v - sy], cell[v - 2 * sy], idyh);
+                else d = grad_c(cell[v + sy], cell[v - sy], idyh);
+                cell[8 + 3 * v + 1] = d;
+            }
+            if (nzg > 1 && ndim == 3) {
+                if (k == 0) d = grad_lo(cell[v], cell[v + sz], cell[v + 2 * sz], idzh);
+                else if (k == nzg - 1) d = grad_hi(cell[v], cell[v - sz], cell[v - 2 * sz], idzh);
+                else d = grad_c(cell[v + sz], cell[v - sz], idzh);
+                cell[8 + 3 * v + 2] = d;
+            }
+        }
+    }
+}
+
+cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg, int nzg,
+                                         double dx, double dy, double dz, cudaStream_t s) {
+    const size_t ncells = (size_t)nxg * nyg * nzg;
+    const int threads = 256;
+    size_t blocks = (ncells + threads - 1) / threads;
+    if (blocks > 65535 * 16) blocks = 65535 * 16;
+    gradients_kernel<<<(unsigned)blocks, threads, 0, s>>>(full, ndim, nxg, nyg, nzg, 0.5 / dx,
+                                                          0.5 / dy, 0.5 / dz);
+    return cudaGetLastError();
+}
+
+template <int R>
+__global__ void pack_kernel(const float *__restrict__ full, float *__restrict__ rec,
+                            size_t ncells) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride) {
+        const float *src = full + 32 * c;
+        float *dst = rec + (size_t)R * c;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int v = (R == kRec2D) ? kPack2D[r] : kPack3D[r];
+            dst[r] = v >= 0 ? src[v] : 0.0f;
+        }
+    }
+}
+
+cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
+                                cudaStream_t s) {
+    const int threads = 256;
+    size_t blocks = (ncells + threads - 1) / threads;
+    if (blocks > 65535 * 16) blocks = 65535 * 16;
+    if (ndim == 2) pack_kernel<kRec2D><<<(unsigned)blocks, threads, 0, s>>>(full, rec, ncells);
+    else pack_kernel<kRec3D><<<(unsigned)blocks, threads, 0, s>>>(full, rec, ncells);
+    return cudaGetLastError();
+}
+
+}  // namespace gpat

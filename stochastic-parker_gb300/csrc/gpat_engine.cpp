@@ -1,0 +1,719 @@
+// Host side of the engine: the C ABI declared in include/gpat_engine.h.
+// Owns the device state of one GPAT rank (particles, fields, counters) and
+// sequences the kernels in the order the reference's module procedures run.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gpat_internal.h"
+
+using namespace gpat;
+
+struct gpat_handle {
+    gpat_params_t prm{};
+    gpat_mhd_config_t cfg{};
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    // fields
+    int nxg = 0, nyg = 0, nzg = 0;
+    size_t ncells = 0;
+    int nslots = 1;
+    float *full[2] = {nullptr, nullptr};
+    float *rec[2] = {nullptr, nullptr};
+    float *staging = nullptr;
+    bool fields_set[2] = {false, false};
+    bool rec_ready[2] = {false, false};
+    // particles (double-buffered SoA)
+    int64_t cap = 0, n = 0;
+    int cur = 0;
+    void *pmem[2] = {nullptr, nullptr};
+    DevParticles P[2]{};
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    DevCounters *dcnt = nullptr;
+    DevCounters hcnt{};
+    unsigned long long *dbins = nullptr;
+    // module state kept on the host
+    std::vector<double> tstamps;
+    int64_t tag_max = 0;
+    int64_t nptl_split = 0;
+    double last_mover_ms = 0.0;
+    uint64_t last_mover_steps = 0;
+};
+
+namespace {
+
+int fail(gpat_handle_t *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(h, GPAT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+double fixed_to_double(unsigned long long hi, unsigned long long lo) {
+    return (double)hi + (double)lo * (1.0 / 18446744073709551616.0);
+}
+
+// Particle arrays carved out of one allocation, 256-byte aligned each.
+size_t particle_bytes(int64_t cap) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t c = (size_t)cap;
+    return 9 * al(8 * c) + 2 * al(c) + 6 * al(4 * c);
+}
+
+DevParticles carve(void *base, int64_t cap) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char *q = static_cast<char *>(base);
+    const size_t c = (size_t)cap;
+    DevParticles P{};
+    double **d[9] = {&P.x, &P.y, &P.z, &P.p, &P.v, &P.mu, &P.weight, &P.t, &P.dt};
+    for (auto *pp : d) { *pp = reinterpret_cast<double *>(q); q += al(8 * c); }
+    P.split_times = reinterpret_cast<int8_t *>(q); q += al(c);
+    P.count_flag = reinterpret_cast<int8_t *>(q); q += al(c);
+    int32_t **i4[5] = {&P.origin, &P.nsteps_tracked, &P.nsteps_pushed, &P.tag_injected,
+                       &P.tag_splitted};
+    for (auto *pp : i4) { *pp = reinterpret_cast<int32_t *>(q); q += al(4 * c); }
+    P.rng_ctr = reinterpret_cast<uint32_t *>(q);
+    return P;
+}
+
+int check_status(gpat_handle_t *h) {
+    if (h->hcnt.status) {
+        const unsigned s = h->hcnt.status;
+        std::string m = "device status:";
+        if (s & kStatusIndexGuard) m += " interpolation index outside the ghost cells;";
+        if (s & kStatusNonFinite) m += " non-finite particle state;";
+        if (s & kStatusStepLimit) m += " per-call push/iteration limit reached;";
+        CK(cudaMemsetAsync(&h->dcnt->status, 0, sizeof(unsigned int), h->stream));
+        h->hcnt.status = 0;
+        return fail(h, GPAT_ERR_DEVICE, m);
+    }
+    return GPAT_OK;
+}
+
+int pull_counters(gpat_handle_t *h) {
+    CK(cudaMemcpyAsync(&h->hcnt, h->dcnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+// conf.dat reading with the reference's get_variable semantics
+// (read_config.f90:20-44): scan forward line by line from the current
+// position for a line containing the key; the value is read list-directed
+// after the first delimiter, up to ';' or the end of the line.  A key that
+// is not found before EOF reads as -1 and leaves the file at EOF.
+struct ConfScanner {
+    std::vector<std::string> lines;
+    size_t pos = 0;
+    bool load(const char *path) {
+        FILE *f = std::fopen(path, "r");
+        if (!f) return false;
+        char buf[4096];
+        while (std::fgets(buf, sizeof buf, f)) {
+            std::string s(buf);
+            while (!s.empty() && (s.back() == '\n' || s.back() == '\r')) s.pop_back();
+            if (s.size() > 150) s.resize(150);   // character(len=150) single_line
+            lines.push_back(s);
+        }
+        std::fclose(f);
+        return true;
+    }
+    double get(const char *key, char delim = '=') {
+        while (pos < lines.size()) {
+            const std::string &s = lines[pos++];
+            if (s.find(key) != std::string::npos) return parse(s, delim);
+        }
+        return -1.0;
+    }
+    static double parse(const std::string &line, char delim) {
+        std::string s = line;
+        while (!s.empty() && (s.back() == ' ' || s.back() == '\t')) s.pop_back();
+        size_t end = s.size();
+        const size_t semi = s.find(';');
+        if (semi != std::string::npos) end = semi;
+        const size_t d = s.find(delim);
+        if (d == std::string::npos || d + 1 > end) return -1.0;
+        std::string v = s.substr(d + 1, end - d - 1);
+        for (char &c : v)
+            if (c == 'd' || c == 'D') c = 'e';   // Fortran D exponent
+        size_t a = v.find_first_not_of(" \t,");
+        if (a == std::string::npos) return -1.0;
+        char *stop = nullptr;
+        const double x = std::strtod(v.c_str() + a, &stop);
+        if (stop == v.c_str() + a) return -1.0;
+        return x;
+    }
+};
+
+int to_int_via_real4(double v) { return (int)(float)v; }
+
+int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fine_steps,
+               MoverArgs &a) {
+    const gpat_params_t &p = h->prm;
+    const gpat_mhd_config_t &c = h->cfg;
+    if (mhd_tframe < 1 || (size_t)mhd_tframe + 1 > h->tstamps.size())
+        return fail(h, GPAT_ERR_ARG, "mhd_tframe outside the time stamps");
+    if (nsteps_interval < 1 || num_fine_steps < 1)
+        return fail(h, GPAT_ERR_ARG, "nsteps_interval and num_fine_steps must be >= 1");
+    if (!h->rec_ready[0] || (p.time_interp && !h->rec_ready[1]))
+        return fail(h, GPAT_ERR_STATE, "fields and their gradients are not set");
+    std::memset(&a, 0, sizeof a);
+    a.P = h->P[h->cur];
+    a.n = h->n;
+    a.rec1 = h->rec[0];
+    a.rec2 = p.time_interp ? h->rec[1] : h->rec[0];
+    a.time_interp = p.time_interp;
+    a.ndim = p.ndim;
+    a.nxg = h->nxg; a.nyg = h->nyg; a.nzg = h->nzg;
+    a.nsteps_interval = nsteps_interval;
+    a.num_fine_steps = num_fine_steps;
+    a.dx = c.dx; a.dy = c.dy; a.dz = c.dz;
+    a.idx = 1.0 / c.dx; a.idy = 1.0 / c.dy; a.idz = 1.0 / c.dz;
+    // set_field_configuration on one rank (simulation_setup.f90:171-253).
+    a.xmin = c.xmin; a.xmax = c.xmin + (double)c.nx * c.dx;
+    a.ymin = c.ymin; a.ymax = c.ymin + (double)c.ny * c.dy;
+    a.zmin = c.zmin;
+    a.zmax = (p.ndim == 3) ? c.zmin + (double)c.nz * c.dz : c.zmax;
+    a.xmin1 = a.xmin - c.dx * 0.5; a.xmax1 = a.xmax + c.dx * 0.5;
+    a.ymin1 = a.ymin - c.dy * 0.5; a.ymax1 = a.ymax + c.dy * 0.5;
+    a.zmin1 = a.zmin - c.dz * 0.5; a.zmax1 = a.zmax + c.dz * 0.5;
+    a.cfg_xmin = c.xmin; a.cfg_ymin = c.ymin; a.cfg_zmin = c.zmin;
+    a.cfg_lx = c.lx; a.cfg_ly = c.ly; a.cfg_lz = c.lz;
+    a.t0 = h->tstamps[mhd_tframe - 1];
+    a.dtf = h->tstamps[mhd_tframe] - a.t0;
+    if (!(a.dtf > 0.0)) return fail(h, GPAT_ERR_ARG, "time stamps must increase");
+    // set_dt_min_max (particle_module.f90:5519-5524).
+    a.dt_min = p.dt_min_rel * a.dtf;
+    a.dt_max = p.dt_max_rel * a.dtf;
+    a.dt_fine = a.dtf / num_fine_steps;
+    a.limit = a.dtf + a.dt_fine * (double)0.1f;
+    const double dt_floor = std::min(a.dt_min, a.dt_max);
+    if (!(dt_floor > 0.0)) return fail(h, GPAT_ERR_ARG, "dt_min_rel and dt_max_rel must be > 0");
+    const double pushes = std::ceil(a.dtf / dt_floor) + 2.0 * num_fine_steps + 16.0;
+    if (pushes > 2.0e9) return fail(h, GPAT_ERR_ARG, "dtf / dt_min exceeds 2e9 pushes");
+    a.max_pushes = (uint32_t)pushes;
+    a.p0 = p.p0; a.pindex = p.pindex; a.gamma_turb = p.gamma_turb;
+    a.kpara0 = p.kpara0; a.kret = p.kret; a.drift1 = p.drift1; a.drift2 = p.drift2;
+    for (int i = 0; i < 6; ++i) a.acc_region[i] = p.acc_region[i];
+    a.charge = p.charge;
+    a.momentum_dependency = p.momentum_dependency;
+    a.mag_dependency = p.mag_dependency;
+    a.acc_region_flag = p.acc_region_flag;
+    a.check_drift_2d = p.check_drift_2d;
+    a.pbcx = p.pbcx; a.pbcy = p.pbcy; a.pbcz = p.pbcz;
+    a.noise = p.noise;
+    a.key0 = (uint32_t)p.seed;
+    a.key1 = (uint32_t)(p.seed >> 32);
+    a.cnt = h->dcnt;
+    return GPAT_OK;
+}
+
+int ensure_scratch(gpat_handle_t *h, int64_t n) {
+    const size_t need = compaction_scratch_bytes(n);
+    if (need <= h->scratch_bytes) return GPAT_OK;
+    if (h->scratch) CK(cudaFree(h->scratch));
+    h->scratch = nullptr;
+    CK(cudaMalloc(&h->scratch, need));
+    h->scratch_bytes = need;
+    return GPAT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gpat_version(void) { return "gpat-gb300 0.1 (sm_103a)"; }
+
+const char *gpat_last_error(const gpat_handle_t *h) { return h ? h->err.c_str() : "null handle"; }
+
+int gpat_get_variable(const char *conf_path, const char *key, double *value) {
+    if (!conf_path || !key || !value) return GPAT_ERR_ARG;
+    ConfScanner sc;
+    if (!sc.load(conf_path)) return GPAT_ERR_IO;
+    *value = sc.get(key);
+    return GPAT_OK;
+}
+
+int gpat_read_particle_params(const char *conf_path, gpat_params_t *p) {
+    if (!conf_path || !p) return GPAT_ERR_ARG;
+    ConfScanner sc;
+    if (!sc.load(conf_path)) return GPAT_ERR_IO;
+    // read_particle_params key order (particle_module.f90:2790-2815).
+    p->b0 = sc.get("b0");
+    p->p0 = sc.get("p0");
+    p->pmin = sc.get("pmin");
+    p->pmax = sc.get("pmax");
+    p->momentum_dependency = to_int_via_real4(sc.get("momentum_dependency"));
+    p->gamma_turb = sc.get("gamma_turb");
+    p->pindex = 3.0 - p->gamma_turb;
+    p->mag_dependency = to_int_via_real4(sc.get("mag_dependency"));
+    p->kpara0 = sc.get("kpara0");
+    p->kret = sc.get("kret");
+    p->dt_min_rel = sc.get("dt_min_rel");
+    p->dt_max_rel = sc.get("dt_max_rel");
+    p->acc_region_flag = to_int_via_real4(sc.get("acc_region_flag"));
+    double acc[6];
+    const char *acc_keys[6] = {"acc_xmin", "acc_xmax", "acc_ymin", "acc_ymax", "acc_zmin", "acc_zmax"};
+    for (int i = 0; i < 6; ++i) acc[i] = sc.get(acc_keys[i]);
+    if (p->acc_region_flag == 1) {
+        for (int i = 0; i < 6; ++i) p->acc_region[i] = acc[i];
+    } else {
+        const double dflt[6] = {0.0, 1.0, 0.0, 1.0, 0.0, 1.0};
+        for (int i = 0; i < 6; ++i) p->acc_region[i] = dflt[i];
+    }
+    // read_particle_boundary_conditions (simulation_setup.f90:104-150).
+    ConfScanner sb;
+    sb.load(conf_path);
+    p->pbcx = to_int_via_real4(sb.get("pbcx"));
+    p->pbcy = to_int_via_real4(sb.get("pbcy"));
+    p->pbcz = to_int_via_real4(sb.get("pbcz"));
+    // read_diagnostics_params (diagnostics.f90:2049-2100): npp_global first.
+    ConfScanner sd;
+    sd.load(conf_path);
+    const double npp = sd.get("npp_global");
+    if (npp > 0) p->npp_global = (int)npp;
+    return GPAT_OK;
+}
+
+int gpat_load_mhd_config(const char *path, gpat_mhd_config_t *cfg) {
+    // The file holds the 156 bytes of the record without trailing padding.
+    constexpr size_t kRecord = 13 * 8 + 13 * 4;
+    static_assert(offsetof(gpat_mhd_config_t, bcz) + 4 == kRecord, "mhd_config layout");
+    if (!path || !cfg) return GPAT_ERR_ARG;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return GPAT_ERR_IO;
+    std::memset(cfg, 0, sizeof(*cfg));
+    const size_t got = std::fread(cfg, 1, kRecord, f);
+    std::fclose(f);
+    return got == kRecord ? GPAT_OK : GPAT_ERR_IO;
+}
+
+int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int device,
+                gpat_handle_t **out) {
+    if (!params || !cfg || !out) return GPAT_ERR_ARG;
+    *out = nullptr;
+    const gpat_params_t &p = *params;
+    if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
+    if (p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag || p.include_3rd_dim ||
+        p.spherical_coord || p.nonuniform_grid)
+        return GPAT_ERR_UNSUPPORTED;
+    if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
+    if (p.noise != GPAT_NOISE_UNIFORM && p.noise != GPAT_NOISE_GAUSS) return GPAT_ERR_ARG;
+    if (p.nptl_max < 1 || p.nptl_max > (int64_t)2000000000) return GPAT_ERR_ARG;
+    if (p.npp_global < 1 || p.npp_global > 4096) return GPAT_ERR_ARG;
+    if (!(p.p0 > 0.0) || !(p.pmin > 0.0) || !(p.pmax > p.pmin)) return GPAT_ERR_ARG;
+    if (cfg->nx < 1 || cfg->ny < 1 || (p.ndim == 3 && cfg->nz < 1)) return GPAT_ERR_ARG;
+    if (!(cfg->dx > 0.0) || !(cfg->dy > 0.0) || (p.ndim == 3 && !(cfg->dz > 0.0))) return GPAT_ERR_ARG;
+
+    gpat_handle_t *h = new gpat_handle_t();
+    h->prm = p;
+    h->cfg = *cfg;
+    h->device = device;
+    auto bail = [&](int code) {
+        gpat_destroy(h);
+        return code;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(GPAT_ERR_CUDA);
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bail(GPAT_ERR_CUDA);
+    h->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+        return bail(GPAT_ERR_CUDA);
+    // init_field_data (mhd_data_parallel.f90:66-105): ghost cells on each
+    // resolved side; the z extent of a 2D run is nz (one plane).
+    h->nxg = cfg->nx + 4;
+    h->nyg = cfg->ny + 4;
+    h->nzg = (p.ndim == 3) ? cfg->nz + 4 : std::max(1, cfg->nz);
+    if (p.ndim == 2 && h->nzg != 1) return bail(GPAT_ERR_UNSUPPORTED);
+    h->ncells = (size_t)h->nxg * h->nyg * h->nzg;
+    h->nslots = p.time_interp ? 2 : 1;
+    const int R = (p.ndim == 2) ? kRec2D : kRec3D;
+    for (int s = 0; s < h->nslots; ++s) {
+        if (cudaMalloc(&h->full[s], 32 * sizeof(float) * h->ncells) != cudaSuccess ||
+            cudaMalloc(&h->rec[s], (size_t)R * sizeof(float) * h->ncells) != cudaSuccess)
+            return bail(GPAT_ERR_OOM);
+        cudaMemsetAsync(h->full[s], 0, 32 * sizeof(float) * h->ncells, h->stream);
+    }
+    // init_particles (particle_module.f90:177-258), double-buffered.
+    h->cap = p.nptl_max;
+    for (int b = 0; b < 2; ++b) {
+        if (cudaMalloc(&h->pmem[b], particle_bytes(h->cap)) != cudaSuccess) return bail(GPAT_ERR_OOM);
+        cudaMemsetAsync(h->pmem[b], 0, particle_bytes(h->cap), h->stream);
+        h->P[b] = carve(h->pmem[b], h->cap);
+    }
+    if (cudaMalloc(&h->dcnt, sizeof(DevCounters)) != cudaSuccess) return bail(GPAT_ERR_OOM);
+    cudaMemsetAsync(h->dcnt, 0, sizeof(DevCounters), h->stream);
+    if (cudaMalloc(&h->dbins, sizeof(unsigned long long) * 3 * (size_t)p.npp_global) != cudaSuccess)
+        return bail(GPAT_ERR_OOM);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(GPAT_ERR_CUDA);
+    *out = h;
+    return GPAT_OK;
+}
+
+int gpat_destroy(gpat_handle_t *h) {
+    if (!h) return GPAT_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (int s = 0; s < 2; ++s) {
+        if (h->full[s]) cudaFree(h->full[s]);
+        if (h->rec[s]) cudaFree(h->rec[s]);
+        if (h->pmem[s]) cudaFree(h->pmem[s]);
+    }
+    if (h->staging) cudaFree(h->staging);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->dcnt) cudaFree(h->dcnt);
+    if (h->dbins) cudaFree(h->dbins);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GPAT_OK;
+}
+
+int gpat_set_tstamps(gpat_handle_t *h, const double *ts, int n) {
+    if (!h || !ts || n < 2) return fail(h, GPAT_ERR_ARG, "need at least two time stamps");
+    h->tstamps.assign(ts, ts + n);
+    return GPAT_OK;
+}
+
+int gpat_calc_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end) {
+    if (!h || t_end <= t_start) return fail(h, GPAT_ERR_ARG, "t_end must exceed t_start");
+    // calc_tstamps_mhd (mhd_config.f90:263-271): tstamps(i) = i * dt_out.
+    h->tstamps.clear();
+    for (int i = t_start; i <= t_end; ++i) h->tstamps.push_back(i * h->cfg.dt_out);
+    return GPAT_OK;
+}
+
+int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nvar) {
+    if (!h || !farray || (nvar != 8 && nvar != 32)) return fail(h, GPAT_ERR_ARG, "nvar must be 8 or 32");
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots) return fail(h, GPAT_ERR_STATE, "farray2 needs time_interp = 1");
+    CK(cudaSetDevice(h->device));
+    if (nvar == 32) {
+        CK(cudaMemcpyAsync(h->full[slot], farray, 32 * sizeof(float) * h->ncells,
+                           cudaMemcpyHostToDevice, h->stream));
+        CK(launch_pack_records(h->full[slot], h->rec[slot], h->prm.ndim, h->ncells, h->stream));
+        h->rec_ready[slot] = true;
+    } else {
+        if (!h->staging) CK(cudaMalloc(&h->staging, 8 * sizeof(float) * h->ncells));
+        CK(cudaMemcpyAsync(h->staging, farray, 8 * sizeof(float) * h->ncells,
+                           cudaMemcpyHostToDevice, h->stream));
+        CK(launch_scatter_raw_fields(h->staging, 8, h->full[slot], h->ncells, h->stream));
+        h->rec_ready[slot] = false;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    h->fields_set[slot] = true;
+    return GPAT_OK;
+}
+
+int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag) {
+    if (!h || !filename) return GPAT_ERR_ARG;
+    FILE *f = std::fopen(filename, "rb");
+    if (!f) return fail(h, GPAT_ERR_IO, std::string("cannot open ") + filename);
+    std::vector<float> buf(8 * h->ncells);
+    const size_t got = std::fread(buf.data(), sizeof(float), buf.size(), f);
+    std::fclose(f);
+    if (got != buf.size()) return fail(h, GPAT_ERR_IO, std::string("short field file ") + filename);
+    return gpat_set_fields(h, var_flag, buf.data(), 8);
+}
+
+int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag) {
+    if (!h) return GPAT_ERR_ARG;
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots || !h->fields_set[slot]) return fail(h, GPAT_ERR_STATE, "fields not set");
+    CK(cudaSetDevice(h->device));
+    const gpat_mhd_config_t &c = h->cfg;
+    CK(launch_calc_fields_gradients(h->full[slot], h->prm.ndim, h->nxg, h->nyg, h->nzg, c.dx, c.dy,
+                                    c.dz, h->stream));
+    CK(launch_pack_records(h->full[slot], h->rec[slot], h->prm.ndim, h->ncells, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->rec_ready[slot] = true;
+    return GPAT_OK;
+}
+
+int gpat_copy_fields(gpat_handle_t *h) {
+    if (!h) return GPAT_ERR_ARG;
+    if (h->nslots < 2) return fail(h, GPAT_ERR_STATE, "copy_fields needs time_interp = 1");
+    CK(cudaSetDevice(h->device));
+    const int R = (h->prm.ndim == 2) ? kRec2D : kRec3D;
+    CK(cudaMemcpyAsync(h->full[0], h->full[1], 32 * sizeof(float) * h->ncells,
+                       cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->rec[0], h->rec[1], (size_t)R * sizeof(float) * h->ncells,
+                       cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->fields_set[0] = h->fields_set[1];
+    h->rec_ready[0] = h->rec_ready[1];
+    return GPAT_OK;
+}
+
+int gpat_get_fields(gpat_handle_t *h, int var_flag, float *farray) {
+    if (!h || !farray) return GPAT_ERR_ARG;
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots) return fail(h, GPAT_ERR_STATE, "no farray2");
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync(farray, h->full[slot], 32 * sizeof(float) * h->ncells,
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, double dt,
+                         int dist_flag, double particle_v0, int ct_mhd, const double *box,
+                         double power_index) {
+    if (nptl < 0) return fail(h, GPAT_ERR_ARG, "nptl < 0");
+    if (dist_flag < 0 || dist_flag > 2) return fail(h, GPAT_ERR_ARG, "dist_flag must be 0, 1 or 2");
+    if (ct_mhd < 1 || (size_t)ct_mhd + 1 > h->tstamps.size())
+        return fail(h, GPAT_ERR_ARG, "ct_mhd outside the time stamps");
+    CK(cudaSetDevice(h->device));
+    const int64_t room = h->cap - h->n;
+    const int64_t count = std::min(nptl, room);
+    InjectArgs a{};
+    a.P = h->P[h->cur];
+    a.base = h->n;
+    a.count = count;
+    a.tag0 = (int32_t)h->tag_max;
+    a.mode = mode;
+    a.dist_flag = dist_flag;
+    a.ndim = h->prm.ndim;
+    const gpat_mhd_config_t &c = h->cfg;
+    if (mode == 0) {
+        for (int i = 0; i < 6; ++i) a.box[i] = box[i];
+    } else {
+        a.box[0] = c.xmin; a.box[3] = c.xmin + (double)c.nx * c.dx;
+        a.box[1] = c.ymin; a.box[4] = c.ymin + (double)c.ny * c.dy;
+        a.box[2] = c.zmin;
+        a.box[5] = (h->prm.ndim == 3) ? c.zmin + (double)c.nz * c.dz : c.zmax;
+    }
+    a.xpos = xpos;
+    a.dt = dt;
+    a.particle_v0 = particle_v0;
+    a.t_frame = h->tstamps[ct_mhd - 1];
+    a.dt_mhd = h->tstamps[ct_mhd] - h->tstamps[ct_mhd - 1];
+    a.power_index = power_index;
+    a.p0 = h->prm.p0; a.pmin = h->prm.pmin; a.pmax = h->prm.pmax;
+    a.key0 = (uint32_t)h->prm.seed;
+    a.key1 = (uint32_t)(h->prm.seed >> 32);
+    CK(launch_inject(a, &h->dcnt->status, h->stream));
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    h->n += count;
+    h->tag_max += count;
+    rc = check_status(h);
+    if (rc) return rc;
+    if (count < nptl) return fail(h, GPAT_ERR_CAPACITY, "nptl_max reached while injecting");
+    return GPAT_OK;
+}
+
+int gpat_inject_particles_spatial_uniform(gpat_handle_t *h, int64_t nptl, double dt, int dist_flag,
+                                          double particle_v0, int ct_mhd, const double part_box[6],
+                                          double power_index) {
+    if (!h || !part_box) return GPAT_ERR_ARG;
+    return inject_common(h, 0, nptl, 0.0, dt, dist_flag, particle_v0, ct_mhd, part_box, power_index);
+}
+
+int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, double dt, int dist_flag,
+                               double particle_v0, int ct_mhd, double power_index) {
+    if (!h) return GPAT_ERR_ARG;
+    return inject_common(h, 1, nptl, xpos, dt, dist_flag, particle_v0, ct_mhd, nullptr, power_index);
+}
+
+int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n) {
+    if (!h || !src || n < 0) return GPAT_ERR_ARG;
+    if (n > h->cap) return fail(h, GPAT_ERR_CAPACITY, "more particles than nptl_max");
+    CK(cudaSetDevice(h->device));
+    const DevParticles &D = h->P[h->cur];
+    const size_t c = (size_t)n;
+    auto cp = [&](void *dst, const void *s, size_t bytes) -> cudaError_t {
+        if (!bytes) return cudaSuccess;
+        if (!s) return cudaErrorInvalidValue;
+        return cudaMemcpyAsync(dst, s, bytes, cudaMemcpyHostToDevice, h->stream);
+    };
+    CK(cp(D.x, src->x, 8 * c)); CK(cp(D.y, src->y, 8 * c)); CK(cp(D.z, src->z, 8 * c));
+    CK(cp(D.p, src->p, 8 * c)); CK(cp(D.v, src->v, 8 * c)); CK(cp(D.mu, src->mu, 8 * c));
+    CK(cp(D.weight, src->weight, 8 * c)); CK(cp(D.t, src->t, 8 * c)); CK(cp(D.dt, src->dt, 8 * c));
+    CK(cp(D.split_times, src->split_times, c)); CK(cp(D.count_flag, src->count_flag, c));
+    CK(cp(D.origin, src->origin, 4 * c)); CK(cp(D.nsteps_tracked, src->nsteps_tracked, 4 * c));
+    CK(cp(D.nsteps_pushed, src->nsteps_pushed, 4 * c));
+    CK(cp(D.tag_injected, src->tag_injected, 4 * c));
+    CK(cp(D.tag_splitted, src->tag_splitted, 4 * c));
+    CK(cp(D.rng_ctr, src->rng_ctr, 4 * c));
+    CK(cudaStreamSynchronize(h->stream));
+    h->n = n;
+    return GPAT_OK;
+}
+
+int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity, int64_t *n) {
+    if (!h || !dst || !n) return GPAT_ERR_ARG;
+    *n = h->n;
+    if (h->n > capacity) return fail(h, GPAT_ERR_CAPACITY, "destination too small");
+    CK(cudaSetDevice(h->device));
+    const DevParticles &S = h->P[h->cur];
+    const size_t c = (size_t)h->n;
+    auto cp = [&](void *d, const void *s, size_t bytes) -> cudaError_t {
+        if (!bytes || !d) return cudaSuccess;   // NULL destination: field skipped
+        return cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToHost, h->stream);
+    };
+    CK(cp(dst->x, S.x, 8 * c)); CK(cp(dst->y, S.y, 8 * c)); CK(cp(dst->z, S.z, 8 * c));
+    CK(cp(dst->p, S.p, 8 * c)); CK(cp(dst->v, S.v, 8 * c)); CK(cp(dst->mu, S.mu, 8 * c));
+    CK(cp(dst->weight, S.weight, 8 * c)); CK(cp(dst->t, S.t, 8 * c)); CK(cp(dst->dt, S.dt, 8 * c));
+    CK(cp(dst->split_times, S.split_times, c)); CK(cp(dst->count_flag, S.count_flag, c));
+    CK(cp(dst->origin, S.origin, 4 * c)); CK(cp(dst->nsteps_tracked, S.nsteps_tracked, 4 * c));
+    CK(cp(dst->nsteps_pushed, S.nsteps_pushed, 4 * c));
+    CK(cp(dst->tag_injected, S.tag_injected, 4 * c));
+    CK(cp(dst->tag_splitted, S.tag_splitted, 4 * c));
+    CK(cp(dst->rng_ctr, S.rng_ctr, 4 * c));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, double kperp_kpara,
+                        int nsteps_interval, int mhd_tframe, int num_fine_steps,
+                        int dump_escaped_dist) {
+    (void)kperp_kpara;
+    if (!h) return GPAT_ERR_ARG;
+    if (focused_transport || nlgc || dump_escaped_dist)
+        return fail(h, GPAT_ERR_UNSUPPORTED,
+                    "focused transport, NLGC and escaped-particle dumps are not in this engine");
+    MoverArgs a;
+    int rc = mover_args(h, mhd_tframe, nsteps_interval, num_fine_steps, a);
+    if (rc) return rc;
+    CK(cudaSetDevice(h->device));
+    rc = ensure_scratch(h, h->n);
+    if (rc) return rc;
+    const unsigned long long steps_before = h->hcnt.steps;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    if (h->prm.precision == GPAT_PREC_FP64) CK(launch_mover_fp64(a, h->sm_count, h->stream));
+    else CK(launch_mover_mixed(a, h->sm_count, h->stream));
+    CK(cudaEventRecord(h->ev1, h->stream));
+    // remove_particles (particle_module.f90:5365-5403), order-preserving.
+    const int nxt = 1 - h->cur;
+    CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt, h->stream));
+    rc = pull_counters(h);
+    if (rc) return rc;
+    h->cur = nxt;
+    h->n = (int64_t)h->hcnt.nkept;
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->last_mover_ms = ms;
+    h->last_mover_steps = h->hcnt.steps - steps_before;
+    return check_status(h);
+}
+
+int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split, int nsteps_interval) {
+    (void)nsteps_interval;
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_scratch(h, h->n);
+    if (rc) return rc;
+    const unsigned long long before = h->hcnt.nsplit;
+    CK(launch_split_particles(h->P[h->cur], h->n, h->cap, split_ratio, pmin_split, h->prm.p0,
+                              h->prm.pmax, h->scratch, h->dcnt, h->stream));
+    rc = pull_counters(h);
+    if (rc) return rc;
+    const int64_t created = (int64_t)(h->hcnt.nsplit - before);
+    const int64_t wanted = (int64_t)h->hcnt.nkept;
+    h->n += created;
+    h->nptl_split += created;
+    if (created < wanted) return fail(h, GPAT_ERR_CAPACITY, "nptl_max reached while splitting");
+    return GPAT_OK;
+}
+
+int gpat_calc_particle_distributions(gpat_handle_t *h, double *fglobal, uint64_t *counts) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    const int npp = h->prm.npp_global;
+    CK(launch_histogram(h->P[h->cur], h->n, npp, h->prm.pmin, h->prm.pmax, h->dbins, h->stream));
+    std::vector<unsigned long long> b(3 * (size_t)npp);
+    CK(cudaMemcpyAsync(b.data(), h->dbins, sizeof(unsigned long long) * b.size(),
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < npp; ++i) {
+        if (counts) counts[i] = b[3 * i];
+        if (fglobal) fglobal[i] = fixed_to_double(b[3 * i + 1], b[3 * i + 2]);
+    }
+    return GPAT_OK;
+}
+
+int gpat_pbins_edges(gpat_handle_t *h, double *edges) {
+    if (!h || !edges) return GPAT_ERR_ARG;
+    const double lo = std::log10(h->prm.pmin), hi = std::log10(h->prm.pmax);
+    const double d = (hi - lo) / h->prm.npp_global;
+    for (int i = 0; i <= h->prm.npp_global; ++i) edges[i] = std::pow(10.0, lo + i * d);
+    return GPAT_OK;
+}
+
+int gpat_quick_check(gpat_handle_t *h, double out[8]) {
+    if (!h || !out) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    DevCounters z{};
+    z.dt_min = 1.0;
+    z.dt_max = 0.0;
+    const size_t off = offsetof(DevCounters, wsum_hi);
+    const size_t len = offsetof(DevCounters, status) - off;
+    CK(cudaMemcpyAsync(reinterpret_cast<char *>(h->dcnt) + off, reinterpret_cast<char *>(&z) + off,
+                       len, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_quick_check(h->P[h->cur], h->n, h->dcnt, h->stream));
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    const DevCounters &c = h->hcnt;
+    out[0] = (double)h->n;
+    out[1] = (double)h->nptl_split;
+    out[2] = fixed_to_double(c.wsum_hi, c.wsum_lo);
+    out[3] = fixed_to_double(c.leak_hi, c.leak_lo);
+    out[4] = fixed_to_double(c.negp_hi, c.negp_lo);
+    out[5] = c.dt_min;
+    out[6] = c.dt_max;
+    out[7] = h->n > 0 ? fixed_to_double(c.dtsum_hi, c.dtsum_lo) / (double)h->n : 0.0;
+    return GPAT_OK;
+}
+
+int gpat_get_counters(gpat_handle_t *h, gpat_counters_t *out) {
+    if (!h || !out) return GPAT_ERR_ARG;
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    const DevCounters &c = h->hcnt;
+    out->nptl_current = h->n;
+    out->nptl_split = h->nptl_split;
+    out->nptl_escaped = (int64_t)c.nescaped;
+    out->tag_max = h->tag_max;
+    out->leak_hi = c.leak_hi; out->leak_lo = c.leak_lo;
+    out->leak_negp_hi = c.negp_hi; out->leak_negp_lo = c.negp_lo;
+    out->leak = fixed_to_double(c.leak_hi, c.leak_lo);
+    out->leak_negp = fixed_to_double(c.negp_hi, c.negp_lo);
+    out->steps = c.steps;
+    out->last_mover_ms = h->last_mover_ms;
+    out->last_mover_steps = h->last_mover_steps;
+    return GPAT_OK;
+}
+
+int gpat_set_counters(gpat_handle_t *h, const gpat_counters_t *in) {
+    if (!h || !in) return GPAT_ERR_ARG;
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    h->nptl_split = in->nptl_split;
+    h->tag_max = in->tag_max;
+    h->hcnt.leak_hi = in->leak_hi; h->hcnt.leak_lo = in->leak_lo;
+    h->hcnt.negp_hi = in->leak_negp_hi; h->hcnt.negp_lo = in->leak_negp_lo;
+    h->hcnt.nescaped = (unsigned long long)in->nptl_escaped;
+    h->hcnt.steps = in->steps;
+    CK(cudaMemcpyAsync(h->dcnt, &h->hcnt, sizeof(DevCounters), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+void *gpat_stream(gpat_handle_t *h) { return h ? (void *)h->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// Internal declarations shared by the engine's host code and CUDA kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "gpat_engine.h"
+
+namespace gpat {
+
+// Device status word bits (DevCounters::status).  Kernels never trap: they
+// record the condition, skip the access and let the host turn it into
+// GPAT_ERR_DEVICE.
+enum : unsigned int {
+    kStatusIndexGuard = 1u,   // interpolation cell outside the ghost range
+    kStatusNonFinite = 2u,    // NaN/Inf position, momentum or time
+    kStatusStepLimit = 4u,    // per-interval push limit reached
+};
+
+// particle_type as SoA device arrays (capacity entries each).
+struct DevParticles {
+    double *x, *y, *z, *p, *v, *mu, *weight, *t, *dt;
+    int8_t *split_times, *count_flag;
+    int32_t *origin, *nsteps_tracked, *nsteps_pushed, *tag_injected, *tag_splitted;
+    uint32_t *rng_ctr;
+};
+
+// Device-side accumulators.  Fixed-point sums are 128-bit (hi, lo) with 64
+// fraction bits.
+struct DevCounters {
+    unsigned long long leak_hi, leak_lo, negp_hi, negp_lo;
+    unsigned long long steps;
+    unsigned long long nescaped;
+    unsigned long long nkept;
+    unsigned long long nsplit;
+    unsigned long long wsum_hi, wsum_lo, dtsum_hi, dtsum_lo;
+    double dt_min, dt_max;
+    unsigned int status;
+    unsigned int pad;
+    unsigned long long bad_value;
+};
+
+// Packed per-cell field records read by the movers.  2D: 16 floats,
+// 3D: 24 floats (see fields.cu for the slot order).
+constexpr int kRec2D = 16;
+constexpr int kRec3D = 24;
+
+// Everything the mover kernels need, passed by value.
+struct MoverArgs {
+    DevParticles P;
+    int64_t n;
+    const float *rec1, *rec2;  // packed records, frame 1 and frame 2
+    int time_interp, ndim, nxg, nyg, nzg;
+    int nsteps_interval, num_fine_steps;
+    double dx, dy, dz, idx, idy, idz;
+    double xmin, ymin, zmin, xmax, ymax, zmax;          // exact box
+    double xmin1, xmax1, ymin1, ymax1, zmin1, zmax1;    // half-cell extended
+    double cfg_xmin, cfg_ymin, cfg_zmin, cfg_lx, cfg_ly, cfg_lz;
+    double dt_min, dt_max, t0, dtf, dt_fine, limit;
+    double p0, pindex, gamma_turb, kpara0, kret, drift1, drift2;
+    double acc_region[6];
+    int charge, momentum_dependency, mag_dependency, acc_region_flag;
+    int check_drift_2d, pbcx, pbcy, pbcz, noise;
+    uint32_t key0, key1;
+    uint32_t max_pushes;        // per particle per call, guards runaway loops
+    DevCounters *cnt;
+};
+
+// Launchers (defined in the .cu files).  All enqueue on `s`.
+cudaError_t launch_scatter_raw_fields(const float *raw, int nvar, float *full, size_t ncells,
+                                      cudaStream_t s);
+cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg, int nzg,
+                                         double dx, double dy, double dz, cudaStream_t s);
+cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
+                                cudaStream_t s);
+cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s);
+cudaError_t launch_mover_mixed(const MoverArgs &a, int sm_count, cudaStream_t s);
+
+struct InjectArgs {
+    DevParticles P;
+    int64_t base, count;
+    int32_t tag0;
+    int mode;         // 0: spatial uniform, 1: plane x = xpos
+    int dist_flag, ndim;
+    double box[6];    // xmin ymin zmin xmax ymax zmax
+    double xpos, dt, particle_v0, t_frame, dt_mhd, power_index;
+    double p0, pmin, pmax;
+    uint32_t key0, key1;
+};
+// Status bits (kStatusStepLimit on a runaway rejection loop) go to *status.
+cudaError_t launch_inject(const InjectArgs &a, unsigned int *status, cudaStream_t s);
+
+// Stable compaction of particles with count_flag == INBOX from src to dst.
+// scratch must hold compaction_scratch_bytes(n) bytes.
+size_t compaction_scratch_bytes(int64_t n);
+cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles &dst, int64_t n,
+                                    void *scratch, DevCounters *cnt, cudaStream_t s);
+// Splitting: children appended after n in parent order, at most cap - n.
+cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,
+                                   double split_ratio, double pmin_split, double p0,
+                                   double pmax, void *scratch, DevCounters *cnt,
+                                   cudaStream_t s);
+// Global f(p) histogram into (count, whi, wlo) triples per bin (zeroed here).
+cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double pmin,
+                             double pmax, unsigned long long *bins, cudaStream_t s);
+// quick_check reductions into cnt (wsum, dtsum, dt_min, dt_max).
+cudaError_t launch_quick_check(const DevParticles &P, int64_t n, DevCounters *cnt,
+                               cudaStream_t s);
+
+}  // namespace gpat

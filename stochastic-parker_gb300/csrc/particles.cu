@@ -1,0 +1,415 @@
+// Particle-set kernels around the mover: injection, stable removal
+// (remove_particles), splitting (split_particle), the global f(p) histogram
+// (calc_particle_distributions) and the quick_check reductions.
+#include <cfloat>
+
+#include "device_common.cuh"
+
+namespace gpat {
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kTile = kScanThreads * kScanItems;   // particles per block
+
+// ---------------------------------------------------------------------------
+// Injection (inject_one_particle and the two injectors, particle_module.f90:
+// 385-633).  One thread per new particle; its draws come from a Philox stream
+// keyed (seed_lo, seed_hi + 1) with counter (tag, call, 'INJC', 0).
+// ---------------------------------------------------------------------------
+struct InjStream {
+    uint32_t k0, k1, tag, call;
+    double buf0, buf1;
+    int avail;
+    __device__ double next() {
+        if (avail == 0) {
+            const uint4 w = philox4x32_10(make_uint4(tag, call, 0x494E4A43u, 0u), k0, k1);
+            call += 1u;
+            buf0 = u01_53(w.x, w.y);
+            buf1 = u01_53(w.z, w.w);
+            avail = 2;
+        }
+        const double u = (avail == 2) ? buf0 : buf1;
+        avail -= 1;
+        return u;
+    }
+};
+
+constexpr int kMaxRejections = 1 << 22;
+
+__device__ double draw_p_power(const InjectArgs &a, InjStream &s) {
+    const double r01 = s.next();
+    if ((int)a.power_index == 1) return pow(a.pmax / a.p0, r01) * a.p0;
+    const double norm = pow(a.pmax, -a.power_index + 1.0) - pow(a.p0, -a.power_index + 1.0);
+    return pow(r01 * norm + pow(a.p0, -a.power_index + 1.0), 1.0 / (-a.power_index + 1.0));
+}
+
+__global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.count) return;
+    const int32_t tag = a.tag0 + (int32_t)i;
+    InjStream s{a.key0, a.key1 + 1u, (uint32_t)tag, 0u, 0.0, 0.0, 0};
+    double x, y, z, p = a.p0, mu, t;
+    const double mu_max = (double)0.99f;
+    if (a.mode == 0) {
+        x = s.next() * (a.box[3] - a.box[0]) + a.box[0];
+        y = s.next() * (a.box[4] - a.box[1]) + a.box[1];
+        z = s.next() * (a.box[5] - a.box[2]) + a.box[2];
+        mu = mu_max * (2.0 * s.next() - 1.0);
+        if (a.dist_flag == 0) {
+            double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
+            int it = 0;
+            while (ftest > fxp) {
+                if (++it > kMaxRejections) { atomicOr(status, kStatusStepLimit); break; }
+                ptmp = (s.next() * (a.pmax - a.pmin) + a.pmin) / a.p0;
+                fxp = ptmp * ptmp * exp(-(ptmp * ptmp));
+                ftest = s.next() * (double)0.37f;
+            }
+            p = ptmp * a.p0;
+        } else if (a.dist_flag == 2) {
+            p = draw_p_power(a, s);
+        }
+        t = a.t_frame + s.next() * a.dt_mhd;
+    } else {
+        x = a.xpos;
+        y = s.next() * (a.box[4] - a.box[1]) + a.box[1];
+        z = s.next() * (a.box[5] - a.box[2]) + a.box[2];
+        if (a.dist_flag == 0) {
+            double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
+            int it = 0;
+            while (ftest > fxp) {
+                if (++it > kMaxRejections) { atomicOr(status, kStatusStepLimit); break; }
+                ptmp = (s.next() * (a.pmax - a.pmin) + a.pmin) / a.p0;
+                fxp = ptmp * ptmp * exp((double)(-0.5f) * (ptmp * ptmp));
+                ftest = s.next() * (double)0.75f;
+            }
+            p = ptmp * a.p0;
+        } else if (a.dist_flag == 2) {
+            p = draw_p_power(a, s);
+        }
+        mu = mu_max * (2.0 * s.next() - 1.0);
+        t = a.t_frame;
+    }
+    const int64_t c = a.base + i;
+    a.P.x[c] = x; a.P.y[c] = y; a.P.z[c] = z; a.P.p[c] = p;
+    a.P.v[c] = a.particle_v0 * p / a.p0;
+    a.P.mu[c] = mu; a.P.weight[c] = 1.0; a.P.t[c] = t; a.P.dt[c] = a.dt;
+    a.P.split_times[c] = 0; a.P.count_flag[c] = 1; a.P.origin[c] = 0;
+    a.P.nsteps_tracked[c] = 0; a.P.nsteps_pushed[c] = 0;
+    a.P.tag_injected[c] = tag; a.P.tag_splitted[c] = 1; a.P.rng_ctr[c] = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Block-tiled stable stream compaction: count per tile, scan the tile
+// counts, scatter with warp-ballot prefixes.  The tile counts and offsets
+// are the scratch buffer (2 * nblocks int64).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double split_threshold(double pmin_split, double p0, double ratio,
+                                                  int k) {
+    double rk = 1.0;
+    for (int j = 0; j < k; ++j) rk = rk * ratio;
+    return pmin_split * p0 * rk;
+}
+
+struct SplitRule {
+    double ratio, pmin_split, p0, pmax;
+};
+
+// mode 0: keep count_flag == INBOX; mode 1: split candidates.
+template <int MODE>
+__device__ __forceinline__ bool select(const DevParticles &P, int64_t i, const SplitRule &r) {
+    if (MODE == 0) return P.count_flag[i] == 1;
+    const double p = P.p[i];
+    return p > split_threshold(r.pmin_split, r.p0, r.ratio, P.split_times[i]) && p <= r.pmax;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kScanThreads) tile_count_kernel(const DevParticles P, int64_t n,
+                                                                  SplitRule r, long long *tile_counts,
+                                                                  DevCounters *cnt) {
+    __shared__ int warp_tot[kScanThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * kTile;
+    int mine = 0, esc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k * kScanThreads + threadIdx.x;
+        if (i < n) {
+            mine += select<MODE>(P, i, r) ? 1 : 0;
+            if (MODE == 0 && P.count_flag[i] < 0) esc += 1;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mine += __shfl_xor_sync(0xffffffffu, mine, o);
+        esc += __shfl_xor_sync(0xffffffffu, esc, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        warp_tot[threadIdx.x >> 5] = mine;
+        if (MODE == 0 && esc) atomicAdd(&cnt->nescaped, (unsigned long long)esc);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += warp_tot[w];
+        tile_counts[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of the tile counts by one block; writes offsets and the total.
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const long long *tile_counts,
+                                                         long long *tile_offsets, int64_t ntiles,
+                                                         unsigned long long *total) {
+    __shared__ long long warp_sums[32];
+    __shared__ long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < ntiles; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const long long v = (i < ntiles) ? tile_counts[i] : 0;
+        long long x = v;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            long long ws = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += y;
+            }
+            warp_sums[lane] = ws;
+        }
+        __syncthreads();
+        const long long excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+        if (i < ntiles) tile_offsets[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = (unsigned long long)carry;
+}
+
+__device__ __forceinline__ void copy_particle(const DevParticles &S, int64_t i,
+                                              const DevParticles &D, int64_t j) {
+    D.x[j] = S.x[i]; D.y[j] = S.y[i]; D.z[j] = S.z[i]; D.p[j] = S.p[i];
+    D.v[j] = S.v[i]; D.mu[j] = S.mu[i]; D.weight[j] = S.weight[i];
+    D.t[j] = S.t[i]; D.dt[j] = S.dt[i];
+    D.split_times[j] = S.split_times[i]; D.count_flag[j] = S.count_flag[i];
+    D.origin[j] = S.origin[i]; D.nsteps_tracked[j] = S.nsteps_tracked[i];
+    D.nsteps_pushed[j] = S.nsteps_pushed[i]; D.tag_injected[j] = S.tag_injected[i];
+    D.tag_splitted[j] = S.tag_splitted[i]; D.rng_ctr[j] = S.rng_ctr[i];
+}
+
+// MODE 0: kept particles of S go to D in order.  MODE 1: S == D; each split
+// candidate gets a child at n + rank (if < cap) and is updated in place.
+template <int MODE>
+__global__ void __launch_bounds__(kScanThreads) tile_scatter_kernel(
+    const DevParticles S, const DevParticles D, int64_t n, int64_t cap, SplitRule r,
+    const long long *tile_offsets, DevCounters *cnt) {
+    __shared__ int warp_pre[kScanThreads / 32];
+    __shared__ int sub_total;
+    const int64_t base = (int64_t)blockIdx.x * kTile;
+    long long running = tile_offsets[blockIdx.x];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int created = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k * kScanThreads + threadIdx.x;
+        const bool sel = (i < n) && select<MODE>(S, i, r);
+        const unsigned bal = __ballot_sync(0xffffffffu, sel);
+        const int wpre = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) warp_pre[wid] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int w = 0; w < kScanThreads / 32; ++w) {
+                const int c = warp_pre[w];
+                warp_pre[w] = acc;
+                acc += c;
+            }
+            sub_total = acc;
+        }
+        __syncthreads();
+        if (sel) {
+            const long long rank = running + warp_pre[wid] + wpre;
+            if (MODE == 0) {
+                copy_particle(S, i, D, rank);
+            } else {
+                const int64_t c = n + rank;
+                if (c < cap) {
+                    const int kk = S.split_times[i];
+                    S.weight[i] = ldexp(1.0, -(kk + 1));
+                    S.split_times[i] = (int8_t)(kk + 1);
+                    copy_particle(S, i, S, c);
+                    S.tag_splitted[c] = (int32_t)((uint32_t)S.tag_splitted[i] + (1u << kk));
+                    created += 1;
+                }
+            }
+        }
+        running += sub_total;
+        __syncthreads();
+    }
+    if (MODE == 1) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) created += __shfl_xor_sync(0xffffffffu, created, o);
+        if (lane == 0 && created) atomicAdd(&cnt->nsplit, (unsigned long long)created);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Global f(p) histogram: block-private shared bins (count, weight hi, lo),
+// warp-aggregated by bin with __match_any_sync, exact 128-bit weights.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) histogram_kernel(const DevParticles P, int64_t n, int npp,
+                                                        double pmin, double pmax, double pmin_log,
+                                                        double dp_log, unsigned long long *bins) {
+    extern __shared__ unsigned long long sh[];  // 3 * npp
+    for (int b = threadIdx.x; b < 3 * npp; b += blockDim.x) sh[b] = 0ull;
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t iters = (n + stride - 1) / stride;
+    for (int64_t it = 0; it < iters; ++it) {
+        const int64_t i = start + it * stride;
+        int bin = -1;
+        unsigned long long wh = 0, wl = 0;
+        if (i < n) {
+            const double p = P.p[i], mu = P.mu[i];
+            if (p > pmin && p <= pmax && mu >= -1.0 && mu <= 1.0) {
+                const int ip = (int)floor((log10(p) - pmin_log) / dp_log);
+                if (ip >= 0 && ip < npp) {
+                    bin = ip;
+                    fixed_split(P.weight[i], wh, wl);
+                }
+            }
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, bin);
+        const int leader = __ffs(grp) - 1;
+        unsigned long long sh_h = 0, sh_l = 0;
+        unsigned m = grp;
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const unsigned long long oh = __shfl_sync(grp, wh, src);
+            const unsigned long long ol = __shfl_sync(grp, wl, src);
+            add_u128(sh_h, sh_l, oh, ol);
+        }
+        if (bin >= 0 && (int)(threadIdx.x & 31) == leader) {
+            atomicAdd(&sh[3 * bin], (unsigned long long)__popc(grp));
+            atomic_add_u128(&sh[3 * bin + 1], &sh[3 * bin + 2], sh_h, sh_l);
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < npp; b += blockDim.x) {
+        if (sh[3 * b]) atomicAdd(&bins[3 * b], sh[3 * b]);
+        atomic_add_u128(&bins[3 * b + 1], &bins[3 * b + 2], sh[3 * b + 1], sh[3 * b + 2]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// quick_check: exact sums of weight and dt, min/max dt (positive doubles
+// order like their bit patterns).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) quick_check_kernel(const DevParticles P, int64_t n,
+                                                          DevCounters *cnt) {
+    unsigned long long wh = 0, wl = 0, th = 0, tl = 0;
+    double mn = 1.0, mx = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        unsigned long long h, l;
+        fixed_split(P.weight[i], h, l);
+        add_u128(wh, wl, h, l);
+        const double dt = P.dt[i];
+        fixed_split(dt, h, l);
+        add_u128(th, tl, h, l);
+        if (dt < mn) mn = dt;
+        if (dt > mx) mx = dt;
+    }
+    warp_sum_u128(wh, wl);
+    warp_sum_u128(th, tl);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_add_u128(&cnt->wsum_hi, &cnt->wsum_lo, wh, wl);
+        atomic_add_u128(&cnt->dtsum_hi, &cnt->dtsum_lo, th, tl);
+        if (mn >= 0.0)
+            atomicMin(reinterpret_cast<unsigned long long *>(&cnt->dt_min),
+                      (unsigned long long)__double_as_longlong(mn));
+        if (mx >= 0.0)
+            atomicMax(reinterpret_cast<unsigned long long *>(&cnt->dt_max),
+                      (unsigned long long)__double_as_longlong(mx));
+    }
+}
+
+}  // namespace
+
+size_t compaction_scratch_bytes(int64_t n) {
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    return (size_t)(2 * (ntiles > 0 ? ntiles : 1)) * sizeof(long long);
+}
+
+cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles &dst, int64_t n,
+                                    void *scratch, DevCounters *cnt, cudaStream_t s) {
+    if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    long long *counts = static_cast<long long *>(scratch);
+    long long *offsets = counts + ntiles;
+    const SplitRule r{0, 0, 0, 0};
+    tile_count_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
+    tile_scatter_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, n, r, offsets, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,
+                                   double split_ratio, double pmin_split, double p0, double pmax,
+                                   void *scratch, DevCounters *cnt, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    long long *counts = static_cast<long long *>(scratch);
+    long long *offsets = counts + ntiles;
+    const SplitRule r{split_ratio, pmin_split, p0, pmax};
+    tile_count_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, n, r, counts, cnt);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
+    tile_scatter_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, P, n, cap, r, offsets, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double pmin, double pmax,
+                             unsigned long long *bins, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * (size_t)npp, s);
+    if (e != cudaSuccess || n <= 0) return e;
+    const double pmin_log = log10(pmin), pmax_log = log10(pmax);
+    const double dp_log = (pmax_log - pmin_log) / npp;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    const size_t shmem = sizeof(unsigned long long) * 3 * (size_t)npp;
+    histogram_kernel<<<(unsigned)blocks, 256, shmem, s>>>(P, n, npp, pmin, pmax, pmin_log, dp_log,
+                                                          bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quick_check(const DevParticles &P, int64_t n, DevCounters *cnt, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 2048) blocks = 2048;
+    quick_check_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, n, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inject(const InjectArgs &a, unsigned int *status, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    const int threads = 128;
+    const int64_t blocks = (a.count + threads - 1) / threads;
+    inject_kernel<<<(unsigned)blocks, threads, 0, s>>>(a, status);
+    return cudaGetLastError();
+}
+
+}  // namespace gpat

@@ -1,0 +1,81 @@
+"""Builds the engine's shared library (CUDA kernels + C ABI) for sm_103a.
+
+The library is compiled in-tree into ``gpat/_lib/libgpat_engine.so`` with
+nvcc, one translation unit per process, then linked.  ``mover_fp64.cu`` is
+compiled with ``-fmad=false`` so the FP64 mover keeps the reference's
+separately rounded operations; every other unit may contract to FMA.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+PROJECT_DIR = PKG_DIR.parent                  # stochastic-parker_gb300/
+REPO_DIR = PROJECT_DIR.parent
+CSRC = PROJECT_DIR / "csrc"
+INCLUDE = REPO_DIR / "include"
+LIB_DIR = PKG_DIR / "_lib"
+BUILD_DIR = PROJECT_DIR / "_build"
+LIB_PATH = LIB_DIR / "libgpat_engine.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = {
+    "gpat_engine.cpp": [],
+    "fields.cu": [],
+    "particles.cu": [],
+    "mover_fp64.cu": ["-fmad=false"],
+    "mover_mixed.cu": [],
+}
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the engine needs the CUDA toolkit to build")
+
+
+def _compile(src: str, extra: list[str], nvcc: str, verbose_ptxas: bool) -> Path:
+    out = BUILD_DIR / (src.replace(".", "_") + ".o")
+    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-I", str(INCLUDE), "-I", str(CSRC), *extra, "-c", str(CSRC / src), "-o", str(out)]
+    if src.endswith(".cpp"):
+        cmd[1:1] = ["-x", "cu"]
+    if verbose_ptxas and src.endswith(".cu"):
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+    if verbose_ptxas:
+        (BUILD_DIR / (src + ".ptxas.txt")).write_text(res.stderr)
+    return out
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    """Compiles and links the engine; returns the library path."""
+    srcs = [CSRC / s for s in SOURCES] + [INCLUDE / "gpat_engine.h",
+                                          CSRC / "gpat_internal.h", CSRC / "device_common.cuh"]
+    if LIB_PATH.exists() and not force:
+        lib_mtime = LIB_PATH.stat().st_mtime
+        if all(s.stat().st_mtime <= lib_mtime for s in srcs):
+            return LIB_PATH
+    nvcc = nvcc_path()
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    LIB_DIR.mkdir(parents=True, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], nvcc, verbose_ptxas), SOURCES.items()))
+    tmp = LIB_PATH.with_suffix(".so.tmp")
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose_ptxas=True))

@@ -1,0 +1,294 @@
+"""Host-side mirror of the reference's particle/MHD-data module API.
+
+``Engine`` wraps one handle of the C ABI (include/gpat_engine.h).  Its
+methods carry the names and argument meanings of the Fortran procedures the
+reference driver (src/programs/stochastic-mhd.f90:312-567) calls on the
+mover path: read_particle_params, calc_fields_gradients, copy_fields,
+inject_particles_spatial_uniform, particle_mover, split_particle,
+calc_particle_distributions (global f(p)) and quick_check.  Errors raise
+GPATError with the engine's code and message; nothing falls back to a host
+implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+
+REFERENCE_DEFAULTS = dict(
+    # conf.dat sample values (config/conf.dat) and CLI defaults
+    # (stochastic-mhd.f90:636-946) for the fields the mover reads.
+    b0=1.0, p0=0.1, pmin=1.0e-2, pmax=1.0e1,
+    momentum_dependency=1, gamma_turb=5.0 / 3.0, mag_dependency=0,
+    kpara0=0.01, kret=0.05, dt_min_rel=1.0e-4, dt_max_rel=1.0e-2,
+    acc_region_flag=0, acc_region=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0),
+    drift1=4.0e7, drift2=2.0e8, charge=-1, check_drift_2d=0,
+    ndim=2, pbcx=0, pbcy=0, pbcz=0, npp_global=128,
+    seed=0x5EED0001, noise=_abi.NOISE_UNIFORM, precision=_abi.PREC_FP64,
+    nptl_max=100_000, time_interp=0,
+)
+
+
+class GPATError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        self.code = code
+        super().__init__(f"{_abi.ERROR_NAMES.get(code, code)}: {message}")
+
+
+class GPATCapacityError(GPATError):
+    pass
+
+
+def make_params(**kw) -> _abi.Params:
+    """Builds a gpat_params_t from keyword values over REFERENCE_DEFAULTS.
+
+    pindex defaults to 3 - gamma_turb as in read_particle_params
+    (particle_module.f90:2798)."""
+    vals = dict(REFERENCE_DEFAULTS)
+    vals.update(kw)
+    if "pindex" not in kw:
+        vals["pindex"] = 3.0 - vals["gamma_turb"]
+    p = _abi.Params()
+    for name, _ in _abi.Params._fields_:
+        if name == "acc_region":
+            p.acc_region = (C.c_double * 6)(*vals["acc_region"])
+        elif name in vals:
+            setattr(p, name, vals[name])
+    return p
+
+
+def params_dict(p: _abi.Params) -> dict:
+    out = {}
+    for name, _ in _abi.Params._fields_:
+        v = getattr(p, name)
+        out[name] = tuple(v) if name == "acc_region" else v
+    return out
+
+
+def make_mhd_config(nx, ny, nz, xmin, xmax, ymin, ymax, zmin=0.0, zmax=1.0, dt_out=1.0,
+                    ndim=2) -> _abi.MhdConfig:
+    """mhd_config for a uniform grid of nx*ny(*nz) cells spanning the box."""
+    c = _abi.MhdConfig()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.dx = (xmax - xmin) / nx
+    c.dy = (ymax - ymin) / ny
+    c.dz = (zmax - zmin) / nz if ndim == 3 else (zmax - zmin)
+    c.xmin, c.xmax, c.ymin, c.ymax, c.zmin, c.zmax = xmin, xmax, ymin, ymax, zmin, zmax
+    c.lx, c.ly, c.lz = xmax - xmin, ymax - ymin, zmax - zmin
+    c.dt_out = dt_out
+    c.nxs, c.nys, c.nzs = nx, ny, nz
+    c.topox = c.topoy = c.topoz = 1
+    c.nvar = 8
+    return c
+
+
+@dataclass
+class ParticleSet:
+    """particle_type as numpy structure-of-arrays."""
+    arrays: dict
+
+    @classmethod
+    def empty(cls, n: int) -> "ParticleSet":
+        return cls({name: np.zeros(n, dtype=t) for name, t in _abi.PARTICLE_FIELDS})
+
+    def __len__(self) -> int:
+        return len(self.arrays["x"])
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+    def ctypes(self) -> _abi.Particles:
+        s = _abi.Particles()
+        for name, t in _abi.PARTICLE_FIELDS:
+            a = self.arrays[name]
+            assert a.flags["C_CONTIGUOUS"] and a.dtype == np.dtype(t), name
+            setattr(s, name, a.ctypes.data_as(C.POINTER(_abi._CT[t])))
+        return s
+
+    def copy(self) -> "ParticleSet":
+        return ParticleSet({k: v.copy() for k, v in self.arrays.items()})
+
+    def take(self, idx) -> "ParticleSet":
+        return ParticleSet({k: np.ascontiguousarray(v[idx]) for k, v in self.arrays.items()})
+
+    def order_by_tags(self) -> "ParticleSet":
+        """Canonical order (tag_injected, tag_splitted), for set comparisons."""
+        key = (self.arrays["tag_injected"].astype(np.int64) << 32) | \
+              (self.arrays["tag_splitted"].astype(np.int64) & 0xFFFFFFFF)
+        return self.take(np.argsort(key, kind="stable"))
+
+
+def read_particle_params(conf_path: str | Path, base: _abi.Params | None = None) -> _abi.Params:
+    """read_particle_params (particle_module.f90:2778-2878) via the engine."""
+    lib = _abi.load()
+    p = base if base is not None else make_params()
+    rc = lib.gpat_read_particle_params(str(conf_path).encode(), C.byref(p))
+    if rc != _abi.GPAT_OK:
+        raise GPATError(rc, f"cannot read {conf_path}")
+    return p
+
+
+def load_mhd_config(path: str | Path) -> _abi.MhdConfig:
+    lib = _abi.load()
+    c = _abi.MhdConfig()
+    rc = lib.gpat_load_mhd_config(str(path).encode(), C.byref(c))
+    if rc != _abi.GPAT_OK:
+        raise GPATError(rc, f"cannot read {path}")
+    return c
+
+
+class Engine:
+    """One GPAT rank's mover state on one GPU."""
+
+    def __init__(self, params: _abi.Params, mhd_config: _abi.MhdConfig, device: int = 0):
+        self.lib = _abi.load()
+        self.params = params
+        self.cfg = mhd_config
+        self.h = _abi.Handle()
+        rc = self.lib.gpat_create(C.byref(params), C.byref(mhd_config), device, C.byref(self.h))
+        if rc != _abi.GPAT_OK:
+            raise GPATError(rc, "gpat_create failed")
+        self.ndim = params.ndim
+        self.nxg = mhd_config.nx + 4
+        self.nyg = mhd_config.ny + 4
+        self.nzg = mhd_config.nz + 4 if params.ndim == 3 else 1
+
+    # -- plumbing ---------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc == _abi.GPAT_OK:
+            return
+        msg = self.lib.gpat_last_error(self.h).decode()
+        if rc == _abi.GPAT_ERR_CAPACITY:
+            raise GPATCapacityError(rc, msg)
+        raise GPATError(rc, msg)
+
+    def close(self):
+        if self.h:
+            self.lib.gpat_destroy(self.h)
+            self.h = _abi.Handle()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        """The engine's cudaStream_t as an integer handle."""
+        return self.lib.gpat_stream(self.h) or 0
+
+    # -- time stamps and fields --------------------------------------------------
+    def set_tstamps(self, tstamps):
+        ts = np.ascontiguousarray(tstamps, dtype=np.float64)
+        self._check(self.lib.gpat_set_tstamps(self.h, ts.ctypes.data_as(C.POINTER(C.c_double)),
+                                              len(ts)))
+
+    def calc_tstamps_mhd(self, t_start: int, t_end: int):
+        self._check(self.lib.gpat_calc_tstamps_mhd(self.h, t_start, t_end))
+
+    def field_shape(self, nvar: int = 8):
+        """numpy (C order) shape of a Fortran (nvar, nxg, nyg, nzg) array."""
+        return (self.nzg, self.nyg, self.nxg, nvar)
+
+    def set_fields(self, farray: np.ndarray, var_flag: int = 0):
+        a = np.ascontiguousarray(farray, dtype=np.float32)
+        nvar = a.shape[-1]
+        if a.shape != self.field_shape(nvar):
+            raise ValueError(f"field array shape {a.shape} != {self.field_shape(nvar)}")
+        self._check(self.lib.gpat_set_fields(self.h, var_flag,
+                                             a.ctypes.data_as(C.POINTER(C.c_float)), nvar))
+
+    def read_field_data(self, filename: str | Path, var_flag: int = 0):
+        self._check(self.lib.gpat_read_field_data(self.h, str(filename).encode(), var_flag))
+
+    def calc_fields_gradients(self, var_flag: int = 0):
+        self._check(self.lib.gpat_calc_fields_gradients(self.h, var_flag))
+
+    def copy_fields(self):
+        self._check(self.lib.gpat_copy_fields(self.h))
+
+    def get_fields(self, var_flag: int = 0) -> np.ndarray:
+        out = np.empty(self.field_shape(32), dtype=np.float32)
+        self._check(self.lib.gpat_get_fields(self.h, var_flag,
+                                             out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    # -- particles ---------------------------------------------------------------
+    def inject_particles_spatial_uniform(self, nptl, dt, dist_flag, particle_v0, ct_mhd,
+                                         part_box, power_index=7.0):
+        box = (C.c_double * 6)(*part_box)
+        self._check(self.lib.gpat_inject_particles_spatial_uniform(
+            self.h, int(nptl), dt, dist_flag, particle_v0, ct_mhd, box, power_index))
+
+    def inject_particles_at_x(self, nptl, xpos, dt, dist_flag, particle_v0, ct_mhd,
+                              power_index=7.0):
+        self._check(self.lib.gpat_inject_particles_at_x(
+            self.h, int(nptl), xpos, dt, dist_flag, particle_v0, ct_mhd, power_index))
+
+    def put_particles(self, ps: ParticleSet):
+        s = ps.ctypes()
+        self._check(self.lib.gpat_put_particles(self.h, C.byref(s), len(ps)))
+
+    def get_particles(self) -> ParticleSet:
+        n = self.counters().nptl_current
+        ps = ParticleSet.empty(n)
+        s = ps.ctypes()
+        got = C.c_int64()
+        self._check(self.lib.gpat_get_particles(self.h, C.byref(s), n, C.byref(got)))
+        return ps
+
+    @property
+    def nptl_current(self) -> int:
+        return self.counters().nptl_current
+
+    # -- the mover path -----------------------------------------------------------
+    def particle_mover(self, focused_transport=False, nlgc=False, kperp_kpara=0.0,
+                       nsteps_interval=10, mhd_tframe=1, num_fine_steps=1,
+                       dump_escaped_dist=False):
+        self._check(self.lib.gpat_particle_mover(
+            self.h, int(focused_transport), int(nlgc), kperp_kpara, nsteps_interval,
+            mhd_tframe, num_fine_steps, int(dump_escaped_dist)))
+
+    def split_particle(self, split_ratio=2.72, pmin_split=2.0, nsteps_interval=10):
+        self._check(self.lib.gpat_split_particle(self.h, split_ratio, pmin_split, nsteps_interval))
+
+    def calc_particle_distributions(self):
+        """Global f(p): (fglobal[npp], counts[npp])."""
+        npp = self.params.npp_global
+        f = np.zeros(npp, dtype=np.float64)
+        c = np.zeros(npp, dtype=np.uint64)
+        self._check(self.lib.gpat_calc_particle_distributions(
+            self.h, f.ctypes.data_as(C.POINTER(C.c_double)),
+            c.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return f, c
+
+    def pbins_edges(self) -> np.ndarray:
+        e = np.zeros(self.params.npp_global + 1, dtype=np.float64)
+        self._check(self.lib.gpat_pbins_edges(self.h, e.ctypes.data_as(C.POINTER(C.c_double))))
+        return e
+
+    def quick_check(self) -> dict:
+        out = (C.c_double * 8)()
+        self._check(self.lib.gpat_quick_check(self.h, out))
+        keys = ("nptl_current", "nptl_split", "ntot", "leak", "leak_negp", "pdt_min",
+                "pdt_max", "pdt_avg")
+        return dict(zip(keys, list(out)))
+
+    def counters(self) -> _abi.Counters:
+        c = _abi.Counters()
+        self._check(self.lib.gpat_get_counters(self.h, C.byref(c)))
+        return c
+
+    def set_counters(self, c: _abi.Counters):
+        self._check(self.lib.gpat_set_counters(self.h, C.byref(c)))

@@ -1,0 +1,150 @@
+"""C ABI and host logic without a GPU: the library loads, exports every
+symbol include/gpat_engine.h declares, and its host-only entry points (the
+conf.dat and mhd_config readers, argument checks) behave like the
+reference's."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gpat import _abi, fields
+from gpat.engine import make_mhd_config, make_params, read_particle_params, load_mhd_config
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "gpat_engine.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(gpat_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(engine_lib, n), n
+    assert set(names) == set(_abi.SIGNATURES), "ctypes table out of sync with the header"
+    assert engine_lib.gpat_version().startswith(b"gpat-gb300")
+
+
+def test_struct_layouts_match_header():
+    # gpat_mhd_config_t: 13 doubles + 13 int32 (+4 bytes tail padding)
+    assert C.sizeof(_abi.MhdConfig) == 160
+    assert _abi.MhdConfig.bcz.offset == 152
+    assert C.sizeof(_abi.Particles) == 17 * C.sizeof(C.c_void_p)
+
+
+CONF = """!< Configuration file written for the tests
+!< Initial magnetic field strength
+b0 = 2.0
+!< momentum normalisation
+p0 = 0.1
+pmin = 1.0E-2
+pmax = 1.0d1
+momentum_dependency = 1
+!< turbulence spectral index
+gamma_turb = 1.6666667
+mag_dependency = 0
+kpara0 = 0.01 ; trailing C-style terminator
+kret = 0.03
+dt_min = 1E-8
+dt_min_rel = 1E-7
+dt_max_rel = 1E-2
+npp_global = 96
+nmu_global = 32
+acc_region_flag = 1
+acc_xmin = -1.0
+acc_xmax = -0.5
+acc_ymin = 0.08
+acc_ymax = 1.0
+acc_zmin = 0.0
+acc_zmax = 1.0
+pbcx = 1
+pbcy = 0
+pbcz = 0
+"""
+
+
+def test_read_particle_params_reference_order(tmp_path, engine_lib):
+    f = tmp_path / "conf.dat"
+    f.write_text(CONF)
+    p = read_particle_params(f)
+    assert (p.b0, p.p0, p.pmin, p.pmax) == (2.0, 0.1, 0.01, 10.0)
+    assert p.momentum_dependency == 1 and p.mag_dependency == 0
+    assert p.gamma_turb == 1.6666667 and p.pindex == pytest.approx(3.0 - 1.6666667)
+    assert p.kpara0 == 0.01 and p.kret == 0.03
+    # 'dt_min' line does not match 'dt_min_rel' (substring search is by key)
+    assert p.dt_min_rel == 1e-7 and p.dt_max_rel == 1e-2
+    assert p.acc_region_flag == 1
+    assert tuple(p.acc_region) == (-1.0, -0.5, 0.08, 1.0, 0.0, 1.0)
+    assert (p.pbcx, p.pbcy, p.pbcz) == (1, 0, 0)
+    assert p.npp_global == 96
+
+
+def test_read_particle_params_forward_scan_and_missing(tmp_path, engine_lib):
+    # gamma_turb appears before momentum_dependency: the forward scan from
+    # the momentum_dependency match never sees it and reads -1 (as
+    # read_config.f90:20-44 does); the sample config/conf.dat has no
+    # gamma_turb key at all, which gives the same -1.
+    text = CONF.replace("gamma_turb = 1.6666667\n", "")
+    text = text.replace("pmax = 1.0d1\n", "pmax = 1.0d1\ngamma_turb = 1.5\n")
+    f = tmp_path / "conf.dat"
+    f.write_text(text)
+    p = read_particle_params(f)
+    assert p.gamma_turb == -1.0 and p.pindex == 4.0
+    # A key missing at the end leaves the scan at EOF: everything after it
+    # reads -1 too.
+    f2 = tmp_path / "conf2.dat"
+    f2.write_text(CONF.split("kret")[0])
+    p2 = read_particle_params(f2)
+    assert p2.kpara0 == 0.01 and p2.kret == -1.0 and p2.dt_min_rel == -1.0
+    assert p2.acc_region_flag == -1   # not 1: default acc region kept
+    assert tuple(p2.acc_region) == (0.0, 1.0, 0.0, 1.0, 0.0, 1.0)
+
+
+def test_get_variable_single_key(tmp_path, engine_lib):
+    f = tmp_path / "conf.dat"
+    f.write_text(CONF)
+    v = C.c_double()
+    assert engine_lib.gpat_get_variable(str(f).encode(), b"nmu_global", C.byref(v)) == 0
+    assert v.value == 32.0
+    assert engine_lib.gpat_get_variable(str(f).encode(), b"no_such_key", C.byref(v)) == 0
+    assert v.value == -1.0
+    assert engine_lib.gpat_get_variable(b"/nonexistent/conf.dat", b"b0", C.byref(v)) == \
+        _abi.GPAT_ERR_IO
+
+
+def test_mhd_config_file_roundtrip(tmp_path, engine_lib):
+    cfg = make_mhd_config(512, 64, 1, 0.0, 1.0, 0.0, 0.125, dt_out=0.1)
+    cfg.bcx, cfg.bcy, cfg.bcz = 1, 0, 0
+    path = tmp_path / "mhd_config.dat"
+    fields.write_mhd_config(path, cfg)
+    assert path.stat().st_size == 156
+    got = load_mhd_config(path)
+    for name, _ in _abi.MhdConfig._fields_:
+        assert getattr(got, name) == getattr(cfg, name), name
+
+
+def test_create_rejects_out_of_scope_options(engine_lib):
+    cfg = make_mhd_config(16, 16, 1, 0.0, 1.0, 0.0, 1.0)
+    h = _abi.Handle()
+    for kw, code in ((dict(ndim=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(dpp_wave=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(spherical_coord=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(precision=7), _abi.GPAT_ERR_ARG),
+                     (dict(nptl_max=0), _abi.GPAT_ERR_ARG),
+                     (dict(npp_global=0), _abi.GPAT_ERR_ARG)):
+        p = make_params(**kw)
+        assert engine_lib.gpat_create(C.byref(p), C.byref(cfg), 0, C.byref(h)) == code, kw
+    assert engine_lib.gpat_create(None, None, 0, C.byref(h)) == _abi.GPAT_ERR_ARG
+
+
+def test_frames_have_reference_layout():
+    frame = fields.planar_shock_2d(32, 8, 0.0, 1.0, 0.0, 0.25, r=4.0, w=0.01)
+    assert frame.shape == (1, 12, 36, 8) and frame.dtype == np.float32
+    # node i (C index) sits at x = xmin + (i - 2) dx: upstream/downstream
+    vx = frame[0, 0, :, 0]
+    assert vx[0] == pytest.approx(1.0) and vx[-1] == pytest.approx(0.25, rel=1e-6)
+    assert np.all(frame[..., 7] == np.sqrt(frame[..., 4].astype(np.float64) ** 2).astype(np.float32))
