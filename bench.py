@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Particle-steps/s of the GPAT mover on one GB300.
+
+Workload: 2D turbulent shock, 2048 x 2048 grid over [0,1]^2 (tanh shock at
+x = 0.5, r = 3.5, w = 0.001; B = x + random-phase Kolmogorov dB/B0 = 0.5 from
+Az), kappa_par = 0.01 (p/p0)^(4/3) along the local B, kperp/kpar = 0.05,
+1e7 particles injected on the shock at p0, dt_min = dtf / 1000 so each
+particle takes 1000 pushes per MHD interval.  One bench step is one pass of
+the driver's per-frame hot path: particle_mover over one interval
+(interpolation + kappa + push + boundaries + landing, then removal),
+split_particle and the global f(p).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's FP64 mover
+(oracle/, OpenMP over all host cores) on a bounded sample of the same
+workload.  Under torchrun each rank runs an independent replica (different
+seed); the engine itself is single-GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+for p in (str(REPO / "stochastic-parker_gb300"), str(REPO / "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "particle-steps/s on 1 GB300 (mixed/learned vs plain FP64) at f(p) tail err ≤2%"
+UNIT = "particle-steps/s"
+# Algorithmic bytes of one 2D push: 4 cell corners x 15 FP32 field values
+# gathered; per particle and launch the FP64 state is read and written once.
+GATHER_BYTES_PER_STEP_2D = 4 * 15 * 4
+STATE_BYTES_PER_PARTICLE = 2 * (7 * 8 + 2 + 4 * 4)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
+    ap.add_argument("--scale", type=float, default=1.0, help="particle-count multiplier")
+    ap.add_argument("--grid", type=int, default=2048)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(world, x: float, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch recorded in profiles/<name>.md ('traffic_bytes_per_launch: N')."""
+    p = REPO / "profiles" / f"{name}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(w, seconds: float, threads: int | None = None):
+    """Oracle (FP64, OpenMP) particle-steps/s on a sample of the workload:
+    particles injected on the shock, one MHD interval each."""
+    import oracle
+    from gpat.engine import make_params
+    prm = oracle.params_from(make_params(**w.params))
+    cfg = oracle.config_from(w.mhd_config)
+    full = oracle.full_fields(w.frame, prm.ndim, w.mhd_config)
+    dtf = float(w.tstamps[1] - w.tstamps[0])
+    nthreads = threads or os.cpu_count() or 1
+
+    def run(n):
+        parts = oracle.Particles(n)
+        cnt = oracle.OrcCounters()
+        oracle.inject_at_x(prm, cfg, parts, n, w.inject["xpos"], 1e-7, 1, 1.0, 0.0, cnt)
+        t0 = time.perf_counter()
+        oracle.mover(prm, cfg, full, parts, 0.0, dtf, nthreads=nthreads, counters=cnt)
+        return cnt.steps, time.perf_counter() - t0
+
+    n = 256 * nthreads
+    steps, dt = run(n)
+    rate = steps / max(dt, 1e-9)
+    n2 = max(n, int(n * seconds / max(dt, 1e-6) * 0.9))
+    n2 = min(n2, 4_000_000)
+    steps, dt = run(n2)
+    return steps / dt, nthreads, n2, steps, dt, rate
+
+
+def run_reference(args, world, rank):
+    from gpat import configs
+    if rank != 0:
+        return
+    w = configs.turbulent_shock_2d(scale=args.scale, n=args.grid, precision=1, nframes=4)
+    vals = []
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    for k in range(args.warmup + args.steps):
+        v, cores, n, steps, dt, _ = cpu_sample(w, per_step)
+        if k >= args.warmup:
+            vals.append((v, n, steps, dt))
+    value = statistics.median(v for v, *_ in vals)
+    n, steps, dt = vals[-1][1:]
+    sample = (f"{n} particles of the {w.name} workload injected on the shock, one MHD "
+              f"interval ({steps / n:.0f} pushes each, {steps} particle-steps in {dt:.2f} s) "
+              f"per step")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * vals[-1][3], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": w.name, "particles_per_rank": w.nptl,
+                       "pushes_per_interval": 1000, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    from gpat import configs
+    from gpat.engine import ParticleSet
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    prec = 1 if args.precision == "mixed" else 0
+    total_frames = args.warmup + args.steps + args.e2e_steps + 2
+    w = configs.turbulent_shock_2d(scale=args.scale, n=args.grid, precision=prec, seed=2 + rank,
+                                   nframes=total_frames)
+    eng = configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6))
+    configs.inject(eng, w)
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+    frame = [1]
+    kernel_ms, kernel_steps, kernel_n = [], [], []
+
+    def step():
+        n_before = eng.nptl_current
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=frame[0], num_fine_steps=1)
+        c = eng.counters()
+        kernel_ms.append(c.last_mover_ms)
+        kernel_steps.append(c.last_mover_steps)
+        kernel_n.append(n_before)
+        eng.split_particle(2.72, 2.0, 10)
+        eng.calc_particle_distributions()
+        frame[0] += 1
+
+    for _ in range(args.warmup):
+        step()
+    kernel_ms.clear(); kernel_steps.clear(); kernel_n.clear()
+
+    clocks = ClockSampler(local)
+    steps0 = eng.counters().steps
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    psteps = eng.counters().steps - steps0
+    t_max = max_over_ranks(world, elapsed, dev)
+    total_steps = sum_over_ranks(world, float(psteps), dev)
+    value = total_steps / t_max
+
+    # End to end through the public API with host buffers: the particle set
+    # goes host -> device, the frame's hot path runs, f(p) and the particle
+    # set come back.
+    n_cap = int(w.nptl * 1.6)
+    pinned = {}
+    from gpat import _abi
+    for name, t in _abi.PARTICLE_FIELDS:
+        tt = torch.empty(n_cap, dtype=getattr(torch, {"f8": "float64", "i1": "int8", "i4": "int32",
+                                                        "u4": "uint32"}[t]), pin_memory=True)
+        pinned[name] = tt.numpy()
+    host = ParticleSet(pinned)
+    cur = eng.get_particles(out=host)
+    e2e_steps, e2e_h2d, e2e_d2h = 0, 0, 0
+    bytes_per_ptl = sum(np.dtype(t).itemsize for _, t in _abi.PARTICLE_FIELDS)
+    barrier(world)
+    torch.cuda.synchronize()
+    t_start = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s0 = eng.counters().steps
+        eng.put_particles(cur)
+        e2e_h2d += len(cur) * bytes_per_ptl
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=frame[0], num_fine_steps=1)
+        eng.split_particle(2.72, 2.0, 10)
+        f, counts = eng.calc_particle_distributions()
+        cur = eng.get_particles(out=host)
+        e2e_d2h += len(cur) * bytes_per_ptl + f.nbytes + counts.nbytes
+        e2e_steps += eng.counters().steps - s0
+        frame[0] += 1
+    torch.cuda.synchronize()
+    e2e_elapsed = max_over_ranks(world, time.perf_counter() - t_start, dev)
+    e2e_total = sum_over_ranks(world, float(e2e_steps), dev)
+    e2e_value = e2e_total / e2e_elapsed if e2e_elapsed > 0 else None
+
+    if rank != 0:
+        eng.close()
+        return
+    peaks = measured_peaks()
+    avg_ms = statistics.mean(kernel_ms)
+    avg_steps = statistics.mean(kernel_steps)
+    avg_n = statistics.mean(kernel_n)
+    bytes_launch = avg_steps * GATHER_BYTES_PER_STEP_2D + avg_n * STATE_BYTES_PER_PARTICLE
+    achieved = bytes_launch / (avg_ms / 1e3) / 1e9
+    kname = f"mover_{args.precision}_turbulent_shock_2d"
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": profiled_traffic(kname),
+                "kernel": f"mover_{args.precision}_kernel<2>",
+                "peak_source": peaks["source"],
+                "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
+                "kernel_steps_per_s": avg_steps / (avg_ms / 1e3),
+                "algorithmic_bytes_per_launch": bytes_launch}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+ff" if prec else "f64", "data": "synthetic",
+            "config": {"workload": w.name, "particles_per_rank": w.nptl,
+                       "pushes_per_interval": 1000, "precision": args.precision,
+                       "step": "particle_mover + split_particle + f(p) over one MHD interval",
+                       "l2": "inputs exceed L2 (fields 269 MB packed, particles ~1 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk, "gpu_launches": 8 * args.steps,
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": e2e_h2d // max(1, args.e2e_steps),
+                    "d2h_bytes_per_step": e2e_d2h // max(1, args.e2e_steps)},
+            "roofline": roofline}
+    eng.close()
+    if world == 1 and not args.no_cpu_baseline:
+        v, cores, n, steps, dt, _ = cpu_sample(w, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} particles injected on the shock, one MHD interval "
+                                          f"of FP64 pushes ({steps} particle-steps in {dt:.2f} s)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -312,7 +312,8 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
     if (p.noise != GPAT_NOISE_UNIFORM && p.noise != GPAT_NOISE_GAUSS) return GPAT_ERR_ARG;
     if (p.nptl_max < 1 || p.nptl_max > (int64_t)2000000000) return GPAT_ERR_ARG;
-    if (p.npp_global < 1 || p.npp_global > 4096) return GPAT_ERR_ARG;
+    // The histogram keeps 3 x 8 bytes per bin in shared memory (48 KB max).
+    if (p.npp_global < 1 || p.npp_global > 2048) return GPAT_ERR_ARG;
     if (!(p.p0 > 0.0) || !(p.pmin > 0.0) || !(p.pmax > p.pmin)) return GPAT_ERR_ARG;
     if (cfg->nx < 1 || cfg->ny < 1 || (p.ndim == 3 && cfg->nz < 1)) return GPAT_ERR_ARG;
     if (!(cfg->dx > 0.0) || !(cfg->dy > 0.0) || (p.ndim == 3 && !(cfg->dz > 0.0))) return GPAT_ERR_ARG;

@@ -1,9 +1,10 @@
 """Builds the engine's shared library (CUDA kernels + C ABI) for sm_103a.
 
 The library is compiled in-tree into ``gpat/_lib/libgpat_engine.so`` with
-nvcc, one translation unit per process, then linked.  ``mover_fp64.cu`` is
-compiled with ``-fmad=false`` so the FP64 mover keeps the reference's
-separately rounded operations; every other unit may contract to FMA.
+nvcc, one translation unit per process, then linked.  ``mover_fp64.cu`` and
+``particles.cu`` are compiled with ``-fmad=false`` so the FP64 mover and the
+injection keep the reference's separately rounded operations; the
+split-precision mover contracts freely to FMA.
 """
 from __future__ import annotations
 
@@ -26,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "gpat_engine.cpp": [],
     "fields.cu": [],
-    "particles.cu": [],
+    "particles.cu": ["-fmad=false"],   # injection draws match the oracle bit for bit
     "mover_fp64.cu": ["-fmad=false"],
     "mover_mixed.cu": [],
 }

@@ -240,13 +240,18 @@ class Engine:
         s = ps.ctypes()
         self._check(self.lib.gpat_put_particles(self.h, C.byref(s), len(ps)))
 
-    def get_particles(self) -> ParticleSet:
+    def get_particles(self, out: ParticleSet | None = None) -> ParticleSet:
+        """Copies the particle set to the host.  With ``out`` (capacity >=
+        nptl_current, e.g. pinned buffers) it fills those arrays and returns
+        a view of the first nptl_current entries."""
         n = self.counters().nptl_current
-        ps = ParticleSet.empty(n)
+        ps = ParticleSet.empty(n) if out is None else out
+        if len(ps) < n:
+            raise ValueError(f"output capacity {len(ps)} < {n} particles")
         s = ps.ctypes()
         got = C.c_int64()
-        self._check(self.lib.gpat_get_particles(self.h, C.byref(s), n, C.byref(got)))
-        return ps
+        self._check(self.lib.gpat_get_particles(self.h, C.byref(s), len(ps), C.byref(got)))
+        return ps if out is None else ParticleSet({k: v[:n] for k, v in ps.arrays.items()})
 
     @property
     def nptl_current(self) -> int:

@@ -86,7 +86,7 @@ def random_field_3d(n: int, slope: float, seed: int, kind: str, kmin_mode: int =
     sol = [vh[i] - comp[i] for i in range(3)]
 
     def to_real(parts):
-        return [np.fft.irfftn(p, s=(n, n, n)).astype(np.float64) for p in parts]
+        return [np.fft.irfftn(p, s=(n, n, n), axes=(0, 1, 2)).astype(np.float64) for p in parts]
 
     if kind == "solenoidal":
         return to_real(sol)
