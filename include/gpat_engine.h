@@ -183,6 +183,26 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc,
  * parent order; stops at nptl_max like the reference. */
 int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
                         int nsteps_interval);
+/* No counterpart in the reference.  split_particle for callers that cannot
+ * call cudaMalloc, e.g. a driver whose particle arrays already live in device
+ * memory it manages itself (CUDA Fortran, OpenACC, an application memory
+ * pool) and that may not allocate inside its time loop.  `dev` holds DEVICE
+ * pointers to caller-owned arrays of `capacity` entries, the first n of which
+ * are particles; children are appended after them as gpat_split_particle
+ * does.  No handle, and no device memory is allocated or freed: the scan
+ * scratch and counters are fixed file-scope device arrays (about 1 MiB on
+ * every GPU that loads the library, held until exit), sized for at most
+ * 2^26 = 67,108,864 parents; larger n returns GPAT_ERR_ARG.  The first call
+ * on a device looks up those arrays' device addresses and should come before
+ * any stream capture.  All calls share the arrays, so calls whose work
+ * overlaps on the GPU (other streams, other threads) race; serialise them.
+ * Work is enqueued on `stream` (a cudaStream_t, NULL for the default
+ * stream), which is synchronised before return.  *n_out is the new particle
+ * count, *n_split (may be NULL) the children created; GPAT_ERR_CAPACITY when
+ * capacity stopped the splitting. */
+int gpat_split_particle_noalloc(const gpat_particles_t *dev, int64_t n, int64_t capacity,
+                                double split_ratio, double pmin_split, double p0, double pmax,
+                                void *stream, int64_t *n_out, int64_t *n_split);
 /* Global f(p) of calc_particle_distributions (diagnostics.f90:738-780):
  * fglobal[npp_global] weighted counts (may be NULL) and counts[npp_global]
  * particle numbers (may be NULL).  Bins are exact. */

@@ -30,6 +30,7 @@ SOURCES = {
     "particles.cu": ["-fmad=false"],   # injection draws match the oracle bit for bit
     "mover_fp64.cu": ["-fmad=false"],
     "mover_mixed.cu": [],
+    "noalloc.cu": [],
 }
 
 
