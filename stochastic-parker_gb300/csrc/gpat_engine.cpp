@@ -597,7 +597,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     const unsigned long long steps_before = h->hcnt.steps;
     CK(cudaEventRecord(h->ev0, h->stream));
     if (h->prm.precision == GPAT_PREC_FP64) CK(launch_mover_fp64(a, h->sm_count, h->stream));
-    else CK(launch_mover_mixed(a, h->sm_count, h->stream));
+    else CK(launch_mover_mixed(a, make_mixed_consts(a), h->sm_count, h->stream));
     CK(cudaEventRecord(h->ev1, h->stream));
     // remove_particles (particle_module.f90:5365-5403), order-preserving.
     const int nxt = 1 - h->cur;

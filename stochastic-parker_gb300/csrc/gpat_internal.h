@@ -68,6 +68,22 @@ struct MoverArgs {
     DevCounters *cnt;
 };
 
+// Single-precision constants of the split-precision mover, derived on the
+// host once per call so they live in the kernel's parameter space rather
+// than in registers.  Positions are measured in cells from the box minimum.
+struct MixedConsts {
+    float idx, idy, idz;               // 1 / cell size
+    float dxf, dyf, dzf;               // cell sizes
+    int nx, ny, nz;                    // cells in the exact box
+    float dt_min, dt_max, dtf, inv_dtf;
+    float ip0, pindex, gm2, kpara0, kret;
+    float vdq;                         // single-precision 1 / (3 charge)
+    float d1p0, d2p0sq;                // drift1 p0, drift2 p0^2
+    float pfloor;                      // 0.25 p0
+    float acc[6];                      // acceleration region, box fractions
+    float acc_off[3], acc_scale[3];    // cell -> box fraction: (c + off) * scale
+};
+
 // Launchers (defined in the .cu files).  All enqueue on `s`.
 cudaError_t launch_scatter_raw_fields(const float *raw, int nvar, float *full, size_t ncells,
                                       cudaStream_t s);
@@ -76,7 +92,9 @@ cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg
 cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
                                 cudaStream_t s);
 cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s);
-cudaError_t launch_mover_mixed(const MoverArgs &a, int sm_count, cudaStream_t s);
+cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
+                               cudaStream_t s);
+MixedConsts make_mixed_consts(const MoverArgs &a);
 
 struct InjectArgs {
     DevParticles P;

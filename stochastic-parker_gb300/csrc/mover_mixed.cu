@@ -1,223 +1,169 @@
 // Split-precision particle mover.
 //
-// Field records, interpolation, the kappa tensor, drift and the adaptive-dt
-// candidates run in FP32.  The quantities that accumulate over thousands of
-// steps -- position, momentum and the particle clock -- are carried as
-// compensated float-float pairs (hi + lo, error-free TwoSum / TwoProduct,
-// about 48 significant bits), so no per-step work lands on the FP64 pipe;
-// the FP64 particle record is read once at entry and written once at exit.
+// Field records, interpolation, the kappa tensor, drift, noise amplitudes and
+// the adaptive-dt candidates run in FP32.  The quantities that accumulate over
+// thousands of steps are kept without FP64 arithmetic in the step loop:
+//  - position as an integer cell index plus an FP32 offset inside the cell
+//    (24 bits per cell, renormalised after every increment), which is also
+//    exactly what interpolation and the boundary tests need;
+//  - momentum and the particle clock as Kahan-compensated FP32 sums.
+// The FP64 particle record is read once at entry and written once at exit as
+// "input + accumulated change", so coordinates a call does not touch keep all
+// their bits.
 //
 // Control flow is the reference's particle_mover_one_cycle
 // (particle_module.f90:1481-1833): fine-step targets, adaptive pushes, the
-// undo-and-redo landing on each target, boundary handling with the
-// half-cell-extended box, and the exact-box pass at the end of the interval.
-// Increments are the reference's (2u-1)*sqrt(3) (or Gaussian) variates from
-// one Philox-4x32-10 call per push.
+// undo-and-redo landing on each target, boundaries on the half-cell-extended
+// box, and the exact-box pass at the end of the interval.  Increments are the
+// reference's (2u-1)*sqrt(3) variates (or Gaussian), four from one
+// Philox-4x32-10 call per push.
 #include <cfloat>
+#include <cmath>
 
 #include "device_common.cuh"
 
 namespace gpat {
+
+MixedConsts make_mixed_consts(const MoverArgs &a) {
+    MixedConsts k{};
+    k.idx = (float)(1.0 / a.dx); k.idy = (float)(1.0 / a.dy); k.idz = (float)(1.0 / a.dz);
+    k.dxf = (float)a.dx; k.dyf = (float)a.dy; k.dzf = (float)a.dz;
+    k.nx = a.nxg - 4; k.ny = a.nyg - 4; k.nz = a.ndim == 3 ? a.nzg - 4 : 1;
+    k.dt_min = (float)a.dt_min; k.dt_max = (float)a.dt_max;
+    k.dtf = (float)a.dtf; k.inv_dtf = (float)(1.0 / a.dtf);
+    k.ip0 = (float)(1.0 / a.p0); k.pindex = (float)a.pindex; k.gm2 = (float)(a.gamma_turb - 2.0);
+    k.kpara0 = (float)a.kpara0; k.kret = (float)a.kret;
+    k.vdq = 1.0f / (float)(3 * a.charge);
+    k.d1p0 = (float)(a.drift1 * a.p0);
+    k.d2p0sq = (float)(a.drift2 * (a.p0 * a.p0));
+    k.pfloor = (float)(0.25 * a.p0);
+    for (int j = 0; j < 6; ++j) k.acc[j] = (float)a.acc_region[j];
+    // box fraction = (x - cfg_min) / l = (cell coordinate + (min - cfg_min)/d) * d / l
+    k.acc_off[0] = (float)((a.xmin - a.cfg_xmin) / a.dx);
+    k.acc_off[1] = (float)((a.ymin - a.cfg_ymin) / a.dy);
+    k.acc_off[2] = (float)((a.zmin - a.cfg_zmin) / a.dz);
+    k.acc_scale[0] = (float)(a.dx / a.cfg_lx);
+    k.acc_scale[1] = (float)(a.dy / a.cfg_ly);
+    k.acc_scale[2] = (float)(a.dz / a.cfg_lz);
+    return k;
+}
+
 namespace {
 
-// ---- float-float arithmetic (Dekker / Knuth error-free transformations) --
-struct ff {
-    float h, l;
-};
-
-__device__ __forceinline__ ff two_sum(float a, float b) {
-    const float s = a + b;
-    const float bb = s - a;
-    const float e = (a - (s - bb)) + (b - bb);
-    return {s, e};
-}
-__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b|
-    const float s = a + b;
-    return {s, b - (s - a)};
-}
-__device__ __forceinline__ ff ff_add_f(ff a, float b) {
-    ff s = two_sum(a.h, b);
-    return fast_two_sum(s.h, s.l + a.l);
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-    ff s = two_sum(a.h, b.h);
-    return fast_two_sum(s.h, s.l + (a.l + b.l));
-}
-__device__ __forceinline__ ff ff_from_d(double d) {
-    const float h = (float)d;
-    return {h, (float)(d - (double)h)};
-}
-__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.h + (double)a.l; }
-__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
-__device__ __forceinline__ bool ff_gt(ff a, ff b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
-__device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
-
-// Grid coordinate of a position relative to the box minimum: integer cell
-// and the in-cell fraction in full float precision.
-__device__ __forceinline__ float grid_coord(ff xr, ff id, int &cell) {
-    const float p = xr.h * id.h;
-    const float e = fmaf(xr.h, id.h, -p);               // exact product error
-    const float tail = e + fmaf(xr.h, id.l, xr.l * id.h);
-    const float fl = floorf(p);
-    float r = (p - fl) + tail;                          // p - fl is exact
-    cell = (int)fl;
-    if (r < 0.0f) { r += 1.0f; cell -= 1; }
-    else if (r >= 1.0f) { r -= 1.0f; cell += 1; }
-    return r;
+// Kahan-compensated running sum: the value is s - c.
+__device__ __forceinline__ void kadd(float &s, float &c, float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
 }
 
-struct Consts {
-    ff idx, idy, idz;               // 1/dx, ...
-    ff lo1x, hi1x, lo1y, hi1y, lo1z, hi1z;   // extended box relative to min
-    ff lox, hix, loy, hiy, loz, hiz;         // exact box relative to min
-    ff perx1, pery1, perz1, perx, pery, perz;  // periods of the two boxes
-    float dxf, dyf, dzf;
-    float dt_min, dt_max;
-    float p0, ip0, pindex, gm2, kpara0, kret;
-    float vdq;                      // single-precision 1/(3 charge)
-    float d1p0, d2p0sq;             // drift1 * p0, drift2 * p0^2
-    float pfloor;
-    float accx0, accx1, accy0, accy1, accz0, accz1, ilx, ily, ilz, offx, offy, offz;
-};
+__device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
-__device__ __forceinline__ Consts make_consts(const MoverArgs &a) {
-    Consts c;
-    c.idx = ff_from_d(a.idx); c.idy = ff_from_d(a.idy); c.idz = ff_from_d(a.idz);
-    c.lo1x = ff_from_d(a.xmin1 - a.xmin); c.hi1x = ff_from_d(a.xmax1 - a.xmin);
-    c.lo1y = ff_from_d(a.ymin1 - a.ymin); c.hi1y = ff_from_d(a.ymax1 - a.ymin);
-    c.lo1z = ff_from_d(a.zmin1 - a.zmin); c.hi1z = ff_from_d(a.zmax1 - a.zmin);
-    c.lox = ff_from_d(0.0); c.hix = ff_from_d(a.xmax - a.xmin);
-    c.loy = ff_from_d(0.0); c.hiy = ff_from_d(a.ymax - a.ymin);
-    c.loz = ff_from_d(0.0); c.hiz = ff_from_d(a.zmax - a.zmin);
-    c.perx1 = ff_from_d(a.xmax1 - a.xmin1); c.pery1 = ff_from_d(a.ymax1 - a.ymin1);
-    c.perz1 = ff_from_d(a.zmax1 - a.zmin1);
-    c.perx = ff_from_d(a.xmax - a.xmin); c.pery = ff_from_d(a.ymax - a.ymin);
-    c.perz = ff_from_d(a.zmax - a.zmin);
-    c.dxf = (float)a.dx; c.dyf = (float)a.dy; c.dzf = (float)a.dz;
-    c.dt_min = (float)a.dt_min; c.dt_max = (float)a.dt_max;
-    c.p0 = (float)a.p0; c.ip0 = (float)(1.0 / a.p0); c.pindex = (float)a.pindex;
-    c.gm2 = (float)(a.gamma_turb - 2.0);
-    c.kpara0 = (float)a.kpara0; c.kret = (float)a.kret;
-    c.vdq = 1.0f / (float)(3 * a.charge);
-    c.d1p0 = (float)(a.drift1 * a.p0);
-    c.d2p0sq = (float)(a.drift2 * (a.p0 * a.p0));
-    c.pfloor = (float)(0.25 * a.p0);
-    c.accx0 = (float)a.acc_region[0]; c.accx1 = (float)a.acc_region[1];
-    c.accy0 = (float)a.acc_region[2]; c.accy1 = (float)a.acc_region[3];
-    c.accz0 = (float)a.acc_region[4]; c.accz1 = (float)a.acc_region[5];
-    c.ilx = (float)(1.0 / a.cfg_lx); c.ily = (float)(1.0 / a.cfg_ly); c.ilz = (float)(1.0 / a.cfg_lz);
-    c.offx = (float)(a.xmin - a.cfg_xmin); c.offy = (float)(a.ymin - a.cfg_ymin);
-    c.offz = (float)(a.zmin - a.cfg_zmin);
-    return c;
+// Adds d cells to (c, f), keeping f in [0, 1).
+__device__ __forceinline__ void advance(int &c, float &f, float d) {
+    f += d;
+    const float fl = floorf(f);
+    f -= fl;
+    c += (int)fl;
+    if (f >= 1.0f) { f -= 1.0f; c += 1; }
 }
 
-struct S {
-    ff x, y, z, p, tau;   // position relative to the box minimum, momentum, t - t0
-    float dt;
-    double w;
-    int flag;
-    int32_t nsp, tag_inj, tag_spl;
-    uint32_t ctr;
-};
-
-struct Acc {
-    unsigned long long leak_h, leak_l, negp_h, negp_l, steps;
-};
-
-__device__ __forceinline__ void acc_add(unsigned long long &h, unsigned long long &l, double w) {
-    unsigned long long bh, bl;
-    fixed_split(w, bh, bl);
-    add_u128(h, l, bh, bl);
-}
-
-// One open/periodic boundary test along one axis.
-__device__ __forceinline__ void bc_axis(ff &x, ff lo, ff hi, ff per, int open, int flo, int fhi,
-                                        S &s, Acc &acc) {
-    if (s.flag != 1) return;
-    if (ff_lt(x, lo)) {
-        if (open) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = flo; }
-        else x = ff_add(x, per);
-    } else if (ff_gt(x, hi)) {
-        if (open) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = fhi; }
-        else x = ff_add(x, ff_neg(per));
-    }
-}
-
-template <int NDIM>
-__device__ __forceinline__ void boundary_ext(const MoverArgs &a, const Consts &c, S &s, Acc &acc) {
-    bc_axis(s.x, c.lo1x, c.hi1x, c.perx1, a.pbcx, -1, -2, s, acc);
-    bc_axis(s.y, c.lo1y, c.hi1y, c.pery1, a.pbcy, -3, -4, s, acc);
-    if (NDIM == 3) bc_axis(s.z, c.lo1z, c.hi1z, c.perz1, a.pbcz, -5, -6, s, acc);
-}
-
-template <int NDIM>
-__device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, const Consts &c, S &s, Acc &acc) {
-    if (s.p.h < 0.0f) {
-        s.flag = 0;
-        acc_add(acc.negp_h, acc.negp_l, s.w);
+// Boundary test along one axis in cell units.  ext: the half-cell-extended
+// box (period n + 1 cells); otherwise the exact box (period n).
+__device__ __forceinline__ void bc_axis(int &c, float f, int n, bool ext, int open, int flo,
+                                        int fhi, int &flag, const MoverArgs &a, int64_t i) {
+    if (flag != 1) return;
+    const bool lo = ext ? (c < -1 || (c == -1 && f < 0.5f)) : (c < 0);
+    const bool hi = ext ? (c > n || (c == n && f > 0.5f)) : (c > n || (c == n && f > 0.0f));
+    if (!lo && !hi) return;
+    if (open) {
+        atomic_add_fixed(&a.cnt->leak_hi, &a.cnt->leak_lo, a.P.weight[i]);
+        flag = lo ? flo : fhi;
     } else {
-        boundary_ext<NDIM>(a, c, s, acc);
+        const int per = ext ? n + 1 : n;
+        c += lo ? per : -per;
     }
 }
 
-// FP32 interpolation of the packed record at the particle.
+struct Pos {
+    int cx, cy, cz;
+    float fx, fy, fz;
+};
+
+template <int NDIM>
+__device__ __forceinline__ void boundary(const MoverArgs &a, const MixedConsts &k, Pos &q,
+                                         bool ext, int &flag, int64_t i) {
+    bc_axis(q.cx, q.fx, k.nx, ext, a.pbcx, -1, -2, flag, a, i);
+    bc_axis(q.cy, q.fy, k.ny, ext, a.pbcy, -3, -4, flag, a, i);
+    if (NDIM == 3) bc_axis(q.cz, q.fz, k.nz, ext, a.pbcz, -5, -6, flag, a, i);
+}
+
+template <int NDIM>
+__device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, const MixedConsts &k, Pos &q,
+                                                 float p, int &flag, int64_t i) {
+    if (p < 0.0f) {
+        flag = 0;
+        atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, a.P.weight[i]);
+    } else {
+        boundary<NDIM>(a, k, q, true, flag, i);
+    }
+}
+
+// FP32 bilinear / trilinear interpolation of the packed record.
 template <int NDIM, int NV>
-__device__ __forceinline__ bool interp(const MoverArgs &a, const Consts &c, const S &s, float f[NV]) {
+__device__ __forceinline__ bool interp(const MoverArgs &a, const Pos &q, float rt, float f[NV]) {
     constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
-    int cx, cy, cz = 0;
-    const float rx = grid_coord(s.x, c.idx, cx);
-    const float ry = grid_coord(s.y, c.idy, cy);
-    const float rz = (NDIM == 3) ? grid_coord(s.z, c.idz, cz) : 0.0f;
-    const int ix = cx + 2, iy = cy + 2, iz = (NDIM == 3) ? cz + 2 : 0;
-    if (ix < 0 || ix + 1 >= a.nxg || iy < 0 || iy + 1 >= a.nyg ||
-        (NDIM == 3 && (iz < 0 || iz + 1 >= a.nzg))) {
+    const int ix = q.cx + 2, iy = q.cy + 2, iz = (NDIM == 3) ? q.cz + 2 : 0;
+    if ((unsigned)ix > (unsigned)(a.nxg - 2) || (unsigned)iy > (unsigned)(a.nyg - 2) ||
+        (NDIM == 3 && (unsigned)iz > (unsigned)(a.nzg - 2))) {
         set_status(a.cnt, kStatusIndexGuard);
         return false;
     }
-    const float rx1 = 1.0f - rx, ry1 = 1.0f - ry, rz1 = 1.0f - rz;
 #pragma unroll
     for (int v = 0; v < NV; ++v) f[v] = 0.0f;
-    const float rt = a.time_interp ? (float)((double)s.tau.h / a.dtf) : 0.0f;
+    const size_t row = (size_t)a.nxg;
+    const size_t plane = (size_t)a.nxg * a.nyg;
+    const size_t base = (size_t)ix + row * iy + plane * iz;
 #pragma unroll
-    for (int k = 0; k < (NDIM == 3 ? 2 : 1); ++k)
+    for (int kk = 0; kk < (NDIM == 3 ? 2 : 1); ++kk)
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                float wc = (i ? rx : rx1) * (j ? ry : ry1);
-                if (NDIM == 3) wc *= (k ? rz : rz1);
-                const size_t cell = (size_t)(ix + i) +
-                                    (size_t)a.nxg * ((size_t)(iy + j) + (size_t)a.nyg * (size_t)(iz + k));
+            for (int ii = 0; ii < 2; ++ii) {
+                float wc = (ii ? q.fx : 1.0f - q.fx) * (j ? q.fy : 1.0f - q.fy);
+                if (NDIM == 3) wc *= (kk ? q.fz : 1.0f - q.fz);
+                const size_t cell = base + ii + row * j + plane * kk;
+                float w1 = wc;
+                if (a.time_interp) w1 = wc * (1.0f - rt);
                 const float4 *r4 = reinterpret_cast<const float4 *>(a.rec1 + (size_t)R * cell);
-                float w1 = wc, w2 = 0.0f;
-                if (a.time_interp) { w1 = wc * (1.0f - rt); w2 = wc * rt; }
 #pragma unroll
-                for (int q = 0; q < (NV + 3) / 4; ++q) {
-                    const float4 v4 = __ldg(r4 + q);
-                    const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+                for (int v4 = 0; v4 < (NV + 3) / 4; ++v4) {
+                    const float4 g = __ldg(r4 + v4);
+                    const float gv[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
-                        if (4 * q + e < NV) f[4 * q + e] = fmaf(vv[e], w1, f[4 * q + e]);
+                        if (4 * v4 + e < NV) f[4 * v4 + e] = fmaf(gv[e], w1, f[4 * v4 + e]);
                 }
                 if (a.time_interp) {
+                    const float w2 = wc * rt;
                     const float4 *s4 = reinterpret_cast<const float4 *>(a.rec2 + (size_t)R * cell);
 #pragma unroll
-                    for (int q = 0; q < (NV + 3) / 4; ++q) {
-                        const float4 v4 = __ldg(s4 + q);
-                        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+                    for (int v4 = 0; v4 < (NV + 3) / 4; ++v4) {
+                        const float4 g = __ldg(s4 + v4);
+                        const float gv[4] = {g.x, g.y, g.z, g.w};
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
-                            if (4 * q + e < NV) f[4 * q + e] = fmaf(vv[e], w2, f[4 * q + e]);
+                            if (4 * v4 + e < NV) f[4 * v4 + e] = fmaf(gv[e], w2, f[4 * v4 + e]);
                     }
                 }
             }
     return true;
 }
 
-__device__ __forceinline__ void noise4(const MoverArgs &a, S &s, float r[4]) {
-    const uint4 w = philox4x32_10(make_uint4(s.ctr, 2u, (uint32_t)s.tag_inj, (uint32_t)s.tag_spl),
-                                  a.key0, a.key1);
-    s.ctr += 1u;
+__device__ __forceinline__ void noise4(const MoverArgs &a, uint32_t ctr, uint32_t ti, uint32_t ts,
+                                       float r[4]) {
+    const uint4 w = philox4x32_10(make_uint4(ctr, 2u, ti, ts), a.key0, a.key1);
     if (a.noise == GPAT_NOISE_UNIFORM) {
         // (2u - 1) sqrt(3) with u at the centre of one of 2^24 cells.
         const float sc = 1.7320508f / 8388608.0f;
@@ -229,7 +175,7 @@ __device__ __forceinline__ void noise4(const MoverArgs &a, S &s, float r[4]) {
     } else {
         const float u0 = ((float)(w.x >> 8) + 0.5f) * (1.0f / 16777216.0f);
         const float u2 = ((float)(w.z >> 8) + 0.5f) * (1.0f / 16777216.0f);
-        const float ra = sqrtf(-2.0f * __logf(u0)), rb = sqrtf(-2.0f * __logf(u2));
+        const float ra = fsqrt(-2.0f * __logf(u0)), rb = fsqrt(-2.0f * __logf(u2));
         float sa, ca, sb, cb;
         __sincosf(6.2831853f * (float)(w.y >> 8) * (1.0f / 16777216.0f), &sa, &ca);
         __sincosf(6.2831853f * (float)(w.w >> 8) * (1.0f / 16777216.0f), &sb, &cb);
@@ -237,305 +183,297 @@ __device__ __forceinline__ void noise4(const MoverArgs &a, S &s, float r[4]) {
     }
 }
 
-__device__ __forceinline__ bool in_acc_region(const Consts &c, const S &s, int ndim) {
-    const float xn = (s.x.h + c.offx) * c.ilx;
-    bool in = (xn >= c.accx0) && (xn <= c.accx1);
-    if (ndim > 1) {
-        const float yn = (s.y.h + c.offy) * c.ily;
-        in = in && (yn >= c.accy0) && (yn <= c.accy1);
-    }
-    if (ndim == 3) {
-        const float zn = (s.z.h + c.offz) * c.ilz;
-        in = in && (zn >= c.accz0) && (zn <= c.accz1);
+template <int NDIM>
+__device__ __forceinline__ bool in_acc_region(const MixedConsts &k, const Pos &q) {
+    const float xn = ((float)q.cx + q.fx + k.acc_off[0]) * k.acc_scale[0];
+    const float yn = ((float)q.cy + q.fy + k.acc_off[1]) * k.acc_scale[1];
+    bool in = xn >= k.acc[0] && xn <= k.acc[1] && yn >= k.acc[2] && yn <= k.acc[3];
+    if (NDIM == 3) {
+        const float zn = ((float)q.cz + q.fz + k.acc_off[2]) * k.acc_scale[2];
+        in = in && zn >= k.acc[4] && zn <= k.acc[5];
     }
     return in;
 }
 
-struct KF {
-    float kperp, skpara, skperp, skpp, kpp, b, ib1, ib2, ib3;
-};
-
-__device__ __forceinline__ KF kappa_f(const MoverArgs &a, const Consts &c, float p, float bx,
-                                      float by, float bz) {
-    KF k;
-    const float b2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
-    k.b = sqrtf(b2);
-    k.ib1 = (k.b < FLT_EPSILON) ? 1.0f : __frcp_rn(k.b);
-    k.ib2 = k.ib1 * k.ib1;
-    k.ib3 = k.ib1 * k.ib2;
-    float knorm = 1.0f;
-    if (a.mag_dependency == 1) knorm = exp2f(c.gm2 * __log2f(k.b));
-    if (a.momentum_dependency == 1) knorm *= exp2f(c.pindex * __log2f(p * c.ip0));
-    const float kpara = c.kpara0 * knorm;
-    k.kperp = kpara * c.kret;
-    k.skpara = sqrtf(2.0f * kpara);
-    k.skperp = sqrtf(2.0f * k.kperp);
-    k.kpp = kpara - k.kperp;
-    k.skpp = sqrtf(2.0f * k.kpp);
-    return k;
-}
-
-__device__ __forceinline__ float vdrift_prefactor(const Consts &c, float p) {
-    const float ip = __frcp_rn(p);
-    const float t1 = c.d1p0 * ip;
-    const float t2 = c.d2p0sq * ip * ip;
-    return c.vdq * rsqrtf(fmaf(t1, t1, t2 * t2));
-}
-
-// Adaptive step: the reference's min() of diffusion / drift / momentum
-// limits, dt_min when any rate is exactly zero, clamped to [dt_min, dt_max].
-__device__ __forceinline__ float pick_dt(const Consts &c, float skpara, float skperp, float dx_dt,
-                                         float dy_dt, float dz_dt, float dp_dt, float p, int ndim) {
-    if (!(dx_dt != 0.0f && dy_dt != 0.0f && dp_dt != 0.0f)) return c.dt_min;
-    const float sk = (skperp > 0.0f) ? skperp : skpara;
-    const float isk = __frcp_rn(skpara);
-    float q = 0.5f * c.dxf * isk, m = q * q;
-    q = 0.5f * c.dyf * isk; m = fminf(m, q * q);
-    if (ndim == 3) { q = 0.5f * c.dzf * isk; m = fminf(m, q * q); }
-    q = __fdividef(sk, dx_dt); m = fminf(m, q * q);
-    q = __fdividef(sk, dy_dt); m = fminf(m, q * q);
-    if (ndim == 3) { q = __fdividef(sk, dz_dt); m = fminf(m, q * q); }
-    m = fminf(m, __fdividef(0.1f * p, fabsf(dp_dt)));
-    return fminf(fmaxf(m, c.dt_min), c.dt_max);
-}
-
-__device__ __forceinline__ void update_p(const MoverArgs &a, const Consts &c, S &s, float dp,
-                                         int ndim, float &dP_o) {
-    if (a.acc_region_flag == 1 && !in_acc_region(c, s, ndim)) dp = 0.0f;
-    ff np = ff_add_f(s.p, dp);
-    if (np.h < c.pfloor) {
-        dp = c.pfloor - s.p.h - s.p.l;
-        np = ff{c.pfloor, 0.0f};
-    }
-    s.p = np;
-    dP_o = dp;
-}
-
+// One push: interpolation, kappa, drift, dt, noise.  Outputs increments in
+// cell units (dX, dY, dZ), the momentum increment dp (before the floor) and,
+// unless fixed, the adaptive dt.
 template <int NDIM>
-__device__ __forceinline__ void push(const MoverArgs &a, const Consts &c, S &s, const float *f,
-                                     bool fixed_dt, float &dX, float &dY, float &dZ, float &dP) {
-    const float p = s.p.h;
+__device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, const Pos &q,
+                                     float p, float rt, bool fixed, float &dt, uint32_t ctr,
+                                     uint32_t ti, uint32_t ts, float &dX, float &dY, float &dZ,
+                                     float &dp) {
+    constexpr int NV = (NDIM == 2) ? 15 : 21;
+    float f[NV];
+    if (!interp<NDIM, NV>(a, q, rt, f)) return false;
+    // slots: 2D vx vy bx by bz dvx/dx dvy/dy dbx/dx dbx/dy dby/dx dby/dy dbz/dx dbz/dy db/dx db/dy
+    //        3D vx vy vz bx by bz dvx/dx dvy/dy dvz/dz dbi/dj (9) db/dx db/dy db/dz
+    constexpr int OB = (NDIM == 2) ? 2 : 3;
+    const float bx = f[OB], by = f[OB + 1], bz = f[OB + 2];
+    const float b2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
+    const bool bzero = b2 < FLT_EPSILON * FLT_EPSILON;
+    const float ib = bzero ? 0.0f : rsqrtf(b2);   // 1/B, or 0 for B = 0 (push)
+    const float b = b2 * ib;
+    const float ib1 = bzero ? 1.0f : ib;           // kappa's guard uses 1
+    const float ib2 = ib1 * ib1, ib3 = ib1 * ib2;
+    float knorm = 1.0f;
+    if (a.mag_dependency == 1) knorm = exp2f(k.gm2 * __log2f(b));
+    if (a.momentum_dependency == 1) knorm *= exp2f(k.pindex * __log2f(p * k.ip0));
+    const float kpara = k.kpara0 * knorm;
+    const float kperp = kpara * k.kret;
+    const float kpp = kpara - kperp;
+    const float skpara = fsqrt(2.0f * kpara), skperp = fsqrt(2.0f * kperp), skpp = fsqrt(2.0f * kpp);
+    const float ip = __fdividef(1.0f, p);
+    const float t1 = k.d1p0 * ip, t2 = k.d2p0sq * ip * ip;
+    const float vdp = k.vdq * rsqrtf(fmaf(t1, t1, t2 * t2));
+    const float jb2 = ib * ib, jb3 = ib * jb2;
+    float dx_dt, dy_dt, dz_dt = 0.0f, divv;
     if (NDIM == 2) {
-        const float bx = f[2], by = f[3], bz = f[4];
-        const KF k = kappa_f(a, c, p, bx, by, bz);
         const float dbx_dx = f[7], dbx_dy = f[8], dby_dx = f[9], dby_dy = f[10];
         const float dbz_dx = f[11], dbz_dy = f[12], db_dx = f[13], db_dy = f[14];
         float dkdx = 0.0f, dkdy = 0.0f;
-        if (a.mag_dependency == 1) { dkdx = db_dx * k.ib1 * c.gm2; dkdy = db_dy * k.ib1 * c.gm2; }
-        const float b = k.b, kpp = k.kpp, ib2 = k.ib2, ib3 = k.ib3;
-        const float dkxx_dx = k.kperp * dkdx + kpp * dkdx * bx * bx * ib2 +
-                              2.0f * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
-        const float dkyy_dy = k.kperp * dkdy + kpp * dkdy * by * by * ib2 +
-                              2.0f * kpp * by * (dby_dy * b - by * db_dy) * ib3;
-        const float dkxy_dx = kpp * dkdx * bx * by * ib2 +
-                              kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0f * bx * by * db_dx * ib3);
-        const float dkxy_dy = kpp * dkdy * bx * by * ib2 +
-                              kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0f * bx * by * db_dy * ib3);
-        const float ib = (b < FLT_EPSILON) ? 0.0f : k.ib1;
-        const float jb2 = ib * ib, jb3 = ib * jb2;
-        const float vdp = vdrift_prefactor(c, p);
+        if (a.mag_dependency == 1) { dkdx = db_dx * ib1 * k.gm2; dkdy = db_dy * ib1 * k.gm2; }
+        const float ax = kpp * ib2, a3 = 2.0f * kpp * ib3;
+        const float dkxx_dx = kperp * dkdx + ax * dkdx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
+        const float dkyy_dy = kperp * dkdy + ax * dkdy * by * by + a3 * by * (dby_dy * b - by * db_dy);
+        const float dkxy_dx = ax * (dkdx * bx * by + dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
+        const float dkxy_dy = ax * (dkdy * bx * by + dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
         const float vdx = vdp * (dbz_dy * jb2 - 2.0f * bz * db_dy * jb3);
         const float vdy = vdp * (2.0f * bz * db_dx * jb3 - dbz_dx * jb2);
-        float vdz = 0.0f;
         if (a.check_drift_2d)
-            vdz = vdp * ((dby_dx - dbx_dy) * jb2 - 2.0f * (by * db_dx - bx * db_dy) * jb3);
-        const float dx_dt = f[0] + vdx + dkxx_dx + dkxy_dy;
-        const float dy_dt = f[1] + vdy + dkxy_dx + dkyy_dy;
-        const float divv = f[5] + f[6];
-        const float dp_dt = -p * divv * (1.0f / 3.0f);
-        if (!fixed_dt) s.dt = pick_dt(c, k.skpara, k.skperp, dx_dt, dy_dt, 0.0f, dp_dt, p, 2);
-        const float dt = s.dt, sdt = sqrtf(dt);
-        float r[4];
-        noise4(a, s, r);
-        const float a3 = r[2] * k.skpp * sdt * ib;
-        dX = fmaf(dx_dt, dt, fmaf(r[0] * k.skperp, sdt, a3 * bx));
-        dY = fmaf(dy_dt, dt, fmaf(r[1] * k.skperp, sdt, a3 * by));
-        dZ = vdz * dt;
-        s.x = ff_add_f(s.x, dX);
-        s.y = ff_add_f(s.y, dY);
-        s.z = ff_add_f(s.z, dZ);
-        s.tau = ff_add_f(s.tau, dt);
-        update_p(a, c, s, dp_dt * dt, 2, dP);
+            dz_dt = vdp * ((dby_dx - dbx_dy) * jb2 - 2.0f * (by * db_dx - bx * db_dy) * jb3);
+        dx_dt = f[0] + vdx + dkxx_dx + dkxy_dy;
+        dy_dt = f[1] + vdy + dkxy_dx + dkyy_dy;
+        divv = f[5] + f[6];
     } else {
-        const float bx = f[3], by = f[4], bz = f[5];
-        const KF k = kappa_f(a, c, p, bx, by, bz);
         const float dbx_dx = f[9], dbx_dy = f[10], dbx_dz = f[11];
         const float dby_dx = f[12], dby_dy = f[13], dby_dz = f[14];
         const float dbz_dx = f[15], dbz_dy = f[16], dbz_dz = f[17];
         const float db_dx = f[18], db_dy = f[19], db_dz = f[20];
         float dkdx = 0.0f, dkdy = 0.0f, dkdz = 0.0f;
-        if (a.mag_dependency == 1) { dkdx = db_dx * c.gm2; dkdy = db_dy * c.gm2; dkdz = db_dz * c.gm2; }
-        const float b = k.b, kpp = k.kpp, kperp = k.kperp, ib2 = k.ib2, ib3 = k.ib3;
-        const float dkxx_dx = kperp * dkdx + kpp * dkdx * bx * bx * ib2 +
-                              2.0f * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
-        const float dkyy_dy = kperp * dkdy + kpp * dkdy * by * by * ib2 +
-                              2.0f * kpp * by * (dby_dy * b - by * db_dy) * ib3;
-        const float dkzz_dz = kperp * dkdz + kpp * dkdz * bz * bz * ib2 +
-                              2.0f * kpp * bz * (dbz_dz * b - bz * db_dz) * ib3;
-        const float dkxy_dx = kpp * dkdx * bx * by * ib2 +
-                              kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0f * bx * by * db_dx * ib3);
-        const float dkxy_dy = kpp * dkdy * bx * by * ib2 +
-                              kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0f * bx * by * db_dy * ib3);
-        const float dkxz_dx = kpp * dkdx * bx * bz * ib2 +
-                              kpp * ((dbx_dx * bz + bx * dbz_dx) * ib2 - 2.0f * bx * bz * db_dx * ib3);
-        const float dkxz_dz = kpp * dkdz * bx * bz * ib2 +
-                              kpp * ((dbx_dz * bz + bx * dbz_dz) * ib2 - 2.0f * bx * bz * db_dz * ib3);
-        const float dkyz_dy = kpp * dkdy * by * bz * ib2 +
-                              kpp * ((dby_dy * bz + by * dbz_dy) * ib2 - 2.0f * by * bz * db_dy * ib3);
-        const float dkyz_dz = kpp * dkdz * by * bz * ib2 +
-                              kpp * ((dby_dz * bz + by * dbz_dz) * ib2 - 2.0f * by * bz * db_dz * ib3);
-        const float ib = (b < FLT_EPSILON) ? 0.0f : k.ib1;
-        const float bxn = bx * ib, byn = by * ib, bzn = bz * ib;
-        const float bxyn = sqrtf(fmaf(bxn, bxn, byn * byn));
-        const float ibxyn = (bxyn < FLT_EPSILON) ? 0.0f : __frcp_rn(bxyn);
-        const float jb2 = ib * ib, jb3 = ib * jb2;
-        const float vdp = vdrift_prefactor(c, p);
+        if (a.mag_dependency == 1) { dkdx = db_dx * k.gm2; dkdy = db_dy * k.gm2; dkdz = db_dz * k.gm2; }
+        const float ax = kpp * ib2, a3 = 2.0f * kpp * ib3;
+        const float dkxx_dx = kperp * dkdx + ax * dkdx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
+        const float dkyy_dy = kperp * dkdy + ax * dkdy * by * by + a3 * by * (dby_dy * b - by * db_dy);
+        const float dkzz_dz = kperp * dkdz + ax * dkdz * bz * bz + a3 * bz * (dbz_dz * b - bz * db_dz);
+        const float dkxy_dx = ax * (dkdx * bx * by + dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
+        const float dkxy_dy = ax * (dkdy * bx * by + dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
+        const float dkxz_dx = ax * (dkdx * bx * bz + dbx_dx * bz + bx * dbz_dx) - a3 * bx * bz * db_dx;
+        const float dkxz_dz = ax * (dkdz * bx * bz + dbx_dz * bz + bx * dbz_dz) - a3 * bx * bz * db_dz;
+        const float dkyz_dy = ax * (dkdy * by * bz + dby_dy * bz + by * dbz_dy) - a3 * by * bz * db_dy;
+        const float dkyz_dz = ax * (dkdz * by * bz + dby_dz * bz + by * dbz_dz) - a3 * by * bz * db_dz;
         const float vdx = vdp * ((dbz_dy - dby_dz) * jb2 - 2.0f * (bz * db_dy - by * db_dz) * jb3);
         const float vdy = vdp * ((dbx_dz - dbz_dx) * jb2 - 2.0f * (bx * db_dz - bz * db_dx) * jb3);
         const float vdz = vdp * ((dby_dx - dbx_dy) * jb2 - 2.0f * (by * db_dx - bx * db_dy) * jb3);
-        const float dx_dt = f[0] + vdx + dkxx_dx + dkxy_dy + dkxz_dz;
-        const float dy_dt = f[1] + vdy + dkxy_dx + dkyy_dy + dkyz_dz;
-        const float dz_dt = f[2] + vdz + dkxz_dx + dkyz_dy + dkzz_dz;
-        const float divv = f[6] + f[7] + f[8];
-        const float dp_dt = -p * divv * (1.0f / 3.0f);
-        if (!fixed_dt) s.dt = pick_dt(c, k.skpara, k.skperp, dx_dt, dy_dt, dz_dt, dp_dt, p, 3);
-        const float dt = s.dt, sdt = sqrtf(dt);
-        float r[4];
-        noise4(a, s, r);
-        const float sp1 = k.skpara * r[0];
-        const float sq = k.skperp * ibxyn;
-        dX = fmaf(dx_dt, dt, (bxn * sp1 - bxn * bzn * sq * r[1] - byn * sq * r[2]) * sdt);
-        dY = fmaf(dy_dt, dt, (byn * sp1 - byn * bzn * sq * r[1] + bxn * sq * r[2]) * sdt);
-        dZ = fmaf(dz_dt, dt, (bzn * sp1 + bxyn * k.skperp * r[1]) * sdt);
-        s.x = ff_add_f(s.x, dX);
-        s.y = ff_add_f(s.y, dY);
-        s.z = ff_add_f(s.z, dZ);
-        s.tau = ff_add_f(s.tau, dt);
-        update_p(a, c, s, dp_dt * dt, 3, dP);
+        dx_dt = f[0] + vdx + dkxx_dx + dkxy_dy + dkxz_dz;
+        dy_dt = f[1] + vdy + dkxy_dx + dkyy_dy + dkyz_dz;
+        dz_dt = f[2] + vdz + dkxz_dx + dkyz_dy + dkzz_dz;
+        divv = f[6] + f[7] + f[8];
     }
-}
-
-template <int NDIM>
-__device__ __forceinline__ bool do_push(const MoverArgs &a, const Consts &c, S &s, bool fixed_dt,
-                                        float &dX, float &dY, float &dZ, float &dP) {
-    constexpr int NV = (NDIM == 2) ? 15 : 21;
-    float f[NV];
-    if (!interp<NDIM, NV>(a, c, s, f)) return false;
-    push<NDIM>(a, c, s, f, fixed_dt, dX, dY, dZ, dP);
-    if (!isfinite(s.x.h) || !isfinite(s.y.h) || !isfinite(s.z.h) || !isfinite(s.p.h) ||
-        !isfinite(s.tau.h)) {
-        set_status(a.cnt, kStatusNonFinite);
-        return false;
+    const float dp_dt = -p * divv * (1.0f / 3.0f);
+    if (!fixed) {
+        // The reference's min() of diffusion / drift / momentum limits; dt_min
+        // when a rate (dx, dy, dp) is exactly zero; clamp to [dt_min, dt_max].
+        if (dx_dt != 0.0f && dy_dt != 0.0f && dp_dt != 0.0f) {
+            const float sk = (skperp > 0.0f) ? skperp : skpara;
+            const float isk = __fdividef(1.0f, skpara);
+            float m = 0.5f * k.dxf * isk;
+            m = fminf(m, 0.5f * k.dyf * isk);
+            if (NDIM == 3) m = fminf(m, 0.5f * k.dzf * isk);
+            m = fminf(m, fabsf(__fdividef(sk, dx_dt)));
+            m = fminf(m, fabsf(__fdividef(sk, dy_dt)));
+            if (NDIM == 3) m = fminf(m, fabsf(__fdividef(sk, dz_dt)));
+            dt = fminf(m * m, __fdividef(0.1f * p, fabsf(dp_dt)));
+        } else {
+            dt = k.dt_min;
+        }
+        dt = fminf(fmaxf(dt, k.dt_min), k.dt_max);
     }
+    const float sdt = fsqrt(dt);
+    float r[4];
+    noise4(a, ctr, ti, ts, r);
+    if (NDIM == 2) {
+        const float a3n = r[2] * skpp * sdt * ib;
+        dX = fmaf(dx_dt, dt, fmaf(r[0] * skperp, sdt, a3n * bx)) * k.idx;
+        dY = fmaf(dy_dt, dt, fmaf(r[1] * skperp, sdt, a3n * by)) * k.idy;
+        dZ = dz_dt * dt;   // physical units; only non-zero with check_drift_2d
+    } else {
+        const float bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+        const float bxy2 = fmaf(bxn, bxn, byn * byn);
+        const bool bxy0 = bxy2 < FLT_EPSILON * FLT_EPSILON;
+        const float ibxyn = bxy0 ? 0.0f : rsqrtf(bxy2);
+        const float bxyn = bxy2 * ibxyn;
+        const float sp1 = skpara * r[0] * sdt;
+        const float sq = skperp * ibxyn * sdt;
+        dX = fmaf(dx_dt, dt, bxn * sp1 - bxn * bzn * sq * r[1] - byn * sq * r[2]) * k.idx;
+        dY = fmaf(dy_dt, dt, byn * sp1 - byn * bzn * sq * r[1] + bxn * sq * r[2]) * k.idy;
+        dZ = fmaf(dz_dt, dt, bzn * sp1 + bxyn * skperp * r[1] * sdt) * k.idz;
+    }
+    dp = dp_dt * dt;
     return true;
 }
 
+// Resident 128-thread blocks per SM the register allocation targets (2D: 6
+// blocks = 80 registers, 3D: 5 blocks = 96 registers, measured best on GB300).
+#ifndef GPAT_MIXED_MINB_2D
+#define GPAT_MIXED_MINB_2D 6
+#endif
+#ifndef GPAT_MIXED_MINB_3D
+#define GPAT_MIXED_MINB_3D 5
+#endif
+
 template <int NDIM>
-__global__ void __launch_bounds__(128) mover_mixed_kernel(const MoverArgs a) {
-    Acc acc = {0, 0, 0, 0, 0};
-    const Consts c = make_consts(a);
+__global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIXED_MINB_3D)
+    mover_mixed_kernel(const MoverArgs a, const MixedConsts k) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t pushes = 0;
     if (i < a.n) {
-        S s;
-        s.x = ff_from_d(a.P.x[i] - a.xmin);
-        s.y = ff_from_d(a.P.y[i] - a.ymin);
-        s.z = ff_from_d(a.P.z[i] - a.zmin);
-        s.p = ff_from_d(a.P.p[i]);
-        s.tau = ff_from_d(a.P.t[i] - a.t0);
-        s.dt = (float)a.P.dt[i];
-        s.w = a.P.weight[i];
-        s.flag = a.P.count_flag[i];
-        s.nsp = a.P.nsteps_pushed[i];
-        s.tag_inj = a.P.tag_injected[i];
-        s.tag_spl = a.P.tag_splitted[i];
-        s.ctr = a.P.rng_ctr[i];
-        const double tau0 = a.P.t[i] - a.t0;
-        const double stepd = ceil(tau0 / a.dt_fine);
+        const double x_in = a.P.x[i], y_in = a.P.y[i], z_in = a.P.z[i];
+        const double p_in = a.P.p[i], t_in = a.P.t[i];
+        Pos q;
+        {
+            const double px = (x_in - a.xmin) / a.dx, py = (y_in - a.ymin) / a.dy;
+            const double fxd = floor(px), fyd = floor(py);
+            q.cx = (int)fxd; q.fx = (float)(px - fxd);
+            q.cy = (int)fyd; q.fy = (float)(py - fyd);
+            if (q.fx >= 1.0f) { q.fx = 0.0f; q.cx += 1; }
+            if (q.fy >= 1.0f) { q.fy = 0.0f; q.cy += 1; }
+            if (NDIM == 3) {
+                const double pz = (z_in - a.zmin) / a.dz, fzd = floor(pz);
+                q.cz = (int)fzd; q.fz = (float)(pz - fzd);
+                if (q.fz >= 1.0f) { q.fz = 0.0f; q.cz += 1; }
+            } else {
+                q.cz = 0; q.fz = 0.0f;
+            }
+        }
+        const Pos q_in = q;
+        float z2 = 0.0f;                       // 2D out-of-plane drift, physical units
+        const float p_f0 = (float)p_in;
+        float p = p_f0, pc = 0.0f;
+        const double tau_in = t_in - a.t0;
+        const float tau_f0 = (float)tau_in;
+        float tau = tau_f0, tc = 0.0f;
+        float dt = (float)a.P.dt[i];
+        int flag = a.P.count_flag[i];
+        int nsp = a.P.nsteps_pushed[i];
+        uint32_t ctr = a.P.rng_ctr[i];
+        const uint32_t ti = (uint32_t)a.P.tag_injected[i], ts = (uint32_t)a.P.tag_splitted[i];
+
+        const double stepd = ceil(tau_in / a.dt_fine);
         double target_d = (stepd <= 0.0) ? a.dt_fine : stepd * a.dt_fine;
         if (target_d > a.dtf) target_d = a.dtf;
-        float dX = 0.0f, dY = 0.0f, dZ = 0.0f, dP = 0.0f;
-        if (s.p.h < 0.0f && s.flag == 1) {
-            s.flag = 0;
-            acc_add(acc.negp_h, acc.negp_l, s.w);
+        double landed_at = -1.0;
+        float uX = 0.0f, uY = 0.0f, uZ = 0.0f, uP = 0.0f;
+
+        if (p < 0.0f && flag == 1) {
+            flag = 0;
+            atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, a.P.weight[i]);
         } else {
-            boundary_ext<NDIM>(a, c, s, acc);
+            boundary<NDIM>(a, k, q, true, flag, i);
         }
-        uint32_t pushes = 0;
-        bool alive = (s.flag == 1);
+        bool alive = (flag == 1);
         while (alive && target_d < a.limit) {
-            if (s.flag != 1) break;
-            const ff target = ff_from_d(target_d);
-            while (ff_lt(s.tau, target) && s.flag == 1) {
-                negp_or_boundary<NDIM>(a, c, s, acc);
-                if (s.flag != 1) break;
+            const float target = (float)target_d;
+            while (tau - tc < target && flag == 1) {
+                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, i);
+                if (flag != 1) break;
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
-                if (!do_push<NDIM>(a, c, s, false, dX, dY, dZ, dP)) { s.flag = 0; alive = false; break; }
+                const float pe = p - pc;
+                float dp;
+                if (!push<NDIM>(a, k, q, pe, tau * k.inv_dtf, false, dt, ctr, ti, ts, uX, uY, uZ, dp)) {
+                    flag = 0; alive = false; break;
+                }
+                ++ctr;
                 ++pushes;
-                s.nsp = (s.nsp + 1) % a.nsteps_interval;
+                advance(q.cx, q.fx, uX);
+                advance(q.cy, q.fy, uY);
+                if (NDIM == 3) advance(q.cz, q.fz, uZ); else z2 += uZ;
+                kadd(tau, tc, dt);
+                if (a.acc_region_flag == 1 && !in_acc_region<NDIM>(k, q)) dp = 0.0f;
+                if (pe + dp < k.pfloor) { dp = k.pfloor - pe; p = k.pfloor; pc = 0.0f; }
+                else kadd(p, pc, dp);
+                uP = dp;
+                landed_at = -1.0;
+                nsp = (nsp + 1) % a.nsteps_interval;
+                if (!(fabsf(tau) < 1e30f) || !(fabsf(p) < 1e30f) || !(q.fx <= 1.0f) ||
+                    !(q.fy <= 1.0f) || !(q.fz <= 1.0f)) {
+                    set_status(a.cnt, kStatusNonFinite);
+                    flag = 0; alive = false; break;
+                }
             }
             if (!alive) break;
-            if (ff_gt(s.tau, target) && s.flag == 1) {
-                // Undo the overshooting push and redo it with dt = target - t.
-                s.x = ff_add_f(s.x, -dX);
-                s.y = ff_add_f(s.y, -dY);
-                s.z = ff_add_f(s.z, -dZ);
-                s.p = ff_add_f(s.p, -dP);
-                s.tau = ff_add_f(s.tau, -s.dt);
-                const float dt_old = s.dt;
-                const ff rem = ff_add(target, ff_neg(s.tau));
-                s.dt = rem.h + rem.l;
-                if (s.dt > 0.0f) {
-                    s.nsp = s.nsp - 1;
-                    if (!do_push<NDIM>(a, c, s, true, dX, dY, dZ, dP)) { s.flag = 0; alive = false; break; }
+            if (tau - tc > target && flag == 1) {
+                // Undo the overshooting push, redo it with dt = target - t.
+                advance(q.cx, q.fx, -uX);
+                advance(q.cy, q.fy, -uY);
+                if (NDIM == 3) advance(q.cz, q.fz, -uZ); else z2 -= uZ;
+                kadd(p, pc, -uP);
+                kadd(tau, tc, -dt);
+                const float dt_old = dt;
+                float dtr = target - (tau - tc);
+                if (dtr > 0.0f) {
+                    nsp = nsp - 1;
+                    const float pe = p - pc;
+                    float dp;
+                    if (!push<NDIM>(a, k, q, pe, tau * k.inv_dtf, true, dtr, ctr, ti, ts, uX, uY,
+                                    uZ, dp)) {
+                        flag = 0; alive = false; break;
+                    }
+                    ++ctr;
                     ++pushes;
-                    s.nsp = (s.nsp + 1) % a.nsteps_interval;
-                    s.tau = target;   // the redo lands on the target by construction
+                    advance(q.cx, q.fx, uX);
+                    advance(q.cy, q.fy, uY);
+                    if (NDIM == 3) advance(q.cz, q.fz, uZ); else z2 += uZ;
+                    if (a.acc_region_flag == 1 && !in_acc_region<NDIM>(k, q)) dp = 0.0f;
+                    if (pe + dp < k.pfloor) { dp = k.pfloor - pe; p = k.pfloor; pc = 0.0f; }
+                    else kadd(p, pc, dp);
+                    uP = dp;
+                    tau = target; tc = 0.0f;
+                    landed_at = target_d;
+                    nsp = (nsp + 1) % a.nsteps_interval;
                 }
-                s.dt = dt_old;
-                negp_or_boundary<NDIM>(a, c, s, acc);
+                dt = dt_old;
+                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, i);
+            } else if (flag == 1 && tau - tc == target) {
+                landed_at = target_d;   // reached the target without overshoot
             }
             target_d = target_d + a.dt_fine;
         }
-        if (s.flag == 1) {
-            bc_axis(s.x, c.lox, c.hix, c.perx, a.pbcx, -1, -2, s, acc);
-            bc_axis(s.y, c.loy, c.hiy, c.pery, a.pbcy, -3, -4, s, acc);
-            if (NDIM == 3) bc_axis(s.z, c.loz, c.hiz, c.perz, a.pbcz, -5, -6, s, acc);
+        if (flag == 1) boundary<NDIM>(a, k, q, false, flag, i);
+        // Write back input + change, computed in FP64.
+        const double dcx = (double)(q.cx - q_in.cx) + ((double)q.fx - (double)q_in.fx);
+        const double dcy = (double)(q.cy - q_in.cy) + ((double)q.fy - (double)q_in.fy);
+        a.P.x[i] = x_in + dcx * a.dx;
+        a.P.y[i] = y_in + dcy * a.dy;
+        if (NDIM == 3) {
+            const double dcz = (double)(q.cz - q_in.cz) + ((double)q.fz - (double)q_in.fz);
+            a.P.z[i] = z_in + dcz * a.dz;
+        } else if (z2 != 0.0f) {
+            a.P.z[i] = z_in + (double)z2;
         }
-        acc.steps = pushes;
-        // Write back input + accumulated change, so untouched coordinates
-        // keep every bit of their FP64 value (a float pair holds 48 bits).
-        const double x0 = a.P.x[i], y0 = a.P.y[i], z0 = a.P.z[i], p0 = a.P.p[i], t0 = a.P.t[i];
-        a.P.x[i] = x0 + ff_to_d(ff_add(s.x, ff_neg(ff_from_d(x0 - a.xmin))));
-        a.P.y[i] = y0 + ff_to_d(ff_add(s.y, ff_neg(ff_from_d(y0 - a.ymin))));
-        a.P.z[i] = z0 + ff_to_d(ff_add(s.z, ff_neg(ff_from_d(z0 - a.zmin))));
-        a.P.p[i] = p0 + ff_to_d(ff_add(s.p, ff_neg(ff_from_d(p0))));
-        a.P.t[i] = t0 + ff_to_d(ff_add(s.tau, ff_neg(ff_from_d(t0 - a.t0))));
-        a.P.dt[i] = (double)s.dt;
-        a.P.count_flag[i] = (int8_t)s.flag;
-        a.P.nsteps_pushed[i] = s.nsp;
+        a.P.p[i] = p_in + (((double)p - (double)pc) - (double)p_f0);
+        a.P.t[i] = landed_at >= 0.0 ? a.t0 + landed_at
+                                    : t_in + (((double)tau - (double)tc) - (double)tau_f0);
+        a.P.dt[i] = (double)dt;
+        a.P.count_flag[i] = (int8_t)flag;
+        a.P.nsteps_pushed[i] = nsp;
         a.P.nsteps_tracked[i] = 1;
-        a.P.rng_ctr[i] = s.ctr;
+        a.P.rng_ctr[i] = ctr;
     }
-    const unsigned long long steps = warp_sum_u64(acc.steps);
-    unsigned long long lh = acc.leak_h, ll = acc.leak_l, nh = acc.negp_h, nl = acc.negp_l;
-    warp_sum_u128(lh, ll);
-    warp_sum_u128(nh, nl);
-    if ((threadIdx.x & 31) == 0) {
-        if (steps) atomicAdd(&a.cnt->steps, steps);
-        if (lh | ll) atomic_add_u128(&a.cnt->leak_hi, &a.cnt->leak_lo, lh, ll);
-        if (nh | nl) atomic_add_u128(&a.cnt->negp_hi, &a.cnt->negp_lo, nh, nl);
-    }
+    const unsigned long long steps = warp_sum_u64(pushes);
+    if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&a.cnt->steps, steps);
 }
 
 }  // namespace
 
-cudaError_t launch_mover_mixed(const MoverArgs &a, int sm_count, cudaStream_t s) {
+cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
+                               cudaStream_t s) {
     (void)sm_count;
     if (a.n <= 0) return cudaSuccess;
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
-    if (a.ndim == 2) mover_mixed_kernel<2><<<(unsigned)blocks, threads, 0, s>>>(a);
-    else mover_mixed_kernel<3><<<(unsigned)blocks, threads, 0, s>>>(a);
+    if (a.ndim == 2) mover_mixed_kernel<2><<<(unsigned)blocks, threads, 0, s>>>(a, c);
+    else mover_mixed_kernel<3><<<(unsigned)blocks, threads, 0, s>>>(a, c);
     return cudaGetLastError();
 }
 

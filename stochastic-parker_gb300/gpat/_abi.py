@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 from . import build as _build
@@ -132,11 +133,15 @@ def lib_path() -> Path:
 
 
 def load(path: str | Path | None = None) -> C.CDLL:
-    """Loads the engine library; raises if it has not been built."""
+    """Loads the engine library; raises if it has not been built.
+
+    The first load without a path fixes the process-wide library; the
+    GPAT_ENGINE_LIB environment variable points it at another build."""
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else lib_path()
+    env = os.environ.get("GPAT_ENGINE_LIB")
+    p = Path(path) if path else (Path(env) if env else lib_path())
     if not p.exists():
         raise RuntimeError(
             f"GPAT engine library not found at {p}; build it with "

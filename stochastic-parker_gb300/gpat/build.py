@@ -41,8 +41,8 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the engine needs the CUDA toolkit to build")
 
 
-def _compile(src: str, extra: list[str], nvcc: str, verbose_ptxas: bool) -> Path:
-    out = BUILD_DIR / (src.replace(".", "_") + ".o")
+def _compile(src: str, extra: list[str], nvcc: str, verbose_ptxas: bool, build_dir: Path) -> Path:
+    out = build_dir / (src.replace(".", "_") + ".o")
     cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-I", str(INCLUDE), "-I", str(CSRC), *extra, "-c", str(CSRC / src), "-o", str(out)]
     if src.endswith(".cpp"):
@@ -53,30 +53,39 @@ def _compile(src: str, extra: list[str], nvcc: str, verbose_ptxas: bool) -> Path
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
     if verbose_ptxas:
-        (BUILD_DIR / (src + ".ptxas.txt")).write_text(res.stderr)
+        (build_dir / (src + ".ptxas.txt")).write_text(res.stderr)
     return out
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
-    """Compiles and links the engine; returns the library path."""
+def build(force: bool = False, verbose_ptxas: bool = False, defines: dict | None = None,
+          lib_path: Path | None = None) -> Path:
+    """Compiles and links the engine; returns the library path.
+
+    ``defines`` adds -D macros (tuning knobs such as GPAT_MIXED_MINB_2D) and
+    ``lib_path`` writes the library elsewhere, so variants can sit side by
+    side; load one with ``gpat._abi.load(path)``."""
+    out_path = Path(lib_path) if lib_path else LIB_PATH
     srcs = [CSRC / s for s in SOURCES] + [INCLUDE / "gpat_engine.h",
                                           CSRC / "gpat_internal.h", CSRC / "device_common.cuh"]
-    if LIB_PATH.exists() and not force:
-        lib_mtime = LIB_PATH.stat().st_mtime
+    if out_path.exists() and not force and not defines:
+        lib_mtime = out_path.stat().st_mtime
         if all(s.stat().st_mtime <= lib_mtime for s in srcs):
-            return LIB_PATH
+            return out_path
     nvcc = nvcc_path()
-    BUILD_DIR.mkdir(parents=True, exist_ok=True)
-    LIB_DIR.mkdir(parents=True, exist_ok=True)
+    build_dir = BUILD_DIR if not lib_path else BUILD_DIR / out_path.stem
+    build_dir.mkdir(parents=True, exist_ok=True)
+    out_path.parent.mkdir(parents=True, exist_ok=True)
+    dflags = [f"-D{k}={v}" for k, v in (defines or {}).items()]
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], nvcc, verbose_ptxas), SOURCES.items()))
-    tmp = LIB_PATH.with_suffix(".so.tmp")
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1] + dflags, nvcc, verbose_ptxas,
+                                               build_dir), SOURCES.items()))
+    tmp = out_path.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, out_path)
+    return out_path
 
 
 if __name__ == "__main__":
