@@ -37,6 +37,9 @@ struct gpat_handle {
     DevParticles P[2]{};
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    // split-precision path: particles kept binned by cell
+    void *sort_scratch = nullptr;
+    bool unsorted = true;   // particles appended since the last binning
     DevCounters *dcnt = nullptr;
     DevCounters hcnt{};
     unsigned long long *dbins = nullptr;
@@ -220,6 +223,29 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     return GPAT_OK;
 }
 
+CellGrid cell_grid(const gpat_handle_t *h) {
+    CellGrid g;
+    g.xmin = h->cfg.xmin; g.ymin = h->cfg.ymin; g.zmin = h->cfg.zmin;
+    g.idx = 1.0 / h->cfg.dx; g.idy = 1.0 / h->cfg.dy;
+    g.idz = h->prm.ndim == 3 ? 1.0 / h->cfg.dz : 0.0;
+    g.nxg = h->nxg; g.nyg = h->nyg; g.nzg = h->nzg;
+    return g;
+}
+
+// Bins the current particles by cell into the other buffer (split-precision
+// path), dropping particles that are not in the box.
+int bin_particles(gpat_handle_t *h) {
+    const int nxt = 1 - h->cur;
+    CK(launch_cell_sort(h->P[h->cur], h->P[nxt], h->n, cell_grid(h), h->sort_scratch, h->dcnt,
+                        h->stream));
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    h->cur = nxt;
+    h->n = (int64_t)h->hcnt.nkept;
+    h->unsorted = false;
+    return GPAT_OK;
+}
+
 int ensure_scratch(gpat_handle_t *h, int64_t n) {
     const size_t need = compaction_scratch_bytes(n);
     if (need <= h->scratch_bytes) return GPAT_OK;
@@ -355,6 +381,10 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
         cudaMemsetAsync(h->pmem[b], 0, particle_bytes(h->cap), h->stream);
         h->P[b] = carve(h->pmem[b], h->cap);
     }
+    if (p.precision == GPAT_PREC_MIXED &&
+        cudaMalloc(&h->sort_scratch, cell_sort_scratch_bytes(h->cap, (int64_t)h->ncells)) !=
+            cudaSuccess)
+        return bail(GPAT_ERR_OOM);
     if (cudaMalloc(&h->dcnt, sizeof(DevCounters)) != cudaSuccess) return bail(GPAT_ERR_OOM);
     cudaMemsetAsync(h->dcnt, 0, sizeof(DevCounters), h->stream);
     if (cudaMalloc(&h->dbins, sizeof(unsigned long long) * 3 * (size_t)p.npp_global) != cudaSuccess)
@@ -375,6 +405,7 @@ int gpat_destroy(gpat_handle_t *h) {
     }
     if (h->staging) cudaFree(h->staging);
     if (h->scratch) cudaFree(h->scratch);
+    if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->dcnt) cudaFree(h->dcnt);
     if (h->dbins) cudaFree(h->dbins);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -511,6 +542,7 @@ static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, 
     int rc = pull_counters(h);
     if (rc) return rc;
     h->n += count;
+    if (count > 0) h->unsorted = true;
     h->tag_max += count;
     rc = check_status(h);
     if (rc) return rc;
@@ -553,6 +585,7 @@ int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n)
     CK(cp(D.rng_ctr, src->rng_ctr, 4 * c));
     CK(cudaStreamSynchronize(h->stream));
     h->n = n;
+    h->unsorted = true;
     return GPAT_OK;
 }
 
@@ -594,18 +627,33 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     CK(cudaSetDevice(h->device));
     rc = ensure_scratch(h, h->n);
     if (rc) return rc;
+    const bool mixed = h->prm.precision == GPAT_PREC_MIXED;
+    if (mixed && h->unsorted) {
+        // New particles since the last binning: bin them before moving.
+        rc = bin_particles(h);
+        if (rc) return rc;
+        a.P = h->P[h->cur];
+        a.n = h->n;
+    }
     const unsigned long long steps_before = h->hcnt.steps;
     CK(cudaEventRecord(h->ev0, h->stream));
-    if (h->prm.precision == GPAT_PREC_FP64) CK(launch_mover_fp64(a, h->sm_count, h->stream));
+    if (!mixed) CK(launch_mover_fp64(a, h->sm_count, h->stream));
     else CK(launch_mover_mixed(a, make_mixed_consts(a), h->sm_count, h->stream));
     CK(cudaEventRecord(h->ev1, h->stream));
-    // remove_particles (particle_module.f90:5365-5403), order-preserving.
-    const int nxt = 1 - h->cur;
-    CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt, h->stream));
-    rc = pull_counters(h);
-    if (rc) return rc;
-    h->cur = nxt;
-    h->n = (int64_t)h->hcnt.nkept;
+    if (mixed) {
+        // remove_particles as a binning by cell, so the next call's warps
+        // gather neighbouring field records.
+        rc = bin_particles(h);
+        if (rc) return rc;
+    } else {
+        // remove_particles (particle_module.f90:5365-5403), order-preserving.
+        const int nxt = 1 - h->cur;
+        CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt, h->stream));
+        rc = pull_counters(h);
+        if (rc) return rc;
+        h->cur = nxt;
+        h->n = (int64_t)h->hcnt.nkept;
+    }
     float ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
     h->last_mover_ms = ms;
@@ -627,6 +675,7 @@ int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
     const int64_t created = (int64_t)(h->hcnt.nsplit - before);
     const int64_t wanted = (int64_t)h->hcnt.nkept;
     h->n += created;
+    if (created > 0) h->unsorted = true;
     h->nptl_split += created;
     if (created < wanted) return fail(h, GPAT_ERR_CAPACITY, "nptl_max reached while splitting");
     return GPAT_OK;

@@ -120,6 +120,16 @@ cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap
                                    double split_ratio, double pmin_split, double p0,
                                    double pmax, void *scratch, DevCounters *cnt,
                                    cudaStream_t s);
+// Grid geometry for spatial binning of particles (one bin per field cell).
+struct CellGrid {
+    double xmin, ymin, zmin, idx, idy, idz;
+    int nxg, nyg, nzg;
+};
+// Counting sort of the in-box particles of src into dst by cell; drops the
+// rest (remove_particles) and counts escapes.  cnt->nkept gets the new count.
+size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins);
+cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, int64_t n,
+                             const CellGrid &g, void *scratch, DevCounters *cnt, cudaStream_t s);
 // Global f(p) histogram into (count, whi, wlo) triples per bin (zeroed here).
 cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double pmin,
                              double pmax, unsigned long long *bins, cudaStream_t s);

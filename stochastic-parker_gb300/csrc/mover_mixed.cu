@@ -110,6 +110,16 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, const Mixed
     }
 }
 
+// 256-bit read-only global load (8 floats, 32-byte aligned address).  Records
+// are 64 B (2D) or 96 B (3D) at 32-byte aligned offsets, so one corner costs 2
+// or 3 of these instead of 4 or 6 128-bit loads.
+__device__ __forceinline__ void ld8(const float *p, float (&v)[8]) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+          "=f"(v[7])
+        : "l"(p));
+}
+
 // FP32 bilinear / trilinear interpolation of the packed record.
 template <int NDIM, int NV>
 __device__ __forceinline__ bool interp(const MoverArgs &a, const Pos &q, float rt, float f[NV]) {
@@ -136,25 +146,25 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const Pos &q, float r
                 const size_t cell = base + ii + row * j + plane * kk;
                 float w1 = wc;
                 if (a.time_interp) w1 = wc * (1.0f - rt);
-                const float4 *r4 = reinterpret_cast<const float4 *>(a.rec1 + (size_t)R * cell);
+                const float *r1 = a.rec1 + (size_t)R * cell;
 #pragma unroll
-                for (int v4 = 0; v4 < (NV + 3) / 4; ++v4) {
-                    const float4 g = __ldg(r4 + v4);
-                    const float gv[4] = {g.x, g.y, g.z, g.w};
+                for (int v8 = 0; v8 < (NV + 7) / 8; ++v8) {
+                    float g[8];
+                    ld8(r1 + 8 * v8, g);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        if (4 * v4 + e < NV) f[4 * v4 + e] = fmaf(gv[e], w1, f[4 * v4 + e]);
+                    for (int e = 0; e < 8; ++e)
+                        if (8 * v8 + e < NV) f[8 * v8 + e] = fmaf(g[e], w1, f[8 * v8 + e]);
                 }
                 if (a.time_interp) {
                     const float w2 = wc * rt;
-                    const float4 *s4 = reinterpret_cast<const float4 *>(a.rec2 + (size_t)R * cell);
+                    const float *r2 = a.rec2 + (size_t)R * cell;
 #pragma unroll
-                    for (int v4 = 0; v4 < (NV + 3) / 4; ++v4) {
-                        const float4 g = __ldg(s4 + v4);
-                        const float gv[4] = {g.x, g.y, g.z, g.w};
+                    for (int v8 = 0; v8 < (NV + 7) / 8; ++v8) {
+                        float g[8];
+                        ld8(r2 + 8 * v8, g);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
-                            if (4 * v4 + e < NV) f[4 * v4 + e] = fmaf(gv[e], w2, f[4 * v4 + e]);
+                        for (int e = 0; e < 8; ++e)
+                            if (8 * v8 + e < NV) f[8 * v8 + e] = fmaf(g[e], w2, f[8 * v8 + e]);
                     }
                 }
             }

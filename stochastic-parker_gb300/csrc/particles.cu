@@ -348,7 +348,150 @@ __global__ void __launch_bounds__(256) quick_check_kernel(const DevParticles P, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Spatial binning: counting sort of the in-box particles by grid cell, which
+// also removes everything else (remove_particles).  Lanes of a warp then
+// gather neighbouring field records.  Cells are the interpolation base cell
+// (Fortran floor(px) + 1, i.e. C index floor(px) + 2); order inside a cell
+// follows atomic arrival and is not reproducible, the particle set is.
+// ---------------------------------------------------------------------------
+constexpr int kBinScanThreads = 256;
+constexpr int kBinScanItems = 8;
+constexpr int kBinTile = kBinScanThreads * kBinScanItems;
+
+__global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int64_t n,
+                                                       const CellGrid g, int32_t *keys,
+                                                       unsigned int *counts, DevCounters *cnt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int esc = 0;
+    if (i < n) {
+        const int flag = P.count_flag[i];
+        int32_t key = -1;
+        if (flag == 1) {
+            const double px = (P.x[i] - g.xmin) * g.idx;
+            const double py = (P.y[i] - g.ymin) * g.idy;
+            int cx = (int)floor(fmin(fmax(px, -2.0), (double)g.nxg)) + 2;
+            int cy = (int)floor(fmin(fmax(py, -2.0), (double)g.nyg)) + 2;
+            cx = min(max(cx, 0), g.nxg - 1);
+            cy = min(max(cy, 0), g.nyg - 1);
+            int cz = 0;
+            if (g.nzg > 1) {
+                const double pz = (P.z[i] - g.zmin) * g.idz;
+                cz = (int)floor(fmin(fmax(pz, -2.0), (double)g.nzg)) + 2;
+                cz = min(max(cz, 0), g.nzg - 1);
+            }
+            key = cx + g.nxg * (cy + g.nyg * cz);
+            atomicAdd(&counts[key], 1u);
+        } else if (flag < 0) {
+            esc = 1;
+        }
+        keys[i] = key;
+    }
+    const unsigned e = __ballot_sync(0xffffffffu, esc);
+    if ((threadIdx.x & 31) == 0 && e) atomicAdd(&cnt->nescaped, (unsigned long long)__popc(e));
+}
+
+__global__ void __launch_bounds__(kBinScanThreads) bin_tile_sum_kernel(const unsigned int *counts,
+                                                                       int64_t nbins,
+                                                                       long long *tile_sums) {
+    __shared__ unsigned int warp_tot[kBinScanThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * kBinTile;
+    unsigned int s = 0;
+#pragma unroll
+    for (int k = 0; k < kBinScanItems; ++k) {
+        const int64_t b = base + k * kBinScanThreads + threadIdx.x;
+        if (b < nbins) s += counts[b];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t = 0;
+        for (int w = 0; w < kBinScanThreads / 32; ++w) t += warp_tot[w];
+        tile_sums[blockIdx.x] = t;
+    }
+}
+
+// In-place exclusive scan of the bin counts, one tile of kBinTile bins per
+// block, offset by the scanned tile sums.  Each thread owns kBinScanItems
+// consecutive bins.
+__global__ void __launch_bounds__(kBinScanThreads) bin_tile_scan_kernel(unsigned int *counts,
+                                                                        int64_t nbins,
+                                                                        const long long *tile_offsets) {
+    __shared__ unsigned int warp_pre[kBinScanThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * kBinTile + (int64_t)threadIdx.x * kBinScanItems;
+    unsigned int v[kBinScanItems];
+    unsigned int mine = 0;
+#pragma unroll
+    for (int k = 0; k < kBinScanItems; ++k) {
+        v[k] = (base + k < nbins) ? counts[base + k] : 0u;
+        mine += v[k];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned int x = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_pre[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int acc = 0;
+        for (int w = 0; w < kBinScanThreads / 32; ++w) {
+            const unsigned int c = warp_pre[w];
+            warp_pre[w] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    unsigned int run = (unsigned int)tile_offsets[blockIdx.x] + warp_pre[wid] + (x - mine);
+#pragma unroll
+    for (int k = 0; k < kBinScanItems; ++k) {
+        if (base + k < nbins) counts[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) cell_scatter_kernel(const DevParticles S, const DevParticles D,
+                                                           int64_t n, const int32_t *keys,
+                                                           unsigned int *cursor) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t key = keys[i];
+    if (key < 0) return;
+    const unsigned int pos = atomicAdd(&cursor[key], 1u);
+    copy_particle(S, i, D, (int64_t)pos);
+}
+
 }  // namespace
+
+size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins) {
+    const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
+    return (size_t)cap * 4 + (size_t)nbins * 4 + (size_t)(2 * ntiles + 2) * 8 + 256;
+}
+
+cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, int64_t n,
+                             const CellGrid &g, void *scratch, DevCounters *cnt, cudaStream_t s) {
+    const int64_t nbins = (int64_t)g.nxg * g.nyg * g.nzg;
+    const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
+    char *q = static_cast<char *>(scratch);
+    long long *tile_sums = reinterpret_cast<long long *>(q);
+    long long *tile_offsets = tile_sums + ntiles + 1;
+    unsigned int *counts = reinterpret_cast<unsigned int *>(tile_offsets + ntiles + 1);
+    int32_t *keys = reinterpret_cast<int32_t *>(counts + nbins);
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(unsigned int) * (size_t)nbins, s);
+    if (e != cudaSuccess) return e;
+    if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    cell_key_kernel<<<blocks, 256, 0, s>>>(src, n, g, keys, counts, cnt);
+    bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
+    bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
+    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, n, keys, counts);
+    return cudaGetLastError();
+}
 
 size_t compaction_scratch_bytes(int64_t n) {
     const int64_t ntiles = (n + kTile - 1) / kTile;
