@@ -1,0 +1,363 @@
+!*******************************************************************************
+!< ISO_C_BINDING interface to the GB300 particle-mover engine
+!< (include/gpat_engine.h).  Compiled into GPAT's own build, it lets
+!< solve_transport_equation call the engine in place of the particle_module
+!< and mhd_data_parallel procedures on the mover path; procedure names carry a
+!< gpu_ prefix and the reference's argument lists.
+!<
+!< Particle records cross the boundary as structure-of-arrays: gpu_put_ptls /
+!< gpu_get_ptls copy ptls(1:nptl_current) field by field.
+!*******************************************************************************
+module gpat_gpu
+    use, intrinsic :: iso_c_binding
+    implicit none
+    private
+    public gpat_mhd_config_t, gpat_params_t
+    public gpu_init, gpu_free, gpu_read_particle_params, gpu_calc_tstamps_mhd, &
+        gpu_set_tstamps, gpu_read_field_data, gpu_calc_fields_gradients, &
+        gpu_copy_fields, gpu_inject_particles_spatial_uniform, &
+        gpu_inject_particles_at_x, gpu_particle_mover, gpu_split_particle, &
+        gpu_global_distribution, gpu_pbins_edges, gpu_quick_check, &
+        gpu_put_ptls, gpu_get_ptls, gpu_nptl_current
+
+    integer(c_int), parameter :: GPAT_OK = 0
+
+    type, bind(c) :: gpat_mhd_config_t
+        real(c_double) :: dx, dy, dz, xmin, ymin, zmin, xmax, ymax, zmax
+        real(c_double) :: lx, ly, lz, dt_out
+        integer(c_int32_t) :: nx, ny, nz, nxs, nys, nzs, topox, topoy, topoz
+        integer(c_int32_t) :: nvar, bcx, bcy, bcz
+    end type gpat_mhd_config_t
+
+    type, bind(c) :: gpat_params_t
+        real(c_double) :: b0, p0, pmin, pmax
+        real(c_double) :: gamma_turb, pindex, kpara0, kret, dt_min_rel, dt_max_rel
+        real(c_double) :: acc_region(6)
+        real(c_double) :: drift1, drift2
+        integer(c_int32_t) :: momentum_dependency, mag_dependency, acc_region_flag, charge
+        integer(c_int32_t) :: check_drift_2d, ndim, pbcx, pbcy, pbcz, npp_global
+        integer(c_int64_t) :: seed
+        integer(c_int32_t) :: noise, precision
+        integer(c_int64_t) :: nptl_max
+        integer(c_int32_t) :: time_interp
+        integer(c_int32_t) :: dpp_wave, dpp_shear, deltab_flag, correlation_flag
+        integer(c_int32_t) :: include_3rd_dim, spherical_coord, nonuniform_grid
+    end type gpat_params_t
+
+    type, bind(c) :: gpat_particles_t
+        type(c_ptr) :: x, y, z, p, v, mu, weight, t, dt
+        type(c_ptr) :: split_times, count_flag
+        type(c_ptr) :: origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted
+        type(c_ptr) :: rng_ctr
+    end type gpat_particles_t
+
+    type, bind(c) :: gpat_counters_t
+        integer(c_int64_t) :: nptl_current, nptl_split, nptl_escaped, tag_max
+        real(c_double) :: leak, leak_negp
+        integer(c_int64_t) :: leak_hi, leak_lo, leak_negp_hi, leak_negp_lo
+        integer(c_int64_t) :: steps
+        real(c_double) :: last_mover_ms
+        integer(c_int64_t) :: last_mover_steps
+    end type gpat_counters_t
+
+    interface
+        integer(c_int) function c_read_particle_params(path, params) &
+                bind(c, name="gpat_read_particle_params")
+            import :: c_int, c_char, gpat_params_t
+            character(kind=c_char), dimension(*), intent(in) :: path
+            type(gpat_params_t), intent(inout) :: params
+        end function
+        integer(c_int) function c_create(params, cfg, device, handle) bind(c, name="gpat_create")
+            import :: c_int, c_ptr, gpat_params_t, gpat_mhd_config_t
+            type(gpat_params_t), intent(in) :: params
+            type(gpat_mhd_config_t), intent(in) :: cfg
+            integer(c_int), value :: device
+            type(c_ptr), intent(out) :: handle
+        end function
+        integer(c_int) function c_destroy(handle) bind(c, name="gpat_destroy")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
+        end function
+        type(c_ptr) function c_last_error(handle) bind(c, name="gpat_last_error")
+            import :: c_ptr
+            type(c_ptr), value :: handle
+        end function
+        integer(c_int) function c_set_tstamps(handle, tstamps, n) bind(c, name="gpat_set_tstamps")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            real(c_double), dimension(*), intent(in) :: tstamps
+            integer(c_int), value :: n
+        end function
+        integer(c_int) function c_calc_tstamps_mhd(handle, t_start, t_end) &
+                bind(c, name="gpat_calc_tstamps_mhd")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
+            integer(c_int), value :: t_start, t_end
+        end function
+        integer(c_int) function c_read_field_data(handle, filename, var_flag) &
+                bind(c, name="gpat_read_field_data")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: filename
+            integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_calc_fields_gradients(handle, var_flag) &
+                bind(c, name="gpat_calc_fields_gradients")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
+            integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_copy_fields(handle) bind(c, name="gpat_copy_fields")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
+        end function
+        integer(c_int) function c_inject_uniform(handle, nptl, dt, dist_flag, particle_v0, &
+                ct_mhd, part_box, power_index) bind(c, name="gpat_inject_particles_spatial_uniform")
+            import :: c_int, c_ptr, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int64_t), value :: nptl
+            real(c_double), value :: dt, particle_v0, power_index
+            integer(c_int), value :: dist_flag, ct_mhd
+            real(c_double), dimension(6), intent(in) :: part_box
+        end function
+        integer(c_int) function c_inject_at_x(handle, nptl, xpos, dt, dist_flag, particle_v0, &
+                ct_mhd, power_index) bind(c, name="gpat_inject_particles_at_x")
+            import :: c_int, c_ptr, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int64_t), value :: nptl
+            real(c_double), value :: xpos, dt, particle_v0, power_index
+            integer(c_int), value :: dist_flag, ct_mhd
+        end function
+        integer(c_int) function c_particle_mover(handle, focused_transport, nlgc, kperp_kpara, &
+                nsteps_interval, mhd_tframe, num_fine_steps, dump_escaped_dist) &
+                bind(c, name="gpat_particle_mover")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            integer(c_int), value :: focused_transport, nlgc, nsteps_interval, mhd_tframe
+            integer(c_int), value :: num_fine_steps, dump_escaped_dist
+            real(c_double), value :: kperp_kpara
+        end function
+        integer(c_int) function c_split_particle(handle, split_ratio, pmin_split, &
+                nsteps_interval) bind(c, name="gpat_split_particle")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            real(c_double), value :: split_ratio, pmin_split
+            integer(c_int), value :: nsteps_interval
+        end function
+        integer(c_int) function c_distributions(handle, fglobal, counts) &
+                bind(c, name="gpat_calc_particle_distributions")
+            import :: c_int, c_ptr, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            real(c_double), dimension(*), intent(out) :: fglobal
+            integer(c_int64_t), dimension(*), intent(out) :: counts
+        end function
+        integer(c_int) function c_pbins_edges(handle, edges) bind(c, name="gpat_pbins_edges")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            real(c_double), dimension(*), intent(out) :: edges
+        end function
+        integer(c_int) function c_quick_check(handle, out) bind(c, name="gpat_quick_check")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            real(c_double), dimension(8), intent(out) :: out
+        end function
+        integer(c_int) function c_put_particles(handle, src, n) bind(c, name="gpat_put_particles")
+            import :: c_int, c_ptr, c_int64_t, gpat_particles_t
+            type(c_ptr), value :: handle
+            type(gpat_particles_t), intent(in) :: src
+            integer(c_int64_t), value :: n
+        end function
+        integer(c_int) function c_get_particles(handle, dst, capacity, n) &
+                bind(c, name="gpat_get_particles")
+            import :: c_int, c_ptr, c_int64_t, gpat_particles_t
+            type(c_ptr), value :: handle
+            type(gpat_particles_t), intent(inout) :: dst
+            integer(c_int64_t), value :: capacity
+            integer(c_int64_t), intent(out) :: n
+        end function
+        integer(c_int) function c_get_counters(handle, out) bind(c, name="gpat_get_counters")
+            import :: c_int, c_ptr, gpat_counters_t
+            type(c_ptr), value :: handle
+            type(gpat_counters_t), intent(out) :: out
+        end function
+    end interface
+
+    type(c_ptr), save :: h = c_null_ptr
+
+    contains
+
+    subroutine check(rc, what)
+        integer(c_int), intent(in) :: rc
+        character(*), intent(in) :: what
+        character(kind=c_char), pointer :: msg(:)
+        integer :: i
+        if (rc == GPAT_OK) return
+        call c_f_pointer(c_last_error(h), msg, [256])
+        write(*, "(A,A,I0)", advance="no") "gpat_gpu: ", what//" failed, code ", rc
+        write(*, "(A)", advance="no") ": "
+        do i = 1, 256
+            if (msg(i) == c_null_char) exit
+            write(*, "(A)", advance="no") msg(i)
+        enddo
+        write(*, *)
+        stop 1
+    end subroutine check
+
+    !< init_particles + init_field_data + init_particle_distributions
+    subroutine gpu_init(params, cfg, device)
+        type(gpat_params_t), intent(in) :: params
+        type(gpat_mhd_config_t), intent(in) :: cfg
+        integer, intent(in) :: device
+        call check(c_create(params, cfg, int(device, c_int), h), "gpat_create")
+    end subroutine gpu_init
+
+    subroutine gpu_free
+        integer(c_int) :: rc
+        if (c_associated(h)) rc = c_destroy(h)
+        h = c_null_ptr
+    end subroutine gpu_free
+
+    !< read_particle_params (particle_module.f90:2778-2878)
+    subroutine gpu_read_particle_params(conf_file, params)
+        character(*), intent(in) :: conf_file
+        type(gpat_params_t), intent(inout) :: params
+        call check(c_read_particle_params(trim(conf_file)//c_null_char, params), &
+            "read_particle_params")
+    end subroutine gpu_read_particle_params
+
+    !< calc_tstamps_mhd (mhd_config.f90:263-271)
+    subroutine gpu_calc_tstamps_mhd(t_start, t_end)
+        integer, intent(in) :: t_start, t_end
+        call check(c_calc_tstamps_mhd(h, int(t_start, c_int), int(t_end, c_int)), "calc_tstamps")
+    end subroutine gpu_calc_tstamps_mhd
+
+    !< tstamps_mhd from load_tstamps_mhd (mhd_config.f90:218-255)
+    subroutine gpu_set_tstamps(tstamps)
+        real(c_double), dimension(:), intent(in) :: tstamps
+        call check(c_set_tstamps(h, tstamps, int(size(tstamps), c_int)), "set_tstamps")
+    end subroutine gpu_set_tstamps
+
+    !< read_field_data_parallel (mhd_data_parallel.f90:224-300)
+    subroutine gpu_read_field_data(filename, var_flag)
+        character(*), intent(in) :: filename
+        integer, intent(in) :: var_flag
+        call check(c_read_field_data(h, trim(filename)//c_null_char, int(var_flag, c_int)), &
+            "read_field_data")
+    end subroutine gpu_read_field_data
+
+    !< calc_fields_gradients (mhd_data_parallel.f90:504-610)
+    subroutine gpu_calc_fields_gradients(var_flag)
+        integer, intent(in) :: var_flag
+        call check(c_calc_fields_gradients(h, int(var_flag, c_int)), "calc_fields_gradients")
+    end subroutine gpu_calc_fields_gradients
+
+    !< copy_fields (mhd_data_parallel.f90:1920-1926)
+    subroutine gpu_copy_fields
+        call check(c_copy_fields(h), "copy_fields")
+    end subroutine gpu_copy_fields
+
+    !< inject_particles_spatial_uniform (particle_module.f90:454-530)
+    subroutine gpu_inject_particles_spatial_uniform(nptl, dt, dist_flag, particle_v0, &
+            ct_mhd, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd
+        real(8), intent(in) :: dt, particle_v0, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call check(c_inject_uniform(h, int(nptl, c_int64_t), dt, int(dist_flag, c_int), &
+            particle_v0, int(ct_mhd, c_int), part_box, power_index), "inject_uniform")
+    end subroutine gpu_inject_particles_spatial_uniform
+
+    !< Injection on the plane x = xpos (inject_particles_at_shock draw order)
+    subroutine gpu_inject_particles_at_x(nptl, xpos, dt, dist_flag, particle_v0, ct_mhd, &
+            power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd
+        real(8), intent(in) :: xpos, dt, particle_v0, power_index
+        call check(c_inject_at_x(h, int(nptl, c_int64_t), xpos, dt, int(dist_flag, c_int), &
+            particle_v0, int(ct_mhd, c_int), power_index), "inject_at_x")
+    end subroutine gpu_inject_particles_at_x
+
+    !< particle_mover (particle_module.f90:1846-1974), same arguments
+    subroutine gpu_particle_mover(focused_transport, nlgc, kperp_kpara, nsteps_interval, &
+            mhd_tframe, num_fine_steps, dump_escaped_dist)
+        logical, intent(in) :: focused_transport, nlgc, dump_escaped_dist
+        real(8), intent(in) :: kperp_kpara
+        integer, intent(in) :: nsteps_interval, mhd_tframe, num_fine_steps
+        call check(c_particle_mover(h, merge(1_c_int, 0_c_int, focused_transport), &
+            merge(1_c_int, 0_c_int, nlgc), kperp_kpara, int(nsteps_interval, c_int), &
+            int(mhd_tframe, c_int), int(num_fine_steps, c_int), &
+            merge(1_c_int, 0_c_int, dump_escaped_dist)), "particle_mover")
+    end subroutine gpu_particle_mover
+
+    !< split_particle (particle_module.f90:5430-5480), same arguments
+    subroutine gpu_split_particle(split_ratio, pmin_split, nsteps_interval)
+        real(8), intent(in) :: split_ratio, pmin_split
+        integer, intent(in) :: nsteps_interval
+        call check(c_split_particle(h, split_ratio, pmin_split, int(nsteps_interval, c_int)), &
+            "split_particle")
+    end subroutine gpu_split_particle
+
+    !< fglobal(1, :) of calc_particle_distributions (diagnostics.f90:738-780)
+    subroutine gpu_global_distribution(fglobal, counts)
+        real(c_double), dimension(:), intent(out) :: fglobal
+        integer(c_int64_t), dimension(:), intent(out) :: counts
+        call check(c_distributions(h, fglobal, counts), "calc_particle_distributions")
+    end subroutine gpu_global_distribution
+
+    !< pbins_edges_global (diagnostics.f90:194-204)
+    subroutine gpu_pbins_edges(edges)
+        real(c_double), dimension(:), intent(out) :: edges
+        call check(c_pbins_edges(h, edges), "pbins_edges")
+    end subroutine gpu_pbins_edges
+
+    !< quick_check sums (diagnostics.f90:116-170)
+    subroutine gpu_quick_check(out)
+        real(c_double), dimension(8), intent(out) :: out
+        call check(c_quick_check(h, out), "quick_check")
+    end subroutine gpu_quick_check
+
+    integer function gpu_nptl_current()
+        type(gpat_counters_t) :: c
+        call check(c_get_counters(h, c), "get_counters")
+        gpu_nptl_current = int(c%nptl_current)
+    end function gpu_nptl_current
+
+    !< Copies particle arrays (structure of arrays, length n) to the engine.
+    subroutine gpu_put_ptls(n, x, y, z, p, v, mu, weight, t, dt, split_times, count_flag, &
+            origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted, rng_ctr)
+        integer, intent(in) :: n
+        real(c_double), dimension(n), intent(in), target :: x, y, z, p, v, mu, weight, t, dt
+        integer(c_int8_t), dimension(n), intent(in), target :: split_times, count_flag
+        integer(c_int32_t), dimension(n), intent(in), target :: origin, nsteps_tracked, &
+            nsteps_pushed, tag_injected, tag_splitted, rng_ctr
+        type(gpat_particles_t) :: s
+        s%x = c_loc(x); s%y = c_loc(y); s%z = c_loc(z); s%p = c_loc(p); s%v = c_loc(v)
+        s%mu = c_loc(mu); s%weight = c_loc(weight); s%t = c_loc(t); s%dt = c_loc(dt)
+        s%split_times = c_loc(split_times); s%count_flag = c_loc(count_flag)
+        s%origin = c_loc(origin); s%nsteps_tracked = c_loc(nsteps_tracked)
+        s%nsteps_pushed = c_loc(nsteps_pushed); s%tag_injected = c_loc(tag_injected)
+        s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_loc(rng_ctr)
+        call check(c_put_particles(h, s, int(n, c_int64_t)), "put_particles")
+    end subroutine gpu_put_ptls
+
+    !< Copies the engine's particles into arrays of length capacity; n on exit.
+    subroutine gpu_get_ptls(capacity, n, x, y, z, p, v, mu, weight, t, dt, split_times, &
+            count_flag, origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted, rng_ctr)
+        integer, intent(in) :: capacity
+        integer, intent(out) :: n
+        real(c_double), dimension(capacity), intent(out), target :: x, y, z, p, v, mu, weight, &
+            t, dt
+        integer(c_int8_t), dimension(capacity), intent(out), target :: split_times, count_flag
+        integer(c_int32_t), dimension(capacity), intent(out), target :: origin, nsteps_tracked, &
+            nsteps_pushed, tag_injected, tag_splitted, rng_ctr
+        type(gpat_particles_t) :: s
+        integer(c_int64_t) :: got
+        s%x = c_loc(x); s%y = c_loc(y); s%z = c_loc(z); s%p = c_loc(p); s%v = c_loc(v)
+        s%mu = c_loc(mu); s%weight = c_loc(weight); s%t = c_loc(t); s%dt = c_loc(dt)
+        s%split_times = c_loc(split_times); s%count_flag = c_loc(count_flag)
+        s%origin = c_loc(origin); s%nsteps_tracked = c_loc(nsteps_tracked)
+        s%nsteps_pushed = c_loc(nsteps_pushed); s%tag_injected = c_loc(tag_injected)
+        s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_loc(rng_ctr)
+        call check(c_get_particles(h, s, int(capacity, c_int64_t), got), "get_particles")
+        n = int(got)
+    end subroutine gpu_get_ptls
+
+end module gpat_gpu
