@@ -55,7 +55,39 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bin-interval", type=int, default=0,
+                    help="pushes between re-binnings (0: engine default, <0: once per call)")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 sample and the f(p) tail-error check")
     return ap.parse_args()
+
+
+def l2_read_gbs(torch, dev) -> float:
+    """Read bandwidth of a 64 MiB L2-resident buffer (torch.sum), an estimate
+    of the cache bound the mover's gathers run against."""
+    x = torch.ones(16 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(5):
+        x.sum()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(50):
+        x.sum()
+    e1.record()
+    torch.cuda.synchronize()
+    return x.numel() * 4 * 50 / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+def fp64_sample(w_kwargs, device, nptl):
+    """Plain FP64 GPU mover on a sample of the same workload: one interval."""
+    from gpat import configs
+    w = configs.turbulent_shock_2d(precision=0, **w_kwargs)
+    eng = configs.build_engine(w, device=device, nptl_max=nptl)
+    configs.inject(eng, w, nptl=nptl)
+    eng.particle_mover(nsteps_interval=10, mhd_tframe=1, num_fine_steps=1)
+    c = eng.counters()
+    eng.close()
+    return c.last_mover_steps / (c.last_mover_ms / 1e3), c.last_mover_steps
 
 
 # ---------------------------------------------------------------------------
@@ -158,12 +190,12 @@ def measured_peaks() -> dict:
 
 
 def profiled_traffic(name: str):
-    """DRAM bytes per launch recorded in profiles/<name>.md ('traffic_bytes_per_launch: N')."""
+    """DRAM bytes per push recorded in profiles/<name>.md ('traffic_bytes_per_push: N')."""
     p = REPO / "profiles" / f"{name}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith("traffic_bytes_per_push:"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
@@ -242,11 +274,12 @@ def run_ours(args, world, rank, local):
     total_frames = args.warmup + args.steps + args.e2e_steps + 2
     w = configs.turbulent_shock_2d(scale=args.scale, n=args.grid, precision=prec, seed=2 + rank,
                                    nframes=total_frames)
-    eng = configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6))
+    eng = configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6),
+                               bin_interval=args.bin_interval)
     configs.inject(eng, w)
     stream = torch.cuda.ExternalStream(eng.stream, device=dev)
     frame = [1]
-    kernel_ms, kernel_steps, kernel_n = [], [], []
+    kernel_ms, kernel_steps, kernel_n, kernel_launches = [], [], [], []
 
     def step():
         n_before = eng.nptl_current
@@ -255,13 +288,14 @@ def run_ours(args, world, rank, local):
         kernel_ms.append(c.last_mover_ms)
         kernel_steps.append(c.last_mover_steps)
         kernel_n.append(n_before)
+        kernel_launches.append(c.last_mover_launches)
         eng.split_particle(2.72, 2.0, 10)
         eng.calc_particle_distributions()
         frame[0] += 1
 
     for _ in range(args.warmup):
         step()
-    kernel_ms.clear(); kernel_steps.clear(); kernel_n.clear()
+    kernel_ms.clear(); kernel_steps.clear(); kernel_n.clear(); kernel_launches.clear()
 
     clocks = ClockSampler(local)
     steps0 = eng.counters().steps
@@ -319,19 +353,27 @@ def run_ours(args, world, rank, local):
         eng.close()
         return
     peaks = measured_peaks()
-    avg_ms = statistics.mean(kernel_ms)
-    avg_steps = statistics.mean(kernel_steps)
+    launches = statistics.mean(kernel_launches)
+    avg_ms = statistics.mean(kernel_ms) / launches          # per mover launch
+    avg_steps = statistics.mean(kernel_steps) / launches
     avg_n = statistics.mean(kernel_n)
     bytes_launch = avg_steps * GATHER_BYTES_PER_STEP_2D + avg_n * STATE_BYTES_PER_PARTICLE
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9
     kname = f"mover_{args.precision}_turbulent_shock_2d"
+    traffic = profiled_traffic(kname)
+    l2 = l2_read_gbs(torch, dev)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": profiled_traffic(kname),
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": traffic * avg_steps if traffic is not None else None,
                 "kernel": f"mover_{args.precision}_kernel<2>",
                 "peak_source": peaks["source"],
                 "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
+                "mover_launches_per_interval": launches,
                 "kernel_steps_per_s": avg_steps / (avg_ms / 1e3),
-                "algorithmic_bytes_per_launch": bytes_launch}
+                "algorithmic_bytes_per_launch": bytes_launch,
+                "note": "gathers are served from L1/L2; frac > 1 means above the HBM roofline "
+                        "of the algorithmic bytes; traffic = ncu DRAM bytes per push x pushes",
+                "l2_read_gbs_measured": l2, "frac_of_l2_read": achieved / l2}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -341,12 +383,23 @@ def run_ours(args, world, rank, local):
                        "step": "particle_mover + split_particle + f(p) over one MHD interval",
                        "l2": "inputs exceed L2 (fields 269 MB packed, particles ~1 GB)",
                        "parallelism": f"replicas x{world}"},
-            "clocks": clk, "gpu_launches": 8 * args.steps,
+            "clocks": clk,
+            # per step: mover launches, a 5-kernel binning after each, split (3), f(p) (1)
+            "gpu_launches": int(round(sum(6 * l + 4 for l in kernel_launches))) if prec
+            else 8 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": e2e_h2d // max(1, args.e2e_steps),
                     "d2h_bytes_per_step": e2e_d2h // max(1, args.e2e_steps)},
             "roofline": roofline}
     eng.close()
+    if not args.no_accuracy and prec == 1:
+        from gpat import accuracy
+        n64 = max(1000, int(1e6 * args.scale))
+        v64, s64 = fp64_sample(dict(scale=args.scale, n=args.grid, seed=2 + rank), local, n64)
+        line["fp64_gpu"] = {"value": v64, "unit": UNIT, "sample": f"{n64} particles, one interval, "
+                                                                  f"{s64} particle-steps",
+                            "mixed_over_fp64": value / v64}
+        line["accuracy"] = accuracy.planar_shock_check(scale=1.0, device=local)
     if world == 1 and not args.no_cpu_baseline:
         v, cores, n, steps, dt, _ = cpu_sample(w, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

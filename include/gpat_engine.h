@@ -20,9 +20,10 @@
  *  - Random increments come from Philox-4x32-10 keyed by (seed, particle
  *    tags, push counter) instead of per-thread MT19937 streams, so results
  *    are reproducible for any launch shape.
- *  - remove_particles keeps the survivors in their original order; the
+ *  - remove_particles keeps the survivors in their original order on the
+ *    FP64 path and bins them by field cell on the split-precision path; the
  *    reference swaps removed particles to the end.  Particle sets, counters
- *    and histograms are unaffected.
+ *    and histograms are unaffected by the order.
  *  - leak, leak_negp and all histogram weights are accumulated as exact
  *    128-bit fixed point (64 fraction bits), so sums do not depend on order.
  */
@@ -47,7 +48,7 @@ extern "C" {
 #define GPAT_ERR_DEVICE (-9)       /* device status word set (NaN / index guard) */
 
 #define GPAT_PREC_FP64 0    /* FP64 everywhere, reference operation order      */
-#define GPAT_PREC_MIXED 1   /* FP32 fields/kappa/drift, FP64 accumulators      */
+#define GPAT_PREC_MIXED 1   /* FP32 fields/kappa/drift, compensated sums       */
 
 #define GPAT_NOISE_UNIFORM 0  /* (2u-1)*sqrt(3), the reference's increment    */
 #define GPAT_NOISE_GAUSS 1    /* Box-Muller Gaussian increments               */
@@ -84,6 +85,11 @@ typedef struct gpat_params {
      * correlation_flag, include_3rd_dim, spherical_coord, nonuniform_grid. */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
+    /* Split-precision mover only: pushes per particle between re-binnings of
+     * the particle set by cell inside one gpat_particle_mover call (0: engine
+     * default of 128; negative: bin once per call).  Results are the same
+     * for any value; it only changes memory locality. */
+    int32_t bin_interval;
 } gpat_params_t;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays.  rng_ctr
@@ -103,6 +109,7 @@ typedef struct gpat_counters {
     uint64_t steps;                             /* particle pushes, cumulative */
     double last_mover_ms;                       /* device time of last mover  */
     uint64_t last_mover_steps;
+    int64_t last_mover_launches;                /* mover kernel launches used */
 } gpat_counters_t;
 
 typedef struct gpat_handle gpat_handle_t;

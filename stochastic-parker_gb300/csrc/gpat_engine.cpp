@@ -49,6 +49,7 @@ struct gpat_handle {
     int64_t nptl_split = 0;
     double last_mover_ms = 0.0;
     uint64_t last_mover_steps = 0;
+    int64_t last_mover_launches = 0;
 };
 
 namespace {
@@ -636,16 +637,38 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         a.n = h->n;
     }
     const unsigned long long steps_before = h->hcnt.steps;
-    CK(cudaEventRecord(h->ev0, h->stream));
-    if (!mixed) CK(launch_mover_fp64(a, h->sm_count, h->stream));
-    else CK(launch_mover_mixed(a, make_mixed_consts(a), h->sm_count, h->stream));
-    CK(cudaEventRecord(h->ev1, h->stream));
+    double mover_ms = 0.0;
+    int64_t launches = 0;
     if (mixed) {
-        // remove_particles as a binning by cell, so the next call's warps
-        // gather neighbouring field records.
-        rc = bin_particles(h);
-        if (rc) return rc;
+        // Chunks of bin_interval pushes per particle; between chunks the set is
+        // binned by cell again (and removal happens), so lanes of a warp keep
+        // gathering neighbouring records while the particles spread out.
+        const int bi = h->prm.bin_interval;
+        a.chunk_pushes = bi == 0 ? 128u : (bi > 0 ? (uint32_t)bi : 0u);
+        const MixedConsts k = make_mixed_consts(a);
+        const int64_t max_chunks = (int64_t)a.max_pushes / (a.chunk_pushes ? a.chunk_pushes : 1) + 4;
+        for (;;) {
+            CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
+            a.P = h->P[h->cur];
+            a.n = h->n;
+            CK(cudaEventRecord(h->ev0, h->stream));
+            CK(launch_mover_mixed(a, k, h->sm_count, h->stream));
+            CK(cudaEventRecord(h->ev1, h->stream));
+            ++launches;
+            rc = bin_particles(h);   // remove_particles as a binning by cell
+            if (rc) return rc;
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            mover_ms += ms;
+            if (h->hcnt.nactive == 0) break;
+            if (launches > max_chunks)
+                return fail(h, GPAT_ERR_DEVICE, "mover chunks did not finish the interval");
+        }
     } else {
+        CK(cudaEventRecord(h->ev0, h->stream));
+        CK(launch_mover_fp64(a, h->sm_count, h->stream));
+        CK(cudaEventRecord(h->ev1, h->stream));
+        launches = 1;
         // remove_particles (particle_module.f90:5365-5403), order-preserving.
         const int nxt = 1 - h->cur;
         CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt, h->stream));
@@ -653,10 +676,12 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         if (rc) return rc;
         h->cur = nxt;
         h->n = (int64_t)h->hcnt.nkept;
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        mover_ms = ms;
     }
-    float ms = 0.0f;
-    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-    h->last_mover_ms = ms;
+    h->last_mover_ms = mover_ms;
+    h->last_mover_launches = launches;
     h->last_mover_steps = h->hcnt.steps - steps_before;
     return check_status(h);
 }
@@ -746,6 +771,7 @@ int gpat_get_counters(gpat_handle_t *h, gpat_counters_t *out) {
     out->steps = c.steps;
     out->last_mover_ms = h->last_mover_ms;
     out->last_mover_steps = h->last_mover_steps;
+    out->last_mover_launches = h->last_mover_launches;
     return GPAT_OK;
 }
 

@@ -36,6 +36,7 @@ struct DevCounters {
     unsigned long long nkept;
     unsigned long long nsplit;
     unsigned long long wsum_hi, wsum_lo, dtsum_hi, dtsum_lo;
+    unsigned long long nactive;   // particles a chunked mover launch left mid-interval
     double dt_min, dt_max;
     unsigned int status;
     unsigned int pad;
@@ -65,6 +66,8 @@ struct MoverArgs {
     int check_drift_2d, pbcx, pbcy, pbcz, noise;
     uint32_t key0, key1;
     uint32_t max_pushes;        // per particle per call, guards runaway loops
+    uint32_t chunk_pushes;      // split-precision mover: stop a particle after this many
+                                // pushes (between pushes) so the set can be re-binned; 0 = off
     DevCounters *cnt;
 };
 

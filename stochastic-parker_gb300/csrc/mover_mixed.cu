@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
     mover_mixed_kernel(const MoverArgs a, const MixedConsts k) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t pushes = 0;
+    bool active = false;
     if (i < a.n) {
         const double x_in = a.P.x[i], y_in = a.P.y[i], z_in = a.P.z[i];
         const double p_in = a.P.p[i], t_in = a.P.t[i];
@@ -382,11 +383,16 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
             boundary<NDIM>(a, k, q, true, flag, i);
         }
         bool alive = (flag == 1);
+        bool paused = false;
         while (alive && target_d < a.limit) {
             const float target = (float)target_d;
             while (tau - tc < target && flag == 1) {
                 negp_or_boundary<NDIM>(a, k, q, p - pc, flag, i);
                 if (flag != 1) break;
+                if (a.chunk_pushes != 0 && pushes >= a.chunk_pushes) {
+                    paused = true;   // between pushes: the next launch resumes from t
+                    break;
+                }
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
                 const float pe = p - pc;
                 float dp;
@@ -411,7 +417,7 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
                     flag = 0; alive = false; break;
                 }
             }
-            if (!alive) break;
+            if (!alive || paused) break;
             if (tau - tc > target && flag == 1) {
                 // Undo the overshooting push, redo it with dt = target - t.
                 advance(q.cx, q.fx, -uX);
@@ -449,7 +455,8 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
             }
             target_d = target_d + a.dt_fine;
         }
-        if (flag == 1) boundary<NDIM>(a, k, q, false, flag, i);
+        if (flag == 1 && !paused) boundary<NDIM>(a, k, q, false, flag, i);
+        active = paused;
         // Write back input + change, computed in FP64.
         const double dcx = (double)(q.cx - q_in.cx) + ((double)q.fx - (double)q_in.fx);
         const double dcy = (double)(q.cy - q_in.cy) + ((double)q.fy - (double)q_in.fy);
@@ -471,7 +478,11 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
         a.P.rng_ctr[i] = ctr;
     }
     const unsigned long long steps = warp_sum_u64(pushes);
-    if ((threadIdx.x & 31) == 0 && steps) atomicAdd(&a.cnt->steps, steps);
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0) {
+        if (steps) atomicAdd(&a.cnt->steps, steps);
+        if (act) atomicAdd(&a.cnt->nactive, (unsigned long long)__popc(act));
+    }
 }
 
 }  // namespace

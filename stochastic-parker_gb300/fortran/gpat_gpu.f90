@@ -42,6 +42,7 @@ module gpat_gpu
         integer(c_int32_t) :: time_interp
         integer(c_int32_t) :: dpp_wave, dpp_shear, deltab_flag, correlation_flag
         integer(c_int32_t) :: include_3rd_dim, spherical_coord, nonuniform_grid
+        integer(c_int32_t) :: bin_interval
     end type gpat_params_t
 
     type, bind(c) :: gpat_particles_t
@@ -58,6 +59,7 @@ module gpat_gpu
         integer(c_int64_t) :: steps
         real(c_double) :: last_mover_ms
         integer(c_int64_t) :: last_mover_steps
+        integer(c_int64_t) :: last_mover_launches
     end type gpat_counters_t
 
     interface

@@ -60,6 +60,7 @@ class Params(C.Structure):
         ("time_interp", i32),
         ("dpp_wave", i32), ("dpp_shear", i32), ("deltab_flag", i32), ("correlation_flag", i32),
         ("include_3rd_dim", i32), ("spherical_coord", i32), ("nonuniform_grid", i32),
+        ("bin_interval", i32),
     ]
 
 
@@ -85,7 +86,7 @@ class Counters(C.Structure):
         ("leak", d), ("leak_negp", d),
         ("leak_hi", u64), ("leak_lo", u64), ("leak_negp_hi", u64), ("leak_negp_lo", u64),
         ("steps", u64),
-        ("last_mover_ms", d), ("last_mover_steps", u64),
+        ("last_mover_ms", d), ("last_mover_steps", u64), ("last_mover_launches", i64),
     ]
 
 

@@ -1,0 +1,90 @@
+"""f(p) agreement of the split-precision mover with the FP64 mover.
+
+Both movers start from the same injected particles (injection is
+deterministic) and run the same intervals with splitting; their noise streams
+are independent, so the comparison carries Monte Carlo error.  The FP64 GPU
+mover is bit-identical to the CPU oracle on these paths (tests/
+test_gpu_parity.py), so it serves as the FP64 oracle at sizes the CPU would
+take minutes for.
+
+tail error: relative difference of the weighted counts summed over the top
+decade of populated p of the FP64 run, with its standard error
+sqrt(sum w^2 over both runs) / W_fp64.  Per-bin differences and a chi-square
+over bins with enough particles are reported too.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import configs
+
+
+def _spectrum(eng, edges):
+    ps = eng.get_particles()
+    p, w = ps["p"], ps["weight"]
+    npp = len(edges) - 1
+    lo = math.log10(edges[0])
+    d = (math.log10(edges[-1]) - lo) / npp
+    ok = (p > edges[0]) & (p <= edges[-1])
+    ib = np.floor((np.log10(p[ok]) - lo) / d).astype(np.int64)
+    keep = (ib >= 0) & (ib < npp)
+    ib, ww = ib[keep], w[ok][keep]
+    f = np.bincount(ib, weights=ww, minlength=npp)
+    f2 = np.bincount(ib, weights=ww * ww, minlength=npp)
+    c = np.bincount(ib, minlength=npp)
+    return f, f2, c
+
+
+def compare(workload: configs.Workload, intervals: int, split=(2.72, 2.0),
+            device: int = 0) -> dict:
+    """Runs the workload in FP64 and split precision; returns the tail error."""
+    out = {}
+    for prec in (0, 1):
+        eng = configs.build_engine(workload, device=device, precision=prec,
+                                   nptl_max=int(workload.nptl * 8))
+        configs.inject(eng, workload)
+        for k in range(intervals):
+            eng.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=1)
+            if split:
+                eng.split_particle(split[0], split[1], 10)
+        edges = eng.pbins_edges()
+        f_dev, _ = eng.calc_particle_distributions()
+        f, f2, c = _spectrum(eng, edges)
+        out[prec] = dict(f=f, f2=f2, c=c, f_dev=f_dev, n=eng.nptl_current,
+                         steps=eng.counters().steps)
+        eng.close()
+    a, b = out[0], out[1]
+    populated = np.nonzero(a["c"])[0]
+    if len(populated) == 0:
+        raise RuntimeError("FP64 run has an empty spectrum")
+    b_hi = int(populated[-1])
+    edges = np.logspace(math.log10(workload.params["pmin"]), math.log10(workload.params["pmax"]),
+                        len(a["f"]) + 1)
+    p_hi = edges[b_hi + 1]
+    top = np.arange(len(a["f"])) [(edges[:-1] >= p_hi / 10.0) & (np.arange(len(a["f"])) <= b_hi)]
+    w64, wmx = a["f"][top].sum(), b["f"][top].sum()
+    sig = math.sqrt(a["f2"][top].sum() + b["f2"][top].sum()) / w64
+    m = (a["c"] + b["c"]) >= 20
+    chi2 = float(np.sum((a["f"][m] - b["f"][m]) ** 2 / (a["f2"][m] + b["f2"][m])))
+    per_bin = np.where(a["f"] > 0, (b["f"] - a["f"]) / np.where(a["f"] > 0, a["f"], 1.0), 0.0)
+    return {
+        "tail_err": float((wmx - w64) / w64), "tail_err_sigma": sig,
+        "top_decade_p": [float(p_hi / 10.0), float(p_hi)],
+        "top_decade_particles_fp64": int(a["c"][top].sum()),
+        "chi2": chi2, "chi2_dof": int(m.sum()),
+        "per_bin_rel_err_top": [float(x) for x in per_bin[top]],
+        "nptl_fp64": a["n"], "nptl_mixed": b["n"],
+        "steps_fp64": int(a["steps"]), "steps_mixed": int(b["steps"]),
+        # the device histogram against a host binning of the same particles
+        "device_hist_matches": bool(np.array_equal(a["f_dev"], a["f"])),
+    }
+
+
+def planar_shock_check(scale: float = 1.0, t_end: float = 2.0, device: int = 0) -> dict:
+    """The planar-shock workload (512x64, r = 4) to t_end with splitting."""
+    w = configs.planar_shock(scale=scale, t_end=t_end)
+    r = compare(w, w.nframes, split=(2.72, 2.0), device=device)
+    r["workload"] = f"{w.name}, {w.nptl} particles injected, t = {t_end}, split 2.72 / 2.0"
+    return r
