@@ -39,8 +39,21 @@ METRIC = "particle-steps/s on 1 GB300 (mixed/learned vs plain FP64) at f(p) tail
 UNIT = "particle-steps/s"
 # Algorithmic bytes of one 2D push: 4 cell corners x 15 FP32 field values
 # gathered; per particle and launch the FP64 state is read and written once.
-GATHER_BYTES_PER_STEP_2D = 4 * 15 * 4
+# 3D: 8 corners x 21 values.
+GATHER_BYTES_PER_STEP = {2: 4 * 15 * 4, 3: 8 * 21 * 4}
 STATE_BYTES_PER_PARTICLE = 2 * (7 * 8 + 2 + 4 * 4)
+WORKLOADS = ("turbulent_shock_2d", "turbulence_3d")
+
+
+def make_workload(args, precision, seed=None, nframes=16, scale=None):
+    from gpat import configs
+    scale = args.scale if scale is None else scale
+    if args.workload == "turbulence_3d":
+        grid = args.grid if args.grid != 2048 else 256
+        return configs.turbulence_3d(scale=scale, n=grid, precision=precision,
+                                     seed=3 if seed is None else seed, nframes=nframes)
+    return configs.turbulent_shock_2d(scale=scale, n=args.grid, precision=precision,
+                                      seed=2 if seed is None else seed, nframes=nframes)
 
 
 def parse_args():
@@ -51,7 +64,9 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
     ap.add_argument("--scale", type=float, default=1.0, help="particle-count multiplier")
-    ap.add_argument("--grid", type=int, default=2048)
+    ap.add_argument("--grid", type=int, default=2048,
+                    help="cells per side (the 3D workload uses 256 unless set)")
+    ap.add_argument("--workload", choices=WORKLOADS, default="turbulent_shock_2d")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -78,10 +93,10 @@ def l2_read_gbs(torch, dev) -> float:
     return x.numel() * 4 * 50 / (e0.elapsed_time(e1) / 1e3) / 1e9
 
 
-def fp64_sample(w_kwargs, device, nptl):
+def fp64_sample(args, seed, device, nptl):
     """Plain FP64 GPU mover on a sample of the same workload: one interval."""
     from gpat import configs
-    w = configs.turbulent_shock_2d(precision=0, **w_kwargs)
+    w = make_workload(args, 0, seed=seed, nframes=2)
     eng = configs.build_engine(w, device=device, nptl_max=nptl)
     configs.inject(eng, w, nptl=nptl)
     eng.particle_mover(nsteps_interval=10, mhd_tframe=1, num_fine_steps=1)
@@ -218,7 +233,14 @@ def cpu_sample(w, seconds: float, threads: int | None = None):
     def run(n):
         parts = oracle.Particles(n)
         cnt = oracle.OrcCounters()
-        oracle.inject_at_x(prm, cfg, parts, n, w.inject["xpos"], 1e-7, 1, 1.0, 0.0, cnt)
+        if w.inject["kind"] == "at_x":
+            oracle.inject_at_x(prm, cfg, parts, n, w.inject["xpos"], 1e-7, 1, 1.0, 0.0, cnt)
+        else:
+            c = w.mhd_config
+            box = (c.xmin, c.ymin, c.zmin, c.xmin + c.nx * c.dx, c.ymin + c.ny * c.dy,
+                   c.zmin + c.nz * c.dz)
+            oracle.inject_spatial_uniform(prm, parts, n, 1e-7, w.inject["dist_flag"], 1.0, 0.0,
+                                          0.0, box, cnt, power_index=w.inject["power_index"])
         t0 = time.perf_counter()
         oracle.mover(prm, cfg, full, parts, 0.0, dtf, nthreads=nthreads, counters=cnt)
         return cnt.steps, time.perf_counter() - t0
@@ -236,8 +258,9 @@ def run_reference(args, world, rank):
     from gpat import configs
     if rank != 0:
         return
-    w = configs.turbulent_shock_2d(scale=args.scale, n=args.grid, precision=1, nframes=4)
+    w = make_workload(args, 1, nframes=4)
     vals = []
+    # the oracle restates the reference's FP64 mover
     per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
     for k in range(args.warmup + args.steps):
         v, cores, n, steps, dt, _ = cpu_sample(w, per_step)
@@ -254,7 +277,7 @@ def run_reference(args, world, rank):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": w.name, "particles_per_rank": w.nptl,
-                       "pushes_per_interval": 1000, "precision": "fp64"},
+                       "precision": "fp64"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -272,8 +295,8 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     prec = 1 if args.precision == "mixed" else 0
     total_frames = args.warmup + args.steps + args.e2e_steps + 2
-    w = configs.turbulent_shock_2d(scale=args.scale, n=args.grid, precision=prec, seed=2 + rank,
-                                   nframes=total_frames)
+    w = make_workload(args, prec, seed=(3 if args.workload == "turbulence_3d" else 2) + rank,
+                      nframes=total_frames)
     eng = configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6),
                                bin_interval=args.bin_interval)
     configs.inject(eng, w)
@@ -289,7 +312,8 @@ def run_ours(args, world, rank, local):
         kernel_steps.append(c.last_mover_steps)
         kernel_n.append(n_before)
         kernel_launches.append(c.last_mover_launches)
-        eng.split_particle(2.72, 2.0, 10)
+        if w.split:
+            eng.split_particle(w.split["ratio"], w.split["pmin"], 10)
         eng.calc_particle_distributions()
         frame[0] += 1
 
@@ -338,7 +362,8 @@ def run_ours(args, world, rank, local):
         eng.put_particles(cur)
         e2e_h2d += len(cur) * bytes_per_ptl
         eng.particle_mover(nsteps_interval=10, mhd_tframe=frame[0], num_fine_steps=1)
-        eng.split_particle(2.72, 2.0, 10)
+        if w.split:
+            eng.split_particle(w.split["ratio"], w.split["pmin"], 10)
         f, counts = eng.calc_particle_distributions()
         cur = eng.get_particles(out=host)
         e2e_d2h += len(cur) * bytes_per_ptl + f.nbytes + counts.nbytes
@@ -357,15 +382,19 @@ def run_ours(args, world, rank, local):
     avg_ms = statistics.mean(kernel_ms) / launches          # per mover launch
     avg_steps = statistics.mean(kernel_steps) / launches
     avg_n = statistics.mean(kernel_n)
-    bytes_launch = avg_steps * GATHER_BYTES_PER_STEP_2D + avg_n * STATE_BYTES_PER_PARTICLE
+    ndim = 3 if args.workload == "turbulence_3d" else 2
+    ncells = (w.mhd_config.nx + 4) * (w.mhd_config.ny + 4) * ((w.mhd_config.nz + 4) if ndim == 3 else 1)
+    rec_mb = ncells * (64 if ndim == 2 else 96) / 1e6
+    state_mb = avg_n * 98 / 1e6
+    bytes_launch = avg_steps * GATHER_BYTES_PER_STEP[ndim] + avg_n * STATE_BYTES_PER_PARTICLE
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9
-    kname = f"mover_{args.precision}_turbulent_shock_2d"
+    kname = f"mover_{args.precision}_{args.workload}"
     traffic = profiled_traffic(kname)
     l2 = l2_read_gbs(torch, dev)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"],
                 "traffic": traffic * avg_steps if traffic is not None else None,
-                "kernel": f"mover_{args.precision}_kernel<2>",
+                "kernel": f"mover_{args.precision}_kernel<{ndim}>",
                 "peak_source": peaks["source"],
                 "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
                 "mover_launches_per_interval": launches,
@@ -379,9 +408,13 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+ff" if prec else "f64", "data": "synthetic",
             "config": {"workload": w.name, "particles_per_rank": w.nptl,
-                       "pushes_per_interval": 1000, "precision": args.precision,
-                       "step": "particle_mover + split_particle + f(p) over one MHD interval",
-                       "l2": "inputs exceed L2 (fields 269 MB packed, particles ~1 GB)",
+                       "pushes_per_particle_per_interval":
+                           round(statistics.mean(kernel_steps) / max(1.0, avg_n), 1),
+                       "precision": args.precision,
+                       "step": "particle_mover" + (" + split_particle" if w.split else "") +
+                               " + f(p) over one MHD interval",
+                       "l2": f"inputs exceed L2 (packed field records {rec_mb:.0f} MB, "
+                             f"particle state {state_mb:.0f} MB)",
                        "parallelism": f"replicas x{world}"},
             "clocks": clk,
             # per step: mover launches, a 5-kernel binning after each, split (3), f(p) (1)
@@ -395,7 +428,8 @@ def run_ours(args, world, rank, local):
     if not args.no_accuracy and prec == 1:
         from gpat import accuracy
         n64 = max(1000, int(1e6 * args.scale))
-        v64, s64 = fp64_sample(dict(scale=args.scale, n=args.grid, seed=2 + rank), local, n64)
+        v64, s64 = fp64_sample(args, (3 if args.workload == "turbulence_3d" else 2) + rank, local,
+                               n64)
         line["fp64_gpu"] = {"value": v64, "unit": UNIT, "sample": f"{n64} particles, one interval, "
                                                                   f"{s64} particle-steps",
                             "mixed_over_fp64": value / v64}
@@ -403,8 +437,9 @@ def run_ours(args, world, rank, local):
     if world == 1 and not args.no_cpu_baseline:
         v, cores, n, steps, dt, _ = cpu_sample(w, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"{n} particles injected on the shock, one MHD interval "
-                                          f"of FP64 pushes ({steps} particle-steps in {dt:.2f} s)"}
+                                "sample": f"{n} particles of {w.name} injected as the workload "
+                                          f"does, one MHD interval of FP64 pushes ({steps} "
+                                          f"particle-steps in {dt:.2f} s)"}
     print(json.dumps(line), flush=True)
 
 

@@ -12,7 +12,8 @@ turbulent_shock_2d
                interval (dt_min = dtf / 1000).
 turbulence_3d  256^3 periodic box, v rms 0.3 (30 % compressive power),
                B = z + solenoidal dB (0.3), kperp/kpar = 0.02, 1e8 particles
-               uniform in space, log-uniform p in [p0, 10 p0], 500 pushes.
+               uniform in space, log-uniform p in [p0, 10 p0], adaptive dt
+               between dt_out/5000 and dt_out/500.
 
 Each builder takes ``scale`` (particle count multiplier) and grid overrides
 so tests can run reduced cases with the same physics.
@@ -57,7 +58,8 @@ def planar_shock(scale: float = 1.0, nx: int = 512, ny: int = 64, t_end: float =
     params["nptl_max"] = nptl
     return Workload("planar_shock_512x64", params, cfg, frame, nptl,
                     dict(kind="at_x", xpos=0.5, dist_flag=1),
-                    np.arange(nframes + 1) * dt_out, nframes)
+                    np.arange(nframes + 1) * dt_out, nframes,
+                    split=dict(ratio=2.72, pmin=2.0))
 
 
 def turbulent_shock_2d(scale: float = 1.0, n: int = 2048, dt_out: float = 0.01,
@@ -78,24 +80,27 @@ def turbulent_shock_2d(scale: float = 1.0, n: int = 2048, dt_out: float = 0.01,
     params["nptl_max"] = nptl
     return Workload(f"turbulent_shock_2d_{n}x{n}", params, cfg, frame, nptl,
                     dict(kind="at_x", xpos=0.5, dist_flag=1),
-                    np.arange(nframes + 1) * dt_out, nframes)
+                    np.arange(nframes + 1) * dt_out, nframes,
+                    split=dict(ratio=2.72, pmin=2.0))
 
 
-def turbulence_3d(scale: float = 1.0, n: int = 256, dt_out: float = 0.01, pushes: int = 500,
+def turbulence_3d(scale: float = 1.0, n: int = 256, dt_out: float = 0.05, pushes: int = 500,
                   precision: int = 1, seed: int = 3, nframes: int = 16) -> Workload:
+    """256^3 periodic box.  dt is adaptive between dt_out/5000 and
+    dt_out/pushes (the reference's rule; compressive regions pick steps
+    below dt_max, about 1800 pushes per interval on average).  Injection is log-uniform in [p0, 10 p0] (dist_flag 2 with power index 1
+    draws p = (pmax/p0)^u p0), so pmax = 10 p0 also bounds f(p)."""
     p0 = 0.1
-    params = dict(p0=p0, pmin=p0, pmax=1.0e4 * p0, momentum_dependency=1, gamma_turb=5.0 / 3.0,
-                  mag_dependency=0, kpara0=0.01, kret=0.02, dt_min_rel=1.0 / pushes,
-                  dt_max_rel=1.0e-2, ndim=3, pbcx=0, pbcy=0, pbcz=0, npp_global=128,
+    params = dict(p0=p0, pmin=p0, pmax=10.0 * p0, momentum_dependency=1, gamma_turb=5.0 / 3.0,
+                  mag_dependency=0, kpara0=0.01, kret=0.02, dt_min_rel=1.0 / (10 * pushes),
+                  dt_max_rel=1.0 / pushes, ndim=3, pbcx=0, pbcy=0, pbcz=0, npp_global=128,
                   precision=precision, seed=seed)
     cfg = make_mhd_config(n, n, n, 0.0, 1.0, 0.0, 1.0, zmin=0.0, zmax=1.0, dt_out=dt_out, ndim=3)
     frame = fields.turbulence_3d(n, seed=3000 + seed)
     nptl = max(1, int(round(1.0e8 * scale)))
     params["nptl_max"] = nptl
-    # log-uniform p in [p0, 10 p0]: dist_flag 2 with power_index 1 uses
-    # p = (pmax/p0)^u p0, so the injector runs with pmax = 10 p0.
     return Workload(f"turbulence_3d_{n}^3", params, cfg, frame, nptl,
-                    dict(kind="uniform", dist_flag=2, power_index=1.0, pmax_inject=10.0 * p0),
+                    dict(kind="uniform", dist_flag=2, power_index=1.0),
                     np.arange(nframes + 1) * dt_out, nframes)
 
 
