@@ -1,0 +1,242 @@
+// gpat_run: replay driver for the engine.  Runs the per-frame sequence of
+// solve_transport_equation (src/programs/stochastic-mhd.f90:312-567) through
+// the C ABI only, with the reference's command-line switches for the options
+// on the mover path (stochastic-mhd.f90:572-946).
+//
+//   gpat_run -dm data/ -cf conf.dat -ts 0 -te 20 -np 100000 -nm 1000000 ...
+//
+// Outputs in the diagnostics directory (-dd): quick.dat with the reference's
+// columns (diagnostics.f90:116-170) and, per frame, fdists_XXXX.dat: int32
+// npp, npp + 1 float64 bin edges, npp float64 weighted counts, npp uint64
+// particle counts (the fglobal / pbins_edges_global datasets of
+// fdists_XXXX.h5, without HDF5).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "gpat_engine.h"
+
+namespace {
+
+struct Options {
+    std::string dir_mhd_data = "data/", mhd_config_filename = "mhd_config.dat";
+    std::string conf_file = "conf.dat", diagnostics_directory = "data/";
+    long long nptl_max = 10000000, nptl = 10000;
+    int time_interp_flag = 0, t_start = 0, t_end = 200, tmax_mhd = 100000;
+    int single_time_frame = 0, dist_flag = 0, split_flag = 1, nsteps_interval = 10;
+    int num_fine_steps = 1, ndim_field = 2, charge = -1, inject_new_ptl = 0;
+    int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
+    double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
+    double particle_v0 = 5.0, drift_param1 = 4e7, drift_param2 = 2e8;
+    double ptl_box[6] = {0.0, 0.0, 0.0, 1.0, 1.0, 1.0};   // xmin ymin zmin xmax ymax zmax
+    // engine options
+    int precision = GPAT_PREC_MIXED, noise = GPAT_NOISE_UNIFORM, device = 0, bin_interval = 0;
+    unsigned long long seed = 0x5EED0001ull;
+    double shock_xpos = 0.5;
+    bool conf_in_config_dir = true;
+};
+
+bool truthy(const std::string &v) {
+    return v == "1" || v == ".true." || v == "true" || v == "T" || v == ".TRUE.";
+}
+
+// Switch table: long and short names of the reference's CLI (and a few of
+// the engine's own, long names only).
+int parse(int argc, char **argv, Options &o) {
+    std::map<std::string, std::string> alias = {
+        {"-dm", "--dir_mhd_data"}, {"-mc", "--mhd_config_filename"}, {"-nm", "--nptl_max"},
+        {"-np", "--nptl"}, {"-ti", "--time_interp_flag"}, {"-dt", "--tinterval"},
+        {"-ts", "--tstart"}, {"-te", "--tend"}, {"-tm", "--tmax_mhd"},
+        {"-st", "--single_time_frame"}, {"-df", "--dist_flag"}, {"-pi", "--power_index"},
+        {"-sf", "--split_flag"}, {"-sr", "--split_ratio"}, {"-ps", "--pmin_split"},
+        {"-ni", "--nsteps_interval"}, {"-dd", "--diagnostics_directory"},
+        {"-is", "--inject_at_shock"}, {"-in", "--inject_new_ptl"}, {"-tti", "--tmax_to_inject"},
+        {"-ip", "--inject_part_box"}, {"-xs", "--ptl_xmin"}, {"-xe", "--ptl_xmax"},
+        {"-ys", "--ptl_ymin"}, {"-ye", "--ptl_ymax"}, {"-zs", "--ptl_zmin"}, {"-ze", "--ptl_zmax"},
+        {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
+        {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
+        {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}};
+    for (int i = 1; i < argc; ++i) {
+        std::string k = argv[i];
+        if (alias.count(k)) k = alias[k];
+        if (k == "--help" || k == "-h") return 1;
+        if (i + 1 >= argc) { std::fprintf(stderr, "gpat_run: %s needs a value\n", argv[i]); return 2; }
+        const std::string v = argv[++i];
+        const double d = std::atof(v.c_str());
+        if (k == "--dir_mhd_data") o.dir_mhd_data = v;
+        else if (k == "--mhd_config_filename") o.mhd_config_filename = v;
+        else if (k == "--nptl_max") o.nptl_max = (long long)d;
+        else if (k == "--nptl") o.nptl = (long long)d;
+        else if (k == "--time_interp_flag") o.time_interp_flag = (int)d;
+        else if (k == "--tinterval") o.tinterval = d;
+        else if (k == "--tstart") o.t_start = (int)d;
+        else if (k == "--tend") o.t_end = (int)d;
+        else if (k == "--tmax_mhd") o.tmax_mhd = (int)d;
+        else if (k == "--single_time_frame") o.single_time_frame = (int)d;
+        else if (k == "--dist_flag") o.dist_flag = (int)d;
+        else if (k == "--power_index") o.power_index = d;
+        else if (k == "--split_flag") o.split_flag = (int)d;
+        else if (k == "--split_ratio") o.split_ratio = d;
+        else if (k == "--pmin_split") o.pmin_split = d;
+        else if (k == "--nsteps_interval") o.nsteps_interval = (int)d;
+        else if (k == "--diagnostics_directory") o.diagnostics_directory = v;
+        else if (k == "--inject_at_shock") o.inject_at_shock = truthy(v);
+        else if (k == "--inject_new_ptl") o.inject_new_ptl = truthy(v);
+        else if (k == "--tmax_to_inject") o.tmax_to_inject = (int)d;
+        else if (k == "--inject_part_box") o.inject_part_box = truthy(v);
+        else if (k == "--ptl_xmin") o.ptl_box[0] = d;
+        else if (k == "--ptl_ymin") o.ptl_box[1] = d;
+        else if (k == "--ptl_zmin") o.ptl_box[2] = d;
+        else if (k == "--ptl_xmax") o.ptl_box[3] = d;
+        else if (k == "--ptl_ymax") o.ptl_box[4] = d;
+        else if (k == "--ptl_zmax") o.ptl_box[5] = d;
+        else if (k == "--conf_file") o.conf_file = v;
+        else if (k == "--num_fine_steps") o.num_fine_steps = (int)d;
+        else if (k == "--ndim_field") o.ndim_field = (int)d;
+        else if (k == "--drift_param1") o.drift_param1 = d;
+        else if (k == "--drift_param2") o.drift_param2 = d;
+        else if (k == "--charge") o.charge = (int)d;
+        else if (k == "--particle_v0") o.particle_v0 = d;
+        else if (k == "--check_drift_2d") o.check_drift_2d = (int)d;
+        else if (k == "--precision") o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
+        else if (k == "--noise") o.noise = (v == "gauss" || v == "1") ? GPAT_NOISE_GAUSS : GPAT_NOISE_UNIFORM;
+        else if (k == "--seed") o.seed = std::strtoull(v.c_str(), nullptr, 0);
+        else if (k == "--device") o.device = (int)d;
+        else if (k == "--bin_interval") o.bin_interval = (int)d;
+        else if (k == "--shock_xpos") o.shock_xpos = d;
+        else if (k == "--conf_path_is_literal") o.conf_in_config_dir = !truthy(v);
+        else { std::fprintf(stderr, "gpat_run: unknown switch %s\n", argv[i - 1]); return 2; }
+    }
+    return 0;
+}
+
+#define CHECK(call)                                                                    \
+    do {                                                                               \
+        int rc_ = (call);                                                              \
+        if (rc_ != GPAT_OK && rc_ != GPAT_ERR_CAPACITY) {                              \
+            std::fprintf(stderr, "gpat_run: %s failed (%d): %s\n", #call, rc_,         \
+                         h ? gpat_last_error(h) : "");                                 \
+            if (h) gpat_destroy(h);                                                    \
+            return 1;                                                                  \
+        }                                                                              \
+    } while (0)
+
+std::string frame_name(const std::string &dir, int tf) {
+    char buf[32];
+    std::snprintf(buf, sizeof buf, "mhd_data_%04d", tf);
+    return dir + buf;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    Options o;
+    const int prc = parse(argc, argv, o);
+    if (prc) {
+        std::fprintf(stderr, "usage: gpat_run [reference switches] (see stochastic-mhd.f90)\n");
+        return prc == 1 ? 0 : 2;
+    }
+    if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
+    gpat_handle_t *h = nullptr;
+
+    gpat_mhd_config_t cfg;
+    const std::string cfg_path = o.dir_mhd_data + o.mhd_config_filename;
+    CHECK(gpat_load_mhd_config(cfg_path.c_str(), &cfg));
+
+    gpat_params_t p;
+    std::memset(&p, 0, sizeof p);
+    p.npp_global = 128;
+    const std::string conf = o.conf_in_config_dir ? "config/" + o.conf_file : o.conf_file;
+    CHECK(gpat_read_particle_params(conf.c_str(), &p));
+    p.drift1 = o.drift_param1;
+    p.drift2 = o.drift_param2;
+    p.charge = o.charge;
+    p.check_drift_2d = o.check_drift_2d;
+    p.ndim = o.ndim_field;
+    p.seed = o.seed;
+    p.noise = o.noise;
+    p.precision = o.precision;
+    p.nptl_max = o.nptl_max;
+    p.time_interp = o.time_interp_flag;
+    p.bin_interval = o.bin_interval;
+    CHECK(gpat_create(&p, &cfg, o.device, &h));
+    CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
+
+    // Frame tmin into farray1, gradients (:321, :350).
+    const int tmin = o.t_start;
+    CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tmin).c_str(), 0));
+    CHECK(gpat_calc_fields_gradients(h, 0));
+    double part_box[6];
+    if (o.inject_part_box) {
+        for (int i = 0; i < 6; ++i) part_box[i] = o.ptl_box[i];
+    } else {
+        part_box[0] = cfg.xmin; part_box[1] = cfg.ymin; part_box[2] = cfg.zmin;
+        part_box[3] = cfg.xmin + cfg.nx * cfg.dx; part_box[4] = cfg.ymin + cfg.ny * cfg.dy;
+        part_box[5] = o.ndim_field == 3 ? cfg.zmin + cfg.nz * cfg.dz : cfg.zmax;
+    }
+
+    const int npp = p.npp_global;
+    std::vector<double> edges(npp + 1), fglobal(npp);
+    std::vector<uint64_t> counts(npp);
+    CHECK(gpat_pbins_edges(h, edges.data()));
+    const std::string qpath = o.diagnostics_directory + "quick.dat";
+    FILE *quick = std::fopen(qpath.c_str(), "w");
+    if (!quick) { std::fprintf(stderr, "gpat_run: cannot write %s\n", qpath.c_str()); gpat_destroy(h); return 1; }
+    std::fprintf(quick, "%6s%13s%13s%13s%13s%13s%13s%13s%13s\n", "iframe", "nptl_current",
+                 "nptl_split", "ntot", "leak", "leak_negp", "pdt_min", "pdt_max", "pdt_avg");
+
+    auto diagnostics = [&](int frame) -> int {
+        double q[8];
+        int rc = gpat_quick_check(h, q);
+        if (rc) return rc;
+        std::fprintf(quick, "%06d%13.6E%13.6E%13.6E%13.6E%13.6E%13.6E%13.6E%13.6E\n", frame, q[0],
+                     q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
+        std::fflush(quick);
+        rc = gpat_calc_particle_distributions(h, fglobal.data(), counts.data());
+        if (rc) return rc;
+        char name[64];
+        std::snprintf(name, sizeof name, "fdists_%04d.dat", frame);
+        FILE *f = std::fopen((o.diagnostics_directory + name).c_str(), "wb");
+        if (!f) return GPAT_ERR_IO;
+        const int32_t n32 = npp;
+        std::fwrite(&n32, 4, 1, f);
+        std::fwrite(edges.data(), 8, edges.size(), f);
+        std::fwrite(fglobal.data(), 8, fglobal.size(), f);
+        std::fwrite(counts.data(), 8, counts.size(), f);
+        std::fclose(f);
+        return GPAT_OK;
+    };
+
+    for (int tf = tmin + 1; tf <= o.t_end; ++tf) {
+        if (o.single_time_frame == 0 && tf <= o.tmax_mhd) {
+            CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tf).c_str(), o.time_interp_flag));
+            CHECK(gpat_calc_fields_gradients(h, o.time_interp_flag));
+        }
+        const int ct = tf - o.t_start;
+        if (o.inject_at_shock) {
+            CHECK(gpat_inject_particles_at_x(h, o.nptl, o.shock_xpos, o.tinterval, o.dist_flag,
+                                             o.particle_v0, ct, o.power_index));
+        } else if ((tf == o.t_start + 1 || o.inject_new_ptl) && tf <= o.tmax_to_inject) {
+            CHECK(gpat_inject_particles_spatial_uniform(h, o.nptl, o.tinterval, o.dist_flag,
+                                                        o.particle_v0, ct, part_box,
+                                                        o.power_index));
+        }
+        if (tf == o.t_start + 1) CHECK(diagnostics(o.t_start));
+        CHECK(gpat_particle_mover(h, 0, 0, 0.0, o.nsteps_interval, ct, o.num_fine_steps, 0));
+        if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
+        CHECK(diagnostics(tf));
+        if (o.time_interp_flag == 1) CHECK(gpat_copy_fields(h));
+        gpat_counters_t c;
+        CHECK(gpat_get_counters(h, &c));
+        std::printf("frame %d: %lld particles, %llu pushes, mover %.2f ms\n", tf,
+                    (long long)c.nptl_current, (unsigned long long)c.last_mover_steps,
+                    c.last_mover_ms);
+    }
+    std::fclose(quick);
+    gpat_destroy(h);
+    return 0;
+}

@@ -85,7 +85,29 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines: dict | None
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, out_path)
+    if not lib_path:
+        build_driver()
     return out_path
+
+
+DRIVER_SRC = CSRC / "gpat_run.cpp"
+DRIVER_PATH = LIB_DIR / "gpat_run"
+
+
+def build_driver(force: bool = False) -> Path:
+    """Compiles the C++ replay driver against the engine library (C ABI only)."""
+    if DRIVER_PATH.exists() and not force and \
+            DRIVER_PATH.stat().st_mtime >= max(DRIVER_SRC.stat().st_mtime, LIB_PATH.stat().st_mtime):
+        return DRIVER_PATH
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for gpat_run")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), str(DRIVER_SRC),
+           "-L", str(LIB_DIR), "-lgpat_engine", "-Wl,-rpath,$ORIGIN", "-o", str(DRIVER_PATH)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"gpat_run build failed:\n{res.stdout}\n{res.stderr}")
+    return DRIVER_PATH
 
 
 if __name__ == "__main__":

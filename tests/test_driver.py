@@ -1,0 +1,98 @@
+"""gpat_run, the C++ replay driver: it drives the C ABI in the order of
+solve_transport_equation (stochastic-mhd.f90:312-567) from the reference's
+on-disk inputs (conf.dat, mhd_config.dat, mhd_data_XXXX) and writes quick.dat
+and fdists_XXXX.dat.  On a GPU its f(p) must equal the same sequence driven
+from Python, bit for bit (FP64 path)."""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gpat import build, configs, fields
+from gpat.engine import Engine, make_params
+
+SEED = 0x1234567
+
+
+def _dataset(tmp_path: Path):
+    w = configs.planar_shock(scale=0.02, t_end=0.3, dt_out=0.1, dt_min=1e-3)
+    data = tmp_path / "data"
+    data.mkdir()
+    (tmp_path / "config").mkdir()
+    out = tmp_path / "out"
+    out.mkdir()
+    fields.write_mhd_config(data / "mhd_config.dat", w.mhd_config)
+    for t in range(4):
+        fields.write_mhd_data(data / f"mhd_data_{t:04d}", w.frame)
+    p = w.params
+    keys = ("b0", "p0", "pmin", "pmax", "momentum_dependency", "gamma_turb", "mag_dependency",
+            "kpara0", "kret", "dt_min_rel", "dt_max_rel")
+    vals = dict(b0=1.0, **p)
+    lines = ["!< conf.dat written by the test"] + [f"{k} = {vals[k]!r}" for k in keys]
+    lines += ["acc_region_flag = 0", "npp_global = 64", "nmu_global = 1",
+              f"pbcx = {p['pbcx']}", f"pbcy = {p['pbcy']}", f"pbcz = {p['pbcz']}"]
+    (tmp_path / "config" / "conf.dat").write_text("\n".join(lines) + "\n")
+    return w, data, out
+
+
+def _run_driver(tmp_path, data, out, precision="fp64"):
+    exe = build.build_driver()
+    cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
+           "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
+           "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
+           "--precision", precision, "--seed", str(SEED)]
+    return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+
+
+def _read_fdists(path: Path):
+    raw = path.read_bytes()
+    npp = int(np.frombuffer(raw[:4], np.int32)[0])
+    off = 4
+    edges = np.frombuffer(raw[off:off + 8 * (npp + 1)], np.float64); off += 8 * (npp + 1)
+    f = np.frombuffer(raw[off:off + 8 * npp], np.float64); off += 8 * npp
+    c = np.frombuffer(raw[off:off + 8 * npp], np.uint64)
+    return edges, f, c
+
+
+def test_driver_usage_without_gpu(engine_lib):
+    exe = build.build_driver()
+    r = subprocess.run([str(exe), "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "usage" in r.stderr
+    r = subprocess.run([str(exe), "--no_such_switch", "1"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 2
+    r = subprocess.run([str(exe), "-dm", "/nonexistent/"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1 and "gpat_load_mhd_config" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_matches_python_sequence(tmp_path):
+    w, data, out = _dataset(tmp_path)
+    r = _run_driver(tmp_path, data, out)
+    assert r.returncode == 0, r.stderr
+    quick = (out / "quick.dat").read_text().splitlines()
+    assert len(quick) == 5 and quick[0].split()[0] == "iframe"
+    edges, f_drv, c_drv = _read_fdists(out / "fdists_0003.dat")
+
+    # The same calls from Python.
+    prm = make_params(**dict(w.params, npp_global=64, nptl_max=40000, seed=SEED, precision=0,
+                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1))
+    eng = Engine(prm, w.mhd_config, 0)
+    eng.calc_tstamps_mhd(0, 3)
+    eng.read_field_data(data / "mhd_data_0000", 0)
+    eng.calc_fields_gradients(0)
+    for tf in range(1, 4):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        eng.inject_particles_at_x(2000, 0.5, 1e-7, 1, 1.0, tf)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1)
+        eng.split_particle(2.72, 2.0, 10)
+    f, c = eng.calc_particle_distributions()
+    assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)
+    np.testing.assert_allclose(edges, eng.pbins_edges(), rtol=0)
+    q = eng.quick_check()
+    last = quick[-1].split()
+    assert int(last[0]) == 3 and float(last[1]) == q["nptl_current"]
+    eng.close()
