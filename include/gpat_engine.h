@@ -214,6 +214,29 @@ int gpat_split_particle_noalloc(const gpat_particles_t *dev, int64_t n, int64_t 
  * fglobal[npp_global] weighted counts (may be NULL) and counts[npp_global]
  * particle numbers (may be NULL).  Bins are exact. */
 int gpat_calc_particle_distributions(gpat_handle_t *h, double *fglobal, uint64_t *counts);
+/* One set of local distribution parameters (conf.dat pmin1 pmax1 npbins1
+ * nmu1 rx1 ry1 rz1 ..., read_diagnostics_params diagnostics.f90:2100-2200). */
+typedef struct gpat_local_dist {
+    double pmin, pmax;
+    int32_t npbins, nmu, rx, ry, rz, reserved;
+} gpat_local_dist_t;
+/* Shape of flocal for a parameter set: {nmu, npbins, nrx, nry, nrz} with
+ * nrx = (nx + rx - 1) / rx (init_local_particle_distributions :231-330). */
+int gpat_local_distribution_dims(gpat_handle_t *h, const gpat_local_dist_t *spec, int32_t dims[5]);
+/* A local distribution of calc_particle_distributions (diagnostics.f90:
+ * 782-878): flocal(imu, ip, ix, iy, iz) in Fortran order (imu fastest),
+ * ix = floor((x - xmin) / (lx / nrx)) + 1, and, as in the reference, only
+ * 0 < ip < npbins (the last p bin stays empty).  Weighted sums are exact;
+ * counts (may be NULL) are particle numbers. */
+int gpat_calc_local_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec, double *flocal,
+                                 uint64_t *counts);
+/* Global distribution of the particles removed through an open boundary
+ * since the last reset (calc_escaped_distributions, diagnostics.f90:913-960):
+ * fescaped(npp_global, 2 * ndim) in Fortran order, column ibc = |count_flag|
+ * (1 low x, 2 high x, 3 low y, 4 high y, 5 low z, 6 high z). */
+int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t *counts);
+/* reset_escaped_particles: clears the escaped distribution. */
+int gpat_reset_escaped_particles(gpat_handle_t *h);
 /* pbins_edges_global (diagnostics.f90:194-204): npp_global + 1 values. */
 int gpat_pbins_edges(gpat_handle_t *h, double *edges);
 /* quick_check (diagnostics.f90:116-170) for one rank: out = {nptl_current,

@@ -666,6 +666,39 @@ static void swap_particles(orc_particles *P, int64_t a, int64_t b)
 #undef SWP
 }
 
+/* Escaped-particle distribution (calc_escaped_distributions,
+ * diagnostics.f90:950-957), filled by remove_particles when enabled. */
+static struct {
+    int npp;
+    double pmin, pmax, pmin_log, dp_log;
+    uint64_t *counts, *whi, *wlo;
+} g_esc;
+
+void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *counts,
+                               uint64_t *whi, uint64_t *wlo)
+{
+    g_esc.npp = npp;
+    g_esc.pmin = pmin;
+    g_esc.pmax = pmax;
+    g_esc.pmin_log = npp > 0 ? log10(pmin) : 0.0;
+    g_esc.dp_log = npp > 0 ? (log10(pmax) - g_esc.pmin_log) / npp : 0.0;
+    g_esc.counts = counts;
+    g_esc.whi = whi;
+    g_esc.wlo = wlo;
+}
+
+static void escaped_add(const orc_particles *P, int64_t i)
+{
+    if (!g_esc.counts || P->count_flag[i] >= 0 || P->count_flag[i] < -6) return;
+    const double p = P->p[i], mu = P->mu[i];
+    if (!(p > g_esc.pmin && p <= g_esc.pmax && mu >= -1.0 && mu <= 1.0)) return;
+    const int ip = (int)floor((log10(p) - g_esc.pmin_log) / g_esc.dp_log);
+    if (ip < 0 || ip >= g_esc.npp) return;
+    const int k = (-P->count_flag[i] - 1) * g_esc.npp + ip;
+    g_esc.counts[k] += 1;
+    orc_fixed_add(&g_esc.whi[k], &g_esc.wlo[k], P->weight[i]);
+}
+
 /* remove_particles: particle_module.f90:5365-5403 (same swap order). */
 int64_t orc_remove_particles(orc_particles *P, int64_t n, orc_counters *cnt)
 {
@@ -676,7 +709,10 @@ int64_t orc_remove_particles(orc_particles *P, int64_t n, orc_counters *cnt)
         if (P->count_flag[i] == 1) {
             i += 1;
         } else {
-            if (P->count_flag[i] < 0) cnt->nptl_escaped += 1;
+            if (P->count_flag[i] < 0) {
+                cnt->nptl_escaped += 1;
+                escaped_add(P, i);
+            }
             swap_particles(P, n - nremoved - 1, i);
             nremoved += 1;
         }
@@ -991,4 +1027,36 @@ void orc_quick_check(const orc_particles *P, int64_t n, double out[4])
         s = s + P->dt[i];
     }
     out[0] = w; out[1] = mn; out[2] = mx; out[3] = s;
+}
+
+/* One local distribution of calc_particle_distributions
+ * (diagnostics.f90:782-878) on one rank, uniform grid: flocal(imu, ip, ix,
+ * iy, iz), imu fastest; 0 < ip < npbins as in the reference. */
+void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmin, double pmax,
+                                 int npbins, int nmu, int rx, int ry, int rz,
+                                 const orc_particles *P, int64_t n, uint64_t *counts,
+                                 uint64_t *whi, uint64_t *wlo, double *flocal)
+{
+    const int nz = ndim == 3 ? cfg->nz : 1;
+    const int nrx = (cfg->nx + rx - 1) / rx, nry = (cfg->ny + ry - 1) / ry, nrz = (nz + rz - 1) / rz;
+    const double dxd = cfg->lx / nrx, dyd = cfg->ly / nry, dzd = cfg->lz / nrz;
+    const double pmin_log = log10(pmin);
+    const double dp_log = (log10(pmax) - pmin_log) / npbins;
+    const double dmu = 2.0 / nmu;
+    const size_t nb = (size_t)nmu * npbins * nrx * nry * nrz;
+    for (size_t b = 0; b < nb; ++b) { counts[b] = 0; whi[b] = 0; wlo[b] = 0; }
+    for (int64_t i = 0; i < n; ++i) {
+        const int ix = (int)floor((P->x[i] - cfg->xmin) / dxd) + 1;
+        const int iy = (int)floor((P->y[i] - cfg->ymin) / dyd) + 1;
+        const int iz = (int)floor((P->z[i] - cfg->zmin) / dzd) + 1;
+        const int ip = (int)floor((log10(P->p[i]) - pmin_log) / dp_log) + 1;
+        const int imu = (int)floor((P->mu[i] + 1.0) / dmu) + 1;
+        if (ix < 1 || ix > nrx || iy < 1 || iy > nry || iz < 1 || iz > nrz) continue;
+        if (!(ip > 0 && ip < npbins) || imu < 1 || imu > nmu) continue;
+        const size_t e = (size_t)(imu - 1) + (size_t)nmu * ((size_t)(ip - 1) + (size_t)npbins *
+                         ((size_t)(ix - 1) + (size_t)nrx * ((size_t)(iy - 1) + (size_t)nry * (iz - 1))));
+        counts[e] += 1;
+        orc_fixed_add(&whi[e], &wlo[e], P->weight[i]);
+    }
+    for (size_t b = 0; b < nb; ++b) flocal[b] = orc_fixed_to_double(whi[b], wlo[b]);
 }

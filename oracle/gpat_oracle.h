@@ -115,6 +115,12 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
                         double particle_v0, double t_frame, double power_index,
                         orc_counters *cnt);
 void orc_quick_check(const orc_particles *ptl, int64_t n, double out[4]);
+void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *counts,
+                               uint64_t *whi, uint64_t *wlo);
+void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmin, double pmax,
+                                 int npbins, int nmu, int rx, int ry, int rz,
+                                 const orc_particles *ptl, int64_t n, uint64_t *counts,
+                                 uint64_t *whi, uint64_t *wlo, double *flocal);
 
 #ifdef __cplusplus
 }

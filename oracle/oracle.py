@@ -115,6 +115,11 @@ def load() -> C.CDLL:
         lib.orc_inject_at_x.argtypes = [P(OrcParams), P(OrcMhdConfig), P(OrcParticles), i64, i64,
                                         i64, d, d, C.c_int, d, d, d, P(OrcCounters)]
         lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
+        lib.orc_set_escaped_histogram.argtypes = [C.c_int, d, d, P(u64), P(u64), P(u64)]
+        lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, d, d, C.c_int,
+                                                    C.c_int, C.c_int, C.c_int, C.c_int,
+                                                    P(OrcParticles), i64, P(u64), P(u64), P(u64),
+                                                    P(d)]
         _lib = lib
     return _lib
 
@@ -239,3 +244,38 @@ def quick_check(parts: Particles):
     out = (d * 4)()
     lib.orc_quick_check(C.byref(parts.c), parts.n, out)
     return list(out)
+
+
+class EscapedHistogram:
+    """Attaches an escaped-particle distribution to the oracle's
+    remove_particles (npp bins x 6 faces); detach() turns it off."""
+
+    def __init__(self, npp: int, pmin: float, pmax: float):
+        self.npp = npp
+        self.counts = np.zeros(6 * npp, np.uint64)
+        self.whi = np.zeros(6 * npp, np.uint64)
+        self.wlo = np.zeros(6 * npp, np.uint64)
+        load().orc_set_escaped_histogram(npp, pmin, pmax, self.counts.ctypes.data_as(P(u64)),
+                                         self.whi.ctypes.data_as(P(u64)),
+                                         self.wlo.ctypes.data_as(P(u64)))
+
+    def detach(self):
+        load().orc_set_escaped_histogram(0, 1.0, 2.0, None, None, None)
+
+    def weights(self) -> np.ndarray:
+        return np.array([fixed_to_double(int(h), int(l)) for h, l in zip(self.whi, self.wlo)])
+
+
+def local_distribution(cfg: OrcMhdConfig, ndim: int, parts: Particles, pmin: float, pmax: float,
+                       npbins: int, nmu: int = 1, rx: int = 1, ry: int = 1, rz: int = 1):
+    nz = cfg.nz if ndim == 3 else 1
+    nb = nmu * npbins * ((cfg.nx + rx - 1) // rx) * ((cfg.ny + ry - 1) // ry) * ((nz + rz - 1) // rz)
+    counts = np.zeros(nb, np.uint64)
+    whi = np.zeros(nb, np.uint64)
+    wlo = np.zeros(nb, np.uint64)
+    f = np.zeros(nb, np.float64)
+    load().orc_calc_local_distribution(C.byref(cfg), ndim, pmin, pmax, npbins, nmu, rx, ry, rz,
+                                       C.byref(parts.c), parts.n, counts.ctypes.data_as(P(u64)),
+                                       whi.ctypes.data_as(P(u64)), wlo.ctypes.data_as(P(u64)),
+                                       f.ctypes.data_as(P(d)))
+    return f, counts

@@ -43,6 +43,7 @@ struct gpat_handle {
     DevCounters *dcnt = nullptr;
     DevCounters hcnt{};
     unsigned long long *dbins = nullptr;
+    unsigned long long *desc = nullptr;   // escaped distribution, 6 faces x npp x 3
     // module state kept on the host
     std::vector<double> tstamps;
     int64_t tag_max = 0;
@@ -235,10 +236,21 @@ CellGrid cell_grid(const gpat_handle_t *h) {
 
 // Bins the current particles by cell into the other buffer (split-precision
 // path), dropping particles that are not in the box.
+EscHist escaped_hist(const gpat_handle_t *h) {
+    EscHist e;
+    e.bins = h->desc;
+    e.npp = h->prm.npp_global;
+    e.pmin = h->prm.pmin;
+    e.pmax = h->prm.pmax;
+    e.pmin_log = std::log10(h->prm.pmin);
+    e.dp_log = (std::log10(h->prm.pmax) - e.pmin_log) / h->prm.npp_global;
+    return e;
+}
+
 int bin_particles(gpat_handle_t *h) {
     const int nxt = 1 - h->cur;
     CK(launch_cell_sort(h->P[h->cur], h->P[nxt], h->n, cell_grid(h), h->sort_scratch, h->dcnt,
-                        h->stream));
+                        escaped_hist(h), h->stream));
     int rc = pull_counters(h);
     if (rc) return rc;
     h->cur = nxt;
@@ -390,6 +402,9 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     cudaMemsetAsync(h->dcnt, 0, sizeof(DevCounters), h->stream);
     if (cudaMalloc(&h->dbins, sizeof(unsigned long long) * 3 * (size_t)p.npp_global) != cudaSuccess)
         return bail(GPAT_ERR_OOM);
+    const size_t esc_bytes = sizeof(unsigned long long) * 3 * 6 * (size_t)p.npp_global;
+    if (cudaMalloc(&h->desc, esc_bytes) != cudaSuccess) return bail(GPAT_ERR_OOM);
+    cudaMemsetAsync(h->desc, 0, esc_bytes, h->stream);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(GPAT_ERR_CUDA);
     *out = h;
     return GPAT_OK;
@@ -409,6 +424,7 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->dcnt) cudaFree(h->dcnt);
     if (h->dbins) cudaFree(h->dbins);
+    if (h->desc) cudaFree(h->desc);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -619,9 +635,9 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
                         int dump_escaped_dist) {
     (void)kperp_kpara;
     if (!h) return GPAT_ERR_ARG;
-    if (focused_transport || nlgc || dump_escaped_dist)
-        return fail(h, GPAT_ERR_UNSUPPORTED,
-                    "focused transport, NLGC and escaped-particle dumps are not in this engine");
+    (void)dump_escaped_dist;   // the escaped distribution is always accumulated
+    if (focused_transport || nlgc)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport and NLGC are not in this engine");
     MoverArgs a;
     int rc = mover_args(h, mhd_tframe, nsteps_interval, num_fine_steps, a);
     if (rc) return rc;
@@ -671,7 +687,8 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         launches = 1;
         // remove_particles (particle_module.f90:5365-5403), order-preserving.
         const int nxt = 1 - h->cur;
-        CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt, h->stream));
+        CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt,
+                                   escaped_hist(h), h->stream));
         rc = pull_counters(h);
         if (rc) return rc;
         h->cur = nxt;
@@ -719,6 +736,90 @@ int gpat_calc_particle_distributions(gpat_handle_t *h, double *fglobal, uint64_t
         if (counts) counts[i] = b[3 * i];
         if (fglobal) fglobal[i] = fixed_to_double(b[3 * i + 1], b[3 * i + 2]);
     }
+    return GPAT_OK;
+}
+
+static int local_args(gpat_handle_t *h, const gpat_local_dist_t *sp, LocalDistArgs &a) {
+    if (!sp || sp->npbins < 1 || sp->nmu < 1 || sp->rx < 1 || sp->ry < 1 || sp->rz < 1 ||
+        !(sp->pmin > 0.0) || !(sp->pmax > sp->pmin))
+        return fail(h, GPAT_ERR_ARG, "bad local distribution parameters");
+    const gpat_mhd_config_t &c = h->cfg;
+    const int nz = h->prm.ndim == 3 ? c.nz : 1;
+    // init_local_particle_distributions (diagnostics.f90:262-270) on one rank
+    a.nrx = (c.nx + sp->rx - 1) / sp->rx;
+    a.nry = (c.ny + sp->ry - 1) / sp->ry;
+    a.nrz = (nz + sp->rz - 1) / sp->rz;
+    a.dxd = c.lx / a.nrx;
+    a.dyd = c.ly / a.nry;
+    a.dzd = c.lz / a.nrz;
+    a.xmin = c.xmin; a.ymin = c.ymin; a.zmin = c.zmin;
+    a.pmin_log = std::log10(sp->pmin);
+    a.dp_log = (std::log10(sp->pmax) - a.pmin_log) / sp->npbins;
+    a.dmu = 2.0 / sp->nmu;
+    a.nmu = sp->nmu;
+    a.npb = sp->npbins;
+    return GPAT_OK;
+}
+
+int gpat_local_distribution_dims(gpat_handle_t *h, const gpat_local_dist_t *spec, int32_t dims[5]) {
+    if (!h || !dims) return GPAT_ERR_ARG;
+    LocalDistArgs a;
+    const int rc = local_args(h, spec, a);
+    if (rc) return rc;
+    dims[0] = a.nmu; dims[1] = a.npb; dims[2] = a.nrx; dims[3] = a.nry; dims[4] = a.nrz;
+    return GPAT_OK;
+}
+
+int gpat_calc_local_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec, double *flocal,
+                                 uint64_t *counts) {
+    if (!h) return GPAT_ERR_ARG;
+    LocalDistArgs a;
+    int rc = local_args(h, spec, a);
+    if (rc) return rc;
+    const size_t nbins = (size_t)a.nmu * a.npb * a.nrx * a.nry * a.nrz;
+    if (nbins > ((size_t)1 << 31)) return fail(h, GPAT_ERR_ARG, "local distribution too large");
+    CK(cudaSetDevice(h->device));
+    unsigned long long *bins = nullptr;
+    CK(cudaMallocAsync((void **)&bins, sizeof(unsigned long long) * 3 * nbins, h->stream));
+    cudaError_t e = launch_local_dist(h->P[h->cur], h->n, a, bins, nbins, h->stream);
+    std::vector<unsigned long long> b(3 * nbins);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.data(), bins, sizeof(unsigned long long) * b.size(),
+                            cudaMemcpyDeviceToHost, h->stream);
+    cudaFreeAsync(bins, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(h, GPAT_ERR_CUDA, cudaGetErrorString(e));
+    for (size_t i = 0; i < nbins; ++i) {
+        if (counts) counts[i] = b[3 * i];
+        if (flocal) flocal[i] = fixed_to_double(b[3 * i + 1], b[3 * i + 2]);
+    }
+    return GPAT_OK;
+}
+
+int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t *counts) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    const size_t npp = (size_t)h->prm.npp_global;
+    const size_t ncol = 2 * (size_t)h->prm.ndim;
+    std::vector<unsigned long long> b(3 * 6 * npp);
+    CK(cudaMemcpyAsync(b.data(), h->desc, sizeof(unsigned long long) * b.size(),
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t f = 0; f < ncol; ++f)
+        for (size_t ip = 0; ip < npp; ++ip) {
+            const size_t k = f * npp + ip;
+            if (counts) counts[k] = b[3 * k];
+            if (fescaped) fescaped[k] = fixed_to_double(b[3 * k + 1], b[3 * k + 2]);
+        }
+    return GPAT_OK;
+}
+
+int gpat_reset_escaped_particles(gpat_handle_t *h) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemsetAsync(h->desc, 0, sizeof(unsigned long long) * 3 * 6 * (size_t)h->prm.npp_global,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
     return GPAT_OK;
 }
 

@@ -113,11 +113,30 @@ struct InjectArgs {
 // Status bits (kStatusStepLimit on a runaway rejection loop) go to *status.
 cudaError_t launch_inject(const InjectArgs &a, unsigned int *status, cudaStream_t s);
 
+// Distribution of removed escaped particles by boundary face
+// (calc_escaped_distributions): bins[(face * npp + ip) * 3 + {0: count,
+// 1: weight hi, 2: weight lo}], face = |count_flag| - 1.
+struct EscHist {
+    unsigned long long *bins;
+    int npp;
+    double pmin, pmax, pmin_log, dp_log;
+};
+
 // Stable compaction of particles with count_flag == INBOX from src to dst.
 // scratch must hold compaction_scratch_bytes(n) bytes.
 size_t compaction_scratch_bytes(int64_t n);
 cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles &dst, int64_t n,
-                                    void *scratch, DevCounters *cnt, cudaStream_t s);
+                                    void *scratch, DevCounters *cnt, const EscHist &esc,
+                                    cudaStream_t s);
+
+// One local distribution (flocal of calc_particle_distributions).
+struct LocalDistArgs {
+    double xmin, ymin, zmin, dxd, dyd, dzd, pmin_log, dp_log, dmu;
+    int nmu, npb, nrx, nry, nrz;
+};
+// bins: (count, whi, wlo) per flocal element, zeroed here.
+cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
+                              unsigned long long *bins, size_t nbins, cudaStream_t s);
 // Splitting: children appended after n in parent order, at most cap - n.
 cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,
                                    double split_ratio, double pmin_split, double p0,
@@ -132,7 +151,8 @@ struct CellGrid {
 // rest (remove_particles) and counts escapes.  cnt->nkept gets the new count.
 size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins);
 cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, int64_t n,
-                             const CellGrid &g, void *scratch, DevCounters *cnt, cudaStream_t s);
+                             const CellGrid &g, void *scratch, DevCounters *cnt,
+                             const EscHist &esc, cudaStream_t s);
 // Global f(p) histogram into (count, whi, wlo) triples per bin (zeroed here).
 cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double pmin,
                              double pmax, unsigned long long *bins, cudaStream_t s);

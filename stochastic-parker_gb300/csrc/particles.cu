@@ -115,6 +115,21 @@ struct SplitRule {
     double ratio, pmin_split, p0, pmax;
 };
 
+// Adds a removed escaped particle to the escaped distribution
+// (calc_escaped_distributions, diagnostics.f90:950-957): global p binning,
+// column |count_flag|.
+__device__ __forceinline__ void escaped_add(const EscHist &e, const DevParticles &P, int64_t i,
+                                            int flag) {
+    if (e.bins == nullptr || flag >= 0 || flag < -6) return;
+    const double p = P.p[i], mu = P.mu[i];
+    if (!(p > e.pmin && p <= e.pmax && mu >= -1.0 && mu <= 1.0)) return;
+    const int ip = (int)floor((log10(p) - e.pmin_log) / e.dp_log);
+    if (ip < 0 || ip >= e.npp) return;
+    unsigned long long *b = e.bins + 3 * ((size_t)(-flag - 1) * e.npp + ip);
+    atomicAdd(b, 1ull);
+    atomic_add_fixed(b + 1, b + 2, P.weight[i]);
+}
+
 // mode 0: keep count_flag == INBOX; mode 1: split candidates.
 template <int MODE>
 __device__ __forceinline__ bool select(const DevParticles &P, int64_t i, const SplitRule &r) {
@@ -126,7 +141,7 @@ __device__ __forceinline__ bool select(const DevParticles &P, int64_t i, const S
 template <int MODE>
 __global__ void __launch_bounds__(kScanThreads) tile_count_kernel(const DevParticles P, int64_t n,
                                                                   SplitRule r, long long *tile_counts,
-                                                                  DevCounters *cnt) {
+                                                                  DevCounters *cnt, const EscHist esc_hist) {
     __shared__ int warp_tot[kScanThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kTile;
     int mine = 0, esc = 0;
@@ -135,7 +150,13 @@ __global__ void __launch_bounds__(kScanThreads) tile_count_kernel(const DevParti
         const int64_t i = base + k * kScanThreads + threadIdx.x;
         if (i < n) {
             mine += select<MODE>(P, i, r) ? 1 : 0;
-            if (MODE == 0 && P.count_flag[i] < 0) esc += 1;
+            if (MODE == 0) {
+                const int f = P.count_flag[i];
+                if (f < 0) {
+                    esc += 1;
+                    escaped_add(esc_hist, P, i, f);
+                }
+            }
         }
     }
 #pragma unroll
@@ -361,7 +382,8 @@ constexpr int kBinTile = kBinScanThreads * kBinScanItems;
 
 __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int64_t n,
                                                        const CellGrid g, int32_t *keys,
-                                                       unsigned int *counts, DevCounters *cnt) {
+                                                       unsigned int *counts, DevCounters *cnt,
+                                                       const EscHist esc_hist) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int esc = 0;
     if (i < n) {
@@ -384,6 +406,7 @@ __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int
             atomicAdd(&counts[key], 1u);
         } else if (flag < 0) {
             esc = 1;
+            escaped_add(esc_hist, P, i, flag);
         }
         keys[i] = key;
     }
@@ -473,7 +496,8 @@ size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins) {
 }
 
 cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, int64_t n,
-                             const CellGrid &g, void *scratch, DevCounters *cnt, cudaStream_t s) {
+                             const CellGrid &g, void *scratch, DevCounters *cnt,
+                             const EscHist &esc, cudaStream_t s) {
     const int64_t nbins = (int64_t)g.nxg * g.nyg * g.nzg;
     const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
     char *q = static_cast<char *>(scratch);
@@ -485,7 +509,7 @@ cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, i
     if (e != cudaSuccess) return e;
     if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    cell_key_kernel<<<blocks, 256, 0, s>>>(src, n, g, keys, counts, cnt);
+    cell_key_kernel<<<blocks, 256, 0, s>>>(src, n, g, keys, counts, cnt, esc);
     bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
     tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
     bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
@@ -499,13 +523,14 @@ size_t compaction_scratch_bytes(int64_t n) {
 }
 
 cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles &dst, int64_t n,
-                                    void *scratch, DevCounters *cnt, cudaStream_t s) {
+                                    void *scratch, DevCounters *cnt, const EscHist &esc,
+                                    cudaStream_t s) {
     if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
     const int64_t ntiles = (n + kTile - 1) / kTile;
     long long *counts = static_cast<long long *>(scratch);
     long long *offsets = counts + ntiles;
     const SplitRule r{0, 0, 0, 0};
-    tile_count_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt);
+    tile_count_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt, esc);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
     tile_scatter_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, n, r, offsets, cnt);
     return cudaGetLastError();
@@ -519,7 +544,8 @@ cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap
     long long *counts = static_cast<long long *>(scratch);
     long long *offsets = counts + ntiles;
     const SplitRule r{split_ratio, pmin_split, p0, pmax};
-    tile_count_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, n, r, counts, cnt);
+    const EscHist none{nullptr, 0, 0.0, 0.0, 0.0, 0.0};
+    tile_count_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, n, r, counts, cnt, none);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
     tile_scatter_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, P, n, cap, r, offsets, cnt);
     return cudaGetLastError();
@@ -536,6 +562,39 @@ cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double p
     const size_t shmem = sizeof(unsigned long long) * 3 * (size_t)npp;
     histogram_kernel<<<(unsigned)blocks, 256, shmem, s>>>(P, n, npp, pmin, pmax, pmin_log, dp_log,
                                                           bins);
+    return cudaGetLastError();
+}
+
+// Local distributions (calc_particle_distributions, diagnostics.f90:782-878):
+// one (count, weight hi, lo) triple per flocal(imu, ip, ix, iy, iz) element.
+__global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, int64_t n,
+                                                         const LocalDistArgs a,
+                                                         unsigned long long *bins) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p = P.p[i], mu = P.mu[i];
+    const int ix = (int)floor((P.x[i] - a.xmin) / a.dxd) + 1;
+    const int iy = (int)floor((P.y[i] - a.ymin) / a.dyd) + 1;
+    const int iz = (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
+    const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
+    const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
+    if (ix < 1 || ix > a.nrx || iy < 1 || iy > a.nry || iz < 1 || iz > a.nrz) return;
+    if (!(ip > 0 && ip < a.npb) || imu < 1 || imu > a.nmu) return;
+    const size_t e = (size_t)(imu - 1) +
+                     (size_t)a.nmu * ((size_t)(ip - 1) +
+                                      (size_t)a.npb * ((size_t)(ix - 1) +
+                                                       (size_t)a.nrx * ((size_t)(iy - 1) +
+                                                                        (size_t)a.nry * (iz - 1))));
+    unsigned long long *b = bins + 3 * e;
+    atomicAdd(b, 1ull);
+    atomic_add_fixed(b + 1, b + 2, P.weight[i]);
+}
+
+cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
+                              unsigned long long *bins, size_t nbins, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, s);
+    if (e != cudaSuccess || n <= 0) return e;
+    local_dist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, bins);
     return cudaGetLastError();
 }
 

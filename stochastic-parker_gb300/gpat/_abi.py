@@ -80,6 +80,12 @@ class Particles(C.Structure):
     _fields_ = [(n, P(_CT[t])) for n, t in PARTICLE_FIELDS]
 
 
+class LocalDist(C.Structure):
+    """gpat_local_dist_t: one set of local distribution parameters."""
+    _fields_ = [("pmin", d), ("pmax", d), ("npbins", i32), ("nmu", i32), ("rx", i32),
+                ("ry", i32), ("rz", i32), ("reserved", i32)]
+
+
 class Counters(C.Structure):
     _fields_ = [
         ("nptl_current", i64), ("nptl_split", i64), ("nptl_escaped", i64), ("tag_max", i64),
@@ -119,6 +125,10 @@ SIGNATURES = {
     "gpat_split_particle_noalloc": (C.c_int, [P(Particles), i64, i64, d, d, d, d, C.c_void_p,
                                               P(i64), P(i64)]),
     "gpat_calc_particle_distributions": (C.c_int, [Handle, P(d), P(u64)]),
+    "gpat_local_distribution_dims": (C.c_int, [Handle, P(LocalDist), P(i32)]),
+    "gpat_calc_local_distribution": (C.c_int, [Handle, P(LocalDist), P(d), P(u64)]),
+    "gpat_calc_escaped_distributions": (C.c_int, [Handle, P(d), P(u64)]),
+    "gpat_reset_escaped_particles": (C.c_int, [Handle]),
     "gpat_pbins_edges": (C.c_int, [Handle, P(d)]),
     "gpat_quick_check": (C.c_int, [Handle, P(d)]),
     "gpat_get_counters": (C.c_int, [Handle, P(Counters)]),

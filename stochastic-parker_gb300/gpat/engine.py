@@ -278,6 +278,33 @@ class Engine:
             c.ctypes.data_as(C.POINTER(C.c_uint64))))
         return f, c
 
+    def local_distribution(self, pmin, pmax, npbins, nmu=1, rx=1, ry=1, rz=1):
+        """One local distribution: (flocal, counts) shaped (nrz, nry, nrx,
+        npbins, nmu), i.e. Fortran flocal(nmu, npbins, nrx, nry, nrz)."""
+        spec = _abi.LocalDist(pmin, pmax, npbins, nmu, rx, ry, rz, 0)
+        dims = (C.c_int32 * 5)()
+        self._check(self.lib.gpat_local_distribution_dims(self.h, C.byref(spec), dims))
+        shape = tuple(reversed(list(dims)))
+        f = np.zeros(shape, np.float64)
+        c = np.zeros(shape, np.uint64)
+        self._check(self.lib.gpat_calc_local_distribution(
+            self.h, C.byref(spec), f.ctypes.data_as(C.POINTER(C.c_double)),
+            c.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return f, c
+
+    def calc_escaped_distributions(self):
+        """(fescaped, counts) shaped (2 * ndim, npp_global)."""
+        npp = self.params.npp_global
+        f = np.zeros((2 * self.ndim, npp), np.float64)
+        c = np.zeros((2 * self.ndim, npp), np.uint64)
+        self._check(self.lib.gpat_calc_escaped_distributions(
+            self.h, f.ctypes.data_as(C.POINTER(C.c_double)),
+            c.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return f, c
+
+    def reset_escaped_particles(self):
+        self._check(self.lib.gpat_reset_escaped_particles(self.h))
+
     def pbins_edges(self) -> np.ndarray:
         e = np.zeros(self.params.npp_global + 1, dtype=np.float64)
         self._check(self.lib.gpat_pbins_edges(self.h, e.ctypes.data_as(C.POINTER(C.c_double))))
