@@ -90,6 +90,10 @@ typedef struct gpat_params {
      * default of 128; negative: bin once per call).  Results are the same
      * for any value; it only changes memory locality. */
     int32_t bin_interval;
+    int32_t reserved;
+    /* Focused transport: pitch-angle diffusion coefficient at p0 (duu_init of
+     * the reference CLI, stochastic-mhd.f90:935-937, default 10). */
+    double duu0;
 } gpat_params_t;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays.  rng_ctr
@@ -181,8 +185,10 @@ int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity
 
 /* particle_mover (particle_module.f90:1846-1974) on one rank:
  * mover cycle (:1481-1833), remove_particles, boundary pass on the exact
- * box, remove_particles.  focused_transport and nlgc must be 0.
- * mhd_tframe indexes tstamps (t0 = tstamps(mhd_tframe)). */
+ * box, remove_particles.  focused_transport selects push_particle_*_ft
+ * (mu and v become state; gpat_params_t.duu0 sets D_mumu), nlgc selects
+ * calc_spatial_diffusion_coefficients_nlgc with kperp_kpara; both need
+ * GPAT_PREC_FP64.  mhd_tframe indexes tstamps (t0 = tstamps(mhd_tframe)). */
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc,
                         double kperp_kpara, int nsteps_interval, int mhd_tframe,
                         int num_fine_steps, int dump_escaped_dist);

@@ -210,17 +210,25 @@ void orc_interp_fields(const float *f1, const float *f2, int time_interp, int nd
 }
 
 /* ------------------------------------------------------------------------ */
-/* calc_spatial_diffusion_coefficients: particle_module.f90:2208-2450 for   */
-/* Parker transport without delta-B or correlation-length inputs.  kappa    */
-/* follows kappa_type (:93-104): knorm_para knorm_perp kpara kperp skpara   */
-/* skperp skpara_perp kxx kyy kzz kxy kxz kyz dkxx_dx dkyy_dy dkzz_dz       */
-/* dkxy_dx dkxy_dy dkxz_dx dkxz_dz dkyz_dy dkyz_dz.                         */
+/* calc_spatial_diffusion_coefficients (particle_module.f90:2208-2450) and   */
+/* calc_spatial_diffusion_coefficients_nlgc (:2464-2771) without delta-B or */
+/* correlation-length inputs.  kappa follows kappa_type (:93-104):          */
+/* knorm_para knorm_perp kpara kperp skpara skperp skpara_perp kxx kyy kzz  */
+/* kxy kxz kyz dkxx_dx dkyy_dy dkzz_dz dkxy_dx dkxy_dy dkxz_dx dkxz_dz      */
+/* dkyz_dy dkyz_dz.  Focused transport keeps only the perpendicular part    */
+/* (kpp = -kperp).                                                          */
 /* ------------------------------------------------------------------------ */
 enum { K_KNORM_PARA, K_KNORM_PERP, K_KPARA, K_KPERP, K_SKPARA, K_SKPERP, K_SKPARA_PERP,
        K_KXX, K_KYY, K_KZZ, K_KXY, K_KXZ, K_KYZ, K_DKXX_DX, K_DKYY_DY, K_DKZZ_DZ,
        K_DKXY_DX, K_DKXY_DY, K_DKXZ_DX, K_DKXZ_DZ, K_DKYZ_DY, K_DKYZ_DZ };
 
-void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p,
+/* Both variants write the gradient terms as
+ *   dkii_di = T_i + A_i * bi^2 / B^2 + 2 kpp bi (dbi_di B - bi dB_di) / B^3
+ *   dkij_dk = A_k * bi bj / B^2 + kpp ((dbi_dk bj + bi dbj_dk) / B^2 - 2 bi bj dB_dk / B^3)
+ * with T_i = kperp dk_i, A_i = kpp dk_i for the fixed ratio (:2351-2449)
+ * and T_i = kperp dkperp_i, A_i = kpara dkpara_i - kperp dkperp_i for NLGC
+ * (:2583-2770); the operation order of each is the reference's. */
+void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, double mu,
                                              const double f[32], double kap[22])
 {
     const double bx = f[4], by = f[5], bz = f[6];
@@ -228,76 +236,92 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p,
     double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
     const double ib2 = ib1 * ib1;
     const double ib3 = ib1 * ib2;
-    double knorm_para = 1.0, knorm;
-    if (pr->mag_dependency == 1) knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
-    if (pr->momentum_dependency == 1) knorm = knorm_para * pow(p / pr->p0, pr->pindex);
-    else knorm = knorm_para;
-    const double kpara = pr->kpara0 * knorm;
-    const double kperp = kpara * pr->kret;
+    const int d3 = (pr->ndim == 3);
+    double kpara, kperp;
+    double knorm_para = 1.0, knorm_perp = 1.0;
+    if (!pr->nlgc) {
+        double knorm;
+        if (pr->mag_dependency == 1) knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
+        if (pr->momentum_dependency == 1) knorm = knorm_para * pow(p / pr->p0, pr->pindex);
+        else knorm = knorm_para;
+        knorm_perp = knorm_para;
+        kpara = pr->kpara0 * knorm;
+        kperp = kpara * pr->kret;
+    } else {
+        double kn_para, kn_perp;
+        if (pr->mag_dependency == 1) {
+            knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
+            knorm_perp = knorm_perp * pow(b, (pr->gamma_turb - 2.0) / 3.0);
+        }
+        if (pr->momentum_dependency == 1) {
+            kn_para = knorm_para * pow(p / pr->p0, pr->pindex);
+            kn_perp = knorm_perp * pow(p / pr->p0, (5.0 - pr->gamma_turb) / 3.0);
+        } else {
+            kn_para = knorm_para;
+            kn_perp = knorm_perp;
+        }
+        kpara = pr->kpara0 * kn_para;
+        kperp = pr->kpara0 * pr->kperp_kpara * kn_perp * (mu * mu);
+    }
     kap[K_KNORM_PARA] = knorm_para;
-    kap[K_KNORM_PERP] = knorm_para;
+    kap[K_KNORM_PERP] = knorm_perp;
     kap[K_KPARA] = kpara;
     kap[K_KPERP] = kperp;
     kap[K_SKPARA] = sqrt(2.0 * kpara);
     kap[K_SKPERP] = sqrt(2.0 * kperp);
     kap[K_SKPARA_PERP] = sqrt(2.0 * (kpara - kperp));
-    const double kpp = kpara - kperp;
-    if (pr->ndim == 2) {
-        const double dbx_dx = f[20], dbx_dy = f[21], dby_dx = f[23], dby_dy = f[24];
-        const double db_dx = f[29], db_dy = f[30];
-        double dkdx = 0.0, dkdy = 0.0;
-        if (pr->mag_dependency == 1) {
-            dkdx = db_dx * ib1 * (pr->gamma_turb - 2.0);
-            dkdy = db_dy * ib1 * (pr->gamma_turb - 2.0);
+    const double kpp = pr->focused_transport ? -kperp : kpara - kperp;
+
+    const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
+    const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
+    const double dbz_dx = f[26], dbz_dy = f[27], dbz_dz = f[28];
+    const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
+    double T[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0};
+    const double db[3] = {db_dx, db_dy, db_dz};
+    const double g2 = pr->gamma_turb - 2.0;
+    for (int k = 0; k < 2 + d3; ++k) {
+        if (!pr->nlgc) {
+            double dk = 0.0;
+            if (pr->mag_dependency == 1)
+                /* the fixed-ratio 3D branch has no 1/B factor (:2406-2408) */
+                dk = d3 ? db[k] * g2 : db[k] * ib1 * g2;
+            T[k] = kperp * dk;
+            A[k] = kpp * dk;
+        } else {
+            double dkpara = 0.0, dkperp = 0.0;
+            if (pr->mag_dependency == 1) {
+                dkpara = db[k] * ib1 * g2;
+                dkperp = db[k] * ib1 * g2 / 3.0;
+            }
+            T[k] = kperp * dkperp;
+            A[k] = kpara * dkpara - kperp * dkperp;
         }
-        kap[K_DKXX_DX] = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2 +
-                         2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
-        kap[K_DKYY_DY] = kperp * dkdy + kpp * dkdy * (by * by) * ib2 +
-                         2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3;
-        kap[K_DKXY_DX] = kpp * dkdx * bx * by * ib2 +
-                         kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0 * bx * by * db_dx * ib3);
-        kap[K_DKXY_DY] = kpp * dkdy * bx * by * ib2 +
-                         kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0 * bx * by * db_dy * ib3);
-        kap[K_KXX] = kperp + kpp * bx * bx * ib2;
-        kap[K_KYY] = kperp + kpp * by * by * ib2;
-        kap[K_KXY] = kpp * bx * by * ib2;
+    }
+    kap[K_DKXX_DX] = T[0] + A[0] * (bx * bx) * ib2 + 2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
+    kap[K_DKYY_DY] = T[1] + A[1] * (by * by) * ib2 + 2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3;
+    kap[K_DKXY_DX] = A[0] * bx * by * ib2 +
+                     kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0 * bx * by * db_dx * ib3);
+    kap[K_DKXY_DY] = A[1] * bx * by * ib2 +
+                     kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0 * bx * by * db_dy * ib3);
+    kap[K_KXX] = kperp + kpp * bx * bx * ib2;
+    kap[K_KYY] = kperp + kpp * by * by * ib2;
+    kap[K_KXY] = kpp * bx * by * ib2;
+    if (!d3) {
         kap[K_KZZ] = 0.0; kap[K_KXZ] = 0.0; kap[K_KYZ] = 0.0;
         kap[K_DKZZ_DZ] = 0.0; kap[K_DKXZ_DX] = 0.0; kap[K_DKXZ_DZ] = 0.0;
         kap[K_DKYZ_DY] = 0.0; kap[K_DKYZ_DZ] = 0.0;
     } else {
-        const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
-        const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
-        const double dbz_dx = f[26], dbz_dy = f[27], dbz_dz = f[28];
-        const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
-        double dkdx = 0.0, dkdy = 0.0, dkdz = 0.0;
-        if (pr->mag_dependency == 1) {
-            /* 3D branch has no 1/B factor here (reference :2406-2408). */
-            dkdx = db_dx * (pr->gamma_turb - 2.0);
-            dkdy = db_dy * (pr->gamma_turb - 2.0);
-            dkdz = db_dz * (pr->gamma_turb - 2.0);
-        }
-        kap[K_DKXX_DX] = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2 +
-                         2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3;
-        kap[K_DKYY_DY] = kperp * dkdy + kpp * dkdy * (by * by) * ib2 +
-                         2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3;
-        kap[K_DKZZ_DZ] = kperp * dkdz + kpp * dkdz * (bz * bz) * ib2 +
+        kap[K_DKZZ_DZ] = T[2] + A[2] * (bz * bz) * ib2 +
                          2.0 * kpp * bz * (dbz_dz * b - bz * db_dz) * ib3;
-        kap[K_DKXY_DX] = kpp * dkdx * bx * by * ib2 +
-                         kpp * ((dbx_dx * by + bx * dby_dx) * ib2 - 2.0 * bx * by * db_dx * ib3);
-        kap[K_DKXY_DY] = kpp * dkdy * bx * by * ib2 +
-                         kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - 2.0 * bx * by * db_dy * ib3);
-        kap[K_DKXZ_DX] = kpp * dkdx * bx * bz * ib2 +
+        kap[K_DKXZ_DX] = A[0] * bx * bz * ib2 +
                          kpp * ((dbx_dx * bz + bx * dbz_dx) * ib2 - 2.0 * bx * bz * db_dx * ib3);
-        kap[K_DKXZ_DZ] = kpp * dkdz * bx * bz * ib2 +
+        kap[K_DKXZ_DZ] = A[2] * bx * bz * ib2 +
                          kpp * ((dbx_dz * bz + bx * dbz_dz) * ib2 - 2.0 * bx * bz * db_dz * ib3);
-        kap[K_DKYZ_DY] = kpp * dkdy * by * bz * ib2 +
+        kap[K_DKYZ_DY] = A[1] * by * bz * ib2 +
                          kpp * ((dby_dy * bz + by * dbz_dy) * ib2 - 2.0 * by * bz * db_dy * ib3);
-        kap[K_DKYZ_DZ] = kpp * dkdz * by * bz * ib2 +
+        kap[K_DKYZ_DZ] = A[2] * by * bz * ib2 +
                          kpp * ((dby_dz * bz + by * dbz_dz) * ib2 - 2.0 * by * bz * db_dz * ib3);
-        kap[K_KXX] = kperp + kpp * bx * bx * ib2;
-        kap[K_KYY] = kperp + kpp * by * by * ib2;
         kap[K_KZZ] = kperp + kpp * bz * bz * ib2;
-        kap[K_KXY] = kpp * bx * by * ib2;
         kap[K_KXZ] = kpp * bx * bz * ib2;
         kap[K_KYZ] = kpp * by * bz * ib2;
     }
@@ -319,7 +343,7 @@ typedef struct mover_ctx {
 } mover_ctx;
 
 typedef struct ptl_state {
-    double x, y, z, p, t, dt, weight;
+    double x, y, z, p, v, mu, t, dt, weight;
     int flag;
     int32_t nsteps_pushed, tag_injected, tag_splitted;
     uint32_t rng_ctr;
@@ -407,7 +431,7 @@ static void push_momentum(const mover_ctx *c, ptl_state *s, double dp_dt, double
 
 /* push_particle_2d, Cartesian uniform grid: particle_module.f90:3358-3606. */
 static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                    int fixed_dt, double *deltax, double *deltay, double *deltaz, double *deltap)
+                    int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
@@ -458,13 +482,15 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     s->y = s->y + dY;
     s->z = s->z + dZ;
     s->t = s->t + s->dt;
-    *deltax = dX; *deltay = dY; *deltaz = dZ;
-    push_momentum(c, s, dp_dt, sdt, r[3], deltap);
+    /* deltaz is local to push_particle_2d: the mover's deltaz stays 0, so an
+     * undone push keeps its out-of-plane drift. */
+    d[0] = dX; d[1] = dY; d[2] = 0.0; d[4] = 0.0; d[5] = 0.0;
+    push_momentum(c, s, dp_dt, sdt, r[3], &d[3]);
 }
 
 /* push_particle_3d, Cartesian uniform grid: particle_module.f90:4625-4907. */
 static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                    int fixed_dt, double *deltax, double *deltay, double *deltaz, double *deltap)
+                    int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
@@ -519,8 +545,253 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     s->y = s->y + dY;
     s->z = s->z + dZ;
     s->t = s->t + s->dt;
-    *deltax = dX; *deltay = dY; *deltaz = dZ;
-    push_momentum(c, s, dp_dt, sdt, r[3], deltap);
+    d[0] = dX; d[1] = dY; d[2] = dZ; d[4] = 0.0; d[5] = 0.0;
+    push_momentum(c, s, dp_dt, sdt, r[3], &d[3]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Focused transport.                                                        */
+/* ------------------------------------------------------------------------ */
+/* calc_duu: particle_module.f90:3116-3155 without delta-B or correlation   */
+/* length.                                                                   */
+static void calc_duu(const orc_params *pr, const ptl_state *s, double b, double div_bnorm,
+                     double divv, double bb_gradv, double bv_gradv, double mu2,
+                     double *dmu_dt, double *duu, double *duu_du)
+{
+    double dm = s->v * div_bnorm + s->mu * divv - 3.0 * s->mu * bb_gradv - 2.0 * bv_gradv / s->v;
+    dm = dm * (1.0 - mu2) * 0.5;
+    const double h0 = (double)0.2f;
+    const double dtmp = pow(fabs(s->mu), pr->gamma_turb - 1.0) + h0;
+    double u = pr->duu0 * (1.0 - mu2) * dtmp;
+    double ud;
+    if (s->mu > 0.0)
+        ud = pr->duu0 * (-(2.0 * s->mu * dtmp) + (1.0 - mu2) * pow(fabs(s->mu), pr->gamma_turb - 2.0));
+    else if (s->mu < 0.0)
+        ud = pr->duu0 * (-(2.0 * s->mu * dtmp) - (1.0 - mu2) * pow(fabs(s->mu), pr->gamma_turb - 2.0));
+    else
+        ud = 0.0;
+    double norm = 1.0;
+    if (pr->mag_dependency == 1) norm = norm * pow(b, 2.0 - pr->gamma_turb);
+    if (pr->momentum_dependency == 1) norm = norm * pow(s->p / pr->p0, pr->gamma_turb - 1.0);
+    ud = ud * norm;
+    u = u * norm;
+    *dmu_dt = dm + ud;
+    *duu = u;
+    *duu_du = ud;
+}
+
+/* 1 / pcharge is single precision in the focused-transport pushes. */
+static double vdrift_prefactor_ft(const orc_params *pr, double p)
+{
+    const float q = 1.0f / (float)pr->charge;
+    const double t1 = pr->drift1 * pr->p0 / p;
+    const double t2 = pr->drift2 * (pr->p0 * pr->p0) / (p * p);
+    return (double)q / sqrt(t1 * t1 + t2 * t2);
+}
+
+/* The tail shared by push_particle_2d_ft and push_particle_3d_ft: the
+ * momentum, speed and pitch-angle increments, the mu_max clamp, the
+ * acceleration-region mask and the 0.25 p0 floor (:3920-3963,
+ * :5280-5323).  r[2] drives momentum diffusion, r[3] pitch-angle. */
+static void push_ft_tail(const mover_ctx *c, ptl_state *s, double dX, double dY, double dZ,
+                         double dp_dt, double dmu_dt, double duu, double sdt,
+                         const double r[4], double d[6])
+{
+    const double dpp = 0.0;
+    double dP = dp_dt * s->dt + r[2] * sqrt(2.0 * dpp) * sdt;
+    double dV = s->v * dP / s->p;
+    double dMu = dmu_dt * s->dt + r[3] * sqrt(2.0 * duu) * sdt;
+    s->x = s->x + dX;
+    s->y = s->y + dY;
+    s->z = s->z + dZ;
+    s->mu = s->mu + dMu;
+    s->t = s->t + s->dt;
+    const double mu_max = (double)0.99f;
+    if (s->mu > mu_max) {
+        dMu = mu_max - (s->mu - dMu);
+        s->mu = mu_max;
+    } else if (s->mu < -mu_max) {
+        dMu = -mu_max - (s->mu - dMu);
+        s->mu = -mu_max;
+    }
+    if (c->pr->acc_region_flag == 1) {
+        if (in_acc_region(c, s)) {
+            s->p = s->p + dP;
+            s->v = s->v + dV;
+        } else {
+            dP = 0.0;
+            dV = 0.0;
+        }
+    } else {
+        s->p = s->p + dP;
+        s->v = s->v + dV;
+    }
+    const double pfloor = 0.25 * c->pr->p0;
+    if (s->p < pfloor) {
+        s->v = s->v - dV;
+        dV = s->v * 0.25 * c->pr->p0 / s->p - s->v;
+        s->v = s->v + dV;
+        s->p = s->p - dP;
+        dP = pfloor - s->p;
+        s->p = pfloor;
+    }
+    d[0] = dX; d[1] = dY; d[2] = dZ; d[3] = dP; d[4] = dV; d[5] = dMu;
+}
+
+/* The adaptive time step of the focused-transport pushes (:3850-3905,
+ * :5170-5230): the minimum of the cell-crossing, drift, momentum and
+ * pitch-angle limits, dt_min when any first-order rate is exactly 0. */
+static void ft_time_step(const mover_ctx *c, ptl_state *s, const double *kap, int ndim,
+                         double dx_dt, double dy_dt, double dz_dt, double dp_dt,
+                         double dmu_dt, double duu)
+{
+    const int rates_nonzero = (dx_dt != 0.0) && (dy_dt != 0.0) && (ndim < 3 || dz_dt != 0.0) &&
+                              (dp_dt != 0.0) && (dmu_dt != 0.0);
+    if (rates_nonzero) {
+        const double sk = (kap[K_SKPERP] > 0.0) ? kap[K_SKPERP] : kap[K_SKPARA];
+        double a = 0.5 * c->dx / sk, m = a * a;
+        a = 0.5 * c->dy / sk; if (a * a < m) m = a * a;
+        if (ndim == 3) { a = 0.5 * c->dz / sk; if (a * a < m) m = a * a; }
+        a = sk / dx_dt; if (a * a < m) m = a * a;
+        a = sk / dy_dt; if (a * a < m) m = a * a;
+        if (ndim == 3) { a = sk / dz_dt; if (a * a < m) m = a * a; }
+        a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
+        a = (double)0.1f / fabs(dmu_dt); if (a < m) m = a;
+        a = 2.0 * duu / (dmu_dt * dmu_dt); if (a < m) m = a;
+        s->dt = m;
+    } else {
+        s->dt = c->dt_min;
+    }
+    if (s->dt < c->dt_min) s->dt = c->dt_min;
+    if (s->dt > c->dt_max) s->dt = c->dt_max;
+}
+
+/* push_particle_2d_ft, Cartesian uniform grid: particle_module.f90:3626-3964. */
+static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
+                       int fixed_dt, double d[6])
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    const double dbx_dx = f[20], dbx_dy = f[21], dby_dx = f[23], dby_dy = f[24];
+    const double dbz_dx = f[26], dbz_dy = f[27], db_dx = f[29], db_dy = f[30];
+    const double ib2 = ib * ib;
+    const double ib3 = ib * ib2;
+    const double vdp = vdrift_prefactor_ft(pr, s->p);
+    const double mu2 = s->mu * s->mu;
+    const double muf1 = 0.5 * (1.0 - mu2);
+    const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
+    const double kx = bx * dbx_dx + by * dbx_dy;
+    const double ky = bx * dby_dx + by * dby_dy;
+    const double kz = bx * dbz_dx + by * dbz_dy;
+    const double bdot_curvb = bx * dbz_dy - by * dbz_dx + bz * (dby_dx - dbx_dy);
+    const double vdx = vdp * (muf1 * (-(bz * db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                              muf1 * bx * bdot_curvb * ib3);
+    const double vdy = vdp * (muf1 * (bz * db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                              muf1 * by * bdot_curvb * ib3);
+    double vdz = 0.0;
+    if (pr->check_drift_2d)
+        vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                     muf1 * bz * bdot_curvb * ib3);
+    double vbx = s->v * s->mu * ib;
+    const double vby = vbx * by;
+    vbx = vbx * bx;
+    const double dvx_dx = f[8], dvx_dy = f[9], dvy_dx = f[11], dvy_dy = f[12];
+    const double dvz_dx = f[14], dvz_dy = f[15];
+    const double dx_dt = vx + vdx + vbx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
+    const double dy_dt = vy + vdy + vby + kap[K_DKXY_DX] + kap[K_DKYY_DY];
+    const double dz_dt = vdz;
+    const double divv = dvx_dx + dvy_dy;
+    const double bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy) +
+                             by * (bx * dvy_dx + by * dvy_dy) +
+                             bz * (bx * dvz_dx + by * dvz_dy)) * ib2;
+    const double bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy) +
+                             by * (vx * dvy_dx + vy * dvy_dy) +
+                             bz * (vx * dvz_dx + vy * dvz_dy)) * ib;
+    const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
+    const double dp_dt = s->p * acc_rate;
+    const double div_bnorm = -((bx * db_dx + by * db_dy) * ib2);
+    double dmu_dt, duu, duu_du;
+    calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
+    if (!fixed_dt) ft_time_step(c, s, kap, 2, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+    const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
+    const double skperp = kap[K_SKPERP];
+    const double dX = dx_dt * s->dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
+    const double dY = dy_dt * s->dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+    const double dZ = dz_dt * s->dt;
+    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
+    d[2] = 0.0;   /* deltaz is local to push_particle_2d_ft, as in push_2d */
+}
+
+/* push_particle_3d_ft, Cartesian uniform grid: particle_module.f90:4930-5324. */
+static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
+                       int fixed_dt, double d[6])
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+    const double bxyn = sqrt(bxn * bxn + byn * byn);
+    const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
+    const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
+    const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
+    const double dbz_dx = f[26], dbz_dy = f[27], dbz_dz = f[28];
+    const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
+    const double ib2 = ib * ib;
+    const double ib3 = ib * ib2;
+    const double vdp = vdrift_prefactor_ft(pr, s->p);
+    const double mu2 = s->mu * s->mu;
+    const double muf1 = 0.5 * (1.0 - mu2);
+    const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
+    const double kx = bx * dbx_dx + by * dbx_dy + bz * dbx_dz;
+    const double ky = bx * dby_dx + by * dby_dy + bz * dby_dz;
+    const double kz = bx * dbz_dx + by * dbz_dy + bz * dbz_dz;
+    const double bdot_curvb = bx * (dbz_dy - dby_dz) + by * (dbx_dz - dbz_dx) + bz * (dby_dx - dbx_dy);
+    const double vdx = vdp * (muf1 * (by * db_dz - bz * db_dy) * ib2 +
+                              mu2 * (by * kz - bz * ky) * ib3 + muf1 * bx * bdot_curvb * ib3);
+    const double vdy = vdp * (muf1 * (bz * db_dx - bx * db_dz) * ib2 +
+                              mu2 * (bz * kx - bx * kz) * ib3 + muf1 * by * bdot_curvb * ib3);
+    const double vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 +
+                              mu2 * (bx * ky - by * kx) * ib3 + muf1 * bz * bdot_curvb * ib3);
+    double vbx = s->v * s->mu * ib;
+    const double vby = vbx * by;
+    const double vbz = vbx * bz;
+    vbx = vbx * bx;
+    const double dvx_dx = f[8], dvx_dy = f[9], dvx_dz = f[10];
+    const double dvy_dx = f[11], dvy_dy = f[12], dvy_dz = f[13];
+    const double dvz_dx = f[14], dvz_dy = f[15], dvz_dz = f[16];
+    const double dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
+    const double dy_dt = vy + vby + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
+    const double dz_dt = vz + vbz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
+    const double divv = dvx_dx + dvy_dy + dvz_dz;
+    const double bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy + bz * dvx_dz) +
+                             by * (bx * dvy_dx + by * dvy_dy + bz * dvy_dz) +
+                             bz * (bx * dvz_dx + by * dvz_dy + bz * dvz_dz)) * ib2;
+    const double bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy + vz * dvx_dz) +
+                             by * (vx * dvy_dx + vy * dvy_dy + vz * dvy_dz) +
+                             bz * (vx * dvz_dx + vy * dvz_dy + vz * dvz_dz)) * ib;
+    const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
+    const double dp_dt = s->p * acc_rate;
+    const double div_bnorm = -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
+    double dmu_dt, duu, duu_du;
+    calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
+    if (!fixed_dt) ft_time_step(c, s, kap, 3, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double skperp = kap[K_SKPERP];
+    const double dX = dx_dt * s->dt +
+        (-(bxn * bzn * skperp * ibxyn * r[0]) - byn * skperp * ibxyn * r[1]) * sdt;
+    const double dY = dy_dt * s->dt +
+        (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
+    const double dZ = dz_dt * s->dt + bxyn * skperp * r[0] * sdt;
+    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
 }
 
 /* particle_boundary_condition on a single rank: particle_module.f90:1984-2129.
@@ -569,8 +840,7 @@ static void check_negp_or_boundary(const mover_ctx *c, ptl_state *s, thread_acc 
 
 /* One push at the particle's current state: interpolation parameters,
  * interp_fields, kappa, push (the body at particle_module.f90:1615-1703). */
-static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double *dX, double *dY,
-                    double *dZ, double *dP)
+static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
 {
     const double px = (s->x - c->xmin) / c->dx;
     const double py = (s->y - c->ymin) / c->dy;
@@ -580,9 +850,14 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double *dX, 
     double w[8], f[32], kap[22];
     orc_get_interp_paramters(c->ndim, px, py, pz, pos, w);
     orc_interp_fields(c->f1, c->f2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, f);
-    orc_calc_spatial_diffusion_coefficients(c->pr, s->p, f, kap);
-    if (c->ndim == 2) push_2d(c, s, f, kap, fixed_dt, dX, dY, dZ, dP);
-    else push_3d(c, s, f, kap, fixed_dt, dX, dY, dZ, dP);
+    orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, kap);
+    if (c->pr->focused_transport) {
+        if (c->ndim == 2) push_2d_ft(c, s, f, kap, fixed_dt, d);
+        else push_3d_ft(c, s, f, kap, fixed_dt, d);
+    } else {
+        if (c->ndim == 2) push_2d(c, s, f, kap, fixed_dt, d);
+        else push_3d(c, s, f, kap, fixed_dt, d);
+    }
 }
 
 /* The per-particle body of particle_mover_one_cycle: :1560-1830. */
@@ -591,7 +866,7 @@ static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
 {
     const double t0 = c->t0, dtf = c->dtf;
     const double dt_fine = dtf / num_fine_steps;
-    double deltax = 0.0, deltay = 0.0, deltaz = 0.0, deltap = 0.0;
+    double dl[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   /* deltax..deltamu */
     const double step = ceil((s->t - t0) / dt_fine);
     double dt_target = (step <= 0.0) ? dt_fine : step * dt_fine;
     if (dt_target > dtf) dt_target = dtf;
@@ -610,21 +885,23 @@ static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
         while ((s->t - t0) < dt_target && s->flag == 1) {
             check_negp_or_boundary(c, s, acc);
             if (s->flag != 1) break;
-            do_push(c, s, 0, &deltax, &deltay, &deltaz, &deltap);
+            do_push(c, s, 0, dl);
             acc->steps += 1;
             s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
         }
         if ((s->t - t0) > dt_target && s->flag == 1) {
-            s->x = s->x - deltax;
-            s->y = s->y - deltay;
-            s->z = s->z - deltaz;
-            s->p = s->p - deltap;
+            s->x = s->x - dl[0];
+            s->y = s->y - dl[1];
+            s->z = s->z - dl[2];
+            s->p = s->p - dl[3];
+            s->v = s->v - dl[4];
+            s->mu = s->mu - dl[5];
             s->t = s->t - s->dt;
             const double dt_old = s->dt;
             s->dt = t0 + dt_target - s->t;
             if (s->dt > 0.0) {
                 s->nsteps_pushed = s->nsteps_pushed - 1;
-                do_push(c, s, 1, &deltax, &deltay, &deltaz, &deltap);
+                do_push(c, s, 1, dl);
                 acc->steps += 1;
                 s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
             }
@@ -638,6 +915,7 @@ static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
 static void load_state(const orc_particles *P, int64_t i, ptl_state *s)
 {
     s->x = P->x[i]; s->y = P->y[i]; s->z = P->z[i]; s->p = P->p[i];
+    s->v = P->v[i]; s->mu = P->mu[i];
     s->t = P->t[i]; s->dt = P->dt[i]; s->weight = P->weight[i];
     s->flag = P->count_flag[i];
     s->nsteps_pushed = P->nsteps_pushed[i];
@@ -649,6 +927,7 @@ static void load_state(const orc_particles *P, int64_t i, ptl_state *s)
 static void store_state(orc_particles *P, int64_t i, const ptl_state *s)
 {
     P->x[i] = s->x; P->y[i] = s->y; P->z[i] = s->z; P->p[i] = s->p;
+    P->v[i] = s->v; P->mu[i] = s->mu;
     P->t[i] = s->t; P->dt[i] = s->dt;
     P->count_flag[i] = (int8_t)s->flag;
     P->nsteps_pushed[i] = s->nsteps_pushed;

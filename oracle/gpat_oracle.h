@@ -50,7 +50,11 @@ typedef struct orc_params {
     int32_t check_drift_2d, ndim, pbcx, pbcy, pbcz, npp_global;
     uint64_t seed;
     int32_t noise;      /* 0: (2u-1)*sqrt(3) as the reference; 1: Gaussian */
+    int32_t focused_transport;  /* particle_mover's focused_transport          */
+    int32_t nlgc;               /* particle_mover's nlgc                       */
     int32_t reserved;
+    double duu0;                /* set_duu_params (:279-283)                   */
+    double kperp_kpara;         /* particle_mover's kperp_kpara                */
 } orc_params;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the
@@ -88,7 +92,7 @@ void orc_get_interp_paramters(int ndim, double px, double py, double pz,
 void orc_interp_fields(const float *f1, const float *f2, int time_interp, int ndim,
                        int nxg, int nyg, const int32_t pos[3], const double weights[8],
                        double rt, double fields[32]);
-void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p,
+void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, double mu,
                                              const double fields[32], double kappa[22]);
 
 int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,

@@ -37,8 +37,13 @@ class OrcParams(C.Structure):
         ("check_drift_2d", i32), ("ndim", i32), ("pbcx", i32), ("pbcy", i32), ("pbcz", i32),
         ("npp_global", i32),
         ("seed", u64),
-        ("noise", i32), ("reserved", i32),
+        ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("reserved", i32),
+        ("duu0", d), ("kperp_kpara", d),
     ]
+
+# Mover arguments of the reference carried in OrcParams rather than in the
+# engine's parameter block.
+_MOVER_ARGS = ("focused_transport", "nlgc", "kperp_kpara", "reserved")
 
 
 FIELDS = [
@@ -95,7 +100,7 @@ def load() -> C.CDLL:
         lib.orc_get_interp_paramters.argtypes = [C.c_int, d, d, d, P(i32), P(d)]
         lib.orc_interp_fields.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_int,
                                           C.c_int, P(i32), P(d), d, P(d)]
-        lib.orc_calc_spatial_diffusion_coefficients.argtypes = [P(OrcParams), d, P(d), P(d)]
+        lib.orc_calc_spatial_diffusion_coefficients.argtypes = [P(OrcParams), d, d, P(d), P(d)]
         lib.orc_particle_mover.restype = i64
         lib.orc_particle_mover.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
                                            P(C.c_float), C.c_int, P(OrcParticles), i64, d, d,
@@ -129,7 +134,7 @@ def params_from(p) -> OrcParams:
     o = OrcParams()
     get = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
     for name, _ in OrcParams._fields_:
-        if name == "reserved":
+        if name in _MOVER_ARGS:
             continue
         v = get(name)
         if name == "acc_region":
@@ -189,8 +194,15 @@ def philox(ctr, key):
 
 def mover(params: OrcParams, cfg: OrcMhdConfig, f1: np.ndarray, parts: Particles, t0: float,
           dtf: float, nsteps_interval: int = 10, num_fine_steps: int = 1, nthreads: int = 0,
-          counters: OrcCounters | None = None, f2: np.ndarray | None = None) -> OrcCounters:
+          counters: OrcCounters | None = None, f2: np.ndarray | None = None,
+          focused_transport: bool = False, nlgc: bool = False,
+          kperp_kpara: float = 0.01) -> OrcCounters:
+    """particle_mover(focused_transport, nlgc, kperp_kpara, ...) on one rank."""
     lib = load()
+    params = OrcParams.from_buffer_copy(params)
+    params.focused_transport = int(bool(focused_transport))
+    params.nlgc = int(bool(nlgc))
+    params.kperp_kpara = kperp_kpara
     cnt = counters if counters is not None else OrcCounters()
     fp1 = f1.ctypes.data_as(P(C.c_float))
     fp2 = (f2 if f2 is not None else f1).ctypes.data_as(P(C.c_float))

@@ -179,6 +179,9 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.n = h->n;
     a.rec1 = h->rec[0];
     a.rec2 = p.time_interp ? h->rec[1] : h->rec[0];
+    a.full1 = h->full[0];
+    a.full2 = p.time_interp ? h->full[1] : h->full[0];
+    a.duu0 = p.duu0;
     a.time_interp = p.time_interp;
     a.ndim = p.ndim;
     a.nxg = h->nxg; a.nyg = h->nyg; a.nzg = h->nzg;
@@ -633,18 +636,20 @@ int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, double kperp_kpara,
                         int nsteps_interval, int mhd_tframe, int num_fine_steps,
                         int dump_escaped_dist) {
-    (void)kperp_kpara;
     if (!h) return GPAT_ERR_ARG;
     (void)dump_escaped_dist;   // the escaped distribution is always accumulated
-    if (focused_transport || nlgc)
-        return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport and NLGC are not in this engine");
+    const bool mixed = h->prm.precision == GPAT_PREC_MIXED;
+    if ((focused_transport || nlgc) && mixed)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport and NLGC run in FP64 precision");
     MoverArgs a;
     int rc = mover_args(h, mhd_tframe, nsteps_interval, num_fine_steps, a);
     if (rc) return rc;
+    a.focused_transport = focused_transport ? 1 : 0;
+    a.nlgc = nlgc ? 1 : 0;
+    a.kperp_kpara = kperp_kpara;
     CK(cudaSetDevice(h->device));
     rc = ensure_scratch(h, h->n);
     if (rc) return rc;
-    const bool mixed = h->prm.precision == GPAT_PREC_MIXED;
     if (mixed && h->unsorted) {
         // New particles since the last binning: bin them before moving.
         rc = bin_particles(h);

@@ -68,6 +68,11 @@ struct MoverArgs {
     uint32_t max_pushes;        // per particle per call, guards runaway loops
     uint32_t chunk_pushes;      // split-precision mover: stop a particle after this many
                                 // pushes (between pushes) so the set can be re-binned; 0 = off
+    // particle_mover's focused_transport / nlgc / kperp_kpara and duu0.
+    // Focused transport interpolates all 32 variables from full1/full2.
+    int focused_transport, nlgc;
+    double kperp_kpara, duu0;
+    const float *full1, *full2;
     DevCounters *cnt;
 };
 

@@ -2,13 +2,16 @@
 // order.  This translation unit is compiled with -fmad=false so every
 // +, -, *, / and sqrt is a single IEEE-rounded operation, which makes the
 // trajectories bit-identical to a CPU FP64 evaluation of the same formulas
-// (only pow() in momentum/|B|-dependent kappa is library-dependent).
+// (only pow() -- momentum/|B|-dependent kappa, focused transport's D_mumu --
+// is library-dependent).
 //
 // Follows particle_mover_one_cycle (particle_module.f90:1481-1833),
 // get_interp_paramters (:642-674), interp_fields (mhd_data_parallel.f90:
-// 1751-1804), calc_spatial_diffusion_coefficients (:2208-2450),
-// push_particle_2d (:3358-3606), push_particle_3d (:4625-4907) and
-// particle_boundary_condition (:1984-2129) on a single rank.
+// 1751-1804), calc_spatial_diffusion_coefficients (:2208-2450) and its NLGC
+// variant (:2464-2771), push_particle_2d (:3358-3606), push_particle_3d
+// (:4625-4907), the focused-transport pushes push_particle_2d_ft
+// (:3626-3964) and push_particle_3d_ft (:4930-5324) with calc_duu
+// (:3116-3155), and particle_boundary_condition (:1984-2129) on one rank.
 #include <cfloat>
 
 #include "device_common.cuh"
@@ -23,10 +26,15 @@ enum R3 { B_VX, B_VY, B_VZ, B_BX, B_BY, B_BZ, B_DVXDX, B_DVYDY, B_DVZDZ, B_DBXDX
           B_DBXDZ, B_DBYDX, B_DBYDY, B_DBYDZ, B_DBZDX, B_DBZDY, B_DBZDZ, B_DBDX, B_DBDY, B_DBDZ };
 
 struct State {
-    double x, y, z, p, t, dt, w;
+    double x, y, z, p, v, mu, t, dt, w;
     int flag;
     int32_t nsteps_pushed, tag_inj, tag_spl;
     uint32_t ctr;
+};
+
+// deltax, deltay, deltaz, deltap, deltav, deltamu of particle_mover_one_cycle.
+struct Delta {
+    double x, y, z, p, v, mu;
 };
 
 struct Acc {
@@ -39,10 +47,10 @@ __device__ __forceinline__ void acc_add(unsigned long long &h, unsigned long lon
     add_u128(h, l, bh, bl);
 }
 
-// Interpolated fields at the particle, in the packed-record slot order.
-template <int NDIM, int NV>
-__device__ __forceinline__ bool interp(const MoverArgs &a, const State &s, double f[NV]) {
-    constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
+// Interpolated fields at the particle: NV variables of records of R floats.
+template <int NDIM, int NV, int R>
+__device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, const float *rec2,
+                                       const State &s, double f[NV]) {
     const double px = (s.x - a.xmin) / a.dx;
     const double py = (s.y - a.ymin) / a.dy;
     const double pz = (s.z - a.zmin) / a.dz;
@@ -82,7 +90,7 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const State &s, doubl
                 const double wc = w[k * 4 + j * 2 + i];
                 const size_t cell = (size_t)(ix + i) +
                                     (size_t)a.nxg * ((size_t)(iy + j) + (size_t)a.nyg * (size_t)(iz + k));
-                const float4 *r4 = reinterpret_cast<const float4 *>(a.rec1 + (size_t)R * cell);
+                const float4 *r4 = reinterpret_cast<const float4 *>(rec1 + (size_t)R * cell);
 #pragma unroll
                 for (int q = 0; q < (NV + 3) / 4; ++q) {
                     const float4 v4 = __ldg(r4 + q);
@@ -92,7 +100,7 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const State &s, doubl
                         if (4 * q + e < NV) f[4 * q + e] = f[4 * q + e] + (double)vv[e] * wc;
                 }
                 if (a.time_interp) {
-                    const float4 *s4 = reinterpret_cast<const float4 *>(a.rec2 + (size_t)R * cell);
+                    const float4 *s4 = reinterpret_cast<const float4 *>(rec2 + (size_t)R * cell);
 #pragma unroll
                     for (int q = 0; q < (NV + 3) / 4; ++q) {
                         const float4 v4 = __ldg(s4 + q);
@@ -108,6 +116,49 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const State &s, doubl
         for (int v = 0; v < NV; ++v) f[v] = f[v] * (1.0 - rt) + f2[v] * rt;
     }
     return true;
+}
+
+// Field values at the particle under the reference's names.
+struct Fld {
+    double vx, vy, vz, bx, by, bz;
+    double dvx_dx, dvx_dy, dvx_dz, dvy_dx, dvy_dy, dvy_dz, dvz_dx, dvz_dy, dvz_dz;
+    double dbx_dx, dbx_dy, dbx_dz, dby_dx, dby_dy, dby_dz, dbz_dx, dbz_dy, dbz_dz;
+    double db_dx, db_dy, db_dz;
+};
+
+// From the full 32-variable layout (interp_fields order, 0-based).
+__device__ __forceinline__ Fld named_full(const double *f) {
+    Fld q;
+    q.vx = f[0]; q.vy = f[1]; q.vz = f[2]; q.bx = f[4]; q.by = f[5]; q.bz = f[6];
+    q.dvx_dx = f[8]; q.dvx_dy = f[9]; q.dvx_dz = f[10];
+    q.dvy_dx = f[11]; q.dvy_dy = f[12]; q.dvy_dz = f[13];
+    q.dvz_dx = f[14]; q.dvz_dy = f[15]; q.dvz_dz = f[16];
+    q.dbx_dx = f[20]; q.dbx_dy = f[21]; q.dbx_dz = f[22];
+    q.dby_dx = f[23]; q.dby_dy = f[24]; q.dby_dz = f[25];
+    q.dbz_dx = f[26]; q.dbz_dy = f[27]; q.dbz_dz = f[28];
+    q.db_dx = f[29]; q.db_dy = f[30]; q.db_dz = f[31];
+    return q;
+}
+
+// From the packed records, which hold what the Parker pushes read.
+template <int NDIM>
+__device__ __forceinline__ Fld named_packed(const double *f) {
+    Fld q = {};
+    if (NDIM == 2) {
+        q.vx = f[A_VX]; q.vy = f[A_VY]; q.bx = f[A_BX]; q.by = f[A_BY]; q.bz = f[A_BZ];
+        q.dvx_dx = f[A_DVXDX]; q.dvy_dy = f[A_DVYDY];
+        q.dbx_dx = f[A_DBXDX]; q.dbx_dy = f[A_DBXDY]; q.dby_dx = f[A_DBYDX]; q.dby_dy = f[A_DBYDY];
+        q.dbz_dx = f[A_DBZDX]; q.dbz_dy = f[A_DBZDY]; q.db_dx = f[A_DBDX]; q.db_dy = f[A_DBDY];
+    } else {
+        q.vx = f[B_VX]; q.vy = f[B_VY]; q.vz = f[B_VZ];
+        q.bx = f[B_BX]; q.by = f[B_BY]; q.bz = f[B_BZ];
+        q.dvx_dx = f[B_DVXDX]; q.dvy_dy = f[B_DVYDY]; q.dvz_dz = f[B_DVZDZ];
+        q.dbx_dx = f[B_DBXDX]; q.dbx_dy = f[B_DBXDY]; q.dbx_dz = f[B_DBXDZ];
+        q.dby_dx = f[B_DBYDX]; q.dby_dy = f[B_DBYDY]; q.dby_dz = f[B_DBYDZ];
+        q.dbz_dx = f[B_DBZDX]; q.dbz_dy = f[B_DBZDY]; q.dbz_dz = f[B_DBZDZ];
+        q.db_dx = f[B_DBDX]; q.db_dy = f[B_DBDY]; q.db_dz = f[B_DBDZ];
+    }
+    return q;
 }
 
 __device__ __forceinline__ void noise4(const MoverArgs &a, State &s, double r[4]) {
@@ -148,8 +199,10 @@ __device__ __forceinline__ bool in_acc_region(const MoverArgs &a, const State &s
     return in;
 }
 
-__device__ __forceinline__ double vdrift_prefactor(const MoverArgs &a, double p) {
-    const float q = __fdiv_rn(1.0f, (float)(3 * a.charge));
+// 1 / (3 pcharge) (Parker) or 1 / pcharge (focused transport) is single
+// precision in the reference.
+__device__ __forceinline__ double vdrift_prefactor(const MoverArgs &a, double p, int qmul) {
+    const float q = __fdiv_rn(1.0f, (float)(qmul * a.charge));
     const double t1 = a.drift1 * a.p0 / p;
     const double t2 = a.drift2 * (a.p0 * a.p0) / (p * p);
     return (double)q / sqrt(t1 * t1 + t2 * t2);
@@ -174,70 +227,117 @@ __device__ __forceinline__ void push_momentum(const MoverArgs &a, State &s, doub
     deltap = dP;
 }
 
-// Kappa (norms, square roots) shared by both dimensions.
-struct KBase {
-    double kpara, kperp, skpara, skperp, skpp, kpp, b, ib1, ib2, ib3;
+// calc_spatial_diffusion_coefficients (:2208-2450) or its NLGC variant
+// (:2464-2771).  The gradient terms are written as
+//   dkii_di = T_i + A_i bi^2 / B^2 + 2 kpp bi (dbi_di B - bi dB_di) / B^3
+//   dkij_dk = A_k bi bj / B^2 + kpp ((dbi_dk bj + bi dbj_dk) / B^2 - 2 bi bj dB_dk / B^3)
+// with T_i = kperp dk_i, A_i = kpp dk_i (fixed ratio) or T_i = kperp dkperp_i,
+// A_i = kpara dkpara_i - kperp dkperp_i (NLGC), each in the reference's order.
+struct Kap {
+    double kpara, kperp, skpara, skperp, skpp;
+    double dkxx_dx, dkyy_dy, dkzz_dz, dkxy_dx, dkxy_dy, dkxz_dx, dkxz_dz, dkyz_dy, dkyz_dz;
 };
 
-__device__ __forceinline__ KBase kappa_base(const MoverArgs &a, double p, double bx, double by,
-                                            double bz) {
-    KBase k;
-    k.b = sqrt(bx * bx + by * by + bz * bz);
-    k.ib1 = (k.b < DBL_EPSILON) ? 1.0 : 1.0 / k.b;
-    k.ib2 = k.ib1 * k.ib1;
-    k.ib3 = k.ib1 * k.ib2;
-    double knorm_para = 1.0, knorm;
-    if (a.mag_dependency == 1) knorm_para = knorm_para * pow(k.b, a.gamma_turb - 2.0);
-    if (a.momentum_dependency == 1) knorm = knorm_para * pow(p / a.p0, a.pindex);
-    else knorm = knorm_para;
-    k.kpara = a.kpara0 * knorm;
-    k.kperp = k.kpara * a.kret;
-    k.skpara = sqrt(2.0 * k.kpara);
-    k.skperp = sqrt(2.0 * k.kperp);
-    k.skpp = sqrt(2.0 * (k.kpara - k.kperp));
-    k.kpp = k.kpara - k.kperp;
+template <int NDIM, bool FT>
+__device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, const Fld &f) {
+    const double bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
+    const double ib2 = ib1 * ib1;
+    const double ib3 = ib1 * ib2;
+    double kpara, kperp;
+    if (!a.nlgc) {
+        double knorm_para = 1.0, knorm;
+        if (a.mag_dependency == 1) knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
+        if (a.momentum_dependency == 1) knorm = knorm_para * pow(p / a.p0, a.pindex);
+        else knorm = knorm_para;
+        kpara = a.kpara0 * knorm;
+        kperp = kpara * a.kret;
+    } else {
+        double knorm_para = 1.0, knorm_perp = 1.0, kn_para, kn_perp;
+        if (a.mag_dependency == 1) {
+            knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
+            knorm_perp = knorm_perp * pow(b, (a.gamma_turb - 2.0) / 3.0);
+        }
+        if (a.momentum_dependency == 1) {
+            kn_para = knorm_para * pow(p / a.p0, a.pindex);
+            kn_perp = knorm_perp * pow(p / a.p0, (5.0 - a.gamma_turb) / 3.0);
+        } else {
+            kn_para = knorm_para;
+            kn_perp = knorm_perp;
+        }
+        kpara = a.kpara0 * kn_para;
+        kperp = a.kpara0 * a.kperp_kpara * kn_perp * (mu * mu);
+    }
+    Kap k;
+    k.kpara = kpara;
+    k.kperp = kperp;
+    k.skpara = sqrt(2.0 * kpara);
+    k.skperp = sqrt(2.0 * kperp);
+    k.skpp = sqrt(2.0 * (kpara - kperp));
+    const double kpp = FT ? -kperp : kpara - kperp;
+    const double db[3] = {f.db_dx, f.db_dy, f.db_dz};
+    const double g2 = a.gamma_turb - 2.0;
+    double T[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+        if (!a.nlgc) {
+            double dk = 0.0;
+            // the fixed-ratio 3D branch has no 1/B factor (:2406-2408)
+            if (a.mag_dependency == 1) dk = (NDIM == 3) ? db[d] * g2 : db[d] * ib1 * g2;
+            T[d] = kperp * dk;
+            A[d] = kpp * dk;
+        } else {
+            double dkpara = 0.0, dkperp = 0.0;
+            if (a.mag_dependency == 1) {
+                dkpara = db[d] * ib1 * g2;
+                dkperp = db[d] * ib1 * g2 / 3.0;
+            }
+            T[d] = kperp * dkperp;
+            A[d] = kpara * dkpara - kperp * dkperp;
+        }
+    }
+    k.dkxx_dx = T[0] + A[0] * (bx * bx) * ib2 + 2.0 * kpp * bx * (f.dbx_dx * b - bx * f.db_dx) * ib3;
+    k.dkyy_dy = T[1] + A[1] * (by * by) * ib2 + 2.0 * kpp * by * (f.dby_dy * b - by * f.db_dy) * ib3;
+    k.dkxy_dx = A[0] * bx * by * ib2 +
+                kpp * ((f.dbx_dx * by + bx * f.dby_dx) * ib2 - 2.0 * bx * by * f.db_dx * ib3);
+    k.dkxy_dy = A[1] * bx * by * ib2 +
+                kpp * ((f.dbx_dy * by + bx * f.dby_dy) * ib2 - 2.0 * bx * by * f.db_dy * ib3);
+    if (NDIM == 3) {
+        k.dkzz_dz = T[2] + A[2] * (bz * bz) * ib2 +
+                    2.0 * kpp * bz * (f.dbz_dz * b - bz * f.db_dz) * ib3;
+        k.dkxz_dx = A[0] * bx * bz * ib2 +
+                    kpp * ((f.dbx_dx * bz + bx * f.dbz_dx) * ib2 - 2.0 * bx * bz * f.db_dx * ib3);
+        k.dkxz_dz = A[2] * bx * bz * ib2 +
+                    kpp * ((f.dbx_dz * bz + bx * f.dbz_dz) * ib2 - 2.0 * bx * bz * f.db_dz * ib3);
+        k.dkyz_dy = A[1] * by * bz * ib2 +
+                    kpp * ((f.dby_dy * bz + by * f.dbz_dy) * ib2 - 2.0 * by * bz * f.db_dy * ib3);
+        k.dkyz_dz = A[2] * by * bz * ib2 +
+                    kpp * ((f.dby_dz * bz + by * f.dbz_dz) * ib2 - 2.0 * by * bz * f.db_dz * ib3);
+    } else {
+        k.dkzz_dz = 0.0; k.dkxz_dx = 0.0; k.dkxz_dz = 0.0; k.dkyz_dy = 0.0; k.dkyz_dz = 0.0;
+    }
     return k;
 }
 
-__device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const double *f, bool fixed_dt,
-                                       double &dX_o, double &dY_o, double &dZ_o, double &dP_o) {
-    const double bx = f[A_BX], by = f[A_BY], bz = f[A_BZ];
-    const KBase k = kappa_base(a, s.p, bx, by, bz);
-    // kappa gradients, 2D branch (:2351-2388)
-    const double dbx_dx = f[A_DBXDX], dbx_dy = f[A_DBXDY], dby_dx = f[A_DBYDX], dby_dy = f[A_DBYDY];
-    const double db_dx = f[A_DBDX], db_dy = f[A_DBDY];
-    double dkdx = 0.0, dkdy = 0.0;
-    if (a.mag_dependency == 1) {
-        dkdx = db_dx * k.ib1 * (a.gamma_turb - 2.0);
-        dkdy = db_dy * k.ib1 * (a.gamma_turb - 2.0);
-    }
-    const double b = k.b, kpp = k.kpp, kperp = k.kperp;
-    const double ib2k = k.ib2, ib3k = k.ib3;
-    const double dkxx_dx = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2k +
-                           2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3k;
-    const double dkyy_dy = kperp * dkdy + kpp * dkdy * (by * by) * ib2k +
-                           2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3k;
-    const double dkxy_dx = kpp * dkdx * bx * by * ib2k +
-                           kpp * ((dbx_dx * by + bx * dby_dx) * ib2k - 2.0 * bx * by * db_dx * ib3k);
-    const double dkxy_dy = kpp * dkdy * bx * by * ib2k +
-                           kpp * ((dbx_dy * by + bx * dby_dy) * ib2k - 2.0 * bx * by * db_dy * ib3k);
-    // push_particle_2d (:3358-3606)
-    const double vx = f[A_VX], vy = f[A_VY];
-    const double dvx_dx = f[A_DVXDX], dvy_dy = f[A_DVYDY];
+// push_particle_2d (:3358-3606).
+__device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
+                                       bool fixed_dt, Delta &d) {
+    const double bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
-    const double dbz_dx = f[A_DBZDX], dbz_dy = f[A_DBZDY];
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
-    const double vdp = vdrift_prefactor(a, s.p);
-    const double vdx = vdp * (dbz_dy * ib2 - 2.0 * bz * db_dy * ib3);
-    const double vdy = vdp * (-(dbz_dx * ib2) + 2.0 * bz * db_dx * ib3);
+    const double vdp = vdrift_prefactor(a, s.p, 3);
+    const double vdx = vdp * (f.dbz_dy * ib2 - 2.0 * bz * f.db_dy * ib3);
+    const double vdy = vdp * (-(f.dbz_dx * ib2) + 2.0 * bz * f.db_dx * ib3);
     double vdz = 0.0;
     if (a.check_drift_2d)
-        vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
-    const double dx_dt = vx + vdx + dkxx_dx + dkxy_dy;
-    const double dy_dt = vy + vdy + dkxy_dx + dkyy_dy;
+        vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
+    const double dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy;
+    const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy;
     const double dz_dt = vdz;
-    const double divv = dvx_dx + dvy_dy;
+    const double divv = f.dvx_dx + f.dvy_dy;
     const double dp_dt = -(s.p * divv / 3.0);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
@@ -266,62 +366,30 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const doubl
     s.y = s.y + dY;
     s.z = s.z + dZ;
     s.t = s.t + s.dt;
-    dX_o = dX; dY_o = dY; dZ_o = dZ;
-    push_momentum(a, s, dp_dt, sdt, r[3], 2, dP_o);
+    // deltaz is local to push_particle_2d: the mover's copy stays 0.
+    d.x = dX; d.y = dY; d.z = 0.0; d.v = 0.0; d.mu = 0.0;
+    push_momentum(a, s, dp_dt, sdt, r[3], 2, d.p);
 }
 
-__device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const double *f, bool fixed_dt,
-                                       double &dX_o, double &dY_o, double &dZ_o, double &dP_o) {
-    const double bx = f[B_BX], by = f[B_BY], bz = f[B_BZ];
-    const KBase k = kappa_base(a, s.p, bx, by, bz);
-    // kappa gradients, 3D branch (:2389-2449); no 1/B in dkdx (reference).
-    const double dbx_dx = f[B_DBXDX], dbx_dy = f[B_DBXDY], dbx_dz = f[B_DBXDZ];
-    const double dby_dx = f[B_DBYDX], dby_dy = f[B_DBYDY], dby_dz = f[B_DBYDZ];
-    const double dbz_dx = f[B_DBZDX], dbz_dy = f[B_DBZDY], dbz_dz = f[B_DBZDZ];
-    const double db_dx = f[B_DBDX], db_dy = f[B_DBDY], db_dz = f[B_DBDZ];
-    double dkdx = 0.0, dkdy = 0.0, dkdz = 0.0;
-    if (a.mag_dependency == 1) {
-        dkdx = db_dx * (a.gamma_turb - 2.0);
-        dkdy = db_dy * (a.gamma_turb - 2.0);
-        dkdz = db_dz * (a.gamma_turb - 2.0);
-    }
-    const double b = k.b, kpp = k.kpp, kperp = k.kperp;
-    const double ib2k = k.ib2, ib3k = k.ib3;
-    const double dkxx_dx = kperp * dkdx + kpp * dkdx * (bx * bx) * ib2k +
-                           2.0 * kpp * bx * (dbx_dx * b - bx * db_dx) * ib3k;
-    const double dkyy_dy = kperp * dkdy + kpp * dkdy * (by * by) * ib2k +
-                           2.0 * kpp * by * (dby_dy * b - by * db_dy) * ib3k;
-    const double dkzz_dz = kperp * dkdz + kpp * dkdz * (bz * bz) * ib2k +
-                           2.0 * kpp * bz * (dbz_dz * b - bz * db_dz) * ib3k;
-    const double dkxy_dx = kpp * dkdx * bx * by * ib2k +
-                           kpp * ((dbx_dx * by + bx * dby_dx) * ib2k - 2.0 * bx * by * db_dx * ib3k);
-    const double dkxy_dy = kpp * dkdy * bx * by * ib2k +
-                           kpp * ((dbx_dy * by + bx * dby_dy) * ib2k - 2.0 * bx * by * db_dy * ib3k);
-    const double dkxz_dx = kpp * dkdx * bx * bz * ib2k +
-                           kpp * ((dbx_dx * bz + bx * dbz_dx) * ib2k - 2.0 * bx * bz * db_dx * ib3k);
-    const double dkxz_dz = kpp * dkdz * bx * bz * ib2k +
-                           kpp * ((dbx_dz * bz + bx * dbz_dz) * ib2k - 2.0 * bx * bz * db_dz * ib3k);
-    const double dkyz_dy = kpp * dkdy * by * bz * ib2k +
-                           kpp * ((dby_dy * bz + by * dbz_dy) * ib2k - 2.0 * by * bz * db_dy * ib3k);
-    const double dkyz_dz = kpp * dkdz * by * bz * ib2k +
-                           kpp * ((dby_dz * bz + by * dbz_dz) * ib2k - 2.0 * by * bz * db_dz * ib3k);
-    // push_particle_3d (:4625-4907)
-    const double vx = f[B_VX], vy = f[B_VY], vz = f[B_VZ];
+// push_particle_3d (:4625-4907).
+__device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
+                                       bool fixed_dt, Delta &d) {
+    const double bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
     const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
     const double bxyn = sqrt(bxn * bxn + byn * byn);
     const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
-    const double dvx_dx = f[B_DVXDX], dvy_dy = f[B_DVYDY], dvz_dz = f[B_DVZDZ];
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
-    const double vdp = vdrift_prefactor(a, s.p);
-    const double vdx = vdp * ((dbz_dy - dby_dz) * ib2 - 2.0 * (bz * db_dy - by * db_dz) * ib3);
-    const double vdy = vdp * ((dbx_dz - dbz_dx) * ib2 - 2.0 * (bx * db_dz - bz * db_dx) * ib3);
-    const double vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
-    const double dx_dt = vx + vdx + dkxx_dx + dkxy_dy + dkxz_dz;
-    const double dy_dt = vy + vdy + dkxy_dx + dkyy_dy + dkyz_dz;
-    const double dz_dt = vz + vdz + dkxz_dx + dkyz_dy + dkzz_dz;
-    const double divv = dvx_dx + dvy_dy + dvz_dz;
+    const double vdp = vdrift_prefactor(a, s.p, 3);
+    const double vdx = vdp * ((f.dbz_dy - f.dby_dz) * ib2 - 2.0 * (bz * f.db_dy - by * f.db_dz) * ib3);
+    const double vdy = vdp * ((f.dbx_dz - f.dbz_dx) * ib2 - 2.0 * (bx * f.db_dz - bz * f.db_dx) * ib3);
+    const double vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
+    const double dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
+    const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
+    const double dz_dt = f.vz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
+    const double divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
     const double dp_dt = -(s.p * divv / 3.0);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
@@ -353,8 +421,201 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const doubl
     s.y = s.y + dY;
     s.z = s.z + dZ;
     s.t = s.t + s.dt;
-    dX_o = dX; dY_o = dY; dZ_o = dZ;
-    push_momentum(a, s, dp_dt, sdt, r[3], 3, dP_o);
+    d.x = dX; d.y = dY; d.z = dZ; d.v = 0.0; d.mu = 0.0;
+    push_momentum(a, s, dp_dt, sdt, r[3], 3, d.p);
+}
+
+// calc_duu (:3116-3155) without delta-B or correlation length.
+__device__ __forceinline__ void calc_duu(const MoverArgs &a, const State &s, double b,
+                                         double div_bnorm, double divv, double bb_gradv,
+                                         double bv_gradv, double mu2, double &dmu_dt,
+                                         double &duu) {
+    double dm = s.v * div_bnorm + s.mu * divv - 3.0 * s.mu * bb_gradv - 2.0 * bv_gradv / s.v;
+    dm = dm * (1.0 - mu2) * 0.5;
+    const double h0 = (double)0.2f;
+    const double dtmp = pow(fabs(s.mu), a.gamma_turb - 1.0) + h0;
+    double u = a.duu0 * (1.0 - mu2) * dtmp;
+    double ud;
+    if (s.mu > 0.0)
+        ud = a.duu0 * (-(2.0 * s.mu * dtmp) + (1.0 - mu2) * pow(fabs(s.mu), a.gamma_turb - 2.0));
+    else if (s.mu < 0.0)
+        ud = a.duu0 * (-(2.0 * s.mu * dtmp) - (1.0 - mu2) * pow(fabs(s.mu), a.gamma_turb - 2.0));
+    else
+        ud = 0.0;
+    double norm = 1.0;
+    if (a.mag_dependency == 1) norm = norm * pow(b, 2.0 - a.gamma_turb);
+    if (a.momentum_dependency == 1) norm = norm * pow(s.p / a.p0, a.gamma_turb - 1.0);
+    ud = ud * norm;
+    u = u * norm;
+    dmu_dt = dm + ud;
+    duu = u;
+}
+
+// Adaptive step of the focused-transport pushes (:3850-3905, :5170-5230).
+template <int NDIM>
+__device__ __forceinline__ void ft_time_step(const MoverArgs &a, State &s, const Kap &k,
+                                             double dx_dt, double dy_dt, double dz_dt,
+                                             double dp_dt, double dmu_dt, double duu) {
+    const bool nonzero = dx_dt != 0.0 && dy_dt != 0.0 && (NDIM < 3 || dz_dt != 0.0) &&
+                         dp_dt != 0.0 && dmu_dt != 0.0;
+    if (nonzero) {
+        const double sk = (k.skperp > 0.0) ? k.skperp : k.skpara;
+        double q = 0.5 * a.dx / sk, m = q * q;
+        q = 0.5 * a.dy / sk; if (q * q < m) m = q * q;
+        if (NDIM == 3) { q = 0.5 * a.dz / sk; if (q * q < m) m = q * q; }
+        q = sk / dx_dt; if (q * q < m) m = q * q;
+        q = sk / dy_dt; if (q * q < m) m = q * q;
+        if (NDIM == 3) { q = sk / dz_dt; if (q * q < m) m = q * q; }
+        q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
+        q = (double)0.1f / fabs(dmu_dt); if (q < m) m = q;
+        q = 2.0 * duu / (dmu_dt * dmu_dt); if (q < m) m = q;
+        s.dt = m;
+    } else {
+        s.dt = a.dt_min;
+    }
+    if (s.dt < a.dt_min) s.dt = a.dt_min;
+    if (s.dt > a.dt_max) s.dt = a.dt_max;
+}
+
+// Shared tail of push_particle_2d_ft / push_particle_3d_ft (:3920-3963,
+// :5280-5323); r[2] drives momentum diffusion, r[3] pitch-angle scattering.
+template <int NDIM>
+__device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, double dX, double dY,
+                                             double dZ, double dp_dt, double dmu_dt, double duu,
+                                             double sdt, const double r[4], Delta &d) {
+    const double dpp = 0.0;
+    double dP = dp_dt * s.dt + r[2] * sqrt(2.0 * dpp) * sdt;
+    double dV = s.v * dP / s.p;
+    double dMu = dmu_dt * s.dt + r[3] * sqrt(2.0 * duu) * sdt;
+    s.x = s.x + dX;
+    s.y = s.y + dY;
+    s.z = s.z + dZ;
+    s.mu = s.mu + dMu;
+    s.t = s.t + s.dt;
+    const double mu_max = (double)0.99f;
+    if (s.mu > mu_max) {
+        dMu = mu_max - (s.mu - dMu);
+        s.mu = mu_max;
+    } else if (s.mu < -mu_max) {
+        dMu = -mu_max - (s.mu - dMu);
+        s.mu = -mu_max;
+    }
+    if (a.acc_region_flag == 1) {
+        if (in_acc_region(a, s, NDIM)) {
+            s.p = s.p + dP;
+            s.v = s.v + dV;
+        } else {
+            dP = 0.0;
+            dV = 0.0;
+        }
+    } else {
+        s.p = s.p + dP;
+        s.v = s.v + dV;
+    }
+    const double pfloor = 0.25 * a.p0;
+    if (s.p < pfloor) {
+        s.v = s.v - dV;
+        dV = s.v * 0.25 * a.p0 / s.p - s.v;
+        s.v = s.v + dV;
+        s.p = s.p - dP;
+        dP = pfloor - s.p;
+        s.p = pfloor;
+    }
+    // deltaz is local to push_particle_2d_ft: the mover's copy stays 0.
+    d.x = dX; d.y = dY; d.z = (NDIM == 3) ? dZ : 0.0; d.p = dP; d.v = dV; d.mu = dMu;
+}
+
+// push_particle_2d_ft (:3626-3964) and push_particle_3d_ft (:4930-5324).
+template <int NDIM>
+__device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
+                                        bool fixed_dt, Delta &d) {
+    const double bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    const double ib2 = ib * ib;
+    const double ib3 = ib * ib2;
+    const double vdp = vdrift_prefactor(a, s.p, 1);
+    const double mu2 = s.mu * s.mu;
+    const double muf1 = 0.5 * (1.0 - mu2);
+    const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
+    double kx, ky, kz, bdot_curvb, vdx, vdy, vdz = 0.0;
+    if (NDIM == 2) {
+        kx = bx * f.dbx_dx + by * f.dbx_dy;
+        ky = bx * f.dby_dx + by * f.dby_dy;
+        kz = bx * f.dbz_dx + by * f.dbz_dy;
+        bdot_curvb = bx * f.dbz_dy - by * f.dbz_dx + bz * (f.dby_dx - f.dbx_dy);
+        vdx = vdp * (muf1 * (-(bz * f.db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                     muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * f.db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                     muf1 * by * bdot_curvb * ib3);
+        if (a.check_drift_2d)
+            vdz = vdp * (muf1 * (bx * f.db_dy - by * f.db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                         muf1 * bz * bdot_curvb * ib3);
+    } else {
+        kx = bx * f.dbx_dx + by * f.dbx_dy + bz * f.dbx_dz;
+        ky = bx * f.dby_dx + by * f.dby_dy + bz * f.dby_dz;
+        kz = bx * f.dbz_dx + by * f.dbz_dy + bz * f.dbz_dz;
+        bdot_curvb = bx * (f.dbz_dy - f.dby_dz) + by * (f.dbx_dz - f.dbz_dx) + bz * (f.dby_dx - f.dbx_dy);
+        vdx = vdp * (muf1 * (by * f.db_dz - bz * f.db_dy) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                     muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * f.db_dx - bx * f.db_dz) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                     muf1 * by * bdot_curvb * ib3);
+        vdz = vdp * (muf1 * (bx * f.db_dy - by * f.db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                     muf1 * bz * bdot_curvb * ib3);
+    }
+    double vbx = s.v * s.mu * ib;
+    const double vby = vbx * by;
+    const double vbz = vbx * bz;
+    vbx = vbx * bx;
+    double dx_dt, dy_dt, dz_dt, divv, bb_gradv, bv_gradv, div_bnorm;
+    if (NDIM == 2) {
+        dx_dt = f.vx + vdx + vbx + k.dkxx_dx + k.dkxy_dy;
+        dy_dt = f.vy + vdy + vby + k.dkxy_dx + k.dkyy_dy;
+        dz_dt = vdz;
+        divv = f.dvx_dx + f.dvy_dy;
+        bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy) + by * (bx * f.dvy_dx + by * f.dvy_dy) +
+                    bz * (bx * f.dvz_dx + by * f.dvz_dy)) * ib2;
+        bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy) + by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy) +
+                    bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy)) * ib;
+        div_bnorm = -((bx * f.db_dx + by * f.db_dy) * ib2);
+    } else {
+        dx_dt = f.vx + vbx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
+        dy_dt = f.vy + vby + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
+        dz_dt = f.vz + vbz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
+        divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
+        bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy + bz * f.dvx_dz) +
+                    by * (bx * f.dvy_dx + by * f.dvy_dy + bz * f.dvy_dz) +
+                    bz * (bx * f.dvz_dx + by * f.dvz_dy + bz * f.dvz_dz)) * ib2;
+        bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy + f.vz * f.dvx_dz) +
+                    by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy + f.vz * f.dvy_dz) +
+                    bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy + f.vz * f.dvz_dz)) * ib;
+        div_bnorm = -((bx * f.db_dx + by * f.db_dy + bz * f.db_dz) * ib2);
+    }
+    const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s.mu * bv_gradv / s.v);
+    const double dp_dt = s.p * acc_rate;
+    double dmu_dt, duu;
+    calc_duu(a, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
+    if (!fixed_dt) ft_time_step<NDIM>(a, s, k, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    const double sdt = sqrt(s.dt);
+    double r[4];
+    noise4(a, s, r);
+    const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+    const double skperp = k.skperp;
+    double dX, dY, dZ;
+    if (NDIM == 2) {
+        // by and bx (not byn, bxn) in the second terms, as the reference.
+        const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
+        dX = dx_dt * s.dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
+        dY = dy_dt * s.dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+        dZ = dz_dt * s.dt;
+    } else {
+        const double bxyn = sqrt(bxn * bxn + byn * byn);
+        const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
+        dX = dx_dt * s.dt + (-(bxn * bzn * skperp * ibxyn * r[0]) - byn * skperp * ibxyn * r[1]) * sdt;
+        dY = dy_dt * s.dt + (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
+        dZ = dz_dt * s.dt + bxyn * skperp * r[0] * sdt;
+    }
+    push_ft_tail<NDIM>(a, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
 }
 
 template <int NDIM>
@@ -395,28 +656,41 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
     }
 }
 
-template <int NDIM>
-__device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, double &dX,
-                                        double &dY, double &dZ, double &dP) {
-    constexpr int NV = (NDIM == 2) ? 15 : 21;
-    double f[NV];
-    if (!interp<NDIM, NV>(a, s, f)) return false;
-    if (NDIM == 2) push2d(a, s, f, fixed_dt, dX, dY, dZ, dP);
-    else push3d(a, s, f, fixed_dt, dX, dY, dZ, dP);
-    if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) || !isfinite(s.t)) {
+template <int NDIM, bool FT>
+__device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, Delta &d) {
+    Fld f;
+    if (FT) {
+        double v[32];
+        if (!interp<NDIM, 32, 32>(a, a.full1, a.full2, s, v)) return false;
+        f = named_full(v);
+    } else {
+        constexpr int NV = (NDIM == 2) ? 15 : 21;
+        constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
+        double v[NV];
+        if (!interp<NDIM, NV, R>(a, a.rec1, a.rec2, s, v)) return false;
+        f = named_packed<NDIM>(v);
+    }
+    const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f);
+    if (FT) push_ft<NDIM>(a, s, f, k, fixed_dt, d);
+    else if (NDIM == 2) push2d(a, s, f, k, fixed_dt, d);
+    else push3d(a, s, f, k, fixed_dt, d);
+    if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) || !isfinite(s.t) ||
+        (FT && (!isfinite(s.v) || !isfinite(s.mu)))) {
         set_status(a.cnt, kStatusNonFinite);
         return false;
     }
     return true;
 }
 
-template <int NDIM>
+template <int NDIM, bool FT>
 __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
     Acc acc = {0, 0, 0, 0, 0};
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n) {
         State s;
         s.x = a.P.x[i]; s.y = a.P.y[i]; s.z = a.P.z[i]; s.p = a.P.p[i];
+        s.v = FT ? a.P.v[i] : 0.0;
+        s.mu = a.P.mu[i];
         s.t = a.P.t[i]; s.dt = a.P.dt[i]; s.w = a.P.weight[i];
         s.flag = a.P.count_flag[i];
         s.nsteps_pushed = a.P.nsteps_pushed[i];
@@ -424,7 +698,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
         s.tag_spl = a.P.tag_splitted[i];
         s.ctr = a.P.rng_ctr[i];
         const double t0 = a.t0, dt_fine = a.dt_fine;
-        double deltax = 0.0, deltay = 0.0, deltaz = 0.0, deltap = 0.0;
+        Delta dl = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         const double step = ceil((s.t - t0) / dt_fine);
         double dt_target = (step <= 0.0) ? dt_fine : step * dt_fine;
         if (dt_target > a.dtf) dt_target = a.dtf;
@@ -442,7 +716,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 negp_or_boundary<NDIM>(a, s, acc);
                 if (s.flag != 1) break;
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
-                if (!do_push<NDIM>(a, s, false, deltax, deltay, deltaz, deltap)) {
+                if (!do_push<NDIM, FT>(a, s, false, dl)) {
                     s.flag = 0; alive = false; break;
                 }
                 ++pushes;
@@ -450,16 +724,20 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
             }
             if (!alive) break;
             if ((s.t - t0) > dt_target && s.flag == 1) {
-                s.x = s.x - deltax;
-                s.y = s.y - deltay;
-                s.z = s.z - deltaz;
-                s.p = s.p - deltap;
+                s.x = s.x - dl.x;
+                s.y = s.y - dl.y;
+                s.z = s.z - dl.z;
+                s.p = s.p - dl.p;
+                if (FT) {
+                    s.v = s.v - dl.v;
+                    s.mu = s.mu - dl.mu;
+                }
                 s.t = s.t - s.dt;
                 const double dt_old = s.dt;
                 s.dt = t0 + dt_target - s.t;
                 if (s.dt > 0.0) {
                     s.nsteps_pushed = s.nsteps_pushed - 1;
-                    if (!do_push<NDIM>(a, s, true, deltax, deltay, deltaz, deltap)) {
+                    if (!do_push<NDIM, FT>(a, s, true, dl)) {
                         s.flag = 0; alive = false; break;
                     }
                     ++pushes;
@@ -476,6 +754,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
             boundary<NDIM>(a, s, a.xmin, a.xmax, a.ymin, a.ymax, a.zmin, a.zmax, acc);
         acc.steps = pushes;
         a.P.x[i] = s.x; a.P.y[i] = s.y; a.P.z[i] = s.z; a.P.p[i] = s.p;
+        if (FT) { a.P.v[i] = s.v; a.P.mu[i] = s.mu; }
         a.P.t[i] = s.t; a.P.dt[i] = s.dt;
         a.P.count_flag[i] = (int8_t)s.flag;
         a.P.nsteps_pushed[i] = s.nsteps_pushed;
@@ -501,8 +780,14 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     if (a.n <= 0) return cudaSuccess;
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
-    if (a.ndim == 2) mover_fp64_kernel<2><<<(unsigned)blocks, threads, 0, s>>>(a);
-    else mover_fp64_kernel<3><<<(unsigned)blocks, threads, 0, s>>>(a);
+    const bool ft = a.focused_transport != 0;
+    if (a.ndim == 2) {
+        if (ft) mover_fp64_kernel<2, true><<<(unsigned)blocks, threads, 0, s>>>(a);
+        else mover_fp64_kernel<2, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+    } else {
+        if (ft) mover_fp64_kernel<3, true><<<(unsigned)blocks, threads, 0, s>>>(a);
+        else mover_fp64_kernel<3, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 

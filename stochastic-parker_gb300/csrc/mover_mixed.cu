@@ -422,7 +422,9 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
                 // Undo the overshooting push, redo it with dt = target - t.
                 advance(q.cx, q.fx, -uX);
                 advance(q.cy, q.fy, -uY);
-                if (NDIM == 3) advance(q.cz, q.fz, -uZ); else z2 -= uZ;
+                // push_particle_2d's deltaz is local to it: the undo keeps the
+                // out-of-plane drift of the overshooting push.
+                if (NDIM == 3) advance(q.cz, q.fz, -uZ);
                 kadd(p, pc, -uP);
                 kadd(tau, tc, -dt);
                 const float dt_old = dt;

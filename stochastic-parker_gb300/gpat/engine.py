@@ -29,7 +29,7 @@ REFERENCE_DEFAULTS = dict(
     drift1=4.0e7, drift2=2.0e8, charge=-1, check_drift_2d=0,
     ndim=2, pbcx=0, pbcy=0, pbcz=0, npp_global=128,
     seed=0x5EED0001, noise=_abi.NOISE_UNIFORM, precision=_abi.PREC_FP64,
-    nptl_max=100_000, time_interp=0,
+    nptl_max=100_000, time_interp=0, duu0=10.0,
 )
 
 
@@ -258,7 +258,7 @@ class Engine:
         return self.counters().nptl_current
 
     # -- the mover path -----------------------------------------------------------
-    def particle_mover(self, focused_transport=False, nlgc=False, kperp_kpara=0.0,
+    def particle_mover(self, focused_transport=False, nlgc=False, kperp_kpara=0.01,
                        nsteps_interval=10, mhd_tframe=1, num_fine_steps=1,
                        dump_escaped_dist=False):
         self._check(self.lib.gpat_particle_mover(

@@ -29,8 +29,10 @@ def turbulent_frame_2d(n=64, seed=5, r=3.0, w=0.02):
 
 
 def run_pair(params_kw, cfg, frame, tstamps, inject, intervals=1, fine=1, frame2=None,
-             split=None, nthreads=0):
-    """Runs the engine and the oracle from the same injected particles."""
+             split=None, nthreads=0, mover_kw=None):
+    """Runs the engine and the oracle from the same injected particles;
+    mover_kw holds particle_mover's focused_transport / nlgc / kperp_kpara."""
+    mover_kw = mover_kw or {}
     prm = make_params(**params_kw)
     eng = Engine(prm, cfg, 0)
     eng.set_tstamps(tstamps)
@@ -48,9 +50,9 @@ def run_pair(params_kw, cfg, frame, tstamps, inject, intervals=1, fine=1, frame2
     parts = oracle.Particles(prm.nptl_max, start.arrays)
     cnt = oracle.OrcCounters()
     for k in range(intervals):
-        eng.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=fine)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=fine, **mover_kw)
         oracle.mover(oprm, ocfg, f1, parts, float(tstamps[k]), float(tstamps[k + 1] - tstamps[k]),
-                     num_fine_steps=fine, counters=cnt, f2=f2, nthreads=nthreads)
+                     num_fine_steps=fine, counters=cnt, f2=f2, nthreads=nthreads, **mover_kw)
         if split:
             eng.split_particle(*split)
             oracle.split(oprm, parts, split[0], split[1], cnt)

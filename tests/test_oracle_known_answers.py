@@ -76,12 +76,12 @@ def test_interp_reproduces_linear_field():
         assert abs(f[0] - (0.25 + 0.5 * x - 0.75 * y)) < 1e-6
 
 
-def _kappa(params, bx, by, bz, p=0.1, ndim=3):
+def _kappa(params, bx, by, bz, p=0.1, ndim=3, mu=0.5):
     prm = oracle.params_from(params)
     f = (C.c_double * 32)()
     f[4], f[5], f[6] = bx, by, bz
     k = (C.c_double * 22)()
-    oracle.load().orc_calc_spatial_diffusion_coefficients(C.byref(prm), p, f, k)
+    oracle.load().orc_calc_spatial_diffusion_coefficients(C.byref(prm), p, mu, f, k)
     return list(k)
 
 
