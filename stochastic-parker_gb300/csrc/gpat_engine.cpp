@@ -639,8 +639,8 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     if (!h) return GPAT_ERR_ARG;
     (void)dump_escaped_dist;   // the escaped distribution is always accumulated
     const bool mixed = h->prm.precision == GPAT_PREC_MIXED;
-    if ((focused_transport || nlgc) && mixed)
-        return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport and NLGC run in FP64 precision");
+    if (focused_transport && mixed)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport runs in FP64 precision");
     MoverArgs a;
     int rc = mover_args(h, mhd_tframe, nsteps_interval, num_fine_steps, a);
     if (rc) return rc;

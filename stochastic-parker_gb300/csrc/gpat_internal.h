@@ -85,6 +85,7 @@ struct MixedConsts {
     int nx, ny, nz;                    // cells in the exact box
     float dt_min, dt_max, dtf, inv_dtf;
     float ip0, pindex, gm2, kpara0, kret;
+    float kperp0, gm2_3, pindex_perp;  // NLGC: kpara0 kperp_kpara, (gamma-2)/3, (5-gamma)/3
     float vdq;                         // single-precision 1 / (3 charge)
     float d1p0, d2p0sq;                // drift1 p0, drift2 p0^2
     float pfloor;                      // 0.25 p0

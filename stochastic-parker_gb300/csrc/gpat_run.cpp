@@ -32,9 +32,14 @@ struct Options {
     int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
     double particle_v0 = 5.0, drift_param1 = 4e7, drift_param2 = 2e8;
+    // particle_mover's switches with the reference CLI's defaults
+    // (stochastic-mhd.f90:631-641, :935-937): NLGC on, fixed kperp/kpara off.
+    bool focused_transport = false, nlgc = true;
+    double kperp_kpara = 0.01, duu_init = 10.0;
     double ptl_box[6] = {0.0, 0.0, 0.0, 1.0, 1.0, 1.0};   // xmin ymin zmin xmax ymax zmax
     // engine options
     int precision = GPAT_PREC_MIXED, noise = GPAT_NOISE_UNIFORM, device = 0, bin_interval = 0;
+    bool precision_set = false;
     unsigned long long seed = 0x5EED0001ull;
     double shock_xpos = 0.5;
     bool conf_in_config_dir = true;
@@ -59,7 +64,8 @@ int parse(int argc, char **argv, Options &o) {
         {"-ys", "--ptl_ymin"}, {"-ye", "--ptl_ymax"}, {"-zs", "--ptl_zmin"}, {"-ze", "--ptl_zmax"},
         {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
         {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
-        {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}};
+        {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-ft", "--focused_transport"},
+        {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -102,7 +108,14 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--charge") o.charge = (int)d;
         else if (k == "--particle_v0") o.particle_v0 = d;
         else if (k == "--check_drift_2d") o.check_drift_2d = (int)d;
-        else if (k == "--precision") o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
+        else if (k == "--focused_transport") o.focused_transport = truthy(v);
+        else if (k == "--nlgc") o.nlgc = truthy(v);
+        else if (k == "--kperp_kpara") o.kperp_kpara = d;
+        else if (k == "--duu_init") o.duu_init = d;
+        else if (k == "--precision") {
+            o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
+            o.precision_set = true;
+        }
         else if (k == "--noise") o.noise = (v == "gauss" || v == "1") ? GPAT_NOISE_GAUSS : GPAT_NOISE_UNIFORM;
         else if (k == "--seed") o.seed = std::strtoull(v.c_str(), nullptr, 0);
         else if (k == "--device") o.device = (int)d;
@@ -141,6 +154,8 @@ int main(int argc, char **argv) {
         return prc == 1 ? 0 : 2;
     }
     if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
+    // Focused transport runs on the FP64 mover unless asked otherwise.
+    if (o.focused_transport && !o.precision_set) o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
     gpat_mhd_config_t cfg;
@@ -163,6 +178,7 @@ int main(int argc, char **argv) {
     p.nptl_max = o.nptl_max;
     p.time_interp = o.time_interp_flag;
     p.bin_interval = o.bin_interval;
+    p.duu0 = o.duu_init;
     CHECK(gpat_create(&p, &cfg, o.device, &h));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
 
@@ -226,7 +242,8 @@ int main(int argc, char **argv) {
                                                         o.power_index));
         }
         if (tf == o.t_start + 1) CHECK(diagnostics(o.t_start));
-        CHECK(gpat_particle_mover(h, 0, 0, 0.0, o.nsteps_interval, ct, o.num_fine_steps, 0));
+        CHECK(gpat_particle_mover(h, o.focused_transport, o.nlgc, o.kperp_kpara, o.nsteps_interval,
+                                  ct, o.num_fine_steps, 0));
         if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
         CHECK(diagnostics(tf));
         if (o.time_interp_flag == 1) CHECK(gpat_copy_fields(h));

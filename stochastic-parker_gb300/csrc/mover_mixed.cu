@@ -33,6 +33,9 @@ MixedConsts make_mixed_consts(const MoverArgs &a) {
     k.dtf = (float)a.dtf; k.inv_dtf = (float)(1.0 / a.dtf);
     k.ip0 = (float)(1.0 / a.p0); k.pindex = (float)a.pindex; k.gm2 = (float)(a.gamma_turb - 2.0);
     k.kpara0 = (float)a.kpara0; k.kret = (float)a.kret;
+    k.kperp0 = (float)(a.kpara0 * a.kperp_kpara);
+    k.gm2_3 = (float)((a.gamma_turb - 2.0) / 3.0);
+    k.pindex_perp = (float)((5.0 - a.gamma_turb) / 3.0);
     k.vdq = 1.0f / (float)(3 * a.charge);
     k.d1p0 = (float)(a.drift1 * a.p0);
     k.d2p0sq = (float)(a.drift2 * (a.p0 * a.p0));
@@ -207,12 +210,16 @@ __device__ __forceinline__ bool in_acc_region(const MixedConsts &k, const Pos &q
 
 // One push: interpolation, kappa, drift, dt, noise.  Outputs increments in
 // cell units (dX, dY, dZ), the momentum increment dp (before the floor) and,
-// unless fixed, the adaptive dt.
-template <int NDIM>
+// unless fixed, the adaptive dt.  NLGC: kperp from
+// calc_spatial_diffusion_coefficients_nlgc (particle_module.f90:2464-2771),
+// kpara0 kperp_kpara |B|^((gamma-2)/3) (p/p0)^((5-gamma)/3) mu^2, with the
+// gradient terms T_i = kperp dkperp_i, A_i = kpara dkpara_i - kperp dkperp_i
+// in place of kperp dk_i and kpp dk_i.
+template <int NDIM, bool NLGC>
 __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, const Pos &q,
-                                     float p, float rt, bool fixed, float &dt, uint32_t ctr,
-                                     uint32_t ti, uint32_t ts, float &dX, float &dY, float &dZ,
-                                     float &dp) {
+                                     float p, float mu, float rt, bool fixed, float &dt,
+                                     uint32_t ctr, uint32_t ti, uint32_t ts, float &dX, float &dY,
+                                     float &dZ, float &dp) {
     constexpr int NV = (NDIM == 2) ? 15 : 21;
     float f[NV];
     if (!interp<NDIM, NV>(a, q, rt, f)) return false;
@@ -226,11 +233,17 @@ __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, c
     const float b = b2 * ib;
     const float ib1 = bzero ? 1.0f : ib;           // kappa's guard uses 1
     const float ib2 = ib1 * ib1, ib3 = ib1 * ib2;
-    float knorm = 1.0f;
-    if (a.mag_dependency == 1) knorm = exp2f(k.gm2 * __log2f(b));
-    if (a.momentum_dependency == 1) knorm *= exp2f(k.pindex * __log2f(p * k.ip0));
+    float knorm = 1.0f, knorm_perp = 1.0f;
+    const float lb = (a.mag_dependency == 1) ? __log2f(b) : 0.0f;
+    const float lp = (a.momentum_dependency == 1) ? __log2f(p * k.ip0) : 0.0f;
+    if (a.mag_dependency == 1) knorm = exp2f(k.gm2 * lb);
+    if (a.momentum_dependency == 1) knorm *= exp2f(k.pindex * lp);
+    if (NLGC) {
+        if (a.mag_dependency == 1) knorm_perp = exp2f(k.gm2_3 * lb);
+        if (a.momentum_dependency == 1) knorm_perp *= exp2f(k.pindex_perp * lp);
+    }
     const float kpara = k.kpara0 * knorm;
-    const float kperp = kpara * k.kret;
+    const float kperp = NLGC ? k.kperp0 * knorm_perp * (mu * mu) : kpara * k.kret;
     const float kpp = kpara - kperp;
     const float skpara = fsqrt(2.0f * kpara), skperp = fsqrt(2.0f * kperp), skpp = fsqrt(2.0f * kpp);
     const float ip = __fdividef(1.0f, p);
@@ -243,11 +256,17 @@ __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, c
         const float dbz_dx = f[11], dbz_dy = f[12], db_dx = f[13], db_dy = f[14];
         float dkdx = 0.0f, dkdy = 0.0f;
         if (a.mag_dependency == 1) { dkdx = db_dx * ib1 * k.gm2; dkdy = db_dy * ib1 * k.gm2; }
+        // T_i and A_i / B^2 of the gradient terms (T_i = kperp dk_i, A_i = kpp dk_i
+        // without NLGC; dkperp_i = dk_i / 3 with it)
+        float tx = kperp * dkdx, ty = kperp * dkdy;
+        if (NLGC) { tx *= (1.0f / 3.0f); ty *= (1.0f / 3.0f); }
+        const float gx = (NLGC ? kpara * dkdx - tx : kpp * dkdx) * ib2;
+        const float gy = (NLGC ? kpara * dkdy - ty : kpp * dkdy) * ib2;
         const float ax = kpp * ib2, a3 = 2.0f * kpp * ib3;
-        const float dkxx_dx = kperp * dkdx + ax * dkdx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
-        const float dkyy_dy = kperp * dkdy + ax * dkdy * by * by + a3 * by * (dby_dy * b - by * db_dy);
-        const float dkxy_dx = ax * (dkdx * bx * by + dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
-        const float dkxy_dy = ax * (dkdy * bx * by + dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
+        const float dkxx_dx = tx + gx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
+        const float dkyy_dy = ty + gy * by * by + a3 * by * (dby_dy * b - by * db_dy);
+        const float dkxy_dx = gx * bx * by + ax * (dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
+        const float dkxy_dy = gy * bx * by + ax * (dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
         const float vdx = vdp * (dbz_dy * jb2 - 2.0f * bz * db_dy * jb3);
         const float vdy = vdp * (2.0f * bz * db_dx * jb3 - dbz_dx * jb2);
         if (a.check_drift_2d)
@@ -261,17 +280,26 @@ __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, c
         const float dbz_dx = f[15], dbz_dy = f[16], dbz_dz = f[17];
         const float db_dx = f[18], db_dy = f[19], db_dz = f[20];
         float dkdx = 0.0f, dkdy = 0.0f, dkdz = 0.0f;
-        if (a.mag_dependency == 1) { dkdx = db_dx * k.gm2; dkdy = db_dy * k.gm2; dkdz = db_dz * k.gm2; }
+        // the fixed-ratio 3D branch has no 1/B factor (:2406-2408); NLGC has
+        if (a.mag_dependency == 1) {
+            const float s = NLGC ? ib1 * k.gm2 : k.gm2;
+            dkdx = db_dx * s; dkdy = db_dy * s; dkdz = db_dz * s;
+        }
+        float tx = kperp * dkdx, ty = kperp * dkdy, tz = kperp * dkdz;
+        if (NLGC) { tx *= (1.0f / 3.0f); ty *= (1.0f / 3.0f); tz *= (1.0f / 3.0f); }
+        const float gx = (NLGC ? kpara * dkdx - tx : kpp * dkdx) * ib2;
+        const float gy = (NLGC ? kpara * dkdy - ty : kpp * dkdy) * ib2;
+        const float gz = (NLGC ? kpara * dkdz - tz : kpp * dkdz) * ib2;
         const float ax = kpp * ib2, a3 = 2.0f * kpp * ib3;
-        const float dkxx_dx = kperp * dkdx + ax * dkdx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
-        const float dkyy_dy = kperp * dkdy + ax * dkdy * by * by + a3 * by * (dby_dy * b - by * db_dy);
-        const float dkzz_dz = kperp * dkdz + ax * dkdz * bz * bz + a3 * bz * (dbz_dz * b - bz * db_dz);
-        const float dkxy_dx = ax * (dkdx * bx * by + dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
-        const float dkxy_dy = ax * (dkdy * bx * by + dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
-        const float dkxz_dx = ax * (dkdx * bx * bz + dbx_dx * bz + bx * dbz_dx) - a3 * bx * bz * db_dx;
-        const float dkxz_dz = ax * (dkdz * bx * bz + dbx_dz * bz + bx * dbz_dz) - a3 * bx * bz * db_dz;
-        const float dkyz_dy = ax * (dkdy * by * bz + dby_dy * bz + by * dbz_dy) - a3 * by * bz * db_dy;
-        const float dkyz_dz = ax * (dkdz * by * bz + dby_dz * bz + by * dbz_dz) - a3 * by * bz * db_dz;
+        const float dkxx_dx = tx + gx * bx * bx + a3 * bx * (dbx_dx * b - bx * db_dx);
+        const float dkyy_dy = ty + gy * by * by + a3 * by * (dby_dy * b - by * db_dy);
+        const float dkzz_dz = tz + gz * bz * bz + a3 * bz * (dbz_dz * b - bz * db_dz);
+        const float dkxy_dx = gx * bx * by + ax * (dbx_dx * by + bx * dby_dx) - a3 * bx * by * db_dx;
+        const float dkxy_dy = gy * bx * by + ax * (dbx_dy * by + bx * dby_dy) - a3 * bx * by * db_dy;
+        const float dkxz_dx = gx * bx * bz + ax * (dbx_dx * bz + bx * dbz_dx) - a3 * bx * bz * db_dx;
+        const float dkxz_dz = gz * bx * bz + ax * (dbx_dz * bz + bx * dbz_dz) - a3 * bx * bz * db_dz;
+        const float dkyz_dy = gy * by * bz + ax * (dby_dy * bz + by * dbz_dy) - a3 * by * bz * db_dy;
+        const float dkyz_dz = gz * by * bz + ax * (dby_dz * bz + by * dbz_dz) - a3 * by * bz * db_dz;
         const float vdx = vdp * ((dbz_dy - dby_dz) * jb2 - 2.0f * (bz * db_dy - by * db_dz) * jb3);
         const float vdy = vdp * ((dbx_dz - dbz_dx) * jb2 - 2.0f * (bx * db_dz - bz * db_dx) * jb3);
         const float vdz = vdp * ((dby_dx - dbx_dy) * jb2 - 2.0f * (by * db_dx - bx * db_dy) * jb3);
@@ -332,7 +360,7 @@ __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, c
 #define GPAT_MIXED_MINB_3D 5
 #endif
 
-template <int NDIM>
+template <int NDIM, bool NLGC>
 __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIXED_MINB_3D)
     mover_mixed_kernel(const MoverArgs a, const MixedConsts k) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,6 +397,7 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
         int nsp = a.P.nsteps_pushed[i];
         uint32_t ctr = a.P.rng_ctr[i];
         const uint32_t ti = (uint32_t)a.P.tag_injected[i], ts = (uint32_t)a.P.tag_splitted[i];
+        const float mu = NLGC ? (float)a.P.mu[i] : 0.0f;
 
         const double stepd = ceil(tau_in / a.dt_fine);
         double target_d = (stepd <= 0.0) ? a.dt_fine : stepd * a.dt_fine;
@@ -396,7 +425,8 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
                 const float pe = p - pc;
                 float dp;
-                if (!push<NDIM>(a, k, q, pe, tau * k.inv_dtf, false, dt, ctr, ti, ts, uX, uY, uZ, dp)) {
+                if (!push<NDIM, NLGC>(a, k, q, pe, mu, tau * k.inv_dtf, false, dt, ctr, ti, ts, uX,
+                                      uY, uZ, dp)) {
                     flag = 0; alive = false; break;
                 }
                 ++ctr;
@@ -433,8 +463,8 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
                     nsp = nsp - 1;
                     const float pe = p - pc;
                     float dp;
-                    if (!push<NDIM>(a, k, q, pe, tau * k.inv_dtf, true, dtr, ctr, ti, ts, uX, uY,
-                                    uZ, dp)) {
+                    if (!push<NDIM, NLGC>(a, k, q, pe, mu, tau * k.inv_dtf, true, dtr, ctr, ti, ts,
+                                          uX, uY, uZ, dp)) {
                         flag = 0; alive = false; break;
                     }
                     ++ctr;
@@ -495,8 +525,14 @@ cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_
     if (a.n <= 0) return cudaSuccess;
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
-    if (a.ndim == 2) mover_mixed_kernel<2><<<(unsigned)blocks, threads, 0, s>>>(a, c);
-    else mover_mixed_kernel<3><<<(unsigned)blocks, threads, 0, s>>>(a, c);
+    const unsigned g = (unsigned)blocks;
+    if (a.ndim == 2) {
+        if (a.nlgc) mover_mixed_kernel<2, true><<<g, threads, 0, s>>>(a, c);
+        else mover_mixed_kernel<2, false><<<g, threads, 0, s>>>(a, c);
+    } else {
+        if (a.nlgc) mover_mixed_kernel<3, true><<<g, threads, 0, s>>>(a, c);
+        else mover_mixed_kernel<3, false><<<g, threads, 0, s>>>(a, c);
+    }
     return cudaGetLastError();
 }
 

@@ -36,12 +36,13 @@ def _dataset(tmp_path: Path):
     return w, data, out
 
 
-def _run_driver(tmp_path, data, out, precision="fp64"):
+def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
     exe = build.build_driver()
     cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
            "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
            "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
-           "--precision", precision, "--seed", str(SEED)]
+           "--precision", precision, "--seed", str(SEED), "-ft", ".true." if ft else ".false.",
+           "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0"]
     return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
 
 
@@ -68,9 +69,10 @@ def test_driver_usage_without_gpu(engine_lib):
 
 
 @pytest.mark.gpu
-def test_driver_matches_python_sequence(tmp_path):
+@pytest.mark.parametrize("ft,nlgc", [(False, False), (True, True)])
+def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
     w, data, out = _dataset(tmp_path)
-    r = _run_driver(tmp_path, data, out)
+    r = _run_driver(tmp_path, data, out, ft=ft, nlgc=nlgc)
     assert r.returncode == 0, r.stderr
     quick = (out / "quick.dat").read_text().splitlines()
     assert len(quick) == 5 and quick[0].split()[0] == "iframe"
@@ -78,7 +80,7 @@ def test_driver_matches_python_sequence(tmp_path):
 
     # The same calls from Python.
     prm = make_params(**dict(w.params, npp_global=64, nptl_max=40000, seed=SEED, precision=0,
-                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1))
+                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1, duu0=3.0))
     eng = Engine(prm, w.mhd_config, 0)
     eng.calc_tstamps_mhd(0, 3)
     eng.read_field_data(data / "mhd_data_0000", 0)
@@ -87,7 +89,8 @@ def test_driver_matches_python_sequence(tmp_path):
         eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
         eng.calc_fields_gradients(0)
         eng.inject_particles_at_x(2000, 0.5, 1e-7, 1, 1.0, tf)
-        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1,
+                           focused_transport=ft, nlgc=nlgc, kperp_kpara=0.05)
         eng.split_particle(2.72, 2.0, 10)
     f, c = eng.calc_particle_distributions()
     assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)

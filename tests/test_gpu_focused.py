@@ -156,3 +156,47 @@ def test_focused_transport_needs_fp64():
     with pytest.raises(GPATError, match="UNSUPPORTED"):
         eng.particle_mover(focused_transport=True)
     eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nlgc_diffusion_covariance(precision):
+    """NLGC kperp = kpara0 kperp_kpara mu^2: two groups of particles with
+    different mu spread with covariance 2 K(mu) t in a uniform oblique B."""
+    import math
+    n = 64
+    cfg = make_mhd_config(n, n, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.05)
+    th = math.radians(35.0)
+    z = np.zeros((n + 4, n + 4))
+    frame = fields.assemble_frame(z, z, z, z + 1, z + math.cos(th), z + math.sin(th), z)[None]
+    kpara, kk, T = 1e-3, 0.3, 0.05
+    N = 100000 if precision else 20000
+    prm = make_params(ndim=2, kpara0=kpara, momentum_dependency=0, dt_min_rel=0.01, pbcx=0,
+                      pbcy=0, p0=0.1, precision=precision, nptl_max=N, seed=3)
+    eng = Engine(prm, cfg, 0)
+    eng.set_tstamps([0.0, T])
+    eng.set_fields(frame, 0)
+    eng.calc_fields_gradients(0)
+    from gpat.engine import ParticleSet
+    ps = ParticleSet.empty(N)
+    a = ps.arrays
+    a["x"][:] = 0.5
+    a["y"][:] = 0.5
+    a["p"][:] = 0.1
+    a["weight"][:] = 1.0
+    a["count_flag"][:] = 1
+    a["tag_splitted"][:] = 1
+    a["tag_injected"][:] = np.arange(N, dtype=np.int32)
+    a["mu"][:] = np.where(np.arange(N) % 2 == 0, 0.25, 0.9)
+    eng.put_particles(ps)
+    eng.particle_mover(mhd_tframe=1, nlgc=True, kperp_kpara=kk)
+    out = eng.get_particles()
+    b = np.array([math.cos(th), math.sin(th)])
+    for mu in (0.25, 0.9):
+        sel = out["mu"] == mu
+        m = int(sel.sum())
+        d = np.stack([out["x"][sel] - 0.5, out["y"][sel] - 0.5])
+        cov = d @ d.T / m
+        kperp = kpara * kk * mu * mu
+        K = kperp * np.eye(2) + (kpara - kperp) * np.outer(b, b)
+        np.testing.assert_allclose(cov, 2 * K * T, atol=5 * math.sqrt(2.0 / m) * 2 * K.max() * T)
+    eng.close()
