@@ -80,9 +80,11 @@ typedef struct gpat_params {
     int32_t precision;          /* GPAT_PREC_*                                 */
     int64_t nptl_max;           /* particle capacity (init_particles)          */
     int32_t time_interp;        /* 1: two field frames, linear in time         */
-    /* Options of the reference that this engine rejects with
-     * GPAT_ERR_UNSUPPORTED when non-zero: dpp_wave, dpp_shear, deltab_flag,
-     * correlation_flag, include_3rd_dim, spherical_coord, nonuniform_grid. */
+    /* dpp_wave / dpp_shear: momentum diffusion by wave scattering and flow
+     * shear (set_dpp_params, particle_module.f90:255-272), FP64 precision
+     * only.  Options of the reference that this engine rejects with
+     * GPAT_ERR_UNSUPPORTED when non-zero: deltab_flag, correlation_flag,
+     * include_3rd_dim, spherical_coord, nonuniform_grid. */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of
@@ -90,10 +92,11 @@ typedef struct gpat_params {
      * default of 128; negative: bin once per call).  Results are the same
      * for any value; it only changes memory locality. */
     int32_t bin_interval;
-    int32_t reserved;
+    int32_t weak_scattering;    /* flow-shear Dpp in the weak-scattering regime */
     /* Focused transport: pitch-angle diffusion coefficient at p0 (duu_init of
      * the reference CLI, stochastic-mhd.f90:935-937, default 10). */
     double duu0;
+    double tau0;                /* scattering time at p0 (tau0_scattering, default 1) */
 } gpat_params_t;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays.  rng_ctr
@@ -187,8 +190,9 @@ int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity
  * mover cycle (:1481-1833), remove_particles, boundary pass on the exact
  * box, remove_particles.  focused_transport selects push_particle_*_ft
  * (mu and v become state; gpat_params_t.duu0 sets D_mumu), nlgc selects
- * calc_spatial_diffusion_coefficients_nlgc with kperp_kpara; both need
- * GPAT_PREC_FP64.  mhd_tframe indexes tstamps (t0 = tstamps(mhd_tframe)). */
+ * calc_spatial_diffusion_coefficients_nlgc with kperp_kpara (both
+ * precisions); focused transport needs GPAT_PREC_FP64.  mhd_tframe indexes
+ * tstamps (t0 = tstamps(mhd_tframe)). */
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc,
                         double kperp_kpara, int nsteps_interval, int mhd_tframe,
                         int num_fine_steps, int dump_escaped_dist);

@@ -407,12 +407,58 @@ static double vdrift_prefactor(const orc_params *pr, double p)
     return (double)q / sqrt(t1 * t1 + t2 * t2);
 }
 
+/* calc_dpp_wave_scattering (:2918-2931) and calc_dpp_flow_shear
+ * (:2946-2979) as called by the pushes (:3479-3496, :4764-4788): they add
+ * to dp_dt and return dpp.  Shear tensor sigma_ij = (dvi/dj + dvj/di)/2 -
+ * delta_ij divv/3 (dvz/dz = 0 and no xz, yz terms in 2D). */
+static double dpp_terms(const orc_params *pr, double p, const double *f, const double *kap,
+                        double b, double divv, double *dp_dt)
+{
+    double dpp = 0.0;
+    if (pr->dpp_wave) {
+        const double va = b / sqrt(f[3]);
+        if (pr->momentum_dependency == 1)
+            *dp_dt = *dp_dt + (8.0 * p / (27.0 * kap[K_KPARA])) * (va * va);
+        else
+            *dp_dt = *dp_dt + (4.0 * p / (9.0 * kap[K_KPARA])) * (va * va);
+        dpp = dpp + (p * va) * (p * va) / (9.0 * kap[K_KPARA]);
+    }
+    if (pr->dpp_shear) {
+        const int d3 = (pr->ndim == 3);
+        const double sxx = f[8] - divv / 3.0;
+        const double syy = f[12] - divv / 3.0;
+        const double szz = d3 ? f[16] - divv / 3.0 : -(divv / 3.0);
+        const double sxy = (f[9] + f[11]) / 2.0;
+        const double sxz = d3 ? (f[10] + f[14]) / 2.0 : 0.0;
+        const double syz = d3 ? (f[13] + f[15]) / 2.0 : 0.0;
+        const double bx = f[4], by = f[5], bz = f[6];
+        double gshear;
+        if (pr->weak_scattering) {
+            const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+            double bbs = sxx * (bx * bx) + syy * (by * by) + szz * (bz * bz) +
+                         2.0 * (sxy * bx * by + sxz * bx * bz + syz * by * bz);
+            bbs = bbs * ib * ib;
+            gshear = bbs * bbs / 5.0;
+        } else {
+            gshear = 2.0 * (sxx * sxx + syy * syy + szz * szz +
+                            2.0 * (sxy * sxy + sxz * sxz + syz * syz)) / 15.0;
+        }
+        if (gshear > 0.0) {
+            const double kn = kap[K_KNORM_PARA];
+            const double p0f = pow(pr->p0, 2.0 - pr->pindex);
+            *dp_dt = *dp_dt + (2.0 + pr->pindex) * gshear * pr->tau0 * kn *
+                     pow(p, pr->pindex - 1.0) * p0f;
+            dpp = dpp + gshear * pr->tau0 * kn * pow(p, pr->pindex) * p0f;
+        }
+    }
+    return dpp;
+}
+
 /* Momentum update, acceleration-region mask and the 0.25 p0 floor, shared
  * by the 2D and 3D pushes (:3591-3605, :4885-4906). */
-static void push_momentum(const mover_ctx *c, ptl_state *s, double dp_dt, double sdt,
+static void push_momentum(const mover_ctx *c, ptl_state *s, double dp_dt, double dpp, double sdt,
                           double ranp, double *deltap)
 {
-    const double dpp = 0.0;
     double dP = dp_dt * s->dt + ranp * sqrt(2.0 * dpp) * sdt;
     if (c->pr->acc_region_flag == 1) {
         if (in_acc_region(c, s)) s->p = s->p + dP;
@@ -454,7 +500,8 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY];
     const double dz_dt = vdz;
     const double divv = dvx_dx + dvy_dy;
-    const double dp_dt = -(s->p * divv / 3.0);
+    double dp_dt = -(s->p * divv / 3.0);
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
@@ -485,7 +532,7 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     /* deltaz is local to push_particle_2d: the mover's deltaz stays 0, so an
      * undone push keeps its out-of-plane drift. */
     d[0] = dX; d[1] = dY; d[2] = 0.0; d[4] = 0.0; d[5] = 0.0;
-    push_momentum(c, s, dp_dt, sdt, r[3], &d[3]);
+    push_momentum(c, s, dp_dt, dpp, sdt, r[3], &d[3]);
 }
 
 /* push_particle_3d, Cartesian uniform grid: particle_module.f90:4625-4907. */
@@ -514,7 +561,8 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
     const double dz_dt = vz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
     const double divv = dvx_dx + dvy_dy + dvz_dz;
-    const double dp_dt = -(s->p * divv / 3.0);
+    double dp_dt = -(s->p * divv / 3.0);
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
@@ -546,7 +594,7 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     s->z = s->z + dZ;
     s->t = s->t + s->dt;
     d[0] = dX; d[1] = dY; d[2] = dZ; d[4] = 0.0; d[5] = 0.0;
-    push_momentum(c, s, dp_dt, sdt, r[3], &d[3]);
+    push_momentum(c, s, dp_dt, dpp, sdt, r[3], &d[3]);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -594,10 +642,9 @@ static double vdrift_prefactor_ft(const orc_params *pr, double p)
  * acceleration-region mask and the 0.25 p0 floor (:3920-3963,
  * :5280-5323).  r[2] drives momentum diffusion, r[3] pitch-angle. */
 static void push_ft_tail(const mover_ctx *c, ptl_state *s, double dX, double dY, double dZ,
-                         double dp_dt, double dmu_dt, double duu, double sdt,
+                         double dp_dt, double dpp, double dmu_dt, double duu, double sdt,
                          const double r[4], double d[6])
 {
-    const double dpp = 0.0;
     double dP = dp_dt * s->dt + r[2] * sqrt(2.0 * dpp) * sdt;
     double dV = s->v * dP / s->p;
     double dMu = dmu_dt * s->dt + r[3] * sqrt(2.0 * duu) * sdt;
@@ -710,7 +757,8 @@ static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
                              by * (vx * dvy_dx + vy * dvy_dy) +
                              bz * (vx * dvz_dx + vy * dvz_dy)) * ib;
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
-    const double dp_dt = s->p * acc_rate;
+    double dp_dt = s->p * acc_rate;
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double div_bnorm = -((bx * db_dx + by * db_dy) * ib2);
     double dmu_dt, duu, duu_du;
     calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
@@ -724,7 +772,7 @@ static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double dX = dx_dt * s->dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
     const double dY = dy_dt * s->dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
     const double dZ = dz_dt * s->dt;
-    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
+    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
     d[2] = 0.0;   /* deltaz is local to push_particle_2d_ft, as in push_2d */
 }
 
@@ -777,7 +825,8 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
                              by * (vx * dvy_dx + vy * dvy_dy + vz * dvy_dz) +
                              bz * (vx * dvz_dx + vy * dvz_dy + vz * dvz_dz)) * ib;
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
-    const double dp_dt = s->p * acc_rate;
+    double dp_dt = s->p * acc_rate;
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double div_bnorm = -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
     double dmu_dt, duu, duu_du;
     calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
@@ -791,7 +840,7 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double dY = dy_dt * s->dt +
         (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
     const double dZ = dz_dt * s->dt + bxyn * skperp * r[0] * sdt;
-    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
+    push_ft_tail(c, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
 /* particle_boundary_condition on a single rank: particle_module.f90:1984-2129.

@@ -52,9 +52,11 @@ typedef struct orc_params {
     int32_t noise;      /* 0: (2u-1)*sqrt(3) as the reference; 1: Gaussian */
     int32_t focused_transport;  /* particle_mover's focused_transport          */
     int32_t nlgc;               /* particle_mover's nlgc                       */
-    int32_t reserved;
+    int32_t dpp_wave;           /* set_dpp_params (:255-272)                   */
     double duu0;                /* set_duu_params (:279-283)                   */
     double kperp_kpara;         /* particle_mover's kperp_kpara                */
+    int32_t dpp_shear, weak_scattering;
+    double tau0;
 } orc_params;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the

@@ -37,13 +37,14 @@ class OrcParams(C.Structure):
         ("check_drift_2d", i32), ("ndim", i32), ("pbcx", i32), ("pbcy", i32), ("pbcz", i32),
         ("npp_global", i32),
         ("seed", u64),
-        ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("reserved", i32),
-        ("duu0", d), ("kperp_kpara", d),
+        ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("dpp_wave", i32),
+        ("duu0", d), ("kperp_kpara", d), ("dpp_shear", i32), ("weak_scattering", i32),
+        ("tau0", d),
     ]
 
 # Mover arguments of the reference carried in OrcParams rather than in the
 # engine's parameter block.
-_MOVER_ARGS = ("focused_transport", "nlgc", "kperp_kpara", "reserved")
+_MOVER_ARGS = ("focused_transport", "nlgc", "kperp_kpara")
 
 
 FIELDS = [

@@ -182,6 +182,10 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.full1 = h->full[0];
     a.full2 = p.time_interp ? h->full[1] : h->full[0];
     a.duu0 = p.duu0;
+    a.dpp_wave = p.dpp_wave;
+    a.dpp_shear = p.dpp_shear;
+    a.weak_scattering = p.weak_scattering;
+    a.tau0 = p.tau0;
     a.time_interp = p.time_interp;
     a.ndim = p.ndim;
     a.nxg = h->nxg; a.nyg = h->nyg; a.nzg = h->nzg;
@@ -348,9 +352,10 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     *out = nullptr;
     const gpat_params_t &p = *params;
     if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
-    if (p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag || p.include_3rd_dim ||
-        p.spherical_coord || p.nonuniform_grid)
+    if (p.deltab_flag || p.correlation_flag || p.include_3rd_dim || p.spherical_coord ||
+        p.nonuniform_grid)
         return GPAT_ERR_UNSUPPORTED;
+    if ((p.dpp_wave || p.dpp_shear) && p.precision != GPAT_PREC_FP64) return GPAT_ERR_UNSUPPORTED;
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
     if (p.noise != GPAT_NOISE_UNIFORM && p.noise != GPAT_NOISE_GAUSS) return GPAT_ERR_ARG;
     if (p.nptl_max < 1 || p.nptl_max > (int64_t)2000000000) return GPAT_ERR_ARG;

@@ -72,6 +72,10 @@ struct MoverArgs {
     // Focused transport interpolates all 32 variables from full1/full2.
     int focused_transport, nlgc;
     double kperp_kpara, duu0;
+    // Momentum diffusion (set_dpp_params); the FP64 mover then reads the full
+    // 32-variable records too.
+    int dpp_wave, dpp_shear, weak_scattering;
+    double tau0;
     const float *full1, *full2;
     DevCounters *cnt;
 };

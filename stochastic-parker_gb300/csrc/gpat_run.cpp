@@ -9,7 +9,11 @@
 // columns (diagnostics.f90:116-170) and, per frame, fdists_XXXX.dat: int32
 // npp, npp + 1 float64 bin edges, npp float64 weighted counts, npp uint64
 // particle counts (the fglobal / pbins_edges_global datasets of
-// fdists_XXXX.h5, without HDF5).
+// fdists_XXXX.h5, without HDF5).  With -pd 1, particles_XXXX.dat per frame,
+// and restart/particles_XXXX.dat at t_end always (dump_particles, see
+// write_particles below).
+#include <sys/stat.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -30,12 +34,16 @@ struct Options {
     int single_time_frame = 0, dist_flag = 0, split_flag = 1, nsteps_interval = 10;
     int num_fine_steps = 1, ndim_field = 2, charge = -1, inject_new_ptl = 0;
     int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
+    int particle_data_dump = 0;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
     double particle_v0 = 5.0, drift_param1 = 4e7, drift_param2 = 2e8;
     // particle_mover's switches with the reference CLI's defaults
     // (stochastic-mhd.f90:631-641, :935-937): NLGC on, fixed kperp/kpara off.
     bool focused_transport = false, nlgc = true;
     double kperp_kpara = 0.01, duu_init = 10.0;
+    // set_dpp_params switches (stochastic-mhd.f90:843-858)
+    int dpp_wave = 0, dpp_shear = 0, weak_scattering = 0;
+    double tau0_scattering = 1.0;
     double ptl_box[6] = {0.0, 0.0, 0.0, 1.0, 1.0, 1.0};   // xmin ymin zmin xmax ymax zmax
     // engine options
     int precision = GPAT_PREC_MIXED, noise = GPAT_NOISE_UNIFORM, device = 0, bin_interval = 0;
@@ -65,7 +73,9 @@ int parse(int argc, char **argv, Options &o) {
         {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
         {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
         {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-ft", "--focused_transport"},
-        {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"}};
+        {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
+        {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
+        {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -112,6 +122,11 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--nlgc") o.nlgc = truthy(v);
         else if (k == "--kperp_kpara") o.kperp_kpara = d;
         else if (k == "--duu_init") o.duu_init = d;
+        else if (k == "--particle_data_dump") o.particle_data_dump = (int)d;
+        else if (k == "--dpp_wave") o.dpp_wave = (int)d;
+        else if (k == "--dpp_shear") o.dpp_shear = (int)d;
+        else if (k == "--weak_scattering") o.weak_scattering = (int)d;
+        else if (k == "--tau0_scattering") o.tau0_scattering = d;
         else if (k == "--precision") {
             o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
             o.precision_set = true;
@@ -138,6 +153,47 @@ int parse(int argc, char **argv, Options &o) {
         }                                                                              \
     } while (0)
 
+// dump_particles (diagnostics.f90:1810-1888) without HDF5.  The file holds
+// int64 nptl and then the datasets of particles_XXXX.h5 in the reference's
+// order, nptl values each: x y z p v mu weight t dt (float64), split_times
+// count_flag (int8), origin nsteps_tracked nsteps_pushed tag_injected
+// tag_splitted (int32).
+int write_particles(gpat_handle_t *h, const std::string &dir, int frame) {
+    gpat_counters_t c;
+    int rc = gpat_get_counters(h, &c);
+    if (rc) return rc;
+    const int64_t n = c.nptl_current;
+    const size_t m = (size_t)(n > 0 ? n : 1);
+    std::vector<double> f64[9];
+    std::vector<int8_t> i8[2];
+    std::vector<int32_t> i32[5];
+    std::vector<uint32_t> ctr(m);
+    for (auto &v : f64) v.resize(m);
+    for (auto &v : i8) v.resize(m);
+    for (auto &v : i32) v.resize(m);
+    gpat_particles_t P;
+    P.x = f64[0].data(); P.y = f64[1].data(); P.z = f64[2].data(); P.p = f64[3].data();
+    P.v = f64[4].data(); P.mu = f64[5].data(); P.weight = f64[6].data(); P.t = f64[7].data();
+    P.dt = f64[8].data();
+    P.split_times = i8[0].data(); P.count_flag = i8[1].data();
+    P.origin = i32[0].data(); P.nsteps_tracked = i32[1].data(); P.nsteps_pushed = i32[2].data();
+    P.tag_injected = i32[3].data(); P.tag_splitted = i32[4].data();
+    P.rng_ctr = ctr.data();
+    int64_t got = 0;
+    rc = gpat_get_particles(h, &P, n, &got);
+    if (rc) return rc;
+    char name[64];
+    std::snprintf(name, sizeof name, "particles_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return GPAT_ERR_IO;
+    bool ok = std::fwrite(&got, 8, 1, f) == 1;
+    for (auto &v : f64) ok = ok && std::fwrite(v.data(), 8, (size_t)got, f) == (size_t)got;
+    for (auto &v : i8) ok = ok && std::fwrite(v.data(), 1, (size_t)got, f) == (size_t)got;
+    for (auto &v : i32) ok = ok && std::fwrite(v.data(), 4, (size_t)got, f) == (size_t)got;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? GPAT_OK : GPAT_ERR_IO;
+}
+
 std::string frame_name(const std::string &dir, int tf) {
     char buf[32];
     std::snprintf(buf, sizeof buf, "mhd_data_%04d", tf);
@@ -154,8 +210,10 @@ int main(int argc, char **argv) {
         return prc == 1 ? 0 : 2;
     }
     if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
-    // Focused transport runs on the FP64 mover unless asked otherwise.
-    if (o.focused_transport && !o.precision_set) o.precision = GPAT_PREC_FP64;
+    // Focused transport and momentum diffusion run on the FP64 mover unless
+    // asked otherwise.
+    if ((o.focused_transport || o.dpp_wave || o.dpp_shear) && !o.precision_set)
+        o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
     gpat_mhd_config_t cfg;
@@ -179,6 +237,10 @@ int main(int argc, char **argv) {
     p.time_interp = o.time_interp_flag;
     p.bin_interval = o.bin_interval;
     p.duu0 = o.duu_init;
+    p.dpp_wave = o.dpp_wave;
+    p.dpp_shear = o.dpp_shear;
+    p.weak_scattering = o.weak_scattering;
+    p.tau0 = o.tau0_scattering;
     CHECK(gpat_create(&p, &cfg, o.device, &h));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
 
@@ -241,11 +303,15 @@ int main(int argc, char **argv) {
                                                         o.particle_v0, ct, part_box,
                                                         o.power_index));
         }
-        if (tf == o.t_start + 1) CHECK(diagnostics(o.t_start));
+        if (tf == o.t_start + 1) {
+            CHECK(diagnostics(o.t_start));
+            if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, o.t_start));
+        }
         CHECK(gpat_particle_mover(h, o.focused_transport, o.nlgc, o.kperp_kpara, o.nsteps_interval,
                                   ct, o.num_fine_steps, 0));
         if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
         CHECK(diagnostics(tf));
+        if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, tf));
         if (o.time_interp_flag == 1) CHECK(gpat_copy_fields(h));
         gpat_counters_t c;
         CHECK(gpat_get_counters(h, &c));
@@ -254,6 +320,10 @@ int main(int argc, char **argv) {
                     c.last_mover_ms);
     }
     std::fclose(quick);
+    // Restart dump at t_end (stochastic-mhd.f90:264).
+    const std::string restart = o.diagnostics_directory + "restart/";
+    mkdir(restart.c_str(), 0755);
+    CHECK(write_particles(h, restart, o.t_end));
     gpat_destroy(h);
     return 0;
 }

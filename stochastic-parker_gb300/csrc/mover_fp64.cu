@@ -120,7 +120,7 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, co
 
 // Field values at the particle under the reference's names.
 struct Fld {
-    double vx, vy, vz, bx, by, bz;
+    double vx, vy, vz, rho, bx, by, bz;
     double dvx_dx, dvx_dy, dvx_dz, dvy_dx, dvy_dy, dvy_dz, dvz_dx, dvz_dy, dvz_dz;
     double dbx_dx, dbx_dy, dbx_dz, dby_dx, dby_dy, dby_dz, dbz_dx, dbz_dy, dbz_dz;
     double db_dx, db_dy, db_dz;
@@ -129,7 +129,7 @@ struct Fld {
 // From the full 32-variable layout (interp_fields order, 0-based).
 __device__ __forceinline__ Fld named_full(const double *f) {
     Fld q;
-    q.vx = f[0]; q.vy = f[1]; q.vz = f[2]; q.bx = f[4]; q.by = f[5]; q.bz = f[6];
+    q.vx = f[0]; q.vy = f[1]; q.vz = f[2]; q.rho = f[3]; q.bx = f[4]; q.by = f[5]; q.bz = f[6];
     q.dvx_dx = f[8]; q.dvx_dy = f[9]; q.dvx_dz = f[10];
     q.dvy_dx = f[11]; q.dvy_dy = f[12]; q.dvy_dz = f[13];
     q.dvz_dx = f[14]; q.dvz_dy = f[15]; q.dvz_dz = f[16];
@@ -209,8 +209,8 @@ __device__ __forceinline__ double vdrift_prefactor(const MoverArgs &a, double p,
 }
 
 __device__ __forceinline__ void push_momentum(const MoverArgs &a, State &s, double dp_dt,
-                                              double sdt, double ranp, int ndim, double &deltap) {
-    const double dpp = 0.0;
+                                              double dpp, double sdt, double ranp, int ndim,
+                                              double &deltap) {
     double dP = dp_dt * s.dt + ranp * sqrt(2.0 * dpp) * sdt;
     if (a.acc_region_flag == 1) {
         if (in_acc_region(a, s, ndim)) s.p = s.p + dP;
@@ -234,7 +234,7 @@ __device__ __forceinline__ void push_momentum(const MoverArgs &a, State &s, doub
 // with T_i = kperp dk_i, A_i = kpp dk_i (fixed ratio) or T_i = kperp dkperp_i,
 // A_i = kpara dkpara_i - kperp dkperp_i (NLGC), each in the reference's order.
 struct Kap {
-    double kpara, kperp, skpara, skperp, skpp;
+    double knorm_para, kpara, kperp, skpara, skperp, skpp;
     double dkxx_dx, dkyy_dy, dkzz_dz, dkxy_dx, dkxy_dy, dkxz_dx, dkxz_dz, dkyz_dy, dkyz_dz;
 };
 
@@ -245,16 +245,16 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
     const double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
     const double ib2 = ib1 * ib1;
     const double ib3 = ib1 * ib2;
-    double kpara, kperp;
+    double kpara, kperp, knorm_para = 1.0;
     if (!a.nlgc) {
-        double knorm_para = 1.0, knorm;
+        double knorm;
         if (a.mag_dependency == 1) knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
         if (a.momentum_dependency == 1) knorm = knorm_para * pow(p / a.p0, a.pindex);
         else knorm = knorm_para;
         kpara = a.kpara0 * knorm;
         kperp = kpara * a.kret;
     } else {
-        double knorm_para = 1.0, knorm_perp = 1.0, kn_para, kn_perp;
+        double knorm_perp = 1.0, kn_para, kn_perp;
         if (a.mag_dependency == 1) {
             knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
             knorm_perp = knorm_perp * pow(b, (a.gamma_turb - 2.0) / 3.0);
@@ -270,6 +270,7 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
         kperp = a.kpara0 * a.kperp_kpara * kn_perp * (mu * mu);
     }
     Kap k;
+    k.knorm_para = knorm_para;
     k.kpara = kpara;
     k.kperp = kperp;
     k.skpara = sqrt(2.0 * kpara);
@@ -320,6 +321,49 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
     return k;
 }
 
+// calc_dpp_wave_scattering (:2918-2931) and calc_dpp_flow_shear
+// (:2946-2979) as the pushes call them (:3479-3496, :4764-4788): they add to
+// dp_dt and return dpp.
+template <int NDIM>
+__device__ __forceinline__ double dpp_terms(const MoverArgs &a, double p, const Fld &f,
+                                            const Kap &k, double b, double divv,
+                                            double &dp_dt) {
+    double dpp = 0.0;
+    if (a.dpp_wave) {
+        const double va = b / sqrt(f.rho);
+        if (a.momentum_dependency == 1) dp_dt = dp_dt + (8.0 * p / (27.0 * k.kpara)) * (va * va);
+        else dp_dt = dp_dt + (4.0 * p / (9.0 * k.kpara)) * (va * va);
+        dpp = dpp + (p * va) * (p * va) / (9.0 * k.kpara);
+    }
+    if (a.dpp_shear) {
+        const double sxx = f.dvx_dx - divv / 3.0;
+        const double syy = f.dvy_dy - divv / 3.0;
+        const double szz = (NDIM == 3) ? f.dvz_dz - divv / 3.0 : -(divv / 3.0);
+        const double sxy = (f.dvx_dy + f.dvy_dx) / 2.0;
+        const double sxz = (NDIM == 3) ? (f.dvx_dz + f.dvz_dx) / 2.0 : 0.0;
+        const double syz = (NDIM == 3) ? (f.dvy_dz + f.dvz_dy) / 2.0 : 0.0;
+        const double bx = f.bx, by = f.by, bz = f.bz;
+        double gshear;
+        if (a.weak_scattering) {
+            const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+            double bbs = sxx * (bx * bx) + syy * (by * by) + szz * (bz * bz) +
+                         2.0 * (sxy * bx * by + sxz * bx * bz + syz * by * bz);
+            bbs = bbs * ib * ib;
+            gshear = bbs * bbs / 5.0;
+        } else {
+            gshear = 2.0 * (sxx * sxx + syy * syy + szz * szz +
+                            2.0 * (sxy * sxy + sxz * sxz + syz * syz)) / 15.0;
+        }
+        if (gshear > 0.0) {
+            const double p0f = pow(a.p0, 2.0 - a.pindex);
+            dp_dt = dp_dt + (2.0 + a.pindex) * gshear * a.tau0 * k.knorm_para *
+                    pow(p, a.pindex - 1.0) * p0f;
+            dpp = dpp + gshear * a.tau0 * k.knorm_para * pow(p, a.pindex) * p0f;
+        }
+    }
+    return dpp;
+}
+
 // push_particle_2d (:3358-3606).
 __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
                                        bool fixed_dt, Delta &d) {
@@ -338,7 +382,8 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &
     const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy;
     const double dz_dt = vdz;
     const double divv = f.dvx_dx + f.dvy_dy;
-    const double dp_dt = -(s.p * divv / 3.0);
+    double dp_dt = -(s.p * divv / 3.0);
+    const double dpp = dpp_terms<2>(a, s.p, f, k, b, divv, dp_dt);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
@@ -368,7 +413,7 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &
     s.t = s.t + s.dt;
     // deltaz is local to push_particle_2d: the mover's copy stays 0.
     d.x = dX; d.y = dY; d.z = 0.0; d.v = 0.0; d.mu = 0.0;
-    push_momentum(a, s, dp_dt, sdt, r[3], 2, d.p);
+    push_momentum(a, s, dp_dt, dpp, sdt, r[3], 2, d.p);
 }
 
 // push_particle_3d (:4625-4907).
@@ -390,7 +435,8 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
     const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
     const double dz_dt = f.vz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
     const double divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
-    const double dp_dt = -(s.p * divv / 3.0);
+    double dp_dt = -(s.p * divv / 3.0);
+    const double dpp = dpp_terms<3>(a, s.p, f, k, b, divv, dp_dt);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
@@ -422,7 +468,7 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
     s.z = s.z + dZ;
     s.t = s.t + s.dt;
     d.x = dX; d.y = dY; d.z = dZ; d.v = 0.0; d.mu = 0.0;
-    push_momentum(a, s, dp_dt, sdt, r[3], 3, d.p);
+    push_momentum(a, s, dp_dt, dpp, sdt, r[3], 3, d.p);
 }
 
 // calc_duu (:3116-3155) without delta-B or correlation length.
@@ -481,9 +527,8 @@ __device__ __forceinline__ void ft_time_step(const MoverArgs &a, State &s, const
 // :5280-5323); r[2] drives momentum diffusion, r[3] pitch-angle scattering.
 template <int NDIM>
 __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, double dX, double dY,
-                                             double dZ, double dp_dt, double dmu_dt, double duu,
-                                             double sdt, const double r[4], Delta &d) {
-    const double dpp = 0.0;
+                                             double dZ, double dp_dt, double dpp, double dmu_dt,
+                                             double duu, double sdt, const double r[4], Delta &d) {
     double dP = dp_dt * s.dt + r[2] * sqrt(2.0 * dpp) * sdt;
     double dV = s.v * dP / s.p;
     double dMu = dmu_dt * s.dt + r[3] * sqrt(2.0 * duu) * sdt;
@@ -592,7 +637,8 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
         div_bnorm = -((bx * f.db_dx + by * f.db_dy + bz * f.db_dz) * ib2);
     }
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s.mu * bv_gradv / s.v);
-    const double dp_dt = s.p * acc_rate;
+    double dp_dt = s.p * acc_rate;
+    const double dpp = dpp_terms<NDIM>(a, s.p, f, k, b, divv, dp_dt);
     double dmu_dt, duu;
     calc_duu(a, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
     if (!fixed_dt) ft_time_step<NDIM>(a, s, k, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
@@ -615,7 +661,7 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
         dY = dy_dt * s.dt + (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
         dZ = dz_dt * s.dt + bxyn * skperp * r[0] * sdt;
     }
-    push_ft_tail<NDIM>(a, s, dX, dY, dZ, dp_dt, dmu_dt, duu, sdt, r, d);
+    push_ft_tail<NDIM>(a, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
 template <int NDIM>
@@ -656,10 +702,10 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
     }
 }
 
-template <int NDIM, bool FT>
+template <int NDIM, bool FT, bool FULL>
 __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, Delta &d) {
     Fld f;
-    if (FT) {
+    if (FULL) {
         double v[32];
         if (!interp<NDIM, 32, 32>(a, a.full1, a.full2, s, v)) return false;
         f = named_full(v);
@@ -682,7 +728,10 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
     return true;
 }
 
-template <int NDIM, bool FT>
+// FT: focused transport.  FULL: interpolate all 32 variables (focused
+// transport and momentum diffusion read velocity gradients and density that
+// the packed records leave out).
+template <int NDIM, bool FT, bool FULL>
 __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
     Acc acc = {0, 0, 0, 0, 0};
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -716,7 +765,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 negp_or_boundary<NDIM>(a, s, acc);
                 if (s.flag != 1) break;
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
-                if (!do_push<NDIM, FT>(a, s, false, dl)) {
+                if (!do_push<NDIM, FT, FULL>(a, s, false, dl)) {
                     s.flag = 0; alive = false; break;
                 }
                 ++pushes;
@@ -737,7 +786,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 s.dt = t0 + dt_target - s.t;
                 if (s.dt > 0.0) {
                     s.nsteps_pushed = s.nsteps_pushed - 1;
-                    if (!do_push<NDIM, FT>(a, s, true, dl)) {
+                    if (!do_push<NDIM, FT, FULL>(a, s, true, dl)) {
                         s.flag = 0; alive = false; break;
                     }
                     ++pushes;
@@ -781,12 +830,16 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
     const bool ft = a.focused_transport != 0;
+    const bool full = ft || a.dpp_wave || a.dpp_shear;
+    const unsigned g = (unsigned)blocks;
     if (a.ndim == 2) {
-        if (ft) mover_fp64_kernel<2, true><<<(unsigned)blocks, threads, 0, s>>>(a);
-        else mover_fp64_kernel<2, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+        if (ft) mover_fp64_kernel<2, true, true><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<2, false, true><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<2, false, false><<<g, threads, 0, s>>>(a);
     } else {
-        if (ft) mover_fp64_kernel<3, true><<<(unsigned)blocks, threads, 0, s>>>(a);
-        else mover_fp64_kernel<3, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+        if (ft) mover_fp64_kernel<3, true, true><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<3, false, true><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<3, false, false><<<g, threads, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

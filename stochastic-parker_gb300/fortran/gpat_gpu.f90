@@ -42,8 +42,8 @@ module gpat_gpu
         integer(c_int32_t) :: time_interp
         integer(c_int32_t) :: dpp_wave, dpp_shear, deltab_flag, correlation_flag
         integer(c_int32_t) :: include_3rd_dim, spherical_coord, nonuniform_grid
-        integer(c_int32_t) :: bin_interval, reserved
-        real(c_double) :: duu0
+        integer(c_int32_t) :: bin_interval, weak_scattering
+        real(c_double) :: duu0, tau0
     end type gpat_params_t
 
     type, bind(c) :: gpat_particles_t

@@ -60,8 +60,8 @@ class Params(C.Structure):
         ("time_interp", i32),
         ("dpp_wave", i32), ("dpp_shear", i32), ("deltab_flag", i32), ("correlation_flag", i32),
         ("include_3rd_dim", i32), ("spherical_coord", i32), ("nonuniform_grid", i32),
-        ("bin_interval", i32), ("reserved", i32),
-        ("duu0", d),
+        ("bin_interval", i32), ("weak_scattering", i32),
+        ("duu0", d), ("tau0", d),
     ]
 
 

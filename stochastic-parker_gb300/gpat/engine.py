@@ -29,7 +29,7 @@ REFERENCE_DEFAULTS = dict(
     drift1=4.0e7, drift2=2.0e8, charge=-1, check_drift_2d=0,
     ndim=2, pbcx=0, pbcy=0, pbcz=0, npp_global=128,
     seed=0x5EED0001, noise=_abi.NOISE_UNIFORM, precision=_abi.PREC_FP64,
-    nptl_max=100_000, time_interp=0, duu0=10.0,
+    nptl_max=100_000, time_interp=0, duu0=10.0, tau0=1.0,
 )
 
 
@@ -120,6 +120,27 @@ class ParticleSet:
         key = (self.arrays["tag_injected"].astype(np.int64) << 32) | \
               (self.arrays["tag_splitted"].astype(np.int64) & 0xFFFFFFFF)
         return self.take(np.argsort(key, kind="stable"))
+
+
+DUMP_FIELDS = [("x", "f8"), ("y", "f8"), ("z", "f8"), ("p", "f8"), ("v", "f8"), ("mu", "f8"),
+               ("weight", "f8"), ("t", "f8"), ("dt", "f8"), ("split_times", "i1"),
+               ("count_flag", "i1"), ("origin", "i4"), ("nsteps_tracked", "i4"),
+               ("nsteps_pushed", "i4"), ("tag_injected", "i4"), ("tag_splitted", "i4")]
+
+
+def read_particle_dump(path: str | Path) -> dict:
+    """particles_XXXX.dat written by gpat_run (the datasets of the
+    reference's particles_XXXX.h5, dump_particles diagnostics.f90:1810-1888)."""
+    raw = Path(path).read_bytes()
+    n = int(np.frombuffer(raw[:8], np.int64)[0])
+    out, off = {}, 8
+    for name, t in DUMP_FIELDS:
+        size = np.dtype(t).itemsize * n
+        out[name] = np.frombuffer(raw[off:off + size], t).copy()
+        off += size
+    if off != len(raw):
+        raise ValueError(f"{path}: {len(raw)} bytes, expected {off} for {n} particles")
+    return out
 
 
 def read_particle_params(conf_path: str | Path, base: _abi.Params | None = None) -> _abi.Params:

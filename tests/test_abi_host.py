@@ -131,7 +131,9 @@ def test_create_rejects_out_of_scope_options(engine_lib):
     cfg = make_mhd_config(16, 16, 1, 0.0, 1.0, 0.0, 1.0)
     h = _abi.Handle()
     for kw, code in ((dict(ndim=1), _abi.GPAT_ERR_UNSUPPORTED),
-                     (dict(dpp_wave=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(dpp_wave=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(dpp_shear=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(deltab_flag=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(spherical_coord=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(precision=7), _abi.GPAT_ERR_ARG),
                      (dict(nptl_max=0), _abi.GPAT_ERR_ARG),

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from gpat import build, configs, fields
-from gpat.engine import Engine, make_params
+from gpat.engine import Engine, make_params, read_particle_dump
 
 SEED = 0x1234567
 
@@ -42,7 +42,7 @@ def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
            "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
            "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
            "--precision", precision, "--seed", str(SEED), "-ft", ".true." if ft else ".false.",
-           "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0"]
+           "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1"]
     return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
 
 
@@ -98,4 +98,12 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
     q = eng.quick_check()
     last = quick[-1].split()
     assert int(last[0]) == 3 and float(last[1]) == q["nptl_current"]
+    # particle dumps (-pd 1) per frame, and the restart dump at t_end
+    assert all((out / f"particles_{t:04d}.dat").exists() for t in range(4))
+    got = eng.get_particles()
+    for path in (out / "particles_0003.dat", out / "restart" / "particles_0003.dat"):
+        d = read_particle_dump(path)
+        assert len(d["x"]) == len(got)
+        for k in d:
+            assert np.array_equal(d[k], got[k]), k
     eng.close()
