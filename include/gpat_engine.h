@@ -180,6 +180,33 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
                                int dist_flag, double particle_v0, int ct_mhd,
                                double power_index);
 
+/* Quantities of inject_particles_at_large_jz / _absj / _divv / _rho
+ * (particle_module.f90:785-1468).  db2 needs the magnetic-fluctuation
+ * arrays of deltab_flag, which this engine does not hold. */
+#define GPAT_LARGE_JZ 0    /* |dBy/dx - dBx/dy|                        */
+#define GPAT_LARGE_ABSJ 1  /* |curl B|                                 */
+#define GPAT_LARGE_DIVV 2  /* -div v (compression)                     */
+#define GPAT_LARGE_RHO 3   /* rho                                      */
+/* get_ncells_large_jz / _absj / _divv / _rho (mhd_data_parallel.f90:
+ * 2211-2498): grid nodes of frame slot 0 strictly inside part_box whose
+ * quantity is > qmin, evaluated in single precision from the stored
+ * gradients as the reference does.  The divv count reads the node two
+ * cells lower in x, y (and z in 3D): the reference assigns the whole
+ * ghost-padded gradient array to a node-sized allocatable, which is
+ * re-allocated with lower bound 1. */
+int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin,
+                           const double part_box[6], int64_t *ncells);
+/* inject_particles_at_large_*: nptl_inject = nptl when inject_same_nptl
+ * (one rank), else int(nptl * ncells / ncells_norm); each particle is
+ * drawn uniformly over the box until it lies in part_box (inclusive) with
+ * the interpolated quantity >= qmin, then mu, p and t as
+ * inject_particles_spatial_uniform.  *ninjected receives nptl_inject. */
+int gpat_inject_particles_at_large(gpat_handle_t *h, int quantity, int64_t nptl, double dt,
+                                   int dist_flag, double particle_v0, int ct_mhd,
+                                   int inject_same_nptl, double qmin, int64_t ncells_norm,
+                                   const double part_box[6], double power_index,
+                                   int64_t *ninjected);
+
 /* Particle exchange with the host (e.g. restart files, the Fortran ptls
  * array).  put replaces the whole particle set. */
 int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n);

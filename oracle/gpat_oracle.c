@@ -1304,6 +1304,119 @@ int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *P, int64
     return n;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* Injection where a field quantity is large: inject_particles_at_large_jz  */
+/* (particle_module.f90:785-903), _absj (:922-1056), _divv (:1205-1337),    */
+/* _rho (:1356-1468), and the cell counts get_ncells_large_*                 */
+/* (mhd_data_parallel.f90:2211-2498) on one rank, uniform grid.             */
+/* ------------------------------------------------------------------------ */
+static double large_quantity(int quantity, int ndim, const double f[32])
+{
+    if (quantity == 0) return fabs(f[23] - f[21]);
+    if (quantity == 1) {
+        const double a = f[25] - f[27], b = f[26] - f[22], c = f[21] - f[23];
+        return sqrt(a * a + b * b + c * c);
+    }
+    if (quantity == 2) {
+        double d = f[8];
+        d = d + f[12];
+        if (ndim > 2) d = d + f[16];
+        return -d;
+    }
+    return f[3];
+}
+
+int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
+                              int quantity, double qmin, const double box[6])
+{
+    const int ndim = pr->ndim;
+    const int nx = cfg->nx, ny = cfg->ny, nz = (ndim == 3) ? cfg->nz : 1;
+    const size_t nxg = (size_t)nx + 4, nyg = (size_t)ny + 4;
+    int64_t count = 0;
+    for (int iz = 1; iz <= nz; ++iz) {
+        const int inz = (ndim > 2) ? (cfg->dz * (double)(iz - 1) + cfg->zmin > box[2] &&
+                                      cfg->dz * (double)(iz - 1) + cfg->zmin < box[5]) : 1;
+        for (int iy = 1; iy <= ny; ++iy) {
+            const double yp = cfg->dy * (double)(iy - 1) + cfg->ymin;
+            const int iny = (ndim > 1) ? (yp > box[1] && yp < box[4]) : 1;
+            for (int ix = 1; ix <= nx; ++ix) {
+                const double xp = cfg->dx * (double)(ix - 1) + cfg->xmin;
+                if (!(inz && iny && xp > box[0] && xp < box[3])) continue;
+                const size_t cz = (ndim == 3) ? (size_t)iz + 1 : 0;
+                const float *r = full + 32 * ((size_t)ix + 1 + nxg * ((size_t)iy + 1 + nyg * cz));
+                double q;
+                if (quantity == 0) {
+                    q = (double)fabsf(r[23] - r[21]);
+                } else if (quantity == 1) {
+                    const float t1 = r[25] - r[27], t2 = r[26] - r[22], t3 = r[21] - r[23];
+                    q = (double)sqrtf(t1 * t1 + t2 * t2 + t3 * t3);
+                } else if (quantity == 2) {
+                    /* divv = farray1(nfields+1, :, :, :) re-allocates divv
+                     * over the ghost-padded extent with lower bound 1:
+                     * node (ix, iy, iz) reads the node two lower per axis. */
+                    const size_t sz = (ndim == 3) ? (size_t)iz - 1 : 0;
+                    const float *u = full + 32 * ((size_t)ix - 1 + nxg * ((size_t)iy - 1 + nyg * sz));
+                    double d = (double)u[8];
+                    d = d + (double)u[12];
+                    if (ndim > 2) d = d + (double)u[16];
+                    q = -d;
+                } else {
+                    q = (double)r[3];
+                }
+                if (q > qmin) count += 1;
+            }
+        }
+    }
+    return count;
+}
+
+int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
+                            orc_particles *P, int64_t n, int64_t nptl_max, int64_t nptl,
+                            double dt, int dist_flag, double particle_v0, double t_frame,
+                            double dt_mhd, int quantity, double qmin, const double box[6],
+                            double power_index, orc_counters *cnt)
+{
+    const int ndim = pr->ndim;
+    const double dom[6] = {cfg->xmin, cfg->ymin, cfg->zmin, cfg->xmin + (double)cfg->nx * cfg->dx,
+                           cfg->ymin + (double)cfg->ny * cfg->dy,
+                           (ndim == 3) ? cfg->zmin + (double)cfg->nz * cfg->dz : cfg->zmax};
+    const int nxg = cfg->nx + 4, nyg = cfg->ny + 4;
+    for (int64_t i = 0; i < nptl && n < nptl_max; ++i) {
+        const int32_t tag = (int32_t)cnt->tag_max;
+        cnt->tag_max += 1;
+        inj_stream s;
+        inj_stream_init(&s, pr, (uint32_t)tag);
+        const int rho = (quantity == 3);
+        double q = rho ? 0.0 : -2.0;
+        double x = box[0], y = box[1], z = box[2];
+        int64_t tries = 0;
+        while (q < qmin && ++tries <= ((int64_t)1 << 22)) {   /* the engine's rejection bound */
+            x = inj_u01(&s) * (dom[3] - dom[0]) + dom[0];
+            y = inj_u01(&s) * (dom[4] - dom[1]) + dom[1];
+            z = inj_u01(&s) * (dom[5] - dom[2]) + dom[2];
+            if (x >= box[0] && x <= box[3] && y >= box[1] && y <= box[4] && z >= box[2] &&
+                z <= box[5]) {
+                int32_t pos[3];
+                double w[8], f[32];
+                orc_get_interp_paramters(ndim, (x - cfg->xmin) / cfg->dx, (y - cfg->ymin) / cfg->dy,
+                                         (z - cfg->zmin) / cfg->dz, pos, w);
+                orc_interp_fields(full, full, 0, ndim, nxg, nyg, pos, w, 0.0, f);
+                q = large_quantity(quantity, ndim, f);
+            } else {
+                q = rho ? 0.0 : -3.0;
+            }
+        }
+        const double mu = (double)0.99f * (2.0 * inj_u01(&s) - 1.0);
+        const double p = draw_p_one(pr, &s, dist_flag, power_index);
+        const double v = particle_v0 * p / pr->p0;
+        const double t = t_frame + inj_u01(&s) * dt_mhd;
+        set_new_particle(P, n, x, y, z, p, v, mu, t, dt, tag);
+        n += 1;
+    }
+    return n;
+}
+
 /* Injection on the plane x = xpos at the frame start, following the draw
  * order of inject_particles_at_shock (particle_module.f90:542-633) with the
  * shock locator replaced by the given x. */

@@ -115,6 +115,15 @@ int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *ptl, int
                                    int dist_flag, double particle_v0, double t_frame,
                                    double dt_mhd, const double part_box[6],
                                    double power_index, orc_counters *cnt);
+/* get_ncells_large_* and inject_particles_at_large_* (quantity 0 jz,
+ * 1 absj, 2 divv, 3 rho); full is frame 1 with gradients. */
+int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
+                              int quantity, double qmin, const double part_box[6]);
+int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
+                            orc_particles *ptl, int64_t n, int64_t nptl_max, int64_t nptl,
+                            double dt, int dist_flag, double particle_v0, double t_frame,
+                            double dt_mhd, int quantity, double qmin,
+                            const double part_box[6], double power_index, orc_counters *cnt);
 int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
                         orc_particles *ptl, int64_t n, int64_t nptl_max,
                         int64_t nptl, double xpos, double dt, int dist_flag,

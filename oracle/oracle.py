@@ -120,6 +120,13 @@ def load() -> C.CDLL:
         lib.orc_inject_at_x.restype = i64
         lib.orc_inject_at_x.argtypes = [P(OrcParams), P(OrcMhdConfig), P(OrcParticles), i64, i64,
                                         i64, d, d, C.c_int, d, d, d, P(OrcCounters)]
+        lib.orc_count_cells_large.restype = i64
+        lib.orc_count_cells_large.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
+                                              C.c_int, d, P(d)]
+        lib.orc_inject_at_large.restype = i64
+        lib.orc_inject_at_large.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
+                                            P(OrcParticles), i64, i64, i64, d, C.c_int, d, d, d,
+                                            C.c_int, d, P(d), d, P(OrcCounters)]
         lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
         lib.orc_set_escaped_histogram.argtypes = [C.c_int, d, d, P(u64), P(u64), P(u64)]
         lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, d, d, C.c_int,
@@ -250,6 +257,27 @@ def inject_spatial_uniform(params: OrcParams, parts: Particles, nptl: int, dt: f
     parts.n = lib.orc_inject_spatial_uniform(C.byref(params), C.byref(parts.c), parts.n,
                                              parts.cap, nptl, dt, dist_flag, particle_v0,
                                              t_frame, dt_mhd, b, power_index, C.byref(counters))
+
+
+def count_cells_large(params: OrcParams, cfg: OrcMhdConfig, full: np.ndarray, quantity: int,
+                      qmin: float, box) -> int:
+    """get_ncells_large_* (quantity 0 jz, 1 absj, 2 divv, 3 rho)."""
+    return load().orc_count_cells_large(C.byref(params), C.byref(cfg),
+                                        full.ctypes.data_as(P(C.c_float)), quantity, qmin,
+                                        (d * 6)(*box))
+
+
+def inject_at_large(params: OrcParams, cfg: OrcMhdConfig, full: np.ndarray, parts: Particles,
+                    nptl: int, dt: float, dist_flag: int, particle_v0: float, t_frame: float,
+                    dt_mhd: float, quantity: int, qmin: float, box, counters: OrcCounters,
+                    power_index: float = 7.0):
+    """inject_particles_at_large_* for nptl particles (nptl_inject given)."""
+    lib = load()
+    parts.n = lib.orc_inject_at_large(C.byref(params), C.byref(cfg),
+                                      full.ctypes.data_as(P(C.c_float)), C.byref(parts.c),
+                                      parts.n, parts.cap, nptl, dt, dist_flag, particle_v0,
+                                      t_frame, dt_mhd, quantity, qmin, (d * 6)(*box),
+                                      power_index, C.byref(counters))
 
 
 def quick_check(parts: Particles):

@@ -527,9 +527,28 @@ int gpat_get_fields(gpat_handle_t *h, int var_flag, float *farray) {
     return GPAT_OK;
 }
 
+// Field access for the large-quantity injection and cell counts: frame slot
+// 0 with its gradients, and the exact box as the sampling domain.
+static LargeArgs large_args(const gpat_handle_t *h, int quantity, double qmin) {
+    const gpat_mhd_config_t &c = h->cfg;
+    LargeArgs g{};
+    g.quantity = quantity;
+    g.qmin = qmin;
+    g.dom[0] = c.xmin; g.dom[3] = c.xmin + (double)c.nx * c.dx;
+    g.dom[1] = c.ymin; g.dom[4] = c.ymin + (double)c.ny * c.dy;
+    g.dom[2] = c.zmin;
+    g.dom[5] = (h->prm.ndim == 3) ? c.zmin + (double)c.nz * c.dz : c.zmax;
+    g.full = h->full[0];
+    g.nx = c.nx; g.ny = c.ny; g.nz = (h->prm.ndim == 3) ? c.nz : 1;
+    g.nxg = h->nxg; g.nyg = h->nyg;
+    g.dx = c.dx; g.dy = c.dy; g.dz = c.dz;
+    g.gxmin = c.xmin; g.gymin = c.ymin; g.gzmin = c.zmin;
+    return g;
+}
+
 static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, double dt,
                          int dist_flag, double particle_v0, int ct_mhd, const double *box,
-                         double power_index) {
+                         double power_index, const LargeArgs *lg = nullptr) {
     if (nptl < 0) return fail(h, GPAT_ERR_ARG, "nptl < 0");
     if (dist_flag < 0 || dist_flag > 2) return fail(h, GPAT_ERR_ARG, "dist_flag must be 0, 1 or 2");
     if (ct_mhd < 1 || (size_t)ct_mhd + 1 > h->tstamps.size())
@@ -546,8 +565,9 @@ static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, 
     a.dist_flag = dist_flag;
     a.ndim = h->prm.ndim;
     const gpat_mhd_config_t &c = h->cfg;
-    if (mode == 0) {
+    if (mode == 0 || mode == 2) {
         for (int i = 0; i < 6; ++i) a.box[i] = box[i];
+        if (mode == 2) a.lg = *lg;
     } else {
         a.box[0] = c.xmin; a.box[3] = c.xmin + (double)c.nx * c.dx;
         a.box[1] = c.ymin; a.box[4] = c.ymin + (double)c.ny * c.dy;
@@ -586,6 +606,45 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
                                double particle_v0, int ct_mhd, double power_index) {
     if (!h) return GPAT_ERR_ARG;
     return inject_common(h, 1, nptl, xpos, dt, dist_flag, particle_v0, ct_mhd, nullptr, power_index);
+}
+
+int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin, const double part_box[6],
+                           int64_t *ncells) {
+    if (!h || !part_box || !ncells) return GPAT_ERR_ARG;
+    if (quantity < GPAT_LARGE_JZ || quantity > GPAT_LARGE_RHO)
+        return fail(h, GPAT_ERR_ARG, "quantity must be GPAT_LARGE_JZ, _ABSJ, _DIVV or _RHO");
+    if (!h->rec_ready[0]) return fail(h, GPAT_ERR_STATE, "fields and their gradients are not set");
+    CK(cudaSetDevice(h->device));
+    const LargeArgs g = large_args(h, quantity, qmin);
+    CK(cudaMemsetAsync(&h->dcnt->ncells, 0, sizeof(unsigned long long), h->stream));
+    CK(launch_count_large(g, h->prm.ndim, part_box, &h->dcnt->ncells, h->stream));
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    *ncells = (int64_t)h->hcnt.ncells;
+    return GPAT_OK;
+}
+
+int gpat_inject_particles_at_large(gpat_handle_t *h, int quantity, int64_t nptl, double dt,
+                                   int dist_flag, double particle_v0, int ct_mhd,
+                                   int inject_same_nptl, double qmin, int64_t ncells_norm,
+                                   const double part_box[6], double power_index,
+                                   int64_t *ninjected) {
+    if (!h || !part_box) return GPAT_ERR_ARG;
+    if (nptl < 0) return fail(h, GPAT_ERR_ARG, "nptl < 0");
+    if (!inject_same_nptl && ncells_norm <= 0)
+        return fail(h, GPAT_ERR_ARG, "ncells_norm must be > 0");
+    int64_t ncells = 0;
+    int rc = gpat_count_cells_large(h, quantity, qmin, part_box, &ncells);
+    if (rc) return rc;
+    // nptl * mpi_sub_size * (ncells / ncells_g or ncells_norm) on one rank;
+    // 0 / 0 (no cell above qmin) injects nothing.
+    int64_t n = 0;
+    if (inject_same_nptl) n = ncells > 0 ? nptl : 0;
+    else n = (int64_t)((double)nptl * ((double)ncells / (double)ncells_norm));
+    if (ninjected) *ninjected = n;
+    const LargeArgs g = large_args(h, quantity, qmin);
+    return inject_common(h, 2, n, 0.0, dt, dist_flag, particle_v0, ct_mhd, part_box, power_index,
+                         &g);
 }
 
 int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n) {

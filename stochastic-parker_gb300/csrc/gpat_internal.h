@@ -37,6 +37,7 @@ struct DevCounters {
     unsigned long long nsplit;
     unsigned long long wsum_hi, wsum_lo, dtsum_hi, dtsum_lo;
     unsigned long long nactive;   // particles a chunked mover launch left mid-interval
+    unsigned long long ncells;    // get_ncells_large_* result
     double dt_min, dt_max;
     unsigned int status;
     unsigned int pad;
@@ -109,19 +110,34 @@ cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_
                                cudaStream_t s);
 MixedConsts make_mixed_consts(const MoverArgs &a);
 
+// Quantities of inject_particles_at_large_* (GPAT_LARGE_*).
+struct LargeArgs {
+    int quantity;          // GPAT_LARGE_JZ / ABSJ / DIVV / RHO
+    double qmin;
+    double dom[6];         // sampling domain (the exact box): xmin ymin zmin xmax ymax zmax
+    const float *full;     // frame 1, 32 variables per node (ghost layout)
+    int nx, ny, nz, nxg, nyg;
+    double dx, dy, dz, gxmin, gymin, gzmin;
+};
+
 struct InjectArgs {
     DevParticles P;
     int64_t base, count;
     int32_t tag0;
-    int mode;         // 0: spatial uniform, 1: plane x = xpos
+    int mode;         // 0: spatial uniform, 1: plane x = xpos, 2: where a quantity is large
     int dist_flag, ndim;
     double box[6];    // xmin ymin zmin xmax ymax zmax
     double xpos, dt, particle_v0, t_frame, dt_mhd, power_index;
     double p0, pmin, pmax;
     uint32_t key0, key1;
+    LargeArgs lg;     // mode 2
 };
 // Status bits (kStatusStepLimit on a runaway rejection loop) go to *status.
 cudaError_t launch_inject(const InjectArgs &a, unsigned int *status, cudaStream_t s);
+// get_ncells_large_*: adds the count of grid nodes inside box (strict) whose
+// quantity exceeds lg.qmin to *ncells.
+cudaError_t launch_count_large(const LargeArgs &lg, int ndim, const double box[6],
+                               unsigned long long *ncells, cudaStream_t s);
 
 // Distribution of removed escaped particles by boundary face
 // (calc_escaped_distributions): bins[(face * npp + ip) * 3 + {0: count,

@@ -35,6 +35,12 @@ struct Options {
     int num_fine_steps = 1, ndim_field = 2, charge = -1, inject_new_ptl = 0;
     int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
     int particle_data_dump = 0;
+    // inject_particles_at_large_* switches (stochastic-mhd.f90:735-806)
+    bool inject_large_jz = false, inject_large_absj = false, inject_large_db2 = false;
+    bool inject_large_divv = false, inject_large_rho = false, inject_same_nptl = false;
+    double jz_min = 100.0, absj_min = 5.0, divv_min = 10.0, rho_min = 5.0;
+    long long ncells_large_jz_norm = 800, ncells_large_absj_norm = 800;
+    long long ncells_large_divv_norm = 800, ncells_large_rho_norm = 800;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
     double particle_v0 = 5.0, drift_param1 = 4e7, drift_param2 = 2e8;
     // particle_mover's switches with the reference CLI's defaults
@@ -75,7 +81,13 @@ int parse(int argc, char **argv, Options &o) {
         {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-ft", "--focused_transport"},
         {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
         {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
-        {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"}};
+        {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"},
+        {"-ij", "--inject_large_jz"}, {"-iaj", "--inject_large_absj"},
+        {"-ib", "--inject_large_db2"}, {"-iv", "--inject_large_divv"},
+        {"-ir", "--inject_large_rho"}, {"-sn", "--inject_same_nptl"}, {"-jz", "--jz_min"},
+        {"-ajm", "--absj_min"}, {"-dv", "--divv_min"}, {"-rm", "--rho_min"},
+        {"-nn", "--ncells_large_jz_norm"}, {"-naj", "--ncells_large_absj_norm"},
+        {"-nv", "--ncells_large_divv_norm"}, {"-nr", "--ncells_large_rho_norm"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -127,6 +139,20 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--dpp_shear") o.dpp_shear = (int)d;
         else if (k == "--weak_scattering") o.weak_scattering = (int)d;
         else if (k == "--tau0_scattering") o.tau0_scattering = d;
+        else if (k == "--inject_large_jz") o.inject_large_jz = truthy(v);
+        else if (k == "--inject_large_absj") o.inject_large_absj = truthy(v);
+        else if (k == "--inject_large_db2") o.inject_large_db2 = truthy(v);
+        else if (k == "--inject_large_divv") o.inject_large_divv = truthy(v);
+        else if (k == "--inject_large_rho") o.inject_large_rho = truthy(v);
+        else if (k == "--inject_same_nptl") o.inject_same_nptl = truthy(v);
+        else if (k == "--jz_min") o.jz_min = d;
+        else if (k == "--absj_min") o.absj_min = d;
+        else if (k == "--divv_min") o.divv_min = d;
+        else if (k == "--rho_min") o.rho_min = d;
+        else if (k == "--ncells_large_jz_norm") o.ncells_large_jz_norm = (long long)d;
+        else if (k == "--ncells_large_absj_norm") o.ncells_large_absj_norm = (long long)d;
+        else if (k == "--ncells_large_divv_norm") o.ncells_large_divv_norm = (long long)d;
+        else if (k == "--ncells_large_rho_norm") o.ncells_large_rho_norm = (long long)d;
         else if (k == "--precision") {
             o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
             o.precision_set = true;
@@ -210,6 +236,11 @@ int main(int argc, char **argv) {
         return prc == 1 ? 0 : 2;
     }
     if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
+    if (o.inject_large_db2) {
+        std::fprintf(stderr, "gpat_run: -ib needs the magnetic-fluctuation arrays (deltab_flag), "
+                             "which this engine does not hold\n");
+        return 2;
+    }
     // Focused transport and momentum diffusion run on the FP64 mover unless
     // asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear) && !o.precision_set)
@@ -299,9 +330,24 @@ int main(int argc, char **argv) {
             CHECK(gpat_inject_particles_at_x(h, o.nptl, o.shock_xpos, o.tinterval, o.dist_flag,
                                              o.particle_v0, ct, o.power_index));
         } else if ((tf == o.t_start + 1 || o.inject_new_ptl) && tf <= o.tmax_to_inject) {
-            CHECK(gpat_inject_particles_spatial_uniform(h, o.nptl, o.tinterval, o.dist_flag,
-                                                        o.particle_v0, ct, part_box,
-                                                        o.power_index));
+            // stochastic-mhd.f90:455-483: the first large-quantity option set wins
+            int quantity = -1;
+            double qmin = 0.0;
+            long long norm = 1;
+            if (o.inject_large_jz) { quantity = GPAT_LARGE_JZ; qmin = o.jz_min; norm = o.ncells_large_jz_norm; }
+            else if (o.inject_large_absj) { quantity = GPAT_LARGE_ABSJ; qmin = o.absj_min; norm = o.ncells_large_absj_norm; }
+            else if (o.inject_large_divv) { quantity = GPAT_LARGE_DIVV; qmin = o.divv_min; norm = o.ncells_large_divv_norm; }
+            else if (o.inject_large_rho) { quantity = GPAT_LARGE_RHO; qmin = o.rho_min; norm = o.ncells_large_rho_norm; }
+            if (quantity >= 0) {
+                int64_t injected = 0;
+                CHECK(gpat_inject_particles_at_large(h, quantity, o.nptl, o.tinterval, o.dist_flag,
+                                                     o.particle_v0, ct, o.inject_same_nptl, qmin,
+                                                     norm, part_box, o.power_index, &injected));
+            } else {
+                CHECK(gpat_inject_particles_spatial_uniform(h, o.nptl, o.tinterval, o.dist_flag,
+                                                            o.particle_v0, ct, part_box,
+                                                            o.power_index));
+            }
         }
         if (tf == o.t_start + 1) {
             CHECK(diagnostics(o.t_start));

@@ -44,6 +44,50 @@ __device__ double draw_p_power(const InjectArgs &a, InjStream &s) {
     return pow(r01 * norm + pow(a.p0, -a.power_index + 1.0), 1.0 / (-a.power_index + 1.0));
 }
 
+// interp_fields of frame 1 at rt = 0 (mhd_data_parallel.f90:1751-1804) at a
+// point inside the box, FP64 accumulation over the corners in the movers'
+// order.
+__device__ void interp_frame1(const LargeArgs &g, int ndim, double x, double y, double z,
+                              double f[32]) {
+    const double px = (x - g.gxmin) / g.dx, py = (y - g.gymin) / g.dy, pz = (z - g.gzmin) / g.dz;
+    const int fx = (int)floor(px), fy = (int)floor(py), fz = (ndim == 3) ? (int)floor(pz) : 0;
+    const double rx = (px - (double)(fx + 1)) + 1.0;
+    const double ry = (py - (double)(fy + 1)) + 1.0;
+    const double rz = (ndim == 3) ? (pz - (double)(fz + 1)) + 1.0 : 0.0;
+    const double rx1 = 1.0 - rx, ry1 = 1.0 - ry, rz1 = 1.0 - rz;
+    const double w[8] = {rx1 * ry1 * rz1, rx * ry1 * rz1, rx1 * ry * rz1, rx * ry * rz1,
+                         rx1 * ry1 * rz,  rx * ry1 * rz,  rx1 * ry * rz,  rx * ry * rz};
+    const int ix = fx + 2, iy = fy + 2, iz = (ndim == 3) ? fz + 2 : 0;
+    for (int v = 0; v < 32; ++v) f[v] = 0.0;
+    for (int k = 0; k < (ndim == 3 ? 2 : 1); ++k)
+        for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 2; ++i) {
+                const double wc = w[k * 4 + j * 2 + i];
+                const size_t cell = (size_t)(ix + i) +
+                                    (size_t)g.nxg * ((size_t)(iy + j) + (size_t)g.nyg * (size_t)(iz + k));
+                const float *r = g.full + 32 * cell;
+                for (int v = 0; v < 32; ++v) f[v] = f[v] + (double)__ldg(r + v) * wc;
+            }
+}
+
+// The quantity each inject_particles_at_large_* tests, from interpolated
+// fields (:874-890, :1027-1044, :1305-1320, :1437); the divv test is on
+// -div v.
+__device__ double large_quantity(int quantity, int ndim, const double f[32]) {
+    if (quantity == GPAT_LARGE_JZ) return fabs(f[23] - f[21]);
+    if (quantity == GPAT_LARGE_ABSJ) {
+        const double a = f[25] - f[27], b = f[26] - f[22], c = f[21] - f[23];
+        return sqrt(a * a + b * b + c * c);
+    }
+    if (quantity == GPAT_LARGE_DIVV) {
+        double d = f[8];
+        d = d + f[12];
+        if (ndim > 2) d = d + f[16];
+        return -d;
+    }
+    return f[3];
+}
+
 __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.count) return;
@@ -61,6 +105,45 @@ __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
             int it = 0;
             while (ftest > fxp) {
                 if (++it > kMaxRejections) { atomicOr(status, kStatusStepLimit); break; }
+                ptmp = (s.next() * (a.pmax - a.pmin) + a.pmin) / a.p0;
+                fxp = ptmp * ptmp * exp(-(ptmp * ptmp));
+                ftest = s.next() * (double)0.37f;
+            }
+            p = ptmp * a.p0;
+        } else if (a.dist_flag == 2) {
+            p = draw_p_power(a, s);
+        }
+        t = a.t_frame + s.next() * a.dt_mhd;
+    } else if (a.mode == 2) {
+        // Rejection over the whole box until the point is in part_box with
+        // the quantity >= qmin.  The loop runs only when the quantity's
+        // starting value (-2; -divv = -2; rho = 0) is below qmin; otherwise
+        // the particle stays at the part_box corner, as in the reference.
+        const LargeArgs &g = a.lg;
+        const bool rho = g.quantity == GPAT_LARGE_RHO;
+        double q = rho ? 0.0 : -2.0;
+        x = a.box[0]; y = a.box[1]; z = a.box[2];
+        int it = 0;
+        while (q < g.qmin) {
+            if (++it > kMaxRejections) { atomicOr(status, kStatusStepLimit); break; }
+            x = s.next() * (g.dom[3] - g.dom[0]) + g.dom[0];
+            y = s.next() * (g.dom[4] - g.dom[1]) + g.dom[1];
+            z = s.next() * (g.dom[5] - g.dom[2]) + g.dom[2];
+            if (x >= a.box[0] && x <= a.box[3] && y >= a.box[1] && y <= a.box[4] &&
+                z >= a.box[2] && z <= a.box[5]) {
+                double f[32];
+                interp_frame1(g, a.ndim, x, y, z, f);
+                q = large_quantity(g.quantity, a.ndim, f);
+            } else {
+                q = rho ? 0.0 : -3.0;
+            }
+        }
+        mu = mu_max * (2.0 * s.next() - 1.0);
+        if (a.dist_flag == 0) {
+            double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
+            int jt = 0;
+            while (ftest > fxp) {
+                if (++jt > kMaxRejections) { atomicOr(status, kStatusStepLimit); break; }
                 ptmp = (s.next() * (a.pmax - a.pmin) + a.pmin) / a.p0;
                 fxp = ptmp * ptmp * exp(-(ptmp * ptmp));
                 ftest = s.next() * (double)0.37f;
@@ -603,6 +686,71 @@ cudaError_t launch_quick_check(const DevParticles &P, int64_t n, DevCounters *cn
     int64_t blocks = (n + 255) / 256;
     if (blocks > 2048) blocks = 2048;
     quick_check_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, n, cnt);
+    return cudaGetLastError();
+}
+
+namespace {
+
+// get_ncells_large_* (mhd_data_parallel.f90:2211-2498) over the nodes
+// ix = 1..nx (position xmin + (ix - 1) dx), single-precision quantities as
+// the reference's real(sp) arrays give them.
+__global__ void count_large_kernel(const LargeArgs g, int ndim, double b0, double b1, double b2,
+                                   double b3, double b4, double b5,
+                                   unsigned long long *ncells) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    bool hit = false;
+    if (i < n) {
+        const int ix = (int)(i % g.nx) + 1;
+        const int iy = (int)((i / g.nx) % g.ny) + 1;
+        const int iz = (int)(i / ((int64_t)g.nx * g.ny)) + 1;
+        const double xp = g.dx * (double)(ix - 1) + g.gxmin;
+        const double yp = g.dy * (double)(iy - 1) + g.gymin;
+        const double zp = g.dz * (double)(iz - 1) + g.gzmin;
+        bool in = xp > b0 && xp < b3;
+        if (ndim > 1) in = in && yp > b1 && yp < b4;
+        if (ndim > 2) in = in && zp > b2 && zp < b5;
+        if (in) {
+            const int cz = (ndim == 3) ? iz + 1 : 0;
+            const float *r = g.full + 32 * ((size_t)(ix + 1) + (size_t)g.nxg *
+                                            ((size_t)(iy + 1) + (size_t)g.nyg * (size_t)cz));
+            double q;
+            if (g.quantity == GPAT_LARGE_JZ) {
+                q = (double)fabsf(r[23] - r[21]);
+            } else if (g.quantity == GPAT_LARGE_ABSJ) {
+                const float t1 = r[25] - r[27], t2 = r[26] - r[22], t3 = r[21] - r[23];
+                q = (double)sqrtf(t1 * t1 + t2 * t2 + t3 * t3);
+            } else if (g.quantity == GPAT_LARGE_DIVV) {
+                // divv = farray1(nfields+1, :, :, :) re-allocates divv over
+                // the ghost-padded extent with lower bound 1, so node (ix, iy,
+                // iz) reads the value two nodes lower along each axis.
+                const int sz = (ndim == 3) ? iz - 1 : 0;
+                const float *u = g.full + 32 * ((size_t)(ix - 1) + (size_t)g.nxg *
+                                                ((size_t)(iy - 1) + (size_t)g.nyg * (size_t)sz));
+                double d = (double)u[8];
+                d = d + (double)u[12];
+                if (ndim > 2) d = d + (double)u[16];
+                q = -d;
+            } else {
+                q = (double)r[3];
+            }
+            hit = q > g.qmin;
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(ncells, (unsigned long long)__popc(m));
+}
+
+}  // namespace
+
+cudaError_t launch_count_large(const LargeArgs &lg, int ndim, const double box[6],
+                               unsigned long long *ncells, cudaStream_t s) {
+    const int64_t n = (int64_t)lg.nx * lg.ny * lg.nz;
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t blocks = (n + threads - 1) / threads;
+    count_large_kernel<<<(unsigned)blocks, threads, 0, s>>>(lg, ndim, box[0], box[1], box[2],
+                                                             box[3], box[4], box[5], ncells);
     return cudaGetLastError();
 }
 

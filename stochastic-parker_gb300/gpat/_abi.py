@@ -26,6 +26,7 @@ ERROR_NAMES = {
     GPAT_ERR_DEVICE: "GPAT_ERR_DEVICE",
 }
 
+LARGE_JZ, LARGE_ABSJ, LARGE_DIVV, LARGE_RHO = 0, 1, 2, 3
 PREC_FP64 = 0
 PREC_MIXED = 1
 NOISE_UNIFORM = 0
@@ -118,6 +119,9 @@ SIGNATURES = {
     "gpat_inject_particles_spatial_uniform": (
         C.c_int, [Handle, i64, d, C.c_int, d, C.c_int, P(d), d]),
     "gpat_inject_particles_at_x": (C.c_int, [Handle, i64, d, d, C.c_int, d, C.c_int, d]),
+    "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),
+    "gpat_inject_particles_at_large": (C.c_int, [Handle, C.c_int, i64, d, C.c_int, d, C.c_int,
+                                                 C.c_int, d, i64, P(d), d, P(i64)]),
     "gpat_put_particles": (C.c_int, [Handle, P(Particles), i64]),
     "gpat_get_particles": (C.c_int, [Handle, P(Particles), i64, P(i64)]),
     "gpat_particle_mover": (C.c_int, [Handle, C.c_int, C.c_int, d, C.c_int, C.c_int, C.c_int,

@@ -257,6 +257,25 @@ class Engine:
         self._check(self.lib.gpat_inject_particles_at_x(
             self.h, int(nptl), xpos, dt, dist_flag, particle_v0, ct_mhd, power_index))
 
+    def count_cells_large(self, quantity, qmin, part_box) -> int:
+        """get_ncells_large_jz / _absj / _divv / _rho (quantity: _abi.LARGE_*)."""
+        box = (C.c_double * 6)(*part_box)
+        n = C.c_int64()
+        self._check(self.lib.gpat_count_cells_large(self.h, quantity, qmin, box, C.byref(n)))
+        return n.value
+
+    def inject_particles_at_large(self, quantity, nptl, dt, dist_flag, particle_v0, ct_mhd,
+                                  inject_same_nptl, qmin, ncells_norm, part_box,
+                                  power_index=7.0) -> int:
+        """inject_particles_at_large_jz / _absj / _divv / _rho; returns the
+        number of particles it injected."""
+        box = (C.c_double * 6)(*part_box)
+        n = C.c_int64()
+        self._check(self.lib.gpat_inject_particles_at_large(
+            self.h, quantity, int(nptl), dt, dist_flag, particle_v0, ct_mhd,
+            int(bool(inject_same_nptl)), qmin, int(ncells_norm), box, power_index, C.byref(n)))
+        return n.value
+
     def put_particles(self, ps: ParticleSet):
         s = ps.ctypes()
         self._check(self.lib.gpat_put_particles(self.h, C.byref(s), len(ps)))
