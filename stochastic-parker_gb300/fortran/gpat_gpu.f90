@@ -18,7 +18,10 @@ module gpat_gpu
         gpu_copy_fields, gpu_inject_particles_spatial_uniform, &
         gpu_inject_particles_at_x, gpu_particle_mover, gpu_split_particle, &
         gpu_global_distribution, gpu_pbins_edges, gpu_quick_check, &
-        gpu_put_ptls, gpu_get_ptls, gpu_nptl_current
+        gpu_put_ptls, gpu_get_ptls, gpu_nptl_current, &
+        gpu_inject_particles_at_large_jz, gpu_inject_particles_at_large_absj, &
+        gpu_inject_particles_at_large_divv, gpu_inject_particles_at_large_rho, &
+        gpu_calc_escaped_distributions, gpu_reset_escaped_particles
 
     integer(c_int), parameter :: GPAT_OK = 0
 
@@ -130,6 +133,28 @@ module gpat_gpu
             integer(c_int64_t), value :: nptl
             real(c_double), value :: xpos, dt, particle_v0, power_index
             integer(c_int), value :: dist_flag, ct_mhd
+        end function
+        integer(c_int) function c_inject_at_large(handle, quantity, nptl, dt, dist_flag, &
+                particle_v0, ct_mhd, inject_same_nptl, qmin, ncells_norm, part_box, &
+                power_index, ninjected) bind(c, name="gpat_inject_particles_at_large")
+            import :: c_int, c_ptr, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int), value :: quantity, dist_flag, ct_mhd, inject_same_nptl
+            integer(c_int64_t), value :: nptl, ncells_norm
+            real(c_double), value :: dt, particle_v0, qmin, power_index
+            real(c_double), dimension(6), intent(in) :: part_box
+            integer(c_int64_t), intent(out) :: ninjected
+        end function
+        integer(c_int) function c_escaped_distributions(handle, fescaped, counts) &
+                bind(c, name="gpat_calc_escaped_distributions")
+            import :: c_int, c_ptr, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            real(c_double), dimension(*), intent(out) :: fescaped
+            integer(c_int64_t), dimension(*), intent(out) :: counts
+        end function
+        integer(c_int) function c_reset_escaped(handle) bind(c, name="gpat_reset_escaped_particles")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
         end function
         integer(c_int) function c_particle_mover(handle, focused_transport, nlgc, kperp_kpara, &
                 nsteps_interval, mhd_tframe, num_fine_steps, dump_escaped_dist) &
@@ -277,6 +302,73 @@ module gpat_gpu
         call check(c_inject_at_x(h, int(nptl, c_int64_t), xpos, dt, int(dist_flag, c_int), &
             particle_v0, int(ct_mhd, c_int), power_index), "inject_at_x")
     end subroutine gpu_inject_particles_at_x
+
+    !< inject_particles_at_large_jz / _absj / _divv / _rho
+    !< (particle_module.f90:785-1468), same arguments
+    subroutine inject_large(quantity, nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, qmin, ncells_norm, part_box, power_index)
+        integer, intent(in) :: quantity, nptl, dist_flag, ct_mhd, ncells_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, qmin, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        integer(c_int64_t) :: ninjected
+        call check(c_inject_at_large(h, int(quantity, c_int), int(nptl, c_int64_t), dt, &
+            int(dist_flag, c_int), particle_v0, int(ct_mhd, c_int), &
+            merge(1_c_int, 0_c_int, inject_same_nptl), qmin, int(ncells_norm, c_int64_t), &
+            part_box, power_index, ninjected), "inject_particles_at_large")
+    end subroutine inject_large
+
+    subroutine gpu_inject_particles_at_large_jz(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, jz_min, ncells_large_jz_norm, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd, ncells_large_jz_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, jz_min, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call inject_large(0, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
+            jz_min, ncells_large_jz_norm, part_box, power_index)
+    end subroutine gpu_inject_particles_at_large_jz
+
+    subroutine gpu_inject_particles_at_large_absj(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, absj_min, ncells_large_absj_norm, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd, ncells_large_absj_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, absj_min, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call inject_large(1, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
+            absj_min, ncells_large_absj_norm, part_box, power_index)
+    end subroutine gpu_inject_particles_at_large_absj
+
+    subroutine gpu_inject_particles_at_large_divv(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, divv_min, ncells_large_divv_norm, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd, ncells_large_divv_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, divv_min, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call inject_large(2, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
+            divv_min, ncells_large_divv_norm, part_box, power_index)
+    end subroutine gpu_inject_particles_at_large_divv
+
+    subroutine gpu_inject_particles_at_large_rho(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, rho_min, ncells_large_rho_norm, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd, ncells_large_rho_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, rho_min, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call inject_large(3, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
+            rho_min, ncells_large_rho_norm, part_box, power_index)
+    end subroutine gpu_inject_particles_at_large_rho
+
+    !< calc_escaped_distributions (diagnostics.f90:913-960): fescaped(npp, 2*ndim)
+    subroutine gpu_calc_escaped_distributions(fescaped, counts)
+        real(8), dimension(:, :), intent(out) :: fescaped
+        integer(8), dimension(:, :), intent(out) :: counts
+        call check(c_escaped_distributions(h, fescaped, counts), "calc_escaped_distributions")
+    end subroutine gpu_calc_escaped_distributions
+
+    !< reset_escaped_particles
+    subroutine gpu_reset_escaped_particles
+        call check(c_reset_escaped(h), "reset_escaped_particles")
+    end subroutine gpu_reset_escaped_particles
 
     !< particle_mover (particle_module.f90:1846-1974), same arguments
     subroutine gpu_particle_mover(focused_transport, nlgc, kperp_kpara, nsteps_interval, &
