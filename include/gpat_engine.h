@@ -89,8 +89,9 @@ typedef struct gpat_params {
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of
      * the particle set by cell inside one gpat_particle_mover call (0: engine
-     * default of 128; negative: bin once per call).  Results are the same
-     * for any value; it only changes memory locality. */
+     * default of 128; negative: bin once per call).  It changes memory
+     * locality; results agree statistically for any value (a paused particle
+     * resumes from its FP64 record, not from the FP32 working state). */
     int32_t bin_interval;
     int32_t weak_scattering;    /* flow-shear Dpp in the weak-scattering regime */
     /* Focused transport: pitch-angle diffusion coefficient at p0 (duu_init of
@@ -286,6 +287,41 @@ int gpat_set_counters(gpat_handle_t *h, const gpat_counters_t *in);
 /* The handle's CUDA stream (a cudaStream_t) for callers that time or
  * order work around the engine. */
 void *gpat_stream(gpat_handle_t *h);
+
+/* ------------------------------------------------------------------------ */
+/* Batched runs.  No counterpart in the reference, whose independent runs    */
+/* are separate jobs.  A batch groups up to 64 runs (handles on one device,  */
+/* GPAT_PREC_MIXED, one ndim) so that their particle_mover calls become one   */
+/* persistent launch per chunk of bin_interval pushes: blocks take           */
+/* 128-particle tiles from one counter across all runs, then every run's     */
+/* particles are binned by cell and removed, with the counts kept on the     */
+/* device, and that chunk is replayed as a CUDA graph until no particle has  */
+/* pushes left.  Each run's result is the one gpat_particle_mover gives on   */
+/* that handle alone; while a call runs, the runs' handles must not be used. */
+/* ------------------------------------------------------------------------ */
+typedef struct gpat_batch gpat_batch_t;
+/* Launch shape picked by gpat_batch_autotune: minb = resident 128-thread
+ * blocks per SM of the kernel variant (its register target), grab = tiles a
+ * block takes per scheduler step; pushes_per_s = the measured rate. */
+typedef struct gpat_batch_tuning {
+    int32_t minb, grab;
+    double pushes_per_s;
+} gpat_batch_tuning_t;
+int gpat_batch_create(gpat_handle_t *const *runs, int nruns, gpat_batch_t **out);
+int gpat_batch_destroy(gpat_batch_t *b);
+const char *gpat_batch_last_error(const gpat_batch_t *b);
+/* particle_mover for every run; mhd_tframe holds one frame index per run. */
+int gpat_batch_particle_mover(gpat_batch_t *b, const int *mhd_tframe, int nlgc,
+                              double kperp_kpara, int nsteps_interval, int num_fine_steps);
+/* Times one chunk of every launch-shape candidate from a snapshot of the
+ * runs (restored afterwards, so the runs are unchanged) and keeps the
+ * fastest for later calls.  Launch shapes do not change results. */
+int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double kperp_kpara,
+                        int nsteps_interval, int num_fine_steps, gpat_batch_tuning_t *best);
+int gpat_batch_get_tuning(const gpat_batch_t *b, gpat_batch_tuning_t *t);
+int gpat_batch_set_tuning(gpat_batch_t *b, const gpat_batch_tuning_t *t);
+/* Device time, pushes and graph launches of the last batched mover call. */
+int gpat_batch_stats(const gpat_batch_t *b, double *ms, uint64_t *pushes, int64_t *graph_launches);
 
 #ifdef __cplusplus
 }

@@ -963,3 +963,374 @@ int gpat_set_counters(gpat_handle_t *h, const gpat_counters_t *in) {
 void *gpat_stream(gpat_handle_t *h) { return h ? (void *)h->stream : nullptr; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched runs: one persistent mover launch per chunk for all runs, the
+// chunk (mover + every run's binning) replayed as a CUDA graph.
+// ---------------------------------------------------------------------------
+struct gpat_batch {
+    std::vector<gpat_handle_t *> runs;
+    int device = 0, sm_count = 0, ndim = 2;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    unsigned long long *dev = nullptr;     // run_n[nruns], tile_counter, nactive_total
+    long long *tile_prefix = nullptr;      // nruns + 1
+    unsigned long long *host_ull = nullptr;   // pinned: run_n readback and nactive
+    std::vector<BatchRun> desc;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int graph_key[3] = {-1, -1, -1};       // nlgc, minb, grab of the captured graphs
+    gpat_batch_tuning_t tuning{};
+    std::string err;
+    double last_ms = 0.0;
+    uint64_t last_steps = 0;
+    int64_t last_graph_launches = 0;
+};
+
+namespace {
+
+int bfail(gpat_batch_t *b, int code, const std::string &msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define BCK(call)                                                                     \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return bfail(b, GPAT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+unsigned long long *run_n_dev(gpat_batch_t *b) { return b->dev; }
+unsigned long long *tile_counter_dev(gpat_batch_t *b) { return b->dev + b->runs.size(); }
+unsigned long long *nactive_dev(gpat_batch_t *b) { return b->dev + b->runs.size() + 1; }
+
+void destroy_graphs(gpat_batch_t *b) {
+    for (auto &e : b->exec) {
+        if (e) cudaGraphExecDestroy(e);
+        e = nullptr;
+    }
+    b->graph_key[0] = b->graph_key[1] = b->graph_key[2] = -1;
+}
+
+// Captures the chunk graph for both buffer parities: scheduler prefix, the
+// persistent batched mover, and each run's binning (removal included) from
+// buffer `parity` into the other one.
+int capture_graphs(gpat_batch_t *b, int nlgc, int minb, int grab) {
+    destroy_graphs(b);
+    const int nr = (int)b->runs.size();
+    for (int parity = 0; parity < 2; ++parity) {
+        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = launch_batch_prefix(nr, run_n_dev(b), b->tile_prefix, tile_counter_dev(b),
+                                            nactive_dev(b), b->stream);
+        if (e == cudaSuccess)
+            e = launch_mover_mixed_batch(b->ndim, nlgc != 0, minb, parity, nr, b->sm_count, grab,
+                                         b->tile_prefix, run_n_dev(b), tile_counter_dev(b),
+                                         nactive_dev(b), b->stream);
+        for (int r = 0; r < nr && e == cudaSuccess; ++r) {
+            gpat_handle_t *h = b->runs[r];
+            e = launch_cell_sort_dev(h->P[parity], h->P[1 - parity], run_n_dev(b) + r, h->cap,
+                                     cell_grid(h), h->sort_scratch, h->dcnt, escaped_hist(h),
+                                     b->stream);
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return bfail(b, GPAT_ERR_CUDA, std::string("batch graph capture: ") +
+                                               cudaGetErrorString(e != cudaSuccess ? e : ee));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&b->exec[parity], g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess)
+            return bfail(b, GPAT_ERR_CUDA, std::string("cudaGraphInstantiate: ") +
+                                               cudaGetErrorString(ie));
+    }
+    b->graph_key[0] = nlgc;
+    b->graph_key[1] = minb;
+    b->graph_key[2] = grab;
+    return GPAT_OK;
+}
+
+// Brings every run to binned particles in buffer 0, builds and uploads the
+// run table and the device particle counts.
+int batch_prepare(gpat_batch_t *b, const int *tframes, int nlgc, double kperp_kpara,
+                  int nsteps_interval, int num_fine_steps) {
+    const int nr = (int)b->runs.size();
+    b->desc.resize(nr);
+    for (int r = 0; r < nr; ++r) {
+        gpat_handle_t *h = b->runs[r];
+        MoverArgs a;
+        int rc = mover_args(h, tframes[r], nsteps_interval, num_fine_steps, a);
+        if (rc) return bfail(b, rc, "run " + std::to_string(r) + ": " + h->err);
+        a.nlgc = nlgc ? 1 : 0;
+        a.kperp_kpara = kperp_kpara;
+        const int bi = h->prm.bin_interval;
+        a.chunk_pushes = bi == 0 ? 128u : (bi > 0 ? (uint32_t)bi : 0u);
+        for (int k = 0; k < 2 && (h->unsorted || h->cur != 0); ++k) {
+            rc = bin_particles(h);
+            if (rc) return bfail(b, rc, "run " + std::to_string(r) + ": " + h->err);
+        }
+        if (h->cur != 0) return bfail(b, GPAT_ERR_STATE, "run could not be brought to buffer 0");
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess)
+            return bfail(b, GPAT_ERR_CUDA, "run stream synchronize failed");
+        BatchRun &d = b->desc[r];
+        d.a = mixed_run_args(a);
+        d.k = make_mixed_consts(a);
+        d.P[0] = h->P[0];
+        d.P[1] = h->P[1];
+        b->host_ull[r] = (unsigned long long)h->n;
+    }
+    BCK(upload_batch_runs(b->desc.data(), nr, b->stream));
+    BCK(cudaMemcpyAsync(run_n_dev(b), b->host_ull, sizeof(unsigned long long) * (size_t)nr,
+                        cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return GPAT_OK;
+}
+
+// Replays chunk graphs until no particle paused; returns the final parity.
+int batch_run_chunks(gpat_batch_t *b, int max_chunks, int *parity_out, int64_t *launches) {
+    const size_t nr = b->runs.size();
+    int parity = 0;
+    *launches = 0;
+    for (;;) {
+        BCK(cudaGraphLaunch(b->exec[parity], b->stream));
+        ++*launches;
+        parity ^= 1;
+        BCK(cudaMemcpyAsync(b->host_ull + nr, nactive_dev(b), sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        if (b->host_ull[nr] == 0 || (max_chunks > 0 && *launches >= max_chunks)) break;
+        if (*launches > 1000000) return bfail(b, GPAT_ERR_DEVICE, "batch chunks did not finish");
+    }
+    *parity_out = parity;
+    return GPAT_OK;
+}
+
+// Reads the runs' counts and counters back into their handles.
+int batch_finish(gpat_batch_t *b, int parity, uint64_t *steps_total) {
+    const size_t nr = b->runs.size();
+    BCK(cudaMemcpyAsync(b->host_ull, run_n_dev(b), sizeof(unsigned long long) * nr,
+                        cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    uint64_t total = 0;
+    int first_err = GPAT_OK;
+    for (size_t r = 0; r < nr; ++r) {
+        gpat_handle_t *h = b->runs[r];
+        const unsigned long long before = h->hcnt.steps;
+        int rc = pull_counters(h);
+        if (rc) return bfail(b, rc, h->err);
+        h->n = (int64_t)b->host_ull[r];
+        h->cur = parity;
+        h->unsorted = false;
+        h->last_mover_steps = h->hcnt.steps - before;
+        total += h->last_mover_steps;
+        rc = check_status(h);
+        if (rc && first_err == GPAT_OK) {
+            first_err = rc;
+            b->err = "run " + std::to_string(r) + ": " + h->err;
+        }
+    }
+    *steps_total = total;
+    return first_err;
+}
+
+}  // namespace
+
+int gpat_batch_create(gpat_handle_t *const *runs, int nruns, gpat_batch_t **out) {
+    if (!runs || !out || nruns < 1 || nruns > kMaxBatchRuns) return GPAT_ERR_ARG;
+    *out = nullptr;
+    const gpat_handle_t *h0 = runs[0];
+    for (int r = 0; r < nruns; ++r) {
+        const gpat_handle_t *h = runs[r];
+        if (!h) return GPAT_ERR_ARG;
+        if (h->prm.precision != GPAT_PREC_MIXED || h->device != h0->device ||
+            h->prm.ndim != h0->prm.ndim)
+            return GPAT_ERR_UNSUPPORTED;
+        for (int q = 0; q < r; ++q)
+            if (runs[q] == h) return GPAT_ERR_ARG;
+    }
+    gpat_batch_t *b = new gpat_batch_t;
+    b->runs.assign(runs, runs + nruns);
+    b->device = h0->device;
+    b->sm_count = h0->sm_count;
+    b->ndim = h0->prm.ndim;
+    int variants[4];
+    batch_minb_variants(b->ndim, variants);
+    b->tuning.minb = b->ndim == 2 ? 6 : 5;   // the single-run kernel's register target
+    b->tuning.grab = 1;
+    cudaSetDevice(b->device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaMalloc(&b->dev, sizeof(unsigned long long) * ((size_t)nruns + 2)) != cudaSuccess ||
+        cudaMalloc(&b->tile_prefix, sizeof(long long) * ((size_t)nruns + 1)) != cudaSuccess ||
+        cudaMallocHost(&b->host_ull, sizeof(unsigned long long) * ((size_t)nruns + 2)) !=
+            cudaSuccess) {
+        gpat_batch_destroy(b);
+        return GPAT_ERR_OOM;
+    }
+    *out = b;
+    return GPAT_OK;
+}
+
+int gpat_batch_destroy(gpat_batch_t *b) {
+    if (!b) return GPAT_ERR_ARG;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    destroy_graphs(b);
+    if (b->dev) cudaFree(b->dev);
+    if (b->tile_prefix) cudaFree(b->tile_prefix);
+    if (b->host_ull) cudaFreeHost(b->host_ull);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GPAT_OK;
+}
+
+const char *gpat_batch_last_error(const gpat_batch_t *b) { return b ? b->err.c_str() : "null batch"; }
+
+int gpat_batch_particle_mover(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double kperp_kpara,
+                              int nsteps_interval, int num_fine_steps) {
+    if (!b || !mhd_tframe) return GPAT_ERR_ARG;
+    BCK(cudaSetDevice(b->device));
+    int rc = batch_prepare(b, mhd_tframe, nlgc, kperp_kpara, nsteps_interval, num_fine_steps);
+    if (rc) return rc;
+    if (!b->exec[0] || b->graph_key[0] != (nlgc ? 1 : 0) || b->graph_key[1] != b->tuning.minb ||
+        b->graph_key[2] != b->tuning.grab) {
+        rc = capture_graphs(b, nlgc ? 1 : 0, b->tuning.minb, b->tuning.grab);
+        if (rc) return rc;
+    }
+    BCK(cudaEventRecord(b->ev0, b->stream));
+    int parity = 0;
+    int64_t launches = 0;
+    rc = batch_run_chunks(b, 0, &parity, &launches);
+    if (rc) return rc;
+    BCK(cudaEventRecord(b->ev1, b->stream));
+    BCK(cudaEventSynchronize(b->ev1));
+    float ms = 0.0f;
+    BCK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    b->last_graph_launches = launches;
+    return batch_finish(b, parity, &b->last_steps);
+}
+
+int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double kperp_kpara,
+                        int nsteps_interval, int num_fine_steps, gpat_batch_tuning_t *best) {
+    if (!b || !mhd_tframe) return GPAT_ERR_ARG;
+    BCK(cudaSetDevice(b->device));
+    int rc = batch_prepare(b, mhd_tframe, nlgc, kperp_kpara, nsteps_interval, num_fine_steps);
+    if (rc) return rc;
+    // Snapshot of every run's particles (buffer 0), counters and escaped
+    // distribution: each trial moves one chunk from the same state.
+    const size_t nr = b->runs.size();
+    std::vector<void *> snap(nr, nullptr);
+    std::vector<DevCounters> hc(nr);
+    std::vector<int64_t> n0(nr);
+    auto release = [&]() {
+        for (void *p : snap)
+            if (p) cudaFree(p);
+    };
+    for (size_t r = 0; r < nr; ++r) {
+        gpat_handle_t *h = b->runs[r];
+        const size_t bytes = particle_bytes(h->cap) + sizeof(DevCounters) +
+                             sizeof(unsigned long long) * 3 * 6 * (size_t)h->prm.npp_global;
+        if (cudaMalloc(&snap[r], bytes) != cudaSuccess) { release(); return bfail(b, GPAT_ERR_OOM, "autotune snapshot"); }
+        char *q = static_cast<char *>(snap[r]);
+        BCK(cudaMemcpyAsync(q, h->pmem[0], particle_bytes(h->cap), cudaMemcpyDeviceToDevice, b->stream));
+        BCK(cudaMemcpyAsync(q + particle_bytes(h->cap), h->dcnt, sizeof(DevCounters),
+                            cudaMemcpyDeviceToDevice, b->stream));
+        BCK(cudaMemcpyAsync(q + particle_bytes(h->cap) + sizeof(DevCounters), h->desc,
+                            sizeof(unsigned long long) * 3 * 6 * (size_t)h->prm.npp_global,
+                            cudaMemcpyDeviceToDevice, b->stream));
+        hc[r] = h->hcnt;
+        n0[r] = h->n;
+    }
+    int variants[4];
+    const int nv = batch_minb_variants(b->ndim, variants);
+    const int grabs[2] = {1, 4};
+    gpat_batch_tuning_t top{};
+    top.pushes_per_s = -1.0;
+    for (int v = 0; v < nv; ++v)
+        for (int gi = 0; gi < 2; ++gi) {
+            rc = capture_graphs(b, nlgc ? 1 : 0, variants[v], grabs[gi]);
+            if (rc) { release(); return rc; }
+            // counts back to the snapshot's
+            for (size_t r = 0; r < nr; ++r) b->host_ull[r] = (unsigned long long)n0[r];
+            BCK(cudaMemcpyAsync(run_n_dev(b), b->host_ull, sizeof(unsigned long long) * nr,
+                                cudaMemcpyHostToDevice, b->stream));
+            BCK(cudaMemsetAsync(b->dev + nr, 0, 2 * sizeof(unsigned long long), b->stream));
+            std::vector<unsigned long long> before(nr);
+            for (size_t r = 0; r < nr; ++r) before[r] = hc[r].steps;
+            BCK(cudaEventRecord(b->ev0, b->stream));
+            int parity = 0;
+            int64_t launches = 0;
+            rc = batch_run_chunks(b, 1, &parity, &launches);
+            if (rc) { release(); return rc; }
+            BCK(cudaEventRecord(b->ev1, b->stream));
+            BCK(cudaEventSynchronize(b->ev1));
+            float ms = 0.0f;
+            BCK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            uint64_t pushes = 0;
+            for (size_t r = 0; r < nr; ++r) {
+                gpat_handle_t *h = b->runs[r];
+                DevCounters c;
+                BCK(cudaMemcpy(&c, h->dcnt, sizeof c, cudaMemcpyDeviceToHost));
+                pushes += c.steps - before[r];
+            }
+            const double rate = ms > 0.0f ? (double)pushes / (ms * 1e-3) : 0.0;
+            if (rate > top.pushes_per_s) {
+                top.minb = variants[v];
+                top.grab = grabs[gi];
+                top.pushes_per_s = rate;
+            }
+            // restore the snapshot
+            for (size_t r = 0; r < nr; ++r) {
+                gpat_handle_t *h = b->runs[r];
+                char *q = static_cast<char *>(snap[r]);
+                BCK(cudaMemcpyAsync(h->pmem[0], q, particle_bytes(h->cap), cudaMemcpyDeviceToDevice,
+                                    b->stream));
+                BCK(cudaMemcpyAsync(h->dcnt, q + particle_bytes(h->cap), sizeof(DevCounters),
+                                    cudaMemcpyDeviceToDevice, b->stream));
+                BCK(cudaMemcpyAsync(h->desc, q + particle_bytes(h->cap) + sizeof(DevCounters),
+                                    sizeof(unsigned long long) * 3 * 6 * (size_t)h->prm.npp_global,
+                                    cudaMemcpyDeviceToDevice, b->stream));
+            }
+            BCK(cudaStreamSynchronize(b->stream));
+        }
+    release();
+    for (size_t r = 0; r < nr; ++r) {
+        gpat_handle_t *h = b->runs[r];
+        h->hcnt = hc[r];
+        h->n = n0[r];
+        h->cur = 0;
+        h->unsorted = false;
+    }
+    b->tuning = top;
+    if (best) *best = top;
+    return GPAT_OK;
+}
+
+int gpat_batch_get_tuning(const gpat_batch_t *b, gpat_batch_tuning_t *t) {
+    if (!b || !t) return GPAT_ERR_ARG;
+    *t = b->tuning;
+    return GPAT_OK;
+}
+
+int gpat_batch_set_tuning(gpat_batch_t *b, const gpat_batch_tuning_t *t) {
+    if (!b || !t) return GPAT_ERR_ARG;
+    int variants[4];
+    const int nv = batch_minb_variants(b->ndim, variants);
+    bool ok = false;
+    for (int v = 0; v < nv; ++v) ok = ok || variants[v] == t->minb;
+    if (!ok || t->grab < 1 || t->grab > 64) return bfail(b, GPAT_ERR_ARG, "tuning outside the variants");
+    b->tuning = *t;
+    return GPAT_OK;
+}
+
+int gpat_batch_stats(const gpat_batch_t *b, double *ms, uint64_t *pushes, int64_t *graph_launches) {
+    if (!b) return GPAT_ERR_ARG;
+    if (ms) *ms = b->last_ms;
+    if (pushes) *pushes = b->last_steps;
+    if (graph_launches) *graph_launches = b->last_graph_launches;
+    return GPAT_OK;
+}

@@ -98,6 +98,27 @@ struct MixedConsts {
     float acc_off[3], acc_scale[3];    // cell -> box fraction: (c + off) * scale
 };
 
+// What the split-precision mover reads besides MixedConsts and the particle
+// arrays: the part of MoverArgs used on the device, small enough that a
+// table of kMaxBatchRuns runs fits in constant memory.
+struct MixedRunArgs {
+    const float *rec1, *rec2;
+    DevCounters *cnt;
+    double dx, dy, dz, xmin, ymin, zmin, t0, dtf, dt_fine, limit;
+    int nxg, nyg, nzg, time_interp, nsteps_interval, acc_region_flag, mag_dependency;
+    int momentum_dependency, check_drift_2d, pbcx, pbcy, pbcz, noise;
+    uint32_t key0, key1, max_pushes, chunk_pushes;
+};
+
+// One run of a batched launch: its arguments, constants and both particle
+// buffers (the launch's parity picks the source).
+constexpr int kMaxBatchRuns = 64;
+struct BatchRun {
+    MixedRunArgs a;
+    MixedConsts k;
+    DevParticles P[2];
+};
+
 // Launchers (defined in the .cu files).  All enqueue on `s`.
 cudaError_t launch_scatter_raw_fields(const float *raw, int nvar, float *full, size_t ncells,
                                       cudaStream_t s);
@@ -109,6 +130,26 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s);
 cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
                                cudaStream_t s);
 MixedConsts make_mixed_consts(const MoverArgs &a);
+MixedRunArgs mixed_run_args(const MoverArgs &a);
+// Batched split-precision mover (see mover_mixed.cu).
+cudaError_t upload_batch_runs(const BatchRun *runs, int nruns, cudaStream_t s);
+cudaError_t launch_batch_prefix(int nruns, const unsigned long long *run_n, long long *tile_prefix,
+                                unsigned long long *tile_counter,
+                                unsigned long long *nactive_total, cudaStream_t s);
+int batch_minb_variants(int ndim, int *out);
+// launch_cell_sort with the particle count in device memory (*n_dev, updated
+// to the kept count), grids sized by the capacity: capturable in a graph.
+struct CellGrid;
+struct EscHist;
+cudaError_t launch_cell_sort_dev(const DevParticles &src, const DevParticles &dst,
+                                 unsigned long long *n_dev, int64_t cap, const CellGrid &g,
+                                 void *scratch, DevCounters *cnt, const EscHist &esc,
+                                 cudaStream_t s);
+cudaError_t launch_mover_mixed_batch(int ndim, bool nlgc, int minb, int parity, int nruns,
+                                     int sm_count, int grab, const long long *tile_prefix,
+                                     const unsigned long long *run_n,
+                                     unsigned long long *tile_counter,
+                                     unsigned long long *nactive_total, cudaStream_t s);
 
 // Quantities of inject_particles_at_large_* (GPAT_LARGE_*).
 struct LargeArgs {

@@ -75,13 +75,14 @@ __device__ __forceinline__ void advance(int &c, float &f, float d) {
 // Boundary test along one axis in cell units.  ext: the half-cell-extended
 // box (period n + 1 cells); otherwise the exact box (period n).
 __device__ __forceinline__ void bc_axis(int &c, float f, int n, bool ext, int open, int flo,
-                                        int fhi, int &flag, const MoverArgs &a, int64_t i) {
+                                        int fhi, int &flag, const MixedRunArgs &a,
+                                        const double *w) {
     if (flag != 1) return;
     const bool lo = ext ? (c < -1 || (c == -1 && f < 0.5f)) : (c < 0);
     const bool hi = ext ? (c > n || (c == n && f > 0.5f)) : (c > n || (c == n && f > 0.0f));
     if (!lo && !hi) return;
     if (open) {
-        atomic_add_fixed(&a.cnt->leak_hi, &a.cnt->leak_lo, a.P.weight[i]);
+        atomic_add_fixed(&a.cnt->leak_hi, &a.cnt->leak_lo, *w);
         flag = lo ? flo : fhi;
     } else {
         const int per = ext ? n + 1 : n;
@@ -95,21 +96,21 @@ struct Pos {
 };
 
 template <int NDIM>
-__device__ __forceinline__ void boundary(const MoverArgs &a, const MixedConsts &k, Pos &q,
-                                         bool ext, int &flag, int64_t i) {
-    bc_axis(q.cx, q.fx, k.nx, ext, a.pbcx, -1, -2, flag, a, i);
-    bc_axis(q.cy, q.fy, k.ny, ext, a.pbcy, -3, -4, flag, a, i);
-    if (NDIM == 3) bc_axis(q.cz, q.fz, k.nz, ext, a.pbcz, -5, -6, flag, a, i);
+__device__ __forceinline__ void boundary(const MixedRunArgs &a, const MixedConsts &k, Pos &q,
+                                         bool ext, int &flag, const double *w) {
+    bc_axis(q.cx, q.fx, k.nx, ext, a.pbcx, -1, -2, flag, a, w);
+    bc_axis(q.cy, q.fy, k.ny, ext, a.pbcy, -3, -4, flag, a, w);
+    if (NDIM == 3) bc_axis(q.cz, q.fz, k.nz, ext, a.pbcz, -5, -6, flag, a, w);
 }
 
 template <int NDIM>
-__device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, const MixedConsts &k, Pos &q,
-                                                 float p, int &flag, int64_t i) {
+__device__ __forceinline__ void negp_or_boundary(const MixedRunArgs &a, const MixedConsts &k, Pos &q,
+                                                 float p, int &flag, const double *w) {
     if (p < 0.0f) {
         flag = 0;
-        atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, a.P.weight[i]);
+        atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, *w);
     } else {
-        boundary<NDIM>(a, k, q, true, flag, i);
+        boundary<NDIM>(a, k, q, true, flag, w);
     }
 }
 
@@ -125,7 +126,7 @@ __device__ __forceinline__ void ld8(const float *p, float (&v)[8]) {
 
 // FP32 bilinear / trilinear interpolation of the packed record.
 template <int NDIM, int NV>
-__device__ __forceinline__ bool interp(const MoverArgs &a, const Pos &q, float rt, float f[NV]) {
+__device__ __forceinline__ bool interp(const MixedRunArgs &a, const Pos &q, float rt, float f[NV]) {
     constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
     const int ix = q.cx + 2, iy = q.cy + 2, iz = (NDIM == 3) ? q.cz + 2 : 0;
     if ((unsigned)ix > (unsigned)(a.nxg - 2) || (unsigned)iy > (unsigned)(a.nyg - 2) ||
@@ -174,7 +175,7 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const Pos &q, float r
     return true;
 }
 
-__device__ __forceinline__ void noise4(const MoverArgs &a, uint32_t ctr, uint32_t ti, uint32_t ts,
+__device__ __forceinline__ void noise4(const MixedRunArgs &a, uint32_t ctr, uint32_t ti, uint32_t ts,
                                        float r[4]) {
     const uint4 w = philox4x32_10(make_uint4(ctr, 2u, ti, ts), a.key0, a.key1);
     if (a.noise == GPAT_NOISE_UNIFORM) {
@@ -216,7 +217,7 @@ __device__ __forceinline__ bool in_acc_region(const MixedConsts &k, const Pos &q
 // gradient terms T_i = kperp dkperp_i, A_i = kpara dkpara_i - kperp dkperp_i
 // in place of kperp dk_i and kpp dk_i.
 template <int NDIM, bool NLGC>
-__device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, const Pos &q,
+__device__ __forceinline__ bool push(const MixedRunArgs &a, const MixedConsts &k, const Pos &q,
                                      float p, float mu, float rt, bool fixed, float &dt,
                                      uint32_t ctr, uint32_t ti, uint32_t ts, float &dX, float &dY,
                                      float &dZ, float &dp) {
@@ -360,15 +361,19 @@ __device__ __forceinline__ bool push(const MoverArgs &a, const MixedConsts &k, c
 #define GPAT_MIXED_MINB_3D 5
 #endif
 
+// One particle's interval (or chunk of it): particle_mover_one_cycle's body
+// for particle i of P.  Returns the pushes made; active is set when the
+// particle paused at chunk_pushes and must be resumed by the next launch.
 template <int NDIM, bool NLGC>
-__global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIXED_MINB_3D)
-    mover_mixed_kernel(const MoverArgs a, const MixedConsts k) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ uint32_t move_particle(const MixedRunArgs &a, const MixedConsts &k,
+                                                  const DevParticles &P, int64_t i,
+                                                  bool &active) {
     uint32_t pushes = 0;
-    bool active = false;
-    if (i < a.n) {
-        const double x_in = a.P.x[i], y_in = a.P.y[i], z_in = a.P.z[i];
-        const double p_in = a.P.p[i], t_in = a.P.t[i];
+    active = false;
+    {
+        const double *wp = P.weight + i;
+        const double x_in = P.x[i], y_in = P.y[i], z_in = P.z[i];
+        const double p_in = P.p[i], t_in = P.t[i];
         Pos q;
         {
             const double px = (x_in - a.xmin) / a.dx, py = (y_in - a.ymin) / a.dy;
@@ -392,12 +397,12 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
         const double tau_in = t_in - a.t0;
         const float tau_f0 = (float)tau_in;
         float tau = tau_f0, tc = 0.0f;
-        float dt = (float)a.P.dt[i];
-        int flag = a.P.count_flag[i];
-        int nsp = a.P.nsteps_pushed[i];
-        uint32_t ctr = a.P.rng_ctr[i];
-        const uint32_t ti = (uint32_t)a.P.tag_injected[i], ts = (uint32_t)a.P.tag_splitted[i];
-        const float mu = NLGC ? (float)a.P.mu[i] : 0.0f;
+        float dt = (float)P.dt[i];
+        int flag = P.count_flag[i];
+        int nsp = P.nsteps_pushed[i];
+        uint32_t ctr = P.rng_ctr[i];
+        const uint32_t ti = (uint32_t)P.tag_injected[i], ts = (uint32_t)P.tag_splitted[i];
+        const float mu = NLGC ? (float)P.mu[i] : 0.0f;
 
         const double stepd = ceil(tau_in / a.dt_fine);
         double target_d = (stepd <= 0.0) ? a.dt_fine : stepd * a.dt_fine;
@@ -407,16 +412,16 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
 
         if (p < 0.0f && flag == 1) {
             flag = 0;
-            atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, a.P.weight[i]);
+            atomic_add_fixed(&a.cnt->negp_hi, &a.cnt->negp_lo, *wp);
         } else {
-            boundary<NDIM>(a, k, q, true, flag, i);
+            boundary<NDIM>(a, k, q, true, flag, wp);
         }
         bool alive = (flag == 1);
         bool paused = false;
         while (alive && target_d < a.limit) {
             const float target = (float)target_d;
             while (tau - tc < target && flag == 1) {
-                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, i);
+                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, wp);
                 if (flag != 1) break;
                 if (a.chunk_pushes != 0 && pushes >= a.chunk_pushes) {
                     paused = true;   // between pushes: the next launch resumes from t
@@ -481,43 +486,135 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
                     nsp = (nsp + 1) % a.nsteps_interval;
                 }
                 dt = dt_old;
-                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, i);
+                negp_or_boundary<NDIM>(a, k, q, p - pc, flag, wp);
             } else if (flag == 1 && tau - tc == target) {
                 landed_at = target_d;   // reached the target without overshoot
             }
             target_d = target_d + a.dt_fine;
         }
-        if (flag == 1 && !paused) boundary<NDIM>(a, k, q, false, flag, i);
+        if (flag == 1 && !paused) boundary<NDIM>(a, k, q, false, flag, wp);
         active = paused;
         // Write back input + change, computed in FP64.
         const double dcx = (double)(q.cx - q_in.cx) + ((double)q.fx - (double)q_in.fx);
         const double dcy = (double)(q.cy - q_in.cy) + ((double)q.fy - (double)q_in.fy);
-        a.P.x[i] = x_in + dcx * a.dx;
-        a.P.y[i] = y_in + dcy * a.dy;
+        P.x[i] = x_in + dcx * a.dx;
+        P.y[i] = y_in + dcy * a.dy;
         if (NDIM == 3) {
             const double dcz = (double)(q.cz - q_in.cz) + ((double)q.fz - (double)q_in.fz);
-            a.P.z[i] = z_in + dcz * a.dz;
+            P.z[i] = z_in + dcz * a.dz;
         } else if (z2 != 0.0f) {
-            a.P.z[i] = z_in + (double)z2;
+            P.z[i] = z_in + (double)z2;
         }
-        a.P.p[i] = p_in + (((double)p - (double)pc) - (double)p_f0);
-        a.P.t[i] = landed_at >= 0.0 ? a.t0 + landed_at
+        P.p[i] = p_in + (((double)p - (double)pc) - (double)p_f0);
+        P.t[i] = landed_at >= 0.0 ? a.t0 + landed_at
                                     : t_in + (((double)tau - (double)tc) - (double)tau_f0);
-        a.P.dt[i] = (double)dt;
-        a.P.count_flag[i] = (int8_t)flag;
-        a.P.nsteps_pushed[i] = nsp;
-        a.P.nsteps_tracked[i] = 1;
-        a.P.rng_ctr[i] = ctr;
+        P.dt[i] = (double)dt;
+        P.count_flag[i] = (int8_t)flag;
+        P.nsteps_pushed[i] = nsp;
+        P.nsteps_tracked[i] = 1;
+        P.rng_ctr[i] = ctr;
     }
+    return pushes;
+}
+
+// Per-warp sums of pushes and paused particles into a run's counters.
+__device__ __forceinline__ void add_warp_counters(DevCounters *cnt, uint32_t pushes, bool active,
+                                                  unsigned long long *nactive_total) {
     const unsigned long long steps = warp_sum_u64(pushes);
     const unsigned act = __ballot_sync(0xffffffffu, active);
     if ((threadIdx.x & 31) == 0) {
-        if (steps) atomicAdd(&a.cnt->steps, steps);
-        if (act) atomicAdd(&a.cnt->nactive, (unsigned long long)__popc(act));
+        if (steps) atomicAdd(&cnt->steps, steps);
+        if (act) {
+            atomicAdd(&cnt->nactive, (unsigned long long)__popc(act));
+            if (nactive_total) atomicAdd(nactive_total, (unsigned long long)__popc(act));
+        }
     }
 }
 
+template <int NDIM, bool NLGC>
+__global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIXED_MINB_3D)
+    mover_mixed_kernel(const MixedRunArgs a, const MixedConsts k, const DevParticles P,
+                       const int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = false;
+    uint32_t pushes = 0;
+    if (i < n) pushes = move_particle<NDIM, NLGC>(a, k, P, i, active);
+    add_warp_counters(a.cnt, pushes, active, nullptr);
+}
+
+// ---------------------------------------------------------------------------
+// Batched runs: one persistent launch moves the particles of up to
+// kMaxBatchRuns independent runs.  Run descriptors sit in constant memory
+// (a block reads its run's with uniform-index constant loads, off the L1
+// path the gathers saturate); blocks take 128-particle tiles from a global
+// counter across all runs, so uneven runs balance over the SMs.
+// ---------------------------------------------------------------------------
+__constant__ BatchRun c_batch_runs[kMaxBatchRuns];
+
+template <int NDIM, bool NLGC, int MINB>
+__global__ void __launch_bounds__(128, MINB)
+    mover_mixed_batch_kernel(const int parity, const int nruns, const long long *tile_prefix,
+                             const unsigned long long *run_n, unsigned long long *tile_counter,
+                             const int grab, unsigned long long *nactive_total) {
+    __shared__ long long s_tile;
+    const long long total = tile_prefix[nruns];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(tile_counter, (unsigned long long)grab);
+        __syncthreads();
+        const long long t0 = s_tile;
+        if (t0 >= total) break;
+        for (int g = 0; g < grab; ++g) {
+            const long long t = t0 + g;
+            if (t >= total) break;
+            int lo = 0, hi = nruns - 1;        // last run with tile_prefix[r] <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (tile_prefix[mid] <= t) lo = mid; else hi = mid - 1;
+            }
+            const BatchRun &d = c_batch_runs[lo];
+            const int64_t i = (t - tile_prefix[lo]) * 128 + threadIdx.x;
+            bool active = false;
+            uint32_t pushes = 0;
+            if (i < (int64_t)run_n[lo])
+                pushes = move_particle<NDIM, NLGC>(d.a, d.k, d.P[parity], i, active);
+            add_warp_counters(d.a.cnt, pushes, active, nactive_total);
+        }
+    }
+}
+
+// Tile prefix over the runs' current particle counts, and a fresh scheduler.
+__global__ void batch_prefix_kernel(const int nruns, const unsigned long long *run_n,
+                                    long long *tile_prefix, unsigned long long *tile_counter,
+                                    unsigned long long *nactive_total) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long acc = 0;
+    for (int r = 0; r < nruns; ++r) {
+        tile_prefix[r] = acc;
+        acc += (long long)((run_n[r] + 127) / 128);
+    }
+    tile_prefix[nruns] = acc;
+    *tile_counter = 0;
+    *nactive_total = 0;
+}
+
 }  // namespace
+
+MixedRunArgs mixed_run_args(const MoverArgs &a) {
+    MixedRunArgs r{};
+    r.rec1 = a.rec1; r.rec2 = a.rec2; r.cnt = a.cnt;
+    r.dx = a.dx; r.dy = a.dy; r.dz = a.dz;
+    r.xmin = a.xmin; r.ymin = a.ymin; r.zmin = a.zmin;
+    r.t0 = a.t0; r.dtf = a.dtf; r.dt_fine = a.dt_fine; r.limit = a.limit;
+    r.nxg = a.nxg; r.nyg = a.nyg; r.nzg = a.nzg;
+    r.time_interp = a.time_interp; r.nsteps_interval = a.nsteps_interval;
+    r.acc_region_flag = a.acc_region_flag; r.mag_dependency = a.mag_dependency;
+    r.momentum_dependency = a.momentum_dependency; r.check_drift_2d = a.check_drift_2d;
+    r.pbcx = a.pbcx; r.pbcy = a.pbcy; r.pbcz = a.pbcz; r.noise = a.noise;
+    r.key0 = a.key0; r.key1 = a.key1; r.max_pushes = a.max_pushes;
+    r.chunk_pushes = a.chunk_pushes;
+    return r;
+}
 
 cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
                                cudaStream_t s) {
@@ -526,13 +623,57 @@ cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
     const unsigned g = (unsigned)blocks;
+    const MixedRunArgs r = mixed_run_args(a);
     if (a.ndim == 2) {
-        if (a.nlgc) mover_mixed_kernel<2, true><<<g, threads, 0, s>>>(a, c);
-        else mover_mixed_kernel<2, false><<<g, threads, 0, s>>>(a, c);
+        if (a.nlgc) mover_mixed_kernel<2, true><<<g, threads, 0, s>>>(r, c, a.P, a.n);
+        else mover_mixed_kernel<2, false><<<g, threads, 0, s>>>(r, c, a.P, a.n);
     } else {
-        if (a.nlgc) mover_mixed_kernel<3, true><<<g, threads, 0, s>>>(a, c);
-        else mover_mixed_kernel<3, false><<<g, threads, 0, s>>>(a, c);
+        if (a.nlgc) mover_mixed_kernel<3, true><<<g, threads, 0, s>>>(r, c, a.P, a.n);
+        else mover_mixed_kernel<3, false><<<g, threads, 0, s>>>(r, c, a.P, a.n);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t upload_batch_runs(const BatchRun *runs, int nruns, cudaStream_t s) {
+    if (nruns < 1 || nruns > kMaxBatchRuns) return cudaErrorInvalidValue;
+    return cudaMemcpyToSymbolAsync(c_batch_runs, runs, sizeof(BatchRun) * (size_t)nruns, 0,
+                                   cudaMemcpyHostToDevice, s);
+}
+
+cudaError_t launch_batch_prefix(int nruns, const unsigned long long *run_n, long long *tile_prefix,
+                                unsigned long long *tile_counter,
+                                unsigned long long *nactive_total, cudaStream_t s) {
+    batch_prefix_kernel<<<1, 32, 0, s>>>(nruns, run_n, tile_prefix, tile_counter, nactive_total);
+    return cudaGetLastError();
+}
+
+// Register-target variants the autotuner chooses from (resident 128-thread
+// blocks per SM): 2D 5 / 6 / 8, 3D 4 / 5.
+int batch_minb_variants(int ndim, int *out) {
+    if (ndim == 2) { out[0] = 5; out[1] = 6; out[2] = 8; return 3; }
+    out[0] = 4; out[1] = 5; return 2;
+}
+
+cudaError_t launch_mover_mixed_batch(int ndim, bool nlgc, int minb, int parity, int nruns,
+                                     int sm_count, int grab, const long long *tile_prefix,
+                                     const unsigned long long *run_n,
+                                     unsigned long long *tile_counter,
+                                     unsigned long long *nactive_total, cudaStream_t s) {
+    const unsigned g = (unsigned)(sm_count * minb);
+#define GPAT_BATCH_LAUNCH(ND, NL, MB)                                                         \
+    mover_mixed_batch_kernel<ND, NL, MB><<<g, 128, 0, s>>>(parity, nruns, tile_prefix, run_n, \
+                                                           tile_counter, grab, nactive_total)
+    if (ndim == 2) {
+        if (minb == 5) { if (nlgc) GPAT_BATCH_LAUNCH(2, true, 5); else GPAT_BATCH_LAUNCH(2, false, 5); }
+        else if (minb == 6) { if (nlgc) GPAT_BATCH_LAUNCH(2, true, 6); else GPAT_BATCH_LAUNCH(2, false, 6); }
+        else if (minb == 8) { if (nlgc) GPAT_BATCH_LAUNCH(2, true, 8); else GPAT_BATCH_LAUNCH(2, false, 8); }
+        else return cudaErrorInvalidValue;
+    } else {
+        if (minb == 4) { if (nlgc) GPAT_BATCH_LAUNCH(3, true, 4); else GPAT_BATCH_LAUNCH(3, false, 4); }
+        else if (minb == 5) { if (nlgc) GPAT_BATCH_LAUNCH(3, true, 5); else GPAT_BATCH_LAUNCH(3, false, 5); }
+        else return cudaErrorInvalidValue;
+    }
+#undef GPAT_BATCH_LAUNCH
     return cudaGetLastError();
 }
 

@@ -463,11 +463,14 @@ constexpr int kBinScanThreads = 256;
 constexpr int kBinScanItems = 8;
 constexpr int kBinTile = kBinScanThreads * kBinScanItems;
 
+// n_dev, when given, holds the particle count on the device (graph replays).
 __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int64_t n,
+                                                       const unsigned long long *n_dev,
                                                        const CellGrid g, int32_t *keys,
                                                        unsigned int *counts, DevCounters *cnt,
                                                        const EscHist esc_hist) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = (int64_t)*n_dev;
     int esc = 0;
     if (i < n) {
         const int flag = P.count_flag[i];
@@ -561,9 +564,12 @@ __global__ void __launch_bounds__(kBinScanThreads) bin_tile_scan_kernel(unsigned
 }
 
 __global__ void __launch_bounds__(256) cell_scatter_kernel(const DevParticles S, const DevParticles D,
-                                                           int64_t n, const int32_t *keys,
+                                                           int64_t n,
+                                                           const unsigned long long *n_dev,
+                                                           const int32_t *keys,
                                                            unsigned int *cursor) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = (int64_t)*n_dev;
     if (i >= n) return;
     const int32_t key = keys[i];
     if (key < 0) return;
@@ -592,12 +598,38 @@ cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, i
     if (e != cudaSuccess) return e;
     if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    cell_key_kernel<<<blocks, 256, 0, s>>>(src, n, g, keys, counts, cnt, esc);
+    cell_key_kernel<<<blocks, 256, 0, s>>>(src, n, nullptr, g, keys, counts, cnt, esc);
     bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
     tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
     bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
-    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, n, keys, counts);
+    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, n, nullptr, keys, counts);
     return cudaGetLastError();
+}
+
+cudaError_t launch_cell_sort_dev(const DevParticles &src, const DevParticles &dst,
+                                 unsigned long long *n_dev, int64_t cap, const CellGrid &g,
+                                 void *scratch, DevCounters *cnt, const EscHist &esc,
+                                 cudaStream_t s) {
+    const int64_t nbins = (int64_t)g.nxg * g.nyg * g.nzg;
+    const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
+    char *q = static_cast<char *>(scratch);
+    long long *tile_sums = reinterpret_cast<long long *>(q);
+    long long *tile_offsets = tile_sums + ntiles + 1;
+    unsigned int *counts = reinterpret_cast<unsigned int *>(tile_offsets + ntiles + 1);
+    int32_t *keys = reinterpret_cast<int32_t *>(counts + nbins);
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(unsigned int) * (size_t)nbins, s);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((cap + 255) / 256);
+    if (blocks == 0) return cudaSuccess;
+    cell_key_kernel<<<blocks, 256, 0, s>>>(src, 0, n_dev, g, keys, counts, cnt, esc);
+    bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
+    bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
+    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, 0, n_dev, keys, counts);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(n_dev, &cnt->nkept, sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, s);
 }
 
 size_t compaction_scratch_bytes(int64_t n) {

@@ -99,6 +99,12 @@ class Counters(C.Structure):
 
 
 Handle = C.c_void_p
+Batch = C.c_void_p
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("minb", i32), ("grab", i32), ("pushes_per_s", d)]
+
 
 # name -> (restype, argtypes); every symbol include/gpat_engine.h declares.
 SIGNATURES = {
@@ -119,6 +125,15 @@ SIGNATURES = {
     "gpat_inject_particles_spatial_uniform": (
         C.c_int, [Handle, i64, d, C.c_int, d, C.c_int, P(d), d]),
     "gpat_inject_particles_at_x": (C.c_int, [Handle, i64, d, d, C.c_int, d, C.c_int, d]),
+    "gpat_batch_create": (C.c_int, [P(Handle), C.c_int, P(Batch)]),
+    "gpat_batch_destroy": (C.c_int, [Batch]),
+    "gpat_batch_last_error": (C.c_char_p, [Batch]),
+    "gpat_batch_particle_mover": (C.c_int, [Batch, P(C.c_int), C.c_int, d, C.c_int, C.c_int]),
+    "gpat_batch_autotune": (C.c_int, [Batch, P(C.c_int), C.c_int, d, C.c_int, C.c_int,
+                                      P(BatchTuning)]),
+    "gpat_batch_get_tuning": (C.c_int, [Batch, P(BatchTuning)]),
+    "gpat_batch_set_tuning": (C.c_int, [Batch, P(BatchTuning)]),
+    "gpat_batch_stats": (C.c_int, [Batch, P(d), P(u64), P(i64)]),
     "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),
     "gpat_inject_particles_at_large": (C.c_int, [Handle, C.c_int, i64, d, C.c_int, d, C.c_int,
                                                  C.c_int, d, i64, P(d), d, P(i64)]),

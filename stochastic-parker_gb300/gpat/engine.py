@@ -364,3 +364,60 @@ class Engine:
 
     def set_counters(self, c: _abi.Counters):
         self._check(self.lib.gpat_set_counters(self.h, C.byref(c)))
+
+
+class Batch:
+    """Independent runs moved together (gpat_batch_*): one persistent,
+    graph-replayed launch per chunk for all of them."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        self.lib = self.engines[0].lib
+        self.b = _abi.Batch()
+        arr = (_abi.Handle * len(self.engines))(*[e.h for e in self.engines])
+        rc = self.lib.gpat_batch_create(arr, len(self.engines), C.byref(self.b))
+        if rc != _abi.GPAT_OK:
+            raise GPATError(rc, "gpat_batch_create failed")
+
+    def _check(self, rc: int):
+        if rc != _abi.GPAT_OK:
+            raise GPATError(rc, self.lib.gpat_batch_last_error(self.b).decode())
+
+    def _frames(self, mhd_tframe):
+        if isinstance(mhd_tframe, int):
+            mhd_tframe = [mhd_tframe] * len(self.engines)
+        return (C.c_int * len(self.engines))(*mhd_tframe)
+
+    def particle_mover(self, mhd_tframe=1, nlgc=False, kperp_kpara=0.01, nsteps_interval=10,
+                       num_fine_steps=1):
+        self._check(self.lib.gpat_batch_particle_mover(
+            self.b, self._frames(mhd_tframe), int(nlgc), kperp_kpara, nsteps_interval,
+            num_fine_steps))
+
+    def autotune(self, mhd_tframe=1, nlgc=False, kperp_kpara=0.01, nsteps_interval=10,
+                 num_fine_steps=1) -> dict:
+        t = _abi.BatchTuning()
+        self._check(self.lib.gpat_batch_autotune(
+            self.b, self._frames(mhd_tframe), int(nlgc), kperp_kpara, nsteps_interval,
+            num_fine_steps, C.byref(t)))
+        return dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s)
+
+    def tuning(self) -> dict:
+        t = _abi.BatchTuning()
+        self._check(self.lib.gpat_batch_get_tuning(self.b, C.byref(t)))
+        return dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s)
+
+    def set_tuning(self, minb, grab):
+        t = _abi.BatchTuning(minb, grab, 0.0)
+        self._check(self.lib.gpat_batch_set_tuning(self.b, C.byref(t)))
+
+    def stats(self) -> dict:
+        ms, pushes, launches = C.c_double(), C.c_uint64(), C.c_int64()
+        self._check(self.lib.gpat_batch_stats(self.b, C.byref(ms), C.byref(pushes),
+                                              C.byref(launches)))
+        return dict(ms=ms.value, pushes=pushes.value, graph_launches=launches.value)
+
+    def close(self):
+        if self.b:
+            self.lib.gpat_batch_destroy(self.b)
+            self.b = _abi.Batch()

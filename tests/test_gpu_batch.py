@@ -1,0 +1,113 @@
+"""Batched runs (gpat_batch_*): many independent runs of uneven sizes and
+parameters moved by one persistent, graph-replayed launch per chunk give
+each run exactly what gpat_particle_mover gives on that run alone."""
+import numpy as np
+import pytest
+
+from gpat import fields
+from gpat.engine import Batch, Engine, make_mhd_config, make_params
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("x", "y", "z", "p", "t", "dt", "weight", "count_flag", "nsteps_pushed", "rng_ctr")
+
+RUNS_2D = [  # (grid, particles, kpara0, kret, r, seed)
+    ((64, 64), 3000, 3e-3, 0.05, 3.0, 1),
+    ((96, 48), 500, 1e-2, 0.1, 2.2, 2),
+    ((48, 48), 12000, 1e-3, 0.02, 3.8, 3),
+    ((128, 64), 7000, 5e-3, 0.2, 2.6, 4),
+    ((32, 32), 1, 2e-3, 0.05, 3.0, 5),
+]
+
+
+def _make(spec, ndim=2, nlgc=False):
+    (nx, ny), nptl, kpara0, kret, r, seed = spec
+    if ndim == 2:
+        cfg = make_mhd_config(nx, ny, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.02)
+        db = fields.kolmogorov_az_2d(nx, ny, 1.0, 1.0, 0.5, 2 * np.pi, 16 * np.pi, seed)
+        frame = fields.planar_shock_2d(nx, ny, 0.0, 1.0, 0.0, 1.0, r=r, w=0.02, db=db)
+    else:
+        cfg = make_mhd_config(nx, nx, nx, 0.0, 1.0, 0.0, 1.0, zmin=0.0, zmax=1.0, dt_out=0.02,
+                              ndim=3)
+        frame = fields.turbulence_3d(nx, seed=seed)
+    prm = make_params(ndim=ndim, p0=0.1, pmin=0.1, pmax=100.0, kpara0=kpara0, kret=kret,
+                      dt_min_rel=2e-3, dt_max_rel=5e-2, pbcx=1, momentum_dependency=1,
+                      precision=1, nptl_max=4 * nptl + 64, seed=100 + seed, bin_interval=64)
+    eng = Engine(prm, cfg, 0)
+    eng.set_tstamps(np.arange(5) * 0.02)
+    eng.set_fields(frame, 0)
+    eng.calc_fields_gradients(0)
+    if ndim == 2:
+        eng.inject_particles_at_x(nptl, 0.5, 1e-6, 1, 1.0, 1)
+    else:
+        eng.inject_particles_spatial_uniform(nptl, 1e-6, 1, 1.0, 1, (0, 0, 0, 1, 1, 1))
+    return eng
+
+
+def _same(a, b):
+    ga, gb = a.get_particles().order_by_tags(), b.get_particles().order_by_tags()
+    assert len(ga) == len(gb)
+    for k in KEYS:
+        assert np.array_equal(ga[k], gb[k]), k
+    ca, cb = a.counters(), b.counters()
+    assert (ca.steps, ca.leak_hi, ca.leak_lo, ca.nptl_escaped) == \
+        (cb.steps, cb.leak_hi, cb.leak_lo, cb.nptl_escaped)
+    fa, na = a.calc_escaped_distributions()
+    fb, nb = b.calc_escaped_distributions()
+    assert np.array_equal(na, nb) and np.array_equal(fa, fb)
+
+
+@pytest.mark.parametrize("nlgc", [False, True])
+def test_batch_equals_separate_runs_2d(nlgc):
+    solo = [_make(s) for s in RUNS_2D]
+    batched = [_make(s) for s in RUNS_2D]
+    batch = Batch(batched)
+    for k in range(3):
+        for e in solo:
+            e.particle_mover(mhd_tframe=k + 1, nlgc=nlgc, kperp_kpara=0.05)
+        batch.particle_mover(mhd_tframe=k + 1, nlgc=nlgc, kperp_kpara=0.05)
+        st = batch.stats()
+        assert st["pushes"] == sum(e.counters().last_mover_steps for e in batched)
+        assert st["graph_launches"] >= 1
+    for a, b in zip(solo, batched):
+        _same(a, b)
+    batch.close()
+    for e in solo + batched:
+        e.close()
+
+
+def test_batch_autotune_leaves_runs_unchanged():
+    solo = [_make(s) for s in RUNS_2D[:3]]
+    batched = [_make(s) for s in RUNS_2D[:3]]
+    batch = Batch(batched)
+    best = batch.autotune(mhd_tframe=1)
+    assert best["minb"] in (5, 6, 8) and best["grab"] in (1, 4) and best["pushes_per_s"] > 0
+    assert batch.tuning()["minb"] == best["minb"]
+    for k in range(2):
+        for e in solo:
+            e.particle_mover(mhd_tframe=k + 1)
+        batch.particle_mover(mhd_tframe=k + 1)
+    for a, b in zip(solo, batched):
+        _same(a, b)
+    # every launch shape gives the same result
+    batch.set_tuning(5, 4)
+    for e in solo:
+        e.particle_mover(mhd_tframe=3)
+    batch.particle_mover(mhd_tframe=3)
+    for a, b in zip(solo, batched):
+        _same(a, b)
+    batch.close()
+
+
+def test_batch_3d():
+    specs = [((16, 16), 2000, 2e-3, 0.05, 3.0, 7), ((20, 20), 5000, 4e-3, 0.1, 3.0, 8)]
+    solo = [_make(s, ndim=3) for s in specs]
+    batched = [_make(s, ndim=3) for s in specs]
+    batch = Batch(batched)
+    for k in range(2):
+        for e in solo:
+            e.particle_mover(mhd_tframe=k + 1)
+        batch.particle_mover(mhd_tframe=k + 1)
+    for a, b in zip(solo, batched):
+        _same(a, b)
+    batch.close()
