@@ -42,12 +42,19 @@ UNIT = "particle-steps/s"
 # 3D: 8 corners x 21 values.
 GATHER_BYTES_PER_STEP = {2: 4 * 15 * 4, 3: 8 * 21 * 4}
 STATE_BYTES_PER_PARTICLE = 2 * (7 * 8 + 2 + 4 * 4)
-WORKLOADS = ("turbulent_shock_2d", "turbulence_3d")
+WORKLOADS = ("turbulent_shock_2d", "turbulence_3d", "batched_shock_2d")
+
+
+# The run of the batched workload the CPU baselines sample (its first run).
+BATCH_SAMPLE_RUN = 0
 
 
 def make_workload(args, precision, seed=None, nframes=16, scale=None):
     from gpat import configs
     scale = args.scale if scale is None else scale
+    if args.workload == "batched_shock_2d":
+        return configs.batched_shock_2d(scale=scale, precision=precision, nframes=nframes,
+                                        only=BATCH_SAMPLE_RUN)[0]
     if args.workload == "turbulence_3d":
         grid = args.grid if args.grid != 2048 else 256
         return configs.turbulence_3d(scale=scale, n=grid, precision=precision,
@@ -443,11 +450,184 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """64 independent 2D turbulent-shock runs of uneven sizes and parameters
+    moved by the batched mover: one persistent launch per chunk for all runs,
+    replayed as a CUDA graph, launch shape from the autotuner."""
+    import numpy as np
+    import torch
+    from gpat import _abi, accuracy, configs
+    from gpat.engine import Batch, ParticleSet
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    total_frames = args.warmup + args.steps + args.e2e_steps + 2
+    runs = configs.batched_shock_2d(scale=args.scale, nframes=total_frames, seed=11 + rank)
+    engines = [configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6) + 16,
+                                    bin_interval=args.bin_interval) for w in runs]
+    for e, w in zip(engines, runs):
+        configs.inject(e, w)
+    batch = Batch(engines)
+    tuning = batch.autotune(mhd_tframe=1)
+    stream = torch.cuda.ExternalStream(engines[0].stream, device=dev)
+    frame = [1]
+    graph_ms, graph_launches, chunk_pushes = [], [], []
+
+    def step():
+        batch.particle_mover(mhd_tframe=frame[0])
+        st = batch.stats()
+        graph_ms.append(st["ms"])
+        graph_launches.append(st["graph_launches"])
+        chunk_pushes.append(st["pushes"])
+        for e, w in zip(engines, runs):
+            e.split_particle(w.split["ratio"], w.split["pmin"], 10)
+            e.calc_particle_distributions()
+        frame[0] += 1
+
+    for _ in range(args.warmup):
+        step()
+    graph_ms.clear(); graph_launches.clear(); chunk_pushes.clear()
+    steps0 = sum(e.counters().steps for e in engines)
+    n_timed = sum(e.nptl_current for e in engines)
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    psteps = sum(e.counters().steps for e in engines) - steps0
+    t_max = max_over_ranks(world, elapsed, dev)
+    value = sum_over_ranks(world, float(psteps), dev) / t_max
+    intervals_done = frame[0] - 1
+
+    # f(p) of the runs nearest 1e5 particles against FP64 runs of the same runs
+    acc = []
+    if not args.no_accuracy:
+        order = sorted(range(len(runs)), key=lambda r: abs(math.log10(runs[r].nptl) - 5.0))[:4]
+        for r in order:
+            w = runs[r]
+            mixed = accuracy.spectrum(engines[r])
+            e64 = configs.build_engine(w, device=local, precision=0, nptl_max=int(w.nptl * 8))
+            configs.inject(e64, w)
+            for k in range(intervals_done):
+                e64.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=1)
+                e64.split_particle(w.split["ratio"], w.split["pmin"], 10)
+            ref = accuracy.spectrum(e64)
+            e64.close()
+            try:
+                t = accuracy.tail_stats(ref, mixed, w.params["pmin"], w.params["pmax"])
+            except RuntimeError:
+                continue
+            acc.append({"run": w.name, "particles": w.nptl, "tail_err": t["tail_err"],
+                        "tail_err_sigma": t["tail_err_sigma"], "chi2": t["chi2"],
+                        "chi2_dof": t["chi2_dof"]})
+
+    # end to end: every run's particles host -> device, the batched frame,
+    # f(p) and particles back
+    bytes_per_ptl = sum(np.dtype(t).itemsize for _, t in _abi.PARTICLE_FIELDS)
+    hosts = []
+    for e in engines:
+        cap = e.params.nptl_max
+        arrs = {name: torch.empty(cap, dtype=getattr(torch, {"f8": "float64", "i1": "int8",
+                                                             "i4": "int32", "u4": "uint32"}[t]),
+                                  pin_memory=True).numpy()
+                for name, t in _abi.PARTICLE_FIELDS}
+        hosts.append(ParticleSet(arrs))
+    curs = [e.get_particles(out=h) for e, h in zip(engines, hosts)]
+    e2e_steps, e2e_h2d, e2e_d2h = 0, 0, 0
+    barrier(world)
+    torch.cuda.synchronize()
+    t_start = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s0 = sum(e.counters().steps for e in engines)
+        for e, c in zip(engines, curs):
+            e.put_particles(c)
+            e2e_h2d += len(c) * bytes_per_ptl
+        batch.particle_mover(mhd_tframe=frame[0])
+        for i, (e, w) in enumerate(zip(engines, runs)):
+            e.split_particle(w.split["ratio"], w.split["pmin"], 10)
+            f, counts = e.calc_particle_distributions()
+            curs[i] = e.get_particles(out=hosts[i])
+            e2e_d2h += len(curs[i]) * bytes_per_ptl + f.nbytes + counts.nbytes
+        e2e_steps += sum(e.counters().steps for e in engines) - s0
+        frame[0] += 1
+    torch.cuda.synchronize()
+    e2e_elapsed = max_over_ranks(world, time.perf_counter() - t_start, dev)
+    e2e_value = sum_over_ranks(world, float(e2e_steps), dev) / e2e_elapsed if e2e_elapsed else None
+
+    if rank != 0:
+        batch.close()
+        for e in engines:
+            e.close()
+        return
+    peaks = measured_peaks()
+    chunks = statistics.mean(graph_launches)
+    ms_chunk = statistics.mean(graph_ms) / chunks
+    pushes_chunk = statistics.mean(chunk_pushes) / chunks
+    bytes_chunk = pushes_chunk * GATHER_BYTES_PER_STEP[2] + n_timed * STATE_BYTES_PER_PARTICLE
+    achieved = bytes_chunk / (ms_chunk / 1e3) / 1e9
+    nruns = len(runs)
+    sizes = sorted({w.mhd_config.nx for w in runs})
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+ff", "data": "synthetic",
+            "config": {"workload": f"batched_shock_2d_{nruns}_runs",
+                       "runs": nruns,
+                       "particles_total": int(sum(w.nptl for w in runs)),
+                       "particles_per_run_min_max": [int(min(w.nptl for w in runs)),
+                                                     int(max(w.nptl for w in runs))],
+                       "grids": [f"{n}x{n}" for n in sizes],
+                       "pushes_per_particle_per_interval": round(psteps / args.steps /
+                                                                 max(1, n_timed), 1),
+                       "step": "batched particle_mover (graph-replayed chunks) + per-run "
+                               "split_particle + f(p) over one MHD interval",
+                       "autotuned": tuning,
+                       "l2": "inputs exceed L2 (fields of 64 runs and their particles)",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk,
+            # per chunk: prefix + batched mover + 5 binning kernels per run; per step and run:
+            # split (3) + f(p) (1)
+            "gpu_launches": int(round(sum(l * (2 + 5 * nruns) for l in graph_launches) +
+                                      args.steps * 4 * nruns)),
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": e2e_h2d // max(1, args.e2e_steps),
+                    "d2h_bytes_per_step": e2e_d2h // max(1, args.e2e_steps)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "kernel": "mover_mixed_batch_kernel<2> chunk graph (mover + binning)",
+                         "peak_source": peaks["source"], "ms_per_chunk": ms_chunk,
+                         "pushes_per_chunk": pushes_chunk, "chunks_per_interval": chunks,
+                         "note": "achieved = algorithmic bytes of the chunk's pushes and particle "
+                                 "state over the whole chunk graph time (binning included)"},
+            "per_run_fp_error": acc}
+    batch.close()
+    for e in engines:
+        e.close()
+    if world == 1 and not args.no_cpu_baseline:
+        w = runs[BATCH_SAMPLE_RUN]
+        v, cores, n, steps, dt, _ = cpu_sample(w, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} particles of {w.name} injected on the shock, one "
+                                          f"MHD interval of FP64 pushes ({steps} particle-steps "
+                                          f"in {dt:.2f} s)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "batched_shock_2d":
+        run_batch(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

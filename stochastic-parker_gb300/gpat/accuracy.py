@@ -55,13 +55,24 @@ def compare(workload: configs.Workload, intervals: int, split=(2.72, 2.0),
         out[prec] = dict(f=f, f2=f2, c=c, f_dev=f_dev, n=eng.nptl_current,
                          steps=eng.counters().steps)
         eng.close()
-    a, b = out[0], out[1]
+    return tail_stats(out[0], out[1], workload.params["pmin"], workload.params["pmax"])
+
+
+def spectrum(eng) -> dict:
+    """Weighted f(p), sum of w^2 and counts on the engine's bins."""
+    edges = eng.pbins_edges()
+    f_dev, _ = eng.calc_particle_distributions()
+    f, f2, c = _spectrum(eng, edges)
+    return dict(f=f, f2=f2, c=c, f_dev=f_dev, n=eng.nptl_current, steps=eng.counters().steps)
+
+
+def tail_stats(a: dict, b: dict, pmin: float, pmax: float) -> dict:
+    """Tail error of spectrum b against the FP64 spectrum a."""
     populated = np.nonzero(a["c"])[0]
     if len(populated) == 0:
         raise RuntimeError("FP64 run has an empty spectrum")
     b_hi = int(populated[-1])
-    edges = np.logspace(math.log10(workload.params["pmin"]), math.log10(workload.params["pmax"]),
-                        len(a["f"]) + 1)
+    edges = np.logspace(math.log10(pmin), math.log10(pmax), len(a["f"]) + 1)
     p_hi = edges[b_hi + 1]
     top = np.arange(len(a["f"])) [(edges[:-1] >= p_hi / 10.0) & (np.arange(len(a["f"])) <= b_hi)]
     w64, wmx = a["f"][top].sum(), b["f"][top].sum()

@@ -10,6 +10,12 @@ turbulent_shock_2d
                same kappa law along the local B, kperp/kpar = 0.05, 1e7
                particles on the shock at p0, 1e3 pushes per particle per
                interval (dt_min = dtf / 1000).
+batched_shock_2d
+               64 independent turbulent-shock runs (seeded): particles
+               log-uniform in [1e4, 1e7], r uniform in [2, 4], kappa_0
+               log-uniform in [1e-3, 1e-1], kperp/kpar uniform in [0.01, 0.2],
+               grids 512^2, 1024^2 or 2048^2 with the turbulent_shock_2d
+               fluctuation; moved together by the batched mover.
 turbulence_3d  256^3 periodic box, v rms 0.3 (30 % compressive power),
                B = z + solenoidal dB (0.3), kperp/kpar = 0.02, 1e8 particles
                uniform in space, log-uniform p in [p0, 10 p0], adaptive dt
@@ -82,6 +88,44 @@ def turbulent_shock_2d(scale: float = 1.0, n: int = 2048, dt_out: float = 0.01,
                     dict(kind="at_x", xpos=0.5, dist_flag=1),
                     np.arange(nframes + 1) * dt_out, nframes,
                     split=dict(ratio=2.72, pmin=2.0))
+
+
+def batched_shock_2d(nruns: int = 64, scale: float = 1.0, sizes=(512, 1024, 2048),
+                     dt_out: float = 0.01, pushes: int = 1000, precision: int = 1,
+                     seed: int = 11, nframes: int = 16, only: int | None = None) -> list:
+    """The runs of the batched workload, each a turbulent_shock_2d variant.
+    Fields of one size share the fluctuation (drawn once per size); the
+    shock compression differs per run.  ``only`` builds that run alone (its
+    parameters are the same as in the full list)."""
+    rng = np.random.default_rng(seed)
+    dbs = {}
+    runs = []
+    for r in range(nruns):
+        nptl = int(round(10.0 ** rng.uniform(4.0, 7.0) * scale))
+        comp = float(rng.uniform(2.0, 4.0))
+        kappa0 = float(10.0 ** rng.uniform(-3.0, -1.0))
+        kret = float(rng.uniform(0.01, 0.2))
+        n = int(sizes[rng.integers(len(sizes))])
+        if only is not None and r != only:
+            continue
+        if n not in dbs:
+            kmax = min(512.0 * np.pi, np.pi * n / 2)
+            dbs[n] = fields.kolmogorov_az_2d(n, n, 1.0, 1.0, db_rms=0.5, kmin=2.0 * np.pi,
+                                             kmax=kmax, seed=2000 + n)
+        p0 = 0.1
+        params = dict(p0=p0, pmin=p0, pmax=1.0e4 * p0, momentum_dependency=1,
+                      gamma_turb=5.0 / 3.0, mag_dependency=0, kpara0=kappa0, kret=kret,
+                      dt_min_rel=1.0 / pushes, dt_max_rel=1.0e-2, ndim=2, pbcx=1, pbcy=0, pbcz=0,
+                      npp_global=128, precision=precision, seed=seed * 1000 + r,
+                      nptl_max=max(1, nptl))
+        cfg = make_mhd_config(n, n, 1, 0.0, 1.0, 0.0, 1.0, zmin=0.0, zmax=1.0, dt_out=dt_out)
+        frame = fields.planar_shock_2d(n, n, 0.0, 1.0, 0.0, 1.0, u1=1.0, r=comp, w=0.001,
+                                       x0=0.5, db=dbs[n])
+        runs.append(Workload(f"batched_shock_2d_run{r}_{n}x{n}_r{comp:.2f}", params, cfg, frame,
+                             max(1, nptl), dict(kind="at_x", xpos=0.5, dist_flag=1),
+                             np.arange(nframes + 1) * dt_out, nframes,
+                             split=dict(ratio=2.72, pmin=2.0)))
+    return runs
 
 
 def turbulence_3d(scale: float = 1.0, n: int = 256, dt_out: float = 0.05, pushes: int = 500,
