@@ -323,6 +323,66 @@ int gpat_batch_set_tuning(gpat_batch_t *b, const gpat_batch_tuning_t *t);
 /* Device time, pushes and graph launches of the last batched mover call. */
 int gpat_batch_stats(const gpat_batch_t *b, double *ms, uint64_t *pushes, int64_t *graph_launches);
 
+/* ------------------------------------------------------------------------ */
+/* Learned splitting.  No counterpart in the reference (its split_particle   */
+/* uses fixed momentum thresholds).  An MLP importance map -- inputs x, y, z */
+/* (box-normalised), log10(p/p0), div v, |B|, |grad B| and normalised time,  */
+/* 3 hidden layers of 64 SiLU units, BF16 weights with FP32 accumulation --  */
+/* predicts the log-odds that a particle's future momentum exceeds a        */
+/* threshold.  It is trained on the GPU (hand-written forward, backward and */
+/* Adam kernels) from records of plain runs, and drives weighted splitting  */
+/* and Russian roulette with a weight window; both keep the expected weight. */
+/* ------------------------------------------------------------------------ */
+#define GPAT_MLP_FEATURES 8
+#define GPAT_MLP_PARAMS 8961   /* W1[64][8] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4 */
+typedef struct gpat_mlp gpat_mlp_t;
+/* record_capacity: training records kept on the device (0: inference only). */
+int gpat_mlp_create(int device, uint64_t seed, int64_t record_capacity, gpat_mlp_t **out);
+int gpat_mlp_destroy(gpat_mlp_t *m);
+const char *gpat_mlp_last_error(const gpat_mlp_t *m);
+/* FP32 master parameters (GPAT_MLP_PARAMS) and the feature standardisation
+ * norm = {mean[8], 1/std[8]}; either may be NULL. */
+int gpat_mlp_set_params(gpat_mlp_t *m, const float *params, const float *norm);
+int gpat_mlp_get_params(gpat_mlp_t *m, float *params, float *norm);
+/* Output (log-odds) for n host feature rows. */
+int gpat_mlp_forward(gpat_mlp_t *m, const float *x, int64_t n, float *z);
+/* Mean binary cross-entropy of n host rows with labels y, and its gradient
+ * with respect to the parameters (the BF16-rounded weights' gradient). */
+int gpat_mlp_loss_grad(gpat_mlp_t *m, const float *x, const float *y, int64_t n, float *loss,
+                       float *grad);
+/* Training records: gpat_mlp_record appends the features (time t_norm) and
+ * injection tag of every live particle of a run; gpat_mlp_label labels each
+ * record 1 when its particle's momentum at the run's current state exceeds
+ * p_threshold (plain runs: one particle per tag). */
+int gpat_mlp_clear_records(gpat_mlp_t *m);
+/* Replaces the records with n host rows of features and labels. */
+int gpat_mlp_set_records(gpat_mlp_t *m, const float *x, const float *labels, int64_t n);
+int gpat_mlp_record(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, int64_t *nrec);
+int gpat_mlp_label(gpat_mlp_t *m, gpat_handle_t *h, double p_threshold, int64_t *npos,
+                   int64_t *nrec);
+/* Adam on all positives and a neg_keep fraction of negatives (the output
+ * bias is corrected by log(neg_keep) afterwards). */
+int gpat_mlp_train(gpat_mlp_t *m, int epochs, int64_t batch, double lr, double neg_keep,
+                   uint64_t seed, double *final_loss);
+/* Over a run's live particles at time t_norm: the mean output and
+ * log(sum_i w_i exp(z_i)).  With z_ref = log_sum_wexpz - log(N) and
+ * w_ref = 1, gpat_weighted_split aims the population at N particles
+ * (sum_i w_i / w_t,i = N). */
+int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_z,
+                   double *log_sum_wexpz);
+/* Weighted split / roulette of a run's particles: target weight
+ * w_t = w_ref exp(z_ref - z), window [w_t / sqrt(window_ratio),
+ * w_t sqrt(window_ratio)]; above it a particle splits into 2^j copies
+ * (j <= max_level, children appended up to nptl_max), below it survives
+ * with probability w / w_t at weight w_t (roulette draws are Philox,
+ * keyed by the particle's tags and push counter). */
+int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
+                        double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled);
+/* Count, sum of weights and of squared weights of live particles with
+ * p > p_threshold: (sum w)^2 / sum w^2 is their effective sample size. */
+int gpat_tail_weights(gpat_handle_t *h, double p_threshold, int64_t *count, double *wsum,
+                      double *w2sum);
+
 #ifdef __cplusplus
 }
 #endif

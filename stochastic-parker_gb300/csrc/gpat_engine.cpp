@@ -1334,3 +1334,463 @@ int gpat_batch_stats(const gpat_batch_t *b, double *ms, uint64_t *pushes, int64_
     if (graph_launches) *graph_launches = b->last_graph_launches;
     return GPAT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Learned splitting: the importance network, its training records and the
+// weighted split / roulette.
+// ---------------------------------------------------------------------------
+struct gpat_mlp {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    float *master = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr;
+    __nv_bfloat16 *w16 = nullptr;
+    float *norm = nullptr;                 // mean[8], 1/std[8]
+    float host_norm[2 * kMlpFeatures] = {};
+    int adam_step = 0;
+    // records: features [cap][8], injection tag, label
+    int64_t rec_cap = 0;
+    float *feat = nullptr, *labels = nullptr;
+    int32_t *tags = nullptr;
+    unsigned long long *dcount = nullptr;  // records written; positives; scratch
+    float *p_by_tag = nullptr;
+    int64_t p_by_tag_n = 0;
+    // minibatch buffers
+    int64_t tb = 0;
+    MlpTrainBuffers t{};
+    float *xbuf = nullptr, *ybuf = nullptr, *zbuf = nullptr, *dloss = nullptr;
+    int64_t xcap = 0;
+    int64_t *index = nullptr;
+    int64_t index_cap = 0;
+};
+
+namespace {
+
+int mfail(gpat_mlp_t *m, int code, const std::string &msg) {
+    if (m) m->err = msg;
+    return code;
+}
+
+#define MCK(call)                                                                     \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return mfail(m, GPAT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int mlp_train_buffers(gpat_mlp_t *m, int64_t b) {
+    if (b <= m->tb) return GPAT_OK;
+    float *ptrs[8] = {m->t.h0, m->t.a1, m->t.a2, m->t.a3, m->t.h1, m->t.h2, m->t.h3, m->t.dz};
+    for (float *p : ptrs)
+        if (p) cudaFree(p);
+    m->t = MlpTrainBuffers{};
+    const size_t H = (size_t)kMlpHidden * (size_t)b;
+    MCK(cudaMalloc(&m->t.h0, sizeof(float) * kMlpFeatures * (size_t)b));
+    MCK(cudaMalloc(&m->t.a1, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.a2, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.a3, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.h1, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.h2, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.h3, sizeof(float) * H));
+    MCK(cudaMalloc(&m->t.dz, sizeof(float) * (size_t)b));
+    m->tb = b;
+    return GPAT_OK;
+}
+
+int mlp_xbuf(gpat_mlp_t *m, int64_t n) {
+    if (n <= m->xcap) return GPAT_OK;
+    if (m->xbuf) cudaFree(m->xbuf);
+    if (m->ybuf) cudaFree(m->ybuf);
+    if (m->zbuf) cudaFree(m->zbuf);
+    MCK(cudaMalloc(&m->xbuf, sizeof(float) * kMlpFeatures * (size_t)n));
+    MCK(cudaMalloc(&m->ybuf, sizeof(float) * (size_t)n));
+    MCK(cudaMalloc(&m->zbuf, sizeof(float) * (size_t)n));
+    m->xcap = n;
+    return GPAT_OK;
+}
+
+FeatureArgs feature_args(const gpat_handle_t *h, double t_norm) {
+    const gpat_mhd_config_t &c = h->cfg;
+    FeatureArgs g{};
+    g.rec = h->rec[0];
+    g.xmin = c.xmin; g.ymin = c.ymin; g.zmin = c.zmin;
+    g.idx = 1.0 / c.dx; g.idy = 1.0 / c.dy; g.idz = h->prm.ndim == 3 ? 1.0 / c.dz : 0.0;
+    g.ilx = 1.0 / ((double)c.nx * c.dx); g.ily = 1.0 / ((double)c.ny * c.dy);
+    g.ilz = h->prm.ndim == 3 ? 1.0 / ((double)c.nz * c.dz) : 0.0;
+    g.ip0 = 1.0 / h->prm.p0;
+    g.nxg = h->nxg; g.nyg = h->nyg; g.nzg = h->nzg;
+    g.t_norm = (float)t_norm;
+    return g;
+}
+
+}  // namespace
+
+int gpat_mlp_create(int device, uint64_t seed, int64_t record_capacity, gpat_mlp_t **out) {
+    if (!out || record_capacity < 0) return GPAT_ERR_ARG;
+    *out = nullptr;
+    gpat_mlp_t *m = new gpat_mlp_t;
+    m->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        mlp_set_kernel_attributes() != cudaSuccess) {
+        delete m;
+        return GPAT_ERR_CUDA;
+    }
+    const size_t P = kMlpParams;
+    bool ok = cudaMalloc(&m->master, 4 * P) == cudaSuccess && cudaMalloc(&m->m1, 4 * P) == cudaSuccess &&
+              cudaMalloc(&m->m2, 4 * P) == cudaSuccess && cudaMalloc(&m->grad, 4 * P) == cudaSuccess &&
+              cudaMalloc(&m->w16, 2 * P) == cudaSuccess &&
+              cudaMalloc(&m->norm, sizeof(float) * 2 * kMlpFeatures) == cudaSuccess &&
+              cudaMalloc(&m->dcount, sizeof(unsigned long long) * 4) == cudaSuccess &&
+              cudaMalloc(&m->dloss, sizeof(float)) == cudaSuccess;
+    m->rec_cap = record_capacity;
+    if (ok && record_capacity > 0)
+        ok = cudaMalloc(&m->feat, sizeof(float) * kMlpFeatures * (size_t)record_capacity) == cudaSuccess &&
+             cudaMalloc(&m->labels, sizeof(float) * (size_t)record_capacity) == cudaSuccess &&
+             cudaMalloc(&m->tags, sizeof(int32_t) * (size_t)record_capacity) == cudaSuccess;
+    if (!ok) {
+        gpat_mlp_destroy(m);
+        return GPAT_ERR_OOM;
+    }
+    // He-style initialisation from a seeded host generator (uniform, var 2/fan_in)
+    std::vector<float> w(P, 0.0f);
+    uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+    auto uni = [&]() {
+        st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+        return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+    };
+    const int H = kMlpHidden, F = kMlpFeatures;
+    auto fill = [&](size_t off, int rows, int cols) {
+        const double a = std::sqrt(6.0 / cols);
+        for (int k = 0; k < rows * cols; ++k) w[off + k] = (float)((2.0 * uni() - 1.0) * a);
+    };
+    fill(0, H, F);
+    fill((size_t)H * F + H, H, H);
+    fill((size_t)H * F + H + H * H + H, H, H);
+    fill((size_t)H * F + 2 * (H + H * H) + H - H, 1, H);   // output row
+    for (int k = 0; k < F; ++k) { m->host_norm[k] = 0.0f; m->host_norm[F + k] = 1.0f; }
+    if (cudaMemcpy(m->master, w.data(), 4 * P, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(m->m1, 0, 4 * P) != cudaSuccess || cudaMemset(m->m2, 0, 4 * P) != cudaSuccess ||
+        cudaMemset(m->grad, 0, 4 * P) != cudaSuccess ||
+        cudaMemcpy(m->norm, m->host_norm, sizeof m->host_norm, cudaMemcpyHostToDevice) != cudaSuccess ||
+        launch_to_bf16(m->master, m->w16, m->stream) != cudaSuccess ||
+        cudaMemsetAsync(m->dcount, 0, sizeof(unsigned long long) * 4, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) {
+        gpat_mlp_destroy(m);
+        return GPAT_ERR_CUDA;
+    }
+    *out = m;
+    return GPAT_OK;
+}
+
+int gpat_mlp_destroy(gpat_mlp_t *m) {
+    if (!m) return GPAT_ERR_ARG;
+    cudaSetDevice(m->device);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    void *ptrs[] = {m->master, m->m1, m->m2, m->grad, m->w16, m->norm, m->feat, m->labels, m->tags,
+                    m->dcount, m->p_by_tag, m->t.h0, m->t.a1, m->t.a2, m->t.a3, m->t.h1, m->t.h2,
+                    m->t.h3, m->t.dz, m->xbuf, m->ybuf, m->zbuf, m->dloss, m->index};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return GPAT_OK;
+}
+
+const char *gpat_mlp_last_error(const gpat_mlp_t *m) { return m ? m->err.c_str() : "null network"; }
+
+int gpat_mlp_set_params(gpat_mlp_t *m, const float *params, const float *norm) {
+    if (!m) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    if (params) {
+        MCK(cudaMemcpy(m->master, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
+        MCK(launch_to_bf16(m->master, m->w16, m->stream));
+    }
+    if (norm) {
+        std::memcpy(m->host_norm, norm, sizeof m->host_norm);
+        MCK(cudaMemcpyAsync(m->norm, m->host_norm, sizeof m->host_norm, cudaMemcpyHostToDevice,
+                            m->stream));
+    }
+    MCK(cudaStreamSynchronize(m->stream));
+    return GPAT_OK;
+}
+
+int gpat_mlp_get_params(gpat_mlp_t *m, float *params, float *norm) {
+    if (!m) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    if (params)
+        MCK(cudaMemcpy(params, m->master, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+    if (norm) std::memcpy(norm, m->host_norm, sizeof m->host_norm);
+    return GPAT_OK;
+}
+
+int gpat_mlp_forward(gpat_mlp_t *m, const float *x, int64_t n, float *z) {
+    if (!m || !x || !z || n < 0) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    int rc = mlp_xbuf(m, n);
+    if (rc) return rc;
+    MCK(cudaMemcpyAsync(m->xbuf, x, sizeof(float) * kMlpFeatures * (size_t)n,
+                        cudaMemcpyHostToDevice, m->stream));
+    MCK(launch_mlp_infer(m->w16, m->norm, m->xbuf, n, m->zbuf, m->stream));
+    MCK(cudaMemcpyAsync(z, m->zbuf, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    return GPAT_OK;
+}
+
+int gpat_mlp_loss_grad(gpat_mlp_t *m, const float *x, const float *y, int64_t n, float *loss,
+                       float *grad) {
+    if (!m || !x || !y || n < 1) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    int rc = mlp_xbuf(m, n);
+    if (rc) return rc;
+    rc = mlp_train_buffers(m, n);
+    if (rc) return rc;
+    MCK(cudaMemcpyAsync(m->xbuf, x, sizeof(float) * kMlpFeatures * (size_t)n,
+                        cudaMemcpyHostToDevice, m->stream));
+    MCK(cudaMemcpyAsync(m->ybuf, y, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, m->stream));
+    MCK(cudaMemsetAsync(m->grad, 0, sizeof(float) * kMlpParams, m->stream));
+    MCK(cudaMemsetAsync(m->dloss, 0, sizeof(float), m->stream));
+    MCK(launch_mlp_train_step(m->t, m->w16, m->norm, m->xbuf, m->ybuf, nullptr, n, m->grad,
+                              m->dloss, m->stream));
+    if (grad)
+        MCK(cudaMemcpyAsync(grad, m->grad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost,
+                            m->stream));
+    if (loss) MCK(cudaMemcpyAsync(loss, m->dloss, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaMemsetAsync(m->grad, 0, sizeof(float) * kMlpParams, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    return GPAT_OK;
+}
+
+int gpat_mlp_clear_records(gpat_mlp_t *m) {
+    if (!m) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    MCK(cudaMemsetAsync(m->dcount, 0, sizeof(unsigned long long) * 4, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    return GPAT_OK;
+}
+
+int gpat_mlp_record(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, int64_t *nrec) {
+    if (!m || !h) return GPAT_ERR_ARG;
+    if (m->rec_cap <= 0) return mfail(m, GPAT_ERR_STATE, "no record capacity");
+    if (!h->rec_ready[0]) return mfail(m, GPAT_ERR_STATE, "run has no fields");
+    MCK(cudaSetDevice(m->device));
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return mfail(m, GPAT_ERR_CUDA, "run stream");
+    MCK(launch_record_features(feature_args(h, t_norm), h->prm.ndim, h->P[h->cur], h->n, m->feat,
+                               m->tags, m->dcount, m->rec_cap, m->stream));
+    unsigned long long c = 0;
+    MCK(cudaMemcpyAsync(&c, m->dcount, sizeof c, cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    if (nrec) *nrec = (int64_t)std::min<unsigned long long>(c, (unsigned long long)m->rec_cap);
+    return GPAT_OK;
+}
+
+int gpat_mlp_label(gpat_mlp_t *m, gpat_handle_t *h, double p_threshold, int64_t *npos,
+                   int64_t *nrec) {
+    if (!m || !h) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    unsigned long long c = 0;
+    MCK(cudaMemcpy(&c, m->dcount, sizeof c, cudaMemcpyDeviceToHost));
+    const int64_t n = (int64_t)std::min<unsigned long long>(c, (unsigned long long)m->rec_cap);
+    const int64_t ntags = std::max<int64_t>(1, h->tag_max);
+    if (ntags > m->p_by_tag_n) {
+        if (m->p_by_tag) cudaFree(m->p_by_tag);
+        m->p_by_tag = nullptr;
+        MCK(cudaMalloc(&m->p_by_tag, sizeof(float) * (size_t)ntags));
+        m->p_by_tag_n = ntags;
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return mfail(m, GPAT_ERR_CUDA, "run stream");
+    MCK(cudaMemsetAsync(m->dcount + 1, 0, sizeof(unsigned long long), m->stream));
+    MCK(launch_label_records(h->P[h->cur], h->n, m->tags, n, m->p_by_tag, ntags,
+                             (float)p_threshold, m->labels, m->dcount + 1, m->stream));
+    unsigned long long pos = 0;
+    MCK(cudaMemcpyAsync(&pos, m->dcount + 1, sizeof pos, cudaMemcpyDeviceToHost, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    if (npos) *npos = (int64_t)pos;
+    if (nrec) *nrec = n;
+    return GPAT_OK;
+}
+
+int gpat_mlp_train(gpat_mlp_t *m, int epochs, int64_t batch, double lr, double neg_keep,
+                   uint64_t seed, double *final_loss) {
+    if (!m || epochs < 1 || batch < 32 || !(lr > 0.0) || !(neg_keep > 0.0) || neg_keep > 1.0)
+        return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    unsigned long long c = 0;
+    MCK(cudaMemcpy(&c, m->dcount, sizeof c, cudaMemcpyDeviceToHost));
+    const int64_t n = (int64_t)std::min<unsigned long long>(c, (unsigned long long)m->rec_cap);
+    if (n < 1) return mfail(m, GPAT_ERR_STATE, "no labelled records");
+    // Training set: every positive and a neg_keep fraction of negatives,
+    // shuffled each epoch on the host (seeded).
+    std::vector<float> lab((size_t)n);
+    MCK(cudaMemcpy(lab.data(), m->labels, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost));
+    uint64_t st = seed * 0xD1B54A32D192ED03ull + 7;
+    auto next = [&]() {
+        st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+        return st;
+    };
+    std::vector<int64_t> keep;
+    keep.reserve((size_t)n);
+    const uint64_t thr = (uint64_t)(neg_keep * 18446744073709551615.0);
+    for (int64_t i = 0; i < n; ++i)
+        if (lab[(size_t)i] > 0.5f || next() <= thr) keep.push_back(i);
+    if (keep.empty()) return mfail(m, GPAT_ERR_STATE, "empty training set");
+    // Feature standardisation from up to 4096 kept records spread evenly.
+    {
+        const size_t ns = std::min<size_t>(keep.size(), 4096);
+        std::vector<float> row(kMlpFeatures);
+        double sum[kMlpFeatures] = {}, sq[kMlpFeatures] = {};
+        for (size_t k = 0; k < ns; ++k) {
+            const size_t idx = (size_t)keep[(k * keep.size()) / ns];
+            MCK(cudaMemcpy(row.data(), m->feat + idx * kMlpFeatures, sizeof(float) * kMlpFeatures,
+                           cudaMemcpyDeviceToHost));
+            for (int j = 0; j < kMlpFeatures; ++j) {
+                sum[j] += row[j];
+                sq[j] += (double)row[j] * row[j];
+            }
+        }
+        for (int j = 0; j < kMlpFeatures; ++j) {
+            const double mu = sum[j] / (double)ns;
+            const double var = std::max(sq[j] / (double)ns - mu * mu, 1e-12);
+            m->host_norm[j] = (float)mu;
+            m->host_norm[kMlpFeatures + j] = (float)(1.0 / std::sqrt(var));
+        }
+        MCK(cudaMemcpy(m->norm, m->host_norm, sizeof m->host_norm, cudaMemcpyHostToDevice));
+    }
+    const int64_t b = std::min<int64_t>(batch, (int64_t)keep.size());
+    int rc = mlp_train_buffers(m, b);
+    if (rc) return rc;
+    if ((int64_t)keep.size() > m->index_cap) {
+        if (m->index) cudaFree(m->index);
+        m->index = nullptr;
+        MCK(cudaMalloc(&m->index, sizeof(int64_t) * keep.size()));
+        m->index_cap = (int64_t)keep.size();
+    }
+    double last = 0.0;
+    for (int e = 0; e < epochs; ++e) {
+        for (size_t k = keep.size(); k > 1; --k) std::swap(keep[k - 1], keep[next() % k]);
+        MCK(cudaMemcpyAsync(m->index, keep.data(), sizeof(int64_t) * keep.size(),
+                            cudaMemcpyHostToDevice, m->stream));
+        MCK(cudaMemsetAsync(m->dloss, 0, sizeof(float), m->stream));
+        int64_t batches = 0;
+        for (int64_t s0 = 0; s0 + b <= (int64_t)keep.size(); s0 += b, ++batches) {
+            MCK(launch_mlp_train_step(m->t, m->w16, m->norm, m->feat, m->labels, m->index + s0, b,
+                                      m->grad, m->dloss, m->stream));
+            MCK(launch_adam(m->master, m->m1, m->m2, m->grad, m->w16, (float)lr, ++m->adam_step,
+                            m->stream));
+        }
+        float l = 0.0f;
+        MCK(cudaMemcpyAsync(&l, m->dloss, sizeof l, cudaMemcpyDeviceToHost, m->stream));
+        MCK(cudaStreamSynchronize(m->stream));
+        last = batches > 0 ? (double)l / (double)batches : 0.0;
+    }
+    // Negatives were kept with probability neg_keep: shift the output bias
+    // by log(neg_keep) so that sigmoid(z) estimates the true probability.
+    float b4 = 0.0f;
+    MCK(cudaMemcpy(&b4, m->master + (kMlpParams - 1), sizeof b4, cudaMemcpyDeviceToHost));
+    b4 += (float)std::log(neg_keep);
+    MCK(cudaMemcpy(m->master + (kMlpParams - 1), &b4, sizeof b4, cudaMemcpyHostToDevice));
+    MCK(launch_to_bf16(m->master, m->w16, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    if (final_loss) *final_loss = last;
+    return GPAT_OK;
+}
+
+int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_z,
+                   double *log_sum_wexpz) {
+    if (!m || !h) return GPAT_ERR_ARG;
+    MCK(cudaSetDevice(m->device));
+    const int64_t n = h->n;
+    if (n < 1) return mfail(m, GPAT_ERR_STATE, "no particles");
+    int rc = mlp_xbuf(m, n);
+    if (rc) return rc;
+    unsigned long long *out = nullptr;
+    MCK(cudaMalloc(&out, 5 * sizeof(unsigned long long) + sizeof(int)));
+    int *zmax_key = reinterpret_cast<int *>(out + 5);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        cudaFree(out);
+        return mfail(m, GPAT_ERR_CUDA, "run stream");
+    }
+    unsigned long long r[5] = {};
+    int key = 0;
+    cudaError_t e = launch_score(m->w16, m->norm, feature_args(h, t_norm), h->prm.ndim, h->P[h->cur],
+                                 n, m->zbuf, zmax_key, out, m->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r, out, sizeof r, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&key, zmax_key, sizeof key, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    cudaFree(out);
+    if (e != cudaSuccess) return mfail(m, GPAT_ERR_CUDA, cudaGetErrorString(e));
+    if (r[0] == 0) return mfail(m, GPAT_ERR_STATE, "no live particles");
+    const int kb = key >= 0 ? key : key ^ 0x7FFFFFFF;
+    float zmax;
+    std::memcpy(&zmax, &kb, sizeof zmax);
+    if (mean_z) *mean_z = fixed_to_double(r[1], r[2]) / (double)r[0] - 64.0;
+    if (log_sum_wexpz) *log_sum_wexpz = (double)zmax + std::log(fixed_to_double(r[3], r[4]));
+    return GPAT_OK;
+}
+
+int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
+                        double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled) {
+    if (!h || !m || !(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8)
+        return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return fail(h, GPAT_ERR_CUDA, "network stream");
+    int rc = pull_counters(h);
+    if (rc) return rc;
+    const unsigned long long split0 = h->hcnt.nsplit, kill0 = h->hcnt.nkilled;
+    WSplitArgs a{};
+    a.w_ref = w_ref;
+    a.z_ref = z_ref;
+    a.sqrt_ratio = std::sqrt(window_ratio);
+    a.max_level = max_level;
+    a.key0 = (uint32_t)h->prm.seed;
+    a.key1 = (uint32_t)(h->prm.seed >> 32) + 2u;
+    // the child counter starts at n; children are appended up to nptl_max
+    unsigned long long n0 = (unsigned long long)h->n;
+    CK(cudaMemcpyAsync(&h->dcnt->ncells, &n0, sizeof n0, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_weighted_split(m->w16, m->norm, feature_args(h, t_norm), h->prm.ndim, h->P[h->cur],
+                             h->n, h->cap, a, &h->dcnt->ncells, h->dcnt, h->stream));
+    rc = pull_counters(h);
+    if (rc) return rc;
+    const int64_t created = (int64_t)h->hcnt.nsplit - (int64_t)split0;
+    h->n = (int64_t)h->hcnt.ncells;
+    h->nptl_split += created;
+    if (created > 0 || h->hcnt.nkilled != kill0) h->unsorted = true;
+    if (nsplit) *nsplit = created;
+    if (nkilled) *nkilled = (int64_t)(h->hcnt.nkilled - kill0);
+    return check_status(h);
+}
+
+int gpat_tail_weights(gpat_handle_t *h, double p_threshold, int64_t *count, double *wsum,
+                      double *w2sum) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    unsigned long long *out = nullptr;
+    CK(cudaMalloc(&out, 5 * sizeof(unsigned long long)));
+    unsigned long long r[5] = {};
+    cudaError_t e = launch_tail(h->P[h->cur], h->n, p_threshold, out, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(r, out, sizeof r, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(h, GPAT_ERR_CUDA, cudaGetErrorString(e));
+    if (count) *count = (int64_t)r[0];
+    if (wsum) *wsum = fixed_to_double(r[1], r[2]);
+    if (w2sum) *w2sum = fixed_to_double(r[3], r[4]);
+    return GPAT_OK;
+}
+
+int gpat_mlp_set_records(gpat_mlp_t *m, const float *x, const float *labels, int64_t n) {
+    if (!m || !x || !labels || n < 0) return GPAT_ERR_ARG;
+    if (n > m->rec_cap) return mfail(m, GPAT_ERR_CAPACITY, "more records than the capacity");
+    MCK(cudaSetDevice(m->device));
+    MCK(cudaMemcpyAsync(m->feat, x, sizeof(float) * kMlpFeatures * (size_t)n,
+                        cudaMemcpyHostToDevice, m->stream));
+    MCK(cudaMemcpyAsync(m->labels, labels, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice,
+                        m->stream));
+    unsigned long long c = (unsigned long long)n;
+    MCK(cudaMemcpyAsync(m->dcount, &c, sizeof c, cudaMemcpyHostToDevice, m->stream));
+    MCK(cudaStreamSynchronize(m->stream));
+    return GPAT_OK;
+}

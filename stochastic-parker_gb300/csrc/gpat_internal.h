@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "gpat_engine.h"
@@ -38,6 +39,7 @@ struct DevCounters {
     unsigned long long wsum_hi, wsum_lo, dtsum_hi, dtsum_lo;
     unsigned long long nactive;   // particles a chunked mover launch left mid-interval
     unsigned long long ncells;    // get_ncells_large_* result
+    unsigned long long nkilled;   // particles removed by roulette
     double dt_min, dt_max;
     unsigned int status;
     unsigned int pad;
@@ -117,6 +119,29 @@ struct BatchRun {
     MixedRunArgs a;
     MixedConsts k;
     DevParticles P[2];
+};
+
+// Learned splitting (learned.cu).
+constexpr int kMlpFeatures = 8;
+constexpr int kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpFeatures + kMlpHidden + 2 * (kMlpHidden * kMlpHidden +
+                                                                          kMlpHidden) +
+                           kMlpHidden + 1;
+// Particle features: interpolation from the packed records plus the box.
+struct FeatureArgs {
+    const float *rec;
+    double xmin, ymin, zmin, idx, idy, idz, ilx, ily, ilz, ip0;
+    int nxg, nyg, nzg;
+    float t_norm;
+};
+struct WSplitArgs {
+    double w_ref, z_ref, sqrt_ratio;
+    int max_level;
+    uint32_t key0, key1;
+};
+// Per-minibatch activations ([64][b] except h0: [b][8]) and output deltas.
+struct MlpTrainBuffers {
+    float *h0, *a1, *a2, *a3, *h1, *h2, *h3, *dz;
 };
 
 // Launchers (defined in the .cu files).  All enqueue on `s`.
@@ -226,5 +251,35 @@ cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double p
 // quick_check reductions into cnt (wsum, dtsum, dt_min, dt_max).
 cudaError_t launch_quick_check(const DevParticles &P, int64_t n, DevCounters *cnt,
                                cudaStream_t s);
+
+// Learned splitting launchers (learned.cu).
+size_t mlp_shared_bytes();
+cudaError_t mlp_set_kernel_attributes();
+cudaError_t launch_to_bf16(const float *master, __nv_bfloat16 *w16, cudaStream_t s);
+cudaError_t launch_mlp_infer(const __nv_bfloat16 *w16, const float *norm, const float *x, int64_t n,
+                             float *z, cudaStream_t s);
+cudaError_t launch_mlp_train_step(const MlpTrainBuffers &t, const __nv_bfloat16 *w16,
+                                  const float *norm, const float *x, const float *y,
+                                  const int64_t *index, int64_t b, float *grad, float *loss,
+                                  cudaStream_t s);
+cudaError_t launch_adam(float *master, float *m1, float *m2, float *grad, __nv_bfloat16 *w16,
+                        float lr, int step, cudaStream_t s);
+cudaError_t launch_record_features(const FeatureArgs &g, int ndim, const DevParticles &P, int64_t n,
+                                   float *feat, int32_t *tags, unsigned long long *count,
+                                   int64_t cap, cudaStream_t s);
+cudaError_t launch_label_records(const DevParticles &P, int64_t n, const int32_t *tags,
+                                 int64_t nrec, float *p_by_tag, int64_t ntags, float threshold,
+                                 float *labels, unsigned long long *npos, cudaStream_t s);
+cudaError_t launch_weighted_split(const __nv_bfloat16 *w16, const float *norm,
+                                  const FeatureArgs &g, int ndim, const DevParticles &P,
+                                  int64_t n, int64_t cap, const WSplitArgs &a,
+                                  unsigned long long *count, DevCounters *cnt, cudaStream_t s);
+cudaError_t launch_tail(const DevParticles &P, int64_t n, double pthr, unsigned long long *out,
+                        cudaStream_t s);
+// z of every live particle (index-aligned), its maximum (order-preserving
+// int key), and exact sums out = {count, sum(z + 64) hi/lo, sum(w exp(z - zmax)) hi/lo}.
+cudaError_t launch_score(const __nv_bfloat16 *w16, const float *norm, const FeatureArgs &g,
+                         int ndim, const DevParticles &P, int64_t n, float *z, int *zmax_key,
+                         unsigned long long *out, cudaStream_t s);
 
 }  // namespace gpat

@@ -100,6 +100,9 @@ class Counters(C.Structure):
 
 Handle = C.c_void_p
 Batch = C.c_void_p
+Mlp = C.c_void_p
+MLP_FEATURES = 8
+MLP_PARAMS = 8961
 
 
 class BatchTuning(C.Structure):
@@ -134,6 +137,22 @@ SIGNATURES = {
     "gpat_batch_get_tuning": (C.c_int, [Batch, P(BatchTuning)]),
     "gpat_batch_set_tuning": (C.c_int, [Batch, P(BatchTuning)]),
     "gpat_batch_stats": (C.c_int, [Batch, P(d), P(u64), P(i64)]),
+    "gpat_mlp_create": (C.c_int, [C.c_int, u64, i64, P(Mlp)]),
+    "gpat_mlp_destroy": (C.c_int, [Mlp]),
+    "gpat_mlp_last_error": (C.c_char_p, [Mlp]),
+    "gpat_mlp_set_params": (C.c_int, [Mlp, P(C.c_float), P(C.c_float)]),
+    "gpat_mlp_get_params": (C.c_int, [Mlp, P(C.c_float), P(C.c_float)]),
+    "gpat_mlp_forward": (C.c_int, [Mlp, P(C.c_float), i64, P(C.c_float)]),
+    "gpat_mlp_loss_grad": (C.c_int, [Mlp, P(C.c_float), P(C.c_float), i64, P(C.c_float),
+                                     P(C.c_float)]),
+    "gpat_mlp_clear_records": (C.c_int, [Mlp]),
+    "gpat_mlp_set_records": (C.c_int, [Mlp, P(C.c_float), P(C.c_float), i64]),
+    "gpat_mlp_record": (C.c_int, [Mlp, Handle, d, P(i64)]),
+    "gpat_mlp_label": (C.c_int, [Mlp, Handle, d, P(i64), P(i64)]),
+    "gpat_mlp_train": (C.c_int, [Mlp, C.c_int, i64, d, d, u64, P(d)]),
+    "gpat_mlp_score": (C.c_int, [Mlp, Handle, d, P(d), P(d)]),
+    "gpat_weighted_split": (C.c_int, [Handle, Mlp, d, d, d, d, C.c_int, P(i64), P(i64)]),
+    "gpat_tail_weights": (C.c_int, [Handle, d, P(i64), P(d), P(d)]),
     "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),
     "gpat_inject_particles_at_large": (C.c_int, [Handle, C.c_int, i64, d, C.c_int, d, C.c_int,
                                                  C.c_int, d, i64, P(d), d, P(i64)]),

@@ -31,6 +31,7 @@ SOURCES = {
     "mover_fp64.cu": ["-fmad=false"],
     "mover_mixed.cu": [],
     "noalloc.cu": [],
+    "learned.cu": [],
 }
 
 

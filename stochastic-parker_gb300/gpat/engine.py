@@ -421,3 +421,102 @@ class Batch:
         if self.b:
             self.lib.gpat_batch_destroy(self.b)
             self.b = _abi.Batch()
+
+
+class Mlp:
+    """The learned-splitting importance network (gpat_mlp_*)."""
+
+    def __init__(self, device: int = 0, seed: int = 1, record_capacity: int = 0):
+        self.lib = _abi.load()
+        self.m = _abi.Mlp()
+        rc = self.lib.gpat_mlp_create(device, seed, int(record_capacity), C.byref(self.m))
+        if rc != _abi.GPAT_OK:
+            raise GPATError(rc, "gpat_mlp_create failed")
+
+    def _check(self, rc: int):
+        if rc != _abi.GPAT_OK:
+            raise GPATError(rc, self.lib.gpat_mlp_last_error(self.m).decode())
+
+    @staticmethod
+    def _f32(a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+    def set_params(self, params=None, norm=None):
+        p, pp = self._f32(params) if params is not None else (None, None)
+        q, qq = self._f32(norm) if norm is not None else (None, None)
+        self._check(self.lib.gpat_mlp_set_params(self.m, pp, qq))
+
+    def get_params(self):
+        p = np.zeros(_abi.MLP_PARAMS, np.float32)
+        q = np.zeros(2 * _abi.MLP_FEATURES, np.float32)
+        self._check(self.lib.gpat_mlp_get_params(self.m, self._f32(p)[1], self._f32(q)[1]))
+        return p, q
+
+    def forward(self, x) -> np.ndarray:
+        x, xp = self._f32(x)
+        z = np.zeros(len(x), np.float32)
+        self._check(self.lib.gpat_mlp_forward(self.m, xp, len(x),
+                                              z.ctypes.data_as(C.POINTER(C.c_float))))
+        return z
+
+    def loss_grad(self, x, y):
+        x, xp = self._f32(x)
+        y, yp = self._f32(y)
+        loss = C.c_float()
+        g = np.zeros(_abi.MLP_PARAMS, np.float32)
+        self._check(self.lib.gpat_mlp_loss_grad(self.m, xp, yp, len(x), C.byref(loss),
+                                                g.ctypes.data_as(C.POINTER(C.c_float))))
+        return float(loss.value), g
+
+    def set_records(self, x, labels):
+        x, xp = self._f32(x)
+        y, yp = self._f32(labels)
+        self._check(self.lib.gpat_mlp_set_records(self.m, xp, yp, len(x)))
+
+    def clear_records(self):
+        self._check(self.lib.gpat_mlp_clear_records(self.m))
+
+    def record(self, eng, t_norm) -> int:
+        n = C.c_int64()
+        self._check(self.lib.gpat_mlp_record(self.m, eng.h, t_norm, C.byref(n)))
+        return n.value
+
+    def label(self, eng, p_threshold):
+        npos, nrec = C.c_int64(), C.c_int64()
+        self._check(self.lib.gpat_mlp_label(self.m, eng.h, p_threshold, C.byref(npos),
+                                            C.byref(nrec)))
+        return npos.value, nrec.value
+
+    def train(self, epochs=3, batch=8192, lr=2e-3, neg_keep=1.0, seed=1) -> float:
+        loss = C.c_double()
+        self._check(self.lib.gpat_mlp_train(self.m, epochs, batch, lr, neg_keep, seed,
+                                            C.byref(loss)))
+        return loss.value
+
+    def score(self, eng, t_norm):
+        """(mean z, log sum w exp(z)) over the run's live particles."""
+        z, lse = C.c_double(), C.c_double()
+        self._check(self.lib.gpat_mlp_score(self.m, eng.h, t_norm, C.byref(z), C.byref(lse)))
+        return z.value, lse.value
+
+    def close(self):
+        if self.m:
+            self.lib.gpat_mlp_destroy(self.m)
+            self.m = _abi.Mlp()
+
+
+def weighted_split(eng, mlp: Mlp, t_norm, w_ref, z_ref, window_ratio=4.0, max_level=4):
+    """gpat_weighted_split; returns (children created, particles killed)."""
+    ns, nk = C.c_int64(), C.c_int64()
+    eng._check(eng.lib.gpat_weighted_split(eng.h, mlp.m, t_norm, w_ref, z_ref, window_ratio,
+                                           max_level, C.byref(ns), C.byref(nk)))
+    return ns.value, nk.value
+
+
+def tail_weights(eng, p_threshold):
+    """(count, sum w, sum w^2) of live particles with p > p_threshold."""
+    n, w, w2 = C.c_int64(), C.c_double(), C.c_double()
+    eng._check(eng.lib.gpat_tail_weights(eng.h, p_threshold, C.byref(n), C.byref(w),
+                                         C.byref(w2)))
+    return n.value, w.value, w2.value

@@ -1,0 +1,96 @@
+"""Learned splitting: the network's GPU forward and gradient against the CPU
+oracle (oracle/mlp_oracle.py), training, and weighted splitting / roulette
+driven by the trained network on a 3D run (unbiased tail, more effective
+samples, unique lineage tags)."""
+import math
+
+import numpy as np
+import pytest
+
+import mlp_oracle as mo
+from gpat import configs
+from gpat.engine import Mlp, tail_weights, weighted_split
+
+pytestmark = pytest.mark.gpu
+
+
+def test_forward_and_gradient_match_oracle():
+    rng = np.random.default_rng(2)
+    m = Mlp(seed=3)
+    params = mo.init_params(7)
+    norm = np.concatenate([rng.normal(size=8) * 0.1, 1.0 + rng.random(8)]).astype(np.float32)
+    m.set_params(params, norm)
+    x = rng.normal(size=(5000, 8)).astype(np.float32)
+    z = m.forward(x)
+    zr = mo.forward(params, norm.astype(np.float64), x)
+    np.testing.assert_allclose(z, zr, rtol=1e-4, atol=1e-4)
+    y = (rng.random(5000) < 0.2).astype(np.float32)
+    loss, g = m.loss_grad(x, y)
+    lr, gr = mo.loss_grad(params, norm.astype(np.float64), x, y)
+    assert abs(loss - lr) < 1e-4 * max(1.0, abs(lr))
+    np.testing.assert_allclose(g, gr, rtol=2e-3, atol=2e-3 * np.abs(gr).max())
+    p2, n2 = m.get_params()
+    assert np.array_equal(p2, params) and np.array_equal(n2, norm)
+    m.close()
+
+
+def test_training_learns_a_rule():
+    rng = np.random.default_rng(4)
+    n = 200_000
+    x = rng.normal(size=(n, 8)).astype(np.float32)
+    logit = 2.0 * x[:, 0] - 1.5 * x[:, 3] * x[:, 3] + 1.0
+    y = (rng.random(n) < 1.0 / (1.0 + np.exp(-logit))).astype(np.float32)
+    m = Mlp(seed=5, record_capacity=n)
+    m.set_records(x, y)
+    l0, _ = m.loss_grad(x[:20000], y[:20000])
+    m.train(epochs=4, batch=4096, lr=3e-3, seed=2)
+    l1, _ = m.loss_grad(x[:20000], y[:20000])
+    # the Bayes loss of this rule is about 0.43; an untrained net sits near 0.7+
+    assert l1 < 0.5 and l1 < l0 - 0.1
+    m.close()
+
+
+def test_learned_splitting_3d_unbiased_and_more_samples():
+    n_grid, nptl, nint = 32, 20000, 8
+    w = configs.turbulence_3d(scale=nptl / 1e8, n=n_grid, nframes=nint)
+
+    def run(recorder=None, learned=None, target=None):
+        eng = configs.build_engine(w, nptl_max=nptl * 40)
+        configs.inject(eng, w)
+        pushes = 0
+        for k in range(nint):
+            if learned is not None:
+                # importance-weighted population of about `target` particles
+                _, lse = learned.score(eng, k / nint)
+                weighted_split(eng, learned, k / nint, 1.0, lse - math.log(target),
+                               window_ratio=4.0, max_level=3)
+            if recorder is not None:
+                recorder.record(eng, k / nint)
+            eng.particle_mover(mhd_tframe=k + 1)
+            pushes += eng.counters().last_mover_steps
+        return eng, pushes
+
+    net = Mlp(seed=9, record_capacity=nptl * nint)
+    plain, pushes_plain = run(recorder=net)
+    # threshold: the top 2 % of the plain run's final momenta
+    pthr = float(np.quantile(plain.get_particles()["p"], 0.98))
+    npos, nrec = net.label(plain, pthr)
+    assert nrec > 0 and 0 < npos < nrec
+    net.train(epochs=4, batch=4096, lr=3e-3, seed=3)
+    c0, w0, w20 = tail_weights(plain, pthr)
+    eng_l, pushes_l = run(learned=net, target=2 * nptl)
+    c1, w1, w21 = tail_weights(eng_l, pthr)
+    ps = eng_l.get_particles()
+    # unbiased: both runs start from the same total weight, so the tail
+    # weights agree within their Monte Carlo errors
+    assert abs(w1 - w0) < 4.0 * math.sqrt(w20 + w21), (w0, w1, w20, w21)
+    # more effective samples in the tail per push
+    ess0, ess1 = w0 * w0 / w20, w1 * w1 / w21
+    assert ess1 / pushes_l > 1.5 * ess0 / pushes_plain, (ess0, ess1, pushes_plain, pushes_l)
+    # lineage tags stay unique
+    key = (ps["tag_injected"].astype(np.int64) << 32) | (ps["tag_splitted"].astype(np.int64) &
+                                                         0xFFFFFFFF)
+    assert len(np.unique(key)) == len(key)
+    for e in (plain, eng_l):
+        e.close()
+    net.close()
