@@ -42,7 +42,7 @@ UNIT = "particle-steps/s"
 # 3D: 8 corners x 21 values.
 GATHER_BYTES_PER_STEP = {2: 4 * 15 * 4, 3: 8 * 21 * 4}
 STATE_BYTES_PER_PARTICLE = 2 * (7 * 8 + 2 + 4 * 4)
-WORKLOADS = ("turbulent_shock_2d", "turbulence_3d", "batched_shock_2d")
+WORKLOADS = ("turbulent_shock_2d", "turbulence_3d", "batched_shock_2d", "learned_3d")
 
 
 # The run of the batched workload the CPU baselines sample (its first run).
@@ -55,7 +55,7 @@ def make_workload(args, precision, seed=None, nframes=16, scale=None):
     if args.workload == "batched_shock_2d":
         return configs.batched_shock_2d(scale=scale, precision=precision, nframes=nframes,
                                         only=BATCH_SAMPLE_RUN)[0]
-    if args.workload == "turbulence_3d":
+    if args.workload in ("turbulence_3d", "learned_3d"):
         grid = args.grid if args.grid != 2048 else 256
         return configs.turbulence_3d(scale=scale, n=grid, precision=precision,
                                      seed=3 if seed is None else seed, nframes=nframes)
@@ -621,6 +621,122 @@ def run_batch(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args, world, rank, local):
+    """Learned splitting on the 3D compressible-turbulence field: a plain run
+    generates training records, the network is trained on the GPU, then
+    plain, fixed-threshold and learned splitting runs of the same size are
+    timed and their effective samples in the momentum tail compared."""
+    import numpy as np
+    import torch
+    from gpat import configs
+    from gpat.engine import GPATCapacityError, Mlp, tail_weights, weighted_split
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nint = 16
+    n_train = max(1000, int(2e6 * args.scale))
+    n_cmp = max(1000, int(1e6 * args.scale))
+    w = make_workload(args, 1, seed=3 + rank, nframes=nint, scale=n_train / 1e8)
+    p0 = w.params["p0"]
+    fixed_ratio, fixed_pmin = 1.5, 6.0
+
+    def arm(kind, n, seed, recorder=None, net=None, target=None, cap=None):
+        eng = configs.build_engine(w, device=local, nptl_max=cap or 2 * n, seed=seed)
+        configs.inject(eng, w, nptl=n)
+        pushes, capped = 0, False
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(nint):
+            if kind == "learned":
+                _, lse = net.score(eng, k / nint)
+                weighted_split(eng, net, k / nint, 1.0, lse - math.log(target), window_ratio=4.0,
+                               max_level=3)
+            if recorder is not None:
+                recorder.record(eng, k / nint)
+            eng.particle_mover(mhd_tframe=k + 1)
+            pushes += eng.counters().last_mover_steps
+            if kind == "fixed" and not capped:
+                try:
+                    eng.split_particle(fixed_ratio, fixed_pmin, 10)
+                except GPATCapacityError:
+                    capped = True
+        torch.cuda.synchronize()
+        return eng, pushes, time.perf_counter() - t0
+
+    # 1. plain run generating the training records
+    net = Mlp(device=local, seed=7 + rank, record_capacity=n_train * nint)
+    eng, train_pushes, train_s = arm("plain", n_train, 100 + rank, recorder=net)
+    p_end = eng.get_particles()["p"]
+    pthr = float(np.quantile(p_end, 0.999))
+    npos, nrec = net.label(eng, pthr)
+    eng.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = net.train(epochs=3, batch=8192, lr=3e-3, neg_keep=0.25, seed=5)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+
+    # 2. the three arms on fresh particles (another injection seed)
+    out = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    # the plain arm runs 4x the particles: it is the tail reference
+    for kind, n, kw in (("plain", 4 * n_cmp, {}), ("fixed", n_cmp, dict(cap=16 * n_cmp)),
+                        ("learned", n_cmp, dict(net=net, target=2 * n_cmp, cap=16 * n_cmp))):
+        e, pushes, secs = arm(kind, n, 200 + rank, **kw)
+        c, ws, w2 = tail_weights(e, pthr)
+        ess = ws * ws / w2 if w2 > 0 else 0.0
+        out[kind] = {"particles": n, "pushes": pushes, "seconds": secs,
+                     "particle_steps_per_s": pushes / secs,
+                     "tail_particles": c, "tail_weight": ws,
+                     "tail_weight_sigma": math.sqrt(w2), "ess": ess,
+                     "ess_per_s": ess / secs, "final_particles": e.nptl_current}
+        e.close()
+    clk = clocks.stop()
+    net.close()
+    # tail fractions (weight above the threshold per injected weight)
+    for d in out.values():
+        d["tail_fraction"] = d["tail_weight"] / d["particles"]
+        d["tail_fraction_sigma"] = d["tail_weight_sigma"] / d["particles"]
+    ref = out["plain"]
+    learned = out["learned"]
+    for kind in ("fixed", "learned"):
+        d = out[kind]
+        if ref["tail_fraction"] > 0:
+            d["tail_err_vs_plain"] = d["tail_fraction"] / ref["tail_fraction"] - 1.0
+            d["tail_err_sigma"] = math.hypot(d["tail_fraction_sigma"],
+                                             ref["tail_fraction_sigma"]) / ref["tail_fraction"]
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": learned["particle_steps_per_s"], "unit": UNIT,
+            "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": 1e3 * learned["seconds"] / nint,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+ff", "data": "synthetic",
+            "config": {"workload": f"learned_splitting_{w.name}", "particles": n_cmp,
+                       "intervals": nint,
+                       "step": "one MHD interval of the learned-splitting arm (weighted split + "
+                               "particle_mover)",
+                       "threshold_p_over_p0": pthr / p0,
+                       "threshold_rule": "99.9th percentile of the plain run's final momenta "
+                                         "(no particle of this field reaches 100 p0 in the run)",
+                       "l2": "inputs exceed L2 (256^3 field records 1.7 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk,
+            "gpu_launches": None,
+            "e2e": None,
+            "learned_splitting": {
+                "network": "8-64-64-64-1 SiLU, BF16 weights, FP32 accumulation",
+                "training": {"trajectories": n_train, "records": nrec, "positives": npos,
+                             "plain_run_seconds": train_s, "fit_seconds": fit_s,
+                             "final_loss": loss, "epochs": 3, "negatives_kept": 0.25},
+                "fixed_threshold": {"split_ratio": fixed_ratio, "pmin_split": fixed_pmin},
+                "arms": out,
+                "ess_per_s_learned_over_fixed": learned["ess_per_s"] / max(out["fixed"]["ess_per_s"], 1e-30),
+                "ess_per_s_learned_over_plain": learned["ess_per_s"] / max(out["plain"]["ess_per_s"], 1e-30)}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
@@ -628,6 +744,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "batched_shock_2d":
         run_batch(args, world, rank, local)
+    elif args.workload == "learned_3d":
+        run_learned(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:
