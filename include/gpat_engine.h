@@ -81,10 +81,13 @@ typedef struct gpat_params {
     int64_t nptl_max;           /* particle capacity (init_particles)          */
     int32_t time_interp;        /* 1: two field frames, linear in time         */
     /* dpp_wave / dpp_shear: momentum diffusion by wave scattering and flow
-     * shear (set_dpp_params, particle_module.f90:255-272), FP64 precision
-     * only.  Options of the reference that this engine rejects with
-     * GPAT_ERR_UNSUPPORTED when non-zero: deltab_flag, correlation_flag,
-     * include_3rd_dim, spherical_coord, nonuniform_grid. */
+     * shear (set_dpp_params, particle_module.f90:255-272); deltab_flag /
+     * correlation_flag: spatially dependent turbulence variance and
+     * correlation length (set_flags_params :285-300, inputs through
+     * gpat_read_magnetic_fluctuation / gpat_read_correlation_length).  These
+     * four need GPAT_PREC_FP64.  Options of the reference that this engine
+     * rejects with GPAT_ERR_UNSUPPORTED when non-zero: include_3rd_dim,
+     * spherical_coord, nonuniform_grid. */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of
@@ -159,6 +162,21 @@ int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nva
 /* read_field_data_parallel from a raw mhd_data_XXXX file (8 vars). */
 int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag);
 /* calc_fields_gradients (mhd_data_parallel.f90:504-610) on the device. */
+/* Turbulence variance and correlation length (deltab_flag /
+ * correlation_flag runs): read_magnetic_fluctuation and
+ * read_correlation_length (mhd_data_parallel.f90:306-497) read a file of two
+ * FP32 arrays over every ghost-padded node (slab, then 2D component); the
+ * gradients are computed as calc_grad_sigma2_* / calc_grad_lc_*
+ * (:771-1604).  gpat_set_fluctuations takes the four arrays from host
+ * memory (NULL keeps a component; every component starts at 1, as the
+ * reference initialises them).  gpat_get_fluctuations returns the 16-float
+ * records {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx, d/dy, d/dz}. */
+int gpat_set_fluctuations(gpat_handle_t *h, int var_flag, const float *db2_slab,
+                          const float *db2_2d, const float *lc_slab, const float *lc_2d);
+int gpat_read_magnetic_fluctuation(gpat_handle_t *h, const char *filename, int var_flag);
+int gpat_read_correlation_length(gpat_handle_t *h, const char *filename, int var_flag);
+int gpat_get_fluctuations(gpat_handle_t *h, int var_flag, float *aux);
+
 int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag);
 /* copy_fields (mhd_data_parallel.f90:1920-1926): farray1 = farray2. */
 int gpat_copy_fields(gpat_handle_t *h);
@@ -181,13 +199,13 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
                                int dist_flag, double particle_v0, int ct_mhd,
                                double power_index);
 
-/* Quantities of inject_particles_at_large_jz / _absj / _divv / _rho
- * (particle_module.f90:785-1468).  db2 needs the magnetic-fluctuation
- * arrays of deltab_flag, which this engine does not hold. */
+/* Quantities of inject_particles_at_large_jz / _absj / _divv / _rho / _db2
+ * (particle_module.f90:785-1468). */
 #define GPAT_LARGE_JZ 0    /* |dBy/dx - dBx/dy|                        */
 #define GPAT_LARGE_ABSJ 1  /* |curl B|                                 */
 #define GPAT_LARGE_DIVV 2  /* -div v (compression)                     */
 #define GPAT_LARGE_RHO 3   /* rho                                      */
+#define GPAT_LARGE_DB2 4   /* db2_slab (needs deltab_flag and its arrays) */
 /* get_ncells_large_jz / _absj / _divv / _rho (mhd_data_parallel.f90:
  * 2211-2498): grid nodes of frame slot 0 strictly inside part_box whose
  * quantity is > qmin, evaluated in single precision from the stored

@@ -88,67 +88,66 @@ double orc_fixed_to_double(uint64_t hi, uint64_t lo)
 /* go to 8+3v, 8+3v+1, 8+3v+2.  Differences are single precision, scaled by */
 /* the double 0.5/dx and rounded back to single.                            */
 /* ------------------------------------------------------------------------ */
-#define FA(a, v, i, j, k) (a)[(size_t)(v) + 32u * ((size_t)(i) + (size_t)nxg * ((size_t)(j) + (size_t)nyg * (size_t)(k)))]
+#define GA(a, v, i, j, k) (a)[(size_t)(v) + (size_t)stride * ((size_t)(i) + (size_t)nxg * ((size_t)(j) + (size_t)nyg * (size_t)(k)))]
 
-void orc_calc_fields_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
-                               double dx, double dy, double dz)
+/* One gradient component of variable v along an axis with node spacing
+ * `step` (in records) at index `i` of `n`: central inside, one-sided 2nd
+ * order at the two outermost nodes; FP32 differences scaled by the FP64
+ * half inverse spacing, as the reference's real(sp) arrays. */
+static float grad_axis(const float *a, size_t c, size_t step, int i, int n, double ih)
+{
+    if (i == 0) {
+        float t = -(3.0f * a[c]);
+        t = t + 4.0f * a[c + step];
+        t = t - a[c + 2 * step];
+        return (float)((double)t * ih);
+    }
+    if (i == n - 1) {
+        float t = 3.0f * a[c];
+        t = t - 4.0f * a[c - step];
+        t = t + a[c - 2 * step];
+        return (float)((double)t * ih);
+    }
+    const float t = a[c + step] - a[c - step];
+    return (float)((double)t * ih);
+}
+
+/* Gradients of nvar variables (value at v * vstride of each record of
+ * `stride` floats) into gbase + v * gstep + axis; the z component only in
+ * 3D (in 2D it keeps whatever it held). */
+static void grad_generic(float *a, int stride, int nvar, int vstride, int gbase, int gstep,
+                         int ndim, int nxg, int nyg, int nzg, double dx, double dy, double dz)
 {
     const double idxh = 0.5 / dx, idyh = 0.5 / dy, idzh = 0.5 / dz;
+    const size_t sx = (size_t)stride, sy = sx * (size_t)nxg, sz = sy * (size_t)nyg;
     for (int k = 0; k < nzg; ++k)
         for (int j = 0; j < nyg; ++j)
             for (int i = 0; i < nxg; ++i)
-                for (int v = 0; v < 8; ++v) {
-                    float d;
-                    if (i == 0) {
-                        float t = -(3.0f * FA(a, v, 0, j, k));
-                        t = t + 4.0f * FA(a, v, 1, j, k);
-                        t = t - FA(a, v, 2, j, k);
-                        d = (float)((double)t * idxh);
-                    } else if (i == nxg - 1) {
-                        float t = 3.0f * FA(a, v, nxg - 1, j, k);
-                        t = t - 4.0f * FA(a, v, nxg - 2, j, k);
-                        t = t + FA(a, v, nxg - 3, j, k);
-                        d = (float)((double)t * idxh);
-                    } else {
-                        float t = FA(a, v, i + 1, j, k) - FA(a, v, i - 1, j, k);
-                        d = (float)((double)t * idxh);
-                    }
-                    FA(a, 8 + 3 * v, i, j, k) = d;
-                    if (nyg > 1) {
-                        if (j == 0) {
-                            float t = -(3.0f * FA(a, v, i, 0, k));
-                            t = t + 4.0f * FA(a, v, i, 1, k);
-                            t = t - FA(a, v, i, 2, k);
-                            d = (float)((double)t * idyh);
-                        } else if (j == nyg - 1) {
-                            float t = 3.0f * FA(a, v, i, nyg - 1, k);
-                            t = t - 4.0f * FA(a, v, i, nyg - 2, k);
-                            t = t + FA(a, v, i, nyg - 3, k);
-                            d = (float)((double)t * idyh);
-                        } else {
-                            float t = FA(a, v, i, j + 1, k) - FA(a, v, i, j - 1, k);
-                            d = (float)((double)t * idyh);
-                        }
-                        FA(a, 8 + 3 * v + 1, i, j, k) = d;
-                    }
-                    if (nzg > 1 && ndim == 3) {
-                        if (k == 0) {
-                            float t = -(3.0f * FA(a, v, i, j, 0));
-                            t = t + 4.0f * FA(a, v, i, j, 1);
-                            t = t - FA(a, v, i, j, 2);
-                            d = (float)((double)t * idzh);
-                        } else if (k == nzg - 1) {
-                            float t = 3.0f * FA(a, v, i, j, nzg - 1);
-                            t = t - 4.0f * FA(a, v, i, j, nzg - 2);
-                            t = t + FA(a, v, i, j, nzg - 3);
-                            d = (float)((double)t * idzh);
-                        } else {
-                            float t = FA(a, v, i, j, k + 1) - FA(a, v, i, j, k - 1);
-                            d = (float)((double)t * idzh);
-                        }
-                        FA(a, 8 + 3 * v + 2, i, j, k) = d;
-                    }
+                for (int v = 0; v < nvar; ++v) {
+                    const size_t c = (size_t)v * vstride + sx * (size_t)i + sy * (size_t)j +
+                                     sz * (size_t)k;
+                    GA(a, gbase + v * gstep, i, j, k) = grad_axis(a, c, sx, i, nxg, idxh);
+                    if (nyg > 1) GA(a, gbase + v * gstep + 1, i, j, k) = grad_axis(a, c, sy, j, nyg, idyh);
+                    if (nzg > 1 && ndim == 3)
+                        GA(a, gbase + v * gstep + 2, i, j, k) = grad_axis(a, c, sz, k, nzg, idzh);
                 }
+}
+
+/* calc_fields_gradients (mhd_data_parallel.f90:504-610): 8 variables of
+ * the 32-float records, gradients at 8 + 3 v + axis. */
+void orc_calc_fields_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
+                               double dx, double dy, double dz)
+{
+    grad_generic(a, 32, 8, 1, 8, 3, ndim, nxg, nyg, nzg, dx, dy, dz);
+}
+
+/* calc_grad_sigma2_slab / _2d and calc_grad_lc_slab / _2d
+ * (mhd_data_parallel.f90:771-1604) on the 16-float fluctuation records
+ * {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx, d/dy, d/dz}. */
+void orc_calc_aux_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
+                            double dx, double dy, double dz)
+{
+    grad_generic(a, 16, 4, 4, 1, 4, ndim, nxg, nyg, nzg, dx, dy, dz);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -209,6 +208,30 @@ void orc_interp_fields(const float *f1, const float *f2, int time_interp, int nd
         for (int v = 0; v < 32; ++v) fields[v] = fields[v] * (1.0 - rt) + fields2[v] * rt;
 }
 
+/* interp_magnetic_fluctuation / interp_correlation_length
+ * (mhd_data_parallel.f90:1806-1915): the 16-float fluctuation records with
+ * the same weights and time interpolation as the fields. */
+void orc_interp_aux(const float *a1, const float *a2, int time_interp, int ndim, int nxg,
+                    int nyg, const int32_t pos[3], const double w[8], double rt, double out[16])
+{
+    const int ix = pos[0] + 1, iy = pos[1] + 1;
+    const int iz = (ndim == 3) ? pos[2] + 1 : 0;
+    const int ze = (ndim == 3) ? 1 : 0;
+    double o2[16];
+    for (int v = 0; v < 16; ++v) { out[v] = 0.0; o2[v] = 0.0; }
+    for (int k = 0; k <= ze; ++k)
+        for (int j = 0; j <= 1; ++j)
+            for (int i = 0; i <= 1; ++i) {
+                const int idx = k * 4 + j * 2 + i;
+                const size_t c = 16u * ((size_t)(ix + i) + (size_t)nxg * ((size_t)(iy + j) + (size_t)nyg * (size_t)(iz + k)));
+                for (int v = 0; v < 16; ++v) out[v] = out[v] + (double)a1[c + v] * w[idx];
+                if (time_interp)
+                    for (int v = 0; v < 16; ++v) o2[v] = o2[v] + (double)a2[c + v] * w[idx];
+            }
+    if (time_interp)
+        for (int v = 0; v < 16; ++v) out[v] = out[v] * (1.0 - rt) + o2[v] * rt;
+}
+
 /* ------------------------------------------------------------------------ */
 /* calc_spatial_diffusion_coefficients (particle_module.f90:2208-2450) and   */
 /* calc_spatial_diffusion_coefficients_nlgc (:2464-2771) without delta-B or */
@@ -229,8 +252,15 @@ enum { K_KNORM_PARA, K_KNORM_PERP, K_KPARA, K_KPERP, K_SKPARA, K_SKPERP, K_SKPAR
  * and T_i = kperp dkperp_i, A_i = kpara dkpara_i - kperp dkperp_i for NLGC
  * (:2583-2770); the operation order of each is the reference's. */
 void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, double mu,
-                                             const double f[32], double kap[22])
+                                             const double f[32], const double *aux,
+                                             double kap[22])
 {
+    /* aux: interpolated {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx,
+     * d/dy, d/dz} (interp_magnetic_fluctuation, interp_correlation_length);
+     * only read when deltab_flag / correlation_flag are on. */
+    const double *s2 = aux, *d2 = aux ? aux + 4 : NULL, *l1 = aux ? aux + 8 : NULL;
+    const double *l2 = aux ? aux + 12 : NULL;
+    const int dbf = pr->deltab_flag && aux, lcf = pr->correlation_flag && aux;
     const double bx = f[4], by = f[5], bz = f[6];
     const double b = sqrt(bx * bx + by * by + bz * bz);
     double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
@@ -242,6 +272,8 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
     if (!pr->nlgc) {
         double knorm;
         if (pr->mag_dependency == 1) knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
+        if (dbf) knorm_para = knorm_para / s2[0];
+        if (lcf) knorm_para = knorm_para * pow(l1[0], pr->gamma_turb - 1.0);
         if (pr->momentum_dependency == 1) knorm = knorm_para * pow(p / pr->p0, pr->pindex);
         else knorm = knorm_para;
         knorm_perp = knorm_para;
@@ -252,6 +284,15 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
         if (pr->mag_dependency == 1) {
             knorm_para = knorm_para * pow(b, pr->gamma_turb - 2.0);
             knorm_perp = knorm_perp * pow(b, (pr->gamma_turb - 2.0) / 3.0);
+        }
+        if (dbf) {
+            knorm_para = knorm_para / s2[0];
+            knorm_perp = knorm_perp * pow(s2[0], -1.0 / 3.0) * pow(d2[0], 2.0 / 3.0);
+        }
+        if (lcf) {
+            knorm_para = knorm_para * pow(l1[0], pr->gamma_turb - 1.0);
+            knorm_perp = knorm_perp * pow(l1[0], (pr->gamma_turb - 1.0) / 3.0) *
+                         pow(l2[0], 2.0 / 3.0);
         }
         if (pr->momentum_dependency == 1) {
             kn_para = knorm_para * pow(p / pr->p0, pr->pindex);
@@ -285,6 +326,8 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
             if (pr->mag_dependency == 1)
                 /* the fixed-ratio 3D branch has no 1/B factor (:2406-2408) */
                 dk = d3 ? db[k] * g2 : db[k] * ib1 * g2;
+            if (dbf) dk = dk - s2[1 + k] / s2[0];
+            if (lcf) dk = dk + (pr->gamma_turb - 1.0) * l1[1 + k] / l1[0];
             T[k] = kperp * dk;
             A[k] = kpp * dk;
         } else {
@@ -292,6 +335,15 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
             if (pr->mag_dependency == 1) {
                 dkpara = db[k] * ib1 * g2;
                 dkperp = db[k] * ib1 * g2 / 3.0;
+            }
+            if (dbf) {
+                dkpara = dkpara - s2[1 + k] / s2[0];
+                dkperp = dkperp - s2[1 + k] / s2[0] / 3.0 + 2.0 * d2[1 + k] / d2[0] / 3.0;
+            }
+            if (lcf) {
+                dkpara = dkpara + (pr->gamma_turb - 1.0) * l1[1 + k] / l1[0];
+                dkperp = dkperp + (pr->gamma_turb - 1.0) * l1[1 + k] / l1[0] / 3.0 +
+                         2.0 * l2[1 + k] / l2[0] / 3.0;
             }
             T[k] = kperp * dkperp;
             A[k] = kpara * dkpara - kperp * dkperp;
@@ -333,6 +385,7 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
 typedef struct mover_ctx {
     const orc_params *pr;
     const float *f1, *f2;
+    const float *aux1, *aux2;      /* 16-float fluctuation records, or NULL */
     int time_interp, ndim, nxg, nyg;
     double dx, dy, dz;
     double xmin, ymin, zmin;                   /* fconfig box (exact)      */
@@ -602,9 +655,9 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
 /* ------------------------------------------------------------------------ */
 /* calc_duu: particle_module.f90:3116-3155 without delta-B or correlation   */
 /* length.                                                                   */
-static void calc_duu(const orc_params *pr, const ptl_state *s, double b, double div_bnorm,
-                     double divv, double bb_gradv, double bv_gradv, double mu2,
-                     double *dmu_dt, double *duu, double *duu_du)
+static void calc_duu(const orc_params *pr, const ptl_state *s, double b, const double *aux,
+                     double div_bnorm, double divv, double bb_gradv, double bv_gradv,
+                     double mu2, double *dmu_dt, double *duu, double *duu_du)
 {
     double dm = s->v * div_bnorm + s->mu * divv - 3.0 * s->mu * bb_gradv - 2.0 * bv_gradv / s->v;
     dm = dm * (1.0 - mu2) * 0.5;
@@ -620,6 +673,8 @@ static void calc_duu(const orc_params *pr, const ptl_state *s, double b, double 
         ud = 0.0;
     double norm = 1.0;
     if (pr->mag_dependency == 1) norm = norm * pow(b, 2.0 - pr->gamma_turb);
+    if (pr->deltab_flag && aux) norm = norm * aux[0];
+    if (pr->correlation_flag && aux) norm = norm * pow(aux[8], 1.0 - pr->gamma_turb);
     if (pr->momentum_dependency == 1) norm = norm * pow(s->p / pr->p0, pr->gamma_turb - 1.0);
     ud = ud * norm;
     u = u * norm;
@@ -714,8 +769,8 @@ static void ft_time_step(const mover_ctx *c, ptl_state *s, const double *kap, in
 }
 
 /* push_particle_2d_ft, Cartesian uniform grid: particle_module.f90:3626-3964. */
-static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                       int fixed_dt, double d[6])
+static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *aux,
+                       const double *kap, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
@@ -761,7 +816,7 @@ static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double div_bnorm = -((bx * db_dx + by * db_dy) * ib2);
     double dmu_dt, duu, duu_du;
-    calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
+    calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
     if (!fixed_dt) ft_time_step(c, s, kap, 2, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s->dt);
     double r[4];
@@ -777,8 +832,8 @@ static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
 }
 
 /* push_particle_3d_ft, Cartesian uniform grid: particle_module.f90:4930-5324. */
-static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                       int fixed_dt, double d[6])
+static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *aux,
+                       const double *kap, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
@@ -829,7 +884,7 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double div_bnorm = -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
     double dmu_dt, duu, duu_du;
-    calc_duu(pr, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
+    calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
     if (!fixed_dt) ft_time_step(c, s, kap, 3, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s->dt);
     double r[4];
@@ -896,13 +951,18 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
     const double pz = (s->z - c->zmin) / c->dz;
     const double rt = (s->t - c->t0) / c->dtf;
     int32_t pos[3];
-    double w[8], f[32], kap[22];
+    double w[8], f[32], kap[22], aux[16];
+    const double *ap = NULL;
     orc_get_interp_paramters(c->ndim, px, py, pz, pos, w);
     orc_interp_fields(c->f1, c->f2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, f);
-    orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, kap);
+    if (c->aux1 && (c->pr->deltab_flag || c->pr->correlation_flag)) {
+        orc_interp_aux(c->aux1, c->aux2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, aux);
+        ap = aux;
+    }
+    orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, ap, kap);
     if (c->pr->focused_transport) {
-        if (c->ndim == 2) push_2d_ft(c, s, f, kap, fixed_dt, d);
-        else push_3d_ft(c, s, f, kap, fixed_dt, d);
+        if (c->ndim == 2) push_2d_ft(c, s, f, ap, kap, fixed_dt, d);
+        else push_3d_ft(c, s, f, ap, kap, fixed_dt, d);
     } else {
         if (c->ndim == 2) push_2d(c, s, f, kap, fixed_dt, d);
         else push_3d(c, s, f, kap, fixed_dt, d);
@@ -1087,13 +1147,16 @@ static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *
  * mover cycle, remove_particles, then the boundary pass on the exact box
  * and a second remove_particles.  Returns the new particle count. */
 int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,
-                           const float *f1, const float *f2, int time_interp,
+                           const float *f1, const float *f2, const float *aux1,
+                           const float *aux2, int time_interp,
                            orc_particles *P, int64_t n, double t0, double dtf,
                            int nsteps_interval, int num_fine_steps, int nthreads,
                            orc_counters *cnt)
 {
     mover_ctx c;
     setup_ctx(&c, pr, cfg, f1, f2, time_interp, t0, dtf);
+    c.aux1 = aux1;
+    c.aux2 = aux2 ? aux2 : aux1;
     for (int64_t i = 0; i < n; ++i) P->nsteps_tracked[i] = 1;
     uint64_t lh = 0, ll = 0, nh = 0, nl = 0, steps = 0;
 #ifdef _OPENMP
@@ -1328,7 +1391,7 @@ static double large_quantity(int quantity, int ndim, const double f[32])
 }
 
 int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
-                              int quantity, double qmin, const double box[6])
+                              const float *aux, int quantity, double qmin, const double box[6])
 {
     const int ndim = pr->ndim;
     const int nx = cfg->nx, ny = cfg->ny, nz = (ndim == 3) ? cfg->nz : 1;
@@ -1361,6 +1424,8 @@ int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, c
                     d = d + (double)u[12];
                     if (ndim > 2) d = d + (double)u[16];
                     q = -d;
+                } else if (quantity == 4) {
+                    q = (double)aux[16 * ((size_t)ix + 1 + nxg * ((size_t)iy + 1 + nyg * cz))];
                 } else {
                     q = (double)r[3];
                 }
@@ -1372,7 +1437,8 @@ int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, c
 }
 
 int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
-                            orc_particles *P, int64_t n, int64_t nptl_max, int64_t nptl,
+                            const float *aux, orc_particles *P, int64_t n, int64_t nptl_max,
+                            int64_t nptl,
                             double dt, int dist_flag, double particle_v0, double t_frame,
                             double dt_mhd, int quantity, double qmin, const double box[6],
                             double power_index, orc_counters *cnt)
@@ -1401,8 +1467,14 @@ int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, con
                 double w[8], f[32];
                 orc_get_interp_paramters(ndim, (x - cfg->xmin) / cfg->dx, (y - cfg->ymin) / cfg->dy,
                                          (z - cfg->zmin) / cfg->dz, pos, w);
-                orc_interp_fields(full, full, 0, ndim, nxg, nyg, pos, w, 0.0, f);
-                q = large_quantity(quantity, ndim, f);
+                if (quantity == 4) {
+                    double a16[16];
+                    orc_interp_aux(aux, aux, 0, ndim, nxg, nyg, pos, w, 0.0, a16);
+                    q = a16[0];
+                } else {
+                    orc_interp_fields(full, full, 0, ndim, nxg, nyg, pos, w, 0.0, f);
+                    q = large_quantity(quantity, ndim, f);
+                }
             } else {
                 q = rho ? 0.0 : -3.0;
             }

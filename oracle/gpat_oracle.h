@@ -57,6 +57,7 @@ typedef struct orc_params {
     double kperp_kpara;         /* particle_mover's kperp_kpara                */
     int32_t dpp_shear, weak_scattering;
     double tau0;
+    int32_t deltab_flag, correlation_flag;   /* set_flags_params (:285-300) */
 } orc_params;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the
@@ -95,10 +96,18 @@ void orc_interp_fields(const float *f1, const float *f2, int time_interp, int nd
                        int nxg, int nyg, const int32_t pos[3], const double weights[8],
                        double rt, double fields[32]);
 void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, double mu,
-                                             const double fields[32], double kappa[22]);
+                                             const double fields[32], const double *aux,
+                                             double kappa[22]);
+void orc_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg,
+                            double dx, double dy, double dz);
+void orc_interp_aux(const float *a1, const float *a2, int time_interp, int ndim, int nxg,
+                    int nyg, const int32_t pos[3], const double w[8], double rt, double out[16]);
 
+/* aux1 / aux2: 16-float fluctuation records of the two frames, or NULL
+ * (read when deltab_flag / correlation_flag are on). */
 int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,
-                           const float *f1, const float *f2, int time_interp,
+                           const float *f1, const float *f2, const float *aux1,
+                           const float *aux2, int time_interp,
                            orc_particles *ptl, int64_t n, double t0, double dtf,
                            int nsteps_interval, int num_fine_steps, int nthreads,
                            orc_counters *cnt);
@@ -116,11 +125,14 @@ int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *ptl, int
                                    double dt_mhd, const double part_box[6],
                                    double power_index, orc_counters *cnt);
 /* get_ncells_large_* and inject_particles_at_large_* (quantity 0 jz,
- * 1 absj, 2 divv, 3 rho); full is frame 1 with gradients. */
+ * 1 absj, 2 divv, 3 rho, 4 db2); full is frame 1 with gradients, aux its
+ * fluctuation records (quantity 4 only). */
 int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
-                              int quantity, double qmin, const double part_box[6]);
+                              const float *aux, int quantity, double qmin,
+                              const double part_box[6]);
 int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
-                            orc_particles *ptl, int64_t n, int64_t nptl_max, int64_t nptl,
+                            const float *aux, orc_particles *ptl, int64_t n, int64_t nptl_max,
+                            int64_t nptl,
                             double dt, int dist_flag, double particle_v0, double t_frame,
                             double dt_mhd, int quantity, double qmin,
                             const double part_box[6], double power_index, orc_counters *cnt);

@@ -39,7 +39,7 @@ class OrcParams(C.Structure):
         ("seed", u64),
         ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("dpp_wave", i32),
         ("duu0", d), ("kperp_kpara", d), ("dpp_shear", i32), ("weak_scattering", i32),
-        ("tau0", d),
+        ("tau0", d), ("deltab_flag", i32), ("correlation_flag", i32),
     ]
 
 # Mover arguments of the reference carried in OrcParams rather than in the
@@ -101,11 +101,15 @@ def load() -> C.CDLL:
         lib.orc_get_interp_paramters.argtypes = [C.c_int, d, d, d, P(i32), P(d)]
         lib.orc_interp_fields.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_int,
                                           C.c_int, P(i32), P(d), d, P(d)]
-        lib.orc_calc_spatial_diffusion_coefficients.argtypes = [P(OrcParams), d, d, P(d), P(d)]
+        lib.orc_calc_spatial_diffusion_coefficients.argtypes = [P(OrcParams), d, d, P(d), P(d),
+                                                                P(d)]
+        lib.orc_calc_aux_gradients.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int,
+                                               d, d, d]
         lib.orc_particle_mover.restype = i64
         lib.orc_particle_mover.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
-                                           P(C.c_float), C.c_int, P(OrcParticles), i64, d, d,
-                                           C.c_int, C.c_int, C.c_int, P(OrcCounters)]
+                                           P(C.c_float), P(C.c_float), P(C.c_float), C.c_int,
+                                           P(OrcParticles), i64, d, d, C.c_int, C.c_int, C.c_int,
+                                           P(OrcCounters)]
         lib.orc_remove_particles.restype = i64
         lib.orc_remove_particles.argtypes = [P(OrcParticles), i64, P(OrcCounters)]
         lib.orc_split_particle.restype = i64
@@ -122,11 +126,12 @@ def load() -> C.CDLL:
                                         i64, d, d, C.c_int, d, d, d, P(OrcCounters)]
         lib.orc_count_cells_large.restype = i64
         lib.orc_count_cells_large.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
-                                              C.c_int, d, P(d)]
+                                              P(C.c_float), C.c_int, d, P(d)]
         lib.orc_inject_at_large.restype = i64
         lib.orc_inject_at_large.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
-                                            P(OrcParticles), i64, i64, i64, d, C.c_int, d, d, d,
-                                            C.c_int, d, P(d), d, P(OrcCounters)]
+                                            P(C.c_float), P(OrcParticles), i64, i64, i64, d,
+                                            C.c_int, d, d, d, C.c_int, d, P(d), d,
+                                            P(OrcCounters)]
         lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
         lib.orc_set_escaped_histogram.argtypes = [C.c_int, d, d, P(u64), P(u64), P(u64)]
         lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, d, d, C.c_int,
@@ -191,6 +196,21 @@ def full_fields(frame8: np.ndarray, ndim: int, cfg) -> np.ndarray:
     return full
 
 
+def aux_fields(db2_slab, db2_2d, lc_slab, lc_2d, ndim: int, cfg) -> np.ndarray:
+    """16-float fluctuation records {db2_slab, db2_2d, lc_slab, lc_2d} x
+    {value, d/dx, d/dy, d/dz} from four (nzg, nyg, nxg) arrays (None: the
+    reference's initial value 1), gradients as the reference computes them."""
+    shape = np.shape(db2_slab if db2_slab is not None else lc_slab)
+    aux = np.ones(shape + (16,), dtype=np.float32)
+    for g, a in enumerate((db2_slab, db2_2d, lc_slab, lc_2d)):
+        if a is not None:
+            aux[..., 4 * g] = a
+    nzg, nyg, nxg = shape
+    load().orc_calc_aux_gradients(aux.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
+                                  cfg.dx, cfg.dy, cfg.dz)
+    return aux
+
+
 def philox(ctr, key):
     lib = load()
     c = (u32 * 4)(*ctr)
@@ -204,7 +224,8 @@ def mover(params: OrcParams, cfg: OrcMhdConfig, f1: np.ndarray, parts: Particles
           dtf: float, nsteps_interval: int = 10, num_fine_steps: int = 1, nthreads: int = 0,
           counters: OrcCounters | None = None, f2: np.ndarray | None = None,
           focused_transport: bool = False, nlgc: bool = False,
-          kperp_kpara: float = 0.01) -> OrcCounters:
+          kperp_kpara: float = 0.01, aux1: np.ndarray | None = None,
+          aux2: np.ndarray | None = None) -> OrcCounters:
     """particle_mover(focused_transport, nlgc, kperp_kpara, ...) on one rank."""
     lib = load()
     params = OrcParams.from_buffer_copy(params)
@@ -214,7 +235,9 @@ def mover(params: OrcParams, cfg: OrcMhdConfig, f1: np.ndarray, parts: Particles
     cnt = counters if counters is not None else OrcCounters()
     fp1 = f1.ctypes.data_as(P(C.c_float))
     fp2 = (f2 if f2 is not None else f1).ctypes.data_as(P(C.c_float))
-    parts.n = lib.orc_particle_mover(C.byref(params), C.byref(cfg), fp1, fp2,
+    a1 = aux1.ctypes.data_as(P(C.c_float)) if aux1 is not None else None
+    a2 = aux2.ctypes.data_as(P(C.c_float)) if aux2 is not None else a1
+    parts.n = lib.orc_particle_mover(C.byref(params), C.byref(cfg), fp1, fp2, a1, a2,
                                      1 if f2 is not None else 0, C.byref(parts.c), parts.n, t0,
                                      dtf, nsteps_interval, num_fine_steps, nthreads, C.byref(cnt))
     return cnt
@@ -260,21 +283,23 @@ def inject_spatial_uniform(params: OrcParams, parts: Particles, nptl: int, dt: f
 
 
 def count_cells_large(params: OrcParams, cfg: OrcMhdConfig, full: np.ndarray, quantity: int,
-                      qmin: float, box) -> int:
-    """get_ncells_large_* (quantity 0 jz, 1 absj, 2 divv, 3 rho)."""
+                      qmin: float, box, aux: np.ndarray | None = None) -> int:
+    """get_ncells_large_* (quantity 0 jz, 1 absj, 2 divv, 3 rho, 4 db2)."""
+    ap = aux.ctypes.data_as(P(C.c_float)) if aux is not None else None
     return load().orc_count_cells_large(C.byref(params), C.byref(cfg),
-                                        full.ctypes.data_as(P(C.c_float)), quantity, qmin,
+                                        full.ctypes.data_as(P(C.c_float)), ap, quantity, qmin,
                                         (d * 6)(*box))
 
 
 def inject_at_large(params: OrcParams, cfg: OrcMhdConfig, full: np.ndarray, parts: Particles,
                     nptl: int, dt: float, dist_flag: int, particle_v0: float, t_frame: float,
                     dt_mhd: float, quantity: int, qmin: float, box, counters: OrcCounters,
-                    power_index: float = 7.0):
+                    power_index: float = 7.0, aux: np.ndarray | None = None):
     """inject_particles_at_large_* for nptl particles (nptl_inject given)."""
     lib = load()
+    ap = aux.ctypes.data_as(P(C.c_float)) if aux is not None else None
     parts.n = lib.orc_inject_at_large(C.byref(params), C.byref(cfg),
-                                      full.ctypes.data_as(P(C.c_float)), C.byref(parts.c),
+                                      full.ctypes.data_as(P(C.c_float)), ap, C.byref(parts.c),
                                       parts.n, parts.cap, nptl, dt, dist_flag, particle_v0,
                                       t_frame, dt_mhd, quantity, qmin, (d * 6)(*box),
                                       power_index, C.byref(counters))

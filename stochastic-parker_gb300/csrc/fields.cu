@@ -48,34 +48,40 @@ __device__ __forceinline__ float grad_c(float ap, float am, double ih) {
     return (float)__dmul_rn((double)__fsub_rn(ap, am), ih);
 }
 
+// Gradients of NVAR variables of records of STRIDE floats (value of v at
+// v * VSTRIDE, its d/dx d/dy d/dz at GBASE + v * GSTEP + axis); the z
+// component only in 3D.  <32, 8, 1, 8, 3>: the field records; <16, 4, 4, 1, 4>:
+// the fluctuation records {db2_slab, db2_2d, lc_slab, lc_2d}.
+template <int STRIDE, int NVAR, int VSTRIDE, int GBASE, int GSTEP>
 __global__ void gradients_kernel(float *__restrict__ a, int ndim, int nxg, int nyg, int nzg,
                                  double idxh, double idyh, double idzh) {
     const size_t ncells = (size_t)nxg * nyg * nzg;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    const size_t sx = 32, sy = 32 * (size_t)nxg, sz = 32 * (size_t)nxg * nyg;
+    const size_t sx = STRIDE, sy = STRIDE * (size_t)nxg, sz = STRIDE * (size_t)nxg * nyg;
     for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride) {
         const int i = (int)(c % nxg);
         const int j = (int)((c / nxg) % nyg);
         const int k = (int)(c / ((size_t)nxg * nyg));
-        float *cell = a + 32 * c;
+        float *cell = a + STRIDE * c;
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
+        for (int v = 0; v < NVAR; ++v) {
+            const int x = v * VSTRIDE, g = GBASE + v * GSTEP;
             float d;
-            if (i == 0) d = grad_lo(cell[v], cell[v + sx], cell[v + 2 * sx], idxh);
-            else if (i == nxg - 1) d = grad_hi(cell[v], cell[v - sx], cell[v - 2 * sx], idxh);
-            else d = grad_c(cell[v + sx], cell[v - sx], idxh);
-            cell[8 + 3 * v] = d;
+            if (i == 0) d = grad_lo(cell[x], cell[x + sx], cell[x + 2 * sx], idxh);
+            else if (i == nxg - 1) d = grad_hi(cell[x], cell[x - sx], cell[x - 2 * sx], idxh);
+            else d = grad_c(cell[x + sx], cell[x - sx], idxh);
+            cell[g] = d;
             if (nyg > 1) {
-                if (j == 0) d = grad_lo(cell[v], cell[v + sy], cell[v + 2 * sy], idyh);
-                else if (j == nyg - 1) d = grad_hi(cell[v], cell[v - sy], cell[v - 2 * sy], idyh);
-                else d = grad_c(cell[v + sy], cell[v - sy], idyh);
-                cell[8 + 3 * v + 1] = d;
+                if (j == 0) d = grad_lo(cell[x], cell[x + sy], cell[x + 2 * sy], idyh);
+                else if (j == nyg - 1) d = grad_hi(cell[x], cell[x - sy], cell[x - 2 * sy], idyh);
+                else d = grad_c(cell[x + sy], cell[x - sy], idyh);
+                cell[g + 1] = d;
             }
             if (nzg > 1 && ndim == 3) {
-                if (k == 0) d = grad_lo(cell[v], cell[v + sz], cell[v + 2 * sz], idzh);
-                else if (k == nzg - 1) d = grad_hi(cell[v], cell[v - sz], cell[v - 2 * sz], idzh);
-                else d = grad_c(cell[v + sz], cell[v - sz], idzh);
-                cell[8 + 3 * v + 2] = d;
+                if (k == 0) d = grad_lo(cell[x], cell[x + sz], cell[x + 2 * sz], idzh);
+                else if (k == nzg - 1) d = grad_hi(cell[x], cell[x - sz], cell[x - 2 * sz], idzh);
+                else d = grad_c(cell[x + sz], cell[x - sz], idzh);
+                cell[g + 2] = d;
             }
         }
     }
@@ -87,8 +93,51 @@ cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg
     const int threads = 256;
     size_t blocks = (ncells + threads - 1) / threads;
     if (blocks > 65535 * 16) blocks = 65535 * 16;
-    gradients_kernel<<<(unsigned)blocks, threads, 0, s>>>(full, ndim, nxg, nyg, nzg, 0.5 / dx,
-                                                          0.5 / dy, 0.5 / dz);
+    gradients_kernel<32, 8, 1, 8, 3><<<(unsigned)blocks, threads, 0, s>>>(
+        full, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg, double dx,
+                                      double dy, double dz, cudaStream_t s) {
+    const size_t ncells = (size_t)nxg * nyg * nzg;
+    const int threads = 256;
+    size_t blocks = (ncells + threads - 1) / threads;
+    if (blocks > 65535 * 16) blocks = 65535 * 16;
+    gradients_kernel<16, 4, 4, 1, 4><<<(unsigned)blocks, threads, 0, s>>>(
+        aux, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz);
+    return cudaGetLastError();
+}
+
+// One scalar field (nzg, nyg, nxg) into component `comp` of the 16-float
+// fluctuation records.
+__global__ void scatter_aux_kernel(const float *__restrict__ src, float *__restrict__ aux,
+                                   int comp, size_t ncells) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride)
+        aux[16 * c + comp] = src[c];
+}
+
+__global__ void fill_kernel(float *__restrict__ a, float v, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += stride) a[c] = v;
+}
+
+cudaError_t launch_scatter_aux(const float *src, float *aux, int comp, size_t ncells,
+                               cudaStream_t s) {
+    const int threads = 256;
+    size_t blocks = (ncells + threads - 1) / threads;
+    if (blocks > 65535 * 16) blocks = 65535 * 16;
+    scatter_aux_kernel<<<(unsigned)blocks, threads, 0, s>>>(src, aux, comp, ncells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill(float *a, float v, size_t n, cudaStream_t s) {
+    const int threads = 256;
+    size_t blocks = (n + threads - 1) / threads;
+    if (blocks > 65535 * 16) blocks = 65535 * 16;
+    if (blocks == 0) return cudaSuccess;
+    fill_kernel<<<(unsigned)blocks, threads, 0, s>>>(a, v, n);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@ struct gpat_handle {
     float *full[2] = {nullptr, nullptr};
     float *rec[2] = {nullptr, nullptr};
     float *staging = nullptr;
+    float *aux[2] = {nullptr, nullptr};   // fluctuation records (deltab / correlation runs)
     bool fields_set[2] = {false, false};
     bool rec_ready[2] = {false, false};
     // particles (double-buffered SoA)
@@ -181,6 +182,10 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.rec2 = p.time_interp ? h->rec[1] : h->rec[0];
     a.full1 = h->full[0];
     a.full2 = p.time_interp ? h->full[1] : h->full[0];
+    a.deltab_flag = p.deltab_flag;
+    a.correlation_flag = p.correlation_flag;
+    a.aux1 = h->aux[0];
+    a.aux2 = p.time_interp ? h->aux[1] : h->aux[0];
     a.duu0 = p.duu0;
     a.dpp_wave = p.dpp_wave;
     a.dpp_shear = p.dpp_shear;
@@ -352,10 +357,10 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     *out = nullptr;
     const gpat_params_t &p = *params;
     if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
-    if (p.deltab_flag || p.correlation_flag || p.include_3rd_dim || p.spherical_coord ||
-        p.nonuniform_grid)
+    if (p.include_3rd_dim || p.spherical_coord || p.nonuniform_grid) return GPAT_ERR_UNSUPPORTED;
+    if ((p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag) &&
+        p.precision != GPAT_PREC_FP64)
         return GPAT_ERR_UNSUPPORTED;
-    if ((p.dpp_wave || p.dpp_shear) && p.precision != GPAT_PREC_FP64) return GPAT_ERR_UNSUPPORTED;
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
     if (p.noise != GPAT_NOISE_UNIFORM && p.noise != GPAT_NOISE_GAUSS) return GPAT_ERR_ARG;
     if (p.nptl_max < 1 || p.nptl_max > (int64_t)2000000000) return GPAT_ERR_ARG;
@@ -394,6 +399,14 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
             cudaMalloc(&h->rec[s], (size_t)R * sizeof(float) * h->ncells) != cudaSuccess)
             return bail(GPAT_ERR_OOM);
         cudaMemsetAsync(h->full[s], 0, 32 * sizeof(float) * h->ncells, h->stream);
+        // init_magnetic_fluctuation / init_correlation_length
+        // (mhd_data_parallel.f90:107-182): every component starts at 1
+        if (p.deltab_flag || p.correlation_flag) {
+            if (cudaMalloc(&h->aux[s], 16 * sizeof(float) * h->ncells) != cudaSuccess)
+                return bail(GPAT_ERR_OOM);
+            if (launch_fill(h->aux[s], 1.0f, 16 * h->ncells, h->stream) != cudaSuccess)
+                return bail(GPAT_ERR_CUDA);
+        }
     }
     // init_particles (particle_module.f90:177-258), double-buffered.
     h->cap = p.nptl_max;
@@ -425,6 +438,7 @@ int gpat_destroy(gpat_handle_t *h) {
     for (int s = 0; s < 2; ++s) {
         if (h->full[s]) cudaFree(h->full[s]);
         if (h->rec[s]) cudaFree(h->rec[s]);
+        if (h->aux[s]) cudaFree(h->aux[s]);
         if (h->pmem[s]) cudaFree(h->pmem[s]);
     }
     if (h->staging) cudaFree(h->staging);
@@ -476,6 +490,74 @@ int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nva
     return GPAT_OK;
 }
 
+int gpat_set_fluctuations(gpat_handle_t *h, int var_flag, const float *db2_slab,
+                          const float *db2_2d, const float *lc_slab, const float *lc_2d) {
+    if (!h) return GPAT_ERR_ARG;
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots) return fail(h, GPAT_ERR_STATE, "slot 1 needs time_interp = 1");
+    if (!h->aux[slot])
+        return fail(h, GPAT_ERR_STATE, "fluctuation arrays need deltab_flag or correlation_flag");
+    CK(cudaSetDevice(h->device));
+    if (!h->staging) CK(cudaMalloc(&h->staging, 8 * sizeof(float) * h->ncells));
+    const float *src[4] = {db2_slab, db2_2d, lc_slab, lc_2d};
+    for (int g = 0; g < 4; ++g) {
+        if (!src[g]) continue;
+        CK(cudaMemcpyAsync(h->staging, src[g], sizeof(float) * h->ncells, cudaMemcpyHostToDevice,
+                           h->stream));
+        CK(launch_scatter_aux(h->staging, h->aux[slot], 4 * g, h->ncells, h->stream));
+        CK(cudaStreamSynchronize(h->stream));   // staging is reused
+    }
+    const gpat_mhd_config_t &c = h->cfg;
+    CK(launch_calc_aux_gradients(h->aux[slot], h->prm.ndim, h->nxg, h->nyg, h->nzg, c.dx, c.dy,
+                                 c.dz, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+namespace {
+// Two consecutive FP32 arrays of every (ghost-padded) node, as
+// read_magnetic_fluctuation / read_correlation_length read them
+// (mhd_data_parallel.f90:306-497).
+int read_pair(gpat_handle_t *h, const char *filename, std::vector<float> &a,
+              std::vector<float> &b) {
+    FILE *f = std::fopen(filename, "rb");
+    if (!f) return fail(h, GPAT_ERR_IO, std::string("cannot open ") + filename);
+    a.resize(h->ncells);
+    b.resize(h->ncells);
+    const size_t ga = std::fread(a.data(), sizeof(float), a.size(), f);
+    const size_t gb = std::fread(b.data(), sizeof(float), b.size(), f);
+    std::fclose(f);
+    if (ga != a.size() || gb != b.size())
+        return fail(h, GPAT_ERR_IO, std::string("short fluctuation file ") + filename);
+    return GPAT_OK;
+}
+}  // namespace
+
+int gpat_read_magnetic_fluctuation(gpat_handle_t *h, const char *filename, int var_flag) {
+    if (!h || !filename) return GPAT_ERR_ARG;
+    std::vector<float> a, b;
+    int rc = read_pair(h, filename, a, b);
+    if (rc) return rc;
+    return gpat_set_fluctuations(h, var_flag, a.data(), b.data(), nullptr, nullptr);
+}
+
+int gpat_read_correlation_length(gpat_handle_t *h, const char *filename, int var_flag) {
+    if (!h || !filename) return GPAT_ERR_ARG;
+    std::vector<float> a, b;
+    int rc = read_pair(h, filename, a, b);
+    if (rc) return rc;
+    return gpat_set_fluctuations(h, var_flag, nullptr, nullptr, a.data(), b.data());
+}
+
+int gpat_get_fluctuations(gpat_handle_t *h, int var_flag, float *aux) {
+    if (!h || !aux) return GPAT_ERR_ARG;
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots || !h->aux[slot]) return fail(h, GPAT_ERR_STATE, "no fluctuation arrays");
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpy(aux, h->aux[slot], 16 * sizeof(float) * h->ncells, cudaMemcpyDeviceToHost));
+    return GPAT_OK;
+}
+
 int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag) {
     if (!h || !filename) return GPAT_ERR_ARG;
     FILE *f = std::fopen(filename, "rb");
@@ -510,6 +592,9 @@ int gpat_copy_fields(gpat_handle_t *h) {
                        cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->rec[0], h->rec[1], (size_t)R * sizeof(float) * h->ncells,
                        cudaMemcpyDeviceToDevice, h->stream));
+    if (h->aux[0] && h->aux[1])   // copy_magnetic_fluctuation / copy_correlation_length
+        CK(cudaMemcpyAsync(h->aux[0], h->aux[1], 16 * sizeof(float) * h->ncells,
+                           cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->fields_set[0] = h->fields_set[1];
     h->rec_ready[0] = h->rec_ready[1];
@@ -539,6 +624,7 @@ static LargeArgs large_args(const gpat_handle_t *h, int quantity, double qmin) {
     g.dom[2] = c.zmin;
     g.dom[5] = (h->prm.ndim == 3) ? c.zmin + (double)c.nz * c.dz : c.zmax;
     g.full = h->full[0];
+    g.aux = h->aux[0];
     g.nx = c.nx; g.ny = c.ny; g.nz = (h->prm.ndim == 3) ? c.nz : 1;
     g.nxg = h->nxg; g.nyg = h->nyg;
     g.dx = c.dx; g.dy = c.dy; g.dz = c.dz;
@@ -611,8 +697,10 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
 int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin, const double part_box[6],
                            int64_t *ncells) {
     if (!h || !part_box || !ncells) return GPAT_ERR_ARG;
-    if (quantity < GPAT_LARGE_JZ || quantity > GPAT_LARGE_RHO)
-        return fail(h, GPAT_ERR_ARG, "quantity must be GPAT_LARGE_JZ, _ABSJ, _DIVV or _RHO");
+    if (quantity < GPAT_LARGE_JZ || quantity > GPAT_LARGE_DB2)
+        return fail(h, GPAT_ERR_ARG, "quantity must be one of GPAT_LARGE_*");
+    if (quantity == GPAT_LARGE_DB2 && !h->aux[0])
+        return fail(h, GPAT_ERR_STATE, "db2 injection needs deltab_flag and the fluctuation arrays");
     if (!h->rec_ready[0]) return fail(h, GPAT_ERR_STATE, "fields and their gradients are not set");
     CK(cudaSetDevice(h->device));
     const LargeArgs g = large_args(h, quantity, qmin);

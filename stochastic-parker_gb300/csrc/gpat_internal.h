@@ -79,6 +79,10 @@ struct MoverArgs {
     // 32-variable records too.
     int dpp_wave, dpp_shear, weak_scattering;
     double tau0;
+    // Spatially dependent turbulence (set_flags_params): fluctuation records
+    // of both frames, read by the FP64 mover when a flag is on.
+    int deltab_flag, correlation_flag;
+    const float *aux1, *aux2;
     const float *full1, *full2;
     DevCounters *cnt;
 };
@@ -151,6 +155,13 @@ cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg
                                          double dx, double dy, double dz, cudaStream_t s);
 cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
                                 cudaStream_t s);
+// Fluctuation records: 16 floats per node, {db2_slab, db2_2d, lc_slab,
+// lc_2d} x {value, d/dx, d/dy, d/dz}.
+cudaError_t launch_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg, double dx,
+                                      double dy, double dz, cudaStream_t s);
+cudaError_t launch_scatter_aux(const float *src, float *aux, int comp, size_t ncells,
+                               cudaStream_t s);
+cudaError_t launch_fill(float *a, float v, size_t n, cudaStream_t s);
 cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s);
 cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
                                cudaStream_t s);
@@ -182,6 +193,7 @@ struct LargeArgs {
     double qmin;
     double dom[6];         // sampling domain (the exact box): xmin ymin zmin xmax ymax zmax
     const float *full;     // frame 1, 32 variables per node (ghost layout)
+    const float *aux;      // frame 1 fluctuation records (GPAT_LARGE_DB2), or null
     int nx, ny, nz, nxg, nyg;
     double dx, dy, dz, gxmin, gymin, gzmin;
 };

@@ -38,7 +38,9 @@ struct Options {
     // inject_particles_at_large_* switches (stochastic-mhd.f90:735-806)
     bool inject_large_jz = false, inject_large_absj = false, inject_large_db2 = false;
     bool inject_large_divv = false, inject_large_rho = false, inject_same_nptl = false;
-    double jz_min = 100.0, absj_min = 5.0, divv_min = 10.0, rho_min = 5.0;
+    double jz_min = 100.0, absj_min = 5.0, divv_min = 10.0, rho_min = 5.0, db2_min = 0.03;
+    long long ncells_large_db2_norm = 800;
+    int deltab_flag = 0, correlation_flag = 0;   // -db, -co (stochastic-mhd.f90:859-866)
     long long ncells_large_jz_norm = 800, ncells_large_absj_norm = 800;
     long long ncells_large_divv_norm = 800, ncells_large_rho_norm = 800;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
@@ -87,7 +89,9 @@ int parse(int argc, char **argv, Options &o) {
         {"-ir", "--inject_large_rho"}, {"-sn", "--inject_same_nptl"}, {"-jz", "--jz_min"},
         {"-ajm", "--absj_min"}, {"-dv", "--divv_min"}, {"-rm", "--rho_min"},
         {"-nn", "--ncells_large_jz_norm"}, {"-naj", "--ncells_large_absj_norm"},
-        {"-nv", "--ncells_large_divv_norm"}, {"-nr", "--ncells_large_rho_norm"}};
+        {"-nv", "--ncells_large_divv_norm"}, {"-nr", "--ncells_large_rho_norm"},
+        {"-db2", "--db2_min"}, {"-nb", "--ncells_large_db2_norm"}, {"-db", "--deltab_flag"},
+        {"-co", "--correlation"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -153,6 +157,10 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--ncells_large_absj_norm") o.ncells_large_absj_norm = (long long)d;
         else if (k == "--ncells_large_divv_norm") o.ncells_large_divv_norm = (long long)d;
         else if (k == "--ncells_large_rho_norm") o.ncells_large_rho_norm = (long long)d;
+        else if (k == "--db2_min") o.db2_min = d;
+        else if (k == "--ncells_large_db2_norm") o.ncells_large_db2_norm = (long long)d;
+        else if (k == "--deltab_flag") o.deltab_flag = (int)d;
+        else if (k == "--correlation") o.correlation_flag = (int)d;
         else if (k == "--precision") {
             o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
             o.precision_set = true;
@@ -236,14 +244,14 @@ int main(int argc, char **argv) {
         return prc == 1 ? 0 : 2;
     }
     if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
-    if (o.inject_large_db2) {
-        std::fprintf(stderr, "gpat_run: -ib needs the magnetic-fluctuation arrays (deltab_flag), "
-                             "which this engine does not hold\n");
+    if (o.inject_large_db2 && o.deltab_flag != 1) {
+        std::fprintf(stderr, "gpat_run: -ib needs -db 1 (the magnetic-fluctuation arrays)\n");
         return 2;
     }
     // Focused transport and momentum diffusion run on the FP64 mover unless
     // asked otherwise.
-    if ((o.focused_transport || o.dpp_wave || o.dpp_shear) && !o.precision_set)
+    if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
+         o.correlation_flag) && !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
@@ -272,12 +280,27 @@ int main(int argc, char **argv) {
     p.dpp_shear = o.dpp_shear;
     p.weak_scattering = o.weak_scattering;
     p.tau0 = o.tau0_scattering;
+    p.deltab_flag = o.deltab_flag;
+    p.correlation_flag = o.correlation_flag;
     CHECK(gpat_create(&p, &cfg, o.device, &h));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
 
     // Frame tmin into farray1, gradients (:321, :350).
     const int tmin = o.t_start;
     CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tmin).c_str(), 0));
+    auto read_turbulence = [&](int tf, int var_flag) -> int {
+        char num[16];
+        std::snprintf(num, sizeof num, "%04d", tf);
+        if (o.deltab_flag == 1) {   // stochastic-mhd.f90:337-346, :417-424
+            int rc = gpat_read_magnetic_fluctuation(h, (o.dir_mhd_data + "deltab_" + num).c_str(),
+                                                    var_flag);
+            if (rc) return rc;
+        }
+        if (o.correlation_flag == 1)
+            return gpat_read_correlation_length(h, (o.dir_mhd_data + "lc_" + num).c_str(), var_flag);
+        return GPAT_OK;
+    };
+    CHECK(read_turbulence(tmin, 0));
     CHECK(gpat_calc_fields_gradients(h, 0));
     double part_box[6];
     if (o.inject_part_box) {
@@ -323,6 +346,7 @@ int main(int argc, char **argv) {
     for (int tf = tmin + 1; tf <= o.t_end; ++tf) {
         if (o.single_time_frame == 0 && tf <= o.tmax_mhd) {
             CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tf).c_str(), o.time_interp_flag));
+            CHECK(read_turbulence(tf, o.time_interp_flag));
             CHECK(gpat_calc_fields_gradients(h, o.time_interp_flag));
         }
         const int ct = tf - o.t_start;
@@ -336,6 +360,7 @@ int main(int argc, char **argv) {
             long long norm = 1;
             if (o.inject_large_jz) { quantity = GPAT_LARGE_JZ; qmin = o.jz_min; norm = o.ncells_large_jz_norm; }
             else if (o.inject_large_absj) { quantity = GPAT_LARGE_ABSJ; qmin = o.absj_min; norm = o.ncells_large_absj_norm; }
+            else if (o.inject_large_db2) { quantity = GPAT_LARGE_DB2; qmin = o.db2_min; norm = o.ncells_large_db2_norm; }
             else if (o.inject_large_divv) { quantity = GPAT_LARGE_DIVV; qmin = o.divv_min; norm = o.ncells_large_divv_norm; }
             else if (o.inject_large_rho) { quantity = GPAT_LARGE_RHO; qmin = o.rho_min; norm = o.ncells_large_rho_norm; }
             if (quantity >= 0) {

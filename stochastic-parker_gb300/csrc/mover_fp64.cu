@@ -238,8 +238,13 @@ struct Kap {
     double dkxx_dx, dkyy_dy, dkzz_dz, dkxy_dx, dkxy_dy, dkxz_dx, dkxz_dz, dkyz_dy, dkyz_dz;
 };
 
+// aux: interpolated {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx, d/dy,
+// d/dz}, or nullptr; read when deltab_flag / correlation_flag are on.
 template <int NDIM, bool FT>
-__device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, const Fld &f) {
+__device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, const Fld &f,
+                                     const double *aux) {
+    const bool dbf = a.deltab_flag && aux, lcf = a.correlation_flag && aux;
+    const double *s2 = aux, *d2 = aux + 4, *l1 = aux + 8, *l2 = aux + 12;
     const double bx = f.bx, by = f.by, bz = f.bz;
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
@@ -249,6 +254,8 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
     if (!a.nlgc) {
         double knorm;
         if (a.mag_dependency == 1) knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
+        if (dbf) knorm_para = knorm_para / s2[0];
+        if (lcf) knorm_para = knorm_para * pow(l1[0], a.gamma_turb - 1.0);
         if (a.momentum_dependency == 1) knorm = knorm_para * pow(p / a.p0, a.pindex);
         else knorm = knorm_para;
         kpara = a.kpara0 * knorm;
@@ -258,6 +265,15 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
         if (a.mag_dependency == 1) {
             knorm_para = knorm_para * pow(b, a.gamma_turb - 2.0);
             knorm_perp = knorm_perp * pow(b, (a.gamma_turb - 2.0) / 3.0);
+        }
+        if (dbf) {
+            knorm_para = knorm_para / s2[0];
+            knorm_perp = knorm_perp * pow(s2[0], -1.0 / 3.0) * pow(d2[0], 2.0 / 3.0);
+        }
+        if (lcf) {
+            knorm_para = knorm_para * pow(l1[0], a.gamma_turb - 1.0);
+            knorm_perp = knorm_perp * pow(l1[0], (a.gamma_turb - 1.0) / 3.0) *
+                         pow(l2[0], 2.0 / 3.0);
         }
         if (a.momentum_dependency == 1) {
             kn_para = knorm_para * pow(p / a.p0, a.pindex);
@@ -286,6 +302,8 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
             double dk = 0.0;
             // the fixed-ratio 3D branch has no 1/B factor (:2406-2408)
             if (a.mag_dependency == 1) dk = (NDIM == 3) ? db[d] * g2 : db[d] * ib1 * g2;
+            if (dbf) dk = dk - s2[1 + d] / s2[0];
+            if (lcf) dk = dk + (a.gamma_turb - 1.0) * l1[1 + d] / l1[0];
             T[d] = kperp * dk;
             A[d] = kpp * dk;
         } else {
@@ -293,6 +311,15 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
             if (a.mag_dependency == 1) {
                 dkpara = db[d] * ib1 * g2;
                 dkperp = db[d] * ib1 * g2 / 3.0;
+            }
+            if (dbf) {
+                dkpara = dkpara - s2[1 + d] / s2[0];
+                dkperp = dkperp - s2[1 + d] / s2[0] / 3.0 + 2.0 * d2[1 + d] / d2[0] / 3.0;
+            }
+            if (lcf) {
+                dkpara = dkpara + (a.gamma_turb - 1.0) * l1[1 + d] / l1[0];
+                dkperp = dkperp + (a.gamma_turb - 1.0) * l1[1 + d] / l1[0] / 3.0 +
+                         2.0 * l2[1 + d] / l2[0] / 3.0;
             }
             T[d] = kperp * dkperp;
             A[d] = kpara * dkpara - kperp * dkperp;
@@ -473,9 +500,9 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
 
 // calc_duu (:3116-3155) without delta-B or correlation length.
 __device__ __forceinline__ void calc_duu(const MoverArgs &a, const State &s, double b,
-                                         double div_bnorm, double divv, double bb_gradv,
-                                         double bv_gradv, double mu2, double &dmu_dt,
-                                         double &duu) {
+                                         const double *aux, double div_bnorm, double divv,
+                                         double bb_gradv, double bv_gradv, double mu2,
+                                         double &dmu_dt, double &duu) {
     double dm = s.v * div_bnorm + s.mu * divv - 3.0 * s.mu * bb_gradv - 2.0 * bv_gradv / s.v;
     dm = dm * (1.0 - mu2) * 0.5;
     const double h0 = (double)0.2f;
@@ -490,6 +517,8 @@ __device__ __forceinline__ void calc_duu(const MoverArgs &a, const State &s, dou
         ud = 0.0;
     double norm = 1.0;
     if (a.mag_dependency == 1) norm = norm * pow(b, 2.0 - a.gamma_turb);
+    if (a.deltab_flag && aux) norm = norm * aux[0];
+    if (a.correlation_flag && aux) norm = norm * pow(aux[8], 1.0 - a.gamma_turb);
     if (a.momentum_dependency == 1) norm = norm * pow(s.p / a.p0, a.gamma_turb - 1.0);
     ud = ud * norm;
     u = u * norm;
@@ -572,8 +601,9 @@ __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, doubl
 
 // push_particle_2d_ft (:3626-3964) and push_particle_3d_ft (:4930-5324).
 template <int NDIM>
-__device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
-                                        bool fixed_dt, Delta &d) {
+__device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld &f,
+                                        const double *aux, const Kap &k, bool fixed_dt,
+                                        Delta &d) {
     const double bx = f.bx, by = f.by, bz = f.bz;
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
@@ -640,7 +670,7 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
     double dp_dt = s.p * acc_rate;
     const double dpp = dpp_terms<NDIM>(a, s.p, f, k, b, divv, dp_dt);
     double dmu_dt, duu;
-    calc_duu(a, s, b, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
+    calc_duu(a, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
     if (!fixed_dt) ft_time_step<NDIM>(a, s, k, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s.dt);
     double r[4];
@@ -705,10 +735,16 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
 template <int NDIM, bool FT, bool FULL>
 __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, Delta &d) {
     Fld f;
+    double av[16];
+    const double *aux = nullptr;
     if (FULL) {
         double v[32];
         if (!interp<NDIM, 32, 32>(a, a.full1, a.full2, s, v)) return false;
         f = named_full(v);
+        if (a.aux1 && (a.deltab_flag || a.correlation_flag)) {
+            if (!interp<NDIM, 16, 16>(a, a.aux1, a.aux2, s, av)) return false;
+            aux = av;
+        }
     } else {
         constexpr int NV = (NDIM == 2) ? 15 : 21;
         constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
@@ -716,8 +752,8 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
         if (!interp<NDIM, NV, R>(a, a.rec1, a.rec2, s, v)) return false;
         f = named_packed<NDIM>(v);
     }
-    const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f);
-    if (FT) push_ft<NDIM>(a, s, f, k, fixed_dt, d);
+    const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
+    if (FT) push_ft<NDIM>(a, s, f, aux, k, fixed_dt, d);
     else if (NDIM == 2) push2d(a, s, f, k, fixed_dt, d);
     else push3d(a, s, f, k, fixed_dt, d);
     if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) || !isfinite(s.t) ||
@@ -830,7 +866,7 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
     const bool ft = a.focused_transport != 0;
-    const bool full = ft || a.dpp_wave || a.dpp_shear;
+    const bool full = ft || a.dpp_wave || a.dpp_shear || a.deltab_flag || a.correlation_flag;
     const unsigned g = (unsigned)blocks;
     if (a.ndim == 2) {
         if (ft) mover_fp64_kernel<2, true, true><<<g, threads, 0, s>>>(a);

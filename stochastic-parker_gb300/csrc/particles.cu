@@ -70,6 +70,29 @@ __device__ void interp_frame1(const LargeArgs &g, int ndim, double x, double y, 
             }
 }
 
+// db2_slab(1) interpolated at a point (interp_magnetic_fluctuation,
+// mhd_data_parallel.f90:1806-1854, rt = 0), same weights as the fields.
+__device__ double interp_db2(const LargeArgs &g, int ndim, double x, double y, double z) {
+    const double px = (x - g.gxmin) / g.dx, py = (y - g.gymin) / g.dy, pz = (z - g.gzmin) / g.dz;
+    const int fx = (int)floor(px), fy = (int)floor(py), fz = (ndim == 3) ? (int)floor(pz) : 0;
+    const double rx = (px - (double)(fx + 1)) + 1.0;
+    const double ry = (py - (double)(fy + 1)) + 1.0;
+    const double rz = (ndim == 3) ? (pz - (double)(fz + 1)) + 1.0 : 0.0;
+    const double rx1 = 1.0 - rx, ry1 = 1.0 - ry, rz1 = 1.0 - rz;
+    const double w[8] = {rx1 * ry1 * rz1, rx * ry1 * rz1, rx1 * ry * rz1, rx * ry * rz1,
+                         rx1 * ry1 * rz,  rx * ry1 * rz,  rx1 * ry * rz,  rx * ry * rz};
+    const int ix = fx + 2, iy = fy + 2, iz = (ndim == 3) ? fz + 2 : 0;
+    double v = 0.0;
+    for (int k = 0; k < (ndim == 3 ? 2 : 1); ++k)
+        for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 2; ++i) {
+                const size_t cell = (size_t)(ix + i) +
+                                    (size_t)g.nxg * ((size_t)(iy + j) + (size_t)g.nyg * (size_t)(iz + k));
+                v = v + (double)__ldg(g.aux + 16 * cell) * w[k * 4 + j * 2 + i];
+            }
+    return v;
+}
+
 // The quantity each inject_particles_at_large_* tests, from interpolated
 // fields (:874-890, :1027-1044, :1305-1320, :1437); the divv test is on
 // -div v.
@@ -131,9 +154,13 @@ __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
             z = s.next() * (g.dom[5] - g.dom[2]) + g.dom[2];
             if (x >= a.box[0] && x <= a.box[3] && y >= a.box[1] && y <= a.box[4] &&
                 z >= a.box[2] && z <= a.box[5]) {
-                double f[32];
-                interp_frame1(g, a.ndim, x, y, z, f);
-                q = large_quantity(g.quantity, a.ndim, f);
+                if (g.quantity == GPAT_LARGE_DB2) {
+                    q = interp_db2(g, a.ndim, x, y, z);
+                } else {
+                    double f[32];
+                    interp_frame1(g, a.ndim, x, y, z, f);
+                    q = large_quantity(g.quantity, a.ndim, f);
+                }
             } else {
                 q = rho ? 0.0 : -3.0;
             }
@@ -763,6 +790,9 @@ __global__ void count_large_kernel(const LargeArgs g, int ndim, double b0, doubl
                 d = d + (double)u[12];
                 if (ndim > 2) d = d + (double)u[16];
                 q = -d;
+            } else if (g.quantity == GPAT_LARGE_DB2) {
+                q = (double)g.aux[16 * ((size_t)(ix + 1) + (size_t)g.nxg *
+                                        ((size_t)(iy + 1) + (size_t)g.nyg * (size_t)cz))];
             } else {
                 q = (double)r[3];
             }

@@ -26,7 +26,7 @@ ERROR_NAMES = {
     GPAT_ERR_DEVICE: "GPAT_ERR_DEVICE",
 }
 
-LARGE_JZ, LARGE_ABSJ, LARGE_DIVV, LARGE_RHO = 0, 1, 2, 3
+LARGE_JZ, LARGE_ABSJ, LARGE_DIVV, LARGE_RHO, LARGE_DB2 = 0, 1, 2, 3, 4
 PREC_FP64 = 0
 PREC_MIXED = 1
 NOISE_UNIFORM = 0
@@ -153,6 +153,11 @@ SIGNATURES = {
     "gpat_mlp_score": (C.c_int, [Mlp, Handle, d, P(d), P(d)]),
     "gpat_weighted_split": (C.c_int, [Handle, Mlp, d, d, d, d, C.c_int, P(i64), P(i64)]),
     "gpat_tail_weights": (C.c_int, [Handle, d, P(i64), P(d), P(d)]),
+    "gpat_set_fluctuations": (C.c_int, [Handle, C.c_int, P(C.c_float), P(C.c_float),
+                                        P(C.c_float), P(C.c_float)]),
+    "gpat_read_magnetic_fluctuation": (C.c_int, [Handle, C.c_char_p, C.c_int]),
+    "gpat_read_correlation_length": (C.c_int, [Handle, C.c_char_p, C.c_int]),
+    "gpat_get_fluctuations": (C.c_int, [Handle, C.c_int, P(C.c_float)]),
     "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),
     "gpat_inject_particles_at_large": (C.c_int, [Handle, C.c_int, i64, d, C.c_int, d, C.c_int,
                                                  C.c_int, d, i64, P(d), d, P(i64)]),

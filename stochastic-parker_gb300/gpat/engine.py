@@ -257,6 +257,35 @@ class Engine:
         self._check(self.lib.gpat_inject_particles_at_x(
             self.h, int(nptl), xpos, dt, dist_flag, particle_v0, ct_mhd, power_index))
 
+    def set_fluctuations(self, var_flag=0, db2_slab=None, db2_2d=None, lc_slab=None, lc_2d=None):
+        """Turbulence variance / correlation length arrays, each (nzg, nyg, nxg)
+        FP32 over the ghost-padded nodes (None keeps that component)."""
+        keep = []
+
+        def ptr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(C.c_float))
+
+        self._check(self.lib.gpat_set_fluctuations(self.h, var_flag, ptr(db2_slab), ptr(db2_2d),
+                                                   ptr(lc_slab), ptr(lc_2d)))
+
+    def read_magnetic_fluctuation(self, path, var_flag=0):
+        self._check(self.lib.gpat_read_magnetic_fluctuation(self.h, str(path).encode(), var_flag))
+
+    def read_correlation_length(self, path, var_flag=0):
+        self._check(self.lib.gpat_read_correlation_length(self.h, str(path).encode(), var_flag))
+
+    def get_fluctuations(self, var_flag=0) -> np.ndarray:
+        """The (nzg, nyg, nxg, 16) records {db2_slab, db2_2d, lc_slab, lc_2d} x
+        {value, d/dx, d/dy, d/dz}."""
+        out = np.zeros((self.nzg, self.nyg, self.nxg, 16), np.float32)
+        self._check(self.lib.gpat_get_fluctuations(self.h, var_flag,
+                                                   out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
     def count_cells_large(self, quantity, qmin, part_box) -> int:
         """get_ncells_large_jz / _absj / _divv / _rho (quantity: _abi.LARGE_*)."""
         box = (C.c_double * 6)(*part_box)

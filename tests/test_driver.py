@@ -107,3 +107,66 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
         for k in d:
             assert np.array_equal(d[k], got[k]), k
     eng.close()
+
+
+def _bump(shape, seed, lo, hi):
+    """Smooth positive per-node array over the ghost-padded grid."""
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = shape
+    Y, X = np.meshgrid(np.linspace(0, 1, ny), np.linspace(0, 1, nx), indexing="ij")
+    f = np.zeros_like(X)
+    for _ in range(3):
+        kx, ky = rng.integers(1, 4, size=2)
+        f += np.sin(2 * np.pi * (kx * X + ky * Y) + rng.uniform(0, 2 * np.pi))
+    f = (f - f.min()) / (f.max() - f.min())
+    return np.broadcast_to(lo + (hi - lo) * f, shape).astype(np.float32)
+
+
+@pytest.mark.gpu
+def test_driver_turbulence_and_db2_injection(tmp_path):
+    """-db 1 -co 1: deltab_XXXX / lc_XXXX read with every frame
+    (stochastic-mhd.f90:337-346, :417-424); -ib 1 injects where db2_slab
+    exceeds -db2, normalised by -nb (:466-469)."""
+    w, data, out = _dataset(tmp_path)
+    shape = w.frame.shape[:3]
+    for t in range(4):
+        db = np.concatenate([_bump(shape, 10 + t, 0.5, 2.0).ravel(),
+                             _bump(shape, 20 + t, 0.3, 1.0).ravel()])
+        lc = np.concatenate([_bump(shape, 30 + t, 0.5, 1.5).ravel(),
+                             _bump(shape, 40 + t, 0.5, 1.5).ravel()])
+        db.tofile(data / f"deltab_{t:04d}")
+        lc.tofile(data / f"lc_{t:04d}")
+    exe = build.build_driver()
+    cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
+           "-ts", "0", "-te", "3", "-np", "300", "-nm", "40000", "-is", "0", "-in", "1",
+           "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2", "--seed", str(SEED),
+           "-db", "1", "-co", "1", "-ib", ".true.", "-db2", "1.4", "-nb", "2000"]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    edges, f_drv, c_drv = _read_fdists(out / "fdists_0003.dat")
+
+    prm = make_params(**dict(w.params, npp_global=64, nptl_max=40000, seed=SEED, precision=0,
+                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1, deltab_flag=1,
+                             correlation_flag=1))
+    eng = Engine(prm, w.mhd_config, 0)
+    eng.calc_tstamps_mhd(0, 3)
+    cfg = w.mhd_config
+    box = (cfg.xmin, cfg.ymin, cfg.zmin, cfg.xmin + cfg.nx * cfg.dx, cfg.ymin + cfg.ny * cfg.dy,
+           cfg.zmax)
+    injected = 0
+    for tf in range(4):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.read_magnetic_fluctuation(data / f"deltab_{tf:04d}", 0)
+        eng.read_correlation_length(data / f"lc_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        if tf == 0:
+            continue
+        injected += eng.inject_particles_at_large(4, 300, 1e-7, 1, 1.0, tf, False, 1.4, 2000,
+                                                  box)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1, nlgc=True,
+                           kperp_kpara=0.01)
+        eng.split_particle(2.72, 2.0, 10)
+    assert injected > 0
+    f, c = eng.calc_particle_distributions()
+    assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)
+    eng.close()

@@ -81,7 +81,7 @@ def _kappa(params, bx, by, bz, p=0.1, ndim=3, mu=0.5):
     f = (C.c_double * 32)()
     f[4], f[5], f[6] = bx, by, bz
     k = (C.c_double * 22)()
-    oracle.load().orc_calc_spatial_diffusion_coefficients(C.byref(prm), p, mu, f, k)
+    oracle.load().orc_calc_spatial_diffusion_coefficients(C.byref(prm), p, mu, f, None, k)
     return list(k)
 
 
