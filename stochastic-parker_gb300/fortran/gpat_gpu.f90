@@ -21,6 +21,8 @@ module gpat_gpu
         gpu_put_ptls, gpu_get_ptls, gpu_nptl_current, &
         gpu_inject_particles_at_large_jz, gpu_inject_particles_at_large_absj, &
         gpu_inject_particles_at_large_divv, gpu_inject_particles_at_large_rho, &
+        gpu_inject_particles_at_large_db2, gpu_read_magnetic_fluctuation, &
+        gpu_read_correlation_length, &
         gpu_calc_escaped_distributions, gpu_reset_escaped_particles
 
     integer(c_int), parameter :: GPAT_OK = 0
@@ -102,6 +104,20 @@ module gpat_gpu
         end function
         integer(c_int) function c_read_field_data(handle, filename, var_flag) &
                 bind(c, name="gpat_read_field_data")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: filename
+            integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_read_magnetic_fluctuation(handle, filename, var_flag) &
+                bind(c, name="gpat_read_magnetic_fluctuation")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: filename
+            integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_read_correlation_length(handle, filename, var_flag) &
+                bind(c, name="gpat_read_correlation_length")
             import :: c_int, c_ptr, c_char
             type(c_ptr), value :: handle
             character(kind=c_char), dimension(*), intent(in) :: filename
@@ -273,6 +289,24 @@ module gpat_gpu
             "read_field_data")
     end subroutine gpu_read_field_data
 
+    !< read_magnetic_fluctuation + calc_grad_sigma2_slab/_2d
+    !< (mhd_data_parallel.f90:306-397, stochastic-mhd.f90:337-361)
+    subroutine gpu_read_magnetic_fluctuation(filename, var_flag)
+        character(*), intent(in) :: filename
+        integer, intent(in) :: var_flag
+        call check(c_read_magnetic_fluctuation(h, trim(filename)//c_null_char, &
+            int(var_flag, c_int)), "read_magnetic_fluctuation")
+    end subroutine gpu_read_magnetic_fluctuation
+
+    !< read_correlation_length + calc_grad_lc_slab/_2d
+    !< (mhd_data_parallel.f90:406-497, stochastic-mhd.f90:342-371)
+    subroutine gpu_read_correlation_length(filename, var_flag)
+        character(*), intent(in) :: filename
+        integer, intent(in) :: var_flag
+        call check(c_read_correlation_length(h, trim(filename)//c_null_char, &
+            int(var_flag, c_int)), "read_correlation_length")
+    end subroutine gpu_read_correlation_length
+
     !< calc_fields_gradients (mhd_data_parallel.f90:504-610)
     subroutine gpu_calc_fields_gradients(var_flag)
         integer, intent(in) :: var_flag
@@ -303,7 +337,7 @@ module gpat_gpu
             particle_v0, int(ct_mhd, c_int), power_index), "inject_at_x")
     end subroutine gpu_inject_particles_at_x
 
-    !< inject_particles_at_large_jz / _absj / _divv / _rho
+    !< inject_particles_at_large_jz / _absj / _divv / _rho / _db2
     !< (particle_module.f90:785-1468), same arguments
     subroutine inject_large(quantity, nptl, dt, dist_flag, particle_v0, ct_mhd, &
             inject_same_nptl, qmin, ncells_norm, part_box, power_index)
@@ -357,6 +391,16 @@ module gpat_gpu
         call inject_large(3, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
             rho_min, ncells_large_rho_norm, part_box, power_index)
     end subroutine gpu_inject_particles_at_large_rho
+
+    subroutine gpu_inject_particles_at_large_db2(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            inject_same_nptl, db2_min, ncells_large_db2_norm, part_box, power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd, ncells_large_db2_norm
+        logical, intent(in) :: inject_same_nptl
+        real(8), intent(in) :: dt, particle_v0, db2_min, power_index
+        real(8), dimension(6), intent(in) :: part_box
+        call inject_large(4, nptl, dt, dist_flag, particle_v0, ct_mhd, inject_same_nptl, &
+            db2_min, ncells_large_db2_norm, part_box, power_index)
+    end subroutine gpu_inject_particles_at_large_db2
 
     !< calc_escaped_distributions (diagnostics.f90:913-960): fescaped(npp, 2*ndim)
     subroutine gpu_calc_escaped_distributions(fescaped, counts)
