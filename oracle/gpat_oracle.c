@@ -13,6 +13,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -116,8 +117,10 @@ static float grad_axis(const float *a, size_t c, size_t step, int i, int n, doub
  * `stride` floats) into gbase + v * gstep + axis; the z component only in
  * 3D (in 2D it keeps whatever it held). */
 static void grad_generic(float *a, int stride, int nvar, int vstride, int gbase, int gstep,
-                         int ndim, int nxg, int nyg, int nzg, double dx, double dy, double dz)
+                         int ndim, int nxg, int nyg, int nzg, double dx, double dy, double dz,
+                         const double *ihx, const double *ihy, const double *ihz)
 {
+    /* ih*: per-node inverse spans of a non-uniform grid (NULL: 0.5/d). */
     const double idxh = 0.5 / dx, idyh = 0.5 / dy, idzh = 0.5 / dz;
     const size_t sx = (size_t)stride, sy = sx * (size_t)nxg, sz = sy * (size_t)nyg;
     for (int k = 0; k < nzg; ++k)
@@ -126,10 +129,14 @@ static void grad_generic(float *a, int stride, int nvar, int vstride, int gbase,
                 for (int v = 0; v < nvar; ++v) {
                     const size_t c = (size_t)v * vstride + sx * (size_t)i + sy * (size_t)j +
                                      sz * (size_t)k;
-                    GA(a, gbase + v * gstep, i, j, k) = grad_axis(a, c, sx, i, nxg, idxh);
-                    if (nyg > 1) GA(a, gbase + v * gstep + 1, i, j, k) = grad_axis(a, c, sy, j, nyg, idyh);
+                    GA(a, gbase + v * gstep, i, j, k) =
+                        grad_axis(a, c, sx, i, nxg, ihx ? ihx[i] : idxh);
+                    if (nyg > 1)
+                        GA(a, gbase + v * gstep + 1, i, j, k) =
+                            grad_axis(a, c, sy, j, nyg, ihy ? ihy[j] : idyh);
                     if (nzg > 1 && ndim == 3)
-                        GA(a, gbase + v * gstep + 2, i, j, k) = grad_axis(a, c, sz, k, nzg, idzh);
+                        GA(a, gbase + v * gstep + 2, i, j, k) =
+                            grad_axis(a, c, sz, k, nzg, ihz ? ihz[k] : idzh);
                 }
 }
 
@@ -138,7 +145,7 @@ static void grad_generic(float *a, int stride, int nvar, int vstride, int gbase,
 void orc_calc_fields_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
                                double dx, double dy, double dz)
 {
-    grad_generic(a, 32, 8, 1, 8, 3, ndim, nxg, nyg, nzg, dx, dy, dz);
+    grad_generic(a, 32, 8, 1, 8, 3, ndim, nxg, nyg, nzg, dx, dy, dz, NULL, NULL, NULL);
 }
 
 /* calc_grad_sigma2_slab / _2d and calc_grad_lc_slab / _2d
@@ -147,7 +154,165 @@ void orc_calc_fields_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
 void orc_calc_aux_gradients(float *a, int ndim, int nxg, int nyg, int nzg,
                             double dx, double dy, double dz)
 {
-    grad_generic(a, 16, 4, 4, 1, 4, ndim, nxg, nyg, nzg, dx, dy, dz);
+    grad_generic(a, 16, 4, 4, 1, 4, ndim, nxg, nyg, nzg, dx, dy, dz, NULL, NULL, NULL);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grid positions for spherical and non-uniform grids.                      */
+/* ------------------------------------------------------------------------ */
+static struct {
+    double *pos[3];   /* node positions, ghost nodes included               */
+    double *ih[3];    /* idxh_grid: inverse spans for the gradients         */
+    int n[3];
+} g_grid;
+
+/* set_local_grid_positions (mhd_data_parallel.f90:2153-2190) on one rank:
+ * 1 / (x[i+1] - x[i-1]) inside, the one-sided spans at the two ends. */
+static void inverse_spans(const double *x, int n, double *ih)
+{
+    if (n < 3) {
+        for (int i = 0; i < n; ++i) ih[i] = 0.0;
+        return;
+    }
+    for (int i = 1; i < n - 1; ++i) ih[i] = 1.0 / (x[i + 1] - x[i - 1]);
+    ih[0] = 1.0 / (-(3.0 * x[0]) + 4.0 * x[1] - x[2]);
+    ih[n - 1] = 1.0 / (3.0 * x[n - 1] - 4.0 * x[n - 2] + x[n - 3]);
+}
+
+void orc_set_grid_positions(const double *xpos, const double *ypos, const double *zpos,
+                            int nxg, int nyg, int nzg)
+{
+    const double *src[3] = {xpos, ypos, zpos};
+    const int n[3] = {nxg, nyg, nzg};
+    for (int a = 0; a < 3; ++a) {
+        free(g_grid.pos[a]);
+        free(g_grid.ih[a]);
+        g_grid.pos[a] = NULL;
+        g_grid.ih[a] = NULL;
+        g_grid.n[a] = 0;
+        if (!src[a] || n[a] <= 0) continue;
+        g_grid.pos[a] = (double *)malloc(sizeof(double) * (size_t)n[a]);
+        g_grid.ih[a] = (double *)malloc(sizeof(double) * (size_t)n[a]);
+        memcpy(g_grid.pos[a], src[a], sizeof(double) * (size_t)n[a]);
+        inverse_spans(g_grid.pos[a], n[a], g_grid.ih[a]);
+        g_grid.n[a] = n[a];
+    }
+}
+
+void orc_uniform_grid_positions(int n, double d, double xmin, double *pos)
+{
+    for (int j = 0; j < n; ++j) pos[j] = d * (double)(j - 2) + xmin;
+}
+
+int orc_binary_search(const double *a, int n, double v)
+{
+    /* For increasing nodes the recursion of binarySearch_R returns the
+     * count of nodes <= v; this is the same count by bisection. */
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = lo + (hi - lo) / 2;
+        if (a[mid] > v) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+void orc_calc_fields_gradients_nonuniform(float *a, int ndim, int nxg, int nyg, int nzg)
+{
+    grad_generic(a, 32, 8, 1, 8, 3, ndim, nxg, nyg, nzg, 1.0, 1.0, 1.0, g_grid.ih[0],
+                 g_grid.ih[1], g_grid.ih[2]);
+}
+
+void orc_calc_aux_gradients_nonuniform(float *a, int ndim, int nxg, int nyg, int nzg)
+{
+    grad_generic(a, 16, 4, 4, 1, 4, ndim, nxg, nyg, nzg, 1.0, 1.0, 1.0, g_grid.ih[0],
+                 g_grid.ih[1], g_grid.ih[2]);
+}
+
+/* The node count along an axis, checked: the particle must lie between the
+ * first and the last ghost node (the engine reports such a particle as an
+ * index-guard error). */
+static int grid_count(int axis, double v)
+{
+    const int n = g_grid.n[axis];
+    const double *x = g_grid.pos[axis];
+    if (!x || !(v >= x[1] && v < x[n - 1])) {
+        fprintf(stderr, "oracle: position %.17g outside the grid along axis %d\n", v, axis);
+        abort();
+    }
+    return orc_binary_search(x, n, v);
+}
+
+/* get_interp_paramters_spherical: particle_module.f90:705-775 (2D and 3D). */
+static void spherical_weights(int ndim, double x, double y, double z, int32_t pos[3], double w[8])
+{
+    const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
+    pos[0] = grid_count(0, x) - 2;
+    pos[1] = grid_count(1, y) - 2;
+    pos[2] = (ndim == 3) ? grid_count(2, z) - 2 : 1;
+    /* xpos_local(i) is X[i + 1]. */
+    const double ctheta1 = cos(Y[pos[1] + 1]);
+    const double ctheta2 = cos(Y[pos[1] + 2]);
+    const double ctheta = cos(y);
+    const double one_third = 1.0 / 3.0;
+    const double x3 = x * x * x * one_third;
+    const double xa = X[pos[0] + 1], xb = X[pos[0] + 2];
+    const double x3_1 = xa * xa * xa * one_third;
+    const double x3_2 = xb * xb * xb * one_third;
+    const double rx = x3 - x3_1, rx1 = x3_2 - x3;
+    const double ry = ctheta1 - ctheta, ry1 = ctheta - ctheta2;
+    double rz = 0.0, rz1 = 1.0;
+    if (ndim == 3) {
+        rz = z - Z[pos[2] + 1];
+        rz1 = Z[pos[2] + 2] - z;
+    }
+    const double dv = (x3_2 - x3_1) * (ry + ry1) * (rz + rz1);
+    w[0] = rx1 * ry1 * rz1;
+    w[1] = rx * ry1 * rz1;
+    w[2] = rx1 * ry * rz1;
+    w[3] = rx * ry * rz1;
+    w[4] = rx1 * ry1 * rz;
+    w[5] = rx * ry1 * rz;
+    w[6] = rx1 * ry * rz;
+    w[7] = rx * ry * rz;
+    for (int k = 0; k < 8; ++k) w[k] = w[k] / dv;
+}
+
+void orc_grid_interp_paramters(const orc_params *pr, const orc_mhd_config *cfg, double x,
+                               double y, double z, int32_t pos[3], double w[8])
+{
+    const int ndim = pr->ndim;
+    if (pr->spherical_coord) {
+        spherical_weights(ndim, x, y, z, pos, w);
+        return;
+    }
+    if (!pr->nonuniform_grid) {
+        orc_get_interp_paramters(ndim, (x - cfg->xmin) / cfg->dx, (y - cfg->ymin) / cfg->dy,
+                                 (z - cfg->zmin) / cfg->dz, pos, w);
+        return;
+    }
+    /* :1620-1625 computes the offset inside the cell found by the search
+     * and get_interp_paramters then places the corner at floor(offset) + 1,
+     * i.e. at the first cell whatever the search found.  The corner is
+     * shifted to the searched cell here (the reference's weights, the
+     * intended cell). */
+    const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
+    const int ix = grid_count(0, x) - 2;
+    const int iy = grid_count(1, y) - 2;
+    const int iz = (ndim == 3) ? grid_count(2, z) - 2 : 1;
+    const double px = (x - X[ix + 1]) / (X[ix + 2] - X[ix + 1]);
+    const double py = (y - Y[iy + 1]) / (Y[iy + 2] - Y[iy + 1]);
+    const double pz = (ndim == 3) ? (z - Z[iz + 1]) / (Z[iz + 2] - Z[iz + 1]) : 0.0;
+    orc_get_interp_paramters(ndim, px, py, pz, pos, w);
+    pos[0] += ix - 1;
+    pos[1] += iy - 1;
+    if (ndim == 3) pos[2] += iz - 1;
+    const int hi[3] = {g_grid.n[0] - 3, g_grid.n[1] - 3, (ndim == 3) ? g_grid.n[2] - 3 : 1};
+    for (int a = 0; a < ndim; ++a)
+        if (pos[a] > hi[a]) {
+            fprintf(stderr, "oracle: interpolation corner outside the grid along axis %d\n", a);
+            abort();
+        }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -393,6 +558,7 @@ typedef struct mover_ctx {
     double cfg_xmin, cfg_ymin, cfg_zmin, cfg_lx, cfg_ly, cfg_lz;
     double dt_min, dt_max, t0, dtf;
     uint32_t key[2];
+    int sph, nonuni;       /* spherical_coord, nonuniform_grid             */
 } mover_ctx;
 
 typedef struct ptl_state {
@@ -408,13 +574,29 @@ typedef struct thread_acc {
 
 /* Four unit-variance increments for one push, drawn in the reference's order
  * ran1, ran2, ran3 (position) then ran1 again (momentum); :3546-3590. */
-static void push_noise(const mover_ctx *c, ptl_state *s, double r[4])
+static void push_noise_n(const mover_ctx *c, ptl_state *s, double *r, int n6)
 {
     uint32_t w[8];
     uint32_t ctr[4] = {s->rng_ctr, 0u, (uint32_t)s->tag_injected, (uint32_t)s->tag_splitted};
     orc_philox4x32_10(ctr, c->key, w);
     ctr[1] = 1u;
     orc_philox4x32_10(ctr, c->key, w + 4);
+    if (n6) {
+        /* A third block for pushes that draw five numbers (3D spherical
+         * focused transport); r[4] and r[5] come from it. */
+        uint32_t w3[4];
+        ctr[1] = 2u;
+        orc_philox4x32_10(ctr, c->key, w3);
+        const double u4 = orc_u01(w3[0], w3[1]), u5 = orc_u01(w3[2], w3[3]);
+        if (c->pr->noise == 0) {
+            r[4] = (2.0 * u4 - 1.0) * sqrt(3.0);
+            r[5] = (2.0 * u5 - 1.0) * sqrt(3.0);
+        } else {
+            const double rc = sqrt(-2.0 * log(1.0 - u4));
+            r[4] = rc * cos(6.283185307179586 * u5);
+            r[5] = rc * sin(6.283185307179586 * u5);
+        }
+    }
     s->rng_ctr += 1u;
     const double u0 = orc_u01(w[0], w[1]), u1 = orc_u01(w[2], w[3]);
     const double u2 = orc_u01(w[4], w[5]), u3 = orc_u01(w[6], w[7]);
@@ -431,6 +613,76 @@ static void push_noise(const mover_ctx *c, ptl_state *s, double r[4])
         r[1] = ra * sin(twopi * u1);
         r[2] = rb * cos(twopi * u3);
         r[3] = rb * sin(twopi * u3);
+    }
+}
+
+static void push_noise(const mover_ctx *c, ptl_state *s, double r[4])
+{
+    push_noise_n(c, s, r, 0);
+}
+
+/* Metric factors of spherical coordinates (x = r, y = theta, z = phi) set
+ * at the top of every push (:3420-3427, :4707-4713). */
+typedef struct sph_terms {
+    double ctheta, istheta, cot_theta, ir, ir2;
+} sph_terms;
+
+static sph_terms spherical_terms(const ptl_state *s)
+{
+    sph_terms t;
+    t.ctheta = cos(s->y);
+    t.istheta = 1.0 / sin(s->y);
+    t.cot_theta = t.ctheta * t.istheta;
+    t.ir = 1.0 / s->x;
+    t.ir2 = 1.0 / (s->x * s->x);
+    return t;
+}
+
+/* The position noise of the 2D spherical pushes: eigen-decomposition of
+ * the (r, theta) diffusion tensor (:3559-3580, :3905-3925). */
+static void spherical_noise_2d(const double *kap, const sph_terms *g, double r1, double r2,
+                               double sdt, double *nx, double *ny)
+{
+    const double a1 = kap[K_KXX];
+    const double b1 = kap[K_KXY] * g->ir;
+    const double c1 = kap[K_KYY] * g->ir2;
+    const double amc = a1 - c1;
+    const double atmp = sqrt(amc * amc + 4.0 * (b1 * b1));
+    const double Qpp = atmp + (a1 + c1);
+    double Qmp = atmp - (a1 + c1);
+    const double Qpm = atmp + (a1 - c1);
+    const double Qmm = atmp - (a1 - c1);
+    if (Qmp > 0.0) Qmp = 0.0;
+    const double qtmp1 = sqrt(-Qmp / (Qmm * Qmm + 4.0 * (b1 * b1)));
+    const double qtmp2 = sqrt(Qpp / (Qpm * Qpm + 4.0 * (b1 * b1)));
+    *nx = (-(Qmm * qtmp1 * r1) + Qpm * qtmp2 * r2) * sdt;
+    *ny = (2.0 * b1 * qtmp1 * r1 + 2.0 * b1 * qtmp2 * r2) * sdt;
+}
+
+/* The 3D spherical noise matrix (upper triangular, P P^T = 2 K in the
+ * metric); `clamp` adds the focused-transport pushes' guards against
+ * small negative radicands (:5253-5278) that the Parker push lacks
+ * (:4852-4863). */
+static void spherical_noise_3d(const double *kap, const sph_terms *g, int clamp, double p[6])
+{
+    const double kxx = kap[K_KXX], kyy = kap[K_KYY], kzz = kap[K_KZZ];
+    const double kxy = kap[K_KXY], kxz = kap[K_KXZ], kyz = kap[K_KYZ];
+    const double num = kxx * (kyz * kyz) + kyy * (kxz * kxz) + kzz * (kxy * kxy) -
+                       2.0 * kxy * kxz * kyz - kxx * kyy * kzz;
+    const double den = kyz * kyz - kyy * kzz;
+    double d = 2.0 * num / den;
+    if (clamp && d < 0.0) d = 0.0;
+    p[0] = sqrt(d);                                            /* p11 */
+    d = 2.0 * (kyy - kyz * kyz / kzz);
+    if (clamp && d < 0.0) d = 0.0;
+    p[1] = (kxz * kyz - kxy * kzz) * sqrt(d) / den;            /* p12 */
+    p[3] = sqrt(d) * g->ir;                                    /* p22 */
+    if (clamp && kzz <= 0.0) {
+        p[2] = 0.0; p[4] = 0.0; p[5] = 0.0;
+    } else {
+        p[2] = sqrt(2.0 / kzz) * kxz;                          /* p13 */
+        p[4] = sqrt(2.0 / kzz) * kyz * g->ir;                  /* p23 */
+        p[5] = sqrt(2.0 * kzz) * g->istheta * g->ir;           /* p33 */
     }
 }
 
@@ -528,31 +780,62 @@ static void push_momentum(const mover_ctx *c, ptl_state *s, double dp_dt, double
     *deltap = dP;
 }
 
-/* push_particle_2d, Cartesian uniform grid: particle_module.f90:3358-3606. */
+/* Cell sizes seen by a push: mhd_config's dx, dy, dz on a uniform grid,
+ * the searched cell's spans on a non-uniform one (:3400-3408, :4689-4700). */
+typedef struct cell_size {
+    double dxm, dym, dzm;
+} cell_size;
+
+/* push_particle_2d: particle_module.f90:3358-3606, Cartesian and
+ * spherical (x = r, y = theta). */
 static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                    int fixed_dt, double d[6])
+                    const cell_size *cs, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double dvx_dx = f[8], dvy_dy = f[12];
-    const double dxm = c->dx, dym = c->dy;
+    const double dxm = cs->dxm, dym = cs->dym;
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    sph_terms g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (c->sph) g = spherical_terms(s);
     const double dbz_dx = f[26], dbz_dy = f[27], db_dx = f[29], db_dy = f[30];
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
     const double vdp = vdrift_prefactor(pr, s->p);
-    const double vdx = vdp * (dbz_dy * ib2 - 2.0 * bz * db_dy * ib3);
-    const double vdy = vdp * (-(dbz_dx * ib2) + 2.0 * bz * db_dx * ib3);
+    double vdx, vdy, gbr = 0.0, gbt = 0.0;
+    if (c->sph) {
+        gbr = db_dx;
+        gbt = db_dy * g.ir;
+        vdx = vdp * ((dbz_dy + g.cot_theta * bz) * g.ir * ib2 - gbt * bz * 2.0 * ib3);
+        vdy = vdp * (-((dbz_dx + bz * g.ir) * ib2) + gbr * bz * 2.0 * ib3);
+    } else {
+        vdx = vdp * (dbz_dy * ib2 - 2.0 * bz * db_dy * ib3);
+        vdy = vdp * (-(dbz_dx * ib2) + 2.0 * bz * db_dx * ib3);
+    }
     double vdz = 0.0;
     if (pr->check_drift_2d) {
         const double dbx_dy = f[21], dby_dx = f[23];
-        vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
+        if (c->sph)
+            vdz = vdp * ((dby_dx + by * g.ir - dbx_dy * g.ir) * ib2 -
+                         (gbr * by - gbt * bx * g.ir) * 2.0 * ib3);
+        else
+            vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
     }
-    const double dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
-    const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY];
-    const double dz_dt = vdz;
-    const double divv = dvx_dx + dvy_dy;
+    double dx_dt, dy_dt, dz_dt, divv;
+    if (c->sph) {
+        dx_dt = vx + vdx + kap[K_DKXX_DX] +
+                (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * g.cot_theta) * g.ir;
+        dy_dt = (vy + vdy + kap[K_DKXY_DX]) * g.ir +
+                (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * g.cot_theta) * g.ir2;
+        dz_dt = vdz * g.istheta * g.ir;
+        divv = dvx_dx + (2.0 * vx + dvy_dy + vy * g.ctheta * g.istheta) * g.ir;
+    } else {
+        dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
+        dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY];
+        dz_dt = vdz;
+        divv = dvx_dx + dvy_dy;
+    }
     double dp_dt = -(s->p * divv / 3.0);
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
@@ -560,9 +843,15 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
             const double sk = (skperp > 0.0) ? skperp : skpara;
             double a = 0.5 * dxm / skpara, m = a * a;
-            a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
-            a = sk / dx_dt; if (a * a < m) m = a * a;
-            a = sk / dy_dt; if (a * a < m) m = a * a;
+            if (c->sph) {
+                a = 0.5 * dym * s->x / skpara; if (a * a < m) m = a * a;
+                a = sk / dx_dt; if (a * a < m) m = a * a;
+                a = sk * g.ir / dy_dt; if (a * a < m) m = a * a;
+            } else {
+                a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
+                a = sk / dx_dt; if (a * a < m) m = a * a;
+                a = sk / dy_dt; if (a * a < m) m = a * a;
+            }
             a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
             s->dt = m;
         } else {
@@ -574,9 +863,17 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     const double sdt = sqrt(s->dt);
     double r[4];
     push_noise(c, s, r);
-    const double skpp = kap[K_SKPARA_PERP];
-    const double dX = dx_dt * s->dt + r[0] * skperp * sdt + r[2] * skpp * sdt * bx * ib;
-    const double dY = dy_dt * s->dt + r[1] * skperp * sdt + r[2] * skpp * sdt * by * ib;
+    double dX, dY;
+    if (c->sph) {
+        double nx, ny;
+        spherical_noise_2d(kap, &g, r[0], r[1], sdt, &nx, &ny);
+        dX = dx_dt * s->dt + nx;
+        dY = dy_dt * s->dt + ny;
+    } else {
+        const double skpp = kap[K_SKPARA_PERP];
+        dX = dx_dt * s->dt + r[0] * skperp * sdt + r[2] * skpp * sdt * bx * ib;
+        dY = dy_dt * s->dt + r[1] * skperp * sdt + r[2] * skpp * sdt * by * ib;
+    }
     const double dZ = dz_dt * s->dt;
     s->x = s->x + dX;
     s->y = s->y + dY;
@@ -588,9 +885,10 @@ static void push_2d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     push_momentum(c, s, dp_dt, dpp, sdt, r[3], &d[3]);
 }
 
-/* push_particle_3d, Cartesian uniform grid: particle_module.f90:4625-4907. */
+/* push_particle_3d: particle_module.f90:4625-4907, Cartesian and spherical
+ * (x = r, y = theta, z = phi), without the acceleration surfaces. */
 static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
-                    int fixed_dt, double d[6])
+                    const cell_size *cs, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
@@ -600,20 +898,46 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     const double bxyn = sqrt(bxn * bxn + byn * byn);
     const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
     const double dvx_dx = f[8], dvy_dy = f[12], dvz_dz = f[16];
-    const double dxm = c->dx, dym = c->dy, dzm = c->dz;
+    const double dxm = cs->dxm, dym = cs->dym, dzm = cs->dzm;
+    sph_terms g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (c->sph) g = spherical_terms(s);
     const double dbx_dy = f[21], dbx_dz = f[22], dby_dx = f[23], dby_dz = f[25];
     const double dbz_dx = f[26], dbz_dy = f[27];
     const double db_dx = f[29], db_dy = f[30], db_dz = f[31];
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
     const double vdp = vdrift_prefactor(pr, s->p);
-    const double vdx = vdp * ((dbz_dy - dby_dz) * ib2 - 2.0 * (bz * db_dy - by * db_dz) * ib3);
-    const double vdy = vdp * ((dbx_dz - dbz_dx) * ib2 - 2.0 * (bx * db_dz - bz * db_dx) * ib3);
-    const double vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
-    const double dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
-    const double dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
-    const double dz_dt = vz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
-    const double divv = dvx_dx + dvy_dy + dvz_dz;
+    double vdx, vdy, vdz;
+    if (c->sph) {
+        const double gbr = db_dx, gbt = db_dy * g.ir, gbp = db_dz * g.ir * g.istheta;
+        vdx = vdp * ((dbz_dy + bz * g.ctheta * g.istheta - dby_dz * g.istheta) * g.ir * ib2 -
+                     (gbt * bz - gbp * by) * 2.0 * ib3);
+        vdy = vdp * ((dbx_dz * g.istheta * g.ir - dbz_dx - bz * g.ir) * ib2 -
+                     (gbp * bx - gbr * bz) * 2.0 * ib3);
+        vdz = vdp * ((dby_dx + by * g.ir - dbx_dy * g.ir) * ib2 -
+                     (gbr * by - gbt * bx) * 2.0 * ib3);
+    } else {
+        vdx = vdp * ((dbz_dy - dby_dz) * ib2 - 2.0 * (bz * db_dy - by * db_dz) * ib3);
+        vdy = vdp * ((dbx_dz - dbz_dx) * ib2 - 2.0 * (bx * db_dz - bz * db_dx) * ib3);
+        vdz = vdp * ((dby_dx - dbx_dy) * ib2 - 2.0 * (by * db_dx - bx * db_dy) * ib3);
+    }
+    double dx_dt, dy_dt, dz_dt, divv;
+    if (c->sph) {
+        dx_dt = vx + vdx + kap[K_DKXX_DX] +
+                (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * g.ctheta * g.istheta +
+                 kap[K_DKXZ_DZ] * g.istheta) * g.ir;
+        dy_dt = (vy + vdy + kap[K_DKXY_DX]) * g.ir +
+                (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * g.ctheta * g.istheta +
+                 kap[K_DKYZ_DZ] * g.istheta) * g.ir2;
+        dz_dt = (vz + vdz + kap[K_DKXZ_DX]) * g.istheta * g.ir +
+                (kap[K_KXZ] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ] * g.istheta) * g.istheta * g.ir2;
+        divv = dvx_dx + (2.0 * vx + dvy_dy + vy * g.ctheta * g.istheta + dvz_dz * g.istheta) * g.ir;
+    } else {
+        dx_dt = vx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
+        dy_dt = vy + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
+        dz_dt = vz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
+        divv = dvx_dx + dvy_dy + dvz_dz;
+    }
     double dp_dt = -(s->p * divv / 3.0);
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
     const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
@@ -621,11 +945,19 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
             const double sk = (skperp > 0.0) ? skperp : skpara;
             double a = 0.5 * dxm / skpara, m = a * a;
-            a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
-            a = 0.5 * dzm / skpara; if (a * a < m) m = a * a;
-            a = sk / dx_dt; if (a * a < m) m = a * a;
-            a = sk / dy_dt; if (a * a < m) m = a * a;
-            a = sk / dz_dt; if (a * a < m) m = a * a;
+            if (c->sph) {
+                a = 0.5 * dym * s->x / skpara; if (a * a < m) m = a * a;
+                a = 0.5 * dzm * s->x * sin(s->y) / skpara; if (a * a < m) m = a * a;
+                a = sk / dx_dt; if (a * a < m) m = a * a;
+                a = sk * g.ir / dy_dt; if (a * a < m) m = a * a;
+                a = sk * g.ir * g.istheta / dz_dt; if (a * a < m) m = a * a;
+            } else {
+                a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
+                a = 0.5 * dzm / skpara; if (a * a < m) m = a * a;
+                a = sk / dx_dt; if (a * a < m) m = a * a;
+                a = sk / dy_dt; if (a * a < m) m = a * a;
+                a = sk / dz_dt; if (a * a < m) m = a * a;
+            }
             a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
             s->dt = m;
         } else {
@@ -637,11 +969,20 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
     const double sdt = sqrt(s->dt);
     double r[4];
     push_noise(c, s, r);
-    const double dX = dx_dt * s->dt +
-        (bxn * skpara * r[0] - bxn * bzn * skperp * ibxyn * r[1] - byn * skperp * ibxyn * r[2]) * sdt;
-    const double dY = dy_dt * s->dt +
-        (byn * skpara * r[0] - byn * bzn * skperp * ibxyn * r[1] + bxn * skperp * ibxyn * r[2]) * sdt;
-    const double dZ = dz_dt * s->dt + (bzn * skpara * r[0] + bxyn * skperp * r[1]) * sdt;
+    double dX, dY, dZ;
+    if (c->sph) {
+        double q[6];
+        spherical_noise_3d(kap, &g, 0, q);
+        dX = dx_dt * s->dt + (q[0] * r[0] + q[1] * r[1] + q[2] * r[2]) * sdt;
+        dY = dy_dt * s->dt + (q[3] * r[1] + q[4] * r[2]) * sdt;
+        dZ = dz_dt * s->dt + q[5] * r[2] * sdt;
+    } else {
+        dX = dx_dt * s->dt +
+            (bxn * skpara * r[0] - bxn * bzn * skperp * ibxyn * r[1] - byn * skperp * ibxyn * r[2]) * sdt;
+        dY = dy_dt * s->dt +
+            (byn * skpara * r[0] - byn * bzn * skperp * ibxyn * r[1] + bxn * skperp * ibxyn * r[2]) * sdt;
+        dZ = dz_dt * s->dt + (bzn * skpara * r[0] + bxyn * skperp * r[1]) * sdt;
+    }
     s->x = s->x + dX;
     s->y = s->y + dY;
     s->z = s->z + dZ;
@@ -742,21 +1083,30 @@ static void push_ft_tail(const mover_ctx *c, ptl_state *s, double dX, double dY,
 
 /* The adaptive time step of the focused-transport pushes (:3850-3905,
  * :5170-5230): the minimum of the cell-crossing, drift, momentum and
- * pitch-angle limits, dt_min when any first-order rate is exactly 0. */
+ * pitch-angle limits, dt_min when any first-order rate is exactly 0.  In
+ * spherical coordinates the theta and phi limits carry r and r sin(theta). */
 static void ft_time_step(const mover_ctx *c, ptl_state *s, const double *kap, int ndim,
-                         double dx_dt, double dy_dt, double dz_dt, double dp_dt,
-                         double dmu_dt, double duu)
+                         const cell_size *cs, const sph_terms *g, double dx_dt, double dy_dt,
+                         double dz_dt, double dp_dt, double dmu_dt, double duu)
 {
     const int rates_nonzero = (dx_dt != 0.0) && (dy_dt != 0.0) && (ndim < 3 || dz_dt != 0.0) &&
                               (dp_dt != 0.0) && (dmu_dt != 0.0);
     if (rates_nonzero) {
         const double sk = (kap[K_SKPERP] > 0.0) ? kap[K_SKPERP] : kap[K_SKPARA];
-        double a = 0.5 * c->dx / sk, m = a * a;
-        a = 0.5 * c->dy / sk; if (a * a < m) m = a * a;
-        if (ndim == 3) { a = 0.5 * c->dz / sk; if (a * a < m) m = a * a; }
-        a = sk / dx_dt; if (a * a < m) m = a * a;
-        a = sk / dy_dt; if (a * a < m) m = a * a;
-        if (ndim == 3) { a = sk / dz_dt; if (a * a < m) m = a * a; }
+        double a = 0.5 * cs->dxm / sk, m = a * a;
+        if (c->sph) {
+            a = 0.5 * cs->dym * s->x / sk; if (a * a < m) m = a * a;
+            if (ndim == 3) { a = 0.5 * cs->dzm * s->x * sin(s->y) / sk; if (a * a < m) m = a * a; }
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = sk * g->ir / dy_dt; if (a * a < m) m = a * a;
+            if (ndim == 3) { a = sk * g->ir * g->istheta / dz_dt; if (a * a < m) m = a * a; }
+        } else {
+            a = 0.5 * cs->dym / sk; if (a * a < m) m = a * a;
+            if (ndim == 3) { a = 0.5 * cs->dzm / sk; if (a * a < m) m = a * a; }
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = sk / dy_dt; if (a * a < m) m = a * a;
+            if (ndim == 3) { a = sk / dz_dt; if (a * a < m) m = a * a; }
+        }
         a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
         a = (double)0.1f / fabs(dmu_dt); if (a < m) m = a;
         a = 2.0 * duu / (dmu_dt * dmu_dt); if (a < m) m = a;
@@ -768,14 +1118,17 @@ static void ft_time_step(const mover_ctx *c, ptl_state *s, const double *kap, in
     if (s->dt > c->dt_max) s->dt = c->dt_max;
 }
 
-/* push_particle_2d_ft, Cartesian uniform grid: particle_module.f90:3626-3964. */
+/* push_particle_2d_ft: particle_module.f90:3626-3964, Cartesian and
+ * spherical. */
 static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *aux,
-                       const double *kap, int fixed_dt, double d[6])
+                       const double *kap, const cell_size *cs, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
-    const double vx = f[0], vy = f[1], bx = f[4], by = f[5], bz = f[6];
+    const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    sph_terms g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (c->sph) g = spherical_terms(s);
     const double dbx_dx = f[20], dbx_dy = f[21], dby_dx = f[23], dby_dy = f[24];
     const double dbz_dx = f[26], dbz_dy = f[27], db_dx = f[29], db_dy = f[30];
     const double ib2 = ib * ib;
@@ -784,56 +1137,105 @@ static void push_2d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double mu2 = s->mu * s->mu;
     const double muf1 = 0.5 * (1.0 - mu2);
     const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
-    const double kx = bx * dbx_dx + by * dbx_dy;
-    const double ky = bx * dby_dx + by * dby_dy;
-    const double kz = bx * dbz_dx + by * dbz_dy;
-    const double bdot_curvb = bx * dbz_dy - by * dbz_dx + bz * (dby_dx - dbx_dy);
-    const double vdx = vdp * (muf1 * (-(bz * db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
-                              muf1 * bx * bdot_curvb * ib3);
-    const double vdy = vdp * (muf1 * (bz * db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
-                              muf1 * by * bdot_curvb * ib3);
+    double kx, ky, kz, bdot_curvb, vdx, vdy, gbr = 0.0, gbt = 0.0;
+    if (c->sph) {
+        const double ir = g.ir, cot = g.cot_theta;
+        gbr = db_dx;
+        gbt = db_dy * ir;
+        kx = bx * dbx_dx + by * dbx_dy * ir - (by * by + bz * bz) * ir;
+        ky = bx * dby_dx + by * dby_dy * ir + (bx * by - cot * (bz * bz)) * ir;
+        kz = bx * dbz_dx + by * dbz_dy * ir + (bx * bz + cot * by * bz) * ir;
+        bdot_curvb = bx * (dbz_dy + cot * bz) * ir + by * (-dbz_dx - bz * ir) +
+                     bz * (dby_dx + by * ir - dbx_dy * ir);
+        vdx = vdp * (muf1 * (-(bz * gbt)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                     muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * gbr) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                     muf1 * by * bdot_curvb * ib3);
+    } else {
+        kx = bx * dbx_dx + by * dbx_dy;
+        ky = bx * dby_dx + by * dby_dy;
+        kz = bx * dbz_dx + by * dbz_dy;
+        bdot_curvb = bx * dbz_dy - by * dbz_dx + bz * (dby_dx - dbx_dy);
+        vdx = vdp * (muf1 * (-(bz * db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                     muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                     muf1 * by * bdot_curvb * ib3);
+    }
     double vdz = 0.0;
-    if (pr->check_drift_2d)
-        vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
-                     muf1 * bz * bdot_curvb * ib3);
+    if (pr->check_drift_2d) {
+        if (c->sph)
+            vdz = vdp * (muf1 * (bx * gbt - by * gbr) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                         muf1 * bz * bdot_curvb * ib3);
+        else
+            vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                         muf1 * bz * bdot_curvb * ib3);
+    }
     double vbx = s->v * s->mu * ib;
     const double vby = vbx * by;
     vbx = vbx * bx;
     const double dvx_dx = f[8], dvx_dy = f[9], dvy_dx = f[11], dvy_dy = f[12];
     const double dvz_dx = f[14], dvz_dy = f[15];
-    const double dx_dt = vx + vdx + vbx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
-    const double dy_dt = vy + vdy + vby + kap[K_DKXY_DX] + kap[K_DKYY_DY];
-    const double dz_dt = vdz;
-    const double divv = dvx_dx + dvy_dy;
-    const double bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy) +
-                             by * (bx * dvy_dx + by * dvy_dy) +
-                             bz * (bx * dvz_dx + by * dvz_dy)) * ib2;
-    const double bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy) +
-                             by * (vx * dvy_dx + vy * dvy_dy) +
-                             bz * (vx * dvz_dx + vy * dvz_dy)) * ib;
+    double dx_dt, dy_dt, dz_dt, divv, bb_gradv, bv_gradv;
+    if (c->sph) {
+        const double ir = g.ir, cot = g.cot_theta;
+        dx_dt = vx + vdx + vbx + kap[K_DKXX_DX] +
+                (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * cot) * ir;
+        dy_dt = (vy + vdy + vby + kap[K_DKXY_DX]) * ir +
+                (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * cot) * g.ir2;
+        dz_dt = vdz * g.istheta * ir;
+        divv = dvx_dx + (2.0 * vx + dvy_dy + vy * cot) * ir;
+        bb_gradv = (bx * bx * dvx_dx + bx * by * dvx_dy * ir - bx * (by * vy + bz * vz) * ir +
+                    by * bx * dvy_dx + by * by * dvy_dy * ir + by * (by * vx - cot * bz * vz) * ir +
+                    bz * bx * dvz_dx + bz * by * dvz_dy * ir + (bz * bz) * (vx + cot * vy) * ir) * ib2;
+        bv_gradv = (bx * vx * dvx_dx + bx * vy * dvx_dy * ir - bx * (vy * vy + vz * vz) * ir +
+                    by * vx * dvy_dx + by * vy * dvy_dy * ir + by * (vy * vx - cot * vz * vz) * ir +
+                    bz * vx * dvz_dx + bz * vy * dvz_dy * ir + bz * vz * (vx + cot * vy) * ir) * ib;
+    } else {
+        dx_dt = vx + vdx + vbx + kap[K_DKXX_DX] + kap[K_DKXY_DY];
+        dy_dt = vy + vdy + vby + kap[K_DKXY_DX] + kap[K_DKYY_DY];
+        dz_dt = vdz;
+        divv = dvx_dx + dvy_dy;
+        bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy) +
+                    by * (bx * dvy_dx + by * dvy_dy) +
+                    bz * (bx * dvz_dx + by * dvz_dy)) * ib2;
+        bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy) +
+                    by * (vx * dvy_dx + vy * dvy_dy) +
+                    bz * (vx * dvz_dx + vy * dvz_dy)) * ib;
+    }
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
     double dp_dt = s->p * acc_rate;
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
-    const double div_bnorm = -((bx * db_dx + by * db_dy) * ib2);
+    const double div_bnorm = c->sph ? -((bx * db_dx + by * db_dy * g.ir) * ib2)
+                                    : -((bx * db_dx + by * db_dy) * ib2);
     double dmu_dt, duu, duu_du;
     calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
-    if (!fixed_dt) ft_time_step(c, s, kap, 2, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    if (!fixed_dt) ft_time_step(c, s, kap, 2, cs, &g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s->dt);
     double r[4];
     push_noise(c, s, r);
-    const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
-    const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
-    const double skperp = kap[K_SKPERP];
-    const double dX = dx_dt * s->dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
-    const double dY = dy_dt * s->dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+    double dX, dY;
+    if (c->sph) {
+        double nx, ny;
+        spherical_noise_2d(kap, &g, r[0], r[1], sdt, &nx, &ny);
+        dX = dx_dt * s->dt + nx;
+        dY = dy_dt * s->dt + ny;
+    } else {
+        const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
+        const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
+        const double skperp = kap[K_SKPERP];
+        dX = dx_dt * s->dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
+        dY = dy_dt * s->dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+    }
     const double dZ = dz_dt * s->dt;
     push_ft_tail(c, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
     d[2] = 0.0;   /* deltaz is local to push_particle_2d_ft, as in push_2d */
 }
 
-/* push_particle_3d_ft, Cartesian uniform grid: particle_module.f90:4930-5324. */
+/* push_particle_3d_ft: particle_module.f90:4930-5324, Cartesian and
+ * spherical.  The spherical position noise draws a third number (ran3);
+ * it comes from the push's extra Philox block. */
 static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *aux,
-                       const double *kap, int fixed_dt, double d[6])
+                       const double *kap, const cell_size *cs, int fixed_dt, double d[6])
 {
     const orc_params *pr = c->pr;
     const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
@@ -842,6 +1244,8 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
     const double bxyn = sqrt(bxn * bxn + byn * byn);
     const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
+    sph_terms g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (c->sph) g = spherical_terms(s);
     const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
     const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
     const double dbz_dx = f[26], dbz_dy = f[27], dbz_dz = f[28];
@@ -852,16 +1256,34 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double mu2 = s->mu * s->mu;
     const double muf1 = 0.5 * (1.0 - mu2);
     const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
-    const double kx = bx * dbx_dx + by * dbx_dy + bz * dbx_dz;
-    const double ky = bx * dby_dx + by * dby_dy + bz * dby_dz;
-    const double kz = bx * dbz_dx + by * dbz_dy + bz * dbz_dz;
-    const double bdot_curvb = bx * (dbz_dy - dby_dz) + by * (dbx_dz - dbz_dx) + bz * (dby_dx - dbx_dy);
-    const double vdx = vdp * (muf1 * (by * db_dz - bz * db_dy) * ib2 +
-                              mu2 * (by * kz - bz * ky) * ib3 + muf1 * bx * bdot_curvb * ib3);
-    const double vdy = vdp * (muf1 * (bz * db_dx - bx * db_dz) * ib2 +
-                              mu2 * (bz * kx - bx * kz) * ib3 + muf1 * by * bdot_curvb * ib3);
-    const double vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 +
-                              mu2 * (bx * ky - by * kx) * ib3 + muf1 * bz * bdot_curvb * ib3);
+    double kx, ky, kz, bdot_curvb, vdx, vdy, vdz;
+    if (c->sph) {
+        const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
+        const double gbr = db_dx, gbt = db_dy * ir, gbp = db_dz * ir * ist;
+        kx = bx * dbx_dx + ir * (by * dbx_dy + bz * dbx_dz * ist - (by * by + bz * bz));
+        ky = bx * dby_dx + ir * (by * dby_dy + bz * dby_dz * ist + (bx * by - cot * (bz * bz)));
+        kz = bx * dbz_dx + ir * (by * dbz_dy + bz * dbz_dz * ist + (bx * bz + cot * by * bz));
+        bdot_curvb = bx * (dbz_dy + cot * bz - dby_dz * ist) * ir +
+                     by * (dbx_dz * ist * ir - dbz_dx - bz * ir) +
+                     bz * (dby_dx + by * ir - dbx_dy * ir);
+        vdx = vdp * (muf1 * (by * gbp - bz * gbt) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                     muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * gbr - bx * gbp) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                     muf1 * by * bdot_curvb * ib3);
+        vdz = vdp * (muf1 * (bx * gbt - by * gbr) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                     muf1 * bz * bdot_curvb * ib3);
+    } else {
+        kx = bx * dbx_dx + by * dbx_dy + bz * dbx_dz;
+        ky = bx * dby_dx + by * dby_dy + bz * dby_dz;
+        kz = bx * dbz_dx + by * dbz_dy + bz * dbz_dz;
+        bdot_curvb = bx * (dbz_dy - dby_dz) + by * (dbx_dz - dbz_dx) + bz * (dby_dx - dbx_dy);
+        vdx = vdp * (muf1 * (by * db_dz - bz * db_dy) * ib2 +
+                     mu2 * (by * kz - bz * ky) * ib3 + muf1 * bx * bdot_curvb * ib3);
+        vdy = vdp * (muf1 * (bz * db_dx - bx * db_dz) * ib2 +
+                     mu2 * (bz * kx - bx * kz) * ib3 + muf1 * by * bdot_curvb * ib3);
+        vdz = vdp * (muf1 * (bx * db_dy - by * db_dx) * ib2 +
+                     mu2 * (bx * ky - by * kx) * ib3 + muf1 * bz * bdot_curvb * ib3);
+    }
     double vbx = s->v * s->mu * ib;
     const double vby = vbx * by;
     const double vbz = vbx * bz;
@@ -869,32 +1291,70 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     const double dvx_dx = f[8], dvx_dy = f[9], dvx_dz = f[10];
     const double dvy_dx = f[11], dvy_dy = f[12], dvy_dz = f[13];
     const double dvz_dx = f[14], dvz_dy = f[15], dvz_dz = f[16];
-    const double dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
-    const double dy_dt = vy + vby + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
-    const double dz_dt = vz + vbz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
-    const double divv = dvx_dx + dvy_dy + dvz_dz;
-    const double bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy + bz * dvx_dz) +
-                             by * (bx * dvy_dx + by * dvy_dy + bz * dvy_dz) +
-                             bz * (bx * dvz_dx + by * dvz_dy + bz * dvz_dz)) * ib2;
-    const double bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy + vz * dvx_dz) +
-                             by * (vx * dvy_dx + vy * dvy_dy + vz * dvy_dz) +
-                             bz * (vx * dvz_dx + vy * dvz_dy + vz * dvz_dz)) * ib;
+    double dx_dt, dy_dt, dz_dt, divv, bb_gradv, bv_gradv;
+    if (c->sph) {
+        const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
+        dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] +
+                (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * g.ctheta * ist +
+                 kap[K_DKXZ_DZ] * ist) * ir;
+        dy_dt = (vy + vby + vdy + kap[K_DKXY_DX]) * ir +
+                (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * g.ctheta * ist +
+                 kap[K_DKYZ_DZ] * ist) * g.ir2;
+        dz_dt = (vz + vbz + vdz + kap[K_DKXZ_DX]) * ist * ir +
+                (kap[K_KXZ] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ] * ist) * ist * g.ir2;
+        divv = dvx_dx + (2.0 * vx + dvy_dy + vy * cot + dvz_dz * ist) * ir;
+        const double dtmp = ist * ir;
+        bb_gradv = (bx * bx * dvx_dx + bx * by * dvx_dy * ir + bx * bz * dvx_dz * dtmp -
+                    bx * (by * vy + bz * vz) * ir +
+                    by * bx * dvy_dx + by * by * dvy_dy * ir + by * bz * dvy_dz * dtmp +
+                    by * (by * vx - cot * bz * vz) * ir +
+                    bz * bx * dvz_dx + bz * by * dvz_dy * ir + bz * bz * dvz_dz * dtmp +
+                    (bz * bz) * (vx + cot * vy) * ir) * ib2;
+        bv_gradv = (bx * vx * dvx_dx + bx * vy * dvx_dy * ir + bx * vz * dvx_dz * dtmp -
+                    bx * (vy * vy + vz * vz) * ir +
+                    by * vx * dvy_dx + by * vy * dvy_dy * ir + by * vz * dvy_dz * dtmp +
+                    by * (vy * vx - cot * vz * vz) * ir +
+                    bz * vx * dvz_dx + bz * vy * dvz_dy * ir + bz * vz * dvz_dz * dtmp +
+                    bz * vz * (vx + cot * vy) * ir) * ib;
+    } else {
+        dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] + kap[K_DKXY_DY] + kap[K_DKXZ_DZ];
+        dy_dt = vy + vby + vdy + kap[K_DKXY_DX] + kap[K_DKYY_DY] + kap[K_DKYZ_DZ];
+        dz_dt = vz + vbz + vdz + kap[K_DKXZ_DX] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ];
+        divv = dvx_dx + dvy_dy + dvz_dz;
+        bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy + bz * dvx_dz) +
+                    by * (bx * dvy_dx + by * dvy_dy + bz * dvy_dz) +
+                    bz * (bx * dvz_dx + by * dvz_dy + bz * dvz_dz)) * ib2;
+        bv_gradv = (bx * (vx * dvx_dx + vy * dvx_dy + vz * dvx_dz) +
+                    by * (vx * dvy_dx + vy * dvy_dy + vz * dvy_dz) +
+                    bz * (vx * dvz_dx + vy * dvz_dy + vz * dvz_dz)) * ib;
+    }
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s->mu * bv_gradv / s->v);
     double dp_dt = s->p * acc_rate;
     const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
-    const double div_bnorm = -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
+    const double div_bnorm =
+        c->sph ? -((bx * db_dx + by * db_dy * g.ir + bz * db_dz * g.ir * g.istheta) * ib2)
+               : -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
     double dmu_dt, duu, duu_du;
     calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
-    if (!fixed_dt) ft_time_step(c, s, kap, 3, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    if (!fixed_dt) ft_time_step(c, s, kap, 3, cs, &g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s->dt);
-    double r[4];
-    push_noise(c, s, r);
-    const double skperp = kap[K_SKPERP];
-    const double dX = dx_dt * s->dt +
-        (-(bxn * bzn * skperp * ibxyn * r[0]) - byn * skperp * ibxyn * r[1]) * sdt;
-    const double dY = dy_dt * s->dt +
-        (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
-    const double dZ = dz_dt * s->dt + bxyn * skperp * r[0] * sdt;
+    double r[6];
+    push_noise_n(c, s, r, c->sph);
+    double dX, dY, dZ;
+    if (c->sph) {
+        double q[6];
+        spherical_noise_3d(kap, &g, 1, q);
+        dX = dx_dt * s->dt + (q[0] * r[0] + q[1] * r[1] + q[2] * r[4]) * sdt;
+        dY = dy_dt * s->dt + (q[3] * r[1] + q[4] * r[4]) * sdt;
+        dZ = dz_dt * s->dt + q[5] * r[4] * sdt;
+    } else {
+        const double skperp = kap[K_SKPERP];
+        dX = dx_dt * s->dt +
+            (-(bxn * bzn * skperp * ibxyn * r[0]) - byn * skperp * ibxyn * r[1]) * sdt;
+        dY = dy_dt * s->dt +
+            (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
+        dZ = dz_dt * s->dt + bxyn * skperp * r[0] * sdt;
+    }
     push_ft_tail(c, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
@@ -946,14 +1406,28 @@ static void check_negp_or_boundary(const mover_ctx *c, ptl_state *s, thread_acc 
  * interp_fields, kappa, push (the body at particle_module.f90:1615-1703). */
 static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
 {
-    const double px = (s->x - c->xmin) / c->dx;
-    const double py = (s->y - c->ymin) / c->dy;
-    const double pz = (s->z - c->zmin) / c->dz;
     const double rt = (s->t - c->t0) / c->dtf;
     int32_t pos[3];
     double w[8], f[32], kap[22], aux[16];
     const double *ap = NULL;
-    orc_get_interp_paramters(c->ndim, px, py, pz, pos, w);
+    cell_size cs = {c->dx, c->dy, c->dz};
+    if (c->sph || c->nonuni) {
+        orc_grid_interp_paramters(c->pr, NULL, s->x, s->y, s->z, pos, w);
+        if (c->nonuni) {
+            /* the pushes search the cell again (:3404-3407, :4693-4699) */
+            const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
+            const int ix = grid_count(0, s->x) - 2, iy = grid_count(1, s->y) - 2;
+            cs.dxm = X[ix + 2] - X[ix + 1];
+            cs.dym = Y[iy + 2] - Y[iy + 1];
+            if (c->ndim == 3) {
+                const int iz = grid_count(2, s->z) - 2;
+                cs.dzm = Z[iz + 2] - Z[iz + 1];
+            }
+        }
+    } else {
+        orc_get_interp_paramters(c->ndim, (s->x - c->xmin) / c->dx, (s->y - c->ymin) / c->dy,
+                                 (s->z - c->zmin) / c->dz, pos, w);
+    }
     orc_interp_fields(c->f1, c->f2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, f);
     if (c->aux1 && (c->pr->deltab_flag || c->pr->correlation_flag)) {
         orc_interp_aux(c->aux1, c->aux2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, aux);
@@ -961,11 +1435,11 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
     }
     orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, ap, kap);
     if (c->pr->focused_transport) {
-        if (c->ndim == 2) push_2d_ft(c, s, f, ap, kap, fixed_dt, d);
-        else push_3d_ft(c, s, f, ap, kap, fixed_dt, d);
+        if (c->ndim == 2) push_2d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
+        else push_3d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
     } else {
-        if (c->ndim == 2) push_2d(c, s, f, kap, fixed_dt, d);
-        else push_3d(c, s, f, kap, fixed_dt, d);
+        if (c->ndim == 2) push_2d(c, s, f, kap, &cs, fixed_dt, d);
+        else push_3d(c, s, f, kap, &cs, fixed_dt, d);
     }
 }
 
@@ -1133,6 +1607,23 @@ static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *
     c->xmin1 = c->xmin - c->dx * 0.5; c->xmax1 = xmax + c->dx * 0.5;
     c->ymin1 = c->ymin - c->dy * 0.5; c->ymax1 = ymax + c->dy * 0.5;
     c->zmin1 = c->zmin - c->dz * 0.5; c->zmax1 = zmax + c->dz * 0.5;
+    c->sph = pr->spherical_coord != 0;
+    c->nonuni = pr->nonuniform_grid != 0;
+    if (c->nonuni) {
+        /* :1535-1546: the half cells beyond the box are those of the first
+         * and last cells; xpos_local(i) is X[i + 1].  The z extension only
+         * matters in 3D. */
+        const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
+        const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
+        c->xmin1 = c->xmin - (X[3] - X[2]) * 0.5;
+        c->xmax1 = xmax + (X[nx + 2] - X[nx + 1]) * 0.5;
+        c->ymin1 = c->ymin - (Y[3] - Y[2]) * 0.5;
+        c->ymax1 = ymax + (Y[ny + 2] - Y[ny + 1]) * 0.5;
+        if (pr->ndim == 3) {
+            c->zmin1 = c->zmin - (Z[3] - Z[2]) * 0.5;
+            c->zmax1 = zmax + (Z[nz + 2] - Z[nz + 1]) * 0.5;
+        }
+    }
     c->cfg_xmin = cfg->xmin; c->cfg_ymin = cfg->ymin; c->cfg_zmin = cfg->zmin;
     c->cfg_lx = cfg->lx; c->cfg_ly = cfg->ly; c->cfg_lz = cfg->lz;
     /* set_dt_min_max: particle_module.f90:5519-5524. */
@@ -1374,8 +1865,30 @@ int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *P, int64
 /* _rho (:1356-1468), and the cell counts get_ncells_large_*                 */
 /* (mhd_data_parallel.f90:2211-2498) on one rank, uniform grid.             */
 /* ------------------------------------------------------------------------ */
-static double large_quantity(int quantity, int ndim, const double f[32])
+static double large_quantity(int quantity, int ndim, int sph, double x, double y,
+                             const double f[32])
 {
+    if (sph) {
+        /* the spherical forms of :866-890, :1030-1043, :1306-1316 */
+        if (quantity == 0) return fabs(f[23] + (f[5] - f[21]) / x);
+        if (quantity == 1) {
+            const double ctheta = cos(y), stheta = sin(y), r = x;
+            const double t1 = (ctheta * f[6] + stheta * f[27] - f[25]) / (r * stheta);
+            const double t2 = (f[22] / stheta - f[6] - r * f[26]) / r;
+            const double t3 = (f[5] + r * f[23] - f[21]) / r;
+            return sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+        }
+        if (quantity == 2) {
+            double d = f[8] + 2.0 * f[0] / x;
+            if (ndim > 1) {
+                const double ctheta = cos(y), istheta = 1.0 / sin(y);
+                d = d + (f[12] + f[1] * ctheta * istheta) / x;
+                if (ndim > 2) d = d + f[2] * istheta / x;   /* vz, as the reference */
+            }
+            return -d;
+        }
+        return f[3];
+    }
     if (quantity == 0) return fabs(f[23] - f[21]);
     if (quantity == 1) {
         const double a = f[25] - f[27], b = f[26] - f[22], c = f[21] - f[23];
@@ -1390,6 +1903,17 @@ static double large_quantity(int quantity, int ndim, const double f[32])
     return f[3];
 }
 
+/* xpos_local(i) for the count loops: the grid's node i + 1 (i 1-based
+ * interior index), or mhd_config's uniform positions. */
+static double node_position(const orc_params *pr, const orc_mhd_config *cfg, int axis, int i)
+{
+    if ((pr->spherical_coord || pr->nonuniform_grid) && g_grid.pos[axis])
+        return g_grid.pos[axis][i + 1];
+    const double d = axis == 0 ? cfg->dx : axis == 1 ? cfg->dy : cfg->dz;
+    const double o = axis == 0 ? cfg->xmin : axis == 1 ? cfg->ymin : cfg->zmin;
+    return d * (double)(i - 1) + o;
+}
+
 int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, const float *full,
                               const float *aux, int quantity, double qmin, const double box[6])
 {
@@ -1397,19 +1921,47 @@ int64_t orc_count_cells_large(const orc_params *pr, const orc_mhd_config *cfg, c
     const int nx = cfg->nx, ny = cfg->ny, nz = (ndim == 3) ? cfg->nz : 1;
     const size_t nxg = (size_t)nx + 4, nyg = (size_t)ny + 4;
     int64_t count = 0;
+    const int sph = pr->spherical_coord != 0;
     for (int iz = 1; iz <= nz; ++iz) {
-        const int inz = (ndim > 2) ? (cfg->dz * (double)(iz - 1) + cfg->zmin > box[2] &&
-                                      cfg->dz * (double)(iz - 1) + cfg->zmin < box[5]) : 1;
+        const double zp = node_position(pr, cfg, 2, iz);
+        const int inz = (ndim > 2) ? (zp > box[2] && zp < box[5]) : 1;
         for (int iy = 1; iy <= ny; ++iy) {
-            const double yp = cfg->dy * (double)(iy - 1) + cfg->ymin;
+            const double yp = node_position(pr, cfg, 1, iy);
             const int iny = (ndim > 1) ? (yp > box[1] && yp < box[4]) : 1;
             for (int ix = 1; ix <= nx; ++ix) {
-                const double xp = cfg->dx * (double)(ix - 1) + cfg->xmin;
+                const double xp = node_position(pr, cfg, 0, ix);
                 if (!(inz && iny && xp > box[0] && xp < box[3])) continue;
                 const size_t cz = (ndim == 3) ? (size_t)iz + 1 : 0;
                 const float *r = full + 32 * ((size_t)ix + 1 + nxg * ((size_t)iy + 1 + nyg * cz));
                 double q;
-                if (quantity == 0) {
+                if (sph && quantity == 0) {
+                    /* get_ncells_large_jz (:2226-2234): (by - dbx_dy) in single */
+                    const float t = r[5] - r[21];
+                    q = fabs((double)r[23] + (double)t / xp);
+                } else if (sph && quantity == 1) {
+                    /* get_ncells_large_absj (:2285-2303) */
+                    const double stheta = sin(yp), ctheta = cos(yp);
+                    const double t1 = (ctheta * (double)r[6] + stheta * (double)r[27] -
+                                       (double)r[25]) / (xp * stheta);
+                    const double t2 = ((double)r[22] / stheta - (double)r[6] -
+                                       xp * (double)r[26]) / xp;
+                    const double t3 = ((double)r[5] - xp * (double)r[23] - (double)r[21]) / xp;
+                    q = sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+                } else if (sph && quantity == 2) {
+                    /* get_ncells_large_divv (:2404-2420).  ctheta and
+                     * istheta are re-allocated over all ny + 4 nodes, so row
+                     * iy reads node iy - 2; the dvz/dz term is added from
+                     * ndim > 1; 2.0 * vx is single precision. */
+                    const double yq = g_grid.pos[1] ? g_grid.pos[1][iy - 1] : 0.0;
+                    const double ctheta = cos(yq), istheta = 1.0 / sin(yq);
+                    const float vx2 = 2.0f * r[0];
+                    double d = (double)r[8] + (double)vx2 / xp;
+                    if (ndim > 1) {
+                        d = d + ((double)r[12] + (double)r[1] * ctheta * istheta) / xp;
+                        d = d + (double)r[16] * istheta / xp;
+                    }
+                    q = -d;
+                } else if (quantity == 0) {
                     q = (double)fabsf(r[23] - r[21]);
                 } else if (quantity == 1) {
                     const float t1 = r[25] - r[27], t2 = r[26] - r[22], t3 = r[21] - r[23];
@@ -1465,15 +2017,14 @@ int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, con
                 z <= box[5]) {
                 int32_t pos[3];
                 double w[8], f[32];
-                orc_get_interp_paramters(ndim, (x - cfg->xmin) / cfg->dx, (y - cfg->ymin) / cfg->dy,
-                                         (z - cfg->zmin) / cfg->dz, pos, w);
+                orc_grid_interp_paramters(pr, cfg, x, y, z, pos, w);
                 if (quantity == 4) {
                     double a16[16];
                     orc_interp_aux(aux, aux, 0, ndim, nxg, nyg, pos, w, 0.0, a16);
                     q = a16[0];
                 } else {
                     orc_interp_fields(full, full, 0, ndim, nxg, nyg, pos, w, 0.0, f);
-                    q = large_quantity(quantity, ndim, f);
+                    q = large_quantity(quantity, ndim, pr->spherical_coord != 0, x, y, f);
                 }
             } else {
                 q = rho ? 0.0 : -3.0;
@@ -1545,11 +2096,16 @@ void orc_quick_check(const orc_particles *P, int64_t n, double out[4])
 /* One local distribution of calc_particle_distributions
  * (diagnostics.f90:782-878) on one rank, uniform grid: flocal(imu, ip, ix,
  * iy, iz), imu fastest; 0 < ip < npbins as in the reference. */
-void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmin, double pmax,
+void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
+                                 int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,
                                  const orc_particles *P, int64_t n, uint64_t *counts,
                                  uint64_t *whi, uint64_t *wlo, double *flocal)
 {
+    /* spherical: the local weight is w / r^2 (/ sin(theta) from 2D on),
+     * diagnostics.f90:765-772; nonuniform: the spatial bin is
+     * (binarySearch_R(xpos_local, x) - 1) / rx + 1 (:785-793), which counts
+     * from the first ghost node. */
     const int nz = ndim == 3 ? cfg->nz : 1;
     const int nrx = (cfg->nx + rx - 1) / rx, nry = (cfg->ny + ry - 1) / ry, nrz = (nz + rz - 1) / rz;
     const double dxd = cfg->lx / nrx, dyd = cfg->ly / nry, dzd = cfg->lz / nrz;
@@ -1559,9 +2115,17 @@ void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmi
     const size_t nb = (size_t)nmu * npbins * nrx * nry * nrz;
     for (size_t b = 0; b < nb; ++b) { counts[b] = 0; whi[b] = 0; wlo[b] = 0; }
     for (int64_t i = 0; i < n; ++i) {
-        const int ix = (int)floor((P->x[i] - cfg->xmin) / dxd) + 1;
-        const int iy = (int)floor((P->y[i] - cfg->ymin) / dyd) + 1;
-        const int iz = (int)floor((P->z[i] - cfg->zmin) / dzd) + 1;
+        int ix, iy, iz;
+        if (nonuniform) {
+            ix = (orc_binary_search(g_grid.pos[0], g_grid.n[0], P->x[i]) - 1) / rx + 1;
+            iy = (orc_binary_search(g_grid.pos[1], g_grid.n[1], P->y[i]) - 1) / ry + 1;
+            iz = (ndim == 3) ? (orc_binary_search(g_grid.pos[2], g_grid.n[2], P->z[i]) - 1) / rz + 1
+                             : (int)floor((P->z[i] - cfg->zmin) / dzd) + 1;
+        } else {
+            ix = (int)floor((P->x[i] - cfg->xmin) / dxd) + 1;
+            iy = (int)floor((P->y[i] - cfg->ymin) / dyd) + 1;
+            iz = (int)floor((P->z[i] - cfg->zmin) / dzd) + 1;
+        }
         const int ip = (int)floor((log10(P->p[i]) - pmin_log) / dp_log) + 1;
         const int imu = (int)floor((P->mu[i] + 1.0) / dmu) + 1;
         if (ix < 1 || ix > nrx || iy < 1 || iy > nry || iz < 1 || iz > nrz) continue;
@@ -1569,7 +2133,12 @@ void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmi
         const size_t e = (size_t)(imu - 1) + (size_t)nmu * ((size_t)(ip - 1) + (size_t)npbins *
                          ((size_t)(ix - 1) + (size_t)nrx * ((size_t)(iy - 1) + (size_t)nry * (iz - 1))));
         counts[e] += 1;
-        orc_fixed_add(&whi[e], &wlo[e], P->weight[i]);
+        double w = P->weight[i];
+        if (spherical) {
+            w = w / (P->x[i] * P->x[i]);
+            if (ndim >= 2) w = w / sin(P->y[i]);
+        }
+        orc_fixed_add(&whi[e], &wlo[e], w);
     }
     for (size_t b = 0; b < nb; ++b) flocal[b] = orc_fixed_to_double(whi[b], wlo[b]);
 }

@@ -58,6 +58,9 @@ typedef struct orc_params {
     int32_t dpp_shear, weak_scattering;
     double tau0;
     int32_t deltab_flag, correlation_flag;   /* set_flags_params (:285-300) */
+    /* set_mhd_grid_type (mhd_config.f90:179-186); with either set, the node
+     * positions come from orc_set_grid_positions. */
+    int32_t spherical_coord, nonuniform_grid;
 } orc_params;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the
@@ -90,6 +93,31 @@ double orc_fixed_to_double(uint64_t hi, uint64_t lo);
 
 void orc_calc_fields_gradients(float *farray, int ndim, int nxg, int nyg, int nzg,
                                double dx, double dy, double dz);
+
+/* Node positions of the ghost-padded grid (xpos_global on one rank,
+ * mhd_data_parallel.f90:2051-2190): nxg x positions, nyg y positions (2D and
+ * 3D) and nzg z positions (3D); y and z may be NULL in fewer dimensions.
+ * The oracle keeps copies; they serve every routine below while
+ * spherical_coord or nonuniform_grid is set. */
+void orc_set_grid_positions(const double *xpos, const double *ypos, const double *zpos,
+                            int nxg, int nyg, int nzg);
+/* calc_global_grid_positions (:2131-2148): pos[j] = d * (j - 2) + xmin. */
+void orc_uniform_grid_positions(int n, double d, double xmin, double *pos);
+/* binarySearch_R (particle_module.f90:680-698): the 1-based index of the
+ * last node <= v, i.e. the number of nodes <= v. */
+int orc_binary_search(const double *a, int n, double v);
+/* calc_fields_gradients_nonuniform (mhd_data_parallel.f90:612-764) and the
+ * fluctuation-record variants (:880-1008 and siblings) with the inverse
+ * spans idxh_grid of set_local_grid_positions (:2153-2190). */
+void orc_calc_fields_gradients_nonuniform(float *farray, int ndim, int nxg, int nyg, int nzg);
+void orc_calc_aux_gradients_nonuniform(float *aux, int ndim, int nxg, int nyg, int nzg);
+/* Interpolation corner (pos, Fortran convention as orc_get_interp_paramters)
+ * and weights for a position under the grid type of pr:
+ * get_interp_paramters_spherical (particle_module.f90:705-775) in spherical
+ * coordinates; on a non-uniform Cartesian grid the cell found by
+ * binarySearch_R with the fractional offset of :1620-1625. */
+void orc_grid_interp_paramters(const orc_params *pr, const orc_mhd_config *cfg, double x,
+                               double y, double z, int32_t pos[3], double weights[8]);
 void orc_get_interp_paramters(int ndim, double px, double py, double pz,
                               int32_t pos[3], double weights[8]);
 void orc_interp_fields(const float *f1, const float *f2, int time_interp, int ndim,
@@ -144,7 +172,8 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
 void orc_quick_check(const orc_particles *ptl, int64_t n, double out[4]);
 void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *counts,
                                uint64_t *whi, uint64_t *wlo);
-void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, double pmin, double pmax,
+void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
+                                 int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,
                                  const orc_particles *ptl, int64_t n, uint64_t *counts,
                                  uint64_t *whi, uint64_t *wlo, double *flocal);

@@ -40,6 +40,7 @@ class OrcParams(C.Structure):
         ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("dpp_wave", i32),
         ("duu0", d), ("kperp_kpara", d), ("dpp_shear", i32), ("weak_scattering", i32),
         ("tau0", d), ("deltab_flag", i32), ("correlation_flag", i32),
+        ("spherical_coord", i32), ("nonuniform_grid", i32),
     ]
 
 # Mover arguments of the reference carried in OrcParams rather than in the
@@ -134,10 +135,21 @@ def load() -> C.CDLL:
                                             P(OrcCounters)]
         lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
         lib.orc_set_escaped_histogram.argtypes = [C.c_int, d, d, P(u64), P(u64), P(u64)]
-        lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, d, d, C.c_int,
+        lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, C.c_int, C.c_int,
+                                                    d, d, C.c_int,
                                                     C.c_int, C.c_int, C.c_int, C.c_int,
                                                     P(OrcParticles), i64, P(u64), P(u64), P(u64),
                                                     P(d)]
+        lib.orc_set_grid_positions.argtypes = [P(d), P(d), P(d), C.c_int, C.c_int, C.c_int]
+        lib.orc_uniform_grid_positions.argtypes = [C.c_int, d, d, P(d)]
+        lib.orc_binary_search.restype = C.c_int
+        lib.orc_binary_search.argtypes = [P(d), C.c_int, d]
+        lib.orc_calc_fields_gradients_nonuniform.argtypes = [P(C.c_float), C.c_int, C.c_int,
+                                                             C.c_int, C.c_int]
+        lib.orc_calc_aux_gradients_nonuniform.argtypes = [P(C.c_float), C.c_int, C.c_int,
+                                                          C.c_int, C.c_int]
+        lib.orc_grid_interp_paramters.argtypes = [P(OrcParams), P(OrcMhdConfig), d, d, d, P(i32),
+                                                  P(d)]
         _lib = lib
     return _lib
 
@@ -185,18 +197,53 @@ class Particles:
         return {k: v[:self.n].copy() for k, v in self.a.items()}
 
 
-def full_fields(frame8: np.ndarray, ndim: int, cfg) -> np.ndarray:
-    """32-variable array with the reference's gradients from an 8-var frame."""
+def full_fields(frame8: np.ndarray, ndim: int, cfg, nonuniform: bool = False) -> np.ndarray:
+    """32-variable array with the reference's gradients from an 8-var frame
+    (calc_fields_gradients_nonuniform on the positions of set_grid_positions
+    when nonuniform)."""
     nzg, nyg, nxg, _ = frame8.shape
     full = np.zeros((nzg, nyg, nxg, 32), dtype=np.float32)
     full[..., :8] = frame8
     lib = load()
-    lib.orc_calc_fields_gradients(full.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
-                                  cfg.dx, cfg.dy, cfg.dz)
+    if nonuniform:
+        lib.orc_calc_fields_gradients_nonuniform(full.ctypes.data_as(P(C.c_float)), ndim, nxg,
+                                                 nyg, nzg)
+    else:
+        lib.orc_calc_fields_gradients(full.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
+                                      cfg.dx, cfg.dy, cfg.dz)
     return full
 
 
-def aux_fields(db2_slab, db2_2d, lc_slab, lc_2d, ndim: int, cfg) -> np.ndarray:
+def set_grid_positions(xpos, ypos=None, zpos=None) -> None:
+    """Node positions (ghost nodes included) for spherical and non-uniform
+    grids; None clears an axis."""
+    keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (xpos, ypos, zpos)]
+    ptrs = [None if a is None else a.ctypes.data_as(P(d)) for a in keep]
+    ns = [0 if a is None else len(a) for a in keep]
+    load().orc_set_grid_positions(*ptrs, *ns)
+
+
+def uniform_grid_positions(n: int, step: float, origin: float) -> np.ndarray:
+    """calc_global_grid_positions: step * (j - 2) + origin for j = 0..n-1."""
+    out = np.zeros(n, np.float64)
+    load().orc_uniform_grid_positions(n, step, origin, out.ctypes.data_as(P(d)))
+    return out
+
+
+def binary_search(a, v: float) -> int:
+    a = np.ascontiguousarray(a, np.float64)
+    return load().orc_binary_search(a.ctypes.data_as(P(d)), len(a), v)
+
+
+def grid_interp_paramters(params: OrcParams, cfg: OrcMhdConfig, x: float, y: float, z: float):
+    pos = (i32 * 3)()
+    w = (d * 8)()
+    load().orc_grid_interp_paramters(C.byref(params), C.byref(cfg), x, y, z, pos, w)
+    return list(pos), np.array(list(w))
+
+
+def aux_fields(db2_slab, db2_2d, lc_slab, lc_2d, ndim: int, cfg,
+               nonuniform: bool = False) -> np.ndarray:
     """16-float fluctuation records {db2_slab, db2_2d, lc_slab, lc_2d} x
     {value, d/dx, d/dy, d/dz} from four (nzg, nyg, nxg) arrays (None: the
     reference's initial value 1), gradients as the reference computes them."""
@@ -206,8 +253,12 @@ def aux_fields(db2_slab, db2_2d, lc_slab, lc_2d, ndim: int, cfg) -> np.ndarray:
         if a is not None:
             aux[..., 4 * g] = a
     nzg, nyg, nxg = shape
-    load().orc_calc_aux_gradients(aux.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
-                                  cfg.dx, cfg.dy, cfg.dz)
+    if nonuniform:
+        load().orc_calc_aux_gradients_nonuniform(aux.ctypes.data_as(P(C.c_float)), ndim, nxg,
+                                                 nyg, nzg)
+    else:
+        load().orc_calc_aux_gradients(aux.ctypes.data_as(P(C.c_float)), ndim, nxg, nyg, nzg,
+                                      cfg.dx, cfg.dy, cfg.dz)
     return aux
 
 
@@ -333,14 +384,16 @@ class EscapedHistogram:
 
 
 def local_distribution(cfg: OrcMhdConfig, ndim: int, parts: Particles, pmin: float, pmax: float,
-                       npbins: int, nmu: int = 1, rx: int = 1, ry: int = 1, rz: int = 1):
+                       npbins: int, nmu: int = 1, rx: int = 1, ry: int = 1, rz: int = 1,
+                       spherical: bool = False, nonuniform: bool = False):
     nz = cfg.nz if ndim == 3 else 1
     nb = nmu * npbins * ((cfg.nx + rx - 1) // rx) * ((cfg.ny + ry - 1) // ry) * ((nz + rz - 1) // rz)
     counts = np.zeros(nb, np.uint64)
     whi = np.zeros(nb, np.uint64)
     wlo = np.zeros(nb, np.uint64)
     f = np.zeros(nb, np.float64)
-    load().orc_calc_local_distribution(C.byref(cfg), ndim, pmin, pmax, npbins, nmu, rx, ry, rz,
+    load().orc_calc_local_distribution(C.byref(cfg), ndim, int(spherical), int(nonuniform),
+                                       pmin, pmax, npbins, nmu, rx, ry, rz,
                                        C.byref(parts.c), parts.n, counts.ctypes.data_as(P(u64)),
                                        whi.ctypes.data_as(P(u64)), wlo.ctypes.data_as(P(u64)),
                                        f.ctypes.data_as(P(d)))
