@@ -84,10 +84,13 @@ typedef struct gpat_params {
      * shear (set_dpp_params, particle_module.f90:255-272); deltab_flag /
      * correlation_flag: spatially dependent turbulence variance and
      * correlation length (set_flags_params :285-300, inputs through
-     * gpat_read_magnetic_fluctuation / gpat_read_correlation_length).  These
-     * four need GPAT_PREC_FP64.  Options of the reference that this engine
-     * rejects with GPAT_ERR_UNSUPPORTED when non-zero: include_3rd_dim,
-     * spherical_coord, nonuniform_grid. */
+     * gpat_read_magnetic_fluctuation / gpat_read_correlation_length);
+     * spherical_coord / nonuniform_grid: the grid type of set_mhd_grid_type
+     * (mhd_config.f90:179-186; x = r, y = theta, z = phi in spherical
+     * coordinates; node positions through gpat_read_grid_positions or
+     * gpat_set_grid_positions when non-uniform).  These six need
+     * GPAT_PREC_FP64.  include_3rd_dim is rejected with
+     * GPAT_ERR_UNSUPPORTED. */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of
@@ -178,6 +181,21 @@ int gpat_read_correlation_length(gpat_handle_t *h, const char *filename, int var
 int gpat_get_fluctuations(gpat_handle_t *h, int var_flag, float *aux);
 
 int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag);
+/* Node positions of a non-uniform grid (nonuniform_grid = 1), ghost nodes
+ * included: nxg x values, nyg y values (2D, 3D) and nzg z values (3D), each
+ * increasing (xpos_global of read_global_grid_positions,
+ * mhd_data_parallel.f90:2087-2126, which gpat_read_grid_positions restates
+ * on <dir>xpos.dat, ypos.dat, zpos.dat).  They replace the uniform
+ * positions dx (i - 2) + xmin the handle starts with and are used by the
+ * gradients (calc_fields_gradients_nonuniform :612-764 with idxh_grid
+ * :2172-2189), the interpolation, the pushes' cell sizes, the boundary
+ * extension, the large-quantity counts and the local distributions.  Set
+ * them before gpat_calc_fields_gradients.  gpat_get_grid_positions copies
+ * them out (spherical or non-uniform grids). */
+int gpat_set_grid_positions(gpat_handle_t *h, const double *xpos, const double *ypos,
+                            const double *zpos);
+int gpat_read_grid_positions(gpat_handle_t *h, const char *dir_mhd_data);
+int gpat_get_grid_positions(gpat_handle_t *h, double *xpos, double *ypos, double *zpos);
 /* copy_fields (mhd_data_parallel.f90:1920-1926): farray1 = farray2. */
 int gpat_copy_fields(gpat_handle_t *h);
 /* Copies a device field array (32 vars per cell, Fortran order) to the host. */

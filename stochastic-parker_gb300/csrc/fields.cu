@@ -51,10 +51,15 @@ __device__ __forceinline__ float grad_c(float ap, float am, double ih) {
 // Gradients of NVAR variables of records of STRIDE floats (value of v at
 // v * VSTRIDE, its d/dx d/dy d/dz at GBASE + v * GSTEP + axis); the z
 // component only in 3D.  <32, 8, 1, 8, 3>: the field records; <16, 4, 4, 1, 4>:
-// the fluctuation records {db2_slab, db2_2d, lc_slab, lc_2d}.
+// the fluctuation records {db2_slab, db2_2d, lc_slab, lc_2d}.  ihx/ihy/ihz:
+// per-node inverse spans of a non-uniform grid (idxh_grid of
+// set_local_grid_positions, mhd_data_parallel.f90:2153-2190, as used by
+// calc_fields_gradients_nonuniform :612-764), or null for 0.5 / d.
 template <int STRIDE, int NVAR, int VSTRIDE, int GBASE, int GSTEP>
 __global__ void gradients_kernel(float *__restrict__ a, int ndim, int nxg, int nyg, int nzg,
-                                 double idxh, double idyh, double idzh) {
+                                 double idxh, double idyh, double idzh,
+                                 const double *__restrict__ ihx, const double *__restrict__ ihy,
+                                 const double *__restrict__ ihz) {
     const size_t ncells = (size_t)nxg * nyg * nzg;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const size_t sx = STRIDE, sy = STRIDE * (size_t)nxg, sz = STRIDE * (size_t)nxg * nyg;
@@ -63,24 +68,27 @@ __global__ void gradients_kernel(float *__restrict__ a, int ndim, int nxg, int n
         const int j = (int)((c / nxg) % nyg);
         const int k = (int)(c / ((size_t)nxg * nyg));
         float *cell = a + STRIDE * c;
+        const double hx = ihx ? ihx[i] : idxh;
+        const double hy = ihy ? ihy[j] : idyh;
+        const double hz = ihz ? ihz[k] : idzh;
 #pragma unroll
         for (int v = 0; v < NVAR; ++v) {
             const int x = v * VSTRIDE, g = GBASE + v * GSTEP;
             float d;
-            if (i == 0) d = grad_lo(cell[x], cell[x + sx], cell[x + 2 * sx], idxh);
-            else if (i == nxg - 1) d = grad_hi(cell[x], cell[x - sx], cell[x - 2 * sx], idxh);
-            else d = grad_c(cell[x + sx], cell[x - sx], idxh);
+            if (i == 0) d = grad_lo(cell[x], cell[x + sx], cell[x + 2 * sx], hx);
+            else if (i == nxg - 1) d = grad_hi(cell[x], cell[x - sx], cell[x - 2 * sx], hx);
+            else d = grad_c(cell[x + sx], cell[x - sx], hx);
             cell[g] = d;
             if (nyg > 1) {
-                if (j == 0) d = grad_lo(cell[x], cell[x + sy], cell[x + 2 * sy], idyh);
-                else if (j == nyg - 1) d = grad_hi(cell[x], cell[x - sy], cell[x - 2 * sy], idyh);
-                else d = grad_c(cell[x + sy], cell[x - sy], idyh);
+                if (j == 0) d = grad_lo(cell[x], cell[x + sy], cell[x + 2 * sy], hy);
+                else if (j == nyg - 1) d = grad_hi(cell[x], cell[x - sy], cell[x - 2 * sy], hy);
+                else d = grad_c(cell[x + sy], cell[x - sy], hy);
                 cell[g + 1] = d;
             }
             if (nzg > 1 && ndim == 3) {
-                if (k == 0) d = grad_lo(cell[x], cell[x + sz], cell[x + 2 * sz], idzh);
-                else if (k == nzg - 1) d = grad_hi(cell[x], cell[x - sz], cell[x - 2 * sz], idzh);
-                else d = grad_c(cell[x + sz], cell[x - sz], idzh);
+                if (k == 0) d = grad_lo(cell[x], cell[x + sz], cell[x + 2 * sz], hz);
+                else if (k == nzg - 1) d = grad_hi(cell[x], cell[x - sz], cell[x - 2 * sz], hz);
+                else d = grad_c(cell[x + sz], cell[x - sz], hz);
                 cell[g + 2] = d;
             }
         }
@@ -88,24 +96,28 @@ __global__ void gradients_kernel(float *__restrict__ a, int ndim, int nxg, int n
 }
 
 cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg, int nzg,
-                                         double dx, double dy, double dz, cudaStream_t s) {
+                                         double dx, double dy, double dz, cudaStream_t s,
+                                         const double *const *ih) {
     const size_t ncells = (size_t)nxg * nyg * nzg;
     const int threads = 256;
     size_t blocks = (ncells + threads - 1) / threads;
     if (blocks > 65535 * 16) blocks = 65535 * 16;
     gradients_kernel<32, 8, 1, 8, 3><<<(unsigned)blocks, threads, 0, s>>>(
-        full, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz);
+        full, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz, ih ? ih[0] : nullptr,
+        ih ? ih[1] : nullptr, ih ? ih[2] : nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg, double dx,
-                                      double dy, double dz, cudaStream_t s) {
+                                      double dy, double dz, cudaStream_t s,
+                                      const double *const *ih) {
     const size_t ncells = (size_t)nxg * nyg * nzg;
     const int threads = 256;
     size_t blocks = (ncells + threads - 1) / threads;
     if (blocks > 65535 * 16) blocks = 65535 * 16;
     gradients_kernel<16, 4, 4, 1, 4><<<(unsigned)blocks, threads, 0, s>>>(
-        aux, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz);
+        aux, ndim, nxg, nyg, nzg, 0.5 / dx, 0.5 / dy, 0.5 / dz, ih ? ih[0] : nullptr,
+        ih ? ih[1] : nullptr, ih ? ih[2] : nullptr);
     return cudaGetLastError();
 }
 

@@ -29,6 +29,12 @@ struct gpat_handle {
     float *rec[2] = {nullptr, nullptr};
     float *staging = nullptr;
     float *aux[2] = {nullptr, nullptr};   // fluctuation records (deltab / correlation runs)
+    // Node positions of spherical / non-uniform grids (ghost nodes included)
+    // and their inverse spans for the non-uniform gradients, per axis.
+    bool grid = false;
+    std::vector<double> gpos[3];
+    double *dpos[3] = {nullptr, nullptr, nullptr};
+    double *dih[3] = {nullptr, nullptr, nullptr};
     bool fields_set[2] = {false, false};
     bool rec_ready[2] = {false, false};
     // particles (double-buffered SoA)
@@ -206,6 +212,23 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.xmin1 = a.xmin - c.dx * 0.5; a.xmax1 = a.xmax + c.dx * 0.5;
     a.ymin1 = a.ymin - c.dy * 0.5; a.ymax1 = a.ymax + c.dy * 0.5;
     a.zmin1 = a.zmin - c.dz * 0.5; a.zmax1 = a.zmax + c.dz * 0.5;
+    a.spherical = p.spherical_coord ? 1 : 0;
+    a.nonuniform = p.nonuniform_grid ? 1 : 0;
+    a.xpos = h->dpos[0]; a.ypos = h->dpos[1]; a.zpos = h->dpos[2];
+    if (p.nonuniform_grid) {
+        // particle_mover_one_cycle (:1535-1546): the half cells beyond the
+        // box are those of the first and last cells (xpos_local(i) is node
+        // i + 1); the z extension only matters in 3D.
+        const std::vector<double> &X = h->gpos[0], &Y = h->gpos[1], &Z = h->gpos[2];
+        a.xmin1 = a.xmin - (X[3] - X[2]) * 0.5;
+        a.xmax1 = a.xmax + (X[c.nx + 2] - X[c.nx + 1]) * 0.5;
+        a.ymin1 = a.ymin - (Y[3] - Y[2]) * 0.5;
+        a.ymax1 = a.ymax + (Y[c.ny + 2] - Y[c.ny + 1]) * 0.5;
+        if (p.ndim == 3) {
+            a.zmin1 = a.zmin - (Z[3] - Z[2]) * 0.5;
+            a.zmax1 = a.zmax + (Z[c.nz + 2] - Z[c.nz + 1]) * 0.5;
+        }
+    }
     a.cfg_xmin = c.xmin; a.cfg_ymin = c.ymin; a.cfg_zmin = c.zmin;
     a.cfg_lx = c.lx; a.cfg_ly = c.ly; a.cfg_lz = c.lz;
     a.t0 = h->tstamps[mhd_tframe - 1];
@@ -269,6 +292,33 @@ int bin_particles(gpat_handle_t *h) {
     h->n = (int64_t)h->hcnt.nkept;
     h->unsorted = false;
     return GPAT_OK;
+}
+
+// Copies the node positions to the device with their inverse spans
+// idxh_grid (set_local_grid_positions, mhd_data_parallel.f90:2172-2189):
+// 1 / (x[i+1] - x[i-1]) inside, the one-sided spans at the two ends.
+int upload_grid(gpat_handle_t *h) {
+    for (int ax = 0; ax < h->prm.ndim; ++ax) {
+        const std::vector<double> &x = h->gpos[ax];
+        const size_t n = x.size();
+        std::vector<double> ih(n, 0.0);
+        if (n >= 3) {
+            for (size_t i = 1; i + 1 < n; ++i) ih[i] = 1.0 / (x[i + 1] - x[i - 1]);
+            ih[0] = 1.0 / (-(3.0 * x[0]) + 4.0 * x[1] - x[2]);
+            ih[n - 1] = 1.0 / (3.0 * x[n - 1] - 4.0 * x[n - 2] + x[n - 3]);
+        }
+        CK(cudaMemcpyAsync(h->dpos[ax], x.data(), sizeof(double) * n, cudaMemcpyHostToDevice,
+                           h->stream));
+        CK(cudaMemcpyAsync(h->dih[ax], ih.data(), sizeof(double) * n, cudaMemcpyHostToDevice,
+                           h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+// The inverse spans for the non-uniform gradients, or null (uniform 0.5/d).
+const double *const *grad_spans(const gpat_handle_t *h) {
+    return h->prm.nonuniform_grid ? h->dih : nullptr;
 }
 
 int ensure_scratch(gpat_handle_t *h, int64_t n) {
@@ -357,8 +407,9 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     *out = nullptr;
     const gpat_params_t &p = *params;
     if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
-    if (p.include_3rd_dim || p.spherical_coord || p.nonuniform_grid) return GPAT_ERR_UNSUPPORTED;
-    if ((p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag) &&
+    if (p.include_3rd_dim) return GPAT_ERR_UNSUPPORTED;
+    if ((p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag || p.spherical_coord ||
+         p.nonuniform_grid) &&
         p.precision != GPAT_PREC_FP64)
         return GPAT_ERR_UNSUPPORTED;
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
@@ -408,6 +459,23 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
                 return bail(GPAT_ERR_CUDA);
         }
     }
+    // Grid positions (init_grid_positions / set_local_grid_positions,
+    // mhd_data_parallel.f90:2051-2190): the uniform positions until
+    // gpat_set_grid_positions or gpat_read_grid_positions replaces them.
+    if (p.spherical_coord || p.nonuniform_grid) {
+        h->grid = true;
+        const int ng[3] = {h->nxg, h->nyg, h->nzg};
+        const double d[3] = {cfg->dx, cfg->dy, cfg->dz};
+        const double o[3] = {cfg->xmin, cfg->ymin, cfg->zmin};
+        for (int ax = 0; ax < p.ndim; ++ax) {
+            h->gpos[ax].resize(ng[ax]);
+            for (int j = 0; j < ng[ax]; ++j) h->gpos[ax][j] = d[ax] * (double)(j - 2) + o[ax];
+            if (cudaMalloc(&h->dpos[ax], sizeof(double) * ng[ax]) != cudaSuccess ||
+                cudaMalloc(&h->dih[ax], sizeof(double) * ng[ax]) != cudaSuccess)
+                return bail(GPAT_ERR_OOM);
+        }
+        if (upload_grid(h) != GPAT_OK) return bail(GPAT_ERR_CUDA);
+    }
     // init_particles (particle_module.f90:177-258), double-buffered.
     h->cap = p.nptl_max;
     for (int b = 0; b < 2; ++b) {
@@ -439,6 +507,12 @@ int gpat_destroy(gpat_handle_t *h) {
         if (h->full[s]) cudaFree(h->full[s]);
         if (h->rec[s]) cudaFree(h->rec[s]);
         if (h->aux[s]) cudaFree(h->aux[s]);
+    }
+    for (int ax = 0; ax < 3; ++ax) {
+        if (h->dpos[ax]) cudaFree(h->dpos[ax]);
+        if (h->dih[ax]) cudaFree(h->dih[ax]);
+    }
+    for (int s = 0; s < 2; ++s) {
         if (h->pmem[s]) cudaFree(h->pmem[s]);
     }
     if (h->staging) cudaFree(h->staging);
@@ -509,7 +583,7 @@ int gpat_set_fluctuations(gpat_handle_t *h, int var_flag, const float *db2_slab,
     }
     const gpat_mhd_config_t &c = h->cfg;
     CK(launch_calc_aux_gradients(h->aux[slot], h->prm.ndim, h->nxg, h->nyg, h->nzg, c.dx, c.dy,
-                                 c.dz, h->stream));
+                                 c.dz, h->stream, grad_spans(h)));
     CK(cudaStreamSynchronize(h->stream));
     return GPAT_OK;
 }
@@ -558,6 +632,55 @@ int gpat_get_fluctuations(gpat_handle_t *h, int var_flag, float *aux) {
     return GPAT_OK;
 }
 
+int gpat_set_grid_positions(gpat_handle_t *h, const double *xpos, const double *ypos,
+                            const double *zpos) {
+    if (!h) return GPAT_ERR_ARG;
+    if (!h->prm.nonuniform_grid)
+        return fail(h, GPAT_ERR_STATE, "grid positions are set only when nonuniform_grid is on");
+    const double *src[3] = {xpos, ypos, zpos};
+    for (int ax = 0; ax < h->prm.ndim; ++ax) {
+        if (!src[ax]) return fail(h, GPAT_ERR_ARG, "missing grid positions");
+        const size_t n = h->gpos[ax].size();
+        for (size_t i = 1; i < n; ++i)
+            if (!(src[ax][i] > src[ax][i - 1]))
+                return fail(h, GPAT_ERR_ARG, "grid positions must increase");
+    }
+    for (int ax = 0; ax < h->prm.ndim; ++ax)
+        h->gpos[ax].assign(src[ax], src[ax] + h->gpos[ax].size());
+    CK(cudaSetDevice(h->device));
+    return upload_grid(h);
+}
+
+int gpat_read_grid_positions(gpat_handle_t *h, const char *dir_mhd_data) {
+    if (!h || !dir_mhd_data) return GPAT_ERR_ARG;
+    if (!h->prm.nonuniform_grid)
+        return fail(h, GPAT_ERR_STATE, "grid positions are read only when nonuniform_grid is on");
+    // read_global_grid_positions (mhd_data_parallel.f90:2087-2126): raw
+    // doubles, xpos.dat, ypos.dat (2D and 3D), zpos.dat (3D).
+    const char *names[3] = {"xpos.dat", "ypos.dat", "zpos.dat"};
+    std::vector<double> v[3];
+    for (int ax = 0; ax < h->prm.ndim; ++ax) {
+        const std::string path = std::string(dir_mhd_data) + names[ax];
+        FILE *f = std::fopen(path.c_str(), "rb");
+        if (!f) return fail(h, GPAT_ERR_IO, "cannot open " + path);
+        v[ax].resize(h->gpos[ax].size());
+        const size_t got = std::fread(v[ax].data(), sizeof(double), v[ax].size(), f);
+        std::fclose(f);
+        if (got != v[ax].size()) return fail(h, GPAT_ERR_IO, "short grid file " + path);
+    }
+    return gpat_set_grid_positions(h, v[0].data(), h->prm.ndim > 1 ? v[1].data() : nullptr,
+                                   h->prm.ndim == 3 ? v[2].data() : nullptr);
+}
+
+int gpat_get_grid_positions(gpat_handle_t *h, double *xpos, double *ypos, double *zpos) {
+    if (!h) return GPAT_ERR_ARG;
+    if (!h->grid) return fail(h, GPAT_ERR_STATE, "uniform Cartesian grid: no node positions kept");
+    double *dst[3] = {xpos, ypos, zpos};
+    for (int ax = 0; ax < h->prm.ndim; ++ax)
+        if (dst[ax]) std::copy(h->gpos[ax].begin(), h->gpos[ax].end(), dst[ax]);
+    return GPAT_OK;
+}
+
 int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag) {
     if (!h || !filename) return GPAT_ERR_ARG;
     FILE *f = std::fopen(filename, "rb");
@@ -576,7 +699,7 @@ int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag) {
     CK(cudaSetDevice(h->device));
     const gpat_mhd_config_t &c = h->cfg;
     CK(launch_calc_fields_gradients(h->full[slot], h->prm.ndim, h->nxg, h->nyg, h->nzg, c.dx, c.dy,
-                                    c.dz, h->stream));
+                                    c.dz, h->stream, grad_spans(h)));
     CK(launch_pack_records(h->full[slot], h->rec[slot], h->prm.ndim, h->ncells, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->rec_ready[slot] = true;
@@ -629,6 +752,10 @@ static LargeArgs large_args(const gpat_handle_t *h, int quantity, double qmin) {
     g.nxg = h->nxg; g.nyg = h->nyg;
     g.dx = c.dx; g.dy = c.dy; g.dz = c.dz;
     g.gxmin = c.xmin; g.gymin = c.ymin; g.gzmin = c.zmin;
+    g.spherical = h->prm.spherical_coord ? 1 : 0;
+    g.nonuniform = h->prm.nonuniform_grid ? 1 : 0;
+    g.xpos = h->dpos[0]; g.ypos = h->dpos[1]; g.zpos = h->dpos[2];
+    g.nzg = h->nzg;
     return g;
 }
 
@@ -915,6 +1042,12 @@ static int local_args(gpat_handle_t *h, const gpat_local_dist_t *sp, LocalDistAr
     a.dmu = 2.0 / sp->nmu;
     a.nmu = sp->nmu;
     a.npb = sp->npbins;
+    a.ndim = h->prm.ndim;
+    a.spherical = h->prm.spherical_coord ? 1 : 0;
+    a.nonuniform = h->prm.nonuniform_grid ? 1 : 0;
+    a.rx = sp->rx; a.ry = sp->ry; a.rz = sp->rz;
+    a.nxg = h->nxg; a.nyg = h->nyg; a.nzg = h->nzg;
+    a.xpos = h->dpos[0]; a.ypos = h->dpos[1]; a.zpos = h->dpos[2];
     return GPAT_OK;
 }
 

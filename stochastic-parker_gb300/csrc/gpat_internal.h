@@ -84,6 +84,12 @@ struct MoverArgs {
     int deltab_flag, correlation_flag;
     const float *aux1, *aux2;
     const float *full1, *full2;
+    // Grid type (set_mhd_grid_type): spherical coordinates (x = r,
+    // y = theta, z = phi) and/or non-uniform node positions; the node
+    // positions (ghost nodes included) are read by the FP64 mover whenever
+    // either is set.
+    int spherical, nonuniform;
+    const double *xpos, *ypos, *zpos;
     DevCounters *cnt;
 };
 
@@ -151,14 +157,18 @@ struct MlpTrainBuffers {
 // Launchers (defined in the .cu files).  All enqueue on `s`.
 cudaError_t launch_scatter_raw_fields(const float *raw, int nvar, float *full, size_t ncells,
                                       cudaStream_t s);
+// ih: per-axis inverse spans of a non-uniform grid (3 device pointers), or
+// null for the uniform 0.5 / d.
 cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg, int nzg,
-                                         double dx, double dy, double dz, cudaStream_t s);
+                                         double dx, double dy, double dz, cudaStream_t s,
+                                         const double *const *ih = nullptr);
 cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
                                 cudaStream_t s);
 // Fluctuation records: 16 floats per node, {db2_slab, db2_2d, lc_slab,
 // lc_2d} x {value, d/dx, d/dy, d/dz}.
 cudaError_t launch_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg, double dx,
-                                      double dy, double dz, cudaStream_t s);
+                                      double dy, double dz, cudaStream_t s,
+                                      const double *const *ih = nullptr);
 cudaError_t launch_scatter_aux(const float *src, float *aux, int comp, size_t ncells,
                                cudaStream_t s);
 cudaError_t launch_fill(float *a, float v, size_t n, cudaStream_t s);
@@ -196,6 +206,9 @@ struct LargeArgs {
     const float *aux;      // frame 1 fluctuation records (GPAT_LARGE_DB2), or null
     int nx, ny, nz, nxg, nyg;
     double dx, dy, dz, gxmin, gymin, gzmin;
+    int spherical, nonuniform;              // grid type, as MoverArgs
+    const double *xpos, *ypos, *zpos;       // node positions when either is set
+    int nzg;
 };
 
 struct InjectArgs {
@@ -237,6 +250,10 @@ cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles 
 struct LocalDistArgs {
     double xmin, ymin, zmin, dxd, dyd, dzd, pmin_log, dp_log, dmu;
     int nmu, npb, nrx, nry, nrz;
+    // spherical: weights divided by r^2 sin(theta); nonuniform: spatial bins
+    // (binarySearch_R(pos, x) - 1) / r + 1 on the node positions.
+    int ndim, spherical, nonuniform, rx, ry, rz, nxg, nyg, nzg;
+    const double *xpos, *ypos, *zpos;
 };
 // bins: (count, whi, wlo) per flocal element, zeroed here.
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,

@@ -15,6 +15,7 @@
 #include <cfloat>
 
 #include "device_common.cuh"
+#include "grid_common.cuh"
 
 namespace gpat {
 namespace {
@@ -47,6 +48,13 @@ __device__ __forceinline__ void acc_add(unsigned long long &h, unsigned long lon
     add_u128(h, l, bh, bl);
 }
 
+// NV variables of records of R floats interpolated with corner (ix, iy, iz)
+// and weights w, time-interpolated between the two frames.
+template <int NDIM, int NV, int R>
+__device__ __forceinline__ void interp_at(const MoverArgs &a, const float *rec1, const float *rec2,
+                                          const State &s, int ix, int iy, int iz, const double *w,
+                                          double f[NV]);
+
 // Interpolated fields at the particle: NV variables of records of R floats.
 template <int NDIM, int NV, int R>
 __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, const float *rec2,
@@ -77,6 +85,14 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, co
     w[6] = rx1 * ry * rz;
     w[7] = rx * ry * rz;
     const int ix = fx + 2, iy = fy + 2, iz = (NDIM == 3) ? fz + 2 : 0;
+    interp_at<NDIM, NV, R>(a, rec1, rec2, s, ix, iy, iz, w, f);
+    return true;
+}
+
+template <int NDIM, int NV, int R>
+__device__ __forceinline__ void interp_at(const MoverArgs &a, const float *rec1, const float *rec2,
+                                          const State &s, int ix, int iy, int iz, const double *w,
+                                          double f[NV]) {
     double f2[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) { f[v] = 0.0; f2[v] = 0.0; }
@@ -115,7 +131,6 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, co
 #pragma unroll
         for (int v = 0; v < NV; ++v) f[v] = f[v] * (1.0 - rt) + f2[v] * rt;
     }
-    return true;
 }
 
 // Field values at the particle under the reference's names.
@@ -185,6 +200,23 @@ __device__ __forceinline__ void noise4(const MoverArgs &a, State &s, double r[4]
     }
 }
 
+// noise4 plus r[4], r[5] from a third Philox block of the same push (the 3D
+// spherical focused-transport push draws five numbers).
+__device__ __forceinline__ void noise6(const MoverArgs &a, State &s, double r[6]) {
+    const uint4 w2 = philox4x32_10(make_uint4(s.ctr, 2u, (uint32_t)s.tag_inj, (uint32_t)s.tag_spl),
+                                   a.key0, a.key1);
+    const double u4 = u01_53(w2.x, w2.y), u5 = u01_53(w2.z, w2.w);
+    if (a.noise == GPAT_NOISE_UNIFORM) {
+        r[4] = (2.0 * u4 - 1.0) * sqrt(3.0);
+        r[5] = (2.0 * u5 - 1.0) * sqrt(3.0);
+    } else {
+        const double rc = sqrt(-2.0 * log(1.0 - u4));
+        r[4] = rc * cos(6.283185307179586 * u5);
+        r[5] = rc * sin(6.283185307179586 * u5);
+    }
+    noise4(a, s, r);
+}
+
 __device__ __forceinline__ bool in_acc_region(const MoverArgs &a, const State &s, int ndim) {
     const double xn = (s.x - a.cfg_xmin) / a.cfg_lx;
     bool in = (xn >= a.acc_region[0]) && (xn <= a.acc_region[1]);
@@ -236,6 +268,7 @@ __device__ __forceinline__ void push_momentum(const MoverArgs &a, State &s, doub
 struct Kap {
     double knorm_para, kpara, kperp, skpara, skperp, skpp;
     double dkxx_dx, dkyy_dy, dkzz_dz, dkxy_dx, dkxy_dy, dkxz_dx, dkxz_dz, dkyz_dy, dkyz_dz;
+    double kxx, kyy, kzz, kxy, kxz, kyz;   // read by the spherical pushes
 };
 
 // aux: interpolated {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx, d/dy,
@@ -331,6 +364,12 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
                 kpp * ((f.dbx_dx * by + bx * f.dby_dx) * ib2 - 2.0 * bx * by * f.db_dx * ib3);
     k.dkxy_dy = A[1] * bx * by * ib2 +
                 kpp * ((f.dbx_dy * by + bx * f.dby_dy) * ib2 - 2.0 * bx * by * f.db_dy * ib3);
+    k.kxx = kperp + kpp * bx * bx * ib2;
+    k.kyy = kperp + kpp * by * by * ib2;
+    k.kxy = kpp * bx * by * ib2;
+    k.kzz = (NDIM == 3) ? kperp + kpp * bz * bz * ib2 : 0.0;
+    k.kxz = (NDIM == 3) ? kpp * bx * bz * ib2 : 0.0;
+    k.kyz = (NDIM == 3) ? kpp * by * bz * ib2 : 0.0;
     if (NDIM == 3) {
         k.dkzz_dz = T[2] + A[2] * (bz * bz) * ib2 +
                     2.0 * kpp * bz * (f.dbz_dz * b - bz * f.db_dz) * ib3;
@@ -391,34 +430,132 @@ __device__ __forceinline__ double dpp_terms(const MoverArgs &a, double p, const 
     return dpp;
 }
 
-// push_particle_2d (:3358-3606).
+// Cell sizes a push sees: mhd_config's dx, dy, dz on a uniform grid, the
+// searched cell's spans on a non-uniform one (:3400-3408, :4689-4700).
+struct Geo {
+    double dxm, dym, dzm;
+};
+
+// Metric factors of spherical coordinates (x = r, y = theta, z = phi) set at
+// the top of every spherical push (:3420-3427, :4707-4713).
+struct Sph {
+    double ctheta, istheta, cot_theta, ir, ir2;
+};
+
+__device__ __forceinline__ Sph spherical_terms(const State &s) {
+    Sph g;
+    g.ctheta = cos(s.y);
+    g.istheta = 1.0 / sin(s.y);
+    g.cot_theta = g.ctheta * g.istheta;
+    g.ir = 1.0 / s.x;
+    g.ir2 = 1.0 / (s.x * s.x);
+    return g;
+}
+
+// Position noise of the 2D spherical pushes: the eigen-decomposition of the
+// (r, theta) diffusion tensor (:3559-3580, :3905-3925).
+__device__ __forceinline__ void spherical_noise_2d(const Kap &k, const Sph &g, double r1, double r2,
+                                                   double sdt, double &nx, double &ny) {
+    const double a1 = k.kxx;
+    const double b1 = k.kxy * g.ir;
+    const double c1 = k.kyy * g.ir2;
+    const double amc = a1 - c1;
+    const double atmp = sqrt(amc * amc + 4.0 * (b1 * b1));
+    const double Qpp = atmp + (a1 + c1);
+    double Qmp = atmp - (a1 + c1);
+    const double Qpm = atmp + (a1 - c1);
+    const double Qmm = atmp - (a1 - c1);
+    if (Qmp > 0.0) Qmp = 0.0;
+    const double qtmp1 = sqrt(-Qmp / (Qmm * Qmm + 4.0 * (b1 * b1)));
+    const double qtmp2 = sqrt(Qpp / (Qpm * Qpm + 4.0 * (b1 * b1)));
+    nx = (-(Qmm * qtmp1 * r1) + Qpm * qtmp2 * r2) * sdt;
+    ny = (2.0 * b1 * qtmp1 * r1 + 2.0 * b1 * qtmp2 * r2) * sdt;
+}
+
+// The 3D spherical noise matrix P (upper triangular, P P^T = 2 K in the
+// metric): p11 p12 p13 p22 p23 p33.  CLAMP: the focused-transport push's
+// guards against small negative radicands (:5253-5278), absent from the
+// Parker push (:4852-4863).
+template <bool CLAMP>
+__device__ __forceinline__ void spherical_noise_3d(const Kap &k, const Sph &g, double p[6]) {
+    const double kxx = k.kxx, kyy = k.kyy, kzz = k.kzz, kxy = k.kxy, kxz = k.kxz, kyz = k.kyz;
+    const double num = kxx * (kyz * kyz) + kyy * (kxz * kxz) + kzz * (kxy * kxy) -
+                       2.0 * kxy * kxz * kyz - kxx * kyy * kzz;
+    const double den = kyz * kyz - kyy * kzz;
+    double q = 2.0 * num / den;
+    if (CLAMP && q < 0.0) q = 0.0;
+    p[0] = sqrt(q);
+    q = 2.0 * (kyy - kyz * kyz / kzz);
+    if (CLAMP && q < 0.0) q = 0.0;
+    p[1] = (kxz * kyz - kxy * kzz) * sqrt(q) / den;
+    p[3] = sqrt(q) * g.ir;
+    if (CLAMP && kzz <= 0.0) {
+        p[2] = 0.0; p[4] = 0.0; p[5] = 0.0;
+    } else {
+        p[2] = sqrt(2.0 / kzz) * kxz;
+        p[4] = sqrt(2.0 / kzz) * kyz * g.ir;
+        p[5] = sqrt(2.0 * kzz) * g.istheta * g.ir;
+    }
+}
+
+// push_particle_2d (:3358-3606), Cartesian or spherical (SPH).
+template <bool SPH>
 __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
-                                       bool fixed_dt, Delta &d) {
+                                       const Geo &geo, bool fixed_dt, Delta &d) {
     const double bx = f.bx, by = f.by, bz = f.bz;
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    Sph g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (SPH) g = spherical_terms(s);
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
     const double vdp = vdrift_prefactor(a, s.p, 3);
-    const double vdx = vdp * (f.dbz_dy * ib2 - 2.0 * bz * f.db_dy * ib3);
-    const double vdy = vdp * (-(f.dbz_dx * ib2) + 2.0 * bz * f.db_dx * ib3);
+    double vdx, vdy, gbr = 0.0, gbt = 0.0;
+    if (SPH) {
+        gbr = f.db_dx;
+        gbt = f.db_dy * g.ir;
+        vdx = vdp * ((f.dbz_dy + g.cot_theta * bz) * g.ir * ib2 - gbt * bz * 2.0 * ib3);
+        vdy = vdp * (-((f.dbz_dx + bz * g.ir) * ib2) + gbr * bz * 2.0 * ib3);
+    } else {
+        vdx = vdp * (f.dbz_dy * ib2 - 2.0 * bz * f.db_dy * ib3);
+        vdy = vdp * (-(f.dbz_dx * ib2) + 2.0 * bz * f.db_dx * ib3);
+    }
     double vdz = 0.0;
-    if (a.check_drift_2d)
-        vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
-    const double dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy;
-    const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy;
-    const double dz_dt = vdz;
-    const double divv = f.dvx_dx + f.dvy_dy;
+    if (a.check_drift_2d) {
+        if (SPH)
+            vdz = vdp * ((f.dby_dx + by * g.ir - f.dbx_dy * g.ir) * ib2 -
+                         (gbr * by - gbt * bx * g.ir) * 2.0 * ib3);
+        else
+            vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
+    }
+    double dx_dt, dy_dt, dz_dt, divv;
+    if (SPH) {
+        dx_dt = f.vx + vdx + k.dkxx_dx + (2.0 * k.kxx + k.dkxy_dy + k.kxy * g.cot_theta) * g.ir;
+        dy_dt = (f.vy + vdy + k.dkxy_dx) * g.ir + (k.kxy + k.dkyy_dy + k.kyy * g.cot_theta) * g.ir2;
+        dz_dt = vdz * g.istheta * g.ir;
+        divv = f.dvx_dx + (2.0 * f.vx + f.dvy_dy + f.vy * g.ctheta * g.istheta) * g.ir;
+    } else {
+        dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy;
+        dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy;
+        dz_dt = vdz;
+        divv = f.dvx_dx + f.dvy_dy;
+    }
     double dp_dt = -(s.p * divv / 3.0);
     const double dpp = dpp_terms<2>(a, s.p, f, k, b, divv, dp_dt);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
             const double sk = (skperp > 0.0) ? skperp : skpara;
-            double q = 0.5 * a.dx / skpara, m = q * q;
-            q = 0.5 * a.dy / skpara; if (q * q < m) m = q * q;
-            q = sk / dx_dt; if (q * q < m) m = q * q;
-            q = sk / dy_dt; if (q * q < m) m = q * q;
+            double q = 0.5 * geo.dxm / skpara, m = q * q;
+            if (SPH) {
+                q = 0.5 * geo.dym * s.x / skpara; if (q * q < m) m = q * q;
+                q = sk / dx_dt; if (q * q < m) m = q * q;
+                q = sk * g.ir / dy_dt; if (q * q < m) m = q * q;
+            } else {
+                q = 0.5 * geo.dym / skpara; if (q * q < m) m = q * q;
+                q = sk / dx_dt; if (q * q < m) m = q * q;
+                q = sk / dy_dt; if (q * q < m) m = q * q;
+            }
             q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
             s.dt = m;
         } else {
@@ -430,9 +567,17 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &
     const double sdt = sqrt(s.dt);
     double r[4];
     noise4(a, s, r);
-    const double skpp = k.skpp;
-    const double dX = dx_dt * s.dt + r[0] * skperp * sdt + r[2] * skpp * sdt * bx * ib;
-    const double dY = dy_dt * s.dt + r[1] * skperp * sdt + r[2] * skpp * sdt * by * ib;
+    double dX, dY;
+    if (SPH) {
+        double nx, ny;
+        spherical_noise_2d(k, g, r[0], r[1], sdt, nx, ny);
+        dX = dx_dt * s.dt + nx;
+        dY = dy_dt * s.dt + ny;
+    } else {
+        const double skpp = k.skpp;
+        dX = dx_dt * s.dt + r[0] * skperp * sdt + r[2] * skpp * sdt * bx * ib;
+        dY = dy_dt * s.dt + r[1] * skperp * sdt + r[2] * skpp * sdt * by * ib;
+    }
     const double dZ = dz_dt * s.dt;
     s.x = s.x + dX;
     s.y = s.y + dY;
@@ -443,37 +588,71 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &
     push_momentum(a, s, dp_dt, dpp, sdt, r[3], 2, d.p);
 }
 
-// push_particle_3d (:4625-4907).
+// push_particle_3d (:4625-4907), Cartesian or spherical (SPH).
+template <bool SPH>
 __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
-                                       bool fixed_dt, Delta &d) {
+                                       const Geo &geo, bool fixed_dt, Delta &d) {
     const double bx = f.bx, by = f.by, bz = f.bz;
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
     const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
     const double bxyn = sqrt(bxn * bxn + byn * byn);
     const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
+    Sph g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (SPH) g = spherical_terms(s);
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
     const double vdp = vdrift_prefactor(a, s.p, 3);
-    const double vdx = vdp * ((f.dbz_dy - f.dby_dz) * ib2 - 2.0 * (bz * f.db_dy - by * f.db_dz) * ib3);
-    const double vdy = vdp * ((f.dbx_dz - f.dbz_dx) * ib2 - 2.0 * (bx * f.db_dz - bz * f.db_dx) * ib3);
-    const double vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
-    const double dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
-    const double dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
-    const double dz_dt = f.vz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
-    const double divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
+    double vdx, vdy, vdz;
+    if (SPH) {
+        const double gbr = f.db_dx, gbt = f.db_dy * g.ir, gbp = f.db_dz * g.ir * g.istheta;
+        vdx = vdp * ((f.dbz_dy + bz * g.ctheta * g.istheta - f.dby_dz * g.istheta) * g.ir * ib2 -
+                     (gbt * bz - gbp * by) * 2.0 * ib3);
+        vdy = vdp * ((f.dbx_dz * g.istheta * g.ir - f.dbz_dx - bz * g.ir) * ib2 -
+                     (gbp * bx - gbr * bz) * 2.0 * ib3);
+        vdz = vdp * ((f.dby_dx + by * g.ir - f.dbx_dy * g.ir) * ib2 -
+                     (gbr * by - gbt * bx) * 2.0 * ib3);
+    } else {
+        vdx = vdp * ((f.dbz_dy - f.dby_dz) * ib2 - 2.0 * (bz * f.db_dy - by * f.db_dz) * ib3);
+        vdy = vdp * ((f.dbx_dz - f.dbz_dx) * ib2 - 2.0 * (bx * f.db_dz - bz * f.db_dx) * ib3);
+        vdz = vdp * ((f.dby_dx - f.dbx_dy) * ib2 - 2.0 * (by * f.db_dx - bx * f.db_dy) * ib3);
+    }
+    double dx_dt, dy_dt, dz_dt, divv;
+    if (SPH) {
+        dx_dt = f.vx + vdx + k.dkxx_dx +
+                (2.0 * k.kxx + k.dkxy_dy + k.kxy * g.ctheta * g.istheta + k.dkxz_dz * g.istheta) * g.ir;
+        dy_dt = (f.vy + vdy + k.dkxy_dx) * g.ir +
+                (k.kxy + k.dkyy_dy + k.kyy * g.ctheta * g.istheta + k.dkyz_dz * g.istheta) * g.ir2;
+        dz_dt = (f.vz + vdz + k.dkxz_dx) * g.istheta * g.ir +
+                (k.kxz + k.dkyz_dy + k.dkzz_dz * g.istheta) * g.istheta * g.ir2;
+        divv = f.dvx_dx +
+               (2.0 * f.vx + f.dvy_dy + f.vy * g.ctheta * g.istheta + f.dvz_dz * g.istheta) * g.ir;
+    } else {
+        dx_dt = f.vx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
+        dy_dt = f.vy + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
+        dz_dt = f.vz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
+        divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
+    }
     double dp_dt = -(s.p * divv / 3.0);
     const double dpp = dpp_terms<3>(a, s.p, f, k, b, divv, dp_dt);
     const double skpara = k.skpara, skperp = k.skperp;
     if (!fixed_dt) {
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
             const double sk = (skperp > 0.0) ? skperp : skpara;
-            double q = 0.5 * a.dx / skpara, m = q * q;
-            q = 0.5 * a.dy / skpara; if (q * q < m) m = q * q;
-            q = 0.5 * a.dz / skpara; if (q * q < m) m = q * q;
-            q = sk / dx_dt; if (q * q < m) m = q * q;
-            q = sk / dy_dt; if (q * q < m) m = q * q;
-            q = sk / dz_dt; if (q * q < m) m = q * q;
+            double q = 0.5 * geo.dxm / skpara, m = q * q;
+            if (SPH) {
+                q = 0.5 * geo.dym * s.x / skpara; if (q * q < m) m = q * q;
+                q = 0.5 * geo.dzm * s.x * sin(s.y) / skpara; if (q * q < m) m = q * q;
+                q = sk / dx_dt; if (q * q < m) m = q * q;
+                q = sk * g.ir / dy_dt; if (q * q < m) m = q * q;
+                q = sk * g.ir * g.istheta / dz_dt; if (q * q < m) m = q * q;
+            } else {
+                q = 0.5 * geo.dym / skpara; if (q * q < m) m = q * q;
+                q = 0.5 * geo.dzm / skpara; if (q * q < m) m = q * q;
+                q = sk / dx_dt; if (q * q < m) m = q * q;
+                q = sk / dy_dt; if (q * q < m) m = q * q;
+                q = sk / dz_dt; if (q * q < m) m = q * q;
+            }
             q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
             s.dt = m;
         } else {
@@ -485,11 +664,20 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
     const double sdt = sqrt(s.dt);
     double r[4];
     noise4(a, s, r);
-    const double dX = dx_dt * s.dt +
-        (bxn * skpara * r[0] - bxn * bzn * skperp * ibxyn * r[1] - byn * skperp * ibxyn * r[2]) * sdt;
-    const double dY = dy_dt * s.dt +
-        (byn * skpara * r[0] - byn * bzn * skperp * ibxyn * r[1] + bxn * skperp * ibxyn * r[2]) * sdt;
-    const double dZ = dz_dt * s.dt + (bzn * skpara * r[0] + bxyn * skperp * r[1]) * sdt;
+    double dX, dY, dZ;
+    if (SPH) {
+        double P[6];
+        spherical_noise_3d<false>(k, g, P);
+        dX = dx_dt * s.dt + (P[0] * r[0] + P[1] * r[1] + P[2] * r[2]) * sdt;
+        dY = dy_dt * s.dt + (P[3] * r[1] + P[4] * r[2]) * sdt;
+        dZ = dz_dt * s.dt + P[5] * r[2] * sdt;
+    } else {
+        dX = dx_dt * s.dt +
+            (bxn * skpara * r[0] - bxn * bzn * skperp * ibxyn * r[1] - byn * skperp * ibxyn * r[2]) * sdt;
+        dY = dy_dt * s.dt +
+            (byn * skpara * r[0] - byn * bzn * skperp * ibxyn * r[1] + bxn * skperp * ibxyn * r[2]) * sdt;
+        dZ = dz_dt * s.dt + (bzn * skpara * r[0] + bxyn * skperp * r[1]) * sdt;
+    }
     s.x = s.x + dX;
     s.y = s.y + dY;
     s.z = s.z + dZ;
@@ -526,21 +714,31 @@ __device__ __forceinline__ void calc_duu(const MoverArgs &a, const State &s, dou
     duu = u;
 }
 
-// Adaptive step of the focused-transport pushes (:3850-3905, :5170-5230).
-template <int NDIM>
+// Adaptive step of the focused-transport pushes (:3850-3905, :5170-5230);
+// in spherical coordinates the theta and phi limits carry r and r sin(theta).
+template <int NDIM, bool SPH>
 __device__ __forceinline__ void ft_time_step(const MoverArgs &a, State &s, const Kap &k,
-                                             double dx_dt, double dy_dt, double dz_dt,
-                                             double dp_dt, double dmu_dt, double duu) {
+                                             const Geo &geo, const Sph &g, double dx_dt,
+                                             double dy_dt, double dz_dt, double dp_dt,
+                                             double dmu_dt, double duu) {
     const bool nonzero = dx_dt != 0.0 && dy_dt != 0.0 && (NDIM < 3 || dz_dt != 0.0) &&
                          dp_dt != 0.0 && dmu_dt != 0.0;
     if (nonzero) {
         const double sk = (k.skperp > 0.0) ? k.skperp : k.skpara;
-        double q = 0.5 * a.dx / sk, m = q * q;
-        q = 0.5 * a.dy / sk; if (q * q < m) m = q * q;
-        if (NDIM == 3) { q = 0.5 * a.dz / sk; if (q * q < m) m = q * q; }
-        q = sk / dx_dt; if (q * q < m) m = q * q;
-        q = sk / dy_dt; if (q * q < m) m = q * q;
-        if (NDIM == 3) { q = sk / dz_dt; if (q * q < m) m = q * q; }
+        double q = 0.5 * geo.dxm / sk, m = q * q;
+        if (SPH) {
+            q = 0.5 * geo.dym * s.x / sk; if (q * q < m) m = q * q;
+            if (NDIM == 3) { q = 0.5 * geo.dzm * s.x * sin(s.y) / sk; if (q * q < m) m = q * q; }
+            q = sk / dx_dt; if (q * q < m) m = q * q;
+            q = sk * g.ir / dy_dt; if (q * q < m) m = q * q;
+            if (NDIM == 3) { q = sk * g.ir * g.istheta / dz_dt; if (q * q < m) m = q * q; }
+        } else {
+            q = 0.5 * geo.dym / sk; if (q * q < m) m = q * q;
+            if (NDIM == 3) { q = 0.5 * geo.dzm / sk; if (q * q < m) m = q * q; }
+            q = sk / dx_dt; if (q * q < m) m = q * q;
+            q = sk / dy_dt; if (q * q < m) m = q * q;
+            if (NDIM == 3) { q = sk / dz_dt; if (q * q < m) m = q * q; }
+        }
         q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
         q = (double)0.1f / fabs(dmu_dt); if (q < m) m = q;
         q = 2.0 * duu / (dmu_dt * dmu_dt); if (q < m) m = q;
@@ -599,14 +797,18 @@ __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, doubl
     d.x = dX; d.y = dY; d.z = (NDIM == 3) ? dZ : 0.0; d.p = dP; d.v = dV; d.mu = dMu;
 }
 
-// push_particle_2d_ft (:3626-3964) and push_particle_3d_ft (:4930-5324).
-template <int NDIM>
+// push_particle_2d_ft (:3626-3964) and push_particle_3d_ft (:4930-5324),
+// Cartesian or spherical (SPH).  The 3D spherical position noise draws a
+// third number (ran3), taken from the push's third Philox block.
+template <int NDIM, bool SPH>
 __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld &f,
-                                        const double *aux, const Kap &k, bool fixed_dt,
-                                        Delta &d) {
+                                        const double *aux, const Kap &k, const Geo &geo,
+                                        bool fixed_dt, Delta &d) {
     const double bx = f.bx, by = f.by, bz = f.bz;
     const double b = sqrt(bx * bx + by * by + bz * bz);
     const double ib = (b < DBL_EPSILON) ? 0.0 : 1.0 / b;
+    Sph g = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (SPH) g = spherical_terms(s);
     const double ib2 = ib * ib;
     const double ib3 = ib * ib2;
     const double vdp = vdrift_prefactor(a, s.p, 1);
@@ -615,28 +817,66 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
     const double muf2 = 0.5 * (3.0 * mu2 - 1.0);
     double kx, ky, kz, bdot_curvb, vdx, vdy, vdz = 0.0;
     if (NDIM == 2) {
-        kx = bx * f.dbx_dx + by * f.dbx_dy;
-        ky = bx * f.dby_dx + by * f.dby_dy;
-        kz = bx * f.dbz_dx + by * f.dbz_dy;
-        bdot_curvb = bx * f.dbz_dy - by * f.dbz_dx + bz * (f.dby_dx - f.dbx_dy);
-        vdx = vdp * (muf1 * (-(bz * f.db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
-                     muf1 * bx * bdot_curvb * ib3);
-        vdy = vdp * (muf1 * (bz * f.db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
-                     muf1 * by * bdot_curvb * ib3);
-        if (a.check_drift_2d)
+        double gbr = 0.0, gbt = 0.0;
+        if (SPH) {
+            const double ir = g.ir, cot = g.cot_theta;
+            gbr = f.db_dx;
+            gbt = f.db_dy * ir;
+            kx = bx * f.dbx_dx + by * f.dbx_dy * ir - (by * by + bz * bz) * ir;
+            ky = bx * f.dby_dx + by * f.dby_dy * ir + (bx * by - cot * (bz * bz)) * ir;
+            kz = bx * f.dbz_dx + by * f.dbz_dy * ir + (bx * bz + cot * by * bz) * ir;
+            bdot_curvb = bx * (f.dbz_dy + cot * bz) * ir + by * (-f.dbz_dx - bz * ir) +
+                         bz * (f.dby_dx + by * ir - f.dbx_dy * ir);
+            vdx = vdp * (muf1 * (-(bz * gbt)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                         muf1 * bx * bdot_curvb * ib3);
+            vdy = vdp * (muf1 * (bz * gbr) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                         muf1 * by * bdot_curvb * ib3);
+        } else {
+            kx = bx * f.dbx_dx + by * f.dbx_dy;
+            ky = bx * f.dby_dx + by * f.dby_dy;
+            kz = bx * f.dbz_dx + by * f.dbz_dy;
+            bdot_curvb = bx * f.dbz_dy - by * f.dbz_dx + bz * (f.dby_dx - f.dbx_dy);
+            vdx = vdp * (muf1 * (-(bz * f.db_dy)) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                         muf1 * bx * bdot_curvb * ib3);
+            vdy = vdp * (muf1 * (bz * f.db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                         muf1 * by * bdot_curvb * ib3);
+        }
+        if (a.check_drift_2d) {
+            if (SPH)
+                vdz = vdp * (muf1 * (bx * gbt - by * gbr) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                             muf1 * bz * bdot_curvb * ib3);
+            else
+                vdz = vdp * (muf1 * (bx * f.db_dy - by * f.db_dx) * ib2 +
+                             mu2 * (bx * ky - by * kx) * ib3 + muf1 * bz * bdot_curvb * ib3);
+        }
+    } else {
+        if (SPH) {
+            const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
+            const double gbr = f.db_dx, gbt = f.db_dy * ir, gbp = f.db_dz * ir * ist;
+            kx = bx * f.dbx_dx + ir * (by * f.dbx_dy + bz * f.dbx_dz * ist - (by * by + bz * bz));
+            ky = bx * f.dby_dx + ir * (by * f.dby_dy + bz * f.dby_dz * ist + (bx * by - cot * (bz * bz)));
+            kz = bx * f.dbz_dx + ir * (by * f.dbz_dy + bz * f.dbz_dz * ist + (bx * bz + cot * by * bz));
+            bdot_curvb = bx * (f.dbz_dy + cot * bz - f.dby_dz * ist) * ir +
+                         by * (f.dbx_dz * ist * ir - f.dbz_dx - bz * ir) +
+                         bz * (f.dby_dx + by * ir - f.dbx_dy * ir);
+            vdx = vdp * (muf1 * (by * gbp - bz * gbt) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                         muf1 * bx * bdot_curvb * ib3);
+            vdy = vdp * (muf1 * (bz * gbr - bx * gbp) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                         muf1 * by * bdot_curvb * ib3);
+            vdz = vdp * (muf1 * (bx * gbt - by * gbr) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
+                         muf1 * bz * bdot_curvb * ib3);
+        } else {
+            kx = bx * f.dbx_dx + by * f.dbx_dy + bz * f.dbx_dz;
+            ky = bx * f.dby_dx + by * f.dby_dy + bz * f.dby_dz;
+            kz = bx * f.dbz_dx + by * f.dbz_dy + bz * f.dbz_dz;
+            bdot_curvb = bx * (f.dbz_dy - f.dby_dz) + by * (f.dbx_dz - f.dbz_dx) + bz * (f.dby_dx - f.dbx_dy);
+            vdx = vdp * (muf1 * (by * f.db_dz - bz * f.db_dy) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
+                         muf1 * bx * bdot_curvb * ib3);
+            vdy = vdp * (muf1 * (bz * f.db_dx - bx * f.db_dz) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
+                         muf1 * by * bdot_curvb * ib3);
             vdz = vdp * (muf1 * (bx * f.db_dy - by * f.db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
                          muf1 * bz * bdot_curvb * ib3);
-    } else {
-        kx = bx * f.dbx_dx + by * f.dbx_dy + bz * f.dbx_dz;
-        ky = bx * f.dby_dx + by * f.dby_dy + bz * f.dby_dz;
-        kz = bx * f.dbz_dx + by * f.dbz_dy + bz * f.dbz_dz;
-        bdot_curvb = bx * (f.dbz_dy - f.dby_dz) + by * (f.dbx_dz - f.dbz_dx) + bz * (f.dby_dx - f.dbx_dy);
-        vdx = vdp * (muf1 * (by * f.db_dz - bz * f.db_dy) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
-                     muf1 * bx * bdot_curvb * ib3);
-        vdy = vdp * (muf1 * (bz * f.db_dx - bx * f.db_dz) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
-                     muf1 * by * bdot_curvb * ib3);
-        vdz = vdp * (muf1 * (bx * f.db_dy - by * f.db_dx) * ib2 + mu2 * (bx * ky - by * kx) * ib3 +
-                     muf1 * bz * bdot_curvb * ib3);
+        }
     }
     double vbx = s.v * s.mu * ib;
     const double vby = vbx * by;
@@ -644,46 +884,102 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
     vbx = vbx * bx;
     double dx_dt, dy_dt, dz_dt, divv, bb_gradv, bv_gradv, div_bnorm;
     if (NDIM == 2) {
-        dx_dt = f.vx + vdx + vbx + k.dkxx_dx + k.dkxy_dy;
-        dy_dt = f.vy + vdy + vby + k.dkxy_dx + k.dkyy_dy;
-        dz_dt = vdz;
-        divv = f.dvx_dx + f.dvy_dy;
-        bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy) + by * (bx * f.dvy_dx + by * f.dvy_dy) +
-                    bz * (bx * f.dvz_dx + by * f.dvz_dy)) * ib2;
-        bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy) + by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy) +
-                    bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy)) * ib;
-        div_bnorm = -((bx * f.db_dx + by * f.db_dy) * ib2);
+        if (SPH) {
+            const double ir = g.ir, cot = g.cot_theta;
+            const double vx = f.vx, vy = f.vy, vz = f.vz;
+            dx_dt = vx + vdx + vbx + k.dkxx_dx + (2.0 * k.kxx + k.dkxy_dy + k.kxy * cot) * ir;
+            dy_dt = (vy + vdy + vby + k.dkxy_dx) * ir + (k.kxy + k.dkyy_dy + k.kyy * cot) * g.ir2;
+            dz_dt = vdz * g.istheta * ir;
+            divv = f.dvx_dx + (2.0 * vx + f.dvy_dy + vy * cot) * ir;
+            bb_gradv = (bx * bx * f.dvx_dx + bx * by * f.dvx_dy * ir - bx * (by * vy + bz * vz) * ir +
+                        by * bx * f.dvy_dx + by * by * f.dvy_dy * ir + by * (by * vx - cot * bz * vz) * ir +
+                        bz * bx * f.dvz_dx + bz * by * f.dvz_dy * ir + (bz * bz) * (vx + cot * vy) * ir) * ib2;
+            bv_gradv = (bx * vx * f.dvx_dx + bx * vy * f.dvx_dy * ir - bx * (vy * vy + vz * vz) * ir +
+                        by * vx * f.dvy_dx + by * vy * f.dvy_dy * ir + by * (vy * vx - cot * vz * vz) * ir +
+                        bz * vx * f.dvz_dx + bz * vy * f.dvz_dy * ir + bz * vz * (vx + cot * vy) * ir) * ib;
+            div_bnorm = -((bx * f.db_dx + by * f.db_dy * ir) * ib2);
+        } else {
+            dx_dt = f.vx + vdx + vbx + k.dkxx_dx + k.dkxy_dy;
+            dy_dt = f.vy + vdy + vby + k.dkxy_dx + k.dkyy_dy;
+            dz_dt = vdz;
+            divv = f.dvx_dx + f.dvy_dy;
+            bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy) + by * (bx * f.dvy_dx + by * f.dvy_dy) +
+                        bz * (bx * f.dvz_dx + by * f.dvz_dy)) * ib2;
+            bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy) + by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy) +
+                        bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy)) * ib;
+            div_bnorm = -((bx * f.db_dx + by * f.db_dy) * ib2);
+        }
     } else {
-        dx_dt = f.vx + vbx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
-        dy_dt = f.vy + vby + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
-        dz_dt = f.vz + vbz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
-        divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
-        bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy + bz * f.dvx_dz) +
-                    by * (bx * f.dvy_dx + by * f.dvy_dy + bz * f.dvy_dz) +
-                    bz * (bx * f.dvz_dx + by * f.dvz_dy + bz * f.dvz_dz)) * ib2;
-        bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy + f.vz * f.dvx_dz) +
-                    by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy + f.vz * f.dvy_dz) +
-                    bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy + f.vz * f.dvz_dz)) * ib;
-        div_bnorm = -((bx * f.db_dx + by * f.db_dy + bz * f.db_dz) * ib2);
+        if (SPH) {
+            const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
+            const double vx = f.vx, vy = f.vy, vz = f.vz;
+            dx_dt = vx + vbx + vdx + k.dkxx_dx +
+                    (2.0 * k.kxx + k.dkxy_dy + k.kxy * g.ctheta * ist + k.dkxz_dz * ist) * ir;
+            dy_dt = (vy + vby + vdy + k.dkxy_dx) * ir +
+                    (k.kxy + k.dkyy_dy + k.kyy * g.ctheta * ist + k.dkyz_dz * ist) * g.ir2;
+            dz_dt = (vz + vbz + vdz + k.dkxz_dx) * ist * ir +
+                    (k.kxz + k.dkyz_dy + k.dkzz_dz * ist) * ist * g.ir2;
+            divv = f.dvx_dx + (2.0 * vx + f.dvy_dy + vy * cot + f.dvz_dz * ist) * ir;
+            const double dtmp = ist * ir;
+            bb_gradv = (bx * bx * f.dvx_dx + bx * by * f.dvx_dy * ir + bx * bz * f.dvx_dz * dtmp -
+                        bx * (by * vy + bz * vz) * ir +
+                        by * bx * f.dvy_dx + by * by * f.dvy_dy * ir + by * bz * f.dvy_dz * dtmp +
+                        by * (by * vx - cot * bz * vz) * ir +
+                        bz * bx * f.dvz_dx + bz * by * f.dvz_dy * ir + bz * bz * f.dvz_dz * dtmp +
+                        (bz * bz) * (vx + cot * vy) * ir) * ib2;
+            bv_gradv = (bx * vx * f.dvx_dx + bx * vy * f.dvx_dy * ir + bx * vz * f.dvx_dz * dtmp -
+                        bx * (vy * vy + vz * vz) * ir +
+                        by * vx * f.dvy_dx + by * vy * f.dvy_dy * ir + by * vz * f.dvy_dz * dtmp +
+                        by * (vy * vx - cot * vz * vz) * ir +
+                        bz * vx * f.dvz_dx + bz * vy * f.dvz_dy * ir + bz * vz * f.dvz_dz * dtmp +
+                        bz * vz * (vx + cot * vy) * ir) * ib;
+            div_bnorm = -((bx * f.db_dx + by * f.db_dy * ir + bz * f.db_dz * ir * ist) * ib2);
+        } else {
+            dx_dt = f.vx + vbx + vdx + k.dkxx_dx + k.dkxy_dy + k.dkxz_dz;
+            dy_dt = f.vy + vby + vdy + k.dkxy_dx + k.dkyy_dy + k.dkyz_dz;
+            dz_dt = f.vz + vbz + vdz + k.dkxz_dx + k.dkyz_dy + k.dkzz_dz;
+            divv = f.dvx_dx + f.dvy_dy + f.dvz_dz;
+            bb_gradv = (bx * (bx * f.dvx_dx + by * f.dvx_dy + bz * f.dvx_dz) +
+                        by * (bx * f.dvy_dx + by * f.dvy_dy + bz * f.dvy_dz) +
+                        bz * (bx * f.dvz_dx + by * f.dvz_dy + bz * f.dvz_dz)) * ib2;
+            bv_gradv = (bx * (f.vx * f.dvx_dx + f.vy * f.dvx_dy + f.vz * f.dvx_dz) +
+                        by * (f.vx * f.dvy_dx + f.vy * f.dvy_dy + f.vz * f.dvy_dz) +
+                        bz * (f.vx * f.dvz_dx + f.vy * f.dvz_dy + f.vz * f.dvz_dz)) * ib;
+            div_bnorm = -((bx * f.db_dx + by * f.db_dy + bz * f.db_dz) * ib2);
+        }
     }
     const double acc_rate = -(muf1 * divv + muf2 * bb_gradv + s.mu * bv_gradv / s.v);
     double dp_dt = s.p * acc_rate;
     const double dpp = dpp_terms<NDIM>(a, s.p, f, k, b, divv, dp_dt);
     double dmu_dt, duu;
     calc_duu(a, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
-    if (!fixed_dt) ft_time_step<NDIM>(a, s, k, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    if (!fixed_dt) ft_time_step<NDIM, SPH>(a, s, k, geo, g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s.dt);
-    double r[4];
-    noise4(a, s, r);
+    double r[6];
+    if (SPH && NDIM == 3) noise6(a, s, r);
+    else noise4(a, s, r);
     const double bxn = bx * ib, byn = by * ib, bzn = bz * ib;
     const double skperp = k.skperp;
     double dX, dY, dZ;
     if (NDIM == 2) {
-        // by and bx (not byn, bxn) in the second terms, as the reference.
-        const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
-        dX = dx_dt * s.dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
-        dY = dy_dt * s.dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+        if (SPH) {
+            double nx, ny;
+            spherical_noise_2d(k, g, r[0], r[1], sdt, nx, ny);
+            dX = dx_dt * s.dt + nx;
+            dY = dy_dt * s.dt + ny;
+        } else {
+            // by and bx (not byn, bxn) in the second terms, as the reference.
+            const double ibxyn = 1.0 / sqrt(bxn * bxn + byn * byn);
+            dX = dx_dt * s.dt + skperp * ibxyn * sdt * (-(bxn * bzn * r[0]) - by * r[1]);
+            dY = dy_dt * s.dt + skperp * ibxyn * sdt * (-(byn * bzn * r[0]) + bx * r[1]);
+        }
         dZ = dz_dt * s.dt;
+    } else if (SPH) {
+        double P[6];
+        spherical_noise_3d<true>(k, g, P);
+        dX = dx_dt * s.dt + (P[0] * r[0] + P[1] * r[1] + P[2] * r[4]) * sdt;
+        dY = dy_dt * s.dt + (P[3] * r[1] + P[4] * r[4]) * sdt;
+        dZ = dz_dt * s.dt + P[5] * r[4] * sdt;
     } else {
         const double bxyn = sqrt(bxn * bxn + byn * byn);
         const double ibxyn = (bxyn < DBL_EPSILON) ? 0.0 : 1.0 / bxyn;
@@ -732,11 +1028,51 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
     }
 }
 
-template <int NDIM, bool FT, bool FULL>
+template <int NDIM, bool FT, bool FULL, bool GRID>
 __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, Delta &d) {
     Fld f;
     double av[16];
     const double *aux = nullptr;
+    if (GRID) {
+        // Spherical or non-uniform grid: corner and weights from the node
+        // positions (:1615-1630), all 32 variables.
+        GridCell c;
+        if (!grid_cell(NDIM, a.spherical, a.xpos, a.nxg, a.ypos, a.nyg, a.zpos, a.nzg, s.x, s.y,
+                       s.z, c)) {
+            set_status(a.cnt, kStatusIndexGuard);
+            return false;
+        }
+        double v[32];
+        interp_at<NDIM, 32, 32>(a, a.full1, a.full2, s, c.ix, c.iy, c.iz, c.w, v);
+        f = named_full(v);
+        if (a.aux1 && (a.deltab_flag || a.correlation_flag)) {
+            interp_at<NDIM, 16, 16>(a, a.aux1, a.aux2, s, c.ix, c.iy, c.iz, c.w, av);
+            aux = av;
+        }
+        Geo geo = {a.dx, a.dy, a.dz};
+        if (a.nonuniform) {
+            // the pushes' own search (no offset shift): X[k] - X[k - 1]
+            geo.dxm = __ldg(a.xpos + c.kx) - __ldg(a.xpos + c.kx - 1);
+            geo.dym = __ldg(a.ypos + c.ky) - __ldg(a.ypos + c.ky - 1);
+            if (NDIM == 3) geo.dzm = __ldg(a.zpos + c.kz) - __ldg(a.zpos + c.kz - 1);
+        }
+        const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
+        if (a.spherical) {
+            if (FT) push_ft<NDIM, true>(a, s, f, aux, k, geo, fixed_dt, d);
+            else if (NDIM == 2) push2d<true>(a, s, f, k, geo, fixed_dt, d);
+            else push3d<true>(a, s, f, k, geo, fixed_dt, d);
+        } else {
+            if (FT) push_ft<NDIM, false>(a, s, f, aux, k, geo, fixed_dt, d);
+            else if (NDIM == 2) push2d<false>(a, s, f, k, geo, fixed_dt, d);
+            else push3d<false>(a, s, f, k, geo, fixed_dt, d);
+        }
+        if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) ||
+            !isfinite(s.t) || (FT && (!isfinite(s.v) || !isfinite(s.mu)))) {
+            set_status(a.cnt, kStatusNonFinite);
+            return false;
+        }
+        return true;
+    }
     if (FULL) {
         double v[32];
         if (!interp<NDIM, 32, 32>(a, a.full1, a.full2, s, v)) return false;
@@ -753,9 +1089,10 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
         f = named_packed<NDIM>(v);
     }
     const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
-    if (FT) push_ft<NDIM>(a, s, f, aux, k, fixed_dt, d);
-    else if (NDIM == 2) push2d(a, s, f, k, fixed_dt, d);
-    else push3d(a, s, f, k, fixed_dt, d);
+    const Geo geo = {a.dx, a.dy, a.dz};
+    if (FT) push_ft<NDIM, false>(a, s, f, aux, k, geo, fixed_dt, d);
+    else if (NDIM == 2) push2d<false>(a, s, f, k, geo, fixed_dt, d);
+    else push3d<false>(a, s, f, k, geo, fixed_dt, d);
     if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) || !isfinite(s.t) ||
         (FT && (!isfinite(s.v) || !isfinite(s.mu)))) {
         set_status(a.cnt, kStatusNonFinite);
@@ -766,8 +1103,9 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
 
 // FT: focused transport.  FULL: interpolate all 32 variables (focused
 // transport and momentum diffusion read velocity gradients and density that
-// the packed records leave out).
-template <int NDIM, bool FT, bool FULL>
+// the packed records leave out).  GRID: spherical coordinates or non-uniform
+// node positions.
+template <int NDIM, bool FT, bool FULL, bool GRID>
 __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
     Acc acc = {0, 0, 0, 0, 0};
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -801,7 +1139,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 negp_or_boundary<NDIM>(a, s, acc);
                 if (s.flag != 1) break;
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
-                if (!do_push<NDIM, FT, FULL>(a, s, false, dl)) {
+                if (!do_push<NDIM, FT, FULL, GRID>(a, s, false, dl)) {
                     s.flag = 0; alive = false; break;
                 }
                 ++pushes;
@@ -822,7 +1160,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 s.dt = t0 + dt_target - s.t;
                 if (s.dt > 0.0) {
                     s.nsteps_pushed = s.nsteps_pushed - 1;
-                    if (!do_push<NDIM, FT, FULL>(a, s, true, dl)) {
+                    if (!do_push<NDIM, FT, FULL, GRID>(a, s, true, dl)) {
                         s.flag = 0; alive = false; break;
                     }
                     ++pushes;
@@ -867,15 +1205,20 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     const int64_t blocks = (a.n + threads - 1) / threads;
     const bool ft = a.focused_transport != 0;
     const bool full = ft || a.dpp_wave || a.dpp_shear || a.deltab_flag || a.correlation_flag;
+    const bool grid = a.spherical || a.nonuniform;
     const unsigned g = (unsigned)blocks;
     if (a.ndim == 2) {
-        if (ft) mover_fp64_kernel<2, true, true><<<g, threads, 0, s>>>(a);
-        else if (full) mover_fp64_kernel<2, false, true><<<g, threads, 0, s>>>(a);
-        else mover_fp64_kernel<2, false, false><<<g, threads, 0, s>>>(a);
+        if (grid && ft) mover_fp64_kernel<2, true, true, true><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<2, false, true, true><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<2, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<2, false, true, false><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<2, false, false, false><<<g, threads, 0, s>>>(a);
     } else {
-        if (ft) mover_fp64_kernel<3, true, true><<<g, threads, 0, s>>>(a);
-        else if (full) mover_fp64_kernel<3, false, true><<<g, threads, 0, s>>>(a);
-        else mover_fp64_kernel<3, false, false><<<g, threads, 0, s>>>(a);
+        if (grid && ft) mover_fp64_kernel<3, true, true, true><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<3, false, true, true><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<3, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<3, false, true, false><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<3, false, false, false><<<g, threads, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

@@ -4,6 +4,7 @@
 #include <cfloat>
 
 #include "device_common.cuh"
+#include "grid_common.cuh"
 
 namespace gpat {
 namespace {
@@ -47,8 +48,26 @@ __device__ double draw_p_power(const InjectArgs &a, InjStream &s) {
 // interp_fields of frame 1 at rt = 0 (mhd_data_parallel.f90:1751-1804) at a
 // point inside the box, FP64 accumulation over the corners in the movers'
 // order.
-__device__ void interp_frame1(const LargeArgs &g, int ndim, double x, double y, double z,
+__device__ bool interp_frame1(const LargeArgs &g, int ndim, double x, double y, double z,
                               double f[32]) {
+    if (g.spherical || g.nonuniform) {
+        // spherical / non-uniform corner and weights (:866-880)
+        GridCell c;
+        if (!grid_cell(ndim, g.spherical, g.xpos, g.nxg, g.ypos, g.nyg, g.zpos, g.nzg, x, y, z, c))
+            return false;
+        for (int v = 0; v < 32; ++v) f[v] = 0.0;
+        for (int k = 0; k < (ndim == 3 ? 2 : 1); ++k)
+            for (int j = 0; j < 2; ++j)
+                for (int i = 0; i < 2; ++i) {
+                    const double wc = c.w[k * 4 + j * 2 + i];
+                    const size_t cell = (size_t)(c.ix + i) +
+                                        (size_t)g.nxg * ((size_t)(c.iy + j) +
+                                                         (size_t)g.nyg * (size_t)(c.iz + k));
+                    const float *r = g.full + 32 * cell;
+                    for (int v = 0; v < 32; ++v) f[v] = f[v] + (double)__ldg(r + v) * wc;
+                }
+        return true;
+    }
     const double px = (x - g.gxmin) / g.dx, py = (y - g.gymin) / g.dy, pz = (z - g.gzmin) / g.dz;
     const int fx = (int)floor(px), fy = (int)floor(py), fz = (ndim == 3) ? (int)floor(pz) : 0;
     const double rx = (px - (double)(fx + 1)) + 1.0;
@@ -68,11 +87,29 @@ __device__ void interp_frame1(const LargeArgs &g, int ndim, double x, double y, 
                 const float *r = g.full + 32 * cell;
                 for (int v = 0; v < 32; ++v) f[v] = f[v] + (double)__ldg(r + v) * wc;
             }
+    return true;
 }
 
 // db2_slab(1) interpolated at a point (interp_magnetic_fluctuation,
 // mhd_data_parallel.f90:1806-1854, rt = 0), same weights as the fields.
-__device__ double interp_db2(const LargeArgs &g, int ndim, double x, double y, double z) {
+__device__ bool interp_db2(const LargeArgs &g, int ndim, double x, double y, double z,
+                           double &out) {
+    if (g.spherical || g.nonuniform) {
+        GridCell c;
+        if (!grid_cell(ndim, g.spherical, g.xpos, g.nxg, g.ypos, g.nyg, g.zpos, g.nzg, x, y, z, c))
+            return false;
+        double v = 0.0;
+        for (int k = 0; k < (ndim == 3 ? 2 : 1); ++k)
+            for (int j = 0; j < 2; ++j)
+                for (int i = 0; i < 2; ++i) {
+                    const size_t cell = (size_t)(c.ix + i) +
+                                        (size_t)g.nxg * ((size_t)(c.iy + j) +
+                                                         (size_t)g.nyg * (size_t)(c.iz + k));
+                    v = v + (double)__ldg(g.aux + 16 * cell) * c.w[k * 4 + j * 2 + i];
+                }
+        out = v;
+        return true;
+    }
     const double px = (x - g.gxmin) / g.dx, py = (y - g.gymin) / g.dy, pz = (z - g.gzmin) / g.dz;
     const int fx = (int)floor(px), fy = (int)floor(py), fz = (ndim == 3) ? (int)floor(pz) : 0;
     const double rx = (px - (double)(fx + 1)) + 1.0;
@@ -90,13 +127,36 @@ __device__ double interp_db2(const LargeArgs &g, int ndim, double x, double y, d
                                     (size_t)g.nxg * ((size_t)(iy + j) + (size_t)g.nyg * (size_t)(iz + k));
                 v = v + (double)__ldg(g.aux + 16 * cell) * w[k * 4 + j * 2 + i];
             }
-    return v;
+    out = v;
+    return true;
 }
 
 // The quantity each inject_particles_at_large_* tests, from interpolated
 // fields (:874-890, :1027-1044, :1305-1320, :1437); the divv test is on
-// -div v.
-__device__ double large_quantity(int quantity, int ndim, const double f[32]) {
+// -div v.  Spherical coordinates use the reference's spherical forms with
+// r = x, theta = y (its divv adds vz / (r sin theta), not dvz/dz / ...).
+__device__ double large_quantity(int quantity, int ndim, bool sph, double x, double y,
+                                 const double f[32]) {
+    if (sph) {
+        if (quantity == GPAT_LARGE_JZ) return fabs(f[23] + (f[5] - f[21]) / x);
+        if (quantity == GPAT_LARGE_ABSJ) {
+            const double ctheta = cos(y), stheta = sin(y), r = x;
+            const double t1 = (ctheta * f[6] + stheta * f[27] - f[25]) / (r * stheta);
+            const double t2 = (f[22] / stheta - f[6] - r * f[26]) / r;
+            const double t3 = (f[5] + r * f[23] - f[21]) / r;
+            return sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+        }
+        if (quantity == GPAT_LARGE_DIVV) {
+            double d = f[8] + 2.0 * f[0] / x;
+            if (ndim > 1) {
+                const double ctheta = cos(y), istheta = 1.0 / sin(y);
+                d = d + (f[12] + f[1] * ctheta * istheta) / x;
+                if (ndim > 2) d = d + f[2] * istheta / x;
+            }
+            return -d;
+        }
+        return f[3];
+    }
     if (quantity == GPAT_LARGE_JZ) return fabs(f[23] - f[21]);
     if (quantity == GPAT_LARGE_ABSJ) {
         const double a = f[25] - f[27], b = f[26] - f[22], c = f[21] - f[23];
@@ -155,11 +215,13 @@ __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
             if (x >= a.box[0] && x <= a.box[3] && y >= a.box[1] && y <= a.box[4] &&
                 z >= a.box[2] && z <= a.box[5]) {
                 if (g.quantity == GPAT_LARGE_DB2) {
-                    q = interp_db2(g, a.ndim, x, y, z);
+                    if (!interp_db2(g, a.ndim, x, y, z, q)) q = rho ? 0.0 : -3.0;
                 } else {
                     double f[32];
-                    interp_frame1(g, a.ndim, x, y, z, f);
-                    q = large_quantity(g.quantity, a.ndim, f);
+                    if (interp_frame1(g, a.ndim, x, y, z, f))
+                        q = large_quantity(g.quantity, a.ndim, g.spherical != 0, x, y, f);
+                    else
+                        q = rho ? 0.0 : -3.0;
                 }
             } else {
                 q = rho ? 0.0 : -3.0;
@@ -715,9 +777,18 @@ __global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, i
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double p = P.p[i], mu = P.mu[i];
-    const int ix = (int)floor((P.x[i] - a.xmin) / a.dxd) + 1;
-    const int iy = (int)floor((P.y[i] - a.ymin) / a.dyd) + 1;
-    const int iz = (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
+    int ix, iy, iz;
+    if (a.nonuniform) {
+        // (binarySearch_R(xpos_local, x) - 1) / rx + 1 (diagnostics.f90:790-792)
+        ix = (grid_count(a.xpos, a.nxg, P.x[i]) - 1) / a.rx + 1;
+        iy = (grid_count(a.ypos, a.nyg, P.y[i]) - 1) / a.ry + 1;
+        iz = (a.ndim == 3) ? (grid_count(a.zpos, a.nzg, P.z[i]) - 1) / a.rz + 1
+                           : (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
+    } else {
+        ix = (int)floor((P.x[i] - a.xmin) / a.dxd) + 1;
+        iy = (int)floor((P.y[i] - a.ymin) / a.dyd) + 1;
+        iz = (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
+    }
     const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
     const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
     if (ix < 1 || ix > a.nrx || iy < 1 || iy > a.nry || iz < 1 || iz > a.nrz) return;
@@ -729,7 +800,13 @@ __global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, i
                                                                         (size_t)a.nry * (iz - 1))));
     unsigned long long *b = bins + 3 * e;
     atomicAdd(b, 1ull);
-    atomic_add_fixed(b + 1, b + 2, P.weight[i]);
+    double w = P.weight[i];
+    if (a.spherical) {
+        // F = f p^2 r^2 (sin theta from 2D on), diagnostics.f90:765-772
+        w = w / (P.x[i] * P.x[i]);
+        if (a.ndim >= 2) w = w / sin(P.y[i]);
+    }
+    atomic_add_fixed(b + 1, b + 2, w);
 }
 
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
@@ -763,9 +840,11 @@ __global__ void count_large_kernel(const LargeArgs g, int ndim, double b0, doubl
         const int ix = (int)(i % g.nx) + 1;
         const int iy = (int)((i / g.nx) % g.ny) + 1;
         const int iz = (int)(i / ((int64_t)g.nx * g.ny)) + 1;
-        const double xp = g.dx * (double)(ix - 1) + g.gxmin;
-        const double yp = g.dy * (double)(iy - 1) + g.gymin;
-        const double zp = g.dz * (double)(iz - 1) + g.gzmin;
+        const bool grid = g.spherical || g.nonuniform;
+        // xpos_local(ix) is node ix + 1 of the ghost-padded positions
+        const double xp = grid ? g.xpos[ix + 1] : g.dx * (double)(ix - 1) + g.gxmin;
+        const double yp = grid ? g.ypos[iy + 1] : g.dy * (double)(iy - 1) + g.gymin;
+        const double zp = (grid && ndim == 3) ? g.zpos[iz + 1] : g.dz * (double)(iz - 1) + g.gzmin;
         bool in = xp > b0 && xp < b3;
         if (ndim > 1) in = in && yp > b1 && yp < b4;
         if (ndim > 2) in = in && zp > b2 && zp < b5;
@@ -774,7 +853,32 @@ __global__ void count_large_kernel(const LargeArgs g, int ndim, double b0, doubl
             const float *r = g.full + 32 * ((size_t)(ix + 1) + (size_t)g.nxg *
                                             ((size_t)(iy + 1) + (size_t)g.nyg * (size_t)cz));
             double q;
-            if (g.quantity == GPAT_LARGE_JZ) {
+            if (g.spherical && g.quantity == GPAT_LARGE_JZ) {
+                // :2226-2234, (by - dbx_dy) in single precision
+                const float t = r[5] - r[21];
+                q = fabs((double)r[23] + (double)t / xp);
+            } else if (g.spherical && g.quantity == GPAT_LARGE_ABSJ) {
+                // :2285-2303
+                const double stheta = sin(yp), ctheta = cos(yp);
+                const double t1 = (ctheta * (double)r[6] + stheta * (double)r[27] - (double)r[25]) /
+                                  (xp * stheta);
+                const double t2 = ((double)r[22] / stheta - (double)r[6] - xp * (double)r[26]) / xp;
+                const double t3 = ((double)r[5] - xp * (double)r[23] - (double)r[21]) / xp;
+                q = sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+            } else if (g.spherical && g.quantity == GPAT_LARGE_DIVV) {
+                // :2404-2420: ctheta and istheta are re-allocated over all
+                // ny + 4 nodes, so row iy reads node iy - 2 (memory iy - 1);
+                // the dvz/dz term is added from ndim > 1; 2.0 * vx is single.
+                const double yq = g.ypos[iy - 1];
+                const double ctheta = cos(yq), istheta = 1.0 / sin(yq);
+                const float vx2 = 2.0f * r[0];
+                double d = (double)r[8] + (double)vx2 / xp;
+                if (ndim > 1) {
+                    d = d + ((double)r[12] + (double)r[1] * ctheta * istheta) / xp;
+                    d = d + (double)r[16] * istheta / xp;
+                }
+                q = -d;
+            } else if (g.quantity == GPAT_LARGE_JZ) {
                 q = (double)fabsf(r[23] - r[21]);
             } else if (g.quantity == GPAT_LARGE_ABSJ) {
                 const float t1 = r[25] - r[27], t2 = r[26] - r[22], t3 = r[21] - r[23];

@@ -286,6 +286,34 @@ class Engine:
                                                    out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
 
+    def _grid_counts(self):
+        return [self.nxg, self.nyg, self.nzg][:self.params.ndim]
+
+    def set_grid_positions(self, xpos, ypos=None, zpos=None):
+        """Node positions of a non-uniform grid (ghost nodes included: nxg,
+        nyg, nzg values); set before calc_fields_gradients."""
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64)
+                for a in (xpos, ypos, zpos)]
+        for a, n in zip(keep, self._grid_counts()):
+            if a is None or len(a) != n:
+                raise ValueError(f"expected {n} grid positions")
+        ptrs = [None if a is None else a.ctypes.data_as(C.POINTER(C.c_double)) for a in keep]
+        self._check(self.lib.gpat_set_grid_positions(self.h, *ptrs))
+
+    def read_grid_positions(self, dir_mhd_data):
+        """read_global_grid_positions: <dir>xpos.dat, ypos.dat, zpos.dat."""
+        d = str(dir_mhd_data)
+        if not d.endswith("/"):
+            d += "/"
+        self._check(self.lib.gpat_read_grid_positions(self.h, d.encode()))
+
+    def get_grid_positions(self):
+        out = [np.zeros(n, np.float64) for n in self._grid_counts()]
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in out] + \
+               [None] * (3 - len(out))
+        self._check(self.lib.gpat_get_grid_positions(self.h, *ptrs))
+        return out
+
     def count_cells_large(self, quantity, qmin, part_box) -> int:
         """get_ncells_large_jz / _absj / _divv / _rho (quantity: _abi.LARGE_*)."""
         box = (C.c_double * 6)(*part_box)

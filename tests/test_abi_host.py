@@ -136,7 +136,8 @@ def test_create_rejects_out_of_scope_options(engine_lib):
                      (dict(deltab_flag=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(correlation_flag=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(include_3rd_dim=1), _abi.GPAT_ERR_UNSUPPORTED),
-                     (dict(spherical_coord=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(spherical_coord=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(nonuniform_grid=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(precision=7), _abi.GPAT_ERR_ARG),
                      (dict(nptl_max=0), _abi.GPAT_ERR_ARG),
                      (dict(npp_global=0), _abi.GPAT_ERR_ARG)):
