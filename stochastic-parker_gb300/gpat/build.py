@@ -4,7 +4,10 @@ The library is compiled in-tree into ``gpat/_lib/libgpat_engine.so`` with
 nvcc, one translation unit per process, then linked.  ``mover_fp64.cu`` and
 ``particles.cu`` are compiled with ``-fmad=false`` so the FP64 mover and the
 injection keep the reference's separately rounded operations; the
-split-precision mover contracts freely to FMA.
+split-precision mover contracts freely to FMA.  Host code is compiled with
+``-ffp-contract=off``: on Arm hosts the compiler would otherwise fuse the
+box and grid arithmetic (xmin + nx * dx, ...) into FMAs and the bounds the
+kernels receive would differ in the last bit from an x86 build.
 """
 from __future__ import annotations
 
@@ -45,6 +48,7 @@ def nvcc_path() -> str:
 def _compile(src: str, extra: list[str], nvcc: str, verbose_ptxas: bool, build_dir: Path) -> Path:
     out = build_dir / (src.replace(".", "_") + ".o")
     cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", str(INCLUDE), "-I", str(CSRC), *extra, "-c", str(CSRC / src), "-o", str(out)]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
@@ -67,7 +71,8 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines: dict | None
     side; load one with ``gpat._abi.load(path)``."""
     out_path = Path(lib_path) if lib_path else LIB_PATH
     srcs = [CSRC / s for s in SOURCES] + [INCLUDE / "gpat_engine.h",
-                                          CSRC / "gpat_internal.h", CSRC / "device_common.cuh"]
+                                          CSRC / "gpat_internal.h", CSRC / "device_common.cuh",
+                                          CSRC / "grid_common.cuh"]
     if out_path.exists() and not force and not defines:
         lib_mtime = out_path.stat().st_mtime
         if all(s.stat().st_mtime <= lib_mtime for s in srcs):
@@ -103,7 +108,7 @@ def build_driver(force: bool = False) -> Path:
     cxx = shutil.which("g++") or shutil.which("c++")
     if cxx is None:
         raise RuntimeError("no C++ compiler for gpat_run")
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), str(DRIVER_SRC),
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", str(INCLUDE), str(DRIVER_SRC),
            "-L", str(LIB_DIR), "-lgpat_engine", "-Wl,-rpath,$ORIGIN", "-o", str(DRIVER_PATH)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
