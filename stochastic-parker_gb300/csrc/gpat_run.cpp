@@ -41,6 +41,9 @@ struct Options {
     double jz_min = 100.0, absj_min = 5.0, divv_min = 10.0, rho_min = 5.0, db2_min = 0.03;
     long long ncells_large_db2_norm = 800;
     int deltab_flag = 0, correlation_flag = 0;   // -db, -co (stochastic-mhd.f90:859-866)
+    // -sc, -ug (stochastic-mhd.f90:883-890): Cartesian and non-uniform by
+    // default, as the reference's CLI; -ug 1 for a uniform grid.
+    int spherical_coord = 0, uniform_grid = 0;
     long long ncells_large_jz_norm = 800, ncells_large_absj_norm = 800;
     long long ncells_large_divv_norm = 800, ncells_large_rho_norm = 800;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
@@ -80,7 +83,8 @@ int parse(int argc, char **argv, Options &o) {
         {"-ys", "--ptl_ymin"}, {"-ye", "--ptl_ymax"}, {"-zs", "--ptl_zmin"}, {"-ze", "--ptl_zmax"},
         {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
         {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
-        {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-ft", "--focused_transport"},
+        {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-sc", "--spherical_coord"},
+        {"-ug", "--uniform_grid"}, {"-ft", "--focused_transport"},
         {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
         {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
         {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"},
@@ -134,6 +138,8 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--charge") o.charge = (int)d;
         else if (k == "--particle_v0") o.particle_v0 = d;
         else if (k == "--check_drift_2d") o.check_drift_2d = (int)d;
+        else if (k == "--spherical_coord") o.spherical_coord = (int)d;
+        else if (k == "--uniform_grid") o.uniform_grid = (int)d;
         else if (k == "--focused_transport") o.focused_transport = truthy(v);
         else if (k == "--nlgc") o.nlgc = truthy(v);
         else if (k == "--kperp_kpara") o.kperp_kpara = d;
@@ -251,7 +257,7 @@ int main(int argc, char **argv) {
     // Focused transport and momentum diffusion run on the FP64 mover unless
     // asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
-         o.correlation_flag) && !o.precision_set)
+         o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1) && !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
@@ -282,7 +288,12 @@ int main(int argc, char **argv) {
     p.tau0 = o.tau0_scattering;
     p.deltab_flag = o.deltab_flag;
     p.correlation_flag = o.correlation_flag;
+    // set_mhd_grid_type (:179)
+    p.spherical_coord = o.spherical_coord == 1 ? 1 : 0;
+    p.nonuniform_grid = o.uniform_grid == 1 ? 0 : 1;
     CHECK(gpat_create(&p, &cfg, o.device, &h));
+    // set_local_grid_positions (:186): xpos.dat, ypos.dat, zpos.dat
+    if (p.nonuniform_grid) CHECK(gpat_read_grid_positions(h, o.dir_mhd_data.c_str()));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
 
     // Frame tmin into farray1, gradients (:321, :350).

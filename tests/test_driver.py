@@ -41,7 +41,8 @@ def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
     cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
            "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
            "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
-           "--precision", precision, "--seed", str(SEED), "-ft", ".true." if ft else ".false.",
+           "--precision", precision, "--seed", str(SEED), "-ug", "1",
+           "-ft", ".true." if ft else ".false.",
            "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1"]
     return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
 
@@ -140,7 +141,7 @@ def test_driver_turbulence_and_db2_injection(tmp_path):
     cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
            "-ts", "0", "-te", "3", "-np", "300", "-nm", "40000", "-is", "0", "-in", "1",
            "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2", "--seed", str(SEED),
-           "-db", "1", "-co", "1", "-ib", ".true.", "-db2", "1.4", "-nb", "2000"]
+           "-db", "1", "-co", "1", "-ib", ".true.", "-db2", "1.4", "-nb", "2000", "-ug", "1"]
     r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     edges, f_drv, c_drv = _read_fdists(out / "fdists_0003.dat")
@@ -169,4 +170,68 @@ def test_driver_turbulence_and_db2_injection(tmp_path):
     assert injected > 0
     f, c = eng.calc_particle_distributions()
     assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_driver_spherical_nonuniform_grid(tmp_path):
+    """-sc 1 with the reference's default -ug 0: node positions from
+    xpos.dat / ypos.dat in the data directory (set_local_grid_positions,
+    stochastic-mhd.f90:186), the FP64 mover in spherical coordinates; f(p)
+    equals the same calls made from Python, bit for bit."""
+    from gpat.engine import make_mhd_config
+    nx, ny = 64, 32
+    rng = np.random.default_rng(4)
+    pos = []
+    for n, lo, hi in ((nx, 0.5, 1.5), (ny, 0.6, np.pi - 0.6)):
+        h = rng.uniform(0.7, 1.3, n + 3)
+        x = np.concatenate([[0.0], np.cumsum(h)])
+        pos.append(lo + (x - x[2]) * (hi - lo) / (x[n + 2] - x[2]))
+    cfg = make_mhd_config(nx, ny, 1, 0.5, 1.5, 0.6, np.pi - 0.6, dt_out=0.05)
+    data = tmp_path / "data"
+    data.mkdir()
+    (tmp_path / "config").mkdir()
+    out = tmp_path / "out"
+    out.mkdir()
+    fields.write_mhd_config(data / "mhd_config.dat", cfg)
+    frame = fields.planar_shock_2d(nx, ny, 0.5, 1.5, 0.6, np.pi - 0.6, r=3.0, w=0.02, x0=1.0,
+                                   db=fields.kolmogorov_az_2d(nx, ny, 1.0, 1.0, 0.5, 2 * np.pi,
+                                                              16 * np.pi, 2))
+    for t in range(3):
+        fields.write_mhd_data(data / f"mhd_data_{t:04d}", frame)
+    pos[0].tofile(data / "xpos.dat")
+    pos[1].tofile(data / "ypos.dat")
+    keys = dict(b0=1.0, p0=0.1, pmin=0.05, pmax=100.0, momentum_dependency=0, gamma_turb=5 / 3,
+                mag_dependency=0, kpara0=2e-3, kret=0.1, dt_min_rel=2e-3, dt_max_rel=5e-2)
+    lines = ["!< conf.dat written by the test"] + [f"{k} = {v!r}" for k, v in keys.items()]
+    lines += ["acc_region_flag = 0", "npp_global = 64", "nmu_global = 1", "pbcx = 1", "pbcy = 1",
+              "pbcz = 0"]
+    (tmp_path / "config" / "conf.dat").write_text("\n".join(lines) + "\n")
+    exe = build.build_driver()
+    cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
+           "-ts", "0", "-te", "2", "-np", "1500", "-nm", "20000", "-is", "0", "-df", "1",
+           "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2", "--seed", str(SEED), "-sc", "1",
+           "-nl", ".false."]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    edges, f_drv, c_drv = _read_fdists(out / "fdists_0002.dat")
+
+    prm = make_params(ndim=2, npp_global=64, nptl_max=20000, seed=SEED, precision=0, b0=1.0,
+                      drift1=4e7, drift2=2e8, charge=-1, pbcx=1, pbcy=1, spherical_coord=1,
+                      nonuniform_grid=1, **{k: v for k, v in keys.items() if k != "b0"})
+    eng = Engine(prm, cfg, 0)
+    eng.calc_tstamps_mhd(0, 2)
+    eng.read_grid_positions(data)
+    box = (0.5, 0.6, cfg.zmin, 0.5 + nx * cfg.dx, 0.6 + ny * cfg.dy, cfg.zmax)
+    for tf in range(3):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        if tf == 0:
+            continue
+        if tf == 1:
+            eng.inject_particles_spatial_uniform(1500, 1e-7, 1, 1.0, tf, box)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1)
+        eng.split_particle(2.72, 2.0, 10)
+    f, c = eng.calc_particle_distributions()
+    assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv) and c.sum() > 0
     eng.close()
