@@ -22,6 +22,7 @@ module gpat_gpu
         gpu_inject_particles_at_large_jz, gpu_inject_particles_at_large_absj, &
         gpu_inject_particles_at_large_divv, gpu_inject_particles_at_large_rho, &
         gpu_inject_particles_at_large_db2, gpu_read_magnetic_fluctuation, &
+        gpu_read_grid_positions, &
         gpu_read_correlation_length, &
         gpu_calc_escaped_distributions, gpu_reset_escaped_particles
 
@@ -108,6 +109,12 @@ module gpat_gpu
             type(c_ptr), value :: handle
             character(kind=c_char), dimension(*), intent(in) :: filename
             integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_read_grid_positions(handle, dirname) &
+                bind(c, name="gpat_read_grid_positions")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: dirname
         end function
         integer(c_int) function c_read_magnetic_fluctuation(handle, filename, var_flag) &
                 bind(c, name="gpat_read_magnetic_fluctuation")
@@ -288,6 +295,14 @@ module gpat_gpu
         call check(c_read_field_data(h, trim(filename)//c_null_char, int(var_flag, c_int)), &
             "read_field_data")
     end subroutine gpu_read_field_data
+
+    !< set_local_grid_positions for uniform_grid = 0 (mhd_data_parallel.f90:
+    !< 2087-2190): xpos.dat, ypos.dat, zpos.dat in dir_mhd_data
+    subroutine gpu_read_grid_positions(dir_mhd_data)
+        character(*), intent(in) :: dir_mhd_data
+        call check(c_read_grid_positions(h, trim(dir_mhd_data)//c_null_char), &
+            "read_grid_positions")
+    end subroutine gpu_read_grid_positions
 
     !< read_magnetic_fluctuation + calc_grad_sigma2_slab/_2d
     !< (mhd_data_parallel.f90:306-397, stochastic-mhd.f90:337-361)
