@@ -431,7 +431,10 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
     double ib1 = (b < DBL_EPSILON) ? 1.0 : 1.0 / b;
     const double ib2 = ib1 * ib1;
     const double ib3 = ib1 * ib2;
-    const int d3 = (pr->ndim == 3);
+    /* include_3rd_dim (2D data, 3D transport): the 3D tensor with the z
+     * derivatives zero and the 2D gradient terms (:2293-2350, :2564-2640). */
+    const int d3 = (pr->ndim == 3) || (pr->ndim == 2 && pr->include_3rd_dim);
+    const int full3 = (pr->ndim == 3);
     double kpara, kperp;
     double knorm_para = 1.0, knorm_perp = 1.0;
     if (!pr->nlgc) {
@@ -485,12 +488,12 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
     double T[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0};
     const double db[3] = {db_dx, db_dy, db_dz};
     const double g2 = pr->gamma_turb - 2.0;
-    for (int k = 0; k < 2 + d3; ++k) {
+    for (int k = 0; k < 2 + full3; ++k) {
         if (!pr->nlgc) {
             double dk = 0.0;
             if (pr->mag_dependency == 1)
                 /* the fixed-ratio 3D branch has no 1/B factor (:2406-2408) */
-                dk = d3 ? db[k] * g2 : db[k] * ib1 * g2;
+                dk = full3 ? db[k] * g2 : db[k] * ib1 * g2;
             if (dbf) dk = dk - s2[1 + k] / s2[0];
             if (lcf) dk = dk + (pr->gamma_turb - 1.0) * l1[1 + k] / l1[0];
             T[k] = kperp * dk;
@@ -559,6 +562,7 @@ typedef struct mover_ctx {
     double dt_min, dt_max, t0, dtf;
     uint32_t key[2];
     int sph, nonuni;       /* spherical_coord, nonuniform_grid             */
+    int i3;                /* include_3rd_dim of a 2D run                  */
 } mover_ctx;
 
 typedef struct ptl_state {
@@ -729,7 +733,7 @@ static double dpp_terms(const orc_params *pr, double p, const double *f, const d
         dpp = dpp + (p * va) * (p * va) / (9.0 * kap[K_KPARA]);
     }
     if (pr->dpp_shear) {
-        const int d3 = (pr->ndim == 3);
+        const int d3 = (pr->ndim == 3) || pr->include_3rd_dim;
         const double sxx = f[8] - divv / 3.0;
         const double syy = f[12] - divv / 3.0;
         const double szz = d3 ? f[16] - divv / 3.0 : -(divv / 3.0);
@@ -945,18 +949,20 @@ static void push_3d(const mover_ctx *c, ptl_state *s, const double *f, const dou
         if (dx_dt != 0.0 && dy_dt != 0.0 && dp_dt != 0.0) {
             const double sk = (skperp > 0.0) ? skperp : skpara;
             double a = 0.5 * dxm / skpara, m = a * a;
+            /* include_3rd_dim keeps the 2D limits (:4141-4175) */
+            const int z = !c->i3;
             if (c->sph) {
                 a = 0.5 * dym * s->x / skpara; if (a * a < m) m = a * a;
-                a = 0.5 * dzm * s->x * sin(s->y) / skpara; if (a * a < m) m = a * a;
+                if (z) { a = 0.5 * dzm * s->x * sin(s->y) / skpara; if (a * a < m) m = a * a; }
                 a = sk / dx_dt; if (a * a < m) m = a * a;
                 a = sk * g.ir / dy_dt; if (a * a < m) m = a * a;
-                a = sk * g.ir * g.istheta / dz_dt; if (a * a < m) m = a * a;
+                if (z) { a = sk * g.ir * g.istheta / dz_dt; if (a * a < m) m = a * a; }
             } else {
                 a = 0.5 * dym / skpara; if (a * a < m) m = a * a;
-                a = 0.5 * dzm / skpara; if (a * a < m) m = a * a;
+                if (z) { a = 0.5 * dzm / skpara; if (a * a < m) m = a * a; }
                 a = sk / dx_dt; if (a * a < m) m = a * a;
                 a = sk / dy_dt; if (a * a < m) m = a * a;
-                a = sk / dz_dt; if (a * a < m) m = a * a;
+                if (z) { a = sk / dz_dt; if (a * a < m) m = a * a; }
             }
             a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
             s->dt = m;
@@ -1294,12 +1300,22 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     double dx_dt, dy_dt, dz_dt, divv, bb_gradv, bv_gradv;
     if (c->sph) {
         const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
-        dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] +
-                (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * g.ctheta * ist +
-                 kap[K_DKXZ_DZ] * ist) * ir;
-        dy_dt = (vy + vby + vdy + kap[K_DKXY_DX]) * ir +
-                (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * g.ctheta * ist +
-                 kap[K_DKYZ_DZ] * ist) * g.ir2;
+        if (c->i3) {
+            /* push_particle_2d_include_3rd_ft (:4417-4425) */
+            dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] +
+                    (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * cot) * ir;
+        } else {
+            dx_dt = vx + vbx + vdx + kap[K_DKXX_DX] +
+                    (2.0 * kap[K_KXX] + kap[K_DKXY_DY] + kap[K_KXY] * g.ctheta * ist +
+                     kap[K_DKXZ_DZ] * ist) * ir;
+        }
+        if (c->i3)
+            dy_dt = (vy + vby + vdy + kap[K_DKXY_DX]) * ir +
+                    (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * cot) * g.ir2;
+        else
+            dy_dt = (vy + vby + vdy + kap[K_DKXY_DX]) * ir +
+                    (kap[K_KXY] + kap[K_DKYY_DY] + kap[K_KYY] * g.ctheta * ist +
+                     kap[K_DKYZ_DZ] * ist) * g.ir2;
         dz_dt = (vz + vbz + vdz + kap[K_DKXZ_DX]) * ist * ir +
                 (kap[K_KXZ] + kap[K_DKYZ_DY] + kap[K_DKZZ_DZ] * ist) * ist * g.ir2;
         divv = dvx_dx + (2.0 * vx + dvy_dy + vy * cot + dvz_dz * ist) * ir;
@@ -1336,14 +1352,17 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
                : -((bx * db_dx + by * db_dy + bz * db_dz) * ib2);
     double dmu_dt, duu, duu_du;
     calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
-    if (!fixed_dt) ft_time_step(c, s, kap, 3, cs, &g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    /* include_3rd_dim keeps the 2D limits (:4481-4532) */
+    if (!fixed_dt)
+        ft_time_step(c, s, kap, c->i3 ? 2 : 3, cs, &g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s->dt);
     double r[6];
     push_noise_n(c, s, r, c->sph);
     double dX, dY, dZ;
     if (c->sph) {
         double q[6];
-        spherical_noise_3d(kap, &g, 1, q);
+        /* the include_3rd_dim variant has no radicand guards (:4544-4560) */
+        spherical_noise_3d(kap, &g, !c->i3, q);
         dX = dx_dt * s->dt + (q[0] * r[0] + q[1] * r[1] + q[2] * r[4]) * sdt;
         dY = dy_dt * s->dt + (q[3] * r[1] + q[4] * r[4]) * sdt;
         dZ = dz_dt * s->dt + q[5] * r[4] * sdt;
@@ -1381,7 +1400,8 @@ static void boundary(const mover_ctx *c, ptl_state *s, double xlo, double xhi, d
             else s->y = s->y - yhi + ylo;
         }
     }
-    if (c->ndim == 3) {
+    /* z too for include_3rd_dim runs (:2084) */
+    if (c->ndim == 3 || c->i3) {
         if (s->z < zlo && s->flag == 1) {
             if (pr->pbcz) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -5; }
             else s->z = s->z - zlo + zhi;
@@ -1435,10 +1455,10 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
     }
     orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, ap, kap);
     if (c->pr->focused_transport) {
-        if (c->ndim == 2) push_2d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
+        if (c->ndim == 2 && !c->i3) push_2d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
         else push_3d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
     } else {
-        if (c->ndim == 2) push_2d(c, s, f, kap, &cs, fixed_dt, d);
+        if (c->ndim == 2 && !c->i3) push_2d(c, s, f, kap, &cs, fixed_dt, d);
         else push_3d(c, s, f, kap, &cs, fixed_dt, d);
     }
 }
@@ -1608,6 +1628,7 @@ static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *
     c->ymin1 = c->ymin - c->dy * 0.5; c->ymax1 = ymax + c->dy * 0.5;
     c->zmin1 = c->zmin - c->dz * 0.5; c->zmax1 = zmax + c->dz * 0.5;
     c->sph = pr->spherical_coord != 0;
+    c->i3 = pr->ndim == 2 && pr->include_3rd_dim != 0;
     c->nonuni = pr->nonuniform_grid != 0;
     if (c->nonuni) {
         /* :1535-1546: the half cells beyond the box are those of the first

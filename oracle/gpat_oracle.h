@@ -61,6 +61,10 @@ typedef struct orc_params {
     /* set_mhd_grid_type (mhd_config.f90:179-186); with either set, the node
      * positions come from orc_set_grid_positions. */
     int32_t spherical_coord, nonuniform_grid;
+    /* set_flags_params' include_3rd_dim (:294-306): a 2D run whose
+     * particles also move along z, pushed by push_particle_2d_include_3rd
+     * (_ft) (:3979-4610) */
+    int32_t include_3rd_dim;
 } orc_params;
 
 /* particle_type (particle_module.f90:38-50) as structure-of-arrays, plus the

@@ -40,7 +40,7 @@ class OrcParams(C.Structure):
         ("noise", i32), ("focused_transport", i32), ("nlgc", i32), ("dpp_wave", i32),
         ("duu0", d), ("kperp_kpara", d), ("dpp_shear", i32), ("weak_scattering", i32),
         ("tau0", d), ("deltab_flag", i32), ("correlation_flag", i32),
-        ("spherical_coord", i32), ("nonuniform_grid", i32),
+        ("spherical_coord", i32), ("nonuniform_grid", i32), ("include_3rd_dim", i32),
     ]
 
 # Mover arguments of the reference carried in OrcParams rather than in the
