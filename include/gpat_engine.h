@@ -88,9 +88,10 @@ typedef struct gpat_params {
      * spherical_coord / nonuniform_grid: the grid type of set_mhd_grid_type
      * (mhd_config.f90:179-186; x = r, y = theta, z = phi in spherical
      * coordinates; node positions through gpat_read_grid_positions or
-     * gpat_set_grid_positions when non-uniform).  These six need
-     * GPAT_PREC_FP64.  include_3rd_dim is rejected with
-     * GPAT_ERR_UNSUPPORTED. */
+     * gpat_set_grid_positions when non-uniform); include_3rd_dim: a 2D
+     * run whose particles also move along z with the 3D diffusion tensor
+     * (push_particle_2d_include_3rd / _ft, particle_module.f90:3979-4610;
+     * ndim must be 2).  These seven need GPAT_PREC_FP64. */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of

@@ -214,6 +214,7 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.zmin1 = a.zmin - c.dz * 0.5; a.zmax1 = a.zmax + c.dz * 0.5;
     a.spherical = p.spherical_coord ? 1 : 0;
     a.nonuniform = p.nonuniform_grid ? 1 : 0;
+    a.include_3rd = (p.ndim == 2 && p.include_3rd_dim) ? 1 : 0;
     a.xpos = h->dpos[0]; a.ypos = h->dpos[1]; a.zpos = h->dpos[2];
     if (p.nonuniform_grid) {
         // particle_mover_one_cycle (:1535-1546): the half cells beyond the
@@ -407,9 +408,9 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     *out = nullptr;
     const gpat_params_t &p = *params;
     if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
-    if (p.include_3rd_dim) return GPAT_ERR_UNSUPPORTED;
+    if (p.include_3rd_dim && p.ndim != 2) return GPAT_ERR_ARG;
     if ((p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag || p.spherical_coord ||
-         p.nonuniform_grid) &&
+         p.nonuniform_grid || p.include_3rd_dim) &&
         p.precision != GPAT_PREC_FP64)
         return GPAT_ERR_UNSUPPORTED;
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;

@@ -90,6 +90,7 @@ struct MoverArgs {
     // either is set.
     int spherical, nonuniform;
     const double *xpos, *ypos, *zpos;
+    int include_3rd;   // 2D run with transport along z (FP64 mover)
     DevCounters *cnt;
 };
 

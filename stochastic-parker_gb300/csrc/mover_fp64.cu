@@ -273,7 +273,9 @@ struct Kap {
 
 // aux: interpolated {db2_slab, db2_2d, lc_slab, lc_2d} x {value, d/dx, d/dy,
 // d/dz}, or nullptr; read when deltab_flag / correlation_flag are on.
-template <int NDIM, bool FT>
+// I3 (with NDIM = 3): include_3rd_dim of a 2D run, the 3D tensor with the z
+// derivatives zero and the 2D gradient terms (:2293-2350, :2564-2640).
+template <int NDIM, bool FT, bool I3 = false>
 __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, const Fld &f,
                                      const double *aux) {
     const bool dbf = a.deltab_flag && aux, lcf = a.correlation_flag && aux;
@@ -330,11 +332,11 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
     const double g2 = a.gamma_turb - 2.0;
     double T[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int d = 0; d < NDIM; ++d) {
+    for (int d = 0; d < (I3 ? 2 : NDIM); ++d) {
         if (!a.nlgc) {
             double dk = 0.0;
             // the fixed-ratio 3D branch has no 1/B factor (:2406-2408)
-            if (a.mag_dependency == 1) dk = (NDIM == 3) ? db[d] * g2 : db[d] * ib1 * g2;
+            if (a.mag_dependency == 1) dk = (NDIM == 3 && !I3) ? db[d] * g2 : db[d] * ib1 * g2;
             if (dbf) dk = dk - s2[1 + d] / s2[0];
             if (lcf) dk = dk + (a.gamma_turb - 1.0) * l1[1 + d] / l1[0];
             T[d] = kperp * dk;
@@ -588,8 +590,11 @@ __device__ __forceinline__ void push2d(const MoverArgs &a, State &s, const Fld &
     push_momentum(a, s, dp_dt, dpp, sdt, r[3], 2, d.p);
 }
 
-// push_particle_3d (:4625-4907), Cartesian or spherical (SPH).
-template <bool SPH>
+// push_particle_3d (:4625-4907), Cartesian or spherical (SPH); I3:
+// push_particle_2d_include_3rd (:3979-4266), the same with 2D field data
+// (z derivatives zero), the 2D time-step limits and the 2D acceleration
+// region.
+template <bool SPH, bool I3 = false>
 __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
                                        const Geo &geo, bool fixed_dt, Delta &d) {
     const double bx = f.bx, by = f.by, bz = f.bz;
@@ -642,16 +647,16 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
             double q = 0.5 * geo.dxm / skpara, m = q * q;
             if (SPH) {
                 q = 0.5 * geo.dym * s.x / skpara; if (q * q < m) m = q * q;
-                q = 0.5 * geo.dzm * s.x * sin(s.y) / skpara; if (q * q < m) m = q * q;
+                if (!I3) { q = 0.5 * geo.dzm * s.x * sin(s.y) / skpara; if (q * q < m) m = q * q; }
                 q = sk / dx_dt; if (q * q < m) m = q * q;
                 q = sk * g.ir / dy_dt; if (q * q < m) m = q * q;
-                q = sk * g.ir * g.istheta / dz_dt; if (q * q < m) m = q * q;
+                if (!I3) { q = sk * g.ir * g.istheta / dz_dt; if (q * q < m) m = q * q; }
             } else {
                 q = 0.5 * geo.dym / skpara; if (q * q < m) m = q * q;
-                q = 0.5 * geo.dzm / skpara; if (q * q < m) m = q * q;
+                if (!I3) { q = 0.5 * geo.dzm / skpara; if (q * q < m) m = q * q; }
                 q = sk / dx_dt; if (q * q < m) m = q * q;
                 q = sk / dy_dt; if (q * q < m) m = q * q;
-                q = sk / dz_dt; if (q * q < m) m = q * q;
+                if (!I3) { q = sk / dz_dt; if (q * q < m) m = q * q; }
             }
             q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
             s.dt = m;
@@ -683,7 +688,7 @@ __device__ __forceinline__ void push3d(const MoverArgs &a, State &s, const Fld &
     s.z = s.z + dZ;
     s.t = s.t + s.dt;
     d.x = dX; d.y = dY; d.z = dZ; d.v = 0.0; d.mu = 0.0;
-    push_momentum(a, s, dp_dt, dpp, sdt, r[3], 3, d.p);
+    push_momentum(a, s, dp_dt, dpp, sdt, r[3], I3 ? 2 : 3, d.p);
 }
 
 // calc_duu (:3116-3155) without delta-B or correlation length.
@@ -752,7 +757,7 @@ __device__ __forceinline__ void ft_time_step(const MoverArgs &a, State &s, const
 
 // Shared tail of push_particle_2d_ft / push_particle_3d_ft (:3920-3963,
 // :5280-5323); r[2] drives momentum diffusion, r[3] pitch-angle scattering.
-template <int NDIM>
+template <int NDIM, int ACC_NDIM = NDIM>
 __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, double dX, double dY,
                                              double dZ, double dp_dt, double dpp, double dmu_dt,
                                              double duu, double sdt, const double r[4], Delta &d) {
@@ -773,7 +778,7 @@ __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, doubl
         s.mu = -mu_max;
     }
     if (a.acc_region_flag == 1) {
-        if (in_acc_region(a, s, NDIM)) {
+        if (in_acc_region(a, s, ACC_NDIM)) {
             s.p = s.p + dP;
             s.v = s.v + dV;
         } else {
@@ -799,8 +804,11 @@ __device__ __forceinline__ void push_ft_tail(const MoverArgs &a, State &s, doubl
 
 // push_particle_2d_ft (:3626-3964) and push_particle_3d_ft (:4930-5324),
 // Cartesian or spherical (SPH).  The 3D spherical position noise draws a
-// third number (ran3), taken from the push's third Philox block.
-template <int NDIM, bool SPH>
+// third number (ran3), taken from the push's third Philox block.  I3 (with
+// NDIM = 3): push_particle_2d_include_3rd_ft (:4267-4610), the 3D push on 2D
+// field data with the 2D time-step limits, cot(theta) in the spherical r and
+// theta rates and no radicand guards in the spherical noise.
+template <int NDIM, bool SPH, bool I3 = false>
 __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld &f,
                                         const double *aux, const Kap &k, const Geo &geo,
                                         bool fixed_dt, Delta &d) {
@@ -913,10 +921,15 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
         if (SPH) {
             const double ir = g.ir, ist = g.istheta, cot = g.cot_theta;
             const double vx = f.vx, vy = f.vy, vz = f.vz;
-            dx_dt = vx + vbx + vdx + k.dkxx_dx +
-                    (2.0 * k.kxx + k.dkxy_dy + k.kxy * g.ctheta * ist + k.dkxz_dz * ist) * ir;
-            dy_dt = (vy + vby + vdy + k.dkxy_dx) * ir +
-                    (k.kxy + k.dkyy_dy + k.kyy * g.ctheta * ist + k.dkyz_dz * ist) * g.ir2;
+            if (I3) {
+                dx_dt = vx + vbx + vdx + k.dkxx_dx + (2.0 * k.kxx + k.dkxy_dy + k.kxy * cot) * ir;
+                dy_dt = (vy + vby + vdy + k.dkxy_dx) * ir + (k.kxy + k.dkyy_dy + k.kyy * cot) * g.ir2;
+            } else {
+                dx_dt = vx + vbx + vdx + k.dkxx_dx +
+                        (2.0 * k.kxx + k.dkxy_dy + k.kxy * g.ctheta * ist + k.dkxz_dz * ist) * ir;
+                dy_dt = (vy + vby + vdy + k.dkxy_dx) * ir +
+                        (k.kxy + k.dkyy_dy + k.kyy * g.ctheta * ist + k.dkyz_dz * ist) * g.ir2;
+            }
             dz_dt = (vz + vbz + vdz + k.dkxz_dx) * ist * ir +
                     (k.kxz + k.dkyz_dy + k.dkzz_dz * ist) * ist * g.ir2;
             divv = f.dvx_dx + (2.0 * vx + f.dvy_dy + vy * cot + f.dvz_dz * ist) * ir;
@@ -953,7 +966,8 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
     const double dpp = dpp_terms<NDIM>(a, s.p, f, k, b, divv, dp_dt);
     double dmu_dt, duu;
     calc_duu(a, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
-    if (!fixed_dt) ft_time_step<NDIM, SPH>(a, s, k, geo, g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
+    if (!fixed_dt)
+        ft_time_step<I3 ? 2 : NDIM, SPH>(a, s, k, geo, g, dx_dt, dy_dt, dz_dt, dp_dt, dmu_dt, duu);
     const double sdt = sqrt(s.dt);
     double r[6];
     if (SPH && NDIM == 3) noise6(a, s, r);
@@ -976,7 +990,7 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
         dZ = dz_dt * s.dt;
     } else if (SPH) {
         double P[6];
-        spherical_noise_3d<true>(k, g, P);
+        spherical_noise_3d<!I3>(k, g, P);
         dX = dx_dt * s.dt + (P[0] * r[0] + P[1] * r[1] + P[2] * r[4]) * sdt;
         dY = dy_dt * s.dt + (P[3] * r[1] + P[4] * r[4]) * sdt;
         dZ = dz_dt * s.dt + P[5] * r[4] * sdt;
@@ -987,7 +1001,7 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
         dY = dy_dt * s.dt + (-(byn * bzn * skperp * ibxyn * r[0]) + bxn * skperp * ibxyn * r[1]) * sdt;
         dZ = dz_dt * s.dt + bxyn * skperp * r[0] * sdt;
     }
-    push_ft_tail<NDIM>(a, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
+    push_ft_tail<NDIM, I3 ? 2 : NDIM>(a, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
 template <int NDIM>
@@ -1007,7 +1021,7 @@ __device__ __forceinline__ void boundary(const MoverArgs &a, State &s, double xl
         if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -4; }
         else s.y = s.y - yhi + ylo;
     }
-    if (NDIM == 3) {
+    if (NDIM == 3 || a.include_3rd) {   // z too for include_3rd_dim runs (:2084)
         if (s.z < zlo && s.flag == 1) {
             if (a.pbcz) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -5; }
             else s.z = s.z - zlo + zhi;
@@ -1028,7 +1042,25 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
     }
 }
 
-template <int NDIM, bool FT, bool FULL, bool GRID>
+// kappa and the push for interpolated fields f: NDIM-dimensional, or the 3D
+// push on 2D data for include_3rd_dim runs (I3).
+template <int NDIM, bool FT, bool SPH, bool I3>
+__device__ __forceinline__ void run_push(const MoverArgs &a, State &s, const Fld &f,
+                                         const double *aux, const Geo &geo, bool fixed_dt,
+                                         Delta &d) {
+    if (I3) {
+        const Kap k = kappa<3, FT, true>(a, s.p, s.mu, f, aux);
+        if (FT) push_ft<3, SPH, true>(a, s, f, aux, k, geo, fixed_dt, d);
+        else push3d<SPH, true>(a, s, f, k, geo, fixed_dt, d);
+    } else {
+        const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
+        if (FT) push_ft<NDIM, SPH>(a, s, f, aux, k, geo, fixed_dt, d);
+        else if (NDIM == 2) push2d<SPH>(a, s, f, k, geo, fixed_dt, d);
+        else push3d<SPH>(a, s, f, k, geo, fixed_dt, d);
+    }
+}
+
+template <int NDIM, bool FT, bool FULL, bool GRID, bool I3>
 __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed_dt, Delta &d) {
     Fld f;
     double av[16];
@@ -1056,16 +1088,8 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
             geo.dym = __ldg(a.ypos + c.ky) - __ldg(a.ypos + c.ky - 1);
             if (NDIM == 3) geo.dzm = __ldg(a.zpos + c.kz) - __ldg(a.zpos + c.kz - 1);
         }
-        const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
-        if (a.spherical) {
-            if (FT) push_ft<NDIM, true>(a, s, f, aux, k, geo, fixed_dt, d);
-            else if (NDIM == 2) push2d<true>(a, s, f, k, geo, fixed_dt, d);
-            else push3d<true>(a, s, f, k, geo, fixed_dt, d);
-        } else {
-            if (FT) push_ft<NDIM, false>(a, s, f, aux, k, geo, fixed_dt, d);
-            else if (NDIM == 2) push2d<false>(a, s, f, k, geo, fixed_dt, d);
-            else push3d<false>(a, s, f, k, geo, fixed_dt, d);
-        }
+        if (a.spherical) run_push<NDIM, FT, true, I3>(a, s, f, aux, geo, fixed_dt, d);
+        else run_push<NDIM, FT, false, I3>(a, s, f, aux, geo, fixed_dt, d);
         if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) ||
             !isfinite(s.t) || (FT && (!isfinite(s.v) || !isfinite(s.mu)))) {
             set_status(a.cnt, kStatusNonFinite);
@@ -1088,11 +1112,8 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
         if (!interp<NDIM, NV, R>(a, a.rec1, a.rec2, s, v)) return false;
         f = named_packed<NDIM>(v);
     }
-    const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
     const Geo geo = {a.dx, a.dy, a.dz};
-    if (FT) push_ft<NDIM, false>(a, s, f, aux, k, geo, fixed_dt, d);
-    else if (NDIM == 2) push2d<false>(a, s, f, k, geo, fixed_dt, d);
-    else push3d<false>(a, s, f, k, geo, fixed_dt, d);
+    run_push<NDIM, FT, false, I3>(a, s, f, aux, geo, fixed_dt, d);
     if (!isfinite(s.x) || !isfinite(s.y) || !isfinite(s.z) || !isfinite(s.p) || !isfinite(s.t) ||
         (FT && (!isfinite(s.v) || !isfinite(s.mu)))) {
         set_status(a.cnt, kStatusNonFinite);
@@ -1104,8 +1125,8 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
 // FT: focused transport.  FULL: interpolate all 32 variables (focused
 // transport and momentum diffusion read velocity gradients and density that
 // the packed records leave out).  GRID: spherical coordinates or non-uniform
-// node positions.
-template <int NDIM, bool FT, bool FULL, bool GRID>
+// node positions.  I3: a 2D run with transport along z (include_3rd_dim).
+template <int NDIM, bool FT, bool FULL, bool GRID, bool I3>
 __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
     Acc acc = {0, 0, 0, 0, 0};
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1139,7 +1160,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 negp_or_boundary<NDIM>(a, s, acc);
                 if (s.flag != 1) break;
                 if (pushes >= a.max_pushes) { set_status(a.cnt, kStatusStepLimit); alive = false; break; }
-                if (!do_push<NDIM, FT, FULL, GRID>(a, s, false, dl)) {
+                if (!do_push<NDIM, FT, FULL, GRID, I3>(a, s, false, dl)) {
                     s.flag = 0; alive = false; break;
                 }
                 ++pushes;
@@ -1160,7 +1181,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 s.dt = t0 + dt_target - s.t;
                 if (s.dt > 0.0) {
                     s.nsteps_pushed = s.nsteps_pushed - 1;
-                    if (!do_push<NDIM, FT, FULL, GRID>(a, s, true, dl)) {
+                    if (!do_push<NDIM, FT, FULL, GRID, I3>(a, s, true, dl)) {
                         s.flag = 0; alive = false; break;
                     }
                     ++pushes;
@@ -1207,18 +1228,25 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     const bool full = ft || a.dpp_wave || a.dpp_shear || a.deltab_flag || a.correlation_flag;
     const bool grid = a.spherical || a.nonuniform;
     const unsigned g = (unsigned)blocks;
-    if (a.ndim == 2) {
-        if (grid && ft) mover_fp64_kernel<2, true, true, true><<<g, threads, 0, s>>>(a);
-        else if (grid) mover_fp64_kernel<2, false, true, true><<<g, threads, 0, s>>>(a);
-        else if (ft) mover_fp64_kernel<2, true, true, false><<<g, threads, 0, s>>>(a);
-        else if (full) mover_fp64_kernel<2, false, true, false><<<g, threads, 0, s>>>(a);
-        else mover_fp64_kernel<2, false, false, false><<<g, threads, 0, s>>>(a);
+    if (a.ndim == 2 && a.include_3rd) {
+        // 2D data, 3D transport: all 32 variables (the pushes read vz and
+        // the in-plane gradients of bz and vz)
+        if (grid && ft) mover_fp64_kernel<2, true, true, true, true><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<2, false, true, true, true><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<2, true, true, false, true><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<2, false, true, false, true><<<g, threads, 0, s>>>(a);
+    } else if (a.ndim == 2) {
+        if (grid && ft) mover_fp64_kernel<2, true, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<2, false, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<2, true, true, false, false><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<2, false, true, false, false><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<2, false, false, false, false><<<g, threads, 0, s>>>(a);
     } else {
-        if (grid && ft) mover_fp64_kernel<3, true, true, true><<<g, threads, 0, s>>>(a);
-        else if (grid) mover_fp64_kernel<3, false, true, true><<<g, threads, 0, s>>>(a);
-        else if (ft) mover_fp64_kernel<3, true, true, false><<<g, threads, 0, s>>>(a);
-        else if (full) mover_fp64_kernel<3, false, true, false><<<g, threads, 0, s>>>(a);
-        else mover_fp64_kernel<3, false, false, false><<<g, threads, 0, s>>>(a);
+        if (grid && ft) mover_fp64_kernel<3, true, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<3, false, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<3, true, true, false, false><<<g, threads, 0, s>>>(a);
+        else if (full) mover_fp64_kernel<3, false, true, false, false><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<3, false, false, false, false><<<g, threads, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

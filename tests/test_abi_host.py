@@ -135,7 +135,8 @@ def test_create_rejects_out_of_scope_options(engine_lib):
                      (dict(dpp_shear=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(deltab_flag=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(correlation_flag=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
-                     (dict(include_3rd_dim=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(include_3rd_dim=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(include_3rd_dim=1, ndim=3, precision=0), _abi.GPAT_ERR_ARG),
                      (dict(spherical_coord=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(nonuniform_grid=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(precision=7), _abi.GPAT_ERR_ARG),

@@ -1,0 +1,92 @@
+"""2D runs with transport along z (include_3rd_dim): the CUDA FP64 mover
+against the oracle through the C ABI.  Without pow() (momentum- and
+|B|-independent kappa, no pitch-angle scattering) the trajectories are
+bit-exact; spherical runs are checked at 1e-9 relative (Parker) or 1e-5
+(focused transport, whose singular perpendicular tensor enters the noise at
+sqrt(eps)) on >= 99.5 % of particles."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from gpat.engine import Engine, ParticleSet, make_mhd_config, make_params
+from test_gpu_focused import FT_STATE, _same
+from test_gpu_parity import STATE, turbulent_frame_2d
+
+pytestmark = pytest.mark.gpu
+
+
+def _frame(n, lo, hi):
+    """The turbulent shock frame with an out-of-plane field and flow."""
+    f = turbulent_frame_2d(n).astype(np.float64)
+    x = np.linspace(lo[0], hi[0], n + 4)
+    y = np.linspace(lo[1], hi[1], n + 4)
+    X, Y = np.meshgrid(x, y)
+    f[0, :, :, 2] = 0.1 * np.sin(2 * np.pi * (X - lo[0]) / (hi[0] - lo[0]))
+    f[0, :, :, 6] = 0.4 + 0.2 * np.cos(2 * np.pi * (Y - lo[1]) / (hi[1] - lo[1]))
+    f[0, :, :, 7] = np.sqrt(f[0, :, :, 4] ** 2 + f[0, :, :, 5] ** 2 + f[0, :, :, 6] ** 2)
+    return f.astype(np.float32)
+
+
+def _run(spherical=False, mover_kw=None, nptl=3000, **kw):
+    n = 48
+    lo, hi = ((0.5, 0.6), (1.5, math.pi - 0.6)) if spherical else ((0.0, 0.0), (1.0, 1.0))
+    cfg = make_mhd_config(n, n, 1, lo[0], hi[0], lo[1], hi[1], zmin=0.0, zmax=1.0, dt_out=0.02)
+    frame = _frame(n, lo, hi)
+    base = dict(ndim=2, p0=0.1, pmin=0.05, pmax=100.0, kpara0=2e-3, kret=0.1, dt_min_rel=2e-3,
+                dt_max_rel=5e-2, pbcx=1, pbcy=0, pbcz=1, momentum_dependency=0, nptl_max=6000,
+                seed=41, precision=0, include_3rd_dim=1, spherical_coord=int(spherical))
+    base.update(kw)
+    prm = make_params(**base)
+    eng = Engine(prm, cfg, 0)
+    eng.set_tstamps(np.arange(4) * 0.02)
+    eng.set_fields(frame, 0)
+    eng.calc_fields_gradients(0)
+    box = (lo[0] + 0.1 * (hi[0] - lo[0]), lo[1] + 0.1 * (hi[1] - lo[1]), 0.3,
+           hi[0] - 0.1 * (hi[0] - lo[0]), hi[1] - 0.1 * (hi[1] - lo[1]), 0.7)
+    eng.inject_particles_spatial_uniform(nptl, 1e-6, 1, 2.0, 1, box)
+    start = eng.get_particles()
+    if spherical:
+        oracle.set_grid_positions(oracle.uniform_grid_positions(n + 4, cfg.dx, lo[0]),
+                                  oracle.uniform_grid_positions(n + 4, cfg.dy, lo[1]))
+    full = oracle.full_fields(frame, 2, cfg)
+    oprm, ocfg = oracle.params_from(prm), oracle.config_from(cfg)
+    parts = oracle.Particles(prm.nptl_max, start.arrays)
+    cnt = oracle.OrcCounters()
+    mover_kw = mover_kw or {}
+    for k in range(2):
+        eng.particle_mover(mhd_tframe=k + 1, **mover_kw)
+        oracle.mover(oprm, ocfg, full, parts, 0.02 * k, 0.02, counters=cnt, **mover_kw)
+    oracle.set_grid_positions(None)
+    return eng, eng.get_particles(), ParticleSet(parts.view()), cnt
+
+
+def test_include_3rd_parker_bit_exact():
+    eng, gpu, ref, cnt = _run()
+    _same(gpu, ref, STATE)
+    assert eng.counters().steps == cnt.steps
+    assert np.std(gpu["z"]) > 1e-3
+    eng.close()
+
+
+def test_include_3rd_nlgc_dpp_shear():
+    eng, gpu, ref, _ = _run(mover_kw=dict(nlgc=True, kperp_kpara=0.05), dpp_shear=1)
+    _same(gpu, ref, STATE, exact=False)
+    eng.close()
+
+
+def test_include_3rd_focused_transport_bit_exact():
+    eng, gpu, ref, _ = _run(mover_kw=dict(focused_transport=True), duu0=0.0)
+    _same(gpu, ref, FT_STATE)
+    eng.close()
+
+
+def test_include_3rd_spherical():
+    eng, gpu, ref, _ = _run(spherical=True)
+    _same(gpu, ref, STATE, exact=False)
+    eng.close()
+    eng, gpu, ref, _ = _run(spherical=True, mover_kw=dict(focused_transport=True), duu0=3.0,
+                            nptl=2000)
+    _same(gpu, ref, FT_STATE, exact=False, rtol=1e-5)
+    eng.close()
