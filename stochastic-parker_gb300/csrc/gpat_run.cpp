@@ -44,6 +44,7 @@ struct Options {
     // -sc, -ug (stochastic-mhd.f90:883-890): Cartesian and non-uniform by
     // default, as the reference's CLI; -ug 1 for a uniform grid.
     int spherical_coord = 0, uniform_grid = 0;
+    int include_3rd_dim = 0;   // -i3 (stochastic-mhd.f90:899-902)
     long long ncells_large_jz_norm = 800, ncells_large_absj_norm = 800;
     long long ncells_large_divv_norm = 800, ncells_large_rho_norm = 800;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
@@ -84,7 +85,7 @@ int parse(int argc, char **argv, Options &o) {
         {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
         {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
         {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-sc", "--spherical_coord"},
-        {"-ug", "--uniform_grid"}, {"-ft", "--focused_transport"},
+        {"-ug", "--uniform_grid"}, {"-i3", "--include_3rd_dim"}, {"-ft", "--focused_transport"},
         {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
         {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
         {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"},
@@ -140,6 +141,7 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--check_drift_2d") o.check_drift_2d = (int)d;
         else if (k == "--spherical_coord") o.spherical_coord = (int)d;
         else if (k == "--uniform_grid") o.uniform_grid = (int)d;
+        else if (k == "--include_3rd_dim") o.include_3rd_dim = (int)d;
         else if (k == "--focused_transport") o.focused_transport = truthy(v);
         else if (k == "--nlgc") o.nlgc = truthy(v);
         else if (k == "--kperp_kpara") o.kperp_kpara = d;
@@ -257,7 +259,8 @@ int main(int argc, char **argv) {
     // Focused transport and momentum diffusion run on the FP64 mover unless
     // asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
-         o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1) && !o.precision_set)
+         o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1 ||
+         o.include_3rd_dim == 1) && !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
@@ -291,6 +294,7 @@ int main(int argc, char **argv) {
     // set_mhd_grid_type (:179)
     p.spherical_coord = o.spherical_coord == 1 ? 1 : 0;
     p.nonuniform_grid = o.uniform_grid == 1 ? 0 : 1;
+    p.include_3rd_dim = (o.include_3rd_dim == 1 && o.ndim_field == 2) ? 1 : 0;
     CHECK(gpat_create(&p, &cfg, o.device, &h));
     // set_local_grid_positions (:186): xpos.dat, ypos.dat, zpos.dat
     if (p.nonuniform_grid) CHECK(gpat_read_grid_positions(h, o.dir_mhd_data.c_str()));
