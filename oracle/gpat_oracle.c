@@ -567,6 +567,7 @@ typedef struct mover_ctx {
 
 typedef struct ptl_state {
     double x, y, z, p, v, mu, t, dt, weight;
+    double h1, h2;   /* acceleration-surface heights at the push's start */
     int flag;
     int32_t nsteps_pushed, tag_injected, tag_splitted;
     uint32_t rng_ctr;
@@ -691,6 +692,98 @@ static void spherical_noise_3d(const double *kap, const sph_terms *g, int clamp,
 }
 
 /* particle_in_acceleration_region: particle_module.f90:2885-2906. */
+/* ------------------------------------------------------------------------ */
+/* Surfaces separating the acceleration region in 3D runs                    */
+/* (acc_region_surface.f90): heights over the plane normal to one axis,      */
+/* ghost-padded, the first index fastest.                                    */
+/* ------------------------------------------------------------------------ */
+static struct {
+    int on, has2, intersection;
+    int axis[2], sign[2];      /* normal axis 0/1/2; +1: the region is above */
+    int ld[2];                 /* leading dimension of each surface array     */
+    double *h[2][2];           /* [surface][slot]                             */
+} g_surf;
+
+static int surf_ld(int axis, int nxg, int nyg)
+{
+    return axis == 0 ? nyg : nxg;   /* x: (nyg, nzg); y: (nxg, nzg); z: (nxg, nyg) */
+}
+
+void orc_set_acc_surface(int axis1, int sign1, int axis2, int sign2, int has2, int intersection,
+                         const double *s11, const double *s12, const double *s21,
+                         const double *s22, int nxg, int nyg, int nzg)
+{
+    for (int k = 0; k < 2; ++k)
+        for (int t = 0; t < 2; ++t) {
+            free(g_surf.h[k][t]);
+            g_surf.h[k][t] = NULL;
+        }
+    g_surf.on = s11 != NULL;
+    if (!g_surf.on) return;
+    g_surf.has2 = has2 && s21;
+    g_surf.intersection = intersection;
+    g_surf.axis[0] = axis1; g_surf.sign[0] = sign1;
+    g_surf.axis[1] = axis2; g_surf.sign[1] = sign2;
+    const int n[3] = {nxg, nyg, nzg};
+    const double *src[2][2] = {{s11, s12}, {s21, s22}};
+    for (int k = 0; k < 1 + g_surf.has2; ++k) {
+        const int ax = g_surf.axis[k];
+        g_surf.ld[k] = surf_ld(ax, nxg, nyg);
+        const size_t cnt = (size_t)g_surf.ld[k] * (size_t)(ax == 2 ? n[1] : n[2]);
+        for (int t = 0; t < 2; ++t) {
+            const double *q = src[k][t] ? src[k][t] : src[k][0];
+            g_surf.h[k][t] = (double *)malloc(sizeof(double) * cnt);
+            memcpy(g_surf.h[k][t], q, sizeof(double) * cnt);
+        }
+    }
+}
+
+/* interp_acc_surface (acc_region_surface.f90:255-335): the 3D weights
+ * summed along the normal, Fortran sum order over the 2 x 2 corners. */
+static double surface_height(int k, const int32_t pos[3], const double w[8], double rt,
+                             int time_interp)
+{
+    const int ax = g_surf.axis[k];
+    int i1, j1;
+    double w2[4];   /* (1,1) (2,1) (1,2) (2,2) */
+    if (ax == 0) {
+        i1 = pos[1] + 1; j1 = pos[2] + 1;
+        w2[0] = w[0] + w[1]; w2[1] = w[2] + w[3]; w2[2] = w[4] + w[5]; w2[3] = w[6] + w[7];
+    } else if (ax == 1) {
+        i1 = pos[0] + 1; j1 = pos[2] + 1;
+        w2[0] = w[0] + w[2]; w2[1] = w[1] + w[3]; w2[2] = w[4] + w[6]; w2[3] = w[5] + w[7];
+    } else {
+        i1 = pos[0] + 1; j1 = pos[1] + 1;
+        w2[0] = w[0] + w[4]; w2[1] = w[1] + w[5]; w2[2] = w[2] + w[6]; w2[3] = w[3] + w[7];
+    }
+    double hs[2];
+    for (int t = 0; t < 1 + (time_interp != 0); ++t) {
+        const double *a = g_surf.h[k][t];
+        const size_t ld = (size_t)g_surf.ld[k];
+        double sum = 0.0;
+        sum = sum + a[(size_t)i1 + ld * (size_t)j1] * w2[0];
+        sum = sum + a[(size_t)i1 + 1 + ld * (size_t)j1] * w2[1];
+        sum = sum + a[(size_t)i1 + ld * (size_t)(j1 + 1)] * w2[2];
+        sum = sum + a[(size_t)i1 + 1 + ld * (size_t)(j1 + 1)] * w2[3];
+        hs[t] = sum;
+    }
+    return time_interp ? hs[0] * (1.0 - rt) + hs[1] * rt : hs[0];
+}
+
+/* check_above_acc_surface (acc_region_surface.f90:343-383). */
+static int above_surfaces(const ptl_state *s)
+{
+    const double xyz[3] = {s->x, s->y, s->z};
+    double ph = xyz[g_surf.axis[0]];
+    int in = g_surf.sign[0] > 0 ? ph > s->h1 : ph < s->h1;
+    if (g_surf.has2) {
+        ph = xyz[g_surf.axis[1]];
+        const int in2 = g_surf.sign[1] > 0 ? ph > s->h2 : ph < s->h2;
+        in = g_surf.intersection ? (in && in2) : (in || in2);
+    }
+    return in;
+}
+
 static int in_acc_region(const mover_ctx *c, const ptl_state *s)
 {
     const double *a = c->pr->acc_region;
@@ -703,6 +796,8 @@ static int in_acc_region(const mover_ctx *c, const ptl_state *s)
     if (c->ndim == 3) {
         const double zn = (s->z - c->cfg_zmin) / c->cfg_lz;
         in = in && (zn >= a[4]) && (zn <= a[5]);
+        /* push_particle_3d / _3d_ft with acc_by_surface (:4889-4893) */
+        if (g_surf.on) in = in && above_surfaces(s);
     }
     return in;
 }
@@ -1449,6 +1544,10 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
                                  (s->z - c->zmin) / c->dz, pos, w);
     }
     orc_interp_fields(c->f1, c->f2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, f);
+    if (c->ndim == 3 && g_surf.on) {
+        s->h1 = surface_height(0, pos, w, rt, c->time_interp);
+        s->h2 = g_surf.has2 ? surface_height(1, pos, w, rt, c->time_interp) : 0.0;
+    }
     if (c->aux1 && (c->pr->deltab_flag || c->pr->correlation_flag)) {
         orc_interp_aux(c->aux1, c->aux2, c->time_interp, c->ndim, c->nxg, c->nyg, pos, w, rt, aux);
         ap = aux;

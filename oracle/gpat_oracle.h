@@ -176,6 +176,15 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
 void orc_quick_check(const orc_particles *ptl, int64_t n, double out[4]);
 void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *counts,
                                uint64_t *whi, uint64_t *wlo);
+/* init_acc_surface / read_acc_surface for 3D runs
+ * (acc_region_surface.f90:27-249): surface k has normal axis axisk
+ * (0 x, 1 y, 2 z) and sign +1 when the acceleration region lies above it;
+ * arrays are ghost-padded (nyg, nzg), (nxg, nzg) or (nxg, nyg), the first
+ * index fastest, for frame 1 (s11, s21) and frame 2 (s12, s22, NULL: the
+ * same).  s11 NULL turns the surfaces off. */
+void orc_set_acc_surface(int axis1, int sign1, int axis2, int sign2, int has2, int intersection,
+                         const double *s11, const double *s12, const double *s21,
+                         const double *s22, int nxg, int nyg, int nzg);
 void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
                                  int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,

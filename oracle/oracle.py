@@ -141,6 +141,7 @@ def load() -> C.CDLL:
                                                     P(OrcParticles), i64, P(u64), P(u64), P(u64),
                                                     P(d)]
         lib.orc_set_grid_positions.argtypes = [P(d), P(d), P(d), C.c_int, C.c_int, C.c_int]
+        lib.orc_set_acc_surface.argtypes = [C.c_int] * 6 + [P(d)] * 4 + [C.c_int] * 3
         lib.orc_uniform_grid_positions.argtypes = [C.c_int, d, d, P(d)]
         lib.orc_binary_search.restype = C.c_int
         lib.orc_binary_search.argtypes = [P(d), C.c_int, d]
@@ -228,6 +229,26 @@ def uniform_grid_positions(n: int, step: float, origin: float) -> np.ndarray:
     out = np.zeros(n, np.float64)
     load().orc_uniform_grid_positions(n, step, origin, out.ctypes.data_as(P(d)))
     return out
+
+
+_AXES = {"x": 0, "y": 1, "z": 2}
+
+
+def set_acc_surface(norm1=None, s11=None, s12=None, norm2=None, s21=None, s22=None,
+                    intersection=True, shape=(0, 0, 0)) -> None:
+    """Acceleration-region surfaces of 3D runs; norm1 = "+y" etc., the
+    arrays ghost-padded with the first index fastest (numpy arrays of shape
+    (n2, n1)); shape = (nxg, nyg, nzg).  norm1 None turns them off."""
+    if norm1 is None:
+        load().orc_set_acc_surface(0, 0, 0, 0, 0, 0, None, None, None, None, 0, 0, 0)
+        return
+    keep = [None if a is None else np.ascontiguousarray(a, np.float64)
+            for a in (s11, s12, s21, s22)]
+    ptr = [None if a is None else a.ctypes.data_as(P(d)) for a in keep]
+    sgn = lambda n: 1 if n[0] == "+" else -1
+    n2 = norm2 or norm1
+    load().orc_set_acc_surface(_AXES[norm1[1]], sgn(norm1), _AXES[n2[1]], sgn(n2),
+                               int(norm2 is not None), int(intersection), *ptr, *shape)
 
 
 def binary_search(a, v: float) -> int:
