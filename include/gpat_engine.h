@@ -197,6 +197,24 @@ int gpat_set_grid_positions(gpat_handle_t *h, const double *xpos, const double *
                             const double *zpos);
 int gpat_read_grid_positions(gpat_handle_t *h, const char *dir_mhd_data);
 int gpat_get_grid_positions(gpat_handle_t *h, double *xpos, double *ypos, double *zpos);
+/* Surfaces separating the acceleration region of 3D runs (acc_by_surface;
+ * init_acc_surface / read_acc_surface / interp_acc_surface /
+ * check_above_acc_surface, acc_region_surface.f90:27-383).  norm1/norm2:
+ * "+x" .. "-z", the normal axis and the side of the region ("+": above);
+ * norm2 NULL for one surface; is_intersection: both conditions (1) or
+ * either (0).  Heights are doubles over the ghost-padded plane normal to
+ * the axis, (nyg, nzg), (nxg, nzg) or (nxg, nyg) with the first index
+ * fastest, all 0 until set; var_flag 0 is frame 1, otherwise frame 2
+ * (copied to frame 1 by gpat_copy_fields).  With acc_region_flag = 1 a
+ * push then changes p only inside the box region and on the region's side
+ * of the surfaces, interpolated at the push's start.  3D and
+ * GPAT_PREC_FP64 only. */
+int gpat_init_acc_surface(gpat_handle_t *h, const char *norm1, const char *norm2,
+                          int is_intersection);
+int gpat_set_acc_surface(gpat_handle_t *h, int var_flag, const double *surface1,
+                         const double *surface2);
+int gpat_read_acc_surface(gpat_handle_t *h, int var_flag, const char *filename1,
+                          const char *filename2);
 /* copy_fields (mhd_data_parallel.f90:1920-1926): farray1 = farray2. */
 int gpat_copy_fields(gpat_handle_t *h);
 /* Copies a device field array (32 vars per cell, Fortran order) to the host. */

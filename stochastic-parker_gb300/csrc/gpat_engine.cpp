@@ -35,6 +35,11 @@ struct gpat_handle {
     std::vector<double> gpos[3];
     double *dpos[3] = {nullptr, nullptr, nullptr};
     double *dih[3] = {nullptr, nullptr, nullptr};
+    // Acceleration-region surfaces (init_acc_surface): [surface][slot].
+    bool surf_on = false, surf_has2 = false, surf_inter = true;
+    int surf_axis[2] = {0, 0}, surf_sign[2] = {1, 1};
+    size_t surf_n[2] = {0, 0}, surf_ld[2] = {0, 0};
+    double *dsurf[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     bool fields_set[2] = {false, false};
     bool rec_ready[2] = {false, false};
     // particles (double-buffered SoA)
@@ -215,6 +220,16 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.spherical = p.spherical_coord ? 1 : 0;
     a.nonuniform = p.nonuniform_grid ? 1 : 0;
     a.include_3rd = (p.ndim == 2 && p.include_3rd_dim) ? 1 : 0;
+    a.surf_on = h->surf_on ? 1 : 0;
+    a.surf_has2 = h->surf_has2 ? 1 : 0;
+    a.surf_inter = h->surf_inter ? 1 : 0;
+    for (int k = 0; k < 2; ++k) {
+        a.surf_axis[k] = h->surf_axis[k];
+        a.surf_sign[k] = h->surf_sign[k];
+        a.surf_ld[k] = (int)h->surf_ld[k];
+        a.surf[k][0] = h->dsurf[k][0];
+        a.surf[k][1] = p.time_interp ? h->dsurf[k][1] : h->dsurf[k][0];
+    }
     a.xpos = h->dpos[0]; a.ypos = h->dpos[1]; a.zpos = h->dpos[2];
     if (p.nonuniform_grid) {
         // particle_mover_one_cycle (:1535-1546): the half cells beyond the
@@ -513,6 +528,9 @@ int gpat_destroy(gpat_handle_t *h) {
         if (h->dpos[ax]) cudaFree(h->dpos[ax]);
         if (h->dih[ax]) cudaFree(h->dih[ax]);
     }
+    for (int k = 0; k < 2; ++k)
+        for (int t = 0; t < 2; ++t)
+            if (h->dsurf[k][t]) cudaFree(h->dsurf[k][t]);
     for (int s = 0; s < 2; ++s) {
         if (h->pmem[s]) cudaFree(h->pmem[s]);
     }
@@ -682,6 +700,82 @@ int gpat_get_grid_positions(gpat_handle_t *h, double *xpos, double *ypos, double
     return GPAT_OK;
 }
 
+namespace {
+// "+x" ... "-z": sign and normal axis of a surface (surface_norm1/2).
+bool parse_norm(const char *n, int &sign, int &axis) {
+    if (!n || (n[0] != '+' && n[0] != '-') || n[1] < 'x' || n[1] > 'z' || n[2] != '\0')
+        return false;
+    sign = n[0] == '+' ? 1 : -1;
+    axis = n[1] - 'x';
+    return true;
+}
+}  // namespace
+
+int gpat_init_acc_surface(gpat_handle_t *h, const char *norm1, const char *norm2,
+                          int is_intersection) {
+    if (!h) return GPAT_ERR_ARG;
+    if (h->prm.ndim != 3) return fail(h, GPAT_ERR_UNSUPPORTED, "acceleration surfaces are 3D only");
+    if (h->prm.precision != GPAT_PREC_FP64)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "acceleration surfaces need GPAT_PREC_FP64");
+    if (h->surf_on) return fail(h, GPAT_ERR_STATE, "acceleration surfaces already set up");
+    int sg[2], ax[2];
+    if (!parse_norm(norm1, sg[0], ax[0]) || (norm2 && !parse_norm(norm2, sg[1], ax[1])))
+        return fail(h, GPAT_ERR_ARG, "surface norms are +x, -x, +y, -y, +z or -z");
+    if (!norm2) { sg[1] = sg[0]; ax[1] = ax[0]; }
+    CK(cudaSetDevice(h->device));
+    const int ng[3] = {h->nxg, h->nyg, h->nzg};
+    for (int k = 0; k < (norm2 ? 2 : 1); ++k) {
+        // (nyg, nzg) for x, (nxg, nzg) for y, (nxg, nyg) for z (:38-89)
+        h->surf_ld[k] = (size_t)(ax[k] == 0 ? ng[1] : ng[0]);
+        h->surf_n[k] = h->surf_ld[k] * (size_t)(ax[k] == 2 ? ng[1] : ng[2]);
+        for (int t = 0; t < h->nslots; ++t) {
+            CK(cudaMalloc(&h->dsurf[k][t], sizeof(double) * h->surf_n[k]));
+            CK(cudaMemsetAsync(h->dsurf[k][t], 0, sizeof(double) * h->surf_n[k], h->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 2; ++k) { h->surf_sign[k] = sg[k]; h->surf_axis[k] = ax[k]; }
+    h->surf_has2 = norm2 != nullptr;
+    h->surf_inter = is_intersection != 0;
+    h->surf_on = true;
+    return GPAT_OK;
+}
+
+int gpat_set_acc_surface(gpat_handle_t *h, int var_flag, const double *surface1,
+                         const double *surface2) {
+    if (!h || !surface1) return GPAT_ERR_ARG;
+    if (!h->surf_on) return fail(h, GPAT_ERR_STATE, "gpat_init_acc_surface first");
+    if (h->surf_has2 && !surface2) return fail(h, GPAT_ERR_ARG, "surface 2 is missing");
+    const int slot = var_flag == 0 ? 0 : 1;
+    if (slot >= h->nslots) return fail(h, GPAT_ERR_STATE, "slot 1 needs time_interp = 1");
+    CK(cudaSetDevice(h->device));
+    const double *src[2] = {surface1, surface2};
+    for (int k = 0; k < (h->surf_has2 ? 2 : 1); ++k)
+        CK(cudaMemcpyAsync(h->dsurf[k][slot], src[k], sizeof(double) * h->surf_n[k],
+                           cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+int gpat_read_acc_surface(gpat_handle_t *h, int var_flag, const char *filename1,
+                          const char *filename2) {
+    if (!h || !filename1) return GPAT_ERR_ARG;
+    if (!h->surf_on) return fail(h, GPAT_ERR_STATE, "gpat_init_acc_surface first");
+    const char *names[2] = {filename1, filename2};
+    std::vector<double> v[2];
+    for (int k = 0; k < (h->surf_has2 ? 2 : 1); ++k) {
+        if (!names[k]) return fail(h, GPAT_ERR_ARG, "surface 2 file is missing");
+        FILE *f = std::fopen(names[k], "rb");
+        if (!f) return fail(h, GPAT_ERR_IO, std::string("cannot open ") + names[k]);
+        v[k].resize(h->surf_n[k]);
+        const size_t got = std::fread(v[k].data(), sizeof(double), v[k].size(), f);
+        std::fclose(f);
+        if (got != v[k].size())
+            return fail(h, GPAT_ERR_IO, std::string("short surface file ") + names[k]);
+    }
+    return gpat_set_acc_surface(h, var_flag, v[0].data(), h->surf_has2 ? v[1].data() : nullptr);
+}
+
 int gpat_read_field_data(gpat_handle_t *h, const char *filename, int var_flag) {
     if (!h || !filename) return GPAT_ERR_ARG;
     FILE *f = std::fopen(filename, "rb");
@@ -719,6 +813,10 @@ int gpat_copy_fields(gpat_handle_t *h) {
     if (h->aux[0] && h->aux[1])   // copy_magnetic_fluctuation / copy_correlation_length
         CK(cudaMemcpyAsync(h->aux[0], h->aux[1], 16 * sizeof(float) * h->ncells,
                            cudaMemcpyDeviceToDevice, h->stream));
+    for (int k = 0; k < 2; ++k)   // copy_acc_surface
+        if (h->dsurf[k][0] && h->dsurf[k][1])
+            CK(cudaMemcpyAsync(h->dsurf[k][0], h->dsurf[k][1], sizeof(double) * h->surf_n[k],
+                               cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->fields_set[0] = h->fields_set[1];
     h->rec_ready[0] = h->rec_ready[1];

@@ -91,6 +91,13 @@ struct MoverArgs {
     int spherical, nonuniform;
     const double *xpos, *ypos, *zpos;
     int include_3rd;   // 2D run with transport along z (FP64 mover)
+    // Acceleration-region surfaces of 3D runs (acc_by_surface): heights over
+    // the plane normal to surf_axis[k] (0 x, 1 y, 2 z), ghost-padded with
+    // leading dimension surf_ld[k], for frame 1 and frame 2; surf_sign[k]
+    // +1 when the region lies above surface k.
+    int surf_on, surf_has2, surf_inter;
+    int surf_axis[2], surf_sign[2], surf_ld[2];
+    const double *surf[2][2];   // [surface][frame]
     DevCounters *cnt;
 };
 

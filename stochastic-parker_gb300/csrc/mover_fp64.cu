@@ -28,6 +28,7 @@ enum R3 { B_VX, B_VY, B_VZ, B_BX, B_BY, B_BZ, B_DVXDX, B_DVYDY, B_DVZDZ, B_DBXDX
 
 struct State {
     double x, y, z, p, v, mu, t, dt, w;
+    double h1, h2;   // acceleration-surface heights at the push's start
     int flag;
     int32_t nsteps_pushed, tag_inj, tag_spl;
     uint32_t ctr;
@@ -55,10 +56,26 @@ __device__ __forceinline__ void interp_at(const MoverArgs &a, const float *rec1,
                                           const State &s, int ix, int iy, int iz, const double *w,
                                           double f[NV]);
 
+// get_interp_paramters on the uniform grid: the lower corner (memory
+// indices) and the 8 weights; false outside the ghost cells.
+template <int NDIM>
+__device__ __forceinline__ bool uniform_cell(const MoverArgs &a, const State &s, int &ix, int &iy,
+                                             int &iz, double w[8]);
+
 // Interpolated fields at the particle: NV variables of records of R floats.
 template <int NDIM, int NV, int R>
 __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, const float *rec2,
                                        const State &s, double f[NV]) {
+    int ix, iy, iz;
+    double w[8];
+    if (!uniform_cell<NDIM>(a, s, ix, iy, iz, w)) return false;
+    interp_at<NDIM, NV, R>(a, rec1, rec2, s, ix, iy, iz, w, f);
+    return true;
+}
+
+template <int NDIM>
+__device__ __forceinline__ bool uniform_cell(const MoverArgs &a, const State &s, int &ix, int &iy,
+                                             int &iz, double w[8]) {
     const double px = (s.x - a.xmin) / a.dx;
     const double py = (s.y - a.ymin) / a.dy;
     const double pz = (s.z - a.zmin) / a.dz;
@@ -75,7 +92,6 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, co
     const double ry = (py - (double)(fy + 1)) + 1.0;
     const double rz = (NDIM == 3) ? (pz - (double)(fz + 1)) + 1.0 : 0.0;
     const double rx1 = 1.0 - rx, ry1 = 1.0 - ry, rz1 = 1.0 - rz;
-    double w[8];
     w[0] = rx1 * ry1 * rz1;
     w[1] = rx * ry1 * rz1;
     w[2] = rx1 * ry * rz1;
@@ -84,8 +100,9 @@ __device__ __forceinline__ bool interp(const MoverArgs &a, const float *rec1, co
     w[5] = rx * ry1 * rz;
     w[6] = rx1 * ry * rz;
     w[7] = rx * ry * rz;
-    const int ix = fx + 2, iy = fy + 2, iz = (NDIM == 3) ? fz + 2 : 0;
-    interp_at<NDIM, NV, R>(a, rec1, rec2, s, ix, iy, iz, w, f);
+    ix = fx + 2;
+    iy = fy + 2;
+    iz = (NDIM == 3) ? fz + 2 : 0;
     return true;
 }
 
@@ -227,8 +244,59 @@ __device__ __forceinline__ bool in_acc_region(const MoverArgs &a, const State &s
     if (ndim == 3) {
         const double zn = (s.z - a.cfg_zmin) / a.cfg_lz;
         in = in && (zn >= a.acc_region[4]) && (zn <= a.acc_region[5]);
+        if (a.surf_on) {
+            // check_above_acc_surface (acc_region_surface.f90:343-383), as
+            // push_particle_3d / _3d_ft apply it (:4889-4893)
+            const double xyz[3] = {s.x, s.y, s.z};
+            double ph = xyz[a.surf_axis[0]];
+            bool up = a.surf_sign[0] > 0 ? ph > s.h1 : ph < s.h1;
+            if (a.surf_has2) {
+                ph = xyz[a.surf_axis[1]];
+                const bool up2 = a.surf_sign[1] > 0 ? ph > s.h2 : ph < s.h2;
+                up = a.surf_inter ? (up && up2) : (up || up2);
+            }
+            in = in && up;
+        }
     }
     return in;
+}
+
+// interp_acc_surface (acc_region_surface.f90:255-335): the 3D weights
+// summed along the surface normal, corners summed in Fortran's order.
+__device__ __forceinline__ double surface_height(const MoverArgs &a, int k, int ix, int iy,
+                                                 int iz, const double *w, double rt) {
+    const int ax = a.surf_axis[k];
+    int i1, j1;
+    double w2[4];
+    if (ax == 0) {
+        i1 = iy; j1 = iz;
+        w2[0] = w[0] + w[1]; w2[1] = w[2] + w[3]; w2[2] = w[4] + w[5]; w2[3] = w[6] + w[7];
+    } else if (ax == 1) {
+        i1 = ix; j1 = iz;
+        w2[0] = w[0] + w[2]; w2[1] = w[1] + w[3]; w2[2] = w[4] + w[6]; w2[3] = w[5] + w[7];
+    } else {
+        i1 = ix; j1 = iy;
+        w2[0] = w[0] + w[4]; w2[1] = w[1] + w[5]; w2[2] = w[2] + w[6]; w2[3] = w[3] + w[7];
+    }
+    const size_t ld = (size_t)a.surf_ld[k];
+    double hs[2] = {0.0, 0.0};
+    for (int t = 0; t < (a.time_interp ? 2 : 1); ++t) {
+        const double *h = a.surf[k][t];
+        double sum = 0.0;
+        sum = sum + __ldg(h + (size_t)i1 + ld * (size_t)j1) * w2[0];
+        sum = sum + __ldg(h + (size_t)i1 + 1 + ld * (size_t)j1) * w2[1];
+        sum = sum + __ldg(h + (size_t)i1 + ld * (size_t)(j1 + 1)) * w2[2];
+        sum = sum + __ldg(h + (size_t)i1 + 1 + ld * (size_t)(j1 + 1)) * w2[3];
+        hs[t] = sum;
+    }
+    return a.time_interp ? hs[0] * (1.0 - rt) + hs[1] * rt : hs[0];
+}
+
+__device__ __forceinline__ void surface_heights(const MoverArgs &a, State &s, int ix, int iy,
+                                                int iz, const double *w) {
+    const double rt = (s.t - a.t0) / a.dtf;
+    s.h1 = surface_height(a, 0, ix, iy, iz, w, rt);
+    s.h2 = a.surf_has2 ? surface_height(a, 1, ix, iy, iz, w, rt) : 0.0;
 }
 
 // 1 / (3 pcharge) (Parker) or 1 / pcharge (focused transport) is single
@@ -1077,6 +1145,7 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
         double v[32];
         interp_at<NDIM, 32, 32>(a, a.full1, a.full2, s, c.ix, c.iy, c.iz, c.w, v);
         f = named_full(v);
+        if (NDIM == 3 && a.surf_on) surface_heights(a, s, c.ix, c.iy, c.iz, c.w);
         if (a.aux1 && (a.deltab_flag || a.correlation_flag)) {
             interp_at<NDIM, 16, 16>(a, a.aux1, a.aux2, s, c.ix, c.iy, c.iz, c.w, av);
             aux = av;
@@ -1099,8 +1168,12 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
     }
     if (FULL) {
         double v[32];
-        if (!interp<NDIM, 32, 32>(a, a.full1, a.full2, s, v)) return false;
+        int ix, iy, iz;
+        double w[8];
+        if (!uniform_cell<NDIM>(a, s, ix, iy, iz, w)) return false;
+        interp_at<NDIM, 32, 32>(a, a.full1, a.full2, s, ix, iy, iz, w, v);
         f = named_full(v);
+        if (NDIM == 3 && a.surf_on) surface_heights(a, s, ix, iy, iz, w);
         if (a.aux1 && (a.deltab_flag || a.correlation_flag)) {
             if (!interp<NDIM, 16, 16>(a, a.aux1, a.aux2, s, av)) return false;
             aux = av;
@@ -1225,7 +1298,8 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
     const int threads = 128;
     const int64_t blocks = (a.n + threads - 1) / threads;
     const bool ft = a.focused_transport != 0;
-    const bool full = ft || a.dpp_wave || a.dpp_shear || a.deltab_flag || a.correlation_flag;
+    const bool full = ft || a.dpp_wave || a.dpp_shear || a.deltab_flag || a.correlation_flag ||
+                      a.surf_on;
     const bool grid = a.spherical || a.nonuniform;
     const unsigned g = (unsigned)blocks;
     if (a.ndim == 2 && a.include_3rd) {

@@ -161,6 +161,9 @@ SIGNATURES = {
     "gpat_set_grid_positions": (C.c_int, [Handle, P(C.c_double), P(C.c_double), P(C.c_double)]),
     "gpat_read_grid_positions": (C.c_int, [Handle, C.c_char_p]),
     "gpat_get_grid_positions": (C.c_int, [Handle, P(C.c_double), P(C.c_double), P(C.c_double)]),
+    "gpat_init_acc_surface": (C.c_int, [Handle, C.c_char_p, C.c_char_p, C.c_int]),
+    "gpat_set_acc_surface": (C.c_int, [Handle, C.c_int, P(C.c_double), P(C.c_double)]),
+    "gpat_read_acc_surface": (C.c_int, [Handle, C.c_int, C.c_char_p, C.c_char_p]),
     "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),
     "gpat_inject_particles_at_large": (C.c_int, [Handle, C.c_int, i64, d, C.c_int, d, C.c_int,
                                                  C.c_int, d, i64, P(d), d, P(i64)]),

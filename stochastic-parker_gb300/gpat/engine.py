@@ -314,6 +314,24 @@ class Engine:
         self._check(self.lib.gpat_get_grid_positions(self.h, *ptrs))
         return out
 
+    def init_acc_surface(self, norm1, norm2=None, is_intersection=True):
+        """init_acc_surface: norm "+y" etc.; a second surface when norm2."""
+        self._check(self.lib.gpat_init_acc_surface(
+            self.h, norm1.encode(), norm2.encode() if norm2 else None, int(is_intersection)))
+
+    def set_acc_surface(self, var_flag, surface1, surface2=None):
+        """Surface heights, numpy arrays (n2, n1) over the ghost-padded plane
+        (first index fastest)."""
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64)
+                for a in (surface1, surface2)]
+        ptr = [None if a is None else a.ctypes.data_as(C.POINTER(C.c_double)) for a in keep]
+        self._check(self.lib.gpat_set_acc_surface(self.h, var_flag, *ptr))
+
+    def read_acc_surface(self, var_flag, filename1, filename2=None):
+        self._check(self.lib.gpat_read_acc_surface(
+            self.h, var_flag, str(filename1).encode(),
+            str(filename2).encode() if filename2 else None))
+
     def count_cells_large(self, quantity, qmin, part_box) -> int:
         """get_ncells_large_jz / _absj / _divv / _rho (quantity: _abi.LARGE_*)."""
         box = (C.c_double * 6)(*part_box)
