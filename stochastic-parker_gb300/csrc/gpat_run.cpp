@@ -45,6 +45,11 @@ struct Options {
     // default, as the reference's CLI; -ug 1 for a uniform grid.
     int spherical_coord = 0, uniform_grid = 0;
     int include_3rd_dim = 0;   // -i3 (stochastic-mhd.f90:899-902)
+    // acceleration surfaces (stochastic-mhd.f90:903-930)
+    int acc_by_surface = 0;
+    bool surface2_existed = false, is_intersection = true;
+    std::string surface_filename1 = "sname_default", surface_filename2 = "sname_default";
+    std::string surface_norm1 = "+y", surface_norm2 = "+y";
     long long ncells_large_jz_norm = 800, ncells_large_absj_norm = 800;
     long long ncells_large_divv_norm = 800, ncells_large_rho_norm = 800;
     double tinterval = 1e-7, power_index = 7.0, split_ratio = 2.72, pmin_split = 2.0;
@@ -85,7 +90,10 @@ int parse(int argc, char **argv, Options &o) {
         {"-cf", "--conf_file"}, {"-nf", "--num_fine_steps"}, {"-nd", "--ndim_field"},
         {"-dp1", "--drift_param1"}, {"-dp2", "--drift_param2"}, {"-ch", "--charge"},
         {"-pv", "--particle_v0"}, {"-cd", "--check_drift_2d"}, {"-sc", "--spherical_coord"},
-        {"-ug", "--uniform_grid"}, {"-i3", "--include_3rd_dim"}, {"-ft", "--focused_transport"},
+        {"-ug", "--uniform_grid"}, {"-i3", "--include_3rd_dim"}, {"-as", "--acc_by_surface"},
+        {"-sf1", "--surface_filename1"}, {"-sn1", "--surface_norm1"},
+        {"-s2e", "--surface2_existed"}, {"-ii", "--is_intersection"},
+        {"-sf2", "--surface_filename2"}, {"-sn2", "--surface_norm2"}, {"-ft", "--focused_transport"},
         {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
         {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
         {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"},
@@ -142,6 +150,13 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--spherical_coord") o.spherical_coord = (int)d;
         else if (k == "--uniform_grid") o.uniform_grid = (int)d;
         else if (k == "--include_3rd_dim") o.include_3rd_dim = (int)d;
+        else if (k == "--acc_by_surface") o.acc_by_surface = (int)d;
+        else if (k == "--surface_filename1") o.surface_filename1 = v;
+        else if (k == "--surface_norm1") o.surface_norm1 = v;
+        else if (k == "--surface2_existed") o.surface2_existed = truthy(v);
+        else if (k == "--is_intersection") o.is_intersection = truthy(v);
+        else if (k == "--surface_filename2") o.surface_filename2 = v;
+        else if (k == "--surface_norm2") o.surface_norm2 = v;
         else if (k == "--focused_transport") o.focused_transport = truthy(v);
         else if (k == "--nlgc") o.nlgc = truthy(v);
         else if (k == "--kperp_kpara") o.kperp_kpara = d;
@@ -260,7 +275,7 @@ int main(int argc, char **argv) {
     // asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
          o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1 ||
-         o.include_3rd_dim == 1) && !o.precision_set)
+         o.include_3rd_dim == 1 || o.acc_by_surface == 1) && !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
@@ -298,11 +313,26 @@ int main(int argc, char **argv) {
     CHECK(gpat_create(&p, &cfg, o.device, &h));
     // set_local_grid_positions (:186): xpos.dat, ypos.dat, zpos.dat
     if (p.nonuniform_grid) CHECK(gpat_read_grid_positions(h, o.dir_mhd_data.c_str()));
+    // init_acc_surface (:196-203)
+    if (o.acc_by_surface == 1)
+        CHECK(gpat_init_acc_surface(h, o.surface_norm1.c_str(),
+                                    o.surface2_existed ? o.surface_norm2.c_str() : nullptr,
+                                    o.is_intersection ? 1 : 0));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
 
     // Frame tmin into farray1, gradients (:321, :350).
     const int tmin = o.t_start;
     CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tmin).c_str(), 0));
+    // read_acc_surface of <dir><surface_filename>_XXXX.dat (:324-333, :406-415)
+    auto read_surfaces = [&](int tf, int var_flag) -> int {
+        if (o.acc_by_surface != 1) return GPAT_OK;
+        char num[16];
+        std::snprintf(num, sizeof num, "_%04d.dat", tf);
+        const std::string f1 = o.dir_mhd_data + o.surface_filename1 + num;
+        const std::string f2 = o.dir_mhd_data + o.surface_filename2 + num;
+        return gpat_read_acc_surface(h, var_flag, f1.c_str(),
+                                     o.surface2_existed ? f2.c_str() : nullptr);
+    };
     auto read_turbulence = [&](int tf, int var_flag) -> int {
         char num[16];
         std::snprintf(num, sizeof num, "%04d", tf);
@@ -315,6 +345,7 @@ int main(int argc, char **argv) {
             return gpat_read_correlation_length(h, (o.dir_mhd_data + "lc_" + num).c_str(), var_flag);
         return GPAT_OK;
     };
+    CHECK(read_surfaces(tmin, 0));
     CHECK(read_turbulence(tmin, 0));
     CHECK(gpat_calc_fields_gradients(h, 0));
     double part_box[6];
@@ -361,6 +392,7 @@ int main(int argc, char **argv) {
     for (int tf = tmin + 1; tf <= o.t_end; ++tf) {
         if (o.single_time_frame == 0 && tf <= o.tmax_mhd) {
             CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tf).c_str(), o.time_interp_flag));
+            CHECK(read_surfaces(tf, o.time_interp_flag));
             CHECK(read_turbulence(tf, o.time_interp_flag));
             CHECK(gpat_calc_fields_gradients(h, o.time_interp_flag));
         }

@@ -22,7 +22,7 @@ module gpat_gpu
         gpu_inject_particles_at_large_jz, gpu_inject_particles_at_large_absj, &
         gpu_inject_particles_at_large_divv, gpu_inject_particles_at_large_rho, &
         gpu_inject_particles_at_large_db2, gpu_read_magnetic_fluctuation, &
-        gpu_read_grid_positions, &
+        gpu_read_grid_positions, gpu_init_acc_surface, gpu_read_acc_surface, &
         gpu_read_correlation_length, &
         gpu_calc_escaped_distributions, gpu_reset_escaped_particles
 
@@ -109,6 +109,22 @@ module gpat_gpu
             type(c_ptr), value :: handle
             character(kind=c_char), dimension(*), intent(in) :: filename
             integer(c_int), value :: var_flag
+        end function
+        integer(c_int) function c_init_acc_surface(handle, norm1, norm2, is_intersection) &
+                bind(c, name="gpat_init_acc_surface")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: norm1
+            type(c_ptr), value :: norm2
+            integer(c_int), value :: is_intersection
+        end function
+        integer(c_int) function c_read_acc_surface(handle, var_flag, file1, file2) &
+                bind(c, name="gpat_read_acc_surface")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            integer(c_int), value :: var_flag
+            character(kind=c_char), dimension(*), intent(in) :: file1
+            type(c_ptr), value :: file2
         end function
         integer(c_int) function c_read_grid_positions(handle, dirname) &
                 bind(c, name="gpat_read_grid_positions")
@@ -303,6 +319,42 @@ module gpat_gpu
         call check(c_read_grid_positions(h, trim(dir_mhd_data)//c_null_char), &
             "read_grid_positions")
     end subroutine gpu_read_grid_positions
+
+    !< init_acc_surface (acc_region_surface.f90:27-93): norm2 and
+    !< is_intersection only for a second surface
+    subroutine gpu_init_acc_surface(surface_norm1, surface_norm2, is_intersection)
+        character(*), intent(in) :: surface_norm1
+        character(*), intent(in), optional :: surface_norm2
+        logical, intent(in), optional :: is_intersection
+        character(kind=c_char, len=3), target :: n2
+        type(c_ptr) :: p2
+        integer(c_int) :: inter
+        p2 = c_null_ptr
+        inter = 1
+        if (present(surface_norm2)) then
+            n2 = surface_norm2(1:2)//c_null_char
+            p2 = c_loc(n2)
+        endif
+        if (present(is_intersection)) inter = merge(1_c_int, 0_c_int, is_intersection)
+        call check(c_init_acc_surface(h, surface_norm1(1:2)//c_null_char, p2, inter), &
+            "init_acc_surface")
+    end subroutine gpu_init_acc_surface
+
+    !< read_acc_surface (acc_region_surface.f90:112-249)
+    subroutine gpu_read_acc_surface(var_flag, filename1, filename2)
+        integer, intent(in) :: var_flag
+        character(*), intent(in) :: filename1
+        character(*), intent(in), optional :: filename2
+        character(kind=c_char, len=:), allocatable, target :: f2
+        type(c_ptr) :: p2
+        p2 = c_null_ptr
+        if (present(filename2)) then
+            f2 = trim(filename2)//c_null_char
+            p2 = c_loc(f2)
+        endif
+        call check(c_read_acc_surface(h, int(var_flag, c_int), trim(filename1)//c_null_char, &
+            p2), "read_acc_surface")
+    end subroutine gpu_read_acc_surface
 
     !< read_magnetic_fluctuation + calc_grad_sigma2_slab/_2d
     !< (mhd_data_parallel.f90:306-397, stochastic-mhd.f90:337-361)

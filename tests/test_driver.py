@@ -235,3 +235,65 @@ def test_driver_spherical_nonuniform_grid(tmp_path):
     f, c = eng.calc_particle_distributions()
     assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv) and c.sum() > 0
     eng.close()
+
+
+@pytest.mark.gpu
+def test_driver_acceleration_surfaces_3d(tmp_path):
+    """-as 1 with two surfaces read from <dir><name>_XXXX.dat with every
+    frame (stochastic-mhd.f90:196-203, :324-333, :406-415); f(p) equals the
+    same calls made from Python, bit for bit."""
+    from gpat.engine import make_mhd_config
+    n = 16
+    g = n + 4
+    cfg = make_mhd_config(n, n, n, 0.0, 1.0, 0.0, 1.0, zmin=0.0, zmax=1.0, dt_out=0.05, ndim=3)
+    data = tmp_path / "data"
+    data.mkdir()
+    (tmp_path / "config").mkdir()
+    out = tmp_path / "out"
+    out.mkdir()
+    fields.write_mhd_config(data / "mhd_config.dat", cfg)
+    frame = fields.turbulence_3d(n, seed=5)
+    rng = np.random.default_rng(6)
+    for t in range(3):
+        fields.write_mhd_data(data / f"mhd_data_{t:04d}", frame)
+        (0.5 + 0.1 * rng.standard_normal((g, g))).tofile(data / f"top_{t:04d}.dat")
+        (0.3 + 0.1 * rng.standard_normal((g, g))).tofile(data / f"side_{t:04d}.dat")
+    keys = dict(b0=1.0, p0=0.1, pmin=0.05, pmax=100.0, momentum_dependency=0, gamma_turb=5 / 3,
+                mag_dependency=0, kpara0=2e-3, kret=0.1, dt_min_rel=2e-3, dt_max_rel=5e-2)
+    lines = ["!< conf.dat written by the test"] + [f"{k} = {v!r}" for k, v in keys.items()]
+    lines += ["acc_region_flag = 1", "acc_xmin = 0.0", "acc_xmax = 1.0", "acc_ymin = 0.0",
+              "acc_ymax = 1.0", "acc_zmin = 0.0", "acc_zmax = 1.0", "npp_global = 64",
+              "nmu_global = 1", "pbcx = 0", "pbcy = 0", "pbcz = 0"]
+    (tmp_path / "config" / "conf.dat").write_text("\n".join(lines) + "\n")
+    exe = build.build_driver()
+    cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
+           "-ts", "0", "-te", "2", "-np", "2000", "-nm", "20000", "-is", "0", "-df", "1",
+           "-pv", "1.0", "-dt", "1e-7", "-sf", "0", "-nd", "3", "--seed", str(SEED), "-ug", "1",
+           "-nl", ".false.", "-ti", "1", "-as", "1", "-sf1", "top", "-sn1", "+z", "-s2e", "T",
+           "-sf2", "side", "-sn2", "-x", "-ii", "F"]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    edges, f_drv, c_drv = _read_fdists(out / "fdists_0002.dat")
+
+    prm = make_params(ndim=3, npp_global=64, nptl_max=20000, seed=SEED, precision=0, b0=1.0,
+                      drift1=4e7, drift2=2e8, charge=-1, pbcx=0, pbcy=0, pbcz=0, time_interp=1,
+                      acc_region_flag=1, acc_region=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0),
+                      **{k: v for k, v in keys.items() if k != "b0"})
+    eng = Engine(prm, cfg, 0)
+    eng.calc_tstamps_mhd(0, 2)
+    eng.init_acc_surface("+z", "-x", False)
+    eng.read_field_data(data / "mhd_data_0000", 0)
+    eng.read_acc_surface(0, data / "top_0000.dat", data / "side_0000.dat")
+    eng.calc_fields_gradients(0)
+    for tf in (1, 2):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 1)
+        eng.read_acc_surface(1, data / f"top_{tf:04d}.dat", data / f"side_{tf:04d}.dat")
+        eng.calc_fields_gradients(1)
+        if tf == 1:
+            eng.inject_particles_spatial_uniform(2000, 1e-7, 1, 1.0, tf,
+                                                 (0.0, 0.0, 0.0, 1.0, 1.0, 1.0))
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1)
+        eng.copy_fields()
+    f, c = eng.calc_particle_distributions()
+    assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv) and c.sum() > 0
+    eng.close()
