@@ -328,7 +328,16 @@ int gpat_calc_local_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec
  * fescaped(npp_global, 2 * ndim) in Fortran order, column ibc = |count_flag|
  * (1 low x, 2 high x, 3 low y, 4 high y, 5 low z, 6 high z). */
 int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t *counts);
-/* reset_escaped_particles: clears the escaped distribution. */
+/* escaped_ptls: the particles removed through an open boundary by
+ * gpat_particle_mover calls made with dump_escaped_dist = 1 since the last
+ * reset (remove_particles, particle_module.f90:5365-5403, as written by
+ * dump_escaped_particles, diagnostics.f90:1896-1978), in removal order;
+ * count_flag holds the boundary face (-1 .. -6).  *n gets their number;
+ * GPAT_ERR_CAPACITY when it exceeds capacity. */
+int gpat_get_escaped_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity,
+                               int64_t *n);
+/* reset_escaped_particles: clears the escaped distribution and the escaped
+ * particles. */
 int gpat_reset_escaped_particles(gpat_handle_t *h);
 /* pbins_edges_global (diagnostics.f90:194-204): npp_global + 1 values. */
 int gpat_pbins_edges(gpat_handle_t *h, double *edges);

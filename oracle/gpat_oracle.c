@@ -1680,7 +1680,32 @@ static void escaped_add(const orc_particles *P, int64_t i)
     orc_fixed_add(&g_esc.whi[k], &g_esc.wlo[k], P->weight[i]);
 }
 
-/* remove_particles: particle_module.f90:5365-5403 (same swap order). */
+static struct {
+    orc_particles *P;
+    int64_t cap, *n;
+} g_estore;
+
+void orc_set_escaped_store(orc_particles *store, int64_t cap, int64_t *n)
+{
+    g_estore.P = store;
+    g_estore.cap = cap;
+    g_estore.n = n;
+}
+
+static void copy_one(const orc_particles *S, int64_t i, orc_particles *D, int64_t j)
+{
+    D->x[j] = S->x[i]; D->y[j] = S->y[i]; D->z[j] = S->z[i]; D->p[j] = S->p[i];
+    D->v[j] = S->v[i]; D->mu[j] = S->mu[i]; D->weight[j] = S->weight[i];
+    D->t[j] = S->t[i]; D->dt[j] = S->dt[i];
+    D->split_times[j] = S->split_times[i]; D->count_flag[j] = S->count_flag[i];
+    D->origin[j] = S->origin[i]; D->nsteps_tracked[j] = S->nsteps_tracked[i];
+    D->nsteps_pushed[j] = S->nsteps_pushed[i]; D->tag_injected[j] = S->tag_injected[i];
+    D->tag_splitted[j] = S->tag_splitted[i]; D->rng_ctr[j] = S->rng_ctr[i];
+}
+
+/* remove_particles: particle_module.f90:5365-5403 (same swap order); with
+ * an escaped store set, escaped particles are copied to it first
+ * (escaped_ptls, :5386-5389). */
 int64_t orc_remove_particles(orc_particles *P, int64_t n, orc_counters *cnt)
 {
     if (n <= 0) return n;
@@ -1693,6 +1718,10 @@ int64_t orc_remove_particles(orc_particles *P, int64_t n, orc_counters *cnt)
             if (P->count_flag[i] < 0) {
                 cnt->nptl_escaped += 1;
                 escaped_add(P, i);
+                if (g_estore.P && *g_estore.n < g_estore.cap) {
+                    copy_one(P, i, g_estore.P, *g_estore.n);
+                    *g_estore.n += 1;
+                }
             }
             swap_particles(P, n - nremoved - 1, i);
             nremoved += 1;

@@ -174,6 +174,9 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
                         double particle_v0, double t_frame, double power_index,
                         orc_counters *cnt);
 void orc_quick_check(const orc_particles *ptl, int64_t n, double out[4]);
+/* Attaches a store for the escaped particles remove_particles drops
+ * (escaped_ptls); store NULL detaches it. */
+void orc_set_escaped_store(orc_particles *store, int64_t cap, int64_t *n);
 void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *counts,
                                uint64_t *whi, uint64_t *wlo);
 /* init_acc_surface / read_acc_surface for 3D runs

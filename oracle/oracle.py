@@ -135,6 +135,7 @@ def load() -> C.CDLL:
                                             P(OrcCounters)]
         lib.orc_quick_check.argtypes = [P(OrcParticles), i64, P(d)]
         lib.orc_set_escaped_histogram.argtypes = [C.c_int, d, d, P(u64), P(u64), P(u64)]
+        lib.orc_set_escaped_store.argtypes = [P(OrcParticles), i64, P(i64)]
         lib.orc_calc_local_distribution.argtypes = [P(OrcMhdConfig), C.c_int, C.c_int, C.c_int,
                                                     d, d, C.c_int,
                                                     C.c_int, C.c_int, C.c_int, C.c_int,
@@ -402,6 +403,22 @@ class EscapedHistogram:
 
     def weights(self) -> np.ndarray:
         return np.array([fixed_to_double(int(h), int(l)) for h, l in zip(self.whi, self.wlo)])
+
+
+class EscapedStore:
+    """Attaches a store for the particles remove_particles drops through an
+    open boundary (escaped_ptls); detach() turns it off."""
+
+    def __init__(self, capacity: int):
+        self.parts = Particles(capacity)
+        self.n = C.c_int64(0)
+        load().orc_set_escaped_store(C.byref(self.parts.c), capacity, C.byref(self.n))
+
+    def detach(self):
+        load().orc_set_escaped_store(None, 0, None)
+
+    def view(self) -> dict:
+        return {k: v[:self.n.value].copy() for k, v in self.parts.a.items()}
 
 
 def local_distribution(cfg: OrcMhdConfig, ndim: int, parts: Particles, pmin: float, pmax: float,

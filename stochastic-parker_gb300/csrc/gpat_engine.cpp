@@ -56,6 +56,12 @@ struct gpat_handle {
     DevCounters hcnt{};
     unsigned long long *dbins = nullptr;
     unsigned long long *desc = nullptr;   // escaped distribution, 6 faces x npp x 3
+    // escaped_ptls: particles removed through an open boundary while the
+    // mover is called with dump_escaped_dist (grown like
+    // resize_escaped_particles, particle_module.f90:5329-5358).
+    void *emem = nullptr;
+    DevParticles E{};
+    int64_t ecap = 0, ne = 0;
     // module state kept on the host
     std::vector<double> tstamps;
     int64_t tag_max = 0;
@@ -337,6 +343,49 @@ const double *const *grad_spans(const gpat_handle_t *h) {
     return h->prm.nonuniform_grid ? h->dih : nullptr;
 }
 
+// Copies the first n particles of one carved buffer to another.
+cudaError_t copy_particles_d2d(const DevParticles &S, const DevParticles &D, int64_t n,
+                               cudaStream_t s) {
+    const size_t c = (size_t)n;
+    const void *src[17] = {S.x, S.y, S.z, S.p, S.v, S.mu, S.weight, S.t, S.dt, S.split_times,
+                           S.count_flag, S.origin, S.nsteps_tracked, S.nsteps_pushed,
+                           S.tag_injected, S.tag_splitted, S.rng_ctr};
+    void *dst[17] = {D.x, D.y, D.z, D.p, D.v, D.mu, D.weight, D.t, D.dt, D.split_times,
+                     D.count_flag, D.origin, D.nsteps_tracked, D.nsteps_pushed,
+                     D.tag_injected, D.tag_splitted, D.rng_ctr};
+    const size_t width[17] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 1, 1, 4, 4, 4, 4, 4, 4};
+    for (int k = 0; k < 17; ++k) {
+        const cudaError_t e = cudaMemcpyAsync(dst[k], src[k], width[k] * c,
+                                              cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// remove_particles' copy of the escaped particles (particle_module.f90:
+// 5368-5392): before the current set drops them, particles with
+// count_flag < 0 are appended to the escaped store in set order.
+int collect_escaped(gpat_handle_t *h) {
+    if (h->n <= 0) return GPAT_OK;
+    if (h->ne + h->n > h->ecap) {
+        const int64_t ncap = std::max((int64_t)(1.25 * (double)h->ecap), h->ne + h->n);
+        void *mem = nullptr;
+        CK(cudaMalloc(&mem, particle_bytes(ncap)));
+        const DevParticles N = carve(mem, ncap);
+        if (h->ne > 0) CK(copy_particles_d2d(h->E, N, h->ne, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (h->emem) CK(cudaFree(h->emem));
+        h->emem = mem;
+        h->E = N;
+        h->ecap = ncap;
+    }
+    CK(launch_select_escaped(h->P[h->cur], h->n, h->E, h->ne, h->scratch, h->dcnt, h->stream));
+    const int rc = pull_counters(h);
+    if (rc) return rc;
+    h->ne += (int64_t)h->hcnt.nselected;
+    return GPAT_OK;
+}
+
 int ensure_scratch(gpat_handle_t *h, int64_t n) {
     const size_t need = compaction_scratch_bytes(n);
     if (need <= h->scratch_bytes) return GPAT_OK;
@@ -535,6 +584,7 @@ int gpat_destroy(gpat_handle_t *h) {
         if (h->pmem[s]) cudaFree(h->pmem[s]);
     }
     if (h->staging) cudaFree(h->staging);
+    if (h->emem) cudaFree(h->emem);
     if (h->scratch) cudaFree(h->scratch);
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->dcnt) cudaFree(h->dcnt);
@@ -1011,11 +1061,39 @@ int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity
     return GPAT_OK;
 }
 
+int gpat_get_escaped_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity,
+                               int64_t *n) {
+    if (!h || !dst || !n) return GPAT_ERR_ARG;
+    *n = h->ne;
+    if (h->ne > capacity) return fail(h, GPAT_ERR_CAPACITY, "destination too small");
+    if (h->ne == 0) return GPAT_OK;
+    CK(cudaSetDevice(h->device));
+    const DevParticles &S = h->E;
+    const size_t c = (size_t)h->ne;
+    auto cp = [&](void *d, const void *s, size_t bytes) -> cudaError_t {
+        if (!bytes || !d) return cudaSuccess;
+        return cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToHost, h->stream);
+    };
+    CK(cp(dst->x, S.x, 8 * c)); CK(cp(dst->y, S.y, 8 * c)); CK(cp(dst->z, S.z, 8 * c));
+    CK(cp(dst->p, S.p, 8 * c)); CK(cp(dst->v, S.v, 8 * c)); CK(cp(dst->mu, S.mu, 8 * c));
+    CK(cp(dst->weight, S.weight, 8 * c)); CK(cp(dst->t, S.t, 8 * c)); CK(cp(dst->dt, S.dt, 8 * c));
+    CK(cp(dst->split_times, S.split_times, c)); CK(cp(dst->count_flag, S.count_flag, c));
+    CK(cp(dst->origin, S.origin, 4 * c)); CK(cp(dst->nsteps_tracked, S.nsteps_tracked, 4 * c));
+    CK(cp(dst->nsteps_pushed, S.nsteps_pushed, 4 * c));
+    CK(cp(dst->tag_injected, S.tag_injected, 4 * c));
+    CK(cp(dst->tag_splitted, S.tag_splitted, 4 * c));
+    CK(cp(dst->rng_ctr, S.rng_ctr, 4 * c));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, double kperp_kpara,
                         int nsteps_interval, int mhd_tframe, int num_fine_steps,
                         int dump_escaped_dist) {
     if (!h) return GPAT_ERR_ARG;
-    (void)dump_escaped_dist;   // the escaped distribution is always accumulated
+    // The escaped distribution is always accumulated; dump_escaped_dist also
+    // keeps the escaped particles themselves (escaped_ptls).
+    const bool keep_escaped = dump_escaped_dist != 0;
     const bool mixed = h->prm.precision == GPAT_PREC_MIXED;
     if (focused_transport && mixed)
         return fail(h, GPAT_ERR_UNSUPPORTED, "focused transport runs in FP64 precision");
@@ -1054,6 +1132,10 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
             CK(launch_mover_mixed(a, k, h->sm_count, h->stream));
             CK(cudaEventRecord(h->ev1, h->stream));
             ++launches;
+            if (keep_escaped) {
+                rc = collect_escaped(h);
+                if (rc) return rc;
+            }
             rc = bin_particles(h);   // remove_particles as a binning by cell
             if (rc) return rc;
             float ms = 0.0f;
@@ -1068,6 +1150,10 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         CK(launch_mover_fp64(a, h->sm_count, h->stream));
         CK(cudaEventRecord(h->ev1, h->stream));
         launches = 1;
+        if (keep_escaped) {
+            rc = collect_escaped(h);
+            if (rc) return rc;
+        }
         // remove_particles (particle_module.f90:5365-5403), order-preserving.
         const int nxt = 1 - h->cur;
         CK(launch_remove_particles(h->P[h->cur], h->P[nxt], h->n, h->scratch, h->dcnt,
@@ -1205,6 +1291,7 @@ int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t
 
 int gpat_reset_escaped_particles(gpat_handle_t *h) {
     if (!h) return GPAT_ERR_ARG;
+    h->ne = 0;   // nptl_escaped = 0 (diagnostics.f90:2227-2246)
     CK(cudaSetDevice(h->device));
     CK(cudaMemsetAsync(h->desc, 0, sizeof(unsigned long long) * 3 * 6 * (size_t)h->prm.npp_global,
                        h->stream));

@@ -40,6 +40,7 @@ struct DevCounters {
     unsigned long long nactive;   // particles a chunked mover launch left mid-interval
     unsigned long long ncells;    // get_ncells_large_* result
     unsigned long long nkilled;   // particles removed by roulette
+    unsigned long long nselected; // escaped particles copied by launch_select_escaped
     double dt_min, dt_max;
     unsigned int status;
     unsigned int pad;
@@ -253,6 +254,12 @@ size_t compaction_scratch_bytes(int64_t n);
 cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles &dst, int64_t n,
                                     void *scratch, DevCounters *cnt, const EscHist &esc,
                                     cudaStream_t s);
+
+// Copies the particles of src with count_flag < 0 (escaped through an open
+// boundary) to dst[base ..] in order; cnt->nselected gets their number.
+// scratch as for launch_remove_particles.
+cudaError_t launch_select_escaped(const DevParticles &src, int64_t n, const DevParticles &dst,
+                                  int64_t base, void *scratch, DevCounters *cnt, cudaStream_t s);
 
 // One local distribution (flocal of calc_particle_distributions).
 struct LocalDistArgs {

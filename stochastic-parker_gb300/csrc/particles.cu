@@ -302,10 +302,12 @@ __device__ __forceinline__ void escaped_add(const EscHist &e, const DevParticles
     atomic_add_fixed(b + 1, b + 2, P.weight[i]);
 }
 
-// mode 0: keep count_flag == INBOX; mode 1: split candidates.
+// mode 0: keep count_flag == INBOX; mode 1: split candidates; mode 2:
+// escaped particles (count_flag < 0).
 template <int MODE>
 __device__ __forceinline__ bool select(const DevParticles &P, int64_t i, const SplitRule &r) {
     if (MODE == 0) return P.count_flag[i] == 1;
+    if (MODE == 2) return P.count_flag[i] < 0;
     const double p = P.p[i];
     return p > split_threshold(r.pmin_split, r.p0, r.ratio, P.split_times[i]) && p <= r.pmax;
 }
@@ -400,6 +402,7 @@ __device__ __forceinline__ void copy_particle(const DevParticles &S, int64_t i,
 
 // MODE 0: kept particles of S go to D in order.  MODE 1: S == D; each split
 // candidate gets a child at n + rank (if < cap) and is updated in place.
+// MODE 2: escaped particles go to D at cap + rank (cap is the base there).
 template <int MODE>
 __global__ void __launch_bounds__(kScanThreads) tile_scatter_kernel(
     const DevParticles S, const DevParticles D, int64_t n, int64_t cap, SplitRule r,
@@ -431,6 +434,8 @@ __global__ void __launch_bounds__(kScanThreads) tile_scatter_kernel(
             const long long rank = running + warp_pre[wid] + wpre;
             if (MODE == 0) {
                 copy_particle(S, i, D, rank);
+            } else if (MODE == 2) {
+                copy_particle(S, i, D, cap + rank);
             } else {
                 const int64_t c = n + rank;
                 if (c < cap) {
@@ -737,6 +742,22 @@ cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles 
     tile_count_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt, esc);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
     tile_scatter_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, n, r, offsets, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_escaped(const DevParticles &src, int64_t n, const DevParticles &dst,
+                                  int64_t base, void *scratch, DevCounters *cnt, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&cnt->nselected, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || n <= 0) return e;
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    long long *counts = static_cast<long long *>(scratch);
+    long long *offsets = counts + ntiles;
+    const SplitRule r{0, 0, 0, 0};
+    const EscHist none{nullptr, 0, 0.0, 0.0, 0.0, 0.0};
+    tile_count_kernel<2><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt, none);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nselected);
+    tile_scatter_kernel<2><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, base, r,
+                                                                     offsets, cnt);
     return cudaGetLastError();
 }
 

@@ -162,6 +162,7 @@ SIGNATURES = {
     "gpat_read_grid_positions": (C.c_int, [Handle, C.c_char_p]),
     "gpat_get_grid_positions": (C.c_int, [Handle, P(C.c_double), P(C.c_double), P(C.c_double)]),
     "gpat_init_acc_surface": (C.c_int, [Handle, C.c_char_p, C.c_char_p, C.c_int]),
+    "gpat_get_escaped_particles": (C.c_int, [Handle, P(Particles), C.c_int64, P(C.c_int64)]),
     "gpat_set_acc_surface": (C.c_int, [Handle, C.c_int, P(C.c_double), P(C.c_double)]),
     "gpat_read_acc_surface": (C.c_int, [Handle, C.c_int, C.c_char_p, C.c_char_p]),
     "gpat_count_cells_large": (C.c_int, [Handle, C.c_int, d, P(d), P(i64)]),

@@ -368,6 +368,20 @@ class Engine:
         self._check(self.lib.gpat_get_particles(self.h, C.byref(s), len(ps), C.byref(got)))
         return ps if out is None else ParticleSet({k: v[:n] for k, v in ps.arrays.items()})
 
+    def get_escaped_particles(self) -> ParticleSet:
+        """escaped_ptls: particles removed through an open boundary by mover
+        calls with dump_escaped_dist since the last reset_escaped_particles."""
+        got = C.c_int64()
+        empty = ParticleSet.empty(0)
+        rc = self.lib.gpat_get_escaped_particles(self.h, C.byref(empty.ctypes()), 0,
+                                                 C.byref(got))
+        if rc not in (_abi.GPAT_OK, _abi.GPAT_ERR_CAPACITY):
+            self._check(rc)
+        ps = ParticleSet.empty(got.value)
+        self._check(self.lib.gpat_get_escaped_particles(self.h, C.byref(ps.ctypes()), len(ps),
+                                                        C.byref(got)))
+        return ps
+
     @property
     def nptl_current(self) -> int:
         return self.counters().nptl_current
