@@ -35,6 +35,7 @@ struct Options {
     int num_fine_steps = 1, ndim_field = 2, charge = -1, inject_new_ptl = 0;
     int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
     int particle_data_dump = 0;
+    bool dump_escaped_dist = false, dump_escaped = false;   // -ded, -de (:939-946)
     // inject_particles_at_large_* switches (stochastic-mhd.f90:735-806)
     bool inject_large_jz = false, inject_large_absj = false, inject_large_db2 = false;
     bool inject_large_divv = false, inject_large_rho = false, inject_same_nptl = false;
@@ -95,7 +96,8 @@ int parse(int argc, char **argv, Options &o) {
         {"-s2e", "--surface2_existed"}, {"-ii", "--is_intersection"},
         {"-sf2", "--surface_filename2"}, {"-sn2", "--surface_norm2"}, {"-ft", "--focused_transport"},
         {"-nl", "--nlgc"}, {"-kk", "--kperp_kpara"}, {"-du", "--duu_init"},
-        {"-pd", "--particle_data_dump"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
+        {"-pd", "--particle_data_dump"}, {"-ded", "--dump_escaped_dist"},
+        {"-de", "--dump_escaped"}, {"-dw", "--dpp_wave"}, {"-ds", "--dpp_shear"},
         {"-ws", "--weak_scattering"}, {"-t0", "--tau0_scattering"},
         {"-ij", "--inject_large_jz"}, {"-iaj", "--inject_large_absj"},
         {"-ib", "--inject_large_db2"}, {"-iv", "--inject_large_divv"},
@@ -162,6 +164,8 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--kperp_kpara") o.kperp_kpara = d;
         else if (k == "--duu_init") o.duu_init = d;
         else if (k == "--particle_data_dump") o.particle_data_dump = (int)d;
+        else if (k == "--dump_escaped_dist") o.dump_escaped_dist = truthy(v);
+        else if (k == "--dump_escaped") o.dump_escaped = truthy(v);
         else if (k == "--dpp_wave") o.dpp_wave = (int)d;
         else if (k == "--dpp_shear") o.dpp_shear = (int)d;
         else if (k == "--weak_scattering") o.weak_scattering = (int)d;
@@ -215,11 +219,22 @@ int parse(int argc, char **argv, Options &o) {
 // order, nptl values each: x y z p v mu weight t dt (float64), split_times
 // count_flag (int8), origin nsteps_tracked nsteps_pushed tag_injected
 // tag_splitted (int32).
-int write_particles(gpat_handle_t *h, const std::string &dir, int frame) {
-    gpat_counters_t c;
-    int rc = gpat_get_counters(h, &c);
-    if (rc) return rc;
-    const int64_t n = c.nptl_current;
+// particles_XXXX.dat (dump_particles), or escaped_particles_XXXX.dat
+// (dump_escaped_particles, diagnostics.f90:1896-1978) when escaped.
+int write_particles(gpat_handle_t *h, const std::string &dir, int frame, bool escaped = false) {
+    int64_t n = 0;
+    int rc;
+    if (escaped) {
+        gpat_particles_t none;
+        std::memset(&none, 0, sizeof none);
+        rc = gpat_get_escaped_particles(h, &none, 0, &n);
+        if (rc && rc != GPAT_ERR_CAPACITY) return rc;
+    } else {
+        gpat_counters_t c;
+        rc = gpat_get_counters(h, &c);
+        if (rc) return rc;
+        n = c.nptl_current;
+    }
     const size_t m = (size_t)(n > 0 ? n : 1);
     std::vector<double> f64[9];
     std::vector<int8_t> i8[2];
@@ -237,10 +252,11 @@ int write_particles(gpat_handle_t *h, const std::string &dir, int frame) {
     P.tag_injected = i32[3].data(); P.tag_splitted = i32[4].data();
     P.rng_ctr = ctr.data();
     int64_t got = 0;
-    rc = gpat_get_particles(h, &P, n, &got);
+    rc = escaped ? gpat_get_escaped_particles(h, &P, n, &got) : gpat_get_particles(h, &P, n, &got);
     if (rc) return rc;
     char name[64];
-    std::snprintf(name, sizeof name, "particles_%04d.dat", frame);
+    std::snprintf(name, sizeof name, escaped ? "escaped_particles_%04d.dat" : "particles_%04d.dat",
+                  frame);
     FILE *f = std::fopen((dir + name).c_str(), "wb");
     if (!f) return GPAT_ERR_IO;
     bool ok = std::fwrite(&got, 8, 1, f) == 1;
@@ -389,6 +405,27 @@ int main(int argc, char **argv) {
         return GPAT_OK;
     };
 
+    // fescaped_XXXX.dat: int32 npp, int32 2 ndim, npp + 1 edges, the
+    // weighted counts fescaped(npp, 2 ndim) (Fortran order), uint64 counts.
+    auto write_escaped_dist = [&](int frame) -> int {
+        const int ncol = 2 * o.ndim_field;
+        std::vector<double> fe((size_t)npp * ncol);
+        std::vector<uint64_t> ce((size_t)npp * ncol);
+        int rc = gpat_calc_escaped_distributions(h, fe.data(), ce.data());
+        if (rc) return rc;
+        char name[64];
+        std::snprintf(name, sizeof name, "fescaped_%04d.dat", frame);
+        FILE *f = std::fopen((o.diagnostics_directory + name).c_str(), "wb");
+        if (!f) return GPAT_ERR_IO;
+        const int32_t hdr[2] = {npp, ncol};
+        std::fwrite(hdr, 4, 2, f);
+        std::fwrite(edges.data(), 8, edges.size(), f);
+        std::fwrite(fe.data(), 8, fe.size(), f);
+        std::fwrite(ce.data(), 8, ce.size(), f);
+        std::fclose(f);
+        return GPAT_OK;
+    };
+
     for (int tf = tmin + 1; tf <= o.t_end; ++tf) {
         if (o.single_time_frame == 0 && tf <= o.tmax_mhd) {
             CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tf).c_str(), o.time_interp_flag));
@@ -426,10 +463,17 @@ int main(int argc, char **argv) {
             if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, o.t_start));
         }
         CHECK(gpat_particle_mover(h, o.focused_transport, o.nlgc, o.kperp_kpara, o.nsteps_interval,
-                                  ct, o.num_fine_steps, 0));
+                                  ct, o.num_fine_steps, o.dump_escaped_dist ? 1 : 0));
         if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
         CHECK(diagnostics(tf));
         if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, tf));
+        if (o.dump_escaped_dist) {
+            // distributions_diagnostics' escaped distributions, then
+            // dump_escaped_particles and reset_escaped_particles (:519-533)
+            CHECK(write_escaped_dist(tf));
+            if (o.dump_escaped) CHECK(write_particles(h, o.diagnostics_directory, tf, true));
+            CHECK(gpat_reset_escaped_particles(h));
+        }
         if (o.time_interp_flag == 1) CHECK(gpat_copy_fields(h));
         gpat_counters_t c;
         CHECK(gpat_get_counters(h, &c));

@@ -43,7 +43,8 @@ def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
            "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
            "--precision", precision, "--seed", str(SEED), "-ug", "1",
            "-ft", ".true." if ft else ".false.",
-           "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1"]
+           "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1",
+           "-ded", ".true.", "-de", ".true."]
     return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
 
 
@@ -91,8 +92,24 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
         eng.calc_fields_gradients(0)
         eng.inject_particles_at_x(2000, 0.5, 1e-7, 1, 1.0, tf)
         eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1,
-                           focused_transport=ft, nlgc=nlgc, kperp_kpara=0.05)
+                           focused_transport=ft, nlgc=nlgc, kperp_kpara=0.05,
+                           dump_escaped_dist=True)
         eng.split_particle(2.72, 2.0, 10)
+        if tf == 3:
+            fe, ce = eng.calc_escaped_distributions()
+            esc = eng.get_escaped_particles()
+        eng.reset_escaped_particles()
+    # escaped distributions and particles of the last frame (-ded, -de)
+    raw = (out / "fescaped_0003.dat").read_bytes()
+    npp, ncol = np.frombuffer(raw[:8], np.int32)
+    off = 8 + 8 * (npp + 1)
+    assert np.array_equal(np.frombuffer(raw[off:off + 8 * npp * ncol], np.float64), fe.ravel())
+    off += 8 * npp * ncol
+    assert np.array_equal(np.frombuffer(raw[off:off + 8 * npp * ncol], np.uint64), ce.ravel())
+    d = read_particle_dump(out / "escaped_particles_0003.dat")
+    assert len(d["x"]) == len(esc) > 0
+    for k in d:
+        assert np.array_equal(d[k], esc[k]), k
     f, c = eng.calc_particle_distributions()
     assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)
     np.testing.assert_allclose(edges, eng.pbins_edges(), rtol=0)
