@@ -248,19 +248,24 @@ static void spherical_weights(int ndim, double x, double y, double z, int32_t po
 {
     const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
     pos[0] = grid_count(0, x) - 2;
-    pos[1] = grid_count(1, y) - 2;
+    pos[1] = (ndim > 1) ? grid_count(1, y) - 2 : 1;
     pos[2] = (ndim == 3) ? grid_count(2, z) - 2 : 1;
     /* xpos_local(i) is X[i + 1]. */
-    const double ctheta1 = cos(Y[pos[1] + 1]);
-    const double ctheta2 = cos(Y[pos[1] + 2]);
-    const double ctheta = cos(y);
     const double one_third = 1.0 / 3.0;
     const double x3 = x * x * x * one_third;
     const double xa = X[pos[0] + 1], xb = X[pos[0] + 2];
     const double x3_1 = xa * xa * xa * one_third;
     const double x3_2 = xb * xb * xb * one_third;
     const double rx = x3 - x3_1, rx1 = x3_2 - x3;
-    const double ry = ctheta1 - ctheta, ry1 = ctheta - ctheta2;
+    double ry = 0.0, ry1 = 1.0;
+    if (ndim > 1) {
+        const double ctheta1 = cos(Y[pos[1] + 1]);
+        const double ctheta2 = cos(Y[pos[1] + 2]);
+        const double ctheta = cos(y);
+        ry = ctheta1 - ctheta;
+        ry1 = ctheta - ctheta2;
+    }
+    /* rz = 0, rz1 = 1 below 3D (1D leaves them unset in the reference) */
     double rz = 0.0, rz1 = 1.0;
     if (ndim == 3) {
         rz = z - Z[pos[2] + 1];
@@ -298,14 +303,14 @@ void orc_grid_interp_paramters(const orc_params *pr, const orc_mhd_config *cfg, 
      * intended cell). */
     const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
     const int ix = grid_count(0, x) - 2;
-    const int iy = grid_count(1, y) - 2;
+    const int iy = (ndim > 1) ? grid_count(1, y) - 2 : 1;
     const int iz = (ndim == 3) ? grid_count(2, z) - 2 : 1;
     const double px = (x - X[ix + 1]) / (X[ix + 2] - X[ix + 1]);
-    const double py = (y - Y[iy + 1]) / (Y[iy + 2] - Y[iy + 1]);
+    const double py = (ndim > 1) ? (y - Y[iy + 1]) / (Y[iy + 2] - Y[iy + 1]) : 0.0;
     const double pz = (ndim == 3) ? (z - Z[iz + 1]) / (Z[iz + 2] - Z[iz + 1]) : 0.0;
     orc_get_interp_paramters(ndim, px, py, pz, pos, w);
     pos[0] += ix - 1;
-    pos[1] += iy - 1;
+    if (ndim > 1) pos[1] += iy - 1;
     if (ndim == 3) pos[2] += iz - 1;
     const int hi[3] = {g_grid.n[0] - 3, g_grid.n[1] - 3, (ndim == 3) ? g_grid.n[2] - 3 : 1};
     for (int a = 0; a < ndim; ++a)
@@ -324,7 +329,12 @@ void orc_get_interp_paramters(int ndim, double px, double py, double pz,
 {
     double rx, ry, rz;
     pos[0] = (int32_t)floor(px) + 1;
-    if (ndim == 2) {
+    if (ndim == 1) {
+        pos[1] = 1;
+        pos[2] = 1;
+        ry = 0.0;
+        rz = 0.0;
+    } else if (ndim == 2) {
         pos[1] = (int32_t)floor(py) + 1;
         pos[2] = 1;
         ry = (py - (double)pos[1]) + 1.0;
@@ -355,13 +365,14 @@ void orc_interp_fields(const float *f1, const float *f2, int time_interp, int nd
                        int nxg, int nyg, const int32_t pos[3], const double w[8],
                        double rt, double fields[32])
 {
-    const int ix = pos[0] + 1, iy = pos[1] + 1;
+    /* 1D arrays are declared (-1:nx+2, 1, 1): y is index 0 there */
+    const int ix = pos[0] + 1, iy = (ndim > 1) ? pos[1] + 1 : 0;
     const int iz = (ndim == 3) ? pos[2] + 1 : 0;
-    const int ze = (ndim == 3) ? 1 : 0;
+    const int ze = (ndim == 3) ? 1 : 0, ye = (ndim > 1) ? 1 : 0;
     double fields2[32];
     for (int v = 0; v < 32; ++v) { fields[v] = 0.0; fields2[v] = 0.0; }
     for (int k = 0; k <= ze; ++k)
-        for (int j = 0; j <= 1; ++j)
+        for (int j = 0; j <= ye; ++j)
             for (int i = 0; i <= 1; ++i) {
                 const int idx = k * 4 + j * 2 + i;
                 const size_t c = 32u * ((size_t)(ix + i) + (size_t)nxg * ((size_t)(iy + j) + (size_t)nyg * (size_t)(iz + k)));
@@ -379,13 +390,13 @@ void orc_interp_fields(const float *f1, const float *f2, int time_interp, int nd
 void orc_interp_aux(const float *a1, const float *a2, int time_interp, int ndim, int nxg,
                     int nyg, const int32_t pos[3], const double w[8], double rt, double out[16])
 {
-    const int ix = pos[0] + 1, iy = pos[1] + 1;
+    const int ix = pos[0] + 1, iy = (ndim > 1) ? pos[1] + 1 : 0;
     const int iz = (ndim == 3) ? pos[2] + 1 : 0;
-    const int ze = (ndim == 3) ? 1 : 0;
+    const int ze = (ndim == 3) ? 1 : 0, ye = (ndim > 1) ? 1 : 0;
     double o2[16];
     for (int v = 0; v < 16; ++v) { out[v] = 0.0; o2[v] = 0.0; }
     for (int k = 0; k <= ze; ++k)
-        for (int j = 0; j <= 1; ++j)
+        for (int j = 0; j <= ye; ++j)
             for (int i = 0; i <= 1; ++i) {
                 const int idx = k * 4 + j * 2 + i;
                 const size_t c = 16u * ((size_t)(ix + i) + (size_t)nxg * ((size_t)(iy + j) + (size_t)nyg * (size_t)(iz + k)));
@@ -480,6 +491,35 @@ void orc_calc_spatial_diffusion_coefficients(const orc_params *pr, double p, dou
     kap[K_SKPERP] = sqrt(2.0 * kperp);
     kap[K_SKPARA_PERP] = sqrt(2.0 * (kpara - kperp));
     const double kpp = pr->focused_transport ? -kperp : kpara - kperp;
+    if (pr->ndim == 1) {
+        /* the 1D branches (:2270-2291, :2536-2562): only dkxx_dx, and kxx
+         * for spherical coordinates */
+        for (int k = K_KXX; k <= K_DKYZ_DZ; ++k) kap[k] = 0.0;
+        const double dbdx = f[29];
+        double dk = 0.0, dkperp = 0.0;
+        if (pr->mag_dependency == 1) {
+            dk = dbdx * ib1 * (pr->gamma_turb - 2.0);
+            dkperp = dbdx * ib1 * (pr->gamma_turb - 2.0) / 3.0;
+        }
+        if (dbf) {
+            dk = dk - s2[1] / s2[0];
+            dkperp = dkperp - s2[1] / s2[0] / 3.0 + 2.0 * d2[1] / d2[0] / 3.0;
+        }
+        if (lcf) {
+            dk = dk + (pr->gamma_turb - 1.0) * l1[1] / l1[0];
+            dkperp = dkperp + (pr->gamma_turb - 1.0) * l1[1] / l1[0] / 3.0 +
+                     2.0 * l2[1] / l2[0] / 3.0;
+        }
+        if (!pr->nlgc) dkperp = dk;   /* the fixed-ratio branch has one dkdx */
+        if (pr->focused_transport) {
+            kap[K_DKXX_DX] = kperp * dkperp;
+            if (pr->spherical_coord) kap[K_KXX] = kperp;
+        } else {
+            kap[K_DKXX_DX] = kpara * dk;
+            if (pr->spherical_coord) kap[K_KXX] = kpara;
+        }
+        return;
+    }
 
     const double dbx_dx = f[20], dbx_dy = f[21], dbx_dz = f[22];
     const double dby_dx = f[23], dby_dy = f[24], dby_dz = f[25];
@@ -832,7 +872,8 @@ static double dpp_terms(const orc_params *pr, double p, const double *f, const d
         const double sxx = f[8] - divv / 3.0;
         const double syy = f[12] - divv / 3.0;
         const double szz = d3 ? f[16] - divv / 3.0 : -(divv / 3.0);
-        const double sxy = (f[9] + f[11]) / 2.0;
+        /* the 1D pushes pass zero off-diagonal shear (:3052-3057) */
+        const double sxy = pr->ndim > 1 ? (f[9] + f[11]) / 2.0 : 0.0;
         const double sxz = d3 ? (f[10] + f[14]) / 2.0 : 0.0;
         const double syz = d3 ? (f[13] + f[15]) / 2.0 : 0.0;
         const double bx = f[4], by = f[5], bz = f[6];
@@ -1472,6 +1513,109 @@ static void push_3d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
     push_ft_tail(c, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
+/* push_particle_1d: particle_module.f90:2993-3110, Cartesian or spherical
+ * (x = r).  r[0] drives x, r[3] momentum. */
+static void push_1d(const mover_ctx *c, ptl_state *s, const double *f, const double *kap,
+                    const cell_size *cs, int fixed_dt, double d[6])
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double dvx_dx = f[8];
+    double dx_dt, divv;
+    if (c->sph) {
+        dx_dt = vx + kap[K_DKXX_DX] + 2.0 * kap[K_KXX] / s->x;
+        divv = dvx_dx + 2.0 * vx / s->x;
+    } else {
+        dx_dt = vx + kap[K_DKXX_DX];
+        divv = dvx_dx;
+    }
+    double dp_dt = -(s->p * divv / 3.0);
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
+    const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dp_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double a = 0.5 * cs->dxm / skpara, m = a * a;
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
+            s->dt = m;
+        } else {
+            s->dt = c->dt_min;
+        }
+        if (s->dt < c->dt_min) s->dt = c->dt_min;
+        if (s->dt > c->dt_max) s->dt = c->dt_max;
+    }
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double dX = dx_dt * s->dt + r[0] * skpara * sdt;
+    s->x = s->x + dX;
+    s->t = s->t + s->dt;
+    d[0] = dX; d[1] = 0.0; d[2] = 0.0; d[4] = 0.0; d[5] = 0.0;
+    push_momentum(c, s, dp_dt, dpp, sdt, r[3], &d[3]);
+}
+
+/* push_particle_1d_ft: particle_module.f90:3174-3357.  The reference
+ * computes the x rate into dv_dt and then reads dx_dt, which it never
+ * sets; the rate it computed is used here.  r[0] drives x, r[2] momentum,
+ * r[3] pitch angle. */
+static void push_1d_ft(const mover_ctx *c, ptl_state *s, const double *f, const double *aux,
+                       const double *kap, const cell_size *cs, int fixed_dt, double d[6])
+{
+    const orc_params *pr = c->pr;
+    const double vx = f[0], vy = f[1], vz = f[2], bx = f[4], by = f[5], bz = f[6];
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double dvx_dx = f[8], dvy_dx = f[11], dvz_dx = f[14];
+    double dx_dt, divv, bb_gradv, bv_gradv;
+    if (c->sph) {
+        const double ir = 1.0 / s->x;
+        dx_dt = vx + s->v * s->mu + kap[K_DKXX_DX] + 2.0 * kap[K_KXX] * ir;
+        const double cot = 1.0 / tan(s->y);
+        divv = dvx_dx + 2.0 * vx * ir;
+        bb_gradv = (bx * bx * dvx_dx - bx * (by * vy + bz * vz) * ir + by * bx * dvy_dx +
+                    by * (by * vx - cot * bz * vz) * ir + bz * bx * dvz_dx +
+                    (bz * bz) * (vx + cot * vy) * ir) / (b * b);
+        bv_gradv = (bx * vx * dvx_dx - bx * (vy * vy + vz * vz) * ir + by * vx * dvy_dx +
+                    by * (vy * vx - cot * vz * vz) * ir + bz * vx * dvz_dx +
+                    bz * vz * (vx + cot * vy) * ir) / (b * b);
+    } else {
+        dx_dt = vx + s->v * s->mu + kap[K_DKXX_DX];
+        divv = dvx_dx;
+        bb_gradv = (bx * bx * dvx_dx + by * bx * dvy_dx + bz * bx * dvz_dx) / (b * b);
+        bv_gradv = (bx * vx * dvx_dx + by * vx * dvy_dx + bz * vx * dvz_dx) / b;
+    }
+    const double mu2 = s->mu * s->mu;
+    const double acc_rate = -(0.5 * (1.0 - mu2) * divv + 0.5 * (3.0 * mu2 - 1.0) * bb_gradv +
+                              s->mu * bv_gradv / s->v);
+    double dp_dt = s->p * acc_rate;
+    const double dpp = dpp_terms(pr, s->p, f, kap, b, divv, &dp_dt);
+    const double div_bnorm = -(bx * f[29] / (b * b));
+    double dmu_dt, duu, duu_du;
+    calc_duu(pr, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, &dmu_dt, &duu, &duu_du);
+    const double skpara = kap[K_SKPARA], skperp = kap[K_SKPERP];
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dp_dt != 0.0 && dmu_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double a = 0.5 * cs->dxm / sk, m = a * a;
+            a = sk / dx_dt; if (a * a < m) m = a * a;
+            a = (double)0.1f * s->p / fabs(dp_dt); if (a < m) m = a;
+            a = (double)0.1f / fabs(dmu_dt); if (a < m) m = a;
+            a = 2.0 * duu / (dmu_dt * dmu_dt); if (a < m) m = a;
+            s->dt = m;
+        } else {
+            s->dt = c->dt_min;
+        }
+        if (s->dt < c->dt_min) s->dt = c->dt_min;
+        if (s->dt > c->dt_max) s->dt = c->dt_max;
+    }
+    const double sdt = sqrt(s->dt);
+    double r[4];
+    push_noise(c, s, r);
+    const double dX = dx_dt * s->dt + r[0] * skpara * sdt;
+    push_ft_tail(c, s, dX, 0.0, 0.0, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
+}
+
 /* particle_boundary_condition on a single rank: particle_module.f90:1984-2129.
  * A periodic direction has itself as neighbour and wraps by the box passed
  * in; an open direction escapes with count_flag -1..-6 and adds to leak. */
@@ -1531,9 +1675,12 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
         if (c->nonuni) {
             /* the pushes search the cell again (:3404-3407, :4693-4699) */
             const double *X = g_grid.pos[0], *Y = g_grid.pos[1], *Z = g_grid.pos[2];
-            const int ix = grid_count(0, s->x) - 2, iy = grid_count(1, s->y) - 2;
+            const int ix = grid_count(0, s->x) - 2;
             cs.dxm = X[ix + 2] - X[ix + 1];
-            cs.dym = Y[iy + 2] - Y[iy + 1];
+            if (c->ndim > 1) {
+                const int iy = grid_count(1, s->y) - 2;
+                cs.dym = Y[iy + 2] - Y[iy + 1];
+            }
             if (c->ndim == 3) {
                 const int iz = grid_count(2, s->z) - 2;
                 cs.dzm = Z[iz + 2] - Z[iz + 1];
@@ -1554,10 +1701,12 @@ static void do_push(const mover_ctx *c, ptl_state *s, int fixed_dt, double d[6])
     }
     orc_calc_spatial_diffusion_coefficients(c->pr, s->p, s->mu, f, ap, kap);
     if (c->pr->focused_transport) {
-        if (c->ndim == 2 && !c->i3) push_2d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
+        if (c->ndim == 1) push_1d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
+        else if (c->ndim == 2 && !c->i3) push_2d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
         else push_3d_ft(c, s, f, ap, kap, &cs, fixed_dt, d);
     } else {
-        if (c->ndim == 2 && !c->i3) push_2d(c, s, f, kap, &cs, fixed_dt, d);
+        if (c->ndim == 1) push_1d(c, s, f, kap, &cs, fixed_dt, d);
+        else if (c->ndim == 2 && !c->i3) push_2d(c, s, f, kap, &cs, fixed_dt, d);
         else push_3d(c, s, f, kap, &cs, fixed_dt, d);
     }
 }
@@ -1737,7 +1886,7 @@ static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *
     c->pr = pr; c->f1 = f1; c->f2 = f2; c->time_interp = time_interp;
     c->ndim = pr->ndim;
     c->nxg = cfg->nx + 4;
-    c->nyg = cfg->ny + 4;
+    c->nyg = (pr->ndim == 1) ? 1 : cfg->ny + 4;   /* 1D arrays are (-1:nx+2, 1, 1) */
     c->dx = cfg->dx; c->dy = cfg->dy; c->dz = cfg->dz;
     /* set_field_configuration on one rank: simulation_setup.f90:171-253. */
     c->xmin = cfg->xmin;
