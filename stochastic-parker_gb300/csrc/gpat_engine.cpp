@@ -471,10 +471,10 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     if (!params || !cfg || !out) return GPAT_ERR_ARG;
     *out = nullptr;
     const gpat_params_t &p = *params;
-    if (p.ndim != 2 && p.ndim != 3) return GPAT_ERR_UNSUPPORTED;
+    if (p.ndim < 1 || p.ndim > 3) return GPAT_ERR_UNSUPPORTED;
     if (p.include_3rd_dim && p.ndim != 2) return GPAT_ERR_ARG;
     if ((p.dpp_wave || p.dpp_shear || p.deltab_flag || p.correlation_flag || p.spherical_coord ||
-         p.nonuniform_grid || p.include_3rd_dim) &&
+         p.nonuniform_grid || p.include_3rd_dim || p.ndim == 1) &&
         p.precision != GPAT_PREC_FP64)
         return GPAT_ERR_UNSUPPORTED;
     if (p.precision != GPAT_PREC_FP64 && p.precision != GPAT_PREC_MIXED) return GPAT_ERR_ARG;
@@ -504,8 +504,10 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
     // init_field_data (mhd_data_parallel.f90:66-105): ghost cells on each
     // resolved side; the z extent of a 2D run is nz (one plane).
     h->nxg = cfg->nx + 4;
-    h->nyg = cfg->ny + 4;
+    // 1D arrays are (-1:nx+2, 1, 1) (init_field_data :80-81)
+    h->nyg = (p.ndim == 1) ? 1 : cfg->ny + 4;
     h->nzg = (p.ndim == 3) ? cfg->nz + 4 : std::max(1, cfg->nz);
+    if (p.ndim == 1) h->nzg = 1;
     if (p.ndim == 2 && h->nzg != 1) return bail(GPAT_ERR_UNSUPPORTED);
     h->ncells = (size_t)h->nxg * h->nyg * h->nzg;
     h->nslots = p.time_interp ? 2 : 1;
@@ -973,6 +975,8 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
 int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin, const double part_box[6],
                            int64_t *ncells) {
     if (!h || !part_box || !ncells) return GPAT_ERR_ARG;
+    if (h->prm.ndim == 1)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "large-quantity injection is 2D and 3D only");
     if (quantity < GPAT_LARGE_JZ || quantity > GPAT_LARGE_DB2)
         return fail(h, GPAT_ERR_ARG, "quantity must be one of GPAT_LARGE_*");
     if (quantity == GPAT_LARGE_DB2 && !h->aux[0])
@@ -994,6 +998,8 @@ int gpat_inject_particles_at_large(gpat_handle_t *h, int quantity, int64_t nptl,
                                    const double part_box[6], double power_index,
                                    int64_t *ninjected) {
     if (!h || !part_box) return GPAT_ERR_ARG;
+    if (h->prm.ndim == 1)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "large-quantity injection is 2D and 3D only");
     if (nptl < 0) return fail(h, GPAT_ERR_ARG, "nptl < 0");
     if (!inject_same_nptl && ncells_norm <= 0)
         return fail(h, GPAT_ERR_ARG, "ncells_norm must be > 0");

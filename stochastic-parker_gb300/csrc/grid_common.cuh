@@ -44,20 +44,17 @@ __device__ __forceinline__ bool grid_cell(int ndim, int spherical, const double 
                                           int nxg, const double *__restrict__ Y, int nyg,
                                           const double *__restrict__ Z, int nzg, double x,
                                           double y, double z, GridCell &c) {
-    if (!grid_inside(X, nxg, x) || !grid_inside(Y, nyg, y) ||
+    if (!grid_inside(X, nxg, x) || (ndim > 1 && !grid_inside(Y, nyg, y)) ||
         (ndim == 3 && !grid_inside(Z, nzg, z)))
         return false;
     c.kx = grid_count(X, nxg, x);
-    c.ky = grid_count(Y, nyg, y);
+    c.ky = (ndim > 1) ? grid_count(Y, nyg, y) : 1;   // 1D: y node 0
     c.kz = (ndim == 3) ? grid_count(Z, nzg, z) : 0;
     double rx, ry, rz, rx1, ry1, rz1;
     if (spherical) {
         c.ix = c.kx - 1;
         c.iy = c.ky - 1;
         c.iz = (ndim == 3) ? c.kz - 1 : 0;
-        const double ctheta1 = cos(__ldg(Y + c.iy));
-        const double ctheta2 = cos(__ldg(Y + c.iy + 1));
-        const double ctheta = cos(y);
         const double one_third = 1.0 / 3.0;
         const double xa = __ldg(X + c.ix), xb = __ldg(X + c.ix + 1);
         const double x3 = x * x * x * one_third;
@@ -65,8 +62,16 @@ __device__ __forceinline__ bool grid_cell(int ndim, int spherical, const double 
         const double x3_2 = xb * xb * xb * one_third;
         rx = x3 - x3_1;
         rx1 = x3_2 - x3;
-        ry = ctheta1 - ctheta;
-        ry1 = ctheta - ctheta2;
+        if (ndim > 1) {
+            const double ctheta1 = cos(__ldg(Y + c.iy));
+            const double ctheta2 = cos(__ldg(Y + c.iy + 1));
+            const double ctheta = cos(y);
+            ry = ctheta1 - ctheta;
+            ry1 = ctheta - ctheta2;
+        } else {
+            ry = 0.0;
+            ry1 = 1.0;
+        }
         if (ndim == 3) {
             rz = z - __ldg(Z + c.iz);
             rz1 = __ldg(Z + c.iz + 1) - z;
@@ -87,18 +92,19 @@ __device__ __forceinline__ bool grid_cell(int ndim, int spherical, const double 
     }
     const int lx = c.kx - 1, ly = c.ky - 1, lz = (ndim == 3) ? c.kz - 1 : 0;
     const double px = (x - __ldg(X + lx)) / (__ldg(X + lx + 1) - __ldg(X + lx));
-    const double py = (y - __ldg(Y + ly)) / (__ldg(Y + ly + 1) - __ldg(Y + ly));
+    const double py = (ndim > 1) ? (y - __ldg(Y + ly)) / (__ldg(Y + ly + 1) - __ldg(Y + ly)) : 0.0;
     const double pz = (ndim == 3) ? (z - __ldg(Z + lz)) / (__ldg(Z + lz + 1) - __ldg(Z + lz))
                                   : 0.0;
-    const int fx = (int)floor(px), fy = (int)floor(py);
+    const int fx = (int)floor(px), fy = (ndim > 1) ? (int)floor(py) : 0;
     const int fz = (ndim == 3) ? (int)floor(pz) : 0;
     rx = (px - (double)(fx + 1)) + 1.0;
-    ry = (py - (double)(fy + 1)) + 1.0;
+    ry = (ndim > 1) ? (py - (double)(fy + 1)) + 1.0 : 0.0;
     rz = (ndim == 3) ? (pz - (double)(fz + 1)) + 1.0 : 0.0;
     c.ix = lx + fx;
     c.iy = ly + fy;
     c.iz = (ndim == 3) ? lz + fz : 0;
-    if (c.ix > nxg - 2 || c.iy > nyg - 2 || (ndim == 3 && c.iz > nzg - 2)) return false;
+    if (c.ix > nxg - 2 || (ndim > 1 && c.iy > nyg - 2) || (ndim == 3 && c.iz > nzg - 2))
+        return false;
     rx1 = 1.0 - rx;
     ry1 = 1.0 - ry;
     rz1 = 1.0 - rz;

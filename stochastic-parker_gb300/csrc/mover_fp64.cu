@@ -80,16 +80,17 @@ __device__ __forceinline__ bool uniform_cell(const MoverArgs &a, const State &s,
     const double py = (s.y - a.ymin) / a.dy;
     const double pz = (s.z - a.zmin) / a.dz;
     const int nx = a.nxg - 4, ny = a.nyg - 4, nz = a.nzg - 4;
-    if (!(px >= -1.0 && px < nx + 1.0) || !(py >= -1.0 && py < ny + 1.0) ||
+    if (!(px >= -1.0 && px < nx + 1.0) || (NDIM > 1 && !(py >= -1.0 && py < ny + 1.0)) ||
         (NDIM == 3 && !(pz >= -1.0 && pz < nz + 1.0))) {
         set_status(a.cnt, kStatusIndexGuard);
         return false;
     }
-    // get_interp_paramters: pos = floor(p) + 1 (Fortran), r = p - pos + 1.
-    const int fx = (int)floor(px), fy = (int)floor(py);
+    // get_interp_paramters: pos = floor(p) + 1 (Fortran), r = p - pos + 1;
+    // 1D: pos = (floor(px) + 1, 1, 1), ry = rz = 0 (:649-652).
+    const int fx = (int)floor(px), fy = (NDIM > 1) ? (int)floor(py) : -2;
     const int fz = (NDIM == 3) ? (int)floor(pz) : 0;
     const double rx = (px - (double)(fx + 1)) + 1.0;
-    const double ry = (py - (double)(fy + 1)) + 1.0;
+    const double ry = (NDIM > 1) ? (py - (double)(fy + 1)) + 1.0 : 0.0;
     const double rz = (NDIM == 3) ? (pz - (double)(fz + 1)) + 1.0 : 0.0;
     const double rx1 = 1.0 - rx, ry1 = 1.0 - ry, rz1 = 1.0 - rz;
     w[0] = rx1 * ry1 * rz1;
@@ -101,7 +102,7 @@ __device__ __forceinline__ bool uniform_cell(const MoverArgs &a, const State &s,
     w[6] = rx1 * ry * rz;
     w[7] = rx * ry * rz;
     ix = fx + 2;
-    iy = fy + 2;
+    iy = fy + 2;   // 0 in 1D, whose arrays have one y node
     iz = (NDIM == 3) ? fz + 2 : 0;
     return true;
 }
@@ -117,7 +118,7 @@ __device__ __forceinline__ void interp_at(const MoverArgs &a, const float *rec1,
 #pragma unroll
     for (int k = 0; k < (NDIM == 3 ? 2 : 1); ++k)
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+        for (int j = 0; j < (NDIM >= 2 ? 2 : 1); ++j)
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
                 const double wc = w[k * 4 + j * 2 + i];
@@ -396,6 +397,31 @@ __device__ __forceinline__ Kap kappa(const MoverArgs &a, double p, double mu, co
     k.skperp = sqrt(2.0 * kperp);
     k.skpp = sqrt(2.0 * (kpara - kperp));
     const double kpp = FT ? -kperp : kpara - kperp;
+    if (NDIM == 1) {
+        // the 1D branches (:2270-2291, :2536-2562): dkxx_dx, and kxx for
+        // spherical coordinates
+        double dk = 0.0, dkperp = 0.0;
+        if (a.mag_dependency == 1) {
+            dk = f.db_dx * ib1 * (a.gamma_turb - 2.0);
+            dkperp = f.db_dx * ib1 * (a.gamma_turb - 2.0) / 3.0;
+        }
+        if (dbf) {
+            dk = dk - s2[1] / s2[0];
+            dkperp = dkperp - s2[1] / s2[0] / 3.0 + 2.0 * d2[1] / d2[0] / 3.0;
+        }
+        if (lcf) {
+            dk = dk + (a.gamma_turb - 1.0) * l1[1] / l1[0];
+            dkperp = dkperp + (a.gamma_turb - 1.0) * l1[1] / l1[0] / 3.0 +
+                     2.0 * l2[1] / l2[0] / 3.0;
+        }
+        if (!a.nlgc) dkperp = dk;
+        k.dkxx_dx = FT ? kperp * dkperp : kpara * dk;
+        k.kxx = a.spherical ? (FT ? kperp : kpara) : 0.0;
+        k.dkyy_dy = 0.0; k.dkzz_dz = 0.0; k.dkxy_dx = 0.0; k.dkxy_dy = 0.0;
+        k.dkxz_dx = 0.0; k.dkxz_dz = 0.0; k.dkyz_dy = 0.0; k.dkyz_dz = 0.0;
+        k.kyy = 0.0; k.kzz = 0.0; k.kxy = 0.0; k.kxz = 0.0; k.kyz = 0.0;
+        return k;
+    }
     const double db[3] = {f.db_dx, f.db_dy, f.db_dz};
     const double g2 = a.gamma_turb - 2.0;
     double T[3] = {0.0, 0.0, 0.0}, A[3] = {0.0, 0.0, 0.0};
@@ -475,7 +501,8 @@ __device__ __forceinline__ double dpp_terms(const MoverArgs &a, double p, const 
         const double sxx = f.dvx_dx - divv / 3.0;
         const double syy = f.dvy_dy - divv / 3.0;
         const double szz = (NDIM == 3) ? f.dvz_dz - divv / 3.0 : -(divv / 3.0);
-        const double sxy = (f.dvx_dy + f.dvy_dx) / 2.0;
+        // the 1D pushes pass zero off-diagonal shear (:3052-3057)
+        const double sxy = (NDIM > 1) ? (f.dvx_dy + f.dvy_dx) / 2.0 : 0.0;
         const double sxz = (NDIM == 3) ? (f.dvx_dz + f.dvz_dx) / 2.0 : 0.0;
         const double syz = (NDIM == 3) ? (f.dvy_dz + f.dvz_dy) / 2.0 : 0.0;
         const double bx = f.bx, by = f.by, bz = f.bz;
@@ -1082,12 +1109,14 @@ __device__ __forceinline__ void boundary(const MoverArgs &a, State &s, double xl
         if (a.pbcx) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -2; }
         else s.x = s.x - xhi + xlo;
     }
-    if (s.y < ylo && s.flag == 1) {
-        if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -3; }
-        else s.y = s.y - ylo + yhi;
-    } else if (s.y > yhi && s.flag == 1) {
-        if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -4; }
-        else s.y = s.y - yhi + ylo;
+    if (NDIM > 1) {
+        if (s.y < ylo && s.flag == 1) {
+            if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -3; }
+            else s.y = s.y - ylo + yhi;
+        } else if (s.y > yhi && s.flag == 1) {
+            if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -4; }
+            else s.y = s.y - yhi + ylo;
+        }
     }
     if (NDIM == 3 || a.include_3rd) {   // z too for include_3rd_dim runs (:2084)
         if (s.z < zlo && s.flag == 1) {
@@ -1110,6 +1139,106 @@ __device__ __forceinline__ void negp_or_boundary(const MoverArgs &a, State &s, A
     }
 }
 
+// push_particle_1d (:2993-3110), Cartesian or spherical (x = r); r[0]
+// drives x, r[3] momentum.
+template <bool SPH>
+__device__ __forceinline__ void push1d(const MoverArgs &a, State &s, const Fld &f, const Kap &k,
+                                       const Geo &geo, bool fixed_dt, Delta &d) {
+    const double bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    double dx_dt, divv;
+    if (SPH) {
+        dx_dt = f.vx + k.dkxx_dx + 2.0 * k.kxx / s.x;
+        divv = f.dvx_dx + 2.0 * f.vx / s.x;
+    } else {
+        dx_dt = f.vx + k.dkxx_dx;
+        divv = f.dvx_dx;
+    }
+    double dp_dt = -(s.p * divv / 3.0);
+    const double dpp = dpp_terms<1>(a, s.p, f, k, b, divv, dp_dt);
+    const double skpara = k.skpara, skperp = k.skperp;
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dp_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double q = 0.5 * geo.dxm / skpara, m = q * q;
+            q = sk / dx_dt; if (q * q < m) m = q * q;
+            q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
+            s.dt = m;
+        } else {
+            s.dt = a.dt_min;
+        }
+        if (s.dt < a.dt_min) s.dt = a.dt_min;
+        if (s.dt > a.dt_max) s.dt = a.dt_max;
+    }
+    const double sdt = sqrt(s.dt);
+    double r[4];
+    noise4(a, s, r);
+    const double dX = dx_dt * s.dt + r[0] * skpara * sdt;
+    s.x = s.x + dX;
+    s.t = s.t + s.dt;
+    d.x = dX; d.y = 0.0; d.z = 0.0; d.v = 0.0; d.mu = 0.0;
+    push_momentum(a, s, dp_dt, dpp, sdt, r[3], 1, d.p);
+}
+
+// push_particle_1d_ft (:3174-3357).  The reference computes the x rate into
+// dv_dt and then reads dx_dt, which it never sets; the computed rate is
+// used.  r[0] drives x, r[2] momentum, r[3] pitch angle.
+template <bool SPH>
+__device__ __forceinline__ void push_ft1d(const MoverArgs &a, State &s, const Fld &f,
+                                          const double *aux, const Kap &k, const Geo &geo,
+                                          bool fixed_dt, Delta &d) {
+    const double vx = f.vx, vy = f.vy, vz = f.vz, bx = f.bx, by = f.by, bz = f.bz;
+    const double b = sqrt(bx * bx + by * by + bz * bz);
+    const double dvx_dx = f.dvx_dx, dvy_dx = f.dvy_dx, dvz_dx = f.dvz_dx;
+    double dx_dt, divv, bb_gradv, bv_gradv;
+    if (SPH) {
+        const double ir = 1.0 / s.x;
+        dx_dt = vx + s.v * s.mu + k.dkxx_dx + 2.0 * k.kxx * ir;
+        const double cot = 1.0 / tan(s.y);
+        divv = dvx_dx + 2.0 * vx * ir;
+        bb_gradv = (bx * bx * dvx_dx - bx * (by * vy + bz * vz) * ir + by * bx * dvy_dx +
+                    by * (by * vx - cot * bz * vz) * ir + bz * bx * dvz_dx +
+                    (bz * bz) * (vx + cot * vy) * ir) / (b * b);
+        bv_gradv = (bx * vx * dvx_dx - bx * (vy * vy + vz * vz) * ir + by * vx * dvy_dx +
+                    by * (vy * vx - cot * vz * vz) * ir + bz * vx * dvz_dx +
+                    bz * vz * (vx + cot * vy) * ir) / (b * b);
+    } else {
+        dx_dt = vx + s.v * s.mu + k.dkxx_dx;
+        divv = dvx_dx;
+        bb_gradv = (bx * bx * dvx_dx + by * bx * dvy_dx + bz * bx * dvz_dx) / (b * b);
+        bv_gradv = (bx * vx * dvx_dx + by * vx * dvy_dx + bz * vx * dvz_dx) / b;
+    }
+    const double mu2 = s.mu * s.mu;
+    const double acc_rate = -(0.5 * (1.0 - mu2) * divv + 0.5 * (3.0 * mu2 - 1.0) * bb_gradv +
+                              s.mu * bv_gradv / s.v);
+    double dp_dt = s.p * acc_rate;
+    const double dpp = dpp_terms<1>(a, s.p, f, k, b, divv, dp_dt);
+    const double div_bnorm = -(bx * f.db_dx / (b * b));
+    double dmu_dt, duu;
+    calc_duu(a, s, b, aux, div_bnorm, divv, bb_gradv, bv_gradv, mu2, dmu_dt, duu);
+    const double skpara = k.skpara, skperp = k.skperp;
+    if (!fixed_dt) {
+        if (dx_dt != 0.0 && dp_dt != 0.0 && dmu_dt != 0.0) {
+            const double sk = (skperp > 0.0) ? skperp : skpara;
+            double q = 0.5 * geo.dxm / sk, m = q * q;
+            q = sk / dx_dt; if (q * q < m) m = q * q;
+            q = (double)0.1f * s.p / fabs(dp_dt); if (q < m) m = q;
+            q = (double)0.1f / fabs(dmu_dt); if (q < m) m = q;
+            q = 2.0 * duu / (dmu_dt * dmu_dt); if (q < m) m = q;
+            s.dt = m;
+        } else {
+            s.dt = a.dt_min;
+        }
+        if (s.dt < a.dt_min) s.dt = a.dt_min;
+        if (s.dt > a.dt_max) s.dt = a.dt_max;
+    }
+    const double sdt = sqrt(s.dt);
+    double r[4];
+    noise4(a, s, r);
+    const double dX = dx_dt * s.dt + r[0] * skpara * sdt;
+    push_ft_tail<1>(a, s, dX, 0.0, 0.0, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
+}
+
 // kappa and the push for interpolated fields f: NDIM-dimensional, or the 3D
 // push on 2D data for include_3rd_dim runs (I3).
 template <int NDIM, bool FT, bool SPH, bool I3>
@@ -1120,6 +1249,10 @@ __device__ __forceinline__ void run_push(const MoverArgs &a, State &s, const Fld
         const Kap k = kappa<3, FT, true>(a, s.p, s.mu, f, aux);
         if (FT) push_ft<3, SPH, true>(a, s, f, aux, k, geo, fixed_dt, d);
         else push3d<SPH, true>(a, s, f, k, geo, fixed_dt, d);
+    } else if (NDIM == 1) {
+        const Kap k = kappa<1, FT>(a, s.p, s.mu, f, aux);
+        if (FT) push_ft1d<SPH>(a, s, f, aux, k, geo, fixed_dt, d);
+        else push1d<SPH>(a, s, f, k, geo, fixed_dt, d);
     } else {
         const Kap k = kappa<NDIM, FT>(a, s.p, s.mu, f, aux);
         if (FT) push_ft<NDIM, SPH>(a, s, f, aux, k, geo, fixed_dt, d);
@@ -1154,7 +1287,7 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
         if (a.nonuniform) {
             // the pushes' own search (no offset shift): X[k] - X[k - 1]
             geo.dxm = __ldg(a.xpos + c.kx) - __ldg(a.xpos + c.kx - 1);
-            geo.dym = __ldg(a.ypos + c.ky) - __ldg(a.ypos + c.ky - 1);
+            if (NDIM > 1) geo.dym = __ldg(a.ypos + c.ky) - __ldg(a.ypos + c.ky - 1);
             if (NDIM == 3) geo.dzm = __ldg(a.zpos + c.kz) - __ldg(a.zpos + c.kz - 1);
         }
         if (a.spherical) run_push<NDIM, FT, true, I3>(a, s, f, aux, geo, fixed_dt, d);
@@ -1302,7 +1435,13 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s) 
                       a.surf_on;
     const bool grid = a.spherical || a.nonuniform;
     const unsigned g = (unsigned)blocks;
-    if (a.ndim == 2 && a.include_3rd) {
+    if (a.ndim == 1) {
+        // 1D runs always interpolate all 32 variables
+        if (grid && ft) mover_fp64_kernel<1, true, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (grid) mover_fp64_kernel<1, false, true, true, false><<<g, threads, 0, s>>>(a);
+        else if (ft) mover_fp64_kernel<1, true, true, false, false><<<g, threads, 0, s>>>(a);
+        else mover_fp64_kernel<1, false, true, false, false><<<g, threads, 0, s>>>(a);
+    } else if (a.ndim == 2 && a.include_3rd) {
         // 2D data, 3D transport: all 32 variables (the pushes read vz and
         // the in-plane gradients of bz and vz)
         if (grid && ft) mover_fp64_kernel<2, true, true, true, true><<<g, threads, 0, s>>>(a);

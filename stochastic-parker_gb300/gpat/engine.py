@@ -175,7 +175,7 @@ class Engine:
             raise GPATError(rc, "gpat_create failed")
         self.ndim = params.ndim
         self.nxg = mhd_config.nx + 4
-        self.nyg = mhd_config.ny + 4
+        self.nyg = mhd_config.ny + 4 if params.ndim > 1 else 1
         self.nzg = mhd_config.nz + 4 if params.ndim == 3 else 1
 
     # -- plumbing ---------------------------------------------------------------

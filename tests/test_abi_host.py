@@ -130,7 +130,8 @@ def test_mhd_config_file_roundtrip(tmp_path, engine_lib):
 def test_create_rejects_out_of_scope_options(engine_lib):
     cfg = make_mhd_config(16, 16, 1, 0.0, 1.0, 0.0, 1.0)
     h = _abi.Handle()
-    for kw, code in ((dict(ndim=1), _abi.GPAT_ERR_UNSUPPORTED),
+    for kw, code in ((dict(ndim=4), _abi.GPAT_ERR_UNSUPPORTED),
+                     (dict(ndim=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(dpp_wave=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(dpp_shear=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
                      (dict(deltab_flag=1, precision=1), _abi.GPAT_ERR_UNSUPPORTED),
