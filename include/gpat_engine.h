@@ -91,7 +91,9 @@ typedef struct gpat_params {
      * gpat_set_grid_positions when non-uniform); include_3rd_dim: a 2D
      * run whose particles also move along z with the 3D diffusion tensor
      * (push_particle_2d_include_3rd / _ft, particle_module.f90:3979-4610;
-     * ndim must be 2).  These seven need GPAT_PREC_FP64. */
+     * ndim must be 2).  These seven need GPAT_PREC_FP64, and so does
+     * ndim = 1 (push_particle_1d / _1d_ft, particle_module.f90:2993-3357;
+     * fields shaped (nx + 4, 1, 1)). */
     int32_t dpp_wave, dpp_shear, deltab_flag, correlation_flag, include_3rd_dim;
     int32_t spherical_coord, nonuniform_grid;
     /* Split-precision mover only: pushes per particle between re-binnings of

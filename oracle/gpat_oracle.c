@@ -1915,8 +1915,10 @@ static void setup_ctx(mover_ctx *c, const orc_params *pr, const orc_mhd_config *
         const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
         c->xmin1 = c->xmin - (X[3] - X[2]) * 0.5;
         c->xmax1 = xmax + (X[nx + 2] - X[nx + 1]) * 0.5;
-        c->ymin1 = c->ymin - (Y[3] - Y[2]) * 0.5;
-        c->ymax1 = ymax + (Y[ny + 2] - Y[ny + 1]) * 0.5;
+        if (pr->ndim > 1) {   /* 1D runs keep no y positions */
+            c->ymin1 = c->ymin - (Y[3] - Y[2]) * 0.5;
+            c->ymax1 = ymax + (Y[ny + 2] - Y[ny + 1]) * 0.5;
+        }
         if (pr->ndim == 3) {
             c->zmin1 = c->zmin - (Z[3] - Z[2]) * 0.5;
             c->zmax1 = zmax + (Z[nz + 2] - Z[nz + 1]) * 0.5;
@@ -2416,7 +2418,8 @@ void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spheri
         int ix, iy, iz;
         if (nonuniform) {
             ix = (orc_binary_search(g_grid.pos[0], g_grid.n[0], P->x[i]) - 1) / rx + 1;
-            iy = (orc_binary_search(g_grid.pos[1], g_grid.n[1], P->y[i]) - 1) / ry + 1;
+            iy = (ndim > 1) ? (orc_binary_search(g_grid.pos[1], g_grid.n[1], P->y[i]) - 1) / ry + 1
+                            : (int)floor((P->y[i] - cfg->ymin) / dyd) + 1;
             iz = (ndim == 3) ? (orc_binary_search(g_grid.pos[2], g_grid.n[2], P->z[i]) - 1) / rz + 1
                              : (int)floor((P->z[i] - cfg->zmin) / dzd) + 1;
         } else {

@@ -244,8 +244,10 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
         const std::vector<double> &X = h->gpos[0], &Y = h->gpos[1], &Z = h->gpos[2];
         a.xmin1 = a.xmin - (X[3] - X[2]) * 0.5;
         a.xmax1 = a.xmax + (X[c.nx + 2] - X[c.nx + 1]) * 0.5;
-        a.ymin1 = a.ymin - (Y[3] - Y[2]) * 0.5;
-        a.ymax1 = a.ymax + (Y[c.ny + 2] - Y[c.ny + 1]) * 0.5;
+        if (p.ndim > 1) {   // 1D runs keep no y positions
+            a.ymin1 = a.ymin - (Y[3] - Y[2]) * 0.5;
+            a.ymax1 = a.ymax + (Y[c.ny + 2] - Y[c.ny + 1]) * 0.5;
+        }
         if (p.ndim == 3) {
             a.zmin1 = a.zmin - (Z[3] - Z[2]) * 0.5;
             a.zmax1 = a.zmax + (Z[c.nz + 2] - Z[c.nz + 1]) * 0.5;

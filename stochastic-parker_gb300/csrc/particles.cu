@@ -802,7 +802,9 @@ __global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, i
     if (a.nonuniform) {
         // (binarySearch_R(xpos_local, x) - 1) / rx + 1 (diagnostics.f90:790-792)
         ix = (grid_count(a.xpos, a.nxg, P.x[i]) - 1) / a.rx + 1;
-        iy = (grid_count(a.ypos, a.nyg, P.y[i]) - 1) / a.ry + 1;
+        // 1D runs keep no y positions (ypos_global is never set there)
+        iy = (a.ndim > 1) ? (grid_count(a.ypos, a.nyg, P.y[i]) - 1) / a.ry + 1
+                          : (int)floor((P.y[i] - a.ymin) / a.dyd) + 1;
         iz = (a.ndim == 3) ? (grid_count(a.zpos, a.nzg, P.z[i]) - 1) / a.rz + 1
                            : (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
     } else {

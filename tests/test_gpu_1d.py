@@ -78,6 +78,17 @@ def test_1d_nlgc_dpp_nonuniform_bit_exact():
     eng, gpu, ref, _ = _run(nonuniform=True, mover_kw=dict(nlgc=True, kperp_kpara=0.05),
                             dpp_wave=1)
     _same(gpu, ref, STATE)
+    # local distributions bin x by the node search, y uniformly (1D keeps
+    # no y positions)
+    f, c = eng.local_distribution(pmin=0.05, pmax=10.0, npbins=16, rx=8)
+    oracle.set_grid_positions(_stretched(N, 0.0, 1.0, 7))
+    parts = oracle.Particles(len(gpu) + 8, gpu.arrays)
+    cfg = make_mhd_config(N, 1, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.02, ndim=1)
+    fo, co = oracle.local_distribution(oracle.config_from(cfg), 1, parts, 0.05, 10.0, 16, 1, 8,
+                                       1, 1, nonuniform=True)
+    oracle.set_grid_positions(None)
+    assert np.array_equal(c.ravel(), co) and c.sum() > 0
+    assert np.array_equal(f.ravel(), fo)
     eng.close()
 
 
