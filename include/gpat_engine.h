@@ -341,6 +341,36 @@ int gpat_get_escaped_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t 
 /* reset_escaped_particles: clears the escaped distribution and the escaped
  * particles. */
 int gpat_reset_escaped_particles(gpat_handle_t *h);
+/* Particle tracking (track_particle_flag, GPAT_PREC_FP64 only).
+ * init_particle_tracking (particle_module.f90:5825-5877): tags is
+ * tags_tracking(nrows, nptl_tracking) in Fortran order, column j = tracked
+ * particle j: {origin, tag_injected, tag_splitted after 1 .. nrows - 2
+ * splits}; particles_tracked(nsteps_tracking_max, nptl_tracking) is
+ * allocated and zeroed, nsteps_tracking_max = ceiling((1 / dt_min_rel) /
+ * nsteps_interval) + 1.  From then on, injection selects listed particles
+ * (negated tags, first record; :434-440), gpat_particle_mover records a
+ * tracked particle every nsteps_interval pushes (:1697-1722, :1806-1812) and
+ * gpat_split_particle follows the tracking branch of split_particle
+ * (:5452-5474).  Records past nsteps_tracking_max are dropped and counted.
+ * A second call replaces the table and clears the records. */
+int gpat_init_particle_tracking(gpat_handle_t *h, const int32_t *tags, int32_t nrows,
+                                int32_t nptl_tracking, int32_t nsteps_interval);
+/* The same from a raw file: int32 nrows, int32 nptl_tracking, then the
+ * table in Fortran order (the "tags" dataset of the reference's tags file). */
+int gpat_read_particle_tracking(gpat_handle_t *h, const char *particle_tags_file,
+                                int32_t nsteps_interval);
+/* nsteps_tracking_max, nptl_tracking and the dropped-record count (each
+ * pointer may be NULL). */
+int gpat_tracking_dims(gpat_handle_t *h, int64_t *nsteps_tracking_max, int32_t *nptl_tracking,
+                       int64_t *dropped);
+/* sync_tracked_particles + the data of dump_tracked_particles (:5994-6030,
+ * :6235-6299) on one rank: each column keeps its records with
+ * tag_splitted < 0, in order, the rest zeroed (this persists, as in the
+ * reference); then every field (NULL: skipped) gets nsteps_tracking_max *
+ * nptl_tracking values, particles_tracked(step, particle) in Fortran order. */
+int gpat_get_tracked_particles(gpat_handle_t *h, gpat_particles_t *dst);
+/* free_particle_tracking (:5905-5911). */
+int gpat_free_particle_tracking(gpat_handle_t *h);
 /* pbins_edges_global (diagnostics.f90:194-204): npp_global + 1 values. */
 int gpat_pbins_edges(gpat_handle_t *h, double *edges);
 /* quick_check (diagnostics.f90:116-170) for one rank: out = {nptl_current,

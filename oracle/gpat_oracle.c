@@ -608,10 +608,187 @@ typedef struct mover_ctx {
 typedef struct ptl_state {
     double x, y, z, p, v, mu, t, dt, weight;
     double h1, h2;   /* acceleration-surface heights at the push's start */
-    int flag;
-    int32_t nsteps_pushed, tag_injected, tag_splitted;
+    int flag, split_times;
+    int32_t nsteps_pushed, tag_injected, tag_splitted, origin, nsteps_tracked;
     uint32_t rng_ctr;
 } ptl_state;
+
+/* ------------------------------------------------------------------------ */
+/* Particle tracking (particle_module.f90:144-150, 5825-6030): the table    */
+/* tags_tracking(nrows, n) and the records particles_tracked(nsteps_max, n), */
+/* both Fortran order, owned by the caller.                                 */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    const int32_t *tags;
+    int nrows, n;
+    int64_t nsteps_max;
+    orc_particles rec;
+    int64_t dropped;
+} orc_tracking;
+static orc_tracking g_trk;
+
+void orc_set_tracking(const int32_t *tags, int nrows, int n, int64_t nsteps_max,
+                      const orc_particles *rec)
+{
+    memset(&g_trk, 0, sizeof g_trk);
+    if (!tags) return;
+    g_trk.tags = tags; g_trk.nrows = nrows; g_trk.n = n; g_trk.nsteps_max = nsteps_max;
+    g_trk.rec = *rec;
+}
+
+int64_t orc_tracking_dropped(void) { return g_trk.dropped; }
+
+/* nsteps_tracking_max = ceiling((1.0 / dt_min_rel) / nsteps_interval) + 1
+ * (:5874). */
+int64_t orc_nsteps_tracking_max(double dt_min_rel, int nsteps_interval)
+{
+    return (int64_t)ceil((1.0 / dt_min_rel) / (double)nsteps_interval) + 1;
+}
+
+/* findloc(tags_tracking(row, from:to), v [, back]) as a 1-based column
+ * (0: none); row and columns 1-based. */
+static int trk_findloc(int row, int32_t v, int from, int to, int back)
+{
+    const int32_t *T = g_trk.tags;
+    if (!back) {
+        for (int j = from; j <= to; ++j)
+            if (T[(size_t)(j - 1) * g_trk.nrows + (row - 1)] == v) return j;
+    } else {
+        for (int j = to; j >= from; --j)
+            if (T[(size_t)(j - 1) * g_trk.nrows + (row - 1)] == v) return j;
+    }
+    return 0;
+}
+
+/* is_particle_selected (:5923-5963) with 1-based iptl_lo / iptl_hi.
+ * locate_particle (:5971-5994) is the same search for a tracked particle,
+ * whose split count never exceeds the table's; one that is not listed
+ * (out-of-range indexing in the reference) records nothing here. */
+static int trk_selected(int32_t origin, int32_t tag_inj, int nsplit, int32_t tag_spl,
+                        int *lo, int *hi)
+{
+    const int split_times_max = g_trk.nrows - 2;
+    *lo = -1; *hi = -1;
+    if (nsplit > split_times_max || nsplit < 0) return 0;
+    const int i1 = trk_findloc(1, origin, 1, g_trk.n, 0);
+    if (i1 == 0) return 0;
+    const int i2 = trk_findloc(1, origin, 1, g_trk.n, 1);
+    const int32_t ai = tag_inj < 0 ? -tag_inj : tag_inj;
+    const int i3 = trk_findloc(2, ai, i1, i2, 0);
+    if (i3 == 0) return 0;
+    const int i4 = trk_findloc(2, ai, i1, i2, 1);
+    if (nsplit > 0) {
+        const int32_t as = tag_spl < 0 ? -tag_spl : tag_spl;
+        const int i5 = trk_findloc(nsplit + 2, as, i3, i4, 0);
+        if (i5 == 0) return 0;
+        *lo = i5;
+        *hi = trk_findloc(nsplit + 2, as, i3, i4, 1);
+    } else {
+        *lo = i3;
+        *hi = i4;
+    }
+    return 1;
+}
+
+/* particles_tracked(row, lo:hi) = ptl (1-based); a row past nsteps_max is
+ * counted instead of written. */
+static void trk_write(int64_t row, int lo, int hi, const orc_particles *S, int64_t i,
+                      const ptl_state *s)
+{
+    if (row < 1 || row > g_trk.nsteps_max) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+        g_trk.dropped += 1;
+        return;
+    }
+    const orc_particles *D = &g_trk.rec;
+    for (int j = lo; j <= hi; ++j) {
+        const size_t e = (size_t)(row - 1) + (size_t)g_trk.nsteps_max * (size_t)(j - 1);
+        if (s) {
+            D->x[e] = s->x; D->y[e] = s->y; D->z[e] = s->z; D->p[e] = s->p;
+            D->v[e] = s->v; D->mu[e] = s->mu; D->weight[e] = s->weight;
+            D->t[e] = s->t; D->dt[e] = s->dt;
+            D->split_times[e] = (int8_t)s->split_times; D->count_flag[e] = (int8_t)s->flag;
+            D->origin[e] = s->origin; D->nsteps_tracked[e] = s->nsteps_tracked;
+            D->nsteps_pushed[e] = s->nsteps_pushed;
+            D->tag_injected[e] = s->tag_injected; D->tag_splitted[e] = s->tag_splitted;
+            D->rng_ctr[e] = s->rng_ctr;
+        } else {
+            D->x[e] = S->x[i]; D->y[e] = S->y[i]; D->z[e] = S->z[i]; D->p[e] = S->p[i];
+            D->v[e] = S->v[i]; D->mu[e] = S->mu[i]; D->weight[e] = S->weight[i];
+            D->t[e] = S->t[i]; D->dt[e] = S->dt[i];
+            D->split_times[e] = S->split_times[i]; D->count_flag[e] = S->count_flag[i];
+            D->origin[e] = S->origin[i]; D->nsteps_tracked[e] = S->nsteps_tracked[i];
+            D->nsteps_pushed[e] = S->nsteps_pushed[i];
+            D->tag_injected[e] = S->tag_injected[i]; D->tag_splitted[e] = S->tag_splitted[i];
+            D->rng_ctr[e] = S->rng_ctr[i];
+        }
+    }
+}
+
+/* The mover's record after a push (:1697-1703, :1806-1812). */
+static void trk_after_push(ptl_state *s)
+{
+    if (!g_trk.tags) return;
+    if (s->tag_splitted < 0 && s->nsteps_pushed == 0) {
+        int lo, hi;
+        const int found = trk_selected(s->origin, s->tag_injected, s->split_times,
+                                       s->tag_splitted, &lo, &hi);
+        s->nsteps_tracked = s->nsteps_tracked + 1;
+        if (found) trk_write(s->nsteps_tracked, lo, hi, NULL, 0, s);
+    }
+}
+
+/* inject_one_particle's tracking block (:434-440, :622-628) for the new
+ * particle c. */
+static void trk_injected(orc_particles *P, int64_t c)
+{
+    int lo, hi;
+    if (!g_trk.tags) return;
+    if (!trk_selected(P->origin[c], P->tag_injected[c], P->split_times[c], P->tag_splitted[c],
+                      &lo, &hi))
+        return;
+    P->nsteps_tracked[c] = 1;
+    P->tag_injected[c] = -P->tag_injected[c];
+    P->tag_splitted[c] = -1;
+    trk_write(1, lo, hi, P, c, NULL);
+}
+
+/* sync_tracked_particles on one rank (:5994-6030): per column, the records
+ * with tag_splitted < 0 shifted to the front in order, the rest zeroed
+ * (the MPI_SCAN offset is 0 and the reductions are copies). */
+void orc_sync_tracked(void)
+{
+    const orc_particles *D = &g_trk.rec;
+    for (int c = 0; c < g_trk.n; ++c) {
+        const size_t base = (size_t)g_trk.nsteps_max * (size_t)c;
+        int64_t j = 0;
+        for (int64_t i = 0; i < g_trk.nsteps_max; ++i) {
+            const size_t a = base + (size_t)i, b = base + (size_t)j;
+            if (D->tag_splitted[a] < 0) {
+                D->x[b] = D->x[a]; D->y[b] = D->y[a]; D->z[b] = D->z[a]; D->p[b] = D->p[a];
+                D->v[b] = D->v[a]; D->mu[b] = D->mu[a]; D->weight[b] = D->weight[a];
+                D->t[b] = D->t[a]; D->dt[b] = D->dt[a];
+                D->split_times[b] = D->split_times[a]; D->count_flag[b] = D->count_flag[a];
+                D->origin[b] = D->origin[a]; D->nsteps_tracked[b] = D->nsteps_tracked[a];
+                D->nsteps_pushed[b] = D->nsteps_pushed[a];
+                D->tag_injected[b] = D->tag_injected[a];
+                D->tag_splitted[b] = D->tag_splitted[a];
+                D->rng_ctr[b] = D->rng_ctr[a];
+                j += 1;
+            }
+        }
+        for (int64_t i = j; i < g_trk.nsteps_max; ++i) {
+            const size_t b = base + (size_t)i;
+            D->x[b] = 0.0; D->y[b] = 0.0; D->z[b] = 0.0; D->p[b] = 0.0; D->v[b] = 0.0;
+            D->mu[b] = 0.0; D->weight[b] = 0.0; D->t[b] = 0.0; D->dt[b] = 0.0;
+            D->split_times[b] = 0; D->count_flag[b] = 0; D->origin[b] = 0;
+            D->nsteps_tracked[b] = 0; D->nsteps_pushed[b] = 0;
+            D->tag_injected[b] = 0; D->tag_splitted[b] = 0; D->rng_ctr[b] = 0;
+        }
+    }
+}
 
 typedef struct thread_acc {
     uint64_t leak_hi, leak_lo, negp_hi, negp_lo, steps;
@@ -1739,6 +1916,7 @@ static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
             do_push(c, s, 0, dl);
             acc->steps += 1;
             s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
+            trk_after_push(s);
         }
         if ((s->t - t0) > dt_target && s->flag == 1) {
             s->x = s->x - dl[0];
@@ -1751,10 +1929,17 @@ static void move_one(const mover_ctx *c, ptl_state *s, int nsteps_interval,
             const double dt_old = s->dt;
             s->dt = t0 + dt_target - s->t;
             if (s->dt > 0.0) {
-                s->nsteps_pushed = s->nsteps_pushed - 1;
+                if (s->tag_splitted < 0 && s->nsteps_pushed == 0) {
+                    /* back one step if necessary (:1716-1722) */
+                    s->nsteps_tracked = s->nsteps_tracked - 1;
+                    s->nsteps_pushed = nsteps_interval - 2;
+                } else {
+                    s->nsteps_pushed = s->nsteps_pushed - 1;
+                }
                 do_push(c, s, 1, dl);
                 acc->steps += 1;
                 s->nsteps_pushed = (s->nsteps_pushed + 1) % nsteps_interval;
+                trk_after_push(s);
             }
             s->dt = dt_old;
             check_negp_or_boundary(c, s, acc);
@@ -1770,6 +1955,9 @@ static void load_state(const orc_particles *P, int64_t i, ptl_state *s)
     s->t = P->t[i]; s->dt = P->dt[i]; s->weight = P->weight[i];
     s->flag = P->count_flag[i];
     s->nsteps_pushed = P->nsteps_pushed[i];
+    s->split_times = P->split_times[i];
+    s->origin = P->origin[i];
+    s->nsteps_tracked = P->nsteps_tracked[i];
     s->tag_injected = P->tag_injected[i];
     s->tag_splitted = P->tag_splitted[i];
     s->rng_ctr = P->rng_ctr[i];
@@ -1782,6 +1970,7 @@ static void store_state(orc_particles *P, int64_t i, const ptl_state *s)
     P->t[i] = s->t; P->dt[i] = s->dt;
     P->count_flag[i] = (int8_t)s->flag;
     P->nsteps_pushed[i] = s->nsteps_pushed;
+    P->nsteps_tracked[i] = s->nsteps_tracked;
     P->rng_ctr[i] = s->rng_ctr;
 }
 
@@ -2004,7 +2193,7 @@ int64_t orc_particle_mover(const orc_params *pr, const orc_mhd_config *cfg,
     return orc_remove_particles(P, n, cnt);
 }
 
-/* split_particle: particle_module.f90:5430-5480 (no tracking).  The
+/* split_particle: particle_module.f90:5430-5480.  The
  * threshold uses split_ratio**split_times by repeated multiplication, the
  * new weight is 0.5**(1+split_times) (exact in single precision). */
 int64_t orc_split_particle(const orc_params *pr, orc_particles *P, int64_t n,
@@ -2031,8 +2220,32 @@ int64_t orc_split_particle(const orc_params *pr, orc_particles *P, int64_t n,
             P->origin[c] = P->origin[i]; P->nsteps_tracked[c] = P->nsteps_tracked[i];
             P->nsteps_pushed[c] = P->nsteps_pushed[i];
             P->tag_injected[c] = P->tag_injected[i];
-            P->tag_splitted[c] = (int32_t)((uint32_t)P->tag_splitted[i] + (1u << k));
             P->rng_ctr[c] = P->rng_ctr[i];
+            if (g_trk.tags && P->tag_splitted[i] < 0) {
+                /* tracked parent (:5452-5474) */
+                const int32_t tg = P->tag_splitted[i];
+                int lo, hi;
+                P->tag_splitted[c] = (int32_t)((uint32_t)tg - (1u << k));
+                if (trk_selected(P->origin[c], P->tag_injected[c], k + 1, P->tag_splitted[c],
+                                 &lo, &hi)) {
+                    if (P->nsteps_pushed[i] == 0) {
+                        P->nsteps_tracked[c] += 1;
+                        trk_write(P->nsteps_tracked[c], lo, hi, P, c, NULL);
+                    }
+                } else {
+                    P->tag_splitted[c] = -P->tag_splitted[c];
+                }
+                if (trk_selected(P->origin[i], P->tag_injected[i], k + 1, tg, &lo, &hi)) {
+                    if (P->nsteps_pushed[i] == 0) {
+                        P->nsteps_tracked[i] += 1;
+                        trk_write(P->nsteps_tracked[i], lo, hi, P, i, NULL);
+                    }
+                } else {
+                    P->tag_splitted[i] = -tg;   /* stop tracking */
+                }
+            } else {
+                P->tag_splitted[c] = (int32_t)((uint32_t)P->tag_splitted[i] + (1u << k));
+            }
         }
     }
     return n;
@@ -2153,6 +2366,7 @@ int64_t orc_inject_spatial_uniform(const orc_params *pr, orc_particles *P, int64
         const double v = particle_v0 * p / pr->p0;
         const double t = t_frame + inj_u01(&s) * dt_mhd;
         set_new_particle(P, n, x, y, z, p, v, mu, t, dt, tag);
+        trk_injected(P, n);
         n += 1;
     }
     return n;
@@ -2335,6 +2549,7 @@ int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, con
         const double v = particle_v0 * p / pr->p0;
         const double t = t_frame + inj_u01(&s) * dt_mhd;
         set_new_particle(P, n, x, y, z, p, v, mu, t, dt, tag);
+        trk_injected(P, n);
         n += 1;
     }
     return n;
@@ -2374,6 +2589,7 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
         const double v = particle_v0 * p / pr->p0;
         const double mu = (double)0.99f * (2.0 * inj_u01(&s) - 1.0);
         set_new_particle(P, n, xpos, y, z, p, v, mu, t_frame, dt, tag);
+        trk_injected(P, n);
         n += 1;
     }
     return n;

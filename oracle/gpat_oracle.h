@@ -188,6 +188,16 @@ void orc_set_escaped_histogram(int npp, double pmin, double pmax, uint64_t *coun
 void orc_set_acc_surface(int axis1, int sign1, int axis2, int sign2, int has2, int intersection,
                          const double *s11, const double *s12, const double *s21,
                          const double *s22, int nxg, int nyg, int nzg);
+/* Particle tracking (init_particle_tracking): tags_tracking(nrows, n) and
+ * the records particles_tracked(nsteps_max, n), Fortran order, owned by the
+ * caller; tags NULL turns tracking off.  With tracking on, injection, the
+ * mover and split_particle select and record as the reference does. */
+void orc_set_tracking(const int32_t *tags, int nrows, int n, int64_t nsteps_max,
+                      const orc_particles *rec);
+int64_t orc_tracking_dropped(void);
+int64_t orc_nsteps_tracking_max(double dt_min_rel, int nsteps_interval);
+/* sync_tracked_particles on one rank. */
+void orc_sync_tracked(void);
 void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
                                  int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,

@@ -143,6 +143,10 @@ def load() -> C.CDLL:
                                                     P(d)]
         lib.orc_set_grid_positions.argtypes = [P(d), P(d), P(d), C.c_int, C.c_int, C.c_int]
         lib.orc_set_acc_surface.argtypes = [C.c_int] * 6 + [P(d)] * 4 + [C.c_int] * 3
+        lib.orc_set_tracking.argtypes = [P(i32), C.c_int, C.c_int, i64, P(OrcParticles)]
+        lib.orc_tracking_dropped.restype = i64
+        lib.orc_nsteps_tracking_max.restype = i64
+        lib.orc_nsteps_tracking_max.argtypes = [d, C.c_int]
         lib.orc_uniform_grid_positions.argtypes = [C.c_int, d, d, P(d)]
         lib.orc_binary_search.restype = C.c_int
         lib.orc_binary_search.argtypes = [P(d), C.c_int, d]
@@ -403,6 +407,34 @@ class EscapedHistogram:
 
     def weights(self) -> np.ndarray:
         return np.array([fixed_to_double(int(h), int(l)) for h, l in zip(self.whi, self.wlo)])
+
+
+class Tracking:
+    """init_particle_tracking for the oracle: tags is tags_tracking as
+    (nptl_tracking, nrows), one row per tracked particle.  While attached,
+    injection, the mover and split_particle record into particles_tracked;
+    detach() turns tracking off."""
+
+    def __init__(self, tags, dt_min_rel: float, nsteps_interval: int):
+        lib = load()
+        self.tags = np.ascontiguousarray(tags, dtype=np.int32)
+        self.ntrk, self.nrows = self.tags.shape
+        self.nsteps_max = lib.orc_nsteps_tracking_max(dt_min_rel, nsteps_interval)
+        self.rec = Particles(self.nsteps_max * self.ntrk)
+        lib.orc_set_tracking(self.tags.ctypes.data_as(P(i32)), self.nrows, self.ntrk,
+                             self.nsteps_max, C.byref(self.rec.c))
+
+    def dropped(self) -> int:
+        return load().orc_tracking_dropped()
+
+    def sync(self) -> dict:
+        """sync_tracked_particles, then every field shaped (nptl_tracking,
+        nsteps_tracking_max)."""
+        load().orc_sync_tracked()
+        return {k: v.reshape(self.ntrk, self.nsteps_max).copy() for k, v in self.rec.a.items()}
+
+    def detach(self):
+        load().orc_set_tracking(None, 0, 0, 0, None)
 
 
 class EscapedStore:

@@ -62,6 +62,13 @@ struct gpat_handle {
     void *emem = nullptr;
     DevParticles E{};
     int64_t ecap = 0, ne = 0;
+    // particle tracking (init_particle_tracking, particle_module.f90:5825-5877):
+    // tags_tracking(trk_rows, trk_n) and particles_tracked(trk_steps, trk_n)
+    int32_t *dtags = nullptr;
+    void *tmem = nullptr;
+    DevParticles T{};
+    int trk_rows = 0, trk_n = 0;
+    int64_t trk_steps = 0;
     // module state kept on the host
     std::vector<double> tstamps;
     int64_t tag_max = 0;
@@ -110,6 +117,17 @@ DevParticles carve(void *base, int64_t cap) {
     for (auto *pp : i4) { *pp = reinterpret_cast<int32_t *>(q); q += al(4 * c); }
     P.rng_ctr = reinterpret_cast<uint32_t *>(q);
     return P;
+}
+
+TrackArgs track_args(const gpat_handle_t *h) {
+    TrackArgs t{};
+    if (!h->dtags) return t;
+    t.tags = h->dtags;
+    t.nrows = h->trk_rows;
+    t.n = h->trk_n;
+    t.nsteps_max = h->trk_steps;
+    t.rec = h->T;
+    return t;
 }
 
 int check_status(gpat_handle_t *h) {
@@ -280,6 +298,7 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.noise = p.noise;
     a.key0 = (uint32_t)p.seed;
     a.key1 = (uint32_t)(p.seed >> 32);
+    a.trk = track_args(h);
     a.cnt = h->dcnt;
     return GPAT_OK;
 }
@@ -589,6 +608,8 @@ int gpat_destroy(gpat_handle_t *h) {
     }
     if (h->staging) cudaFree(h->staging);
     if (h->emem) cudaFree(h->emem);
+    if (h->tmem) cudaFree(h->tmem);
+    if (h->dtags) cudaFree(h->dtags);
     if (h->scratch) cudaFree(h->scratch);
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->dcnt) cudaFree(h->dcnt);
@@ -950,6 +971,7 @@ static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, 
     a.key0 = (uint32_t)h->prm.seed;
     a.key1 = (uint32_t)(h->prm.seed >> 32);
     CK(launch_inject(a, &h->dcnt->status, h->stream));
+    CK(launch_track_injected(a.P, h->n, h->n + count, track_args(h), h->dcnt, h->stream));
     int rc = pull_counters(h);
     if (rc) return rc;
     h->n += count;
@@ -1187,8 +1209,9 @@ int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
     int rc = ensure_scratch(h, h->n);
     if (rc) return rc;
     const unsigned long long before = h->hcnt.nsplit;
+    const TrackArgs trk = track_args(h);
     CK(launch_split_particles(h->P[h->cur], h->n, h->cap, split_ratio, pmin_split, h->prm.p0,
-                              h->prm.pmax, h->scratch, h->dcnt, h->stream));
+                              h->prm.pmax, h->scratch, h->dcnt, h->stream, &trk));
     rc = pull_counters(h);
     if (rc) return rc;
     const int64_t created = (int64_t)(h->hcnt.nsplit - before);
@@ -1294,6 +1317,117 @@ int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t
             if (counts) counts[k] = b[3 * k];
             if (fescaped) fescaped[k] = fixed_to_double(b[3 * k + 1], b[3 * k + 2]);
         }
+    return GPAT_OK;
+}
+
+int gpat_free_particle_tracking(gpat_handle_t *h) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->tmem) cudaFree(h->tmem);
+    if (h->dtags) cudaFree(h->dtags);
+    h->tmem = nullptr;
+    h->dtags = nullptr;
+    h->T = DevParticles{};
+    h->trk_rows = h->trk_n = 0;
+    h->trk_steps = 0;
+    return GPAT_OK;
+}
+
+int gpat_init_particle_tracking(gpat_handle_t *h, const int32_t *tags, int32_t nrows,
+                                int32_t nptl_tracking, int32_t nsteps_interval) {
+    if (!h || !tags) return GPAT_ERR_ARG;
+    if (nrows < 2 || nptl_tracking < 1 || nsteps_interval < 1)
+        return fail(h, GPAT_ERR_ARG, "tags_tracking needs >= 2 rows, >= 1 column, nsteps_interval >= 1");
+    if (h->prm.precision != GPAT_PREC_FP64)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "particle tracking runs in FP64 precision");
+    // nsteps_tracking_max = ceiling((1.0 / dt_min_rel) / nsteps_interval) + 1
+    const double steps = std::ceil((1.0 / h->prm.dt_min_rel) / (double)nsteps_interval);
+    if (!(steps >= 0.0) || steps > 2.0e9)
+        return fail(h, GPAT_ERR_ARG, "dt_min_rel gives no usable nsteps_tracking_max");
+    int rc = gpat_free_particle_tracking(h);
+    if (rc) return rc;
+    const int64_t nsteps_max = (int64_t)steps + 1;
+    const int64_t nrec = nsteps_max * (int64_t)nptl_tracking;
+    if (cudaMalloc(&h->tmem, particle_bytes(nrec)) != cudaSuccess) {
+        cudaGetLastError();
+        h->tmem = nullptr;
+        return fail(h, GPAT_ERR_OOM, "particles_tracked does not fit on the device");
+    }
+    const size_t tbytes = sizeof(int32_t) * (size_t)nrows * (size_t)nptl_tracking;
+    if (cudaMalloc(&h->dtags, tbytes) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(h->tmem);
+        h->tmem = nullptr;
+        h->dtags = nullptr;
+        return fail(h, GPAT_ERR_OOM, "tags_tracking does not fit on the device");
+    }
+    // reset_tracked_particles (:5880-5898): every record zero
+    CK(cudaMemsetAsync(h->tmem, 0, particle_bytes(nrec), h->stream));
+    CK(cudaMemcpyAsync(h->dtags, tags, tbytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(&h->dcnt->trk_dropped, 0, sizeof(unsigned long long), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->T = carve(h->tmem, nrec);
+    h->trk_rows = nrows;
+    h->trk_n = nptl_tracking;
+    h->trk_steps = nsteps_max;
+    return GPAT_OK;
+}
+
+int gpat_read_particle_tracking(gpat_handle_t *h, const char *particle_tags_file,
+                                int32_t nsteps_interval) {
+    if (!h || !particle_tags_file) return GPAT_ERR_ARG;
+    FILE *f = std::fopen(particle_tags_file, "rb");
+    if (!f) return fail(h, GPAT_ERR_IO, std::string("cannot open ") + particle_tags_file);
+    int32_t dims[2] = {0, 0};
+    if (std::fread(dims, sizeof(int32_t), 2, f) != 2 || dims[0] < 2 || dims[1] < 1) {
+        std::fclose(f);
+        return fail(h, GPAT_ERR_IO, "tags file: bad dimensions");
+    }
+    std::vector<int32_t> tags((size_t)dims[0] * (size_t)dims[1]);
+    const size_t got = std::fread(tags.data(), sizeof(int32_t), tags.size(), f);
+    std::fclose(f);
+    if (got != tags.size()) return fail(h, GPAT_ERR_IO, "tags file: short read");
+    return gpat_init_particle_tracking(h, tags.data(), dims[0], dims[1], nsteps_interval);
+}
+
+int gpat_tracking_dims(gpat_handle_t *h, int64_t *nsteps_tracking_max, int32_t *nptl_tracking,
+                       int64_t *dropped) {
+    if (!h) return GPAT_ERR_ARG;
+    if (!h->dtags) return fail(h, GPAT_ERR_STATE, "particle tracking is not initialised");
+    if (nsteps_tracking_max) *nsteps_tracking_max = h->trk_steps;
+    if (nptl_tracking) *nptl_tracking = h->trk_n;
+    if (dropped) {
+        CK(cudaSetDevice(h->device));
+        int rc = pull_counters(h);
+        if (rc) return rc;
+        *dropped = (int64_t)h->hcnt.trk_dropped;
+    }
+    return GPAT_OK;
+}
+
+int gpat_get_tracked_particles(gpat_handle_t *h, gpat_particles_t *dst) {
+    if (!h || !dst) return GPAT_ERR_ARG;
+    if (!h->dtags) return fail(h, GPAT_ERR_STATE, "particle tracking is not initialised");
+    CK(cudaSetDevice(h->device));
+    // sync_tracked_particles (:5994-6030) compacts the records in place
+    CK(launch_sync_tracked(track_args(h), h->stream));
+    const DevParticles &S = h->T;
+    const size_t c = (size_t)(h->trk_steps * (int64_t)h->trk_n);
+    auto cp = [&](void *d, const void *s, size_t bytes) -> cudaError_t {
+        if (!bytes || !d) return cudaSuccess;   // NULL destination: field skipped
+        return cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToHost, h->stream);
+    };
+    CK(cp(dst->x, S.x, 8 * c)); CK(cp(dst->y, S.y, 8 * c)); CK(cp(dst->z, S.z, 8 * c));
+    CK(cp(dst->p, S.p, 8 * c)); CK(cp(dst->v, S.v, 8 * c)); CK(cp(dst->mu, S.mu, 8 * c));
+    CK(cp(dst->weight, S.weight, 8 * c)); CK(cp(dst->t, S.t, 8 * c)); CK(cp(dst->dt, S.dt, 8 * c));
+    CK(cp(dst->split_times, S.split_times, c)); CK(cp(dst->count_flag, S.count_flag, c));
+    CK(cp(dst->origin, S.origin, 4 * c)); CK(cp(dst->nsteps_tracked, S.nsteps_tracked, 4 * c));
+    CK(cp(dst->nsteps_pushed, S.nsteps_pushed, 4 * c));
+    CK(cp(dst->tag_injected, S.tag_injected, 4 * c));
+    CK(cp(dst->tag_splitted, S.tag_splitted, 4 * c));
+    CK(cp(dst->rng_ctr, S.rng_ctr, 4 * c));
+    CK(cudaStreamSynchronize(h->stream));
     return GPAT_OK;
 }
 
@@ -2148,6 +2282,8 @@ int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w
                         double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled) {
     if (!h || !m || !(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8)
         return GPAT_ERR_ARG;
+    if (h->dtags)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "weighted splitting keeps no particle tracks");
     CK(cudaSetDevice(h->device));
     if (cudaStreamSynchronize(m->stream) != cudaSuccess)
         return fail(h, GPAT_ERR_CUDA, "network stream");

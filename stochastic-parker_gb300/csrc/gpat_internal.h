@@ -45,12 +45,24 @@ struct DevCounters {
     unsigned int status;
     unsigned int pad;
     unsigned long long bad_value;
+    unsigned long long trk_dropped;  // tracked records past nsteps_tracking_max
 };
 
 // Packed per-cell field records read by the movers.  2D: 16 floats,
 // 3D: 24 floats (see fields.cu for the slot order).
 constexpr int kRec2D = 16;
 constexpr int kRec3D = 24;
+
+// Particle tracking (track_particle_flag, particle_module.f90:144-150):
+// tags_tracking(nrows, n) and particles_tracked(nsteps_max, n), both in
+// Fortran order (column j of the table is tracked particle j).  tags ==
+// nullptr: tracking off.
+struct TrackArgs {
+    const int32_t *tags;
+    int nrows, n;            // split_times_max + 2, nptl_tracking
+    int64_t nsteps_max;      // nsteps_tracking_max
+    DevParticles rec;
+};
 
 // Everything the mover kernels need, passed by value.
 struct MoverArgs {
@@ -99,6 +111,7 @@ struct MoverArgs {
     int surf_on, surf_has2, surf_inter;
     int surf_axis[2], surf_sign[2], surf_ld[2];
     const double *surf[2][2];   // [surface][frame]
+    TrackArgs trk;              // FP64 mover only
     DevCounters *cnt;
 };
 
@@ -274,10 +287,18 @@ struct LocalDistArgs {
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
                               unsigned long long *bins, size_t nbins, cudaStream_t s);
 // Splitting: children appended after n in parent order, at most cap - n.
+// With tracking on, tracked parents follow split_particle's tracking branch.
 cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,
                                    double split_ratio, double pmin_split, double p0,
                                    double pmax, void *scratch, DevCounters *cnt,
-                                   cudaStream_t s);
+                                   cudaStream_t s, const TrackArgs *trk = nullptr);
+// Tracking of particles injected in [first, n): inject_one_particle's
+// selection (particle_module.f90:434-440).
+cudaError_t launch_track_injected(const DevParticles &P, int64_t first, int64_t n,
+                                  const TrackArgs &trk, DevCounters *cnt, cudaStream_t s);
+// sync_tracked_particles on one rank (particle_module.f90:5994-6030): each
+// column keeps its records with tag_splitted < 0 in order, the rest zeroed.
+cudaError_t launch_sync_tracked(const TrackArgs &trk, cudaStream_t s);
 // Grid geometry for spatial binning of particles (one bin per field cell).
 struct CellGrid {
     double xmin, ymin, zmin, idx, idy, idz;

@@ -11,7 +11,11 @@
 // particle counts (the fglobal / pbins_edges_global datasets of
 // fdists_XXXX.h5, without HDF5).  With -pd 1, particles_XXXX.dat per frame,
 // and restart/particles_XXXX.dat at t_end always (dump_particles, see
-// write_particles below).
+// write_particles below).  With -tf .true. (particle tracking) the tags
+// table is read from particle_tracking/<-ptf> under the diagnostics
+// directory (int32 nrows, int32 nptl_tracking, the table in Fortran order)
+// and particle_tracking/particles_tracked_XXXX.dat is written per frame
+// (write_tracked below) instead of the distributions.
 #include <sys/stat.h>
 
 #include <cmath>
@@ -36,6 +40,9 @@ struct Options {
     int inject_at_shock = 0, inject_part_box = 0, tmax_to_inject = 100000, check_drift_2d = 0;
     int particle_data_dump = 0;
     bool dump_escaped_dist = false, dump_escaped = false;   // -ded, -de (:939-946)
+    // -tf, -ptf (stochastic-mhd.f90:711-722)
+    bool track_particle_flag = false;
+    std::string particle_tags_file = "tags_selected_01.dat";
     // inject_particles_at_large_* switches (stochastic-mhd.f90:735-806)
     bool inject_large_jz = false, inject_large_absj = false, inject_large_db2 = false;
     bool inject_large_divv = false, inject_large_rho = false, inject_same_nptl = false;
@@ -106,7 +113,8 @@ int parse(int argc, char **argv, Options &o) {
         {"-nn", "--ncells_large_jz_norm"}, {"-naj", "--ncells_large_absj_norm"},
         {"-nv", "--ncells_large_divv_norm"}, {"-nr", "--ncells_large_rho_norm"},
         {"-db2", "--db2_min"}, {"-nb", "--ncells_large_db2_norm"}, {"-db", "--deltab_flag"},
-        {"-co", "--correlation"}};
+        {"-co", "--correlation"}, {"-tf", "--track_particle_flag"},
+        {"-ptf", "--particle_tags_file"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -188,6 +196,8 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--ncells_large_db2_norm") o.ncells_large_db2_norm = (long long)d;
         else if (k == "--deltab_flag") o.deltab_flag = (int)d;
         else if (k == "--correlation") o.correlation_flag = (int)d;
+        else if (k == "--track_particle_flag") o.track_particle_flag = truthy(v);
+        else if (k == "--particle_tags_file") o.particle_tags_file = v;
         else if (k == "--precision") {
             o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
             o.precision_set = true;
@@ -267,6 +277,50 @@ int write_particles(gpat_handle_t *h, const std::string &dir, int frame, bool es
     return ok ? GPAT_OK : GPAT_ERR_IO;
 }
 
+// dump_tracked_particles (particle_module.f90:6235-6299) without HDF5:
+// int64 nsteps_tracking_max, int64 nptl_tracking, then the datasets of
+// particles_tracked_XXXX.h5 in the reference's order, each
+// particles_tracked(nsteps_tracking_max, nptl_tracking) in Fortran order:
+// x y z p v mu weight t dt (float64), split_times count_flag (int8), origin
+// nsteps_tracked nsteps_pushed tag_injected tag_splitted (int32).
+int write_tracked(gpat_handle_t *h, const std::string &dir, int frame) {
+    int64_t nsteps = 0, dropped = 0;
+    int32_t ntrk = 0;
+    int rc = gpat_tracking_dims(h, &nsteps, &ntrk, &dropped);
+    if (rc) return rc;
+    const size_t m = (size_t)nsteps * (size_t)ntrk;
+    std::vector<double> f64[9];
+    std::vector<int8_t> i8[2];
+    std::vector<int32_t> i32[5];
+    for (auto &v : f64) v.resize(m);
+    for (auto &v : i8) v.resize(m);
+    for (auto &v : i32) v.resize(m);
+    gpat_particles_t P;
+    P.x = f64[0].data(); P.y = f64[1].data(); P.z = f64[2].data(); P.p = f64[3].data();
+    P.v = f64[4].data(); P.mu = f64[5].data(); P.weight = f64[6].data(); P.t = f64[7].data();
+    P.dt = f64[8].data();
+    P.split_times = i8[0].data(); P.count_flag = i8[1].data();
+    P.origin = i32[0].data(); P.nsteps_tracked = i32[1].data(); P.nsteps_pushed = i32[2].data();
+    P.tag_injected = i32[3].data(); P.tag_splitted = i32[4].data();
+    P.rng_ctr = nullptr;
+    rc = gpat_get_tracked_particles(h, &P);
+    if (rc) return rc;
+    char name[64];
+    std::snprintf(name, sizeof name, "particles_tracked_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return GPAT_ERR_IO;
+    const int64_t dims[2] = {nsteps, (int64_t)ntrk};
+    bool ok = std::fwrite(dims, 8, 2, f) == 2;
+    for (auto &v : f64) ok = ok && std::fwrite(v.data(), 8, m, f) == m;
+    for (auto &v : i8) ok = ok && std::fwrite(v.data(), 1, m, f) == m;
+    for (auto &v : i32) ok = ok && std::fwrite(v.data(), 4, m, f) == m;
+    ok = (std::fclose(f) == 0) && ok;
+    if (dropped)
+        std::fprintf(stderr, "gpat_run: %lld tracked records past nsteps_tracking_max dropped\n",
+                     (long long)dropped);
+    return ok ? GPAT_OK : GPAT_ERR_IO;
+}
+
 std::string frame_name(const std::string &dir, int tf) {
     char buf[32];
     std::snprintf(buf, sizeof buf, "mhd_data_%04d", tf);
@@ -291,7 +345,8 @@ int main(int argc, char **argv) {
     // asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
          o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1 ||
-         o.include_3rd_dim == 1 || o.acc_by_surface == 1) && !o.precision_set)
+         o.include_3rd_dim == 1 || o.acc_by_surface == 1 || o.track_particle_flag) &&
+        !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;
 
@@ -335,6 +390,11 @@ int main(int argc, char **argv) {
                                     o.surface2_existed ? o.surface_norm2.c_str() : nullptr,
                                     o.is_intersection ? 1 : 0));
     CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
+    // init_particle_tracking (stochastic-mhd.f90:241-244)
+    const std::string track_dir = o.diagnostics_directory + "particle_tracking/";
+    if (o.track_particle_flag)
+        CHECK(gpat_read_particle_tracking(h, (track_dir + o.particle_tags_file).c_str(),
+                                          o.nsteps_interval));
 
     // Frame tmin into farray1, gradients (:321, :350).
     const int tmin = o.t_start;
@@ -458,21 +518,27 @@ int main(int argc, char **argv) {
                                                             o.power_index));
             }
         }
-        if (tf == o.t_start + 1) {
+        // initial diagnostics unless tracking (:486-495)
+        if (tf == o.t_start + 1 && !o.track_particle_flag) {
             CHECK(diagnostics(o.t_start));
             if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, o.t_start));
         }
+        // a tracked run moves with one fine step (:498-504)
         CHECK(gpat_particle_mover(h, o.focused_transport, o.nlgc, o.kperp_kpara, o.nsteps_interval,
-                                  ct, o.num_fine_steps, o.dump_escaped_dist ? 1 : 0));
+                                  ct, o.track_particle_flag ? 1 : o.num_fine_steps,
+                                  o.dump_escaped_dist ? 1 : 0));
+        if (o.track_particle_flag) CHECK(write_tracked(h, track_dir, tf));
         if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
-        CHECK(diagnostics(tf));
-        if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, tf));
-        if (o.dump_escaped_dist) {
-            // distributions_diagnostics' escaped distributions, then
-            // dump_escaped_particles and reset_escaped_particles (:519-533)
-            CHECK(write_escaped_dist(tf));
-            if (o.dump_escaped) CHECK(write_particles(h, o.diagnostics_directory, tf, true));
-            CHECK(gpat_reset_escaped_particles(h));
+        if (!o.track_particle_flag) {
+            CHECK(diagnostics(tf));
+            if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, tf));
+            if (o.dump_escaped_dist) {
+                // distributions_diagnostics' escaped distributions, then
+                // dump_escaped_particles and reset_escaped_particles (:519-533)
+                CHECK(write_escaped_dist(tf));
+                if (o.dump_escaped) CHECK(write_particles(h, o.diagnostics_directory, tf, true));
+                CHECK(gpat_reset_escaped_particles(h));
+            }
         }
         if (o.time_interp_flag == 1) CHECK(gpat_copy_fields(h));
         gpat_counters_t c;

@@ -16,6 +16,7 @@
 
 #include "device_common.cuh"
 #include "grid_common.cuh"
+#include "track_common.cuh"
 
 namespace gpat {
 namespace {
@@ -1328,6 +1329,29 @@ __device__ __forceinline__ bool do_push(const MoverArgs &a, State &s, bool fixed
     return true;
 }
 
+// Particle tracking after a push (particle_module.f90:1697-1703 and
+// :1806-1812): a tracked particle (tag_splitted < 0) whose push count wraps
+// to 0 appends its state to its columns of particles_tracked.  The columns
+// are searched once per call (they depend on tags and split_times only).
+template <bool FT>
+__device__ __forceinline__ void track_push(const MoverArgs &a, const State &s, int64_t i,
+                                           int32_t &ntrk, int &lo, int &hi, int &found) {
+    if (!a.trk.tags || s.tag_spl >= 0 || s.nsteps_pushed != 0) return;
+    if (found == 0)
+        found = trk_select(a.trk, a.P.origin[i], s.tag_inj, a.P.split_times[i], s.tag_spl, lo,
+                           hi) ? 1 : 2;
+    ntrk += 1;
+    if (found != 1) return;
+    TrkRecord r;
+    r.x = s.x; r.y = s.y; r.z = s.z; r.p = s.p;
+    r.v = FT ? s.v : a.P.v[i];
+    r.mu = s.mu; r.w = s.w; r.t = s.t; r.dt = s.dt;
+    r.split_times = a.P.split_times[i]; r.count_flag = s.flag;
+    r.origin = a.P.origin[i]; r.nsteps_tracked = ntrk; r.nsteps_pushed = s.nsteps_pushed;
+    r.tag_inj = s.tag_inj; r.tag_spl = s.tag_spl; r.ctr = s.ctr;
+    trk_write(a.trk, ntrk, lo, hi, r, a.cnt);
+}
+
 // FT: focused transport.  FULL: interpolate all 32 variables (focused
 // transport and momentum diffusion read velocity gradients and density that
 // the packed records leave out).  GRID: spherical coordinates or non-uniform
@@ -1359,6 +1383,9 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
             boundary<NDIM>(a, s, a.xmin1, a.xmax1, a.ymin1, a.ymax1, a.zmin1, a.zmax1, acc);
         }
         uint32_t pushes = 0;
+        // nsteps_tracked restarts at 1 every call (particle_mover :1910-1913)
+        int32_t ntrk = 1;
+        int trk_lo = 0, trk_hi = -1, trk_found = 0;
         bool alive = (s.flag == 1);
         while (alive && dt_target < a.limit) {
             if (s.flag != 1) break;
@@ -1371,6 +1398,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 }
                 ++pushes;
                 s.nsteps_pushed = (s.nsteps_pushed + 1) % a.nsteps_interval;
+                track_push<FT>(a, s, i, ntrk, trk_lo, trk_hi, trk_found);
             }
             if (!alive) break;
             if ((s.t - t0) > dt_target && s.flag == 1) {
@@ -1386,12 +1414,20 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
                 const double dt_old = s.dt;
                 s.dt = t0 + dt_target - s.t;
                 if (s.dt > 0.0) {
-                    s.nsteps_pushed = s.nsteps_pushed - 1;
+                    // a tracked particle whose undone push was recorded takes
+                    // the record back (:1716-1722)
+                    if (s.tag_spl < 0 && s.nsteps_pushed == 0) {
+                        ntrk -= 1;
+                        s.nsteps_pushed = a.nsteps_interval - 2;
+                    } else {
+                        s.nsteps_pushed = s.nsteps_pushed - 1;
+                    }
                     if (!do_push<NDIM, FT, FULL, GRID, I3>(a, s, true, dl)) {
                         s.flag = 0; alive = false; break;
                     }
                     ++pushes;
                     s.nsteps_pushed = (s.nsteps_pushed + 1) % a.nsteps_interval;
+                    track_push<FT>(a, s, i, ntrk, trk_lo, trk_hi, trk_found);
                 }
                 s.dt = dt_old;
                 negp_or_boundary<NDIM>(a, s, acc);
@@ -1408,7 +1444,7 @@ __global__ void __launch_bounds__(128) mover_fp64_kernel(const MoverArgs a) {
         a.P.t[i] = s.t; a.P.dt[i] = s.dt;
         a.P.count_flag[i] = (int8_t)s.flag;
         a.P.nsteps_pushed[i] = s.nsteps_pushed;
-        a.P.nsteps_tracked[i] = 1;
+        a.P.nsteps_tracked[i] = ntrk;
         a.P.rng_ctr[i] = s.ctr;
     }
     // Warp-aggregated counters.

@@ -5,6 +5,7 @@
 
 #include "device_common.cuh"
 #include "grid_common.cuh"
+#include "track_common.cuh"
 
 namespace gpat {
 namespace {
@@ -400,13 +401,43 @@ __device__ __forceinline__ void copy_particle(const DevParticles &S, int64_t i,
     D.tag_splitted[j] = S.tag_splitted[i]; D.rng_ctr[j] = S.rng_ctr[i];
 }
 
+// split_particle's branch for a tracked parent (particle_module.f90:5452-5474)
+// once child c is a copy of parent i with split_times = kk + 1: the child's
+// tag_splitted counts down, and child and parent each stay tracked (and
+// record their state when the push count is 0) only if the table lists
+// them at the new split level.
+__device__ void split_tracked(const TrackArgs &t, const DevParticles &S, int64_t i, int64_t c,
+                              int kk, DevCounters *cnt) {
+    const int32_t tg = S.tag_splitted[i];
+    const int32_t tc = (int32_t)((uint32_t)tg - (1u << kk));
+    S.tag_splitted[c] = tc;
+    const bool rec = S.nsteps_pushed[i] == 0;
+    int lo, hi;
+    if (trk_select(t, S.origin[c], S.tag_injected[c], kk + 1, tc, lo, hi)) {
+        if (rec) {
+            S.nsteps_tracked[c] += 1;
+            trk_write(t, S.nsteps_tracked[c], lo, hi, trk_from(S, c), cnt);
+        }
+    } else {
+        S.tag_splitted[c] = -tc;
+    }
+    if (trk_select(t, S.origin[i], S.tag_injected[i], kk + 1, tg, lo, hi)) {
+        if (rec) {
+            S.nsteps_tracked[i] += 1;
+            trk_write(t, S.nsteps_tracked[i], lo, hi, trk_from(S, i), cnt);
+        }
+    } else {
+        S.tag_splitted[i] = -tg;   // stop tracking
+    }
+}
+
 // MODE 0: kept particles of S go to D in order.  MODE 1: S == D; each split
 // candidate gets a child at n + rank (if < cap) and is updated in place.
 // MODE 2: escaped particles go to D at cap + rank (cap is the base there).
 template <int MODE>
 __global__ void __launch_bounds__(kScanThreads) tile_scatter_kernel(
     const DevParticles S, const DevParticles D, int64_t n, int64_t cap, SplitRule r,
-    const long long *tile_offsets, DevCounters *cnt) {
+    const long long *tile_offsets, DevCounters *cnt, const TrackArgs trk) {
     __shared__ int warp_pre[kScanThreads / 32];
     __shared__ int sub_total;
     const int64_t base = (int64_t)blockIdx.x * kTile;
@@ -443,7 +474,10 @@ __global__ void __launch_bounds__(kScanThreads) tile_scatter_kernel(
                     S.weight[i] = ldexp(1.0, -(kk + 1));
                     S.split_times[i] = (int8_t)(kk + 1);
                     copy_particle(S, i, S, c);
-                    S.tag_splitted[c] = (int32_t)((uint32_t)S.tag_splitted[i] + (1u << kk));
+                    if (trk.tags && S.tag_splitted[i] < 0)
+                        split_tracked(trk, S, i, c, kk, cnt);
+                    else
+                        S.tag_splitted[c] = (int32_t)((uint32_t)S.tag_splitted[i] + (1u << kk));
                     created += 1;
                 }
             }
@@ -741,7 +775,8 @@ cudaError_t launch_remove_particles(const DevParticles &src, const DevParticles 
     const SplitRule r{0, 0, 0, 0};
     tile_count_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt, esc);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
-    tile_scatter_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, n, r, offsets, cnt);
+    tile_scatter_kernel<0><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, n, r, offsets, cnt,
+                                                                     TrackArgs{});
     return cudaGetLastError();
 }
 
@@ -757,13 +792,14 @@ cudaError_t launch_select_escaped(const DevParticles &src, int64_t n, const DevP
     tile_count_kernel<2><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, n, r, counts, cnt, none);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nselected);
     tile_scatter_kernel<2><<<(unsigned)ntiles, kScanThreads, 0, s>>>(src, dst, n, base, r,
-                                                                     offsets, cnt);
+                                                                     offsets, cnt, TrackArgs{});
     return cudaGetLastError();
 }
 
 cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,
                                    double split_ratio, double pmin_split, double p0, double pmax,
-                                   void *scratch, DevCounters *cnt, cudaStream_t s) {
+                                   void *scratch, DevCounters *cnt, cudaStream_t s,
+                                   const TrackArgs *trk) {
     if (n <= 0) return cudaSuccess;
     const int64_t ntiles = (n + kTile - 1) / kTile;
     long long *counts = static_cast<long long *>(scratch);
@@ -772,7 +808,84 @@ cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap
     const EscHist none{nullptr, 0, 0.0, 0.0, 0.0, 0.0};
     tile_count_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, n, r, counts, cnt, none);
     tile_scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, ntiles, &cnt->nkept);
-    tile_scatter_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, P, n, cap, r, offsets, cnt);
+    tile_scatter_kernel<1><<<(unsigned)ntiles, kScanThreads, 0, s>>>(P, P, n, cap, r, offsets, cnt,
+                                                                     trk ? *trk : TrackArgs{});
+    return cudaGetLastError();
+}
+
+namespace {
+
+// inject_one_particle's tracking block (particle_module.f90:434-440; the
+// same at :622-628): a new particle the table lists is tracked from its
+// first record.
+__global__ void __launch_bounds__(256) track_injected_kernel(const DevParticles P, int64_t first,
+                                                             int64_t n, const TrackArgs t,
+                                                             DevCounters *cnt) {
+    const int64_t i = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int lo, hi;
+    if (!trk_select(t, P.origin[i], P.tag_injected[i], P.split_times[i], P.tag_splitted[i], lo,
+                    hi))
+        return;
+    P.nsteps_tracked[i] = 1;
+    P.tag_injected[i] = -P.tag_injected[i];
+    P.tag_splitted[i] = -1;
+    trk_write(t, 1, lo, hi, trk_from(P, i), cnt);
+}
+
+__device__ __forceinline__ void trk_store(const DevParticles &D, size_t e, const TrkRecord &r) {
+    D.x[e] = r.x; D.y[e] = r.y; D.z[e] = r.z; D.p[e] = r.p; D.v[e] = r.v; D.mu[e] = r.mu;
+    D.weight[e] = r.w; D.t[e] = r.t; D.dt[e] = r.dt;
+    D.split_times[e] = (int8_t)r.split_times; D.count_flag[e] = (int8_t)r.count_flag;
+    D.origin[e] = r.origin; D.nsteps_tracked[e] = r.nsteps_tracked;
+    D.nsteps_pushed[e] = r.nsteps_pushed;
+    D.tag_injected[e] = r.tag_inj; D.tag_splitted[e] = r.tag_spl;
+    D.rng_ctr[e] = r.ctr;
+}
+
+// sync_tracked_particles on one rank: one warp per column compacts the rows
+// with tag_splitted < 0 to the front in order (32 rows at a time, every
+// lane reading before any lane writes; a kept row only moves up) and zeroes
+// the rest.
+__global__ void __launch_bounds__(256) sync_tracked_kernel(const TrackArgs t) {
+    const int col = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    if (col >= t.n) return;
+    const int lane = threadIdx.x & 31;
+    const DevParticles &D = t.rec;
+    const size_t base = (size_t)t.nsteps_max * (size_t)col;
+    int64_t kept = 0;
+    for (int64_t r0 = 0; r0 < t.nsteps_max; r0 += 32) {
+        const int64_t r = r0 + lane;
+        bool keep = false;
+        TrkRecord rec{};
+        if (r < t.nsteps_max && D.tag_splitted[base + r] < 0) {
+            keep = true;
+            rec = trk_from(D, (int64_t)(base + r));
+        }
+        __syncwarp();   // every read of this block of rows before any write
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) trk_store(D, base + kept + __popc(bal & ((1u << lane) - 1u)), rec);
+        kept += __popc(bal);
+        __syncwarp();
+    }
+    const TrkRecord zero{};
+    for (int64_t r = kept + lane; r < t.nsteps_max; r += 32) trk_store(D, base + r, zero);
+}
+
+}  // namespace
+
+cudaError_t launch_track_injected(const DevParticles &P, int64_t first, int64_t n,
+                                  const TrackArgs &trk, DevCounters *cnt, cudaStream_t s) {
+    if (!trk.tags || n <= first) return cudaSuccess;
+    const int64_t m = n - first;
+    track_injected_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(P, first, n, trk, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sync_tracked(const TrackArgs &trk, cudaStream_t s) {
+    if (!trk.tags || trk.n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((trk.n + 7) / 8);
+    sync_tracked_kernel<<<blocks, 256, 0, s>>>(trk);
     return cudaGetLastError();
 }
 

@@ -247,6 +247,37 @@ module gpat_gpu
             type(c_ptr), value :: handle
             type(gpat_counters_t), intent(out) :: out
         end function
+        integer(c_int) function c_init_tracking(handle, tags, nrows, nptl_tracking, &
+                nsteps_interval) bind(c, name="gpat_init_particle_tracking")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: handle
+            integer(c_int32_t), dimension(*), intent(in) :: tags
+            integer(c_int32_t), value :: nrows, nptl_tracking, nsteps_interval
+        end function
+        integer(c_int) function c_read_tracking(handle, filename, nsteps_interval) &
+                bind(c, name="gpat_read_particle_tracking")
+            import :: c_int, c_ptr, c_char, c_int32_t
+            type(c_ptr), value :: handle
+            character(kind=c_char), dimension(*), intent(in) :: filename
+            integer(c_int32_t), value :: nsteps_interval
+        end function
+        integer(c_int) function c_tracking_dims(handle, nsteps, nptl_tracking, dropped) &
+                bind(c, name="gpat_tracking_dims")
+            import :: c_int, c_ptr, c_int32_t, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int64_t), intent(out) :: nsteps, dropped
+            integer(c_int32_t), intent(out) :: nptl_tracking
+        end function
+        integer(c_int) function c_get_tracked(handle, dst) &
+                bind(c, name="gpat_get_tracked_particles")
+            import :: c_int, c_ptr, gpat_particles_t
+            type(c_ptr), value :: handle
+            type(gpat_particles_t), intent(inout) :: dst
+        end function
+        integer(c_int) function c_free_tracking(handle) bind(c, name="gpat_free_particle_tracking")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle
+        end function
     end interface
 
     type(c_ptr), save :: h = c_null_ptr
@@ -565,5 +596,58 @@ module gpat_gpu
         call check(c_get_particles(h, s, int(capacity, c_int64_t), got), "get_particles")
         n = int(got)
     end subroutine gpu_get_ptls
+
+    !< init_particle_tracking (particle_module.f90:5825-5877) from the
+    !< tags_tracking table itself, (split_times_max + 2, nptl_tracking)
+    subroutine gpu_init_particle_tracking(tags_tracking, nsteps_interval)
+        integer(c_int32_t), dimension(:, :), intent(in) :: tags_tracking
+        integer, intent(in) :: nsteps_interval
+        call check(c_init_tracking(h, tags_tracking, int(size(tags_tracking, 1), c_int32_t), &
+            int(size(tags_tracking, 2), c_int32_t), int(nsteps_interval, c_int32_t)), &
+            "init_particle_tracking")
+    end subroutine gpu_init_particle_tracking
+
+    !< init_particle_tracking from a raw tags file (int32 nrows, int32
+    !< nptl_tracking, then the table)
+    subroutine gpu_read_particle_tracking(particle_tags_file, nsteps_interval)
+        character(*), intent(in) :: particle_tags_file
+        integer, intent(in) :: nsteps_interval
+        call check(c_read_tracking(h, trim(particle_tags_file)//c_null_char, &
+            int(nsteps_interval, c_int32_t)), "init_particle_tracking")
+    end subroutine gpu_read_particle_tracking
+
+    !< nsteps_tracking_max and nptl_tracking, the shape of particles_tracked
+    subroutine gpu_tracking_dims(nsteps_tracking_max, nptl_tracking)
+        integer, intent(out) :: nsteps_tracking_max, nptl_tracking
+        integer(c_int64_t) :: nsteps, dropped
+        integer(c_int32_t) :: ntrk
+        call check(c_tracking_dims(h, nsteps, ntrk, dropped), "tracking_dims")
+        nsteps_tracking_max = int(nsteps)
+        nptl_tracking = int(ntrk)
+    end subroutine gpu_tracking_dims
+
+    !< sync_tracked_particles and the datasets of dump_tracked_particles
+    !< (:5994-6030, :6235-6299): particles_tracked(nsteps_tracking_max,
+    !< nptl_tracking) field by field
+    subroutine gpu_get_tracked_particles(x, y, z, p, v, mu, weight, t, dt, split_times, &
+            count_flag, origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted)
+        real(c_double), dimension(:, :), intent(out), target :: x, y, z, p, v, mu, weight, t, dt
+        integer(c_int8_t), dimension(:, :), intent(out), target :: split_times, count_flag
+        integer(c_int32_t), dimension(:, :), intent(out), target :: origin, nsteps_tracked, &
+            nsteps_pushed, tag_injected, tag_splitted
+        type(gpat_particles_t) :: s
+        s%x = c_loc(x); s%y = c_loc(y); s%z = c_loc(z); s%p = c_loc(p); s%v = c_loc(v)
+        s%mu = c_loc(mu); s%weight = c_loc(weight); s%t = c_loc(t); s%dt = c_loc(dt)
+        s%split_times = c_loc(split_times); s%count_flag = c_loc(count_flag)
+        s%origin = c_loc(origin); s%nsteps_tracked = c_loc(nsteps_tracked)
+        s%nsteps_pushed = c_loc(nsteps_pushed); s%tag_injected = c_loc(tag_injected)
+        s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_null_ptr
+        call check(c_get_tracked(h, s), "dump_tracked_particles")
+    end subroutine gpu_get_tracked_particles
+
+    !< free_particle_tracking (:5905-5911)
+    subroutine gpu_free_particle_tracking
+        call check(c_free_tracking(h), "free_particle_tracking")
+    end subroutine gpu_free_particle_tracking
 
 end module gpat_gpu

@@ -180,6 +180,12 @@ SIGNATURES = {
     "gpat_calc_local_distribution": (C.c_int, [Handle, P(LocalDist), P(d), P(u64)]),
     "gpat_calc_escaped_distributions": (C.c_int, [Handle, P(d), P(u64)]),
     "gpat_reset_escaped_particles": (C.c_int, [Handle]),
+    "gpat_init_particle_tracking": (C.c_int, [Handle, P(C.c_int32), C.c_int32, C.c_int32,
+                                              C.c_int32]),
+    "gpat_read_particle_tracking": (C.c_int, [Handle, C.c_char_p, C.c_int32]),
+    "gpat_tracking_dims": (C.c_int, [Handle, P(C.c_int64), P(C.c_int32), P(C.c_int64)]),
+    "gpat_get_tracked_particles": (C.c_int, [Handle, P(Particles)]),
+    "gpat_free_particle_tracking": (C.c_int, [Handle]),
     "gpat_pbins_edges": (C.c_int, [Handle, P(d)]),
     "gpat_quick_check": (C.c_int, [Handle, P(d)]),
     "gpat_get_counters": (C.c_int, [Handle, P(Counters)]),

@@ -382,6 +382,39 @@ class Engine:
                                                         C.byref(got)))
         return ps
 
+    # -- particle tracking -------------------------------------------------------
+    def init_particle_tracking(self, tags, nsteps_interval=10):
+        """init_particle_tracking: tags is tags_tracking as (nptl_tracking,
+        nrows), one row per tracked particle: origin, tag_injected and
+        tag_splitted after each split."""
+        t = np.ascontiguousarray(tags, dtype=np.int32)
+        if t.ndim != 2:
+            raise ValueError("tags must be (nptl_tracking, nrows)")
+        self._check(self.lib.gpat_init_particle_tracking(
+            self.h, t.ctypes.data_as(C.POINTER(C.c_int32)), t.shape[1], t.shape[0],
+            nsteps_interval))
+
+    def read_particle_tracking(self, path, nsteps_interval=10):
+        self._check(self.lib.gpat_read_particle_tracking(self.h, str(path).encode(),
+                                                         nsteps_interval))
+
+    def tracking_dims(self):
+        """(nsteps_tracking_max, nptl_tracking, dropped records)."""
+        s, n, d = C.c_int64(), C.c_int32(), C.c_int64()
+        self._check(self.lib.gpat_tracking_dims(self.h, C.byref(s), C.byref(n), C.byref(d)))
+        return s.value, n.value, d.value
+
+    def get_tracked_particles(self) -> dict:
+        """sync_tracked_particles and the datasets of dump_tracked_particles:
+        each field shaped (nptl_tracking, nsteps_tracking_max)."""
+        nsteps, ntrk, _ = self.tracking_dims()
+        ps = ParticleSet.empty(nsteps * ntrk)
+        self._check(self.lib.gpat_get_tracked_particles(self.h, C.byref(ps.ctypes())))
+        return {k: v.reshape(ntrk, nsteps) for k, v in ps.arrays.items()}
+
+    def free_particle_tracking(self):
+        self._check(self.lib.gpat_free_particle_tracking(self.h))
+
     @property
     def nptl_current(self) -> int:
         return self.counters().nptl_current

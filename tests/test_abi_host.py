@@ -29,6 +29,16 @@ def test_library_exports_every_declared_symbol(engine_lib):
     assert engine_lib.gpat_version().startswith(b"gpat-gb300")
 
 
+def test_fortran_shim_binds_exported_symbols(engine_lib):
+    """Every bind(c, name=...) of the Fortran shim names an exported entry
+    point (no Fortran compiler is needed to check the names)."""
+    shim = HEADER.parent.parent / "stochastic-parker_gb300" / "fortran" / "gpat_gpu.f90"
+    names = re.findall(r'bind\(c,\s*name="(gpat_[a-z0-9_]+)"\)', shim.read_text())
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(engine_lib, n), n
+
+
 def test_struct_layouts_match_header():
     # gpat_mhd_config_t: 13 doubles + 13 int32 (+4 bytes tail padding)
     assert C.sizeof(_abi.MhdConfig) == 160

@@ -36,7 +36,7 @@ def _dataset(tmp_path: Path):
     return w, data, out
 
 
-def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
+def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False, extra=()):
     exe = build.build_driver()
     cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
            "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
@@ -44,7 +44,7 @@ def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False):
            "--precision", precision, "--seed", str(SEED), "-ug", "1",
            "-ft", ".true." if ft else ".false.",
            "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1",
-           "-ded", ".true.", "-de", ".true."]
+           "-ded", ".true.", "-de", ".true.", *extra]
     return subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
 
 
@@ -124,6 +124,70 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
         assert len(d["x"]) == len(got)
         for k in d:
             assert np.array_equal(d[k], got[k]), k
+    eng.close()
+
+
+def _read_tracked(path: Path) -> dict:
+    """particles_tracked_XXXX.dat: int64 nsteps_tracking_max, int64
+    nptl_tracking, then each dataset in Fortran order."""
+    raw = path.read_bytes()
+    nsteps, ntrk = np.frombuffer(raw[:16], np.int64)
+    m = int(nsteps * ntrk)
+    out, off = {}, 16
+    names = [("x", "f8"), ("y", "f8"), ("z", "f8"), ("p", "f8"), ("v", "f8"), ("mu", "f8"),
+             ("weight", "f8"), ("t", "f8"), ("dt", "f8"), ("split_times", "i1"),
+             ("count_flag", "i1"), ("origin", "i4"), ("nsteps_tracked", "i4"),
+             ("nsteps_pushed", "i4"), ("tag_injected", "i4"), ("tag_splitted", "i4")]
+    for k, t in names:
+        size = np.dtype(t).itemsize * m
+        out[k] = np.frombuffer(raw[off:off + size], t).reshape(int(ntrk), int(nsteps))
+        off += size
+    assert off == len(raw)
+    return out
+
+
+@pytest.mark.gpu
+def test_driver_particle_tracking(tmp_path):
+    """-tf .true. -ptf -ni: the tags table is read from
+    particle_tracking/, the mover runs with one fine step, and
+    particles_tracked_XXXX.dat per frame equals the records of the same
+    calls made from Python; the distributions are not written."""
+    w, data, out = _dataset(tmp_path)
+    (out / "particle_tracking").mkdir()
+    table = np.array([(0, t, a, b) for t in (3, 50, 777, 2100)
+                      for a, b in ((1, 1), (1, 3), (2, 2), (2, 4))], np.int32)
+    tags_file = out / "particle_tracking" / "tags.dat"
+    with open(tags_file, "wb") as f:
+        np.array([table.shape[1], table.shape[0]], np.int32).tofile(f)
+        table.tofile(f)
+    r = _run_driver(tmp_path, data, out, extra=("-tf", ".true.", "-ptf", "tags.dat",
+                                                "-ni", "5", "-nf", "4"))
+    assert r.returncode == 0, r.stderr
+    assert not (out / "fdists_0001.dat").exists()
+    assert len((out / "quick.dat").read_text().splitlines()) == 1
+
+    prm = make_params(**dict(w.params, npp_global=64, nptl_max=40000, seed=SEED, precision=0,
+                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1, duu0=3.0))
+    eng = Engine(prm, w.mhd_config, 0)
+    eng.calc_tstamps_mhd(0, 3)
+    eng.read_particle_tracking(tags_file, 5)
+    eng.read_field_data(data / "mhd_data_0000", 0)
+    eng.calc_fields_gradients(0)
+    for tf in range(1, 4):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        eng.inject_particles_at_x(2000, 0.5, 1e-7, 1, 1.0, tf)
+        eng.particle_mover(nsteps_interval=5, mhd_tframe=tf, num_fine_steps=1)
+        rec = eng.get_tracked_particles()
+        d = _read_tracked(out / "particle_tracking" / f"particles_tracked_{tf:04d}.dat")
+        for k in d:
+            assert np.array_equal(d[k], rec[k]), (tf, k)
+        assert (d["tag_splitted"] < 0).sum() > 0
+        eng.split_particle(2.72, 2.0, 5)
+    got = eng.get_particles()
+    d = read_particle_dump(out / "restart" / "particles_0003.dat")
+    for k in d:
+        assert np.array_equal(d[k], got[k]), k
     eng.close()
 
 
