@@ -159,6 +159,12 @@ const char *gpat_last_error(const gpat_handle_t *h);
  * tstamps[0] is the reference's tstamps_mhd(1). */
 int gpat_set_tstamps(gpat_handle_t *h, const double *tstamps, int n);
 int gpat_calc_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end);
+/* load_tstamps_mhd (mhd_config.f90:221-255), for a varying MHD output
+ * interval: <dir_mhd_data>time_stamps.dat holds the first frame as int32
+ * (in an 8-byte slot), then one float64 per frame from the second slot on;
+ * frames past tmax_mhd continue with the last interval. */
+int gpat_load_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end, int tmax_mhd,
+                          const char *dir_mhd_data);
 
 /* read_field_data_parallel (mhd_data_parallel.f90:224-300) from memory:
  * farray is the Fortran-order (nvar, nxg, nyg, nzg) single-precision array,
@@ -371,6 +377,9 @@ int gpat_tracking_dims(gpat_handle_t *h, int64_t *nsteps_tracking_max, int32_t *
 int gpat_get_tracked_particles(gpat_handle_t *h, gpat_particles_t *dst);
 /* free_particle_tracking (:5905-5911). */
 int gpat_free_particle_tracking(gpat_handle_t *h);
+/* get_pmax_global (diagnostics.f90:1691-1721): the largest particle momentum
+ * (0 without particles). */
+int gpat_get_pmax_global(gpat_handle_t *h, double *pmax);
 /* pbins_edges_global (diagnostics.f90:194-204): npp_global + 1 values. */
 int gpat_pbins_edges(gpat_handle_t *h, double *edges);
 /* quick_check (diagnostics.f90:116-170) for one rank: out = {nptl_current,

@@ -2627,7 +2627,7 @@ void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spheri
     const double dxd = cfg->lx / nrx, dyd = cfg->ly / nry, dzd = cfg->lz / nrz;
     const double pmin_log = log10(pmin);
     const double dp_log = (log10(pmax) - pmin_log) / npbins;
-    const double dmu = 2.0 / nmu;
+    const double dmu = (double)(2.0f / (float)nmu);   /* single precision, :273 */
     const size_t nb = (size_t)nmu * npbins * nrx * nry * nrz;
     for (size_t b = 0; b < nb; ++b) { counts[b] = 0; whi[b] = 0; wlo[b] = 0; }
     for (int64_t i = 0; i < n; ++i) {

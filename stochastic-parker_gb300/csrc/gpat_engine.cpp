@@ -636,6 +636,34 @@ int gpat_calc_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end) {
     return GPAT_OK;
 }
 
+int gpat_load_tstamps_mhd(gpat_handle_t *h, int t_start, int t_end, int tmax_mhd,
+                          const char *dir_mhd_data) {
+    if (!h || !dir_mhd_data) return GPAT_ERR_ARG;
+    if (t_end <= t_start) return fail(h, GPAT_ERR_ARG, "t_end must exceed t_start");
+    // load_tstamps_mhd (mhd_config.f90:221-255): int32 first frame ts_mhd at
+    // byte 0, the stamp of frame i in 8-byte slot i - ts_mhd + 2; frames past
+    // tmax_mhd continue with the last interval.
+    const std::string path = std::string(dir_mhd_data) + "time_stamps.dat";
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return fail(h, GPAT_ERR_IO, "cannot open " + path);
+    int32_t ts_mhd = 0;
+    const int n = t_end - t_start + 1;
+    const int nread = std::min(tmax_mhd, t_end) - t_start + 1;
+    std::vector<double> ts((size_t)n, 0.0);
+    bool ok = std::fread(&ts_mhd, sizeof ts_mhd, 1, f) == 1 && t_start >= ts_mhd && nread >= 1;
+    if (ok) ok = std::fseek(f, (long)(t_start - ts_mhd + 2) * 8, SEEK_SET) == 0;
+    if (ok) ok = std::fread(ts.data(), sizeof(double), (size_t)nread, f) == (size_t)nread;
+    std::fclose(f);
+    if (!ok) return fail(h, GPAT_ERR_IO, "time_stamps.dat does not cover t_start .. tmax_mhd");
+    if (nread < n) {
+        if (nread < 2) return fail(h, GPAT_ERR_ARG, "tmax_mhd leaves fewer than two stamps");
+        const double dt_last = ts[nread - 1] - ts[nread - 2];
+        for (int i = nread; i < n; ++i) ts[i] = ts[i - 1] + dt_last;
+    }
+    h->tstamps = ts;
+    return GPAT_OK;
+}
+
 int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nvar) {
     if (!h || !farray || (nvar != 8 && nvar != 32)) return fail(h, GPAT_ERR_ARG, "nvar must be 8 or 32");
     const int slot = var_flag == 0 ? 0 : 1;
@@ -1255,7 +1283,7 @@ static int local_args(gpat_handle_t *h, const gpat_local_dist_t *sp, LocalDistAr
     a.xmin = c.xmin; a.ymin = c.ymin; a.zmin = c.zmin;
     a.pmin_log = std::log10(sp->pmin);
     a.dp_log = (std::log10(sp->pmax) - a.pmin_log) / sp->npbins;
-    a.dmu = 2.0 / sp->nmu;
+    a.dmu = (double)(2.0f / (float)sp->nmu);   // 2.0 / nmu1 in single precision (:273)
     a.nmu = sp->nmu;
     a.npb = sp->npbins;
     a.ndim = h->prm.ndim;
@@ -1317,6 +1345,18 @@ int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t
             if (counts) counts[k] = b[3 * k];
             if (fescaped) fescaped[k] = fixed_to_double(b[3 * k + 1], b[3 * k + 2]);
         }
+    return GPAT_OK;
+}
+
+int gpat_get_pmax_global(gpat_handle_t *h, double *pmax) {
+    if (!h || !pmax) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemsetAsync(&h->dcnt->pmax_bits, 0, sizeof(unsigned long long), h->stream));
+    CK(launch_pmax(h->P[h->cur], h->n, &h->dcnt->pmax_bits, h->stream));
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, &h->dcnt->pmax_bits, sizeof bits, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::memcpy(pmax, &bits, sizeof bits);
     return GPAT_OK;
 }
 

@@ -46,6 +46,7 @@ struct DevCounters {
     unsigned int pad;
     unsigned long long bad_value;
     unsigned long long trk_dropped;  // tracked records past nsteps_tracking_max
+    unsigned long long pmax_bits;    // get_pmax_global: bits of the largest p >= 0
 };
 
 // Packed per-cell field records read by the movers.  2D: 16 floats,
@@ -299,6 +300,11 @@ cudaError_t launch_track_injected(const DevParticles &P, int64_t first, int64_t 
 // sync_tracked_particles on one rank (particle_module.f90:5994-6030): each
 // column keeps its records with tag_splitted < 0 in order, the rest zeroed.
 cudaError_t launch_sync_tracked(const TrackArgs &trk, cudaStream_t s);
+// get_pmax_global (diagnostics.f90:1691-1721): the largest p over the
+// particles, from 0, as the bits of a non-negative double in *bits (zeroed
+// by the caller).
+cudaError_t launch_pmax(const DevParticles &P, int64_t n, unsigned long long *bits,
+                        cudaStream_t s);
 // Grid geometry for spatial binning of particles (one bin per field cell).
 struct CellGrid {
     double xmin, ymin, zmin, idx, idy, idz;

@@ -18,6 +18,7 @@
 // (write_tracked below) instead of the distributions.
 #include <sys/stat.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -43,6 +44,10 @@ struct Options {
     // -tf, -ptf (stochastic-mhd.f90:711-722)
     bool track_particle_flag = false;
     std::string particle_tags_file = "tags_selected_01.dat";
+    // -vdt, -rf, -qh, -ld, -sm (stochastic-mhd.f90:623-649, :839-842, :931-933)
+    bool varying_dt_mhd = false, restart_flag = false, local_dist = false;
+    double quota_hour = 48.0;
+    int size_mpi_sub = 1;
     // inject_particles_at_large_* switches (stochastic-mhd.f90:735-806)
     bool inject_large_jz = false, inject_large_absj = false, inject_large_db2 = false;
     bool inject_large_divv = false, inject_large_rho = false, inject_same_nptl = false;
@@ -114,7 +119,9 @@ int parse(int argc, char **argv, Options &o) {
         {"-nv", "--ncells_large_divv_norm"}, {"-nr", "--ncells_large_rho_norm"},
         {"-db2", "--db2_min"}, {"-nb", "--ncells_large_db2_norm"}, {"-db", "--deltab_flag"},
         {"-co", "--correlation"}, {"-tf", "--track_particle_flag"},
-        {"-ptf", "--particle_tags_file"}};
+        {"-ptf", "--particle_tags_file"}, {"-vdt", "--varying_dt_mhd"},
+        {"-rf", "--restart_flag"}, {"-qh", "--quota_hour"}, {"-ld", "--local_dist"},
+        {"-sm", "--size_mpi_sub"}};
     for (int i = 1; i < argc; ++i) {
         std::string k = argv[i];
         if (alias.count(k)) k = alias[k];
@@ -198,6 +205,11 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--correlation") o.correlation_flag = (int)d;
         else if (k == "--track_particle_flag") o.track_particle_flag = truthy(v);
         else if (k == "--particle_tags_file") o.particle_tags_file = v;
+        else if (k == "--varying_dt_mhd") o.varying_dt_mhd = truthy(v);
+        else if (k == "--restart_flag") o.restart_flag = truthy(v);
+        else if (k == "--quota_hour") o.quota_hour = d;
+        else if (k == "--local_dist") o.local_dist = truthy(v);
+        else if (k == "--size_mpi_sub") o.size_mpi_sub = (int)d;
         else if (k == "--precision") {
             o.precision = (v == "fp64" || v == "0") ? GPAT_PREC_FP64 : GPAT_PREC_MIXED;
             o.precision_set = true;
@@ -321,6 +333,114 @@ int write_tracked(gpat_handle_t *h, const std::string &dir, int frame) {
     return ok ? GPAT_OK : GPAT_ERR_IO;
 }
 
+// read_particles for a restart: particles_XXXX.dat as write_particles makes
+// it, with the Philox counters of prng_state_XXXX.dat when present (they
+// take the place of the MT19937 states of save_prng / init_prng).
+int read_particles(gpat_handle_t *h, const std::string &dir, int frame) {
+    char name[64];
+    std::snprintf(name, sizeof name, "particles_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "rb");
+    if (!f) return GPAT_ERR_IO;
+    int64_t n = 0;
+    bool ok = std::fread(&n, 8, 1, f) == 1 && n >= 0;
+    const size_t m = (size_t)(ok && n > 0 ? n : 1);
+    std::vector<double> f64[9];
+    std::vector<int8_t> i8[2];
+    std::vector<int32_t> i32[5];
+    std::vector<uint32_t> ctr(m, 0u);
+    for (auto &v : f64) { v.resize(m); if (ok) ok = std::fread(v.data(), 8, (size_t)n, f) == (size_t)n; }
+    for (auto &v : i8) { v.resize(m); if (ok) ok = std::fread(v.data(), 1, (size_t)n, f) == (size_t)n; }
+    for (auto &v : i32) { v.resize(m); if (ok) ok = std::fread(v.data(), 4, (size_t)n, f) == (size_t)n; }
+    std::fclose(f);
+    if (!ok) return GPAT_ERR_IO;
+    std::snprintf(name, sizeof name, "prng_state_%04d.dat", frame);
+    if (FILE *g = std::fopen((dir + name).c_str(), "rb")) {
+        int64_t nc = 0;
+        ok = std::fread(&nc, 8, 1, g) == 1 && nc == n &&
+             std::fread(ctr.data(), 4, (size_t)n, g) == (size_t)n;
+        std::fclose(g);
+        if (!ok) return GPAT_ERR_IO;
+    }
+    gpat_particles_t P;
+    P.x = f64[0].data(); P.y = f64[1].data(); P.z = f64[2].data(); P.p = f64[3].data();
+    P.v = f64[4].data(); P.mu = f64[5].data(); P.weight = f64[6].data(); P.t = f64[7].data();
+    P.dt = f64[8].data();
+    P.split_times = i8[0].data(); P.count_flag = i8[1].data();
+    P.origin = i32[0].data(); P.nsteps_tracked = i32[1].data(); P.nsteps_pushed = i32[2].data();
+    P.tag_injected = i32[3].data(); P.tag_splitted = i32[4].data();
+    P.rng_ctr = ctr.data();
+    return gpat_put_particles(h, &P, n);
+}
+
+// prng_state_XXXX.dat: int64 nptl, then the particles' Philox counters in
+// the order of particles_XXXX.dat.
+int write_prng_state(gpat_handle_t *h, const std::string &dir, int frame) {
+    gpat_counters_t c;
+    int rc = gpat_get_counters(h, &c);
+    if (rc) return rc;
+    const int64_t n = c.nptl_current;
+    std::vector<uint32_t> ctr((size_t)(n > 0 ? n : 1));
+    gpat_particles_t P;
+    std::memset(&P, 0, sizeof P);
+    P.rng_ctr = ctr.data();
+    int64_t got = 0;
+    rc = gpat_get_particles(h, &P, n, &got);
+    if (rc) return rc;
+    char name[64];
+    std::snprintf(name, sizeof name, "prng_state_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return GPAT_ERR_IO;
+    bool ok = std::fwrite(&got, 8, 1, f) == 1 &&
+              std::fwrite(ctr.data(), 4, (size_t)got, f) == (size_t)got;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? GPAT_OK : GPAT_ERR_IO;
+}
+
+// save_particle_module_state / read_particle_module_state
+// (particle_module.f90:5532-5660) for one rank without HDF5:
+// particle_module_state_XXXX.dat holds int64 nptl_current, nptl_split,
+// tag_max, float64 leak, leak_negp, then the exact fixed-point sums
+// (uint64 leak_hi, leak_lo, leak_negp_hi, leak_negp_lo).
+int write_module_state(gpat_handle_t *h, const std::string &dir, int frame) {
+    gpat_counters_t c;
+    int rc = gpat_get_counters(h, &c);
+    if (rc) return rc;
+    char name[64];
+    std::snprintf(name, sizeof name, "particle_module_state_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "wb");
+    if (!f) return GPAT_ERR_IO;
+    const int64_t i3[3] = {c.nptl_current, c.nptl_split, c.tag_max};
+    const double d2[2] = {c.leak, c.leak_negp};
+    const uint64_t u4[4] = {c.leak_hi, c.leak_lo, c.leak_negp_hi, c.leak_negp_lo};
+    bool ok = std::fwrite(i3, 8, 3, f) == 3 && std::fwrite(d2, 8, 2, f) == 2 &&
+              std::fwrite(u4, 8, 4, f) == 4;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? GPAT_OK : GPAT_ERR_IO;
+}
+
+int read_module_state(gpat_handle_t *h, const std::string &dir, int frame) {
+    char name[64];
+    std::snprintf(name, sizeof name, "particle_module_state_%04d.dat", frame);
+    FILE *f = std::fopen((dir + name).c_str(), "rb");
+    if (!f) return GPAT_ERR_IO;
+    int64_t i3[3];
+    double d2[2];
+    uint64_t u4[4];
+    bool ok = std::fread(i3, 8, 3, f) == 3 && std::fread(d2, 8, 2, f) == 2 &&
+              std::fread(u4, 8, 4, f) == 4;
+    std::fclose(f);
+    if (!ok) return GPAT_ERR_IO;
+    gpat_counters_t c;
+    int rc = gpat_get_counters(h, &c);
+    if (rc) return rc;
+    c.nptl_split = i3[1];
+    c.tag_max = i3[2];
+    c.leak = d2[0];
+    c.leak_negp = d2[1];
+    c.leak_hi = u4[0]; c.leak_lo = u4[1]; c.leak_negp_hi = u4[2]; c.leak_negp_lo = u4[3];
+    return gpat_set_counters(h, &c);
+}
+
 std::string frame_name(const std::string &dir, int tf) {
     char buf[32];
     std::snprintf(buf, sizeof buf, "mhd_data_%04d", tf);
@@ -389,7 +509,35 @@ int main(int argc, char **argv) {
         CHECK(gpat_init_acc_surface(h, o.surface_norm1.c_str(),
                                     o.surface2_existed ? o.surface_norm2.c_str() : nullptr,
                                     o.is_intersection ? 1 : 0));
-    CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
+    const auto wall_start = std::chrono::steady_clock::now();
+    // the time stamps of the MHD frames (stochastic-mhd.f90:173-178)
+    if (o.varying_dt_mhd)
+        CHECK(gpat_load_tstamps_mhd(h, o.t_start, o.t_end, o.tmax_mhd, o.dir_mhd_data.c_str()));
+    else
+        CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
+    if (o.size_mpi_sub != 1) {
+        std::fprintf(stderr, "gpat_run: one rank per device; -sm must be 1\n");
+        gpat_destroy(h);
+        return 2;
+    }
+    // restart (stochastic-mhd.f90:224-238): the frame of restart/latest_restart,
+    // its particles and module state
+    const std::string restart = o.diagnostics_directory + "restart/";
+    int tmin = o.t_start;
+    if (o.restart_flag) {
+        FILE *lr = std::fopen((restart + "latest_restart").c_str(), "rb");
+        int32_t t32 = 0;
+        const bool got = lr && std::fread(&t32, 4, 1, lr) == 1;
+        if (lr) std::fclose(lr);
+        if (!got) {
+            std::fprintf(stderr, "gpat_run: cannot read %slatest_restart\n", restart.c_str());
+            gpat_destroy(h);
+            return 1;
+        }
+        tmin = t32;
+        CHECK(read_particles(h, restart, tmin));
+        CHECK(read_module_state(h, restart, tmin));
+    }
     // init_particle_tracking (stochastic-mhd.f90:241-244)
     const std::string track_dir = o.diagnostics_directory + "particle_tracking/";
     if (o.track_particle_flag)
@@ -397,7 +545,6 @@ int main(int argc, char **argv) {
                                           o.nsteps_interval));
 
     // Frame tmin into farray1, gradients (:321, :350).
-    const int tmin = o.t_start;
     CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tmin).c_str(), 0));
     // read_acc_surface of <dir><surface_filename>_XXXX.dat (:324-333, :406-415)
     auto read_surfaces = [&](int tf, int var_flag) -> int {
@@ -438,10 +585,91 @@ int main(int argc, char **argv) {
     std::vector<uint64_t> counts(npp);
     CHECK(gpat_pbins_edges(h, edges.data()));
     const std::string qpath = o.diagnostics_directory + "quick.dat";
-    FILE *quick = std::fopen(qpath.c_str(), "w");
+    FILE *quick = std::fopen(qpath.c_str(), o.restart_flag ? "a" : "w");
     if (!quick) { std::fprintf(stderr, "gpat_run: cannot write %s\n", qpath.c_str()); gpat_destroy(h); return 1; }
-    std::fprintf(quick, "%6s%13s%13s%13s%13s%13s%13s%13s%13s\n", "iframe", "nptl_current",
-                 "nptl_split", "ntot", "leak", "leak_negp", "pdt_min", "pdt_max", "pdt_avg");
+    if (!o.restart_flag)
+        std::fprintf(quick, "%6s%13s%13s%13s%13s%13s%13s%13s%13s\n", "iframe", "nptl_current",
+                     "nptl_split", "ntot", "leak", "leak_negp", "pdt_min", "pdt_max", "pdt_avg");
+
+    // read_diagnostics_params (diagnostics.f90:2049-2222): local-distribution
+    // set k is on when dump_intervalk < t_end - t_start; mu bins only with
+    // focused transport.
+    struct LocalSet { int k; gpat_local_dist_t spec; };
+    std::vector<LocalSet> local_sets;
+    if (o.local_dist) {
+        auto var = [&](const std::string &key) -> double {
+            double v = -1.0;
+            return gpat_get_variable(conf.c_str(), key.c_str(), &v) == GPAT_OK ? v : -1.0;
+        };
+        for (int k = 1; k <= 4; ++k) {
+            const std::string s = std::to_string(k);
+            if (!((int)var("dump_interval" + s) < o.t_end - o.t_start)) continue;
+            gpat_local_dist_t sp;
+            std::memset(&sp, 0, sizeof sp);
+            sp.pmin = var("pmin" + s);
+            sp.pmax = var("pmax" + s);
+            sp.npbins = (int)var("npbins" + s);
+            sp.nmu = o.focused_transport ? (int)var("nmu" + s) : 1;
+            sp.rx = (int)var("rx" + s);
+            sp.ry = (int)var("ry" + s);
+            sp.rz = (int)var("rz" + s);
+            if (!(sp.pmin > 0.0 && sp.pmax > sp.pmin) || sp.npbins < 1 || sp.nmu < 1 ||
+                sp.rx < 1 || sp.ry < 1 || sp.rz < 1) {
+                std::fprintf(stderr, "gpat_run: local distribution %d: bad or missing "
+                             "pmin/pmax/npbins/nmu/rx/ry/rz in %s\n", k, conf.c_str());
+                gpat_destroy(h);
+                return 2;
+            }
+            local_sets.push_back({k, sp});
+        }
+    }
+    // flocalK_XXXX.dat: int32 {nmu, npbins, nrx, nry, nrz}, the npbins + 1
+    // p edges and nmu + 1 mu edges (pbinsK_edges, mubinsK_edges), flocalK
+    // in Fortran order, then the uint64 particle counts.
+    auto write_local = [&](int frame) -> int {
+        for (const LocalSet &ls : local_sets) {
+            int32_t dims[5];
+            int rc = gpat_local_distribution_dims(h, &ls.spec, dims);
+            if (rc) return rc;
+            const size_t nb = (size_t)dims[0] * dims[1] * dims[2] * dims[3] * dims[4];
+            std::vector<double> fl(nb);
+            std::vector<uint64_t> cl(nb);
+            rc = gpat_calc_local_distribution(h, &ls.spec, fl.data(), cl.data());
+            if (rc) return rc;
+            // init_local_particle_distributions (:262-290)
+            const double lo = std::log10(ls.spec.pmin), hi = std::log10(ls.spec.pmax);
+            const double dlog = (hi - lo) / ls.spec.npbins;
+            const double dmu = (double)(2.0f / (float)ls.spec.nmu);
+            std::vector<double> pe(ls.spec.npbins + 1), me(ls.spec.nmu + 1);
+            for (int i = 0; i <= ls.spec.npbins; ++i) pe[i] = std::pow(10.0, lo + i * dlog);
+            for (int i = 0; i <= ls.spec.nmu; ++i) me[i] = -1.0 + i * dmu;
+            char name[64];
+            std::snprintf(name, sizeof name, "flocal%d_%04d.dat", ls.k, frame);
+            FILE *f = std::fopen((o.diagnostics_directory + name).c_str(), "wb");
+            if (!f) return GPAT_ERR_IO;
+            bool ok = std::fwrite(dims, 4, 5, f) == 5 &&
+                      std::fwrite(pe.data(), 8, pe.size(), f) == pe.size() &&
+                      std::fwrite(me.data(), 8, me.size(), f) == me.size() &&
+                      std::fwrite(fl.data(), 8, nb, f) == nb &&
+                      std::fwrite(cl.data(), 8, nb, f) == nb;
+            ok = (std::fclose(f) == 0) && ok;
+            if (!ok) return GPAT_ERR_IO;
+        }
+        return GPAT_OK;
+    };
+    // get_pmax_global (diagnostics.f90:1691-1721): pmax_global.dat, one
+    // line per frame, created at the initial diagnostics
+    auto write_pmax = [&](bool create) -> int {
+        double pm = 0.0;
+        int rc = gpat_get_pmax_global(h, &pm);
+        if (rc) return rc;
+        FILE *f = std::fopen((o.diagnostics_directory + "pmax_global.dat").c_str(),
+                             create ? "w" : "a");
+        if (!f) return GPAT_ERR_IO;
+        std::fprintf(f, "%13.6E\n", pm);
+        std::fclose(f);
+        return GPAT_OK;
+    };
 
     auto diagnostics = [&](int frame) -> int {
         double q[8];
@@ -462,7 +690,7 @@ int main(int argc, char **argv) {
         std::fwrite(fglobal.data(), 8, fglobal.size(), f);
         std::fwrite(counts.data(), 8, counts.size(), f);
         std::fclose(f);
-        return GPAT_OK;
+        return write_local(frame);
     };
 
     // fescaped_XXXX.dat: int32 npp, int32 2 ndim, npp + 1 edges, the
@@ -486,6 +714,8 @@ int main(int argc, char **argv) {
         return GPAT_OK;
     };
 
+    int tf_done = o.t_end;
+    bool reached_quota = false;
     for (int tf = tmin + 1; tf <= o.t_end; ++tf) {
         if (o.single_time_frame == 0 && tf <= o.tmax_mhd) {
             CHECK(gpat_read_field_data(h, frame_name(o.dir_mhd_data, tf).c_str(), o.time_interp_flag));
@@ -520,6 +750,7 @@ int main(int argc, char **argv) {
         }
         // initial diagnostics unless tracking (:486-495)
         if (tf == o.t_start + 1 && !o.track_particle_flag) {
+            CHECK(write_pmax(true));
             CHECK(diagnostics(o.t_start));
             if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, o.t_start));
         }
@@ -530,6 +761,7 @@ int main(int argc, char **argv) {
         if (o.track_particle_flag) CHECK(write_tracked(h, track_dir, tf));
         if (o.split_flag == 1) CHECK(gpat_split_particle(h, o.split_ratio, o.pmin_split, o.nsteps_interval));
         if (!o.track_particle_flag) {
+            CHECK(write_pmax(false));
             CHECK(diagnostics(tf));
             if (o.particle_data_dump == 1) CHECK(write_particles(h, o.diagnostics_directory, tf));
             if (o.dump_escaped_dist) {
@@ -546,12 +778,39 @@ int main(int argc, char **argv) {
         std::printf("frame %d: %lld particles, %llu pushes, mover %.2f ms\n", tf,
                     (long long)c.nptl_current, (unsigned long long)c.last_mover_steps,
                     c.last_mover_ms);
+        // stop 30 minutes before the wall-time quota (:559-565)
+        const double uptime = std::chrono::duration<double>(std::chrono::steady_clock::now() -
+                                                            wall_start).count();
+        if (uptime > (o.quota_hour - 0.5) * 3600.0) {
+            reached_quota = true;
+            tf_done = tf;
+            break;
+        }
     }
     std::fclose(quick);
-    // Restart dump at t_end (stochastic-mhd.f90:264).
-    const std::string restart = o.diagnostics_directory + "restart/";
+    // Restart files (stochastic-mhd.f90:252-273): particles and module state
+    // under t_end and latest_restart holding the last finished frame.  When
+    // the quota stopped the loop early they are also written under that
+    // frame, which is the one a restart reads.
     mkdir(restart.c_str(), 0755);
-    CHECK(write_particles(h, restart, o.t_end));
+    if (reached_quota) std::printf("reached the quota time at frame %d\n", tf_done);
+    for (int fr : {o.t_end, tf_done}) {
+        CHECK(write_particles(h, restart, fr));
+        CHECK(write_prng_state(h, restart, fr));
+        CHECK(write_module_state(h, restart, fr));
+        if (fr == tf_done) break;
+    }
+    {
+        FILE *lr = std::fopen((restart + "latest_restart").c_str(), "wb");
+        const int32_t t32 = tf_done;
+        const bool ok = lr && std::fwrite(&t32, 4, 1, lr) == 1;
+        if (lr) std::fclose(lr);
+        if (!ok) {
+            std::fprintf(stderr, "gpat_run: cannot write %slatest_restart\n", restart.c_str());
+            gpat_destroy(h);
+            return 1;
+        }
+    }
     gpat_destroy(h);
     return 0;
 }

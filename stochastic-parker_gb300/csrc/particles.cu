@@ -882,6 +882,41 @@ cudaError_t launch_track_injected(const DevParticles &P, int64_t first, int64_t 
     return cudaGetLastError();
 }
 
+namespace {
+
+// Non-negative doubles order like their bit patterns, so the maximum is an
+// integer atomicMax of the bits (p <= 0 and NaN are left out; the start is
+// +0.0).
+__global__ void __launch_bounds__(256) pmax_kernel(const DevParticles P, int64_t n,
+                                                   unsigned long long *bits) {
+    unsigned long long m = 0ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double p = P.p[i];
+        if (p > 0.0) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(p);
+            if (b > m) m = b;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+        if (v > m) m = v;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(bits, m);
+}
+
+}  // namespace
+
+cudaError_t launch_pmax(const DevParticles &P, int64_t n, unsigned long long *bits,
+                        cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 2048) blocks = 2048;
+    pmax_kernel<<<(unsigned)blocks, 256, 0, s>>>(P, n, bits);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sync_tracked(const TrackArgs &trk, cudaStream_t s) {
     if (!trk.tags || trk.n <= 0) return cudaSuccess;
     const unsigned blocks = (unsigned)((trk.n + 7) / 8);

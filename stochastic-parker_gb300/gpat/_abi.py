@@ -186,6 +186,8 @@ SIGNATURES = {
     "gpat_tracking_dims": (C.c_int, [Handle, P(C.c_int64), P(C.c_int32), P(C.c_int64)]),
     "gpat_get_tracked_particles": (C.c_int, [Handle, P(Particles)]),
     "gpat_free_particle_tracking": (C.c_int, [Handle]),
+    "gpat_load_tstamps_mhd": (C.c_int, [Handle, C.c_int, C.c_int, C.c_int, C.c_char_p]),
+    "gpat_get_pmax_global": (C.c_int, [Handle, P(C.c_double)]),
     "gpat_pbins_edges": (C.c_int, [Handle, P(d)]),
     "gpat_quick_check": (C.c_int, [Handle, P(d)]),
     "gpat_get_counters": (C.c_int, [Handle, P(Counters)]),

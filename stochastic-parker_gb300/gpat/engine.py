@@ -218,6 +218,17 @@ class Engine:
     def calc_tstamps_mhd(self, t_start: int, t_end: int):
         self._check(self.lib.gpat_calc_tstamps_mhd(self.h, t_start, t_end))
 
+    def load_tstamps_mhd(self, t_start: int, t_end: int, tmax_mhd: int, dir_mhd_data):
+        """load_tstamps_mhd: <dir_mhd_data>time_stamps.dat (varying dt_mhd)."""
+        d = str(dir_mhd_data)
+        d = d if d.endswith("/") else d + "/"
+        self._check(self.lib.gpat_load_tstamps_mhd(self.h, t_start, t_end, tmax_mhd, d.encode()))
+
+    def get_pmax_global(self) -> float:
+        v = C.c_double()
+        self._check(self.lib.gpat_get_pmax_global(self.h, C.byref(v)))
+        return v.value
+
     def field_shape(self, nvar: int = 8):
         """numpy (C order) shape of a Fortran (nvar, nxg, nyg, nzg) array."""
         return (self.nzg, self.nyg, self.nxg, nvar)

@@ -191,6 +191,91 @@ def test_driver_particle_tracking(tmp_path):
     eng.close()
 
 
+def _read_flocal(path: Path):
+    """flocalK_XXXX.dat: int32 dims {nmu, npbins, nrx, nry, nrz}, p edges,
+    mu edges, flocal and counts in Fortran order."""
+    raw = path.read_bytes()
+    dims = np.frombuffer(raw[:20], np.int32)
+    nb = int(np.prod(dims))
+    off = 20
+    pe = np.frombuffer(raw[off:off + 8 * (dims[1] + 1)], np.float64); off += 8 * (dims[1] + 1)
+    me = np.frombuffer(raw[off:off + 8 * (dims[0] + 1)], np.float64); off += 8 * (dims[0] + 1)
+    f = np.frombuffer(raw[off:off + 8 * nb], np.float64); off += 8 * nb
+    c = np.frombuffer(raw[off:off + 8 * nb], np.uint64); off += 8 * nb
+    assert off == len(raw)
+    return dims, pe, me, f, c
+
+
+@pytest.mark.gpu
+def test_driver_restart_quota_local_dist(tmp_path):
+    """A run stopped by -qh after its first frame and resumed with -rf ends
+    with the particles, f(p), local distributions (-ld), quick.dat and
+    pmax_global.dat of an uninterrupted run, bit for bit; -vdt reads the
+    frame time stamps from time_stamps.dat."""
+    w, data, out = _dataset(tmp_path)
+    conf = tmp_path / "config" / "conf.dat"
+    conf.write_text(conf.read_text() + "\n".join([
+        "dump_interval1 = 1", "pmin1 = 0.1", "pmax1 = 100.0", "npbins1 = 16", "nmu1 = 4",
+        "rx1 = 8", "ry1 = 4", "rz1 = 1",
+        "dump_interval2 = 100", "pmin2 = 0.1", "pmax2 = 10.0", "npbins2 = 8", "nmu2 = 1",
+        "rx2 = 1", "ry2 = 1", "rz2 = 1", "dump_interval3 = 100", "dump_interval4 = 100"])
+        + "\n")
+    with open(data / "time_stamps.dat", "wb") as f:
+        np.array([0, 3], np.int64).tofile(f)
+        (np.arange(4) * w.mhd_config.dt_out).tofile(f)
+    extra = ("-ld", ".true.", "-vdt", ".true.", "-tm", "3")
+    r = _run_driver(tmp_path, data, out, extra=extra)
+    assert r.returncode == 0, r.stderr
+    out2 = tmp_path / "out2"
+    out2.mkdir()
+    r = _run_driver(tmp_path, data, out2, extra=extra + ("-qh", "0.5"))
+    assert r.returncode == 0, r.stderr
+    assert "reached the quota time at frame 1" in r.stdout
+    assert np.fromfile(out2 / "restart" / "latest_restart", np.int32)[0] == 1
+    assert (out2 / "restart" / "particles_0001.dat").exists()
+    assert not (out2 / "fdists_0002.dat").exists()
+    r = _run_driver(tmp_path, data, out2, extra=extra + ("-rf", ".true."))
+    assert r.returncode == 0, r.stderr
+    assert np.fromfile(out2 / "restart" / "latest_restart", np.int32)[0] == 3
+    a = read_particle_dump(out / "restart" / "particles_0003.dat")
+    b = read_particle_dump(out2 / "restart" / "particles_0003.dat")
+    assert len(a["x"]) == len(b["x"]) > 0
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    for name in ("fdists_0003.dat", "flocal1_0003.dat", "pmax_global.dat", "quick.dat",
+                 "restart/particle_module_state_0003.dat", "restart/prng_state_0003.dat"):
+        assert (out / name).read_bytes() == (out2 / name).read_bytes(), name
+    dims, pe, me, f, c = _read_flocal(out / "flocal1_0003.dat")
+    nx, ny = w.mhd_config.nx, w.mhd_config.ny
+    assert list(dims) == [1, 16, (nx + 7) // 8, (ny + 3) // 4, 1] and c.sum() > 0 and f.sum() > 0
+    assert pe[0] == pytest.approx(0.1) and pe[-1] == pytest.approx(100.0)
+    assert list(me) == [-1.0, 1.0]
+    assert not (out / "flocal2_0003.dat").exists()
+    assert len((out / "pmax_global.dat").read_text().splitlines()) == 4
+
+
+@pytest.mark.gpu
+def test_load_tstamps_mhd(tmp_path):
+    """load_tstamps_mhd: stamps from time_stamps.dat, frames past tmax_mhd
+    continued with the last interval (injection times show them)."""
+    w, data, _ = _dataset(tmp_path)
+    with open(data / "time_stamps.dat", "wb") as f:
+        np.array([0, 5], np.int64).tofile(f)
+        np.array([0.0, 0.1, 0.25, 0.3, 0.5, 0.9]).tofile(f)
+    prm = make_params(**dict(w.params, nptl_max=1000, precision=0))
+    eng = Engine(prm, w.mhd_config, 0)
+    eng.load_tstamps_mhd(1, 4, 2, data)          # frames 1..4: 0.1, 0.25, then +0.15
+    eng.read_field_data(data / "mhd_data_0000", 0)
+    eng.calc_fields_gradients(0)
+    eng.inject_particles_spatial_uniform(200, 1e-6, 1, 1.0, 3, (0, 0, 0, 1, 0.125, 1))
+    t = eng.get_particles()["t"]
+    assert t.min() >= 0.4 - 1e-12 and t.max() < 0.55 + 1e-12 and t.max() > 0.5
+    assert eng.get_pmax_global() == pytest.approx(w.params["p0"])
+    with pytest.raises(Exception):
+        eng.load_tstamps_mhd(1, 4, 2, tmp_path / "nowhere")
+    eng.close()
+
+
 def _bump(shape, seed, lo, hi):
     """Smooth positive per-node array over the ghost-padded grid."""
     rng = np.random.default_rng(seed)
