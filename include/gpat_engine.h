@@ -336,6 +336,26 @@ int gpat_calc_local_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec
  * fescaped(npp_global, 2 * ndim) in Fortran order, column ibc = |count_flag|
  * (1 low x, 2 high x, 3 low y, 4 high y, 5 low z, 6 high z). */
 int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t *counts);
+/* The global distribution with pitch-angle bins (calc_particle_distributions,
+ * diagnostics.f90:773-779; nmu_global bins for focused transport):
+ * fglobal(nmu, npp_global) in Fortran order over pmin < p <= pmax and
+ * -1 <= mu <= 1, imu = floor((mu + 1) / dmu) + 1 with dmu = 2.0 / nmu in
+ * single precision as the reference computes it; the particle's own weight. */
+int gpat_calc_particle_distributions_mu(gpat_handle_t *h, int32_t nmu, double *fglobal,
+                                        uint64_t *counts);
+/* fescaped(nmu, npp_global, 2 * ndim) of calc_escaped_distributions
+ * (:949-957) over the escaped particles kept by mover calls with
+ * dump_escaped_dist = 1 since the last reset, column |count_flag|. */
+int gpat_calc_escaped_distributions_mu(gpat_handle_t *h, int32_t nmu, double *fescaped,
+                                       uint64_t *counts);
+/* Local escaped distributions of one parameter set (calc_escaped_
+ * distributions :958-1230) over the same escaped particles, binned like the
+ * local distributions: fx(nmu, npbins, nry, nrz, 2) for the low / high x
+ * faces, fy(nmu, npbins, nrx, nrz, 2) (ndim > 1), fz(nmu, npbins, nrx, nry,
+ * 2) (ndim 3); Fortran order; a NULL pair skips a face. */
+int gpat_calc_local_escaped_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec,
+                                         double *fx, double *fy, double *fz, uint64_t *cx,
+                                         uint64_t *cy, uint64_t *cz);
 /* escaped_ptls: the particles removed through an open boundary by
  * gpat_particle_mover calls made with dump_escaped_dist = 1 since the last
  * reset (remove_particles, particle_module.f90:5365-5403, as written by

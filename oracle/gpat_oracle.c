@@ -2612,6 +2612,133 @@ void orc_quick_check(const orc_particles *P, int64_t n, double out[4])
 /* One local distribution of calc_particle_distributions
  * (diagnostics.f90:782-878) on one rank, uniform grid: flocal(imu, ip, ix,
  * iy, iz), imu fastest; 0 < ip < npbins as in the reference. */
+/* One parameter set of the local distributions (init_local_particle_
+ * distributions, diagnostics.f90:262-290, on one rank). */
+typedef struct {
+    int ndim, spherical, nonuniform, nrx, nry, nrz, npb, nmu, rx, ry, rz;
+    double xmin, ymin, zmin, dxd, dyd, dzd, pmin_log, dp_log, dmu;
+} local_set;
+
+static local_set local_set_of(const orc_mhd_config *cfg, int ndim, int spherical, int nonuniform,
+                              double pmin, double pmax, int npbins, int nmu, int rx, int ry,
+                              int rz)
+{
+    local_set s;
+    const int nz = ndim == 3 ? cfg->nz : 1;
+    s.ndim = ndim; s.spherical = spherical; s.nonuniform = nonuniform;
+    s.nrx = (cfg->nx + rx - 1) / rx; s.nry = (cfg->ny + ry - 1) / ry; s.nrz = (nz + rz - 1) / rz;
+    s.dxd = cfg->lx / s.nrx; s.dyd = cfg->ly / s.nry; s.dzd = cfg->lz / s.nrz;
+    s.xmin = cfg->xmin; s.ymin = cfg->ymin; s.zmin = cfg->zmin;
+    s.pmin_log = log10(pmin);
+    s.dp_log = (log10(pmax) - s.pmin_log) / npbins;
+    s.dmu = (double)(2.0f / (float)nmu);   /* single precision, :273 */
+    s.npb = npbins; s.nmu = nmu; s.rx = rx; s.ry = ry; s.rz = rz;
+    return s;
+}
+
+/* The bins of particle i (:785-800) and its weight (w / r^2 [/ sin(theta)]
+ * in spherical coordinates, :765-772). */
+static void local_bin(const local_set *s, const orc_particles *P, int64_t i, int *ix, int *iy,
+                      int *iz, int *ip, int *imu, double *w)
+{
+    if (s->nonuniform) {
+        *ix = (orc_binary_search(g_grid.pos[0], g_grid.n[0], P->x[i]) - 1) / s->rx + 1;
+        *iy = (s->ndim > 1) ? (orc_binary_search(g_grid.pos[1], g_grid.n[1], P->y[i]) - 1) / s->ry + 1
+                            : (int)floor((P->y[i] - s->ymin) / s->dyd) + 1;
+        *iz = (s->ndim == 3) ? (orc_binary_search(g_grid.pos[2], g_grid.n[2], P->z[i]) - 1) / s->rz + 1
+                             : (int)floor((P->z[i] - s->zmin) / s->dzd) + 1;
+    } else {
+        *ix = (int)floor((P->x[i] - s->xmin) / s->dxd) + 1;
+        *iy = (int)floor((P->y[i] - s->ymin) / s->dyd) + 1;
+        *iz = (int)floor((P->z[i] - s->zmin) / s->dzd) + 1;
+    }
+    *ip = (int)floor((log10(P->p[i]) - s->pmin_log) / s->dp_log) + 1;
+    *imu = (int)floor((P->mu[i] + 1.0) / s->dmu) + 1;
+    double ww = P->weight[i];
+    if (s->spherical) {
+        ww = ww / (P->x[i] * P->x[i]);
+        if (s->ndim >= 2) ww = ww / sin(P->y[i]);
+    }
+    *w = ww;
+}
+
+/* Local escaped distributions (calc_escaped_distributions,
+ * diagnostics.f90:958-1230) over escaped particles: the x faces into
+ * fx(nmu, npbins, nry, nrz, 2), y into fy(nmu, npbins, nrx, nrz, 2) (ndim >
+ * 1), z into fz(nmu, npbins, nrx, nry, 2) (ndim 3); each array as counts and
+ * fixed-point (whi, wlo), zeroed here; NULL skips a face. */
+void orc_calc_local_escaped_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
+                                         int nonuniform, double pmin, double pmax, int npbins,
+                                         int nmu, int rx, int ry, int rz,
+                                         const orc_particles *P, int64_t n,
+                                         uint64_t *cx, uint64_t *hx, uint64_t *lx,
+                                         uint64_t *cy, uint64_t *hy, uint64_t *ly,
+                                         uint64_t *cz, uint64_t *hz, uint64_t *lz)
+{
+    const local_set s = local_set_of(cfg, ndim, spherical, nonuniform, pmin, pmax, npbins, nmu,
+                                     rx, ry, rz);
+    const size_t mp = (size_t)nmu * npbins;
+    const size_t sz[3] = {mp * s.nry * s.nrz * 2, mp * s.nrx * s.nrz * 2, mp * s.nrx * s.nry * 2};
+    uint64_t *C3[3] = {cx, cy, cz}, *H3[3] = {hx, hy, hz}, *L3[3] = {lx, ly, lz};
+    for (int f = 0; f < 3; ++f)
+        if (C3[f])
+            for (size_t b = 0; b < sz[f]; ++b) { C3[f][b] = 0; H3[f][b] = 0; L3[f][b] = 0; }
+    for (int64_t i = 0; i < n; ++i) {
+        int ix, iy, iz, ip, imu;
+        double w;
+        local_bin(&s, P, i, &ix, &iy, &iz, &ip, &imu, &w);
+        const int condx = ix >= 1 && ix <= s.nrx, condy = iy >= 1 && iy <= s.nry;
+        const int condz = iz >= 1 && iz <= s.nrz;
+        if (!(ip > 0 && ip < npbins && imu >= 1 && imu <= nmu)) continue;
+        const int flag = P->count_flag[i];
+        const size_t e0 = (size_t)(imu - 1) + (size_t)nmu * (size_t)(ip - 1);
+        int f = -1;
+        size_t e = 0;
+        if ((flag == -1 || flag == -2) && condy && condz) {
+            f = 0; e = e0 + mp * ((size_t)(iy - 1) + (size_t)s.nry * ((size_t)(iz - 1) + (size_t)s.nrz * (size_t)(-flag - 1)));
+        } else if ((flag == -3 || flag == -4) && ndim > 1 && condx && condz) {
+            f = 1; e = e0 + mp * ((size_t)(ix - 1) + (size_t)s.nrx * ((size_t)(iz - 1) + (size_t)s.nrz * (size_t)(-flag - 3)));
+        } else if ((flag == -5 || flag == -6) && ndim > 2 && condx && condy) {
+            f = 2; e = e0 + mp * ((size_t)(ix - 1) + (size_t)s.nrx * ((size_t)(iy - 1) + (size_t)s.nry * (size_t)(-flag - 5)));
+        }
+        if (f < 0 || !C3[f]) continue;
+        C3[f][e] += 1;
+        orc_fixed_add(&H3[f][e], &L3[f][e], w);
+    }
+}
+
+/* The global distribution with pitch-angle bins (calc_particle_distributions
+ * :773-779) or, by_face, the escaped one (calc_escaped_distributions
+ * :949-957, column |count_flag|): the particle's own weight; the bins
+ * p == pmax and mu == 1 would take (past the last) are dropped. */
+void orc_calc_distribution_mu(const orc_params *pr, const orc_particles *P, int64_t n, int nmu,
+                              int by_face, int nfaces, uint64_t *counts, uint64_t *whi,
+                              uint64_t *wlo)
+{
+    const int npp = pr->npp_global;
+    const double pmin_log = log10(pr->pmin);
+    const double dp_log = (log10(pr->pmax) - pmin_log) / npp;
+    const double dmu = (double)(2.0f / (float)nmu);   /* :206 */
+    const size_t nb = (size_t)nmu * npp * (by_face ? nfaces : 1);
+    for (size_t b = 0; b < nb; ++b) { counts[b] = 0; whi[b] = 0; wlo[b] = 0; }
+    for (int64_t i = 0; i < n; ++i) {
+        const double p = P->p[i], mu = P->mu[i];
+        if (!(p > pr->pmin && p <= pr->pmax && mu >= -1.0 && mu <= 1.0)) continue;
+        const int ip = (int)floor((log10(p) - pmin_log) / dp_log) + 1;
+        const int imu = (int)floor((mu + 1.0) / dmu) + 1;
+        if (ip < 1 || ip > npp || imu < 1 || imu > nmu) continue;
+        int face = 0;
+        if (by_face) {
+            const int flag = P->count_flag[i];
+            if (flag >= 0 || -flag > nfaces) continue;
+            face = -flag - 1;
+        }
+        const size_t e = (size_t)(imu - 1) + (size_t)nmu * ((size_t)(ip - 1) + (size_t)npp * face);
+        counts[e] += 1;
+        orc_fixed_add(&whi[e], &wlo[e], P->weight[i]);
+    }
+}
+
 void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
                                  int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,

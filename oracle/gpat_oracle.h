@@ -198,6 +198,16 @@ int64_t orc_tracking_dropped(void);
 int64_t orc_nsteps_tracking_max(double dt_min_rel, int nsteps_interval);
 /* sync_tracked_particles on one rank. */
 void orc_sync_tracked(void);
+void orc_calc_local_escaped_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
+                                         int nonuniform, double pmin, double pmax, int npbins,
+                                         int nmu, int rx, int ry, int rz,
+                                         const orc_particles *ptl, int64_t n,
+                                         uint64_t *cx, uint64_t *hx, uint64_t *lx,
+                                         uint64_t *cy, uint64_t *hy, uint64_t *ly,
+                                         uint64_t *cz, uint64_t *hz, uint64_t *lz);
+void orc_calc_distribution_mu(const orc_params *pr, const orc_particles *ptl, int64_t n, int nmu,
+                              int by_face, int nfaces, uint64_t *counts, uint64_t *whi,
+                              uint64_t *wlo);
 void orc_calc_local_distribution(const orc_mhd_config *cfg, int ndim, int spherical,
                                  int nonuniform, double pmin, double pmax,
                                  int npbins, int nmu, int rx, int ry, int rz,

@@ -141,6 +141,11 @@ def load() -> C.CDLL:
                                                     C.c_int, C.c_int, C.c_int, C.c_int,
                                                     P(OrcParticles), i64, P(u64), P(u64), P(u64),
                                                     P(d)]
+        lib.orc_calc_local_escaped_distribution.argtypes = (
+            [P(OrcMhdConfig), C.c_int, C.c_int, C.c_int, d, d] + [C.c_int] * 5 +
+            [P(OrcParticles), i64] + [P(u64)] * 9)
+        lib.orc_calc_distribution_mu.argtypes = [P(OrcParams), P(OrcParticles), i64, C.c_int,
+                                                 C.c_int, C.c_int, P(u64), P(u64), P(u64)]
         lib.orc_set_grid_positions.argtypes = [P(d), P(d), P(d), C.c_int, C.c_int, C.c_int]
         lib.orc_set_acc_surface.argtypes = [C.c_int] * 6 + [P(d)] * 4 + [C.c_int] * 3
         lib.orc_set_tracking.argtypes = [P(i32), C.c_int, C.c_int, i64, P(OrcParticles)]
@@ -468,3 +473,37 @@ def local_distribution(cfg: OrcMhdConfig, ndim: int, parts: Particles, pmin: flo
                                        whi.ctypes.data_as(P(u64)), wlo.ctypes.data_as(P(u64)),
                                        f.ctypes.data_as(P(d)))
     return f, counts
+
+
+def _unpack(counts, whi, wlo):
+    return np.array([fixed_to_double(int(h), int(l)) for h, l in zip(whi, wlo)]), counts
+
+
+def distribution_mu(params: OrcParams, parts: Particles, nmu: int, by_face: bool = False,
+                    nfaces: int = 1):
+    """fglobal(nmu, npp_global) (or, by_face, fescaped(nmu, npp, nfaces))
+    flattened in Fortran order: (weights, counts)."""
+    nb = nmu * params.npp_global * (nfaces if by_face else 1)
+    c, h, l = (np.zeros(nb, np.uint64) for _ in range(3))
+    load().orc_calc_distribution_mu(C.byref(params), C.byref(parts.c), parts.n, nmu,
+                                    int(by_face), nfaces, c.ctypes.data_as(P(u64)),
+                                    h.ctypes.data_as(P(u64)), l.ctypes.data_as(P(u64)))
+    return _unpack(c, h, l)
+
+
+def local_escaped_distribution(cfg: OrcMhdConfig, ndim: int, parts: Particles, pmin: float,
+                               pmax: float, npbins: int, nmu: int = 1, rx: int = 1, ry: int = 1,
+                               rz: int = 1, spherical: bool = False, nonuniform: bool = False):
+    """[(weights, counts)] for the x, y and z faces (None beyond ndim), each
+    flattened in Fortran order (nmu, npbins, n1, n2, 2)."""
+    nz = cfg.nz if ndim == 3 else 1
+    nrx, nry, nrz = (cfg.nx + rx - 1) // rx, (cfg.ny + ry - 1) // ry, (nz + rz - 1) // rz
+    mp = nmu * npbins
+    sizes = [mp * nry * nrz * 2, mp * nrx * nrz * 2, mp * nrx * nry * 2]
+    arrs = [[np.zeros(sz, np.uint64) for _ in range(3)] if k < ndim else [None] * 3
+            for k, sz in enumerate(sizes)]
+    ptrs = [None if a is None else a.ctypes.data_as(P(u64)) for trio in arrs for a in trio]
+    load().orc_calc_local_escaped_distribution(C.byref(cfg), ndim, int(spherical),
+                                               int(nonuniform), pmin, pmax, npbins, nmu, rx, ry,
+                                               rz, C.byref(parts.c), parts.n, *ptrs)
+    return [None if trio[0] is None else _unpack(*trio) for trio in arrs]

@@ -1348,6 +1348,92 @@ int gpat_calc_escaped_distributions(gpat_handle_t *h, double *fescaped, uint64_t
     return GPAT_OK;
 }
 
+extern "C++" {
+// Runs a (count, whi, wlo) binning into a temporary device buffer and
+// unpacks it into counts / weights (either may be NULL).
+template <class Launch>
+static int run_bins(gpat_handle_t *h, size_t nbins, Launch launch, double *f, uint64_t *c) {
+    if (nbins > ((size_t)1 << 31)) return fail(h, GPAT_ERR_ARG, "distribution too large");
+    CK(cudaSetDevice(h->device));
+    unsigned long long *bins = nullptr;
+    CK(cudaMallocAsync((void **)&bins, sizeof(unsigned long long) * 3 * nbins, h->stream));
+    cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, h->stream);
+    if (e == cudaSuccess) e = launch(bins);
+    std::vector<unsigned long long> b(3 * nbins);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.data(), bins, sizeof(unsigned long long) * b.size(),
+                            cudaMemcpyDeviceToHost, h->stream);
+    cudaFreeAsync(bins, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(h, GPAT_ERR_CUDA, cudaGetErrorString(e));
+    for (size_t i = 0; i < nbins; ++i) {
+        if (c) c[i] = b[3 * i];
+        if (f) f[i] = fixed_to_double(b[3 * i + 1], b[3 * i + 2]);
+    }
+    return GPAT_OK;
+}
+
+static MuDistArgs mu_args(const gpat_handle_t *h, int nmu, int by_face) {
+    MuDistArgs a;
+    a.pmin = h->prm.pmin;
+    a.pmax = h->prm.pmax;
+    a.pmin_log = std::log10(h->prm.pmin);
+    a.dp_log = (std::log10(h->prm.pmax) - a.pmin_log) / h->prm.npp_global;
+    a.dmu = (double)(2.0f / (float)nmu);   // dmu = 2.0 / nmu_global (diagnostics.f90:206)
+    a.npp = h->prm.npp_global;
+    a.nmu = nmu;
+    a.by_face = by_face;
+    return a;
+}
+}  // extern "C++"
+
+int gpat_calc_particle_distributions_mu(gpat_handle_t *h, int32_t nmu, double *fglobal,
+                                        uint64_t *counts) {
+    if (!h) return GPAT_ERR_ARG;
+    if (nmu < 1) return fail(h, GPAT_ERR_ARG, "nmu must be >= 1");
+    const MuDistArgs a = mu_args(h, nmu, 0);
+    const size_t nbins = (size_t)nmu * (size_t)a.npp;
+    return run_bins(h, nbins, [&](unsigned long long *bins) {
+        return launch_mu_dist(h->P[h->cur], h->n, a, bins, nbins, h->stream);
+    }, fglobal, counts);
+}
+
+int gpat_calc_escaped_distributions_mu(gpat_handle_t *h, int32_t nmu, double *fescaped,
+                                       uint64_t *counts) {
+    if (!h) return GPAT_ERR_ARG;
+    if (nmu < 1) return fail(h, GPAT_ERR_ARG, "nmu must be >= 1");
+    const MuDistArgs a = mu_args(h, nmu, 1);
+    const size_t nbins = (size_t)nmu * (size_t)a.npp * 2 * (size_t)h->prm.ndim;
+    return run_bins(h, nbins, [&](unsigned long long *bins) {
+        return launch_mu_dist(h->E, h->ne, a, bins, nbins, h->stream);
+    }, fescaped, counts);
+}
+
+int gpat_calc_local_escaped_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec,
+                                         double *fx, double *fy, double *fz, uint64_t *cx,
+                                         uint64_t *cy, uint64_t *cz) {
+    if (!h) return GPAT_ERR_ARG;
+    LocalDistArgs a;
+    int rc = local_args(h, spec, a);
+    if (rc) return rc;
+    const size_t mp = (size_t)a.nmu * (size_t)a.npb;
+    const size_t nx = mp * a.nry * a.nrz * 2, ny = mp * a.nrx * a.nrz * 2;
+    const size_t nz = mp * a.nrx * a.nry * 2;
+    const size_t sizes[3] = {nx, h->prm.ndim > 1 ? ny : 0, h->prm.ndim > 2 ? nz : 0};
+    double *f[3] = {fx, fy, fz};
+    uint64_t *c[3] = {cx, cy, cz};
+    for (int face = 0; face < 3; ++face) {
+        if (!sizes[face] || (!f[face] && !c[face])) continue;
+        rc = run_bins(h, sizes[face], [&](unsigned long long *bins) {
+            unsigned long long *b[3] = {nullptr, nullptr, nullptr};
+            b[face] = bins;
+            return launch_local_escaped(h->E, h->ne, a, b[0], b[1], b[2], h->stream);
+        }, f[face], c[face]);
+        if (rc) return rc;
+    }
+    return GPAT_OK;
+}
+
 int gpat_get_pmax_global(gpat_handle_t *h, double *pmax) {
     if (!h || !pmax) return GPAT_ERR_ARG;
     CK(cudaSetDevice(h->device));

@@ -287,6 +287,18 @@ struct LocalDistArgs {
 // bins: (count, whi, wlo) per flocal element, zeroed here.
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
                               unsigned long long *bins, size_t nbins, cudaStream_t s);
+// Local escaped distributions into the per-face (count, whi, wlo) arrays
+// fx, fy, fz (zeroed by the caller; nullptr skips a face).
+cudaError_t launch_local_escaped(const DevParticles &P, int64_t n, const LocalDistArgs &a,
+                                 unsigned long long *fx, unsigned long long *fy,
+                                 unsigned long long *fz, cudaStream_t s);
+// Global (or, with by_face, escaped) distribution with pitch-angle bins.
+struct MuDistArgs {
+    double pmin, pmax, pmin_log, dp_log, dmu;
+    int npp, nmu, by_face;
+};
+cudaError_t launch_mu_dist(const DevParticles &P, int64_t n, const MuDistArgs &a,
+                           unsigned long long *bins, size_t nbins, cudaStream_t s);
 // Splitting: children appended after n in parent order, at most cap - n.
 // With tracking on, tracked parents follow split_particle's tracking branch.
 cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap,

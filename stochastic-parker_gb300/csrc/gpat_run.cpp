@@ -657,6 +657,74 @@ int main(int argc, char **argv) {
         }
         return GPAT_OK;
     };
+    // With focused transport the global and escaped distributions carry
+    // nmu_global pitch-angle bins (read_diagnostics_params :2105-2111):
+    // fglobal_mu_XXXX.dat / fescaped_mu_XXXX.dat hold int32 nmu, npp, nface
+    // (1 for fglobal), the nmu + 1 mu edges, the npp + 1 p edges, the
+    // weights (nmu, npp, nface) in Fortran order and the uint64 counts.
+    int nmu_global = 1;
+    if (o.focused_transport) {
+        double v = -1.0;
+        if (gpat_get_variable(conf.c_str(), "nmu_global", &v) == GPAT_OK && v >= 1.0)
+            nmu_global = (int)v;
+    }
+    auto write_mu = [&](const char *stem, int frame, bool escaped) -> int {
+        const int nface = escaped ? 2 * o.ndim_field : 1;
+        const size_t nb = (size_t)nmu_global * npp * nface;
+        std::vector<double> fm(nb);
+        std::vector<uint64_t> cm(nb);
+        int rc = escaped ? gpat_calc_escaped_distributions_mu(h, nmu_global, fm.data(), cm.data())
+                         : gpat_calc_particle_distributions_mu(h, nmu_global, fm.data(), cm.data());
+        if (rc) return rc;
+        const double dmu = (double)(2.0f / (float)nmu_global);
+        std::vector<double> me(nmu_global + 1);
+        for (int i = 0; i <= nmu_global; ++i) me[i] = -1.0 + i * dmu;
+        char name[64];
+        std::snprintf(name, sizeof name, "%s_%04d.dat", stem, frame);
+        FILE *f = std::fopen((o.diagnostics_directory + name).c_str(), "wb");
+        if (!f) return GPAT_ERR_IO;
+        const int32_t hdr[3] = {nmu_global, npp, nface};
+        bool ok = std::fwrite(hdr, 4, 3, f) == 3 &&
+                  std::fwrite(me.data(), 8, me.size(), f) == me.size() &&
+                  std::fwrite(edges.data(), 8, edges.size(), f) == edges.size() &&
+                  std::fwrite(fm.data(), 8, nb, f) == nb && std::fwrite(cm.data(), 8, nb, f) == nb;
+        ok = (std::fclose(f) == 0) && ok;
+        return ok ? GPAT_OK : GPAT_ERR_IO;
+    };
+    // save_local_escaped_distributions (diagnostics.f90:1536-1600):
+    // fescapedK_XXXX.dat holds int32 {nmu, npbins, nrx, nry, nrz}, then for
+    // the x faces (and y from 2D, z in 3D) the weights fescapedK_x(nmu,
+    // npbins, nry, nrz, 2) etc. in Fortran order followed by their uint64
+    // counts.
+    auto write_local_escaped = [&](int frame) -> int {
+        for (const LocalSet &ls : local_sets) {
+            int32_t dims[5];
+            int rc = gpat_local_distribution_dims(h, &ls.spec, dims);
+            if (rc) return rc;
+            const size_t mp = (size_t)dims[0] * dims[1];
+            const size_t sz[3] = {mp * dims[3] * dims[4] * 2, mp * dims[2] * dims[4] * 2,
+                                  mp * dims[2] * dims[3] * 2};
+            std::vector<double> fv[3];
+            std::vector<uint64_t> cv[3];
+            for (int k = 0; k < o.ndim_field; ++k) { fv[k].resize(sz[k]); cv[k].resize(sz[k]); }
+            auto dp = [&](int k) { return k < o.ndim_field ? fv[k].data() : nullptr; };
+            auto up = [&](int k) { return k < o.ndim_field ? cv[k].data() : nullptr; };
+            rc = gpat_calc_local_escaped_distribution(h, &ls.spec, dp(0), dp(1), dp(2), up(0),
+                                                      up(1), up(2));
+            if (rc) return rc;
+            char name[64];
+            std::snprintf(name, sizeof name, "fescaped%d_%04d.dat", ls.k, frame);
+            FILE *f = std::fopen((o.diagnostics_directory + name).c_str(), "wb");
+            if (!f) return GPAT_ERR_IO;
+            bool ok = std::fwrite(dims, 4, 5, f) == 5;
+            for (int k = 0; k < o.ndim_field; ++k)
+                ok = ok && std::fwrite(fv[k].data(), 8, sz[k], f) == sz[k] &&
+                     std::fwrite(cv[k].data(), 8, sz[k], f) == sz[k];
+            ok = (std::fclose(f) == 0) && ok;
+            if (!ok) return GPAT_ERR_IO;
+        }
+        return GPAT_OK;
+    };
     // get_pmax_global (diagnostics.f90:1691-1721): pmax_global.dat, one
     // line per frame, created at the initial diagnostics
     auto write_pmax = [&](bool create) -> int {
@@ -690,6 +758,10 @@ int main(int argc, char **argv) {
         std::fwrite(fglobal.data(), 8, fglobal.size(), f);
         std::fwrite(counts.data(), 8, counts.size(), f);
         std::fclose(f);
+        if (o.focused_transport) {
+            const int rc = write_mu("fglobal_mu", frame, false);
+            if (rc) return rc;
+        }
         return write_local(frame);
     };
 
@@ -711,7 +783,11 @@ int main(int argc, char **argv) {
         std::fwrite(fe.data(), 8, fe.size(), f);
         std::fwrite(ce.data(), 8, ce.size(), f);
         std::fclose(f);
-        return GPAT_OK;
+        if (o.focused_transport) {
+            rc = write_mu("fescaped_mu", frame, true);
+            if (rc) return rc;
+        }
+        return write_local_escaped(frame);
     };
 
     int tf_done = o.t_end;

@@ -938,13 +938,17 @@ cudaError_t launch_histogram(const DevParticles &P, int64_t n, int npp, double p
     return cudaGetLastError();
 }
 
-// Local distributions (calc_particle_distributions, diagnostics.f90:782-878):
-// one (count, weight hi, lo) triple per flocal(imu, ip, ix, iy, iz) element.
-__global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, int64_t n,
-                                                         const LocalDistArgs a,
-                                                         unsigned long long *bins) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// The bins of particle i for one local-distribution parameter set
+// (diagnostics.f90:785-800): spatial ix, iy, iz, momentum ip, pitch imu and
+// the weight (over r^2 sin(theta) in spherical coordinates, :765-772).
+struct LocalBin {
+    int ix, iy, iz, ip, imu;
+    double w;
+};
+
+__device__ __forceinline__ LocalBin local_bin(const DevParticles &P, int64_t i,
+                                              const LocalDistArgs &a) {
+    LocalBin b;
     const double p = P.p[i], mu = P.mu[i];
     int ix, iy, iz;
     if (a.nonuniform) {
@@ -960,24 +964,103 @@ __global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, i
         iy = (int)floor((P.y[i] - a.ymin) / a.dyd) + 1;
         iz = (int)floor((P.z[i] - a.zmin) / a.dzd) + 1;
     }
-    const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
-    const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
-    if (ix < 1 || ix > a.nrx || iy < 1 || iy > a.nry || iz < 1 || iz > a.nrz) return;
-    if (!(ip > 0 && ip < a.npb) || imu < 1 || imu > a.nmu) return;
-    const size_t e = (size_t)(imu - 1) +
-                     (size_t)a.nmu * ((size_t)(ip - 1) +
-                                      (size_t)a.npb * ((size_t)(ix - 1) +
-                                                       (size_t)a.nrx * ((size_t)(iy - 1) +
-                                                                        (size_t)a.nry * (iz - 1))));
-    unsigned long long *b = bins + 3 * e;
-    atomicAdd(b, 1ull);
+    b.ix = ix; b.iy = iy; b.iz = iz;
+    b.ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
+    b.imu = (int)floor((mu + 1.0) / a.dmu) + 1;
     double w = P.weight[i];
     if (a.spherical) {
         // F = f p^2 r^2 (sin theta from 2D on), diagnostics.f90:765-772
         w = w / (P.x[i] * P.x[i]);
         if (a.ndim >= 2) w = w / sin(P.y[i]);
     }
+    b.w = w;
+    return b;
+}
+
+__device__ __forceinline__ void bin_add(unsigned long long *bins, size_t e, double w) {
+    unsigned long long *b = bins + 3 * e;
+    atomicAdd(b, 1ull);
     atomic_add_fixed(b + 1, b + 2, w);
+}
+
+// Local distributions (calc_particle_distributions, diagnostics.f90:782-878):
+// one (count, weight hi, lo) triple per flocal element.
+__global__ void __launch_bounds__(256) local_dist_kernel(const DevParticles P, int64_t n,
+                                                         const LocalDistArgs a,
+                                                         unsigned long long *bins) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const LocalBin b = local_bin(P, i, a);
+    if (b.ix < 1 || b.ix > a.nrx || b.iy < 1 || b.iy > a.nry || b.iz < 1 || b.iz > a.nrz) return;
+    if (!(b.ip > 0 && b.ip < a.npb) || b.imu < 1 || b.imu > a.nmu) return;
+    const size_t e = (size_t)(b.imu - 1) +
+                     (size_t)a.nmu * ((size_t)(b.ip - 1) +
+                                      (size_t)a.npb * ((size_t)(b.ix - 1) +
+                                                       (size_t)a.nrx * ((size_t)(b.iy - 1) +
+                                                                        (size_t)a.nry * (b.iz - 1))));
+    bin_add(bins, e, b.w);
+}
+
+// Local escaped distributions (calc_escaped_distributions, diagnostics.f90:
+// 958-1230) over escaped particles: the x faces into fx(nmu, npb, nry, nrz,
+// 2), the y faces into fy(nmu, npb, nrx, nrz, 2) and the z faces into
+// fz(nmu, npb, nrx, nry, 2), low face first; a face whose array the
+// reference does not allocate (y below 2D, z below 3D) is skipped.
+__global__ void __launch_bounds__(256) local_escaped_kernel(const DevParticles P, int64_t n,
+                                                            const LocalDistArgs a,
+                                                            unsigned long long *fx,
+                                                            unsigned long long *fy,
+                                                            unsigned long long *fz) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const LocalBin b = local_bin(P, i, a);
+    if (!(b.ip > 0 && b.ip < a.npb) || b.imu < 1 || b.imu > a.nmu) return;
+    const bool cx = b.ix >= 1 && b.ix <= a.nrx, cy = b.iy >= 1 && b.iy <= a.nry;
+    const bool cz = b.iz >= 1 && b.iz <= a.nrz;
+    const int flag = P.count_flag[i];
+    const size_t mp = (size_t)(b.imu - 1) + (size_t)a.nmu * (size_t)(b.ip - 1);
+    const size_t nmp = (size_t)a.nmu * (size_t)a.npb;
+    if ((flag == -1 || flag == -2) && cy && cz && fx) {
+        const size_t side = (size_t)(-flag - 1);
+        bin_add(fx, mp + nmp * ((size_t)(b.iy - 1) + (size_t)a.nry * ((size_t)(b.iz - 1) +
+                                                                       (size_t)a.nrz * side)),
+                b.w);
+    } else if ((flag == -3 || flag == -4) && a.ndim > 1 && cx && cz && fy) {
+        const size_t side = (size_t)(-flag - 3);
+        bin_add(fy, mp + nmp * ((size_t)(b.ix - 1) + (size_t)a.nrx * ((size_t)(b.iz - 1) +
+                                                                       (size_t)a.nrz * side)),
+                b.w);
+    } else if ((flag == -5 || flag == -6) && a.ndim > 2 && cx && cy && fz) {
+        const size_t side = (size_t)(-flag - 5);
+        bin_add(fz, mp + nmp * ((size_t)(b.ix - 1) + (size_t)a.nrx * ((size_t)(b.iy - 1) +
+                                                                       (size_t)a.nry * side)),
+                b.w);
+    }
+}
+
+// Global distribution with pitch-angle bins (calc_particle_distributions
+// :773-779, calc_escaped_distributions :949-957): fglobal(nmu, npp) or, with
+// by_face, fescaped(nmu, npp, |count_flag|); the particle's own weight.
+// p == pmax and mu == 1 index past the last bin in the reference and are
+// dropped.
+__global__ void __launch_bounds__(256) mu_dist_kernel(const DevParticles P, int64_t n,
+                                                      const MuDistArgs a,
+                                                      unsigned long long *bins) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p = P.p[i], mu = P.mu[i];
+    if (!(p > a.pmin && p <= a.pmax && mu >= -1.0 && mu <= 1.0)) return;
+    const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
+    const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
+    if (ip < 1 || ip > a.npp || imu < 1 || imu > a.nmu) return;
+    size_t face = 0;
+    if (a.by_face) {
+        const int flag = P.count_flag[i];
+        if (flag >= 0 || flag < -6) return;
+        face = (size_t)(-flag - 1);
+    }
+    bin_add(bins, (size_t)(imu - 1) + (size_t)a.nmu * ((size_t)(ip - 1) + (size_t)a.npp * face),
+            P.weight[i]);
 }
 
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
@@ -985,6 +1068,22 @@ cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistA
     cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, s);
     if (e != cudaSuccess || n <= 0) return e;
     local_dist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local_escaped(const DevParticles &P, int64_t n, const LocalDistArgs &a,
+                                 unsigned long long *fx, unsigned long long *fy,
+                                 unsigned long long *fz, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    local_escaped_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, fx, fy, fz);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mu_dist(const DevParticles &P, int64_t n, const MuDistArgs &a,
+                           unsigned long long *bins, size_t nbins, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, s);
+    if (e != cudaSuccess || n <= 0) return e;
+    mu_dist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, bins);
     return cudaGetLastError();
 }
 

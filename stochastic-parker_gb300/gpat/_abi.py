@@ -188,6 +188,12 @@ SIGNATURES = {
     "gpat_free_particle_tracking": (C.c_int, [Handle]),
     "gpat_load_tstamps_mhd": (C.c_int, [Handle, C.c_int, C.c_int, C.c_int, C.c_char_p]),
     "gpat_get_pmax_global": (C.c_int, [Handle, P(C.c_double)]),
+    "gpat_calc_particle_distributions_mu": (C.c_int, [Handle, C.c_int32, P(C.c_double),
+                                                      P(C.c_uint64)]),
+    "gpat_calc_escaped_distributions_mu": (C.c_int, [Handle, C.c_int32, P(C.c_double),
+                                                     P(C.c_uint64)]),
+    "gpat_calc_local_escaped_distribution": (C.c_int, [Handle, P(LocalDist)] +
+                                             [P(C.c_double)] * 3 + [P(C.c_uint64)] * 3),
     "gpat_pbins_edges": (C.c_int, [Handle, P(d)]),
     "gpat_quick_check": (C.c_int, [Handle, P(d)]),
     "gpat_get_counters": (C.c_int, [Handle, P(Counters)]),

@@ -379,6 +379,45 @@ class Engine:
         self._check(self.lib.gpat_get_particles(self.h, C.byref(s), len(ps), C.byref(got)))
         return ps if out is None else ParticleSet({k: v[:n] for k, v in ps.arrays.items()})
 
+    def particle_distributions_mu(self, nmu: int):
+        """fglobal(nmu, npp_global) and counts, as numpy (npp_global, nmu)."""
+        npp = self.params.npp_global
+        f = np.zeros((npp, nmu), np.float64)
+        c = np.zeros((npp, nmu), np.uint64)
+        self._check(self.lib.gpat_calc_particle_distributions_mu(
+            self.h, nmu, f.ctypes.data_as(C.POINTER(C.c_double)),
+            c.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return f, c
+
+    def escaped_distributions_mu(self, nmu: int):
+        """fescaped(nmu, npp_global, 2 ndim) as numpy (2 ndim, npp_global, nmu)."""
+        npp, nf = self.params.npp_global, 2 * self.params.ndim
+        f = np.zeros((nf, npp, nmu), np.float64)
+        c = np.zeros((nf, npp, nmu), np.uint64)
+        self._check(self.lib.gpat_calc_escaped_distributions_mu(
+            self.h, nmu, f.ctypes.data_as(C.POINTER(C.c_double)),
+            c.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return f, c
+
+    def local_escaped_distribution(self, pmin, pmax, npbins, nmu=1, rx=1, ry=1, rz=1):
+        """(fx, fy, fz), (cx, cy, cz): numpy (2, nrz, nry, npbins, nmu),
+        (2, nrz, nrx, npbins, nmu) and (2, nry, nrx, npbins, nmu), i.e.
+        Fortran fx(nmu, npbins, nry, nrz, 2) etc.; faces beyond ndim are
+        None."""
+        spec = _abi.LocalDist(pmin, pmax, npbins, nmu, rx, ry, rz, 0)
+        dims = (C.c_int32 * 5)()
+        self._check(self.lib.gpat_local_distribution_dims(self.h, C.byref(spec), dims))
+        nmu_, npb, nrx, nry, nrz = list(dims)
+        shapes = [(2, nrz, nry, npb, nmu_), (2, nrz, nrx, npb, nmu_), (2, nry, nrx, npb, nmu_)]
+        nd = self.params.ndim
+        f = [np.zeros(s, np.float64) if k < nd else None for k, s in enumerate(shapes)]
+        c = [np.zeros(s, np.uint64) if k < nd else None for k, s in enumerate(shapes)]
+        dp = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+        up = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint64))
+        self._check(self.lib.gpat_calc_local_escaped_distribution(
+            self.h, C.byref(spec), dp(f[0]), dp(f[1]), dp(f[2]), up(c[0]), up(c[1]), up(c[2])))
+        return tuple(f), tuple(c)
+
     def get_escaped_particles(self) -> ParticleSet:
         """escaped_ptls: particles removed through an open boundary by mover
         calls with dump_escaped_dist since the last reset_escaped_particles."""

@@ -30,7 +30,7 @@ def _dataset(tmp_path: Path):
             "kpara0", "kret", "dt_min_rel", "dt_max_rel")
     vals = dict(b0=1.0, **p)
     lines = ["!< conf.dat written by the test"] + [f"{k} = {vals[k]!r}" for k in keys]
-    lines += ["acc_region_flag = 0", "npp_global = 64", "nmu_global = 1",
+    lines += ["acc_region_flag = 0", "npp_global = 64", "nmu_global = 4",
               f"pbcx = {p['pbcx']}", f"pbcy = {p['pbcy']}", f"pbcz = {p['pbcz']}"]
     (tmp_path / "config" / "conf.dat").write_text("\n".join(lines) + "\n")
     return w, data, out
@@ -98,6 +98,7 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
         if tf == 3:
             fe, ce = eng.calc_escaped_distributions()
             esc = eng.get_escaped_particles()
+            fem, cem = eng.escaped_distributions_mu(4)
         eng.reset_escaped_particles()
     # escaped distributions and particles of the last frame (-ded, -de)
     raw = (out / "fescaped_0003.dat").read_bytes()
@@ -113,6 +114,19 @@ def test_driver_matches_python_sequence(tmp_path, ft, nlgc):
     f, c = eng.calc_particle_distributions()
     assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv)
     np.testing.assert_allclose(edges, eng.pbins_edges(), rtol=0)
+    # focused transport: nmu_global = 4 pitch-angle bins (Parker keeps 1)
+    assert (out / "fglobal_mu_0003.dat").exists() == ft
+    if ft:
+        for name, (fr, cr) in (("fglobal_mu_0003.dat", eng.particle_distributions_mu(4)),
+                               ("fescaped_mu_0003.dat", (fem, cem))):
+            raw = (out / name).read_bytes()
+            nmu, npp_, nface = np.frombuffer(raw[:12], np.int32)
+            nb = int(nmu * npp_ * nface)
+            off = 12 + 8 * (nmu + 1) + 8 * (npp_ + 1)
+            assert nmu == 4 and npp_ == 64
+            assert np.array_equal(np.frombuffer(raw[off:off + 8 * nb], np.float64), fr.ravel())
+            assert np.array_equal(np.frombuffer(raw[off + 8 * nb:], np.uint64), cr.ravel())
+            assert cr.sum() > 0 or name.startswith("fescaped")   # frame 3 may have no escapes
     q = eng.quick_check()
     last = quick[-1].split()
     assert int(last[0]) == 3 and float(last[1]) == q["nptl_current"]
@@ -251,6 +265,11 @@ def test_driver_restart_quota_local_dist(tmp_path):
     assert pe[0] == pytest.approx(0.1) and pe[-1] == pytest.approx(100.0)
     assert list(me) == [-1.0, 1.0]
     assert not (out / "flocal2_0003.dat").exists()
+    # local escaped distributions of set 1 (-ld with -ded): x and y faces
+    raw = (out / "fescaped1_0003.dat").read_bytes()
+    assert np.array_equal(np.frombuffer(raw[:20], np.int32), dims)
+    assert len(raw) == 20 + 16 * 2 * 16 * (dims[3] + dims[2])
+    assert raw == (out2 / "fescaped1_0003.dat").read_bytes()
     assert len((out / "pmax_global.dat").read_text().splitlines()) == 4
 
 
