@@ -63,7 +63,7 @@ def make_workload(args, precision, seed=None, nframes=16, scale=None):
                                       seed=2 if seed is None else seed, nframes=nframes)
 
 
-def parse_args():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -81,7 +81,7 @@ def parse_args():
                     help="pushes between re-binnings (0: engine default, <0: once per call)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 sample and the f(p) tail-error check")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def l2_read_gbs(torch, dev) -> float:
@@ -172,7 +172,9 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl"
+        # NCCL between GPU ranks; GPAT_DIST_BACKEND=gloo runs the same
+        # rank logic on CPU processes
+        backend = os.environ.get("GPAT_DIST_BACKEND", "nccl")
         dist.init_process_group(backend=backend)
     return world, rank, local
 
