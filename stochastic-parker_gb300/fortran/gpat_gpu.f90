@@ -12,7 +12,7 @@ module gpat_gpu
     use, intrinsic :: iso_c_binding
     implicit none
     private
-    public gpat_mhd_config_t, gpat_params_t
+    public gpat_mhd_config_t, gpat_params_t, gpat_local_dist_t
     public gpu_init, gpu_free, gpu_read_particle_params, gpu_calc_tstamps_mhd, &
         gpu_set_tstamps, gpu_read_field_data, gpu_calc_fields_gradients, &
         gpu_copy_fields, gpu_inject_particles_spatial_uniform, &
@@ -24,7 +24,12 @@ module gpat_gpu
         gpu_inject_particles_at_large_db2, gpu_read_magnetic_fluctuation, &
         gpu_read_grid_positions, gpu_init_acc_surface, gpu_read_acc_surface, &
         gpu_read_correlation_length, &
-        gpu_calc_escaped_distributions, gpu_reset_escaped_particles
+        gpu_calc_escaped_distributions, gpu_reset_escaped_particles, &
+        gpu_init_particle_tracking, gpu_read_particle_tracking, gpu_tracking_dims, &
+        gpu_get_tracked_particles, gpu_free_particle_tracking, &
+        gpu_load_tstamps_mhd, gpu_get_pmax_global, gpu_global_distribution_mu, &
+        gpu_escaped_distribution_mu, gpu_local_distribution, gpu_local_escaped_distribution, &
+        gpu_get_escaped_ptls, gpu_get_counters, gpu_set_counters, gpat_counters_t
 
     integer(c_int), parameter :: GPAT_OK = 0
 
@@ -58,6 +63,13 @@ module gpat_gpu
         type(c_ptr) :: origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted
         type(c_ptr) :: rng_ctr
     end type gpat_particles_t
+
+    !< One parameter set of the local distributions (pminK, pmaxK, npbinsK,
+    !< nmuK, rxK, ryK, rzK of read_diagnostics_params).
+    type, bind(c) :: gpat_local_dist_t
+        real(c_double) :: pmin, pmax
+        integer(c_int32_t) :: npbins, nmu, rx, ry, rz, reserved
+    end type gpat_local_dist_t
 
     type, bind(c) :: gpat_counters_t
         integer(c_int64_t) :: nptl_current, nptl_split, nptl_escaped, tag_max
@@ -277,6 +289,62 @@ module gpat_gpu
         integer(c_int) function c_free_tracking(handle) bind(c, name="gpat_free_particle_tracking")
             import :: c_int, c_ptr
             type(c_ptr), value :: handle
+        end function
+        integer(c_int) function c_load_tstamps(handle, t_start, t_end, tmax_mhd, dirname) &
+                bind(c, name="gpat_load_tstamps_mhd")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: handle
+            integer(c_int), value :: t_start, t_end, tmax_mhd
+            character(kind=c_char), dimension(*), intent(in) :: dirname
+        end function
+        integer(c_int) function c_pmax(handle, pmax) bind(c, name="gpat_get_pmax_global")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: handle
+            real(c_double), intent(out) :: pmax
+        end function
+        integer(c_int) function c_distributions_mu(handle, nmu, f, counts) &
+                bind(c, name="gpat_calc_particle_distributions_mu")
+            import :: c_int, c_ptr, c_int32_t, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int32_t), value :: nmu
+            real(c_double), dimension(*), intent(out) :: f
+            integer(c_int64_t), dimension(*), intent(out) :: counts
+        end function
+        integer(c_int) function c_escaped_mu(handle, nmu, f, counts) &
+                bind(c, name="gpat_calc_escaped_distributions_mu")
+            import :: c_int, c_ptr, c_int32_t, c_double, c_int64_t
+            type(c_ptr), value :: handle
+            integer(c_int32_t), value :: nmu
+            real(c_double), dimension(*), intent(out) :: f
+            integer(c_int64_t), dimension(*), intent(out) :: counts
+        end function
+        integer(c_int) function c_local_dist(handle, spec, flocal, counts) &
+                bind(c, name="gpat_calc_local_distribution")
+            import :: c_int, c_ptr, c_double, c_int64_t, gpat_local_dist_t
+            type(c_ptr), value :: handle
+            type(gpat_local_dist_t), intent(in) :: spec
+            real(c_double), dimension(*), intent(out) :: flocal
+            integer(c_int64_t), dimension(*), intent(out) :: counts
+        end function
+        integer(c_int) function c_local_escaped(handle, spec, fx, fy, fz, cx, cy, cz) &
+                bind(c, name="gpat_calc_local_escaped_distribution")
+            import :: c_int, c_ptr, gpat_local_dist_t
+            type(c_ptr), value :: handle
+            type(gpat_local_dist_t), intent(in) :: spec
+            type(c_ptr), value :: fx, fy, fz, cx, cy, cz
+        end function
+        integer(c_int) function c_get_escaped(handle, dst, capacity, n) &
+                bind(c, name="gpat_get_escaped_particles")
+            import :: c_int, c_ptr, c_int64_t, gpat_particles_t
+            type(c_ptr), value :: handle
+            type(gpat_particles_t), intent(inout) :: dst
+            integer(c_int64_t), value :: capacity
+            integer(c_int64_t), intent(out) :: n
+        end function
+        integer(c_int) function c_set_counters(handle, in) bind(c, name="gpat_set_counters")
+            import :: c_int, c_ptr, gpat_counters_t
+            type(c_ptr), value :: handle
+            type(gpat_counters_t), intent(in) :: in
         end function
     end interface
 
@@ -631,10 +699,12 @@ module gpat_gpu
     !< nptl_tracking) field by field
     subroutine gpu_get_tracked_particles(x, y, z, p, v, mu, weight, t, dt, split_times, &
             count_flag, origin, nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted)
-        real(c_double), dimension(:, :), intent(out), target :: x, y, z, p, v, mu, weight, t, dt
-        integer(c_int8_t), dimension(:, :), intent(out), target :: split_times, count_flag
-        integer(c_int32_t), dimension(:, :), intent(out), target :: origin, nsteps_tracked, &
-            nsteps_pushed, tag_injected, tag_splitted
+        real(c_double), dimension(:, :), intent(out), target, contiguous :: x, y, z, p, v, mu, &
+            weight, t, dt
+        integer(c_int8_t), dimension(:, :), intent(out), target, contiguous :: split_times, &
+            count_flag
+        integer(c_int32_t), dimension(:, :), intent(out), target, contiguous :: origin, &
+            nsteps_tracked, nsteps_pushed, tag_injected, tag_splitted
         type(gpat_particles_t) :: s
         s%x = c_loc(x); s%y = c_loc(y); s%z = c_loc(z); s%p = c_loc(p); s%v = c_loc(v)
         s%mu = c_loc(mu); s%weight = c_loc(weight); s%t = c_loc(t); s%dt = c_loc(dt)
@@ -644,6 +714,106 @@ module gpat_gpu
         s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_null_ptr
         call check(c_get_tracked(h, s), "dump_tracked_particles")
     end subroutine gpu_get_tracked_particles
+
+    !< load_tstamps_mhd (mhd_config.f90:221-255) for varying_dt_mhd
+    subroutine gpu_load_tstamps_mhd(t_start, t_end, tmax_mhd, dir_mhd_data)
+        integer, intent(in) :: t_start, t_end, tmax_mhd
+        character(*), intent(in) :: dir_mhd_data
+        call check(c_load_tstamps(h, int(t_start, c_int), int(t_end, c_int), &
+            int(tmax_mhd, c_int), trim(dir_mhd_data)//c_null_char), "load_tstamps_mhd")
+    end subroutine gpu_load_tstamps_mhd
+
+    !< get_pmax_global (diagnostics.f90:1691-1721) without the file
+    subroutine gpu_get_pmax_global(pmax)
+        real(c_double), intent(out) :: pmax
+        call check(c_pmax(h, pmax), "get_pmax_global")
+    end subroutine gpu_get_pmax_global
+
+    !< fglobal(nmu_global, npp_global) of calc_particle_distributions
+    !< (diagnostics.f90:773-779)
+    subroutine gpu_global_distribution_mu(fglobal, counts)
+        real(c_double), dimension(:, :), intent(out) :: fglobal
+        integer(c_int64_t), dimension(:, :), intent(out) :: counts
+        call check(c_distributions_mu(h, int(size(fglobal, 1), c_int32_t), fglobal, counts), &
+            "calc_particle_distributions")
+    end subroutine gpu_global_distribution_mu
+
+    !< fescaped(nmu_global, npp_global, 2 ndim) of calc_escaped_distributions
+    !< (:949-957) over the escaped particles kept since the last reset
+    subroutine gpu_escaped_distribution_mu(fescaped, counts)
+        real(c_double), dimension(:, :, :), intent(out) :: fescaped
+        integer(c_int64_t), dimension(:, :, :), intent(out) :: counts
+        call check(c_escaped_mu(h, int(size(fescaped, 1), c_int32_t), fescaped, counts), &
+            "calc_escaped_distributions")
+    end subroutine gpu_escaped_distribution_mu
+
+    !< flocalK(nmu, npbins, nrx, nry, nrz) of calc_particle_distributions
+    !< (:782-878) for one parameter set
+    subroutine gpu_local_distribution(spec, flocal, counts)
+        type(gpat_local_dist_t), intent(in) :: spec
+        real(c_double), dimension(:, :, :, :, :), intent(out) :: flocal
+        integer(c_int64_t), dimension(:, :, :, :, :), intent(out) :: counts
+        call check(c_local_dist(h, spec, flocal, counts), "calc_particle_distributions")
+    end subroutine gpu_local_distribution
+
+    !< fescapedK_x / _y / _z of calc_escaped_distributions (:958-1230); the
+    !< y and z arrays are left out below 2D and 3D
+    subroutine gpu_local_escaped_distribution(spec, fx, cx, fy, cy, fz, cz)
+        type(gpat_local_dist_t), intent(in) :: spec
+        real(c_double), dimension(:, :, :, :, :), intent(out), target, contiguous :: fx
+        integer(c_int64_t), dimension(:, :, :, :, :), intent(out), target, contiguous :: cx
+        real(c_double), dimension(:, :, :, :, :), intent(out), target, contiguous, &
+            optional :: fy, fz
+        integer(c_int64_t), dimension(:, :, :, :, :), intent(out), target, contiguous, &
+            optional :: cy, cz
+        type(c_ptr) :: pfy, pfz, pcy, pcz
+        pfy = c_null_ptr; pfz = c_null_ptr; pcy = c_null_ptr; pcz = c_null_ptr
+        if (present(fy)) pfy = c_loc(fy)
+        if (present(cy)) pcy = c_loc(cy)
+        if (present(fz)) pfz = c_loc(fz)
+        if (present(cz)) pcz = c_loc(cz)
+        call check(c_local_escaped(h, spec, c_loc(fx), pfy, pfz, c_loc(cx), pcy, pcz), &
+            "calc_escaped_distributions")
+    end subroutine gpu_local_escaped_distribution
+
+    !< escaped_ptls (dump_escaped_particles, diagnostics.f90:1896-1978) into
+    !< arrays of length capacity; n on exit
+    subroutine gpu_get_escaped_ptls(capacity, n, x, y, z, p, v, mu, weight, t, dt, &
+            split_times, count_flag, origin, nsteps_tracked, nsteps_pushed, tag_injected, &
+            tag_splitted, rng_ctr)
+        integer, intent(in) :: capacity
+        integer, intent(out) :: n
+        real(c_double), dimension(capacity), intent(out), target :: x, y, z, p, v, mu, weight, &
+            t, dt
+        integer(c_int8_t), dimension(capacity), intent(out), target :: split_times, count_flag
+        integer(c_int32_t), dimension(capacity), intent(out), target :: origin, nsteps_tracked, &
+            nsteps_pushed, tag_injected, tag_splitted, rng_ctr
+        type(gpat_particles_t) :: s
+        integer(c_int64_t) :: got
+        integer(c_int) :: rc
+        s%x = c_loc(x); s%y = c_loc(y); s%z = c_loc(z); s%p = c_loc(p); s%v = c_loc(v)
+        s%mu = c_loc(mu); s%weight = c_loc(weight); s%t = c_loc(t); s%dt = c_loc(dt)
+        s%split_times = c_loc(split_times); s%count_flag = c_loc(count_flag)
+        s%origin = c_loc(origin); s%nsteps_tracked = c_loc(nsteps_tracked)
+        s%nsteps_pushed = c_loc(nsteps_pushed); s%tag_injected = c_loc(tag_injected)
+        s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_loc(rng_ctr)
+        rc = c_get_escaped(h, s, int(capacity, c_int64_t), got)
+        n = int(got)
+        call check(rc, "get_escaped_particles")
+    end subroutine gpu_get_escaped_ptls
+
+    !< Module state for save_particle_module_state / read_particle_module_state
+    !< (particle_module.f90:5532-5660): nptl_split, tag_max and the exact leak
+    !< sums travel in gpat_counters_t
+    subroutine gpu_get_counters(c)
+        type(gpat_counters_t), intent(out) :: c
+        call check(c_get_counters(h, c), "get_counters")
+    end subroutine gpu_get_counters
+
+    subroutine gpu_set_counters(c)
+        type(gpat_counters_t), intent(in) :: c
+        call check(c_set_counters(h, c), "set_counters")
+    end subroutine gpu_set_counters
 
     !< free_particle_tracking (:5905-5911)
     subroutine gpu_free_particle_tracking
