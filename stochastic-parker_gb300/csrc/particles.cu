@@ -800,7 +800,8 @@ cudaError_t launch_split_particles(const DevParticles &P, int64_t n, int64_t cap
                                    double split_ratio, double pmin_split, double p0, double pmax,
                                    void *scratch, DevCounters *cnt, cudaStream_t s,
                                    const TrackArgs *trk) {
-    if (n <= 0) return cudaSuccess;
+    // nkept is read back as the number of split candidates
+    if (n <= 0) return cudaMemsetAsync(&cnt->nkept, 0, sizeof(unsigned long long), s);
     const int64_t ntiles = (n + kTile - 1) / kTile;
     long long *counts = static_cast<long long *>(scratch);
     long long *offsets = counts + ntiles;
