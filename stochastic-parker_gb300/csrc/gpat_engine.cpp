@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <new>
 #include <vector>
 
 #include "gpat_internal.h"
@@ -1314,9 +1315,14 @@ int gpat_calc_local_distribution(gpat_handle_t *h, const gpat_local_dist_t *spec
     if (nbins > ((size_t)1 << 31)) return fail(h, GPAT_ERR_ARG, "local distribution too large");
     CK(cudaSetDevice(h->device));
     unsigned long long *bins = nullptr;
+    std::vector<unsigned long long> b;
+    try {
+        b.resize(3 * nbins);
+    } catch (const std::bad_alloc &) {
+        return fail(h, GPAT_ERR_OOM, "local distribution does not fit in host memory");
+    }
     CK(cudaMallocAsync((void **)&bins, sizeof(unsigned long long) * 3 * nbins, h->stream));
     cudaError_t e = launch_local_dist(h->P[h->cur], h->n, a, bins, nbins, h->stream);
-    std::vector<unsigned long long> b(3 * nbins);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b.data(), bins, sizeof(unsigned long long) * b.size(),
                             cudaMemcpyDeviceToHost, h->stream);
@@ -1356,10 +1362,15 @@ static int run_bins(gpat_handle_t *h, size_t nbins, Launch launch, double *f, ui
     if (nbins > ((size_t)1 << 31)) return fail(h, GPAT_ERR_ARG, "distribution too large");
     CK(cudaSetDevice(h->device));
     unsigned long long *bins = nullptr;
+    std::vector<unsigned long long> b;
+    try {
+        b.resize(3 * nbins);
+    } catch (const std::bad_alloc &) {
+        return fail(h, GPAT_ERR_OOM, "distribution does not fit in host memory");
+    }
     CK(cudaMallocAsync((void **)&bins, sizeof(unsigned long long) * 3 * nbins, h->stream));
     cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, h->stream);
     if (e == cudaSuccess) e = launch(bins);
-    std::vector<unsigned long long> b(3 * nbins);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b.data(), bins, sizeof(unsigned long long) * b.size(),
                             cudaMemcpyDeviceToHost, h->stream);
@@ -1465,6 +1476,8 @@ int gpat_init_particle_tracking(gpat_handle_t *h, const int32_t *tags, int32_t n
     if (!h || !tags) return GPAT_ERR_ARG;
     if (nrows < 2 || nptl_tracking < 1 || nsteps_interval < 1)
         return fail(h, GPAT_ERR_ARG, "tags_tracking needs >= 2 rows, >= 1 column, nsteps_interval >= 1");
+    if (nrows > 2 + 127)   // split_times is an int8
+        return fail(h, GPAT_ERR_ARG, "tags_tracking has more split levels than split_times holds");
     if (h->prm.precision != GPAT_PREC_FP64)
         return fail(h, GPAT_ERR_UNSUPPORTED, "particle tracking runs in FP64 precision");
     // nsteps_tracking_max = ceiling((1.0 / dt_min_rel) / nsteps_interval) + 1
@@ -1475,6 +1488,8 @@ int gpat_init_particle_tracking(gpat_handle_t *h, const int32_t *tags, int32_t n
     if (rc) return rc;
     const int64_t nsteps_max = (int64_t)steps + 1;
     const int64_t nrec = nsteps_max * (int64_t)nptl_tracking;
+    if (nrec > ((int64_t)1 << 36))   // beyond any device, and particle_bytes stays exact
+        return fail(h, GPAT_ERR_OOM, "particles_tracked does not fit on the device");
     if (cudaMalloc(&h->tmem, particle_bytes(nrec)) != cudaSuccess) {
         cudaGetLastError();
         h->tmem = nullptr;
@@ -1506,11 +1521,18 @@ int gpat_read_particle_tracking(gpat_handle_t *h, const char *particle_tags_file
     FILE *f = std::fopen(particle_tags_file, "rb");
     if (!f) return fail(h, GPAT_ERR_IO, std::string("cannot open ") + particle_tags_file);
     int32_t dims[2] = {0, 0};
-    if (std::fread(dims, sizeof(int32_t), 2, f) != 2 || dims[0] < 2 || dims[1] < 1) {
+    if (std::fread(dims, sizeof(int32_t), 2, f) != 2 || dims[0] < 2 || dims[0] > 2 + 127 ||
+        dims[1] < 1) {
         std::fclose(f);
         return fail(h, GPAT_ERR_IO, "tags file: bad dimensions");
     }
-    std::vector<int32_t> tags((size_t)dims[0] * (size_t)dims[1]);
+    std::vector<int32_t> tags;
+    try {
+        tags.resize((size_t)dims[0] * (size_t)dims[1]);
+    } catch (const std::bad_alloc &) {
+        std::fclose(f);
+        return fail(h, GPAT_ERR_OOM, "tags file: table does not fit in host memory");
+    }
     const size_t got = std::fread(tags.data(), sizeof(int32_t), tags.size(), f);
     std::fclose(f);
     if (got != tags.size()) return fail(h, GPAT_ERR_IO, "tags file: short read");

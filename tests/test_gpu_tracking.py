@@ -111,9 +111,19 @@ def test_tracking_entry_points_check_arguments():
         eng.init_particle_tracking(np.zeros((4, 1), np.int32), 10)   # < 2 rows
     with pytest.raises(GPATError):
         eng.get_tracked_particles()                          # not initialised
+    with pytest.raises(GPATError):
+        eng.init_particle_tracking(np.zeros((1, 200), np.int32), 10)  # > int8 split levels
     eng.init_particle_tracking(_table(), 10)
     nsteps, ntrk, dropped = eng.tracking_dims()
     assert nsteps == int(np.ceil((1.0 / params["dt_min_rel"]) / 10)) + 1 and dropped == 0
     rec = eng.get_tracked_particles()
     assert rec["x"].shape == (ntrk, nsteps) and not rec["tag_splitted"].any()
+    eng.close()
+    # records for 1e9 steps x 32 particles (~3 TB) fail cleanly
+    params, cfg = shock_case(precision=0, dt_min_rel=1e-9)
+    eng = Engine(make_params(**params), cfg, 0)
+    with pytest.raises(GPATError):
+        eng.init_particle_tracking(_table(), 1)
+    eng.init_particle_tracking(_table()[:2], 10 ** 6)   # still usable afterwards
+    assert eng.tracking_dims()[1] == 2
     eng.close()
