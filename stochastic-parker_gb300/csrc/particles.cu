@@ -1044,25 +1044,74 @@ __global__ void __launch_bounds__(256) local_escaped_kernel(const DevParticles P
 // by_face, fescaped(nmu, npp, |count_flag|); the particle's own weight.
 // p == pmax and mu == 1 index past the last bin in the reference and are
 // dropped.
+__device__ __forceinline__ int64_t mu_bin(const DevParticles &P, int64_t i, const MuDistArgs &a) {
+    const double p = P.p[i], mu = P.mu[i];
+    if (!(p > a.pmin && p <= a.pmax && mu >= -1.0 && mu <= 1.0)) return -1;
+    const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
+    const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
+    if (ip < 1 || ip > a.npp || imu < 1 || imu > a.nmu) return -1;
+    int64_t face = 0;
+    if (a.by_face) {
+        const int flag = P.count_flag[i];
+        if (flag >= 0 || flag < -6) return -1;
+        face = -flag - 1;
+    }
+    return (int64_t)(imu - 1) + (int64_t)a.nmu * ((int64_t)(ip - 1) + (int64_t)a.npp * face);
+}
+
 __global__ void __launch_bounds__(256) mu_dist_kernel(const DevParticles P, int64_t n,
                                                       const MuDistArgs a,
                                                       unsigned long long *bins) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double p = P.p[i], mu = P.mu[i];
-    if (!(p > a.pmin && p <= a.pmax && mu >= -1.0 && mu <= 1.0)) return;
-    const int ip = (int)floor((log10(p) - a.pmin_log) / a.dp_log) + 1;
-    const int imu = (int)floor((mu + 1.0) / a.dmu) + 1;
-    if (ip < 1 || ip > a.npp || imu < 1 || imu > a.nmu) return;
-    size_t face = 0;
-    if (a.by_face) {
-        const int flag = P.count_flag[i];
-        if (flag >= 0 || flag < -6) return;
-        face = (size_t)(-flag - 1);
-    }
-    bin_add(bins, (size_t)(imu - 1) + (size_t)a.nmu * ((size_t)(ip - 1) + (size_t)a.npp * face),
-            P.weight[i]);
+    const int64_t b = mu_bin(P, i, a);
+    if (b >= 0) bin_add(bins, (size_t)b, P.weight[i]);
 }
+
+// The same with block-private bins in shared memory (nbins triples) and
+// lanes of a warp that share a bin merged first, as histogram_kernel does.
+__global__ void __launch_bounds__(256) mu_dist_shared_kernel(const DevParticles P, int64_t n,
+                                                             const MuDistArgs a, int nbins,
+                                                             unsigned long long *bins) {
+    extern __shared__ unsigned long long sh[];
+    for (int b = threadIdx.x; b < 3 * nbins; b += blockDim.x) sh[b] = 0ull;
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t iters = (n + stride - 1) / stride;
+    for (int64_t it = 0; it < iters; ++it) {
+        const int64_t i = start + it * stride;
+        int bin = -1;
+        unsigned long long wh = 0, wl = 0;
+        if (i < n) {
+            bin = (int)mu_bin(P, i, a);
+            if (bin >= 0) fixed_split(P.weight[i], wh, wl);
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, bin);
+        const int leader = __ffs(grp) - 1;
+        unsigned long long sh_h = 0, sh_l = 0;
+        unsigned m = grp;
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const unsigned long long oh = __shfl_sync(grp, wh, src);
+            const unsigned long long ol = __shfl_sync(grp, wl, src);
+            add_u128(sh_h, sh_l, oh, ol);
+        }
+        if (bin >= 0 && (int)(threadIdx.x & 31) == leader) {
+            atomicAdd(&sh[3 * bin], (unsigned long long)__popc(grp));
+            atomic_add_u128(&sh[3 * bin + 1], &sh[3 * bin + 2], sh_h, sh_l);
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+        if (sh[3 * b]) atomicAdd(&bins[3 * b], sh[3 * b]);
+        atomic_add_u128(&bins[3 * b + 1], &bins[3 * b + 2], sh[3 * b + 1], sh[3 * b + 2]);
+    }
+}
+
+// Largest table the shared-memory path holds: 8192 triples, 192 KiB.
+constexpr int kMuSharedBins = 8192;
 
 cudaError_t launch_local_dist(const DevParticles &P, int64_t n, const LocalDistArgs &a,
                               unsigned long long *bins, size_t nbins, cudaStream_t s) {
@@ -1084,7 +1133,18 @@ cudaError_t launch_mu_dist(const DevParticles &P, int64_t n, const MuDistArgs &a
                            unsigned long long *bins, size_t nbins, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(unsigned long long) * 3 * nbins, s);
     if (e != cudaSuccess || n <= 0) return e;
-    mu_dist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, bins);
+    if (nbins <= (size_t)kMuSharedBins) {
+        const size_t shmem = sizeof(unsigned long long) * 3 * nbins;
+        // per device, so set on every call (it is cheap)
+        e = cudaFuncSetAttribute(mu_dist_shared_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(unsigned long long) * 3 * kMuSharedBins));
+        if (e != cudaSuccess) return e;
+        int64_t blocks = (n + 255) / 256;
+        if (blocks > 1024) blocks = 1024;
+        mu_dist_shared_kernel<<<(unsigned)blocks, 256, shmem, s>>>(P, n, a, (int)nbins, bins);
+    } else {
+        mu_dist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, n, a, bins);
+    }
     return cudaGetLastError();
 }
 
