@@ -258,6 +258,20 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
  * cells lower in x, y (and z in 3D): the reference assigns the whole
  * ghost-padded gradient array to a node-sized allocatable, which is
  * re-allocated with lower bound 1. */
+/* locate_shock_xpos (mhd_data_parallel.f90:1988-2006) on frame 1: for each
+ * row of the ghost-padded grid (nyg * nzg rows, y fastest) the first 1-based
+ * x index of the largest |dvx/dx|; shock_ix may be NULL. */
+int gpat_locate_shock_xpos(gpat_handle_t *h, int32_t *shock_ix);
+/* inject_particles_at_shock (particle_module.f90:542-633): nptl particles
+ * with y (and z) uniform over the box, at the shock of locate_shock_xpos
+ * interpolated linearly between the rows either side, x = xmin + (index - 3)
+ * dx, t = the frame's time stamp; momenta, mu and tags as
+ * gpat_inject_particles_at_x.  The reference's interpolation weights, row
+ * offset and index-to-x mapping are not usable as written (rz from dpy,
+ * weights that do not sum to 1, uninitialised sums, frame 2 read at rt = 0);
+ * this is the interpolation they describe.  Uniform Cartesian grids. */
+int gpat_inject_particles_at_shock(gpat_handle_t *h, int64_t nptl, double dt, int dist_flag,
+                                   double particle_v0, int ct_mhd, double power_index);
 int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin,
                            const double part_box[6], int64_t *ncells);
 /* inject_particles_at_large_*: nptl_inject = nptl when inject_same_nptl

@@ -2558,11 +2558,86 @@ int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, con
 /* Injection on the plane x = xpos at the frame start, following the draw
  * order of inject_particles_at_shock (particle_module.f90:542-633) with the
  * shock locator replaced by the given x. */
+/* locate_shock_xpos (mhd_data_parallel.f90:1988-2006) on a 32-variable
+ * frame: per row (y fastest over nyg * nzg) maxloc of |dvx/dx| along x,
+ * 1-based, first occurrence. */
+void orc_locate_shock_xpos(const float *full, int nxg, int nyg, int nzg, int32_t *S)
+{
+    for (int r = 0; r < nyg * nzg; ++r) {
+        float best = -1.0f;
+        int at = 0;
+        for (int ix = 0; ix < nxg; ++ix) {
+            const float v = fabsf(full[8 + 32 * ((size_t)ix + (size_t)nxg * (size_t)r)]);
+            if (v > best) { best = v; at = ix; }
+        }
+        S[r] = at + 1;
+    }
+}
+
+/* The x of inject_particles_at_shock (particle_module.f90:568-588) with
+ * interp_shock_location (mhd_data_parallel.f90:2017-2046) as described:
+ * linear between the rows either side of y (and z), x = xmin + (index - 3) dx. */
+static double shock_x(const orc_params *pr, const orc_mhd_config *cfg, const int32_t *S, int nyg,
+                      int nzg, double y, double z)
+{
+    double sx;
+    if (pr->ndim == 1) {
+        sx = (double)S[0];
+    } else {
+        const double dpy = (y - cfg->ymin) / cfg->dy;
+        const int jy = (int)floor(dpy);
+        const double ry = dpy - (double)jy;
+        int r0 = jy + 2, r1 = jy + 3;
+        r0 = r0 < 0 ? 0 : (r0 > nyg - 1 ? nyg - 1 : r0);
+        r1 = r1 < 0 ? 0 : (r1 > nyg - 1 ? nyg - 1 : r1);
+        if (pr->ndim == 2) {
+            sx = (1.0 - ry) * (double)S[r0] + ry * (double)S[r1];
+        } else {
+            const double dpz = (z - cfg->zmin) / cfg->dz;
+            const int jz = (int)floor(dpz);
+            const double rz = dpz - (double)jz;
+            int k0 = jz + 2, k1 = jz + 3;
+            k0 = k0 < 0 ? 0 : (k0 > nzg - 1 ? nzg - 1 : k0);
+            k1 = k1 < 0 ? 0 : (k1 > nzg - 1 ? nzg - 1 : k1);
+            sx = (1.0 - ry) * (1.0 - rz) * (double)S[r0 + nyg * k0] +
+                 ry * (1.0 - rz) * (double)S[r1 + nyg * k0] +
+                 (1.0 - ry) * rz * (double)S[r0 + nyg * k1] + ry * rz * (double)S[r1 + nyg * k1];
+        }
+    }
+    return cfg->xmin + (sx - 3.0) * cfg->dx;
+}
+
+static int64_t inject_plane(const orc_params *pr, const orc_mhd_config *cfg, orc_particles *P,
+                            int64_t n, int64_t nptl_max, int64_t nptl, double xpos,
+                            const int32_t *S, int nyg, int nzg, double dt, int dist_flag,
+                            double particle_v0, double t_frame, double power_index,
+                            orc_counters *cnt);
+
+int64_t orc_inject_at_shock(const orc_params *pr, const orc_mhd_config *cfg, const int32_t *S,
+                            int nyg, int nzg, orc_particles *P, int64_t n, int64_t nptl_max,
+                            int64_t nptl, double dt, int dist_flag, double particle_v0,
+                            double t_frame, double power_index, orc_counters *cnt)
+{
+    return inject_plane(pr, cfg, P, n, nptl_max, nptl, 0.0, S, nyg, nzg, dt, dist_flag,
+                        particle_v0, t_frame, power_index, cnt);
+}
+
 int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
                         orc_particles *P, int64_t n, int64_t nptl_max,
                         int64_t nptl, double xpos, double dt, int dist_flag,
                         double particle_v0, double t_frame, double power_index,
                         orc_counters *cnt)
+{
+    return inject_plane(pr, cfg, P, n, nptl_max, nptl, xpos, NULL, 0, 0, dt, dist_flag,
+                        particle_v0, t_frame, power_index, cnt);
+}
+
+/* The shared body: a plane at xpos, or the shock when S is given. */
+static int64_t inject_plane(const orc_params *pr, const orc_mhd_config *cfg, orc_particles *P,
+                            int64_t n, int64_t nptl_max, int64_t nptl, double xpos,
+                            const int32_t *S, int nyg, int nzg, double dt, int dist_flag,
+                            double particle_v0, double t_frame, double power_index,
+                            orc_counters *cnt)
 {
     const double ymin = cfg->ymin, ymax = cfg->ymin + (double)cfg->ny * cfg->dy;
     double zmin = cfg->zmin, zmax = cfg->zmax;
@@ -2588,7 +2663,8 @@ int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
         }
         const double v = particle_v0 * p / pr->p0;
         const double mu = (double)0.99f * (2.0 * inj_u01(&s) - 1.0);
-        set_new_particle(P, n, xpos, y, z, p, v, mu, t_frame, dt, tag);
+        const double x = S ? shock_x(pr, cfg, S, nyg, nzg, y, z) : xpos;
+        set_new_particle(P, n, x, y, z, p, v, mu, t_frame, dt, tag);
         trk_injected(P, n);
         n += 1;
     }

@@ -168,6 +168,11 @@ int64_t orc_inject_at_large(const orc_params *pr, const orc_mhd_config *cfg, con
                             double dt, int dist_flag, double particle_v0, double t_frame,
                             double dt_mhd, int quantity, double qmin,
                             const double part_box[6], double power_index, orc_counters *cnt);
+void orc_locate_shock_xpos(const float *full, int nxg, int nyg, int nzg, int32_t *S);
+int64_t orc_inject_at_shock(const orc_params *pr, const orc_mhd_config *cfg, const int32_t *S,
+                            int nyg, int nzg, orc_particles *ptl, int64_t n, int64_t nptl_max,
+                            int64_t nptl, double dt, int dist_flag, double particle_v0,
+                            double t_frame, double power_index, orc_counters *cnt);
 int64_t orc_inject_at_x(const orc_params *pr, const orc_mhd_config *cfg,
                         orc_particles *ptl, int64_t n, int64_t nptl_max,
                         int64_t nptl, double xpos, double dt, int dist_flag,

@@ -125,6 +125,11 @@ def load() -> C.CDLL:
         lib.orc_inject_at_x.restype = i64
         lib.orc_inject_at_x.argtypes = [P(OrcParams), P(OrcMhdConfig), P(OrcParticles), i64, i64,
                                         i64, d, d, C.c_int, d, d, d, P(OrcCounters)]
+        lib.orc_locate_shock_xpos.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, P(i32)]
+        lib.orc_inject_at_shock.restype = i64
+        lib.orc_inject_at_shock.argtypes = [P(OrcParams), P(OrcMhdConfig), P(i32), C.c_int,
+                                            C.c_int, P(OrcParticles), i64, i64, i64, d, C.c_int,
+                                            d, d, d, P(OrcCounters)]
         lib.orc_count_cells_large.restype = i64
         lib.orc_count_cells_large.argtypes = [P(OrcParams), P(OrcMhdConfig), P(C.c_float),
                                               P(C.c_float), C.c_int, d, P(d)]
@@ -352,6 +357,27 @@ def inject_at_x(params: OrcParams, cfg: OrcMhdConfig, parts: Particles, nptl: in
     parts.n = lib.orc_inject_at_x(C.byref(params), C.byref(cfg), C.byref(parts.c), parts.n,
                                   parts.cap, nptl, xpos, dt, dist_flag, particle_v0, t_frame,
                                   power_index, C.byref(counters))
+
+
+def locate_shock_xpos(full: np.ndarray) -> np.ndarray:
+    """Per (y, z) row of a (nzg, nyg, nxg, 32) frame the 1-based x index of
+    the largest |dvx/dx|, shaped (nzg, nyg)."""
+    nzg, nyg, nxg, _ = full.shape
+    S = np.zeros((nzg, nyg), np.int32)
+    f = np.ascontiguousarray(full, np.float32)
+    load().orc_locate_shock_xpos(f.ctypes.data_as(P(C.c_float)), nxg, nyg, nzg,
+                                 S.ctypes.data_as(P(i32)))
+    return S
+
+
+def inject_at_shock(params: OrcParams, cfg: OrcMhdConfig, full: np.ndarray, parts: Particles,
+                    nptl: int, dt: float, dist_flag: int, particle_v0: float, t_frame: float,
+                    counters: OrcCounters, power_index: float = 7.0):
+    S = locate_shock_xpos(full)
+    parts.n = load().orc_inject_at_shock(C.byref(params), C.byref(cfg), S.ctypes.data_as(P(i32)),
+                                         S.shape[1], S.shape[0], C.byref(parts.c), parts.n,
+                                         parts.cap, nptl, dt, dist_flag, particle_v0, t_frame,
+                                         power_index, C.byref(counters))
 
 
 def inject_spatial_uniform(params: OrcParams, parts: Particles, nptl: int, dt: float,

@@ -67,6 +67,7 @@ struct gpat_handle {
     // tags_tracking(trk_rows, trk_n) and particles_tracked(trk_steps, trk_n)
     int32_t *dtags = nullptr;
     void *tmem = nullptr;
+    int32_t *dshock = nullptr;   // shock x index per (y, z) row (locate_shock_xpos)
     DevParticles T{};
     int trk_rows = 0, trk_n = 0;
     int64_t trk_steps = 0;
@@ -611,6 +612,7 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->emem) cudaFree(h->emem);
     if (h->tmem) cudaFree(h->tmem);
     if (h->dtags) cudaFree(h->dtags);
+    if (h->dshock) cudaFree(h->dshock);
     if (h->scratch) cudaFree(h->scratch);
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->dcnt) cudaFree(h->dcnt);
@@ -962,6 +964,21 @@ static LargeArgs large_args(const gpat_handle_t *h, int quantity, double qmin) {
     return g;
 }
 
+// locate_shock_xpos on frame 1 into h->dshock (nyg * nzg rows).
+static int locate_shock(gpat_handle_t *h) {
+    if (!h->rec_ready[0]) return fail(h, GPAT_ERR_STATE, "fields and their gradients are not set");
+    const int nrows = h->nyg * h->nzg;
+    if (!h->dshock) {
+        if (cudaMalloc(&h->dshock, sizeof(int32_t) * (size_t)nrows) != cudaSuccess) {
+            cudaGetLastError();
+            h->dshock = nullptr;
+            return fail(h, GPAT_ERR_OOM, "shock table");
+        }
+    }
+    CK(launch_locate_shock(h->full[0], h->nxg, nrows, h->dshock, h->stream));
+    return GPAT_OK;
+}
+
 static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, double dt,
                          int dist_flag, double particle_v0, int ct_mhd, const double *box,
                          double power_index, const LargeArgs *lg = nullptr) {
@@ -991,6 +1008,12 @@ static int inject_common(gpat_handle_t *h, int mode, int64_t nptl, double xpos, 
         a.box[5] = (h->prm.ndim == 3) ? c.zmin + (double)c.nz * c.dz : c.zmax;
     }
     a.xpos = xpos;
+    if (mode == 3) {
+        a.shock_ix = h->dshock;
+        a.nyg = h->nyg; a.nzg = h->nzg;
+        a.gxmin = c.xmin; a.gymin = c.ymin; a.gzmin = c.zmin;
+        a.dx = c.dx; a.dy = c.dy; a.dz = c.dz;
+    }
     a.dt = dt;
     a.particle_v0 = particle_v0;
     a.t_frame = h->tstamps[ct_mhd - 1];
@@ -1023,6 +1046,29 @@ int gpat_inject_particles_at_x(gpat_handle_t *h, int64_t nptl, double xpos, doub
                                double particle_v0, int ct_mhd, double power_index) {
     if (!h) return GPAT_ERR_ARG;
     return inject_common(h, 1, nptl, xpos, dt, dist_flag, particle_v0, ct_mhd, nullptr, power_index);
+}
+
+int gpat_locate_shock_xpos(gpat_handle_t *h, int32_t *shock_ix) {
+    if (!h) return GPAT_ERR_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = locate_shock(h);
+    if (rc) return rc;
+    if (shock_ix)
+        CK(cudaMemcpyAsync(shock_ix, h->dshock, sizeof(int32_t) * (size_t)(h->nyg * h->nzg),
+                           cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GPAT_OK;
+}
+
+int gpat_inject_particles_at_shock(gpat_handle_t *h, int64_t nptl, double dt, int dist_flag,
+                                   double particle_v0, int ct_mhd, double power_index) {
+    if (!h) return GPAT_ERR_ARG;
+    if (h->prm.spherical_coord || h->prm.nonuniform_grid)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "shock injection needs a uniform Cartesian grid");
+    CK(cudaSetDevice(h->device));
+    const int rc = locate_shock(h);
+    if (rc) return rc;
+    return inject_common(h, 3, nptl, 0.0, dt, dist_flag, particle_v0, ct_mhd, nullptr, power_index);
 }
 
 int gpat_count_cells_large(gpat_handle_t *h, int quantity, double qmin, const double part_box[6],

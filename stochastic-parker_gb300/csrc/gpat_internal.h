@@ -238,16 +238,26 @@ struct InjectArgs {
     DevParticles P;
     int64_t base, count;
     int32_t tag0;
-    int mode;         // 0: spatial uniform, 1: plane x = xpos, 2: where a quantity is large
+    int mode;         // 0: spatial uniform, 1: plane x = xpos, 2: where a quantity is large,
+                      // 3: at the shock located per row (shock_ix)
     int dist_flag, ndim;
     double box[6];    // xmin ymin zmin xmax ymax zmax
     double xpos, dt, particle_v0, t_frame, dt_mhd, power_index;
     double p0, pmin, pmax;
     uint32_t key0, key1;
     LargeArgs lg;     // mode 2
+    // mode 3: 1-based x index of the shock per (y, z) row of the ghost-padded
+    // grid (nyg x nzg rows), and the grid origin and spacing
+    const int32_t *shock_ix;
+    int nyg, nzg;
+    double gxmin, gymin, gzmin, dx, dy, dz;
 };
 // Status bits (kStatusStepLimit on a runaway rejection loop) go to *status.
 cudaError_t launch_inject(const InjectArgs &a, unsigned int *status, cudaStream_t s);
+// locate_shock_xpos (mhd_data_parallel.f90:1988-2006) on frame 1: per row of
+// the ghost-padded grid, the first 1-based x index of the largest |dvx/dx|.
+cudaError_t launch_locate_shock(const float *full, int nxg, int nrows, int32_t *shock_ix,
+                                cudaStream_t s);
 // get_ncells_large_*: adds the count of grid nodes inside box (strict) whose
 // quantity exceeds lg.qmin to *ncells.
 cudaError_t launch_count_large(const LargeArgs &lg, int ndim, const double box[6],

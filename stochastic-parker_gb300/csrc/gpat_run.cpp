@@ -80,6 +80,7 @@ struct Options {
     bool precision_set = false;
     unsigned long long seed = 0x5EED0001ull;
     double shock_xpos = 0.5;
+    bool shock_xpos_set = false;   // --shock_xpos: a fixed plane instead of the located shock
     bool conf_in_config_dir = true;
 };
 
@@ -218,7 +219,7 @@ int parse(int argc, char **argv, Options &o) {
         else if (k == "--seed") o.seed = std::strtoull(v.c_str(), nullptr, 0);
         else if (k == "--device") o.device = (int)d;
         else if (k == "--bin_interval") o.bin_interval = (int)d;
-        else if (k == "--shock_xpos") o.shock_xpos = d;
+        else if (k == "--shock_xpos") { o.shock_xpos = d; o.shock_xpos_set = true; }
         else if (k == "--conf_path_is_literal") o.conf_in_config_dir = !truthy(v);
         else { std::fprintf(stderr, "gpat_run: unknown switch %s\n", argv[i - 1]); return 2; }
     }
@@ -801,8 +802,14 @@ int main(int argc, char **argv) {
         }
         const int ct = tf - o.t_start;
         if (o.inject_at_shock) {
-            CHECK(gpat_inject_particles_at_x(h, o.nptl, o.shock_xpos, o.tinterval, o.dist_flag,
-                                             o.particle_v0, ct, o.power_index));
+            // locate_shock_xpos + inject_particles_at_shock (:451-454), or a
+            // fixed plane with --shock_xpos
+            if (o.shock_xpos_set)
+                CHECK(gpat_inject_particles_at_x(h, o.nptl, o.shock_xpos, o.tinterval,
+                                                 o.dist_flag, o.particle_v0, ct, o.power_index));
+            else
+                CHECK(gpat_inject_particles_at_shock(h, o.nptl, o.tinterval, o.dist_flag,
+                                                     o.particle_v0, ct, o.power_index));
         } else if ((tf == o.t_start + 1 || o.inject_new_ptl) && tf <= o.tmax_to_inject) {
             // stochastic-mhd.f90:455-483: the first large-quantity option set wins
             int quantity = -1;

@@ -172,6 +172,57 @@ __device__ double large_quantity(int quantity, int ndim, bool sph, double x, dou
     return f[3];
 }
 
+// inject_particles_at_shock's position (particle_module.f90:568-588) with
+// interp_shock_location (mhd_data_parallel.f90:2017-2046) as intended: the
+// shock index of the rows either side of y (and z), linear in (y - ymin) / dy,
+// mapped to x = xmin + (index - 3) dx (index 3 is the first physical node).
+__device__ double shock_x(const InjectArgs &a, double y, double z) {
+    const int32_t *S = a.shock_ix;
+    double sx;
+    if (a.ndim == 1) {
+        sx = (double)S[0];
+    } else {
+        const double dpy = (y - a.gymin) / a.dy;
+        const int jy = (int)floor(dpy);
+        const double ry = dpy - (double)jy;
+        const int r0 = min(max(jy + 2, 0), a.nyg - 1), r1 = min(max(jy + 3, 0), a.nyg - 1);
+        if (a.ndim == 2) {
+            sx = (1.0 - ry) * (double)S[r0] + ry * (double)S[r1];
+        } else {
+            const double dpz = (z - a.gzmin) / a.dz;
+            const int jz = (int)floor(dpz);
+            const double rz = dpz - (double)jz;
+            const int k0 = min(max(jz + 2, 0), a.nzg - 1), k1 = min(max(jz + 3, 0), a.nzg - 1);
+            sx = (1.0 - ry) * (1.0 - rz) * (double)S[r0 + a.nyg * k0] +
+                 ry * (1.0 - rz) * (double)S[r1 + a.nyg * k0] +
+                 (1.0 - ry) * rz * (double)S[r0 + a.nyg * k1] + ry * rz * (double)S[r1 + a.nyg * k1];
+        }
+    }
+    return a.gxmin + (sx - 3.0) * a.dx;
+}
+
+// One warp per row: the first x index of the largest |dvx/dx| (slot 8 of the
+// 32-variable records), NaN never wins; written 1-based like maxloc.
+__global__ void __launch_bounds__(256) locate_shock_kernel(const float *full, int nxg, int nrows,
+                                                           int32_t *shock_ix) {
+    const int row = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    if (row >= nrows) return;
+    const int lane = threadIdx.x & 31;
+    float best = -1.0f;
+    int at = nxg;
+    for (int ix = lane; ix < nxg; ix += 32) {
+        const float v = fabsf(full[8 + 32 * ((size_t)ix + (size_t)nxg * (size_t)row)]);
+        if (v > best) { best = v; at = ix; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oa = __shfl_xor_sync(0xffffffffu, at, o);
+        if (ob > best || (ob == best && oa < at)) { best = ob; at = oa; }
+    }
+    if (lane == 0) shock_ix[row] = (at < nxg ? at : 0) + 1;
+}
+
 __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.count) return;
@@ -247,6 +298,7 @@ __global__ void inject_kernel(const InjectArgs a, unsigned int *status) {
         x = a.xpos;
         y = s.next() * (a.box[4] - a.box[1]) + a.box[1];
         z = s.next() * (a.box[5] - a.box[2]) + a.box[2];
+        if (a.mode == 3) x = shock_x(a, y, z);
         if (a.dist_flag == 0) {
             double ftest = 1.0, fxp = 0.5, ptmp = 0.0;
             int it = 0;
@@ -1248,6 +1300,13 @@ cudaError_t launch_count_large(const LargeArgs &lg, int ndim, const double box[6
     const int64_t blocks = (n + threads - 1) / threads;
     count_large_kernel<<<(unsigned)blocks, threads, 0, s>>>(lg, ndim, box[0], box[1], box[2],
                                                              box[3], box[4], box[5], ncells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_locate_shock(const float *full, int nxg, int nrows, int32_t *shock_ix,
+                                cudaStream_t s) {
+    if (nrows <= 0) return cudaSuccess;
+    locate_shock_kernel<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(full, nxg, nrows, shock_ix);
     return cudaGetLastError();
 }
 

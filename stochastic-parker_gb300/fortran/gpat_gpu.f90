@@ -29,7 +29,8 @@ module gpat_gpu
         gpu_get_tracked_particles, gpu_free_particle_tracking, &
         gpu_load_tstamps_mhd, gpu_get_pmax_global, gpu_global_distribution_mu, &
         gpu_escaped_distribution_mu, gpu_local_distribution, gpu_local_escaped_distribution, &
-        gpu_get_escaped_ptls, gpu_get_counters, gpu_set_counters, gpat_counters_t
+        gpu_get_escaped_ptls, gpu_get_counters, gpu_set_counters, gpat_counters_t, &
+        gpu_inject_particles_at_shock
 
     integer(c_int), parameter :: GPAT_OK = 0
 
@@ -340,6 +341,14 @@ module gpat_gpu
             type(gpat_particles_t), intent(inout) :: dst
             integer(c_int64_t), value :: capacity
             integer(c_int64_t), intent(out) :: n
+        end function
+        integer(c_int) function c_inject_at_shock(handle, nptl, dt, dist_flag, particle_v0, &
+                ct_mhd, power_index) bind(c, name="gpat_inject_particles_at_shock")
+            import :: c_int, c_ptr, c_int64_t, c_double
+            type(c_ptr), value :: handle
+            integer(c_int64_t), value :: nptl
+            real(c_double), value :: dt, particle_v0, power_index
+            integer(c_int), value :: dist_flag, ct_mhd
         end function
         integer(c_int) function c_set_counters(handle, in) bind(c, name="gpat_set_counters")
             import :: c_int, c_ptr, gpat_counters_t
@@ -714,6 +723,16 @@ module gpat_gpu
         s%tag_splitted = c_loc(tag_splitted); s%rng_ctr = c_null_ptr
         call check(c_get_tracked(h, s), "dump_tracked_particles")
     end subroutine gpu_get_tracked_particles
+
+    !< locate_shock_xpos + inject_particles_at_shock (particle_module.f90:
+    !< 542-633), same arguments
+    subroutine gpu_inject_particles_at_shock(nptl, dt, dist_flag, particle_v0, ct_mhd, &
+            power_index)
+        integer, intent(in) :: nptl, dist_flag, ct_mhd
+        real(8), intent(in) :: dt, particle_v0, power_index
+        call check(c_inject_at_shock(h, int(nptl, c_int64_t), dt, int(dist_flag, c_int), &
+            particle_v0, int(ct_mhd, c_int), power_index), "inject_particles_at_shock")
+    end subroutine gpu_inject_particles_at_shock
 
     !< load_tstamps_mhd (mhd_config.f90:221-255) for varying_dt_mhd
     subroutine gpu_load_tstamps_mhd(t_start, t_end, tmax_mhd, dir_mhd_data)

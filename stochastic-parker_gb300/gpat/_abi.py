@@ -188,6 +188,9 @@ SIGNATURES = {
     "gpat_free_particle_tracking": (C.c_int, [Handle]),
     "gpat_load_tstamps_mhd": (C.c_int, [Handle, C.c_int, C.c_int, C.c_int, C.c_char_p]),
     "gpat_get_pmax_global": (C.c_int, [Handle, P(C.c_double)]),
+    "gpat_locate_shock_xpos": (C.c_int, [Handle, P(C.c_int32)]),
+    "gpat_inject_particles_at_shock": (C.c_int, [Handle, C.c_int64, C.c_double, C.c_int,
+                                                 C.c_double, C.c_int, C.c_double]),
     "gpat_calc_particle_distributions_mu": (C.c_int, [Handle, C.c_int32, P(C.c_double),
                                                       P(C.c_uint64)]),
     "gpat_calc_escaped_distributions_mu": (C.c_int, [Handle, C.c_int32, P(C.c_double),

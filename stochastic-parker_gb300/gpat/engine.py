@@ -263,6 +263,17 @@ class Engine:
         self._check(self.lib.gpat_inject_particles_spatial_uniform(
             self.h, int(nptl), dt, dist_flag, particle_v0, ct_mhd, box, power_index))
 
+    def locate_shock_xpos(self) -> np.ndarray:
+        """locate_shock_xpos on frame 1: (nzg, nyg) 1-based x indices."""
+        S = np.zeros((self.nzg, self.nyg), np.int32)
+        self._check(self.lib.gpat_locate_shock_xpos(self.h, S.ctypes.data_as(C.POINTER(C.c_int32))))
+        return S
+
+    def inject_particles_at_shock(self, nptl, dt, dist_flag, particle_v0, ct_mhd,
+                                  power_index=7.0):
+        self._check(self.lib.gpat_inject_particles_at_shock(
+            self.h, int(nptl), dt, dist_flag, particle_v0, ct_mhd, power_index))
+
     def inject_particles_at_x(self, nptl, xpos, dt, dist_flag, particle_v0, ct_mhd,
                               power_index=7.0):
         self._check(self.lib.gpat_inject_particles_at_x(

@@ -36,11 +36,12 @@ def _dataset(tmp_path: Path):
     return w, data, out
 
 
-def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False, extra=()):
+def _run_driver(tmp_path, data, out, precision="fp64", ft=False, nlgc=False, extra=(),
+                shock_plane=True):
     exe = build.build_driver()
+    plane = ["--shock_xpos", "0.5"] if shock_plane else []
     cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/",
-           "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", "--shock_xpos",
-           "0.5", "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
+           "-ts", "0", "-te", "3", "-np", "2000", "-nm", "40000", "-is", "1", *plane, "-df", "1", "-pv", "1.0", "-dt", "1e-7", "-sf", "1", "-nd", "2",
            "--precision", precision, "--seed", str(SEED), "-ug", "1",
            "-ft", ".true." if ft else ".false.",
            "-nl", ".true." if nlgc else ".false.", "-kk", "0.05", "-du", "3.0", "-pd", "1",
@@ -292,6 +293,39 @@ def test_load_tstamps_mhd(tmp_path):
     assert eng.get_pmax_global() == pytest.approx(w.params["p0"])
     with pytest.raises(Exception):
         eng.load_tstamps_mhd(1, 4, 2, tmp_path / "nowhere")
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_driver_injects_at_the_located_shock(tmp_path):
+    """-is without --shock_xpos locates the shock each frame
+    (locate_shock_xpos + inject_particles_at_shock): the restart dump equals
+    the same calls made from Python, and the particles start on the shock."""
+    w, data, out = _dataset(tmp_path)
+    r = _run_driver(tmp_path, data, out, shock_plane=False)
+    assert r.returncode == 0, r.stderr
+    prm = make_params(**dict(w.params, npp_global=64, nptl_max=40000, seed=SEED, precision=0,
+                             b0=1.0, drift1=4e7, drift2=2e8, charge=-1, duu0=3.0))
+    eng = Engine(prm, w.mhd_config, 0)
+    eng.calc_tstamps_mhd(0, 3)
+    eng.read_field_data(data / "mhd_data_0000", 0)
+    eng.calc_fields_gradients(0)
+    for tf in range(1, 4):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        eng.inject_particles_at_shock(2000, 1e-7, 1, 1.0, tf)
+        if tf == 1:
+            x0 = eng.get_particles()["x"]
+            assert np.all(np.abs(x0 - 0.5) <= w.mhd_config.dx)   # the planar shock at 0.5
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1,
+                           dump_escaped_dist=True)
+        eng.split_particle(2.72, 2.0, 10)
+        eng.reset_escaped_particles()
+    got = eng.get_particles()
+    d = read_particle_dump(out / "restart" / "particles_0003.dat")
+    assert len(d["x"]) == len(got)
+    for k in d:
+        assert np.array_equal(d[k], got[k]), k
     eng.close()
 
 
