@@ -462,11 +462,13 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "gpat_run: -ib needs -db 1 (the magnetic-fluctuation arrays)\n");
         return 2;
     }
-    // Focused transport and momentum diffusion run on the FP64 mover unless
-    // asked otherwise.
+    // Options the split-precision mover does not have (focused transport,
+    // Dpp, turbulence arrays, spherical or non-uniform grids, include_3rd_dim,
+    // surfaces, tracking, 1D) run on the FP64 mover unless asked otherwise.
     if ((o.focused_transport || o.dpp_wave || o.dpp_shear || o.deltab_flag ||
          o.correlation_flag || o.spherical_coord == 1 || o.uniform_grid != 1 ||
-         o.include_3rd_dim == 1 || o.acc_by_surface == 1 || o.track_particle_flag) &&
+         o.include_3rd_dim == 1 || o.acc_by_surface == 1 || o.track_particle_flag ||
+         o.ndim_field == 1) &&
         !o.precision_set)
         o.precision = GPAT_PREC_FP64;
     gpat_handle_t *h = nullptr;

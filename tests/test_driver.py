@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from gpat import build, configs, fields
-from gpat.engine import Engine, make_params, read_particle_dump
+from gpat.engine import Engine, make_mhd_config, make_params, read_particle_dump
 
 SEED = 0x1234567
 
@@ -326,6 +326,56 @@ def test_driver_injects_at_the_located_shock(tmp_path):
     assert len(d["x"]) == len(got)
     for k in d:
         assert np.array_equal(d[k], got[k]), k
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_driver_1d_run(tmp_path):
+    """-nd 1 runs on the FP64 mover by default and ends with the particles
+    and f(p) of the same calls made from Python."""
+    n = 128
+    cfg = make_mhd_config(n, 1, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.05, ndim=1)
+    x = fields.node_coords(n, 0.0, 1.0 / n)[None, None, :]
+    z = np.zeros_like(x)
+    vx = 1.0 - 0.75 * (1.0 + np.tanh((x - 0.5) / 0.01)) / 2.0
+    frame = fields.assemble_frame(vx, z, z, 1.0 + z, 1.0 + z, 0.2 + z, z).astype(np.float32)
+    data, out = tmp_path / "data", tmp_path / "out"
+    data.mkdir()
+    out.mkdir()
+    (tmp_path / "config").mkdir()
+    fields.write_mhd_config(data / "mhd_config.dat", cfg)
+    for t in range(3):
+        fields.write_mhd_data(data / f"mhd_data_{t:04d}", frame)
+    vals = dict(b0=1.0, p0=0.1, pmin=0.1, pmax=100.0, momentum_dependency=0, gamma_turb=5 / 3,
+                mag_dependency=0, kpara0=1e-3, kret=0.1, dt_min_rel=1e-3, dt_max_rel=1e-2)
+    lines = [f"{k} = {v!r}" for k, v in vals.items()]
+    lines += ["acc_region_flag = 0", "npp_global = 32", "nmu_global = 1", "pbcx = 1",
+              "pbcy = 0", "pbcz = 0"]
+    (tmp_path / "config" / "conf.dat").write_text("\n".join(lines) + "\n")
+    exe = build.build_driver()
+    cmd = [str(exe), "-dm", str(data) + "/", "-cf", "conf.dat", "-dd", str(out) + "/", "-ts", "0",
+           "-te", "2", "-np", "500", "-nm", "5000", "-is", "1", "--shock_xpos", "0.5", "-df", "1",
+           "-pv", "1.0", "-dt", "1e-7", "-sf", "0", "-nd", "1", "-ug", "1", "-nl", ".false.",
+           "--seed", str(SEED)]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    prm = make_params(**dict(vals, ndim=1, npp_global=32, nptl_max=5000, seed=SEED, precision=0,
+                             pbcx=1, drift1=4e7, drift2=2e8, charge=-1))
+    eng = Engine(prm, cfg, 0)
+    eng.calc_tstamps_mhd(0, 2)
+    for tf in range(1, 3):
+        eng.read_field_data(data / f"mhd_data_{tf:04d}", 0)
+        eng.calc_fields_gradients(0)
+        eng.inject_particles_at_x(500, 0.5, 1e-7, 1, 1.0, tf)
+        eng.particle_mover(nsteps_interval=10, mhd_tframe=tf, num_fine_steps=1)
+    got = eng.get_particles()
+    d = read_particle_dump(out / "restart" / "particles_0002.dat")
+    assert len(d["x"]) == len(got) > 0
+    for k in d:
+        assert np.array_equal(d[k], got[k]), k
+    _, f_drv, c_drv = _read_fdists(out / "fdists_0002.dat")
+    f, c = eng.calc_particle_distributions()
+    assert np.array_equal(c, c_drv) and np.array_equal(f, f_drv) and c.sum() > 0
     eng.close()
 
 
