@@ -458,6 +458,10 @@ int main(int argc, char **argv) {
         return prc == 1 ? 0 : 2;
     }
     if (o.single_time_frame == 1) o.time_interp_flag = 0;   // stochastic-mhd.f90:134-136
+    if (o.size_mpi_sub != 1) {
+        std::fprintf(stderr, "gpat_run: one rank per device; -sm must be 1\n");
+        return 2;
+    }
     if (o.inject_large_db2 && o.deltab_flag != 1) {
         std::fprintf(stderr, "gpat_run: -ib needs -db 1 (the magnetic-fluctuation arrays)\n");
         return 2;
@@ -518,11 +522,6 @@ int main(int argc, char **argv) {
         CHECK(gpat_load_tstamps_mhd(h, o.t_start, o.t_end, o.tmax_mhd, o.dir_mhd_data.c_str()));
     else
         CHECK(gpat_calc_tstamps_mhd(h, o.t_start, o.t_end));
-    if (o.size_mpi_sub != 1) {
-        std::fprintf(stderr, "gpat_run: one rank per device; -sm must be 1\n");
-        gpat_destroy(h);
-        return 2;
-    }
     // restart (stochastic-mhd.f90:224-238): the frame of restart/latest_restart,
     // its particles and module state
     const std::string restart = o.diagnostics_directory + "restart/";

@@ -69,6 +69,8 @@ def test_driver_usage_without_gpu(engine_lib):
     r = subprocess.run([str(exe), "-dm", "/nonexistent/"], capture_output=True, text=True,
                        timeout=60)
     assert r.returncode == 1 and "gpat_load_mhd_config" in r.stderr
+    r = subprocess.run([str(exe), "-sm", "2"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "-sm must be 1" in r.stderr
 
 
 @pytest.mark.gpu
