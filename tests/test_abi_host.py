@@ -39,6 +39,23 @@ def test_fortran_shim_binds_exported_symbols(engine_lib):
         assert hasattr(engine_lib, n), n
 
 
+def test_header_compiles_as_c(tmp_path):
+    """include/gpat_engine.h is plain C99: no C++ or torch types."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "hdr.c"
+    src.write_text('#include "gpat_engine.h"\n'
+                   "int main(void) { gpat_params_t p; gpat_particles_t s; gpat_counters_t c;\n"
+                   "  gpat_local_dist_t l; (void)p; (void)s; (void)c; (void)l; return GPAT_OK; }\n")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-I", str(HEADER.parent), "-c", str(src), "-o", str(tmp_path / "hdr.o")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+
+
 def test_struct_layouts_match_header():
     # gpat_mhd_config_t: 13 doubles + 13 int32 (+4 bytes tail padding)
     assert C.sizeof(_abi.MhdConfig) == 160
