@@ -182,3 +182,109 @@ def test_frames_have_reference_layout():
     vx = frame[0, 0, :, 0]
     assert vx[0] == pytest.approx(1.0) and vx[-1] == pytest.approx(0.25, rel=1e-6)
     assert np.all(frame[..., 7] == np.sqrt(frame[..., 4].astype(np.float64) ** 2).astype(np.float32))
+
+
+# --- Fortran bind(c) interfaces against the C prototypes -------------------
+# Each dummy argument of a bind(c) interface in the shim is reduced to the C
+# type it passes (value or reference, element type), and so is each parameter
+# of the header's prototype; the two lists must agree.  An int passed where
+# the header takes int64_t, a missing `value`, or a dropped argument fails
+# here without a Fortran compiler.
+
+_F_KIND = {"c_int": "i32", "c_int32_t": "i32", "c_int64_t": "i64", "c_int8_t": "i8",
+           "c_double": "f64", "c_float": "f32", "c_char": "char"}
+
+
+def _fortran_interfaces(text):
+    out = {}
+    blocks = re.findall(
+        r'^\s*(?:(integer\(c_int\)|type\(c_ptr\))\s+function|subroutine)\s+(\w+)\s*\(([^)]*)\)'
+        r'[\s&]*bind\(c,\s*name="(gpat_\w+)"\)(.*?)^\s*end\s+(?:function|subroutine)',
+        text, flags=re.M | re.S | re.I)
+    for result, _, args, cname, body in blocks:
+        names = [a.strip().lower() for a in args.replace("&", " ").split(",") if a.strip()]
+        decl = {}
+        for line in body.splitlines():
+            if "::" not in line or line.strip().lower().startswith("import"):
+                continue
+            spec, vars_ = line.split("::", 1)
+            spec = spec.strip().lower()
+            for v in vars_.split(","):
+                decl[v.strip().lower().split("(")[0]] = spec
+        kinds = []
+        for n in names:
+            spec = decl[n]
+            by_value = "value" in spec
+            m = re.match(r"(integer|real|character|type)\((?:kind=)?(\w+)\)", spec)
+            base = m.group(2)
+            if m.group(1) == "type":
+                k = "ptr" if base == "c_ptr" else base
+            else:
+                k = _F_KIND[base]
+            kinds.append(k if by_value else k + "*")
+        ret = {"integer(c_int)": "i32", "type(c_ptr)": "ptr"}.get(result.lower(), "void")
+        out[cname] = (ret, kinds)
+    return out
+
+
+_C_BASE = {"int": "i32", "int32_t": "i32", "int64_t": "i64", "uint64_t": "i64",
+           "int8_t": "i8", "double": "f64", "float": "f32", "char": "char", "void": "void"}
+
+
+def _c_kind(decl):
+    d = decl.replace("const", " ").strip()
+    stars = d.count("*") + d.count("[")      # an array parameter is a pointer
+    words = d.replace("*", " ").split()
+    base = words[0]
+    if base in ("gpat_handle_t", "gpat_batch_t", "gpat_mlp_t") or (base == "void" and stars):
+        k, stars = "ptr", stars - 1          # opaque handles and void * travel as c_ptr
+    else:
+        k = _C_BASE.get(base, base)
+    return k + "*" * stars
+
+
+def _c_prototypes(text):
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for ret, name, args in re.findall(r"([\w\s\*]+?)\b(gpat_\w+)\s*\(([^;{]*?)\)\s*;", text):
+        params = [a.strip() for a in args.split(",") if a.strip() and a.strip() != "void"]
+        out[name] = (_c_kind(ret.strip().split("\n")[-1]), [_c_kind(p) for p in params])
+    return out
+
+
+def _same_kind(f, c):
+    if f == c:
+        return True
+    # a c_ptr by value stands for any single pointer (e.g. an optional
+    # file name or a device array)
+    return f == "ptr" and c.endswith("*") and c.count("*") == 1
+
+
+def test_fortran_interfaces_match_c_prototypes():
+    shim = HEADER.parent.parent / "stochastic-parker_gb300" / "fortran" / "gpat_gpu.f90"
+    fort = _fortran_interfaces(shim.read_text())
+    cproto = _c_prototypes(HEADER.read_text())
+    bound = set(re.findall(r'bind\(c,\s*name="(gpat_\w+)"\)', shim.read_text()))
+    assert set(fort) == bound, bound - set(fort)
+    for name, (fret, fargs) in sorted(fort.items()):
+        assert name in cproto, name
+        cret, cargs = cproto[name]
+        assert len(fargs) == len(cargs), (name, fargs, cargs)
+        for i, (f, c) in enumerate(zip(fargs, cargs)):
+            assert _same_kind(f, c), (name, i, f, c)
+        if fret == "ptr":
+            assert cret.endswith("*"), (name, cret)
+        else:
+            assert fret == cret, (name, fret, cret)
+
+
+def test_fortran_interface_check_catches_a_mismatch():
+    """The check above fails on an int count where the header has int64_t."""
+    shim = HEADER.parent.parent / "stochastic-parker_gb300" / "fortran" / "gpat_gpu.f90"
+    text = shim.read_text()
+    fort = _fortran_interfaces(text)
+    name = next(n for n, (_, a) in fort.items() if "i64" in a)
+    i = fort[name][1].index("i64")
+    cargs = _c_prototypes(HEADER.read_text())[name][1]
+    assert cargs[i] == "i64"
+    assert not _same_kind("i32", cargs[i])
