@@ -87,7 +87,21 @@ def parse_args(argv=None):
                     help="pushes between re-binnings (0: engine default, <0: once per call)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 sample and the f(p) tail-error check")
+    ap.add_argument("--tiles", default="off",
+                    help="split-precision mover field bricks: 'off' (global gathers) or "
+                         "'bx,by,bz[,hx,hy,hz[,threads[,items]]]': cells per brick and halo "
+                         "cells per side staged in shared memory")
     return ap.parse_args(argv)
+
+
+def parse_tiles(spec: str):
+    """(bx, by, bz, hx, hy, hz, threads, items) of --tiles, or None for 'off'."""
+    if spec in ("off", "0", ""):
+        return None
+    v = [int(x) for x in spec.split(",")]
+    if len(v) == 2:
+        v.append(1)
+    return tuple((v + [0] * 8)[:8])
 
 
 def l2_read_gbs(torch, dev) -> float:
@@ -314,6 +328,9 @@ def run_ours(args, world, rank, local):
                       nframes=total_frames)
     eng = configs.build_engine(w, device=local, nptl_max=int(w.nptl * 1.6),
                                bin_interval=args.bin_interval)
+    tiles = parse_tiles(args.tiles) if prec == 1 else None
+    if tiles:
+        eng.set_mover_tiles(*tiles)
     configs.inject(eng, w)
     stream = torch.cuda.ExternalStream(eng.stream, device=dev)
     frame = [1]

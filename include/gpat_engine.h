@@ -301,6 +301,26 @@ int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc,
                         double kperp_kpara, int nsteps_interval, int mhd_tframe,
                         int num_fine_steps, int dump_escaped_dist);
+/* No counterpart in the reference, whose particles read field arrays in host
+ * memory.  Selects how the split-precision mover (GPAT_PREC_MIXED, 2D and 3D)
+ * of gpat_particle_mover reads the fields: bx = 0 gathers the packed field
+ * records from device memory through the caches; bx > 0 cuts the grid into
+ * bricks of bx x by x bz cells (bz, hz ignored in 2D), keeps the particle set
+ * binned brick-major, and has each CTA copy the records of one brick plus a
+ * halo of hx, hy, hz cells on every side into shared memory (TMA) and move
+ * that brick's particles for a chunk of bin_interval pushes; a particle that
+ * walks out of the staged region finishes its chunk with global gathers.
+ * threads: per CTA, 256 or 512 (0: 512); items: particles a CTA takes per
+ * brick visit (0: 4096).  The staged records ((sx+1)(sy+1)(sz+1) nodes,
+ * s = b + 2h, x 64 or 96 bytes, twice with time_interp) must fit in one CTA's
+ * shared memory (GPAT_ERR_ARG otherwise); a brick larger than the grid is cut
+ * to it.  Both forms give the same trajectories to FP32 rounding (the same
+ * increments for the same push; paused particles are rebuilt from their FP64
+ * record at other pushes), not bit for bit. */
+int gpat_set_mover_tiles(gpat_handle_t *h, int bx, int by, int bz, int hx, int hy, int hz,
+                         int threads, int items);
+/* out[8] = {bx, by, bz, hx, hy, hz, threads, items} as set (bx = 0: no bricks). */
+int gpat_get_mover_tiles(const gpat_handle_t *h, int *out);
 /* split_particle (particle_module.f90:5430-5480): children appended in
  * parent order; stops at nptl_max like the reference. */
 int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
@@ -315,9 +335,14 @@ int gpat_split_particle(gpat_handle_t *h, double split_ratio, double pmin_split,
  * scratch and counters are fixed file-scope device arrays (about 1 MiB on
  * every GPU that loads the library, held until exit), sized for at most
  * 2^26 = 67,108,864 parents; larger n returns GPAT_ERR_ARG.  The first call
- * on a device looks up those arrays' device addresses and should come before
- * any stream capture.  All calls share the arrays, so calls whose work
- * overlaps on the GPU (other streams, other threads) race; serialise them.
+ * on a device looks up those arrays' device addresses; with CUDA's lazy
+ * module loading (the default) that first call also makes the driver load
+ * the library's device code and reserve the arrays.  So make one warm-up
+ * call with n = 0 (valid dev and n_out) on each device before the time loop
+ * and before any stream capture.  All calls share the arrays, so calls whose
+ * work overlaps on the GPU (other streams, other threads) race; serialise
+ * them.  Particle tracking is not supported here: pass no tracked particles
+ * (tag_splitted < 0); the handle's gpat_split_particle tracks them.
  * Work is enqueued on `stream` (a cudaStream_t, NULL for the default
  * stream), which is synchronised before return.  *n_out is the new particle
  * count, *n_split (may be NULL) the children created; GPAT_ERR_CAPACITY when

@@ -179,3 +179,36 @@ cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t 
 }
 
 }  // namespace gpat
+
+namespace gpat {
+namespace {
+
+// Chunk-planar copy of the packed records: float4 chunk j of every node
+// contiguous, planes[j * ncells + c] = rec[c * R + 4 j .. 4 j + 3].  The
+// tile mover stages these planes, so neighbouring nodes of one chunk sit in
+// neighbouring shared-memory bank groups.
+template <int R>
+__global__ void planarize_kernel(const float4 *__restrict__ rec, float4 *__restrict__ planes,
+                                 size_t ncells) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += stride) {
+#pragma unroll
+        for (int j = 0; j < R / 4; ++j) planes[(size_t)j * ncells + c] = rec[c * (R / 4) + j];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_planarize_records(const float *rec, float *planes, int ndim, size_t ncells,
+                                     cudaStream_t s) {
+    const int threads = 256;
+    size_t blocks = (ncells + threads - 1) / threads;
+    if (blocks > 65535 * 8) blocks = 65535 * 8;
+    const float4 *r = reinterpret_cast<const float4 *>(rec);
+    float4 *o = reinterpret_cast<float4 *>(planes);
+    if (ndim == 2) planarize_kernel<kRec2D><<<(unsigned)blocks, threads, 0, s>>>(r, o, ncells);
+    else planarize_kernel<kRec3D><<<(unsigned)blocks, threads, 0, s>>>(r, o, ncells);
+    return cudaGetLastError();
+}
+
+}  // namespace gpat

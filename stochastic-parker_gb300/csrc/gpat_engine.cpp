@@ -52,7 +52,25 @@ struct gpat_handle {
     size_t scratch_bytes = 0;
     // split-precision path: particles kept binned by cell
     void *sort_scratch = nullptr;
+    int64_t sort_bins = 0;   // bins the sort scratch is sized for
     bool unsorted = true;   // particles appended since the last binning
+    // Split-precision mover with field bricks in shared memory (mover_tile.cu):
+    // brick cells per axis (tile_b[0] = 0: the global-gather mover), threads
+    // per CTA, particles per work item; binned_tiles: the last binning was
+    // brick-major with this shape.
+    int tile_b[3] = {0, 0, 0};
+    int tile_h[3] = {0, 0, 0};       // halo cells staged around a brick
+    int tile_threads = 512;
+    int tile_items = 4096;
+    bool binned_tiles = false;
+    long long *tile_dev = nullptr;   // item prefix (nbricks + 1) and the item counter
+    int64_t tile_dev_n = 0;
+    void *tile_ovf = nullptr;        // overflow list: indices, pushes done, count
+    int64_t tile_ovf_cap = 0;
+    // Chunk-planar copies of the packed records the tile mover stages, per
+    // frame slot; rec_gen counts writes of rec[s], plane_gen the copy's source.
+    float *planes[2] = {nullptr, nullptr};
+    uint64_t rec_gen[2] = {1, 1}, plane_gen[2] = {0, 0};
     DevCounters *dcnt = nullptr;
     DevCounters hcnt{};
     unsigned long long *dbins = nullptr;
@@ -136,9 +154,28 @@ int check_status(gpat_handle_t *h) {
     if (h->hcnt.status) {
         const unsigned s = h->hcnt.status;
         std::string m = "device status:";
-        if (s & kStatusIndexGuard) m += " interpolation index outside the ghost cells;";
+        if (s & kStatusIndexGuard) {
+            m += " interpolation index outside the ghost cells;";
+            const unsigned long long v = h->hcnt.bad_value;
+            if (v && !(s & kStatusTileMiss)) {
+                m += " (node " + std::to_string((short)(v & 0xffff)) + ", " +
+                     std::to_string((short)((v >> 16) & 0xffff)) + ", " +
+                     std::to_string((short)((v >> 32) & 0xffff)) + "; " +
+                     (((v >> 48) & 0xff) == 2 ? "brick" : "global") + " gather)";
+                CK(cudaMemsetAsync(&h->dcnt->bad_value, 0, sizeof(unsigned long long), h->stream));
+            }
+        }
         if (s & kStatusNonFinite) m += " non-finite particle state;";
         if (s & kStatusStepLimit) m += " per-call push/iteration limit reached;";
+        if (s & kStatusTileTimeout) m += " a field brick copy into shared memory timed out;";
+        if (s & kStatusTileMiss) {
+            const unsigned long long v = h->hcnt.bad_value;
+            m += " a particle outside the staged brick it was binned in (node " +
+                 std::to_string(v & 0xffff) + ", " + std::to_string((v >> 16) & 0xffff) +
+                 ", region origin " + std::to_string((short)((v >> 32) & 0xffff)) + ", " +
+                 std::to_string((short)((v >> 48) & 0xffff)) + ");";
+            CK(cudaMemsetAsync(&h->dcnt->bad_value, 0, sizeof(unsigned long long), h->stream));
+        }
         CK(cudaMemsetAsync(&h->dcnt->status, 0, sizeof(unsigned int), h->stream));
         h->hcnt.status = 0;
         return fail(h, GPAT_ERR_DEVICE, m);
@@ -305,13 +342,27 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     return GPAT_OK;
 }
 
-CellGrid cell_grid(const gpat_handle_t *h) {
-    CellGrid g;
+// tiled: bins ordered brick-major with the handle's brick shape (tile mover).
+CellGrid cell_grid(const gpat_handle_t *h, bool tiled = false) {
+    CellGrid g{};
     g.xmin = h->cfg.xmin; g.ymin = h->cfg.ymin; g.zmin = h->cfg.zmin;
     g.idx = 1.0 / h->cfg.dx; g.idy = 1.0 / h->cfg.dy;
     g.idz = h->prm.ndim == 3 ? 1.0 / h->cfg.dz : 0.0;
     g.nxg = h->nxg; g.nyg = h->nyg; g.nzg = h->nzg;
+    if (tiled) {
+        g.tile = 1;
+        g.dx = h->cfg.dx; g.dy = h->cfg.dy; g.dz = h->cfg.dz;
+        g.bx = h->tile_b[0]; g.by = h->tile_b[1];
+        g.bz = h->prm.ndim == 3 ? h->tile_b[2] : 1;
+        g.nbx = (h->nxg + g.bx - 1) / g.bx;
+        g.nby = (h->nyg + g.by - 1) / g.by;
+        g.nbz = (h->nzg + g.bz - 1) / g.bz;
+    }
     return g;
+}
+
+bool tiles_on(const gpat_handle_t *h) {
+    return h->tile_b[0] > 0 && h->prm.precision == GPAT_PREC_MIXED;
 }
 
 // Bins the current particles by cell into the other buffer (split-precision
@@ -327,15 +378,30 @@ EscHist escaped_hist(const gpat_handle_t *h) {
     return e;
 }
 
-int bin_particles(gpat_handle_t *h) {
+// tiled: brick-major bins for the tile mover (the sort scratch grows to fit).
+int bin_particles(gpat_handle_t *h, bool tiled = false) {
     const int nxt = 1 - h->cur;
-    CK(launch_cell_sort(h->P[h->cur], h->P[nxt], h->n, cell_grid(h), h->sort_scratch, h->dcnt,
+    const CellGrid g = cell_grid(h, tiled);
+    const int64_t nbins = cell_grid_bins(g);
+    if (nbins > h->sort_bins) {
+        CK(cudaStreamSynchronize(h->stream));
+        if (h->sort_scratch) CK(cudaFree(h->sort_scratch));
+        h->sort_scratch = nullptr;
+        h->sort_bins = 0;
+        if (cudaMalloc(&h->sort_scratch, cell_sort_scratch_bytes(h->cap, nbins)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, GPAT_ERR_OOM, "binning scratch");
+        }
+        h->sort_bins = nbins;
+    }
+    CK(launch_cell_sort(h->P[h->cur], h->P[nxt], h->n, g, h->sort_scratch, h->dcnt,
                         escaped_hist(h), h->stream));
     int rc = pull_counters(h);
     if (rc) return rc;
     h->cur = nxt;
     h->n = (int64_t)h->hcnt.nkept;
     h->unsorted = false;
+    h->binned_tiles = tiled;
     return GPAT_OK;
 }
 
@@ -573,10 +639,12 @@ int gpat_create(const gpat_params_t *params, const gpat_mhd_config_t *cfg, int d
         cudaMemsetAsync(h->pmem[b], 0, particle_bytes(h->cap), h->stream);
         h->P[b] = carve(h->pmem[b], h->cap);
     }
-    if (p.precision == GPAT_PREC_MIXED &&
-        cudaMalloc(&h->sort_scratch, cell_sort_scratch_bytes(h->cap, (int64_t)h->ncells)) !=
+    if (p.precision == GPAT_PREC_MIXED) {
+        if (cudaMalloc(&h->sort_scratch, cell_sort_scratch_bytes(h->cap, (int64_t)h->ncells)) !=
             cudaSuccess)
-        return bail(GPAT_ERR_OOM);
+            return bail(GPAT_ERR_OOM);
+        h->sort_bins = (int64_t)h->ncells;
+    }
     if (cudaMalloc(&h->dcnt, sizeof(DevCounters)) != cudaSuccess) return bail(GPAT_ERR_OOM);
     cudaMemsetAsync(h->dcnt, 0, sizeof(DevCounters), h->stream);
     if (cudaMalloc(&h->dbins, sizeof(unsigned long long) * 3 * (size_t)p.npp_global) != cudaSuccess)
@@ -615,6 +683,10 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->dshock) cudaFree(h->dshock);
     if (h->scratch) cudaFree(h->scratch);
     if (h->sort_scratch) cudaFree(h->sort_scratch);
+    if (h->tile_dev) cudaFree(h->tile_dev);
+    if (h->tile_ovf) cudaFree(h->tile_ovf);
+    for (int s = 0; s < 2; ++s)
+        if (h->planes[s]) cudaFree(h->planes[s]);
     if (h->dcnt) cudaFree(h->dcnt);
     if (h->dbins) cudaFree(h->dbins);
     if (h->desc) cudaFree(h->desc);
@@ -677,6 +749,7 @@ int gpat_set_fields(gpat_handle_t *h, int var_flag, const float *farray, int nva
                            cudaMemcpyHostToDevice, h->stream));
         CK(launch_pack_records(h->full[slot], h->rec[slot], h->prm.ndim, h->ncells, h->stream));
         h->rec_ready[slot] = true;
+        ++h->rec_gen[slot];
     } else {
         if (!h->staging) CK(cudaMalloc(&h->staging, 8 * sizeof(float) * h->ncells));
         CK(cudaMemcpyAsync(h->staging, farray, 8 * sizeof(float) * h->ncells,
@@ -904,6 +977,7 @@ int gpat_calc_fields_gradients(gpat_handle_t *h, int var_flag) {
     CK(launch_pack_records(h->full[slot], h->rec[slot], h->prm.ndim, h->ncells, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->rec_ready[slot] = true;
+    ++h->rec_gen[slot];
     return GPAT_OK;
 }
 
@@ -926,6 +1000,7 @@ int gpat_copy_fields(gpat_handle_t *h) {
     CK(cudaStreamSynchronize(h->stream));
     h->fields_set[0] = h->fields_set[1];
     h->rec_ready[0] = h->rec_ready[1];
+    ++h->rec_gen[0];
     return GPAT_OK;
 }
 
@@ -1192,6 +1267,54 @@ int gpat_get_escaped_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t 
     return GPAT_OK;
 }
 
+int gpat_set_mover_tiles(gpat_handle_t *h, int bx, int by, int bz, int hx, int hy, int hz,
+                         int threads, int items) {
+    if (!h) return GPAT_ERR_ARG;
+    if (bx == 0) {
+        h->tile_b[0] = h->tile_b[1] = h->tile_b[2] = 0;
+        h->tile_h[0] = h->tile_h[1] = h->tile_h[2] = 0;
+        return GPAT_OK;
+    }
+    if (h->prm.precision != GPAT_PREC_MIXED || h->prm.ndim < 2)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "field bricks need the split-precision 2D/3D mover");
+    if (h->prm.ndim == 2) { bz = 1; hz = 0; }
+    if (bx < 2 || by < 2 || (h->prm.ndim == 3 && bz < 2))
+        return fail(h, GPAT_ERR_ARG, "bricks need at least 2 cells per axis");
+    if (hx < 0 || hy < 0 || hz < 0 || hx > 64 || hy > 64 || hz > 64)
+        return fail(h, GPAT_ERR_ARG, "halo cells must be in [0, 64]");
+    if (threads == 0) threads = 512;
+    if (threads != 256 && threads != 512) return fail(h, GPAT_ERR_ARG, "threads must be 256 or 512");
+    if (items == 0) items = 4096;
+    if (items < 32 || items > (1 << 24)) return fail(h, GPAT_ERR_ARG, "items out of range");
+    // a brick larger than the grid is the grid; TMA boxes hold at most 256 nodes per axis
+    bx = std::min(bx, h->nxg - 1);
+    by = std::min(by, h->nyg - 1);
+    if (h->prm.ndim == 3) bz = std::min(bz, h->nzg - 1);
+    const int sx = bx + 2 * hx, sy = by + 2 * hy, sz = bz + 2 * hz;   // staged cells
+    if (sx + 1 > 256 || sy + 1 > 256 || sz + 1 > 256)
+        return fail(h, GPAT_ERR_ARG, "at most 255 staged cells per axis");
+    int smem_max = 0;
+    CK(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    const size_t need = tile_smem_bytes(h->prm.ndim, sx, sy, sz, h->prm.time_interp, nullptr, nullptr);
+    if (need + 1024 > (size_t)smem_max)
+        return fail(h, GPAT_ERR_ARG, "staged records exceed the shared memory of one CTA (" +
+                                         std::to_string(need) + " bytes)");
+    if (bx != h->tile_b[0] || by != h->tile_b[1] || bz != h->tile_b[2]) h->binned_tiles = false;
+    h->tile_b[0] = bx; h->tile_b[1] = by; h->tile_b[2] = bz;
+    h->tile_h[0] = hx; h->tile_h[1] = hy; h->tile_h[2] = hz;
+    h->tile_threads = threads;
+    h->tile_items = items;
+    return GPAT_OK;
+}
+
+int gpat_get_mover_tiles(const gpat_handle_t *h, int *out) {
+    if (!h || !out) return GPAT_ERR_ARG;
+    out[0] = h->tile_b[0]; out[1] = h->tile_b[1]; out[2] = h->tile_b[2];
+    out[3] = h->tile_h[0]; out[4] = h->tile_h[1]; out[5] = h->tile_h[2];
+    out[6] = h->tile_threads; out[7] = h->tile_items;
+    return GPAT_OK;
+}
+
 int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, double kperp_kpara,
                         int nsteps_interval, int mhd_tframe, int num_fine_steps,
                         int dump_escaped_dist) {
@@ -1211,9 +1334,11 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     CK(cudaSetDevice(h->device));
     rc = ensure_scratch(h, h->n);
     if (rc) return rc;
-    if (mixed && h->unsorted) {
-        // New particles since the last binning: bin them before moving.
-        rc = bin_particles(h);
+    const bool tiled = mixed && tiles_on(h);
+    if (mixed && (h->unsorted || (tiled && !h->binned_tiles))) {
+        // New particles since the last binning (or a binning for another
+        // brick shape): bin them before moving.
+        rc = bin_particles(h, tiled);
         if (rc) return rc;
         a.P = h->P[h->cur];
         a.n = h->n;
@@ -1221,7 +1346,102 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     const unsigned long long steps_before = h->hcnt.steps;
     double mover_ms = 0.0;
     int64_t launches = 0;
-    if (mixed) {
+    if (tiled) {
+        // Field bricks in shared memory: a particle pauses after bin_interval
+        // pushes; one that walks out of its staged region on the way finishes
+        // those pushes in the overflow kernel.  Between launches the set is
+        // binned brick-major again (removal included).  Every launch pushes
+        // each paused particle at least once, so the launches are bounded by
+        // the push limit.
+        const int bi = h->prm.bin_interval;
+        a.chunk_pushes = bi == 0 ? 128u : (bi > 0 ? (uint32_t)bi : 0u);
+        const MixedConsts k = make_mixed_consts(a);
+        TileSched s{};
+        const CellGrid g = cell_grid(h, true);
+        s.bx = g.bx; s.by = g.by; s.bz = g.bz;
+        s.hx = h->tile_h[0]; s.hy = h->tile_h[1]; s.hz = h->prm.ndim == 3 ? h->tile_h[2] : 0;
+        s.nbx = g.nbx; s.nby = g.nby; s.nbz = g.nbz;
+        s.nbricks = (long long)g.nbx * g.nby * g.nbz;
+        s.cpb = g.bx * g.by * g.bz;
+        s.items = h->tile_items;
+        const int sx = s.bx + 2 * s.hx, sy = s.by + 2 * s.hy, sz = s.bz + 2 * s.hz;
+        tile_smem_bytes(h->prm.ndim, sx, sy, sz, a.time_interp, &s.tile_bytes, &s.tile2_off);
+        if (h->tile_ovf_cap < h->cap) {
+            CK(cudaStreamSynchronize(h->stream));
+            if (h->tile_ovf) CK(cudaFree(h->tile_ovf));
+            h->tile_ovf = nullptr;
+            h->tile_ovf_cap = 0;
+            if (cudaMalloc(&h->tile_ovf, (size_t)h->cap * 12 + 256) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(h, GPAT_ERR_OOM, "tile overflow list");
+            }
+            h->tile_ovf_cap = h->cap;
+        }
+        s.ovf_idx = static_cast<long long *>(h->tile_ovf);
+        s.ovf_done = reinterpret_cast<unsigned int *>(s.ovf_idx + h->cap);
+        s.ovf_count = reinterpret_cast<unsigned long long *>(
+            (reinterpret_cast<uintptr_t>(s.ovf_done + h->cap) + 15) & ~(uintptr_t)15);
+        if (h->tile_dev_n < s.nbricks + 2) {
+            CK(cudaStreamSynchronize(h->stream));
+            if (h->tile_dev) CK(cudaFree(h->tile_dev));
+            h->tile_dev = nullptr;
+            h->tile_dev_n = 0;
+            if (cudaMalloc(&h->tile_dev, sizeof(long long) * (size_t)(s.nbricks + 2)) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(h, GPAT_ERR_OOM, "tile work items");
+            }
+            h->tile_dev_n = s.nbricks + 2;
+        }
+        s.item_prefix = h->tile_dev;
+        s.item_counter = reinterpret_cast<unsigned long long *>(h->tile_dev + s.nbricks + 1);
+        s.nodes = (uint32_t)((sx + 1) * (sy + 1) * (h->prm.ndim == 3 ? sz + 1 : 1));
+        // chunk-planar copies of the frames' records, rebuilt when the records changed
+        const int R = (h->prm.ndim == 2) ? kRec2D : kRec3D;
+        for (int slot = 0; slot < (a.time_interp ? 2 : 1); ++slot) {
+            if (!h->planes[slot]) {
+                if (cudaMalloc(&h->planes[slot], (size_t)R * sizeof(float) * h->ncells) !=
+                    cudaSuccess) {
+                    cudaGetLastError();
+                    return fail(h, GPAT_ERR_OOM, "chunk-planar field records");
+                }
+                h->plane_gen[slot] = 0;
+            }
+            if (h->plane_gen[slot] != h->rec_gen[slot]) {
+                CK(launch_planarize_records(h->rec[slot], h->planes[slot], h->prm.ndim, h->ncells,
+                                            h->stream));
+                h->plane_gen[slot] = h->rec_gen[slot];
+            }
+        }
+        CUtensorMap tm1, tm2;
+        CK(encode_brick_map(&tm1, h->planes[0], h->prm.ndim, h->nxg, h->nyg, h->nzg, sx, sy, sz));
+        CK(encode_brick_map(&tm2, a.time_interp ? h->planes[1] : h->planes[0], h->prm.ndim, h->nxg,
+                            h->nyg, h->nzg, sx, sy, sz));
+        const int64_t max_launches = (int64_t)a.max_pushes + 4;
+        for (;;) {
+            CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
+            CK(cudaMemsetAsync(s.ovf_count, 0, sizeof(unsigned long long), h->stream));
+            a.P = h->P[h->cur];
+            a.n = h->n;
+            s.incl = cell_sort_counts(h->sort_scratch, cell_grid_bins(g));
+            CK(cudaEventRecord(h->ev0, h->stream));
+            CK(launch_mover_tile(a, k, s, tm1, tm2, h->tile_threads, h->sm_count, h->stream));
+            CK(cudaEventRecord(h->ev1, h->stream));
+            ++launches;
+            if (keep_escaped) {
+                rc = collect_escaped(h);
+                if (rc) return rc;
+            }
+            rc = bin_particles(h, true);
+            if (rc) return rc;
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            mover_ms += ms;
+            if (h->hcnt.status) break;   // reported below
+            if (h->hcnt.nactive == 0) break;
+            if (launches > max_launches)
+                return fail(h, GPAT_ERR_DEVICE, "tile mover launches did not finish the interval");
+        }
+    } else if (mixed) {
         // Chunks of bin_interval pushes per particle; between chunks the set is
         // binned by cell again (and removal happens), so lanes of a warp keep
         // gathering neighbouring records while the particles spread out.
@@ -1722,6 +1942,7 @@ struct gpat_batch {
     std::vector<BatchRun> desc;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int graph_key[3] = {-1, -1, -1};       // nlgc, minb, grab of the captured graphs
+    std::vector<void *> graph_scratch;     // each run's binning scratch in the graphs
     gpat_batch_tuning_t tuning{};
     std::string err;
     double last_ms = 0.0;
@@ -1791,6 +2012,8 @@ int capture_graphs(gpat_batch_t *b, int nlgc, int minb, int grab) {
     b->graph_key[0] = nlgc;
     b->graph_key[1] = minb;
     b->graph_key[2] = grab;
+    b->graph_scratch.clear();
+    for (gpat_handle_t *h : b->runs) b->graph_scratch.push_back(h->sort_scratch);
     return GPAT_OK;
 }
 
@@ -1938,8 +2161,11 @@ int gpat_batch_particle_mover(gpat_batch_t *b, const int *mhd_tframe, int nlgc, 
     BCK(cudaSetDevice(b->device));
     int rc = batch_prepare(b, mhd_tframe, nlgc, kperp_kpara, nsteps_interval, num_fine_steps);
     if (rc) return rc;
+    bool same_scratch = b->graph_scratch.size() == b->runs.size();
+    for (size_t r = 0; same_scratch && r < b->runs.size(); ++r)
+        same_scratch = b->graph_scratch[r] == b->runs[r]->sort_scratch;
     if (!b->exec[0] || b->graph_key[0] != (nlgc ? 1 : 0) || b->graph_key[1] != b->tuning.minb ||
-        b->graph_key[2] != b->tuning.grab) {
+        b->graph_key[2] != b->tuning.grab || !same_scratch) {
         rc = capture_graphs(b, nlgc ? 1 : 0, b->tuning.minb, b->tuning.grab);
         if (rc) return rc;
     }

@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -18,6 +19,8 @@ enum : unsigned int {
     kStatusIndexGuard = 1u,   // interpolation cell outside the ghost range
     kStatusNonFinite = 2u,    // NaN/Inf position, momentum or time
     kStatusStepLimit = 4u,    // per-interval push limit reached
+    kStatusTileTimeout = 8u,  // a brick copy into shared memory did not complete in time
+    kStatusTileMiss = 16u,    // a particle outside the staged region of the brick it is binned in
 };
 
 // particle_type as SoA device arrays (capacity entries each).
@@ -187,6 +190,10 @@ cudaError_t launch_calc_fields_gradients(float *full, int ndim, int nxg, int nyg
                                          const double *const *ih = nullptr);
 cudaError_t launch_pack_records(const float *full, float *rec, int ndim, size_t ncells,
                                 cudaStream_t s);
+// Chunk-planar copy of packed records (R / 4 planes of float4, one per
+// 16-byte chunk of the record) for the tile mover.
+cudaError_t launch_planarize_records(const float *rec, float *planes, int ndim, size_t ncells,
+                                     cudaStream_t s);
 // Fluctuation records: 16 floats per node, {db2_slab, db2_2d, lc_slab,
 // lc_2d} x {value, d/dx, d/dy, d/dz}.
 cudaError_t launch_calc_aux_gradients(float *aux, int ndim, int nxg, int nyg, int nzg, double dx,
@@ -219,6 +226,44 @@ cudaError_t launch_mover_mixed_batch(int ndim, bool nlgc, int minb, int parity, 
                                      const unsigned long long *run_n,
                                      unsigned long long *tile_counter,
                                      unsigned long long *nactive_total, cudaStream_t s);
+
+// Split-precision mover with bricks of field records staged in shared memory
+// (mover_tile.cu).  The particle set must be binned brick-major with the same
+// brick shape (CellGrid::tile); incl is the sort's per-bin inclusive prefix.
+struct TileSched {
+    int bx, by, bz;                  // cells per brick and axis (bz = 1 in 2D)
+    int hx, hy, hz;                  // halo: staged cells beyond the brick on each side
+    int nbx, nby, nbz;               // bricks per axis
+    long long nbricks;
+    int cpb;                         // cells per brick
+    int items;                       // particles per work item at most
+    const unsigned int *incl;
+    const long long *item_prefix;    // nbricks + 1 entries, written by the launch
+    unsigned long long *item_counter;
+    uint32_t tile_bytes;             // one frame's staged records
+    uint32_t tile2_off;              // frame 2's staged records, in float4 from the start
+    uint32_t nodes;                  // staged nodes: one chunk plane, in float4
+    // Particles that left the staged region mid-chunk: their indices and the
+    // pushes they had made, finished by the global-gather overflow kernel.
+    long long *ovf_idx;
+    unsigned int *ovf_done;
+    unsigned long long *ovf_count;
+};
+// Dynamic shared memory of one CTA for a staged region of (s + 1) nodes per
+// axis, s = brick cells + 2 halo cells, and the layout values TileSched needs.
+size_t tile_smem_bytes(int ndim, int sx, int sy, int sz, int time_interp, uint32_t *tile_bytes,
+                       uint32_t *tile2_off);
+// TMA tensor map over a frame's chunk-planar records (launch_planarize_records)
+// with a {4, sx+1, sy+1(, sz+1), R/4} box: every chunk plane of the staged
+// region in one copy.
+cudaError_t encode_brick_map(CUtensorMap *m, const float *planes, int ndim, int nxg, int nyg,
+                             int nzg, int sx, int sy, int sz);
+// Work items of the current binning, one persistent tile mover launch
+// (threads per CTA: 256 or 512), then the overflow kernel (its count is
+// zeroed by the caller before).
+cudaError_t launch_mover_tile(const MoverArgs &a, const MixedConsts &c, const TileSched &s,
+                              const CUtensorMap &tm1, const CUtensorMap &tm2, int threads,
+                              int sm_count, cudaStream_t st);
 
 // Quantities of inject_particles_at_large_* (GPAT_LARGE_*).
 struct LargeArgs {
@@ -328,10 +373,22 @@ cudaError_t launch_sync_tracked(const TrackArgs &trk, cudaStream_t s);
 cudaError_t launch_pmax(const DevParticles &P, int64_t n, unsigned long long *bits,
                         cudaStream_t s);
 // Grid geometry for spatial binning of particles (one bin per field cell).
+// tile != 0 orders the bins brick-major for the tile mover: bricks of
+// bx x by x bz cells (nbx x nby x nbz of them, the last ones padded), cells
+// x-fastest inside a brick, and the cell taken with cell_of() from dx, dy, dz
+// exactly as the mover takes it.
 struct CellGrid {
     double xmin, ymin, zmin, idx, idy, idz;
     int nxg, nyg, nzg;
+    int tile;
+    double dx, dy, dz;
+    int bx, by, bz, nbx, nby, nbz;
 };
+// Bins of a grid: cells, or bricks x cells per brick.
+int64_t cell_grid_bins(const CellGrid &g);
+// The per-bin counts inside the sort scratch; after a sort they hold the
+// inclusive prefix (the end of every bin's particle range).
+const unsigned int *cell_sort_counts(const void *scratch, int64_t nbins);
 // Counting sort of the in-box particles of src into dst by cell; drops the
 // rest (remove_particles) and counts escapes.  cnt->nkept gets the new count.
 size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins);

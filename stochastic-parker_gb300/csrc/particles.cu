@@ -3,6 +3,7 @@
 // (calc_particle_distributions) and the quick_check reductions.
 #include <cfloat>
 
+#include "cell_index.cuh"
 #include "device_common.cuh"
 #include "grid_common.cuh"
 #include "track_common.cuh"
@@ -655,7 +656,25 @@ __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int
     if (i < n) {
         const int flag = P.count_flag[i];
         int32_t key = -1;
-        if (flag == 1) {
+        if (flag == 1 && g.tile) {
+            // the mover's own cell (cell_of), so the particle lands in the
+            // brick whose records are staged for it; clamped into the grid
+            int cx, cy, cz = 0;
+            float f;
+            cell_of(P.x[i], g.xmin, g.dx, cx, f);
+            cell_of(P.y[i], g.ymin, g.dy, cy, f);
+            cx = min(max(cx + 2, 0), g.nxg - 1);
+            cy = min(max(cy + 2, 0), g.nyg - 1);
+            if (g.nzg > 1) {
+                cell_of(P.z[i], g.zmin, g.dz, cz, f);
+                cz = min(max(cz + 2, 0), g.nzg - 1);
+            }
+            const int bxi = cx / g.bx, byi = cy / g.by, bzi = cz / g.bz;
+            const int lx = cx - bxi * g.bx, ly = cy - byi * g.by, lz = cz - bzi * g.bz;
+            const int64_t brick = ((int64_t)bzi * g.nby + byi) * g.nbx + bxi;
+            key = (int32_t)(brick * ((int64_t)g.bx * g.by * g.bz) + (lz * g.by + ly) * g.bx + lx);
+            atomicAdd(&counts[key], 1u);
+        } else if (flag == 1) {
             const double px = (P.x[i] - g.xmin) * g.idx;
             const double py = (P.y[i] - g.ymin) * g.idy;
             int cx = (int)floor(fmin(fmax(px, -2.0), (double)g.nxg)) + 2;
@@ -759,6 +778,17 @@ __global__ void __launch_bounds__(256) cell_scatter_kernel(const DevParticles S,
 
 }  // namespace
 
+int64_t cell_grid_bins(const CellGrid &g) {
+    if (g.tile) return (int64_t)g.nbx * g.nby * g.nbz * ((int64_t)g.bx * g.by * g.bz);
+    return (int64_t)g.nxg * g.nyg * g.nzg;
+}
+
+const unsigned int *cell_sort_counts(const void *scratch, int64_t nbins) {
+    const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
+    const long long *tile_sums = static_cast<const long long *>(scratch);
+    return reinterpret_cast<const unsigned int *>(tile_sums + 2 * (ntiles + 1));
+}
+
 size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins) {
     const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
     return (size_t)cap * 4 + (size_t)nbins * 4 + (size_t)(2 * ntiles + 2) * 8 + 256;
@@ -767,7 +797,7 @@ size_t cell_sort_scratch_bytes(int64_t cap, int64_t nbins) {
 cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, int64_t n,
                              const CellGrid &g, void *scratch, DevCounters *cnt,
                              const EscHist &esc, cudaStream_t s) {
-    const int64_t nbins = (int64_t)g.nxg * g.nyg * g.nzg;
+    const int64_t nbins = cell_grid_bins(g);
     const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
     char *q = static_cast<char *>(scratch);
     long long *tile_sums = reinterpret_cast<long long *>(q);
@@ -790,7 +820,7 @@ cudaError_t launch_cell_sort_dev(const DevParticles &src, const DevParticles &ds
                                  unsigned long long *n_dev, int64_t cap, const CellGrid &g,
                                  void *scratch, DevCounters *cnt, const EscHist &esc,
                                  cudaStream_t s) {
-    const int64_t nbins = (int64_t)g.nxg * g.nyg * g.nzg;
+    const int64_t nbins = cell_grid_bins(g);
     const int64_t ntiles = (nbins + kBinTile - 1) / kBinTile;
     char *q = static_cast<char *>(scratch);
     long long *tile_sums = reinterpret_cast<long long *>(q);

@@ -173,6 +173,8 @@ SIGNATURES = {
     "gpat_particle_mover": (C.c_int, [Handle, C.c_int, C.c_int, d, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
     "gpat_split_particle": (C.c_int, [Handle, d, d, C.c_int]),
+    "gpat_set_mover_tiles": (C.c_int, [Handle] + [C.c_int] * 8),
+    "gpat_get_mover_tiles": (C.c_int, [Handle, C.POINTER(C.c_int)]),
     "gpat_split_particle_noalloc": (C.c_int, [P(Particles), i64, i64, d, d, d, d, C.c_void_p,
                                               P(i64), P(i64)]),
     "gpat_calc_particle_distributions": (C.c_int, [Handle, P(d), P(u64)]),

@@ -33,6 +33,7 @@ SOURCES = {
     "particles.cu": ["-fmad=false"],   # injection draws match the oracle bit for bit
     "mover_fp64.cu": ["-fmad=false"],
     "mover_mixed.cu": [],
+    "mover_tile.cu": [],
     "noalloc.cu": [],
     "learned.cu": [],
 }
@@ -72,7 +73,8 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines: dict | None
     out_path = Path(lib_path) if lib_path else LIB_PATH
     srcs = [CSRC / s for s in SOURCES] + [INCLUDE / "gpat_engine.h",
                                           CSRC / "gpat_internal.h", CSRC / "device_common.cuh",
-                                          CSRC / "grid_common.cuh", CSRC / "track_common.cuh"]
+                                          CSRC / "grid_common.cuh", CSRC / "track_common.cuh",
+                                          CSRC / "mixed_body.cuh", CSRC / "cell_index.cuh"]
     if out_path.exists() and not force and not defines:
         lib_mtime = out_path.stat().st_mtime
         if all(s.stat().st_mtime <= lib_mtime for s in srcs):

@@ -488,6 +488,18 @@ class Engine:
             self.h, int(focused_transport), int(nlgc), kperp_kpara, nsteps_interval,
             mhd_tframe, num_fine_steps, int(dump_escaped_dist)))
 
+    def set_mover_tiles(self, bx=0, by=0, bz=0, hx=0, hy=0, hz=0, threads=0, items=0):
+        """Brick shape of the split-precision mover (gpat_set_mover_tiles):
+        bx = 0 gathers field records from device memory, bx > 0 stages
+        bricks of bx x by x bz cells plus hx, hy, hz halo cells per side in
+        shared memory."""
+        self._check(self.lib.gpat_set_mover_tiles(self.h, bx, by, bz, hx, hy, hz, threads, items))
+
+    def mover_tiles(self) -> dict:
+        out = (C.c_int * 8)()
+        self._check(self.lib.gpat_get_mover_tiles(self.h, out))
+        return dict(zip(("bx", "by", "bz", "hx", "hy", "hz", "threads", "items"), list(out)))
+
     def split_particle(self, split_ratio=2.72, pmin_split=2.0, nsteps_interval=10):
         self._check(self.lib.gpat_split_particle(self.h, split_ratio, pmin_split, nsteps_interval))
 
