@@ -9,11 +9,15 @@
 // accumulated in FP32; the optimizer keeps an FP32 master copy (Adam).
 // Features: box-normalised x, y, z; log10(p / p0); div v; |B|; |grad B|;
 // normalised time -- each standardised by the training set's mean and std.
+// Every network evaluation (training, scoring, splitting) runs on the tensor
+// cores through mlp_mma.cuh: BF16 weights and activations, FP32 accumulation.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cfloat>
 
 #include "device_common.cuh"
+#include "mlp_mma.cuh"
 
 namespace gpat {
 namespace {
@@ -32,51 +36,6 @@ __device__ __forceinline__ void clone_particle(const DevParticles &P, int64_t i,
     P.origin[j] = P.origin[i]; P.nsteps_tracked[j] = P.nsteps_tracked[i];
     P.nsteps_pushed[j] = P.nsteps_pushed[i]; P.tag_injected[j] = P.tag_injected[i];
     P.tag_splitted[j] = P.tag_splitted[i]; P.rng_ctr[j] = P.rng_ctr[i];
-}
-
-__device__ __forceinline__ float sigm(float a) { return 1.0f / (1.0f + expf(-a)); }
-__device__ __forceinline__ float silu(float a) { return a * sigm(a); }
-__device__ __forceinline__ float dsilu(float a) {
-    const float s = sigm(a);
-    return s * (1.0f + a * (1.0f - s));
-}
-
-// Weights (BF16 in global memory) -> FP32 in shared memory for one block.
-__device__ __forceinline__ void load_weights(const __nv_bfloat16 *w16, float *sw) {
-    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) sw[k] = __bfloat162float(w16[k]);
-    __syncthreads();
-}
-
-// Forward pass of one sample; pre-activations go to a1..a3 when given.
-__device__ float mlp_forward(const float *sw, const float h0[kIn], float *a1, float *a2,
-                             float *a3, int stride) {
-    float h1[kH], h2[kH];
-#pragma unroll 4
-    for (int i = 0; i < kH; ++i) {
-        float s = sw[kOffB1 + i];
-#pragma unroll
-        for (int j = 0; j < kIn; ++j) s = fmaf(sw[kOffW1 + i * kIn + j], h0[j], s);
-        if (a1) a1[i * stride] = s;
-        h1[i] = silu(s);
-    }
-#pragma unroll 2
-    for (int i = 0; i < kH; ++i) {
-        float s = sw[kOffB2 + i];
-#pragma unroll 16
-        for (int j = 0; j < kH; ++j) s = fmaf(sw[kOffW2 + i * kH + j], h1[j], s);
-        if (a2) a2[i * stride] = s;
-        h2[i] = silu(s);
-    }
-    float z = sw[kOffB4];
-#pragma unroll 2
-    for (int i = 0; i < kH; ++i) {
-        float s = sw[kOffB3 + i];
-#pragma unroll 16
-        for (int j = 0; j < kH; ++j) s = fmaf(sw[kOffW3 + i * kH + j], h2[j], s);
-        if (a3) a3[i * stride] = s;
-        z = fmaf(sw[kOffW4 + i], silu(s), z);
-    }
-    return z;
 }
 
 __device__ __forceinline__ void standardise(const float *x, const float *mean, const float *istd,
@@ -170,135 +129,203 @@ __global__ void label_kernel(const int32_t *tags, int64_t nrec, const float *p_b
 }
 
 // ---------------------------------------------------------------------------
-// Training: forward with stored pre-activations, per-sample deltas, weight
-// gradients as sample-chunked outer-product sums, Adam.
+// Training step on the tensor cores: one CTA takes 128 samples (8 warps x 16),
+// runs the forward pass, the loss, and the backward pass with register-
+// resident fragments, then stages the activations h0..h3 and the deltas
+// d1..d3 in shared memory feature-major (BF16) and forms the weight
+// gradients dW_l = d_l^T h_(l-1) as mma products whose K dimension is the
+// CTA's samples; they are added to the FP32 gradient with atomics.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) train_forward_kernel(
-    const __nv_bfloat16 *w16, const float *norm, const float *x, const float *y,
-    const int64_t *index, int64_t b, float *h0s, float *a1, float *a2, float *a3, float *dz,
-    float *loss) {
-    extern __shared__ float sw[];
-    load_weights(w16, sw);
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    float l = 0.0f;
-    if (s < b) {
-        const int64_t r = index ? index[s] : s;
-        float h0[kIn];
-        standardise(x + (size_t)r * kIn, norm, norm + kIn, h0);
+constexpr int kTS = 128;          // samples per CTA
+constexpr int kTP = kTS + 8;      // staging row (bf16): 68 words, lanes land in distinct banks
+struct TrainSmem {
+    mma_mlp::Smem w;
+    __nv_bfloat16 h0T[kIn * kTP];       // standardised inputs [feature][sample]
+    __nv_bfloat16 hT[3][kH * kTP];      // h1, h2, h3
+    __nv_bfloat16 dT[3][kH * kTP];      // d1, d2, d3
+    float dz[kTS];
+};
+
+__device__ __forceinline__ void stage_frag(__nv_bfloat16 *T, const uint32_t (&a)[4][4], int row0,
+                                           int g, int t) {
 #pragma unroll
-        for (int j = 0; j < kIn; ++j) h0s[(size_t)s * kIn + j] = h0[j];
-        const float z = mlp_forward(sw, h0, a1 + s, a2 + s, a3 + s, (int)b);
-        const float t = y[r];
-        // BCE with logits: max(z, 0) - t z + log(1 + exp(-|z|))
-        l = fmaxf(z, 0.0f) - t * z + log1pf(expf(-fabsf(z)));
-        dz[s] = (sigm(z) - t) / (float)b;
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int col = 16 * kk + 2 * t + ((e & 2) ? 8 : 0);
+            const int row = row0 + g + ((e & 1) ? 8 : 0);
+            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&a[kk][e]);
+            T[col * kTP + row] = v.x;
+            T[(col + 1) * kTP + row] = v.y;
+        }
+}
+
+// delta = (incoming C tiles) * silu'(a) as packed A fragments.
+__device__ __forceinline__ void times_dsilu(const float (&c)[8][4], const uint32_t (&ds)[4][4],
+                                            uint32_t (&d)[4][4]) {
+    using namespace mma_mlp;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+        const float *p = c[2 * kk], *q = c[2 * kk + 1];
+        d[kk][0] = pack(p[0] * lo_of(ds[kk][0]), p[1] * hi_of(ds[kk][0]));
+        d[kk][1] = pack(p[2] * lo_of(ds[kk][1]), p[3] * hi_of(ds[kk][1]));
+        d[kk][2] = pack(q[0] * lo_of(ds[kk][2]), q[1] * hi_of(ds[kk][2]));
+        d[kk][3] = pack(q[2] * lo_of(ds[kk][3]), q[3] * hi_of(ds[kk][3]));
     }
+}
+
+// dH = D x W (W as its transposed image): C tiles over the 64 inputs of W.
+__device__ __forceinline__ void back_product(const uint32_t (&d)[4][4], const __nv_bfloat16 *wt,
+                                             int g, int t, float (&c)[8][4]) {
+    using namespace mma_mlp;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            uint32_t b0, b1;
+            bfrag(wt, kS, 8 * nt, 16 * kk, g, t, b0, b1);
+            mma16816(c[nt], d[kk], b0, b1);
+        }
+    }
+}
+
+// One 16 x 8 tile of dW = D^T H over the staged samples: rows i0.., columns j0..
+__device__ __forceinline__ void wgrad_tile(const __nv_bfloat16 *DT, const __nv_bfloat16 *HT, int i0,
+                                           int j0, int g, int t, float (&acc)[4]) {
+    using namespace mma_mlp;
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.0f;
+#pragma unroll 2
+    for (int s = 0; s < kTS; s += 16) {
+        uint32_t a[4];
+        a[0] = *reinterpret_cast<const uint32_t *>(DT + (i0 + g) * kTP + s + 2 * t);
+        a[1] = *reinterpret_cast<const uint32_t *>(DT + (i0 + g + 8) * kTP + s + 2 * t);
+        a[2] = *reinterpret_cast<const uint32_t *>(DT + (i0 + g) * kTP + s + 8 + 2 * t);
+        a[3] = *reinterpret_cast<const uint32_t *>(DT + (i0 + g + 8) * kTP + s + 8 + 2 * t);
+        const uint32_t b0 = *reinterpret_cast<const uint32_t *>(HT + (j0 + g) * kTP + s + 2 * t);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t *>(HT + (j0 + g) * kTP + s + 8 + 2 * t);
+        mma16816(acc, a, b0, b1);
+    }
+}
+
+__device__ __forceinline__ void add_tile(float *gw, int nin, int i0, int j0, int g, int t,
+                                         const float (&acc)[4]) {
+    atomicAdd(&gw[(i0 + g) * nin + j0 + 2 * t], acc[0]);
+    atomicAdd(&gw[(i0 + g) * nin + j0 + 2 * t + 1], acc[1]);
+    atomicAdd(&gw[(i0 + g + 8) * nin + j0 + 2 * t], acc[2]);
+    atomicAdd(&gw[(i0 + g + 8) * nin + j0 + 2 * t + 1], acc[3]);
+}
+
+__global__ void __launch_bounds__(256, 1) train_mma_kernel(
+    const __nv_bfloat16 *w16, const float *norm, const float *x, const float *y,
+    const int64_t *index, int64_t b, float *grad, float *loss) {
+    using namespace mma_mlp;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TrainSmem &S = *reinterpret_cast<TrainSmem *>(smem_raw);
+    load_smem(w16, S.w, true);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int row0 = 16 * warp;
+    const int64_t sg0 = (int64_t)blockIdx.x * kTS + row0 + g, sg1 = sg0 + 8;
+    const bool v0 = sg0 < b, v1 = sg1 < b;
+    const int64_t r0 = v0 ? (index ? index[sg0] : sg0) : 0, r1 = v1 ? (index ? index[sg1] : sg1) : 0;
+    // standardised inputs 2t, 2t+1 of rows g and g+8 (padded samples: zero)
+    const float m0 = norm[2 * t], m1 = norm[2 * t + 1];
+    const float i0s = norm[kIn + 2 * t], i1s = norm[kIn + 2 * t + 1];
+    float x0g = 0.0f, x1g = 0.0f, x0h = 0.0f, x1h = 0.0f;
+    if (v0) { x0g = (x[r0 * kIn + 2 * t] - m0) * i0s; x1g = (x[r0 * kIn + 2 * t + 1] - m1) * i1s; }
+    if (v1) { x0h = (x[r1 * kIn + 2 * t] - m0) * i0s; x1h = (x[r1 * kIn + 2 * t + 1] - m1) * i1s; }
+    uint32_t a1[4];
+    input_frag(x0g, x1g, x0h, x1h, a1);
+    {
+        const __nv_bfloat162 u = *reinterpret_cast<const __nv_bfloat162 *>(&a1[0]);
+        const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&a1[1]);
+        S.h0T[(2 * t) * kTP + row0 + g] = u.x;
+        S.h0T[(2 * t + 1) * kTP + row0 + g] = u.y;
+        S.h0T[(2 * t) * kTP + row0 + g + 8] = v.x;
+        S.h0T[(2 * t + 1) * kTP + row0 + g + 8] = v.y;
+    }
+    Stash st;
+    float zr[2];
+    forward_tile<true>(S.w, a1, g, t, zr, &st);
+    // loss and dL/dz (lanes with t == 0 hold z of rows g and g + 8)
+    float l = 0.0f, dz0 = 0.0f, dz1 = 0.0f;
+    if (t == 0) {
+        if (v0) {
+            const float yy = y[r0], z = zr[0];
+            l += fmaxf(z, 0.0f) - yy * z + log1pf(__expf(-fabsf(z)));
+            dz0 = (sigm(z) - yy) / (float)b;
+        }
+        if (v1) {
+            const float yy = y[r1], z = zr[1];
+            l += fmaxf(z, 0.0f) - yy * z + log1pf(__expf(-fabsf(z)));
+            dz1 = (sigm(z) - yy) / (float)b;
+        }
+        S.dz[row0 + g] = dz0;
+        S.dz[row0 + g + 8] = dz1;
+    }
+    dz0 = __shfl_sync(0xffffffffu, dz0, 4 * g);
+    dz1 = __shfl_sync(0xffffffffu, dz1, 4 * g);
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-    if ((threadIdx.x & 31) == 0 && l != 0.0f) atomicAdd(loss, l / (float)b);
-}
-
-// d3 = dz W4 * silu'(a3), d2 = (W3^T d3) * silu'(a2), d1 = (W2^T d2) * silu'(a1);
-// pre-activation arrays are overwritten by the deltas (column s of [64][b]).
-__global__ void __launch_bounds__(128) train_backward_kernel(const __nv_bfloat16 *w16,
-                                                             int64_t b, const float *dz,
-                                                             float *a1, float *a2, float *a3,
-                                                             float *h1s, float *h2s, float *h3s) {
-    extern __shared__ float sw[];
-    load_weights(w16, sw);
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= b) return;
-    const float g = dz[s];
-    float d[kH], dn[kH];
-#pragma unroll 8
-    for (int i = 0; i < kH; ++i) {
-        const float a = a3[i * b + s];
-        h3s[i * b + s] = silu(a);
-        d[i] = g * sw[kOffW4 + i] * dsilu(a);
-        a3[i * b + s] = d[i];
-    }
-#pragma unroll 4
-    for (int j = 0; j < kH; ++j) {
-        float acc = 0.0f;
-#pragma unroll 16
-        for (int i = 0; i < kH; ++i) acc = fmaf(sw[kOffW3 + i * kH + j], d[i], acc);
-        const float a = a2[j * b + s];
-        h2s[j * b + s] = silu(a);
-        dn[j] = acc * dsilu(a);
-        a2[j * b + s] = dn[j];
-    }
-#pragma unroll 4
-    for (int j = 0; j < kH; ++j) {
-        float acc = 0.0f;
-#pragma unroll 16
-        for (int i = 0; i < kH; ++i) acc = fmaf(sw[kOffW2 + i * kH + j], dn[i], acc);
-        const float a = a1[j * b + s];
-        h1s[j * b + s] = silu(a);
-        a1[j * b + s] = acc * dsilu(a);
-    }
-}
-
-// grad[W][i][j] += sum_s delta[i][s] * prev[j][s] (+ bias: sum_s delta[i][s])
-// for one layer, over the sample chunk of this block.  Layouts [rows][b].
-constexpr int kChunk = 256;
-__global__ void __launch_bounds__(256) weight_grad_kernel(const float *delta, int nout,
-                                                          const float *prev, int nin,
-                                                          bool prev_sample_major, int64_t b,
-                                                          float *gw, float *gb) {
-    __shared__ float sd[kH][33], sp[kH][33];
-    const int64_t s0 = (int64_t)blockIdx.x * kChunk;
-    const int64_t s1 = min(s0 + kChunk, b);
-    const int nent = nout * nin;
-    float acc[16], accb[1] = {0.0f};
-    for (int k = 0; k < 16; ++k) acc[k] = 0.0f;
-    for (int64_t c = s0; c < s1; c += 32) {
-        const int m = (int)min((int64_t)32, s1 - c);
-        for (int k = threadIdx.x; k < kH * 32; k += blockDim.x) {
-            const int row = k / 32, col = k % 32;
-            float dv = 0.0f, pv = 0.0f;
-            if (col < m) {
-                if (row < nout) dv = delta[(size_t)row * b + c + col];
-                if (row < nin)
-                    pv = prev_sample_major ? prev[(size_t)(c + col) * nin + row]
-                                           : prev[(size_t)row * b + c + col];
-            }
-            sd[row][col] = dv;
-            sp[row][col] = pv;
+    if (lane == 0 && l != 0.0f) atomicAdd(loss, l / (float)b);
+    // backward: d3 = dz W4 silu'(a3); d2 = (d3 W3) silu'(a2); d1 = (d2 W2) silu'(a1)
+    uint32_t d3[4][4], d2[4][4], d1[4][4];
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int col = 16 * kk + 2 * t + ((e & 2) ? 8 : 0);
+            const float dz = (e & 1) ? dz1 : dz0;
+            const uint32_t ds = st.ds[2][kk][e];
+            d3[kk][e] = pack(dz * S.w.w4f[col] * lo_of(ds), dz * S.w.w4f[col + 1] * hi_of(ds));
         }
-        __syncthreads();
-        for (int k = 0; k < 16; ++k) {
-            const int e = threadIdx.x + k * 256;
-            if (e < nent) {
-                const int i = e / nin, j = e % nin;
-                float a = acc[k];
-                for (int t = 0; t < m; ++t) a = fmaf(sd[i][t], sp[j][t], a);
-                acc[k] = a;
-            }
+    float c[8][4];
+    back_product(d3, S.w.w3t, g, t, c);
+    times_dsilu(c, st.ds[1], d2);
+    back_product(d2, S.w.w2t, g, t, c);
+    times_dsilu(c, st.ds[0], d1);
+    // stage h1..h3 and d1..d3 feature-major
+    stage_frag(S.hT[0], st.h[0], row0, g, t);
+    stage_frag(S.hT[1], st.h[1], row0, g, t);
+    stage_frag(S.hT[2], st.h[2], row0, g, t);
+    stage_frag(S.dT[0], d1, row0, g, t);
+    stage_frag(S.dT[1], d2, row0, g, t);
+    stage_frag(S.dT[2], d3, row0, g, t);
+    __syncthreads();
+    // weight gradients: dW3 and dW2 (4 x 8 tiles each, 4 per warp), dW1 (4 tiles)
+    float acc[4];
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int tile = 4 * warp + q, i0 = 16 * (tile >> 3), j0 = 8 * (tile & 7);
+        wgrad_tile(S.dT[2], S.hT[1], i0, j0, g, t, acc);
+        add_tile(grad + kOffW3, kH, i0, j0, g, t, acc);
+        wgrad_tile(S.dT[1], S.hT[0], i0, j0, g, t, acc);
+        add_tile(grad + kOffW2, kH, i0, j0, g, t, acc);
+    }
+    if (warp < 4) {
+        wgrad_tile(S.dT[0], S.h0T, 16 * warp, 0, g, t, acc);
+        add_tile(grad + kOffW1, kIn, 16 * warp, 0, g, t, acc);
+    }
+    // biases (sum of deltas over the samples) and the output layer
+    const int tid = threadIdx.x;
+    if (tid < 3 * kH) {
+        const int layer = tid / kH, i = tid % kH;
+        const __nv_bfloat16 *row = S.dT[layer] + i * kTP;
+        float s = 0.0f;
+        for (int k = 0; k < kTS; ++k) s += __bfloat162float(row[k]);
+        const int off = layer == 0 ? kOffB1 : (layer == 1 ? kOffB2 : kOffB3);
+        if (s != 0.0f) atomicAdd(&grad[off + i], s);
+    } else {
+        const int i = tid - 3 * kH;   // 0..63
+        const __nv_bfloat16 *row = S.hT[2] + i * kTP;
+        float s = 0.0f, sb = 0.0f;
+        for (int k = 0; k < kTS; ++k) {
+            s = fmaf(S.dz[k], __bfloat162float(row[k]), s);
+            sb += S.dz[k];
         }
-        if (threadIdx.x < nout)
-            for (int t = 0; t < m; ++t) accb[0] += sd[threadIdx.x][t];
-        __syncthreads();
-    }
-    for (int k = 0; k < 16; ++k) {
-        const int e = threadIdx.x + k * 256;
-        if (e < nent && acc[k] != 0.0f) atomicAdd(&gw[e], acc[k]);
-    }
-    if (threadIdx.x < nout && accb[0] != 0.0f) atomicAdd(&gb[threadIdx.x], accb[0]);
-}
-
-// Layer-4 gradient: gw[i] = sum_s dz[s] h3[i][s], gb = sum_s dz[s].
-__global__ void __launch_bounds__(256) out_grad_kernel(const float *dz, const float *h3, int64_t b,
-                                                       float *gw, float *gb) {
-    const int64_t s0 = (int64_t)blockIdx.x * kChunk;
-    const int64_t s1 = min(s0 + kChunk, b);
-    const int i = threadIdx.x;
-    if (i < kH) {
-        float a = 0.0f;
-        for (int64_t s = s0; s < s1; ++s) a = fmaf(dz[s], h3[(size_t)i * b + s], a);
-        if (a != 0.0f) atomicAdd(&gw[i], a);
-    } else if (i == kH) {
-        float a = 0.0f;
-        for (int64_t s = s0; s < s1; ++s) a += dz[s];
-        if (a != 0.0f) atomicAdd(gb, a);
+        if (s != 0.0f) atomicAdd(&grad[kOffW4 + i], s);
+        if (i == 0 && sb != 0.0f) atomicAdd(&grad[kOffB4], sb);
     }
 }
 
@@ -323,16 +350,34 @@ __global__ void to_bf16_kernel(const float *master, __nv_bfloat16 *w16) {
     if (k < kMlpParams) w16[k] = __float2bfloat16_rn(master[k]);
 }
 
-// Forward on given feature rows (tests, scoring).
-__global__ void __launch_bounds__(128) infer_kernel(const __nv_bfloat16 *w16, const float *norm,
-                                                    const float *x, int64_t n, float *z) {
-    extern __shared__ float sw[];
-    load_weights(w16, sw);
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    float h0[kIn];
-    standardise(x + (size_t)s * kIn, norm, norm + kIn, h0);
-    z[s] = mlp_forward(sw, h0, nullptr, nullptr, nullptr, 1);
+// Forward on given feature rows (tests, scoring): each warp takes tiles of
+// 16 rows.
+__global__ void __launch_bounds__(128) infer_mma_kernel(const __nv_bfloat16 *w16,
+                                                        const float *norm, const float *x,
+                                                        int64_t n, float *z) {
+    using namespace mma_mlp;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+    load_smem(w16, S, false);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const float m0 = norm[2 * t], m1 = norm[2 * t + 1];
+    const float i0s = norm[kIn + 2 * t], i1s = norm[kIn + 2 * t + 1];
+    const int64_t tiles = (n + 15) / 16;
+    for (int64_t tl = (int64_t)blockIdx.x * 4 + warp; tl < tiles; tl += (int64_t)gridDim.x * 4) {
+        const int64_t r0 = 16 * tl + g, r1 = r0 + 8;
+        float x0g = 0.0f, x1g = 0.0f, x0h = 0.0f, x1h = 0.0f;
+        if (r0 < n) { x0g = (x[r0 * kIn + 2 * t] - m0) * i0s; x1g = (x[r0 * kIn + 2 * t + 1] - m1) * i1s; }
+        if (r1 < n) { x0h = (x[r1 * kIn + 2 * t] - m0) * i0s; x1h = (x[r1 * kIn + 2 * t + 1] - m1) * i1s; }
+        uint32_t a1[4];
+        input_frag(x0g, x1g, x0h, x1h, a1);
+        float zr[2];
+        forward_tile<false>(S, a1, g, t, zr, nullptr);
+        if (t == 0) {
+            if (r0 < n) z[r0] = zr[0];
+            if (r1 < n) z[r1] = zr[1];
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -347,16 +392,25 @@ template <int NDIM>
 __global__ void __launch_bounds__(128) weighted_split_kernel(
     const __nv_bfloat16 *w16, const float *norm, const FeatureArgs g, DevParticles P, int64_t n,
     int64_t cap, WSplitArgs a, unsigned long long *count, DevCounters *cnt) {
-    extern __shared__ float sw[];
-    load_weights(w16, sw);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    mma_mlp::Smem &S = *reinterpret_cast<mma_mlp::Smem *>(smem_raw);
+    mma_mlp::load_smem(w16, S, false);
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int j = 0;
-    double w = 0.0;
-    if (i < n && P.count_flag[i] == 1) {
-        float f[kIn], h0[kIn];
+    const bool live = i < n && P.count_flag[i] == 1;
+    float h0[kIn];
+    if (live) {
+        float f[kIn];
         particle_features<NDIM>(g, P, i, f);
         standardise(f, norm, norm + kIn, h0);
-        const float z = mlp_forward(sw, h0, nullptr, nullptr, nullptr, 1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kIn; ++k) h0[k] = 0.0f;
+    }
+    const float z = mma_mlp::warp_forward(S, h0);   // every lane of the warp takes part
+    int j = 0;
+    double w = 0.0;
+    if (live) {
         const double wt = a.w_ref * exp(-((double)fminf(fmaxf(z, -60.0f), 60.0f) - a.z_ref));
         w = P.weight[i];
         if (w > wt * a.sqrt_ratio) {
@@ -421,14 +475,24 @@ template <int NDIM>
 __global__ void __launch_bounds__(128) score_kernel(const __nv_bfloat16 *w16, const float *norm,
                                                     const FeatureArgs g, const DevParticles P,
                                                     int64_t n, float *z, int *zmax_key) {
-    extern __shared__ float sw[];
-    load_weights(w16, sw);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    mma_mlp::Smem &S = *reinterpret_cast<mma_mlp::Smem *>(smem_raw);
+    mma_mlp::load_smem(w16, S, false);
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || P.count_flag[i] != 1) return;
-    float f[kIn], h0[kIn];
-    particle_features<NDIM>(g, P, i, f);
-    standardise(f, norm, norm + kIn, h0);
-    const float v = fminf(fmaxf(mlp_forward(sw, h0, nullptr, nullptr, nullptr, 1), -60.0f), 60.0f);
+    const bool live = i < n && P.count_flag[i] == 1;
+    float h0[kIn];
+    if (live) {
+        float f[kIn];
+        particle_features<NDIM>(g, P, i, f);
+        standardise(f, norm, norm + kIn, h0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kIn; ++k) h0[k] = 0.0f;
+    }
+    const float zw = mma_mlp::warp_forward(S, h0);   // every lane of the warp takes part
+    if (!live) return;
+    const float v = fminf(fmaxf(zw, -60.0f), 60.0f);
     z[i] = v;
     const int b = __float_as_int(v);
     atomicMax(zmax_key, b >= 0 ? b : b ^ 0x7FFFFFFF);
@@ -459,17 +523,15 @@ __global__ void tail_kernel(const DevParticles P, int64_t n, double pthr,
 
 }  // namespace
 
-size_t mlp_shared_bytes() { return sizeof(float) * kMlpParams; }
+size_t mlp_shared_bytes() { return sizeof(mma_mlp::Smem); }
 
 cudaError_t mlp_set_kernel_attributes() {
     const int smem = (int)mlp_shared_bytes();
-    cudaError_t e = cudaFuncSetAttribute(train_forward_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(train_mma_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(TrainSmem));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(train_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(infer_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(weighted_split_kernel<2>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -491,7 +553,9 @@ cudaError_t launch_to_bf16(const float *master, __nv_bfloat16 *w16, cudaStream_t
 cudaError_t launch_mlp_infer(const __nv_bfloat16 *w16, const float *norm, const float *x, int64_t n,
                              float *z, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    infer_kernel<<<(unsigned)((n + 127) / 128), 128, mlp_shared_bytes(), s>>>(w16, norm, x, n, z);
+    const int64_t tiles = (n + 15) / 16;
+    const unsigned blocks = (unsigned)std::min<int64_t>((tiles + 3) / 4, 65535);
+    infer_mma_kernel<<<blocks, 128, mlp_shared_bytes(), s>>>(w16, norm, x, n, z);
     return cudaGetLastError();
 }
 
@@ -499,20 +563,10 @@ cudaError_t launch_mlp_train_step(const MlpTrainBuffers &t, const __nv_bfloat16 
                                   const float *norm, const float *x, const float *y,
                                   const int64_t *index, int64_t b, float *grad, float *loss,
                                   cudaStream_t s) {
-    const unsigned blocks = (unsigned)((b + 127) / 128);
-    train_forward_kernel<<<blocks, 128, mlp_shared_bytes(), s>>>(w16, norm, x, y, index, b, t.h0,
-                                                                 t.a1, t.a2, t.a3, t.dz, loss);
-    train_backward_kernel<<<blocks, 128, mlp_shared_bytes(), s>>>(w16, b, t.dz, t.a1, t.a2, t.a3,
-                                                                  t.h1, t.h2, t.h3);
-    const unsigned chunks = (unsigned)((b + kChunk - 1) / kChunk);
-    // after the backward pass a1..a3 hold the deltas d1..d3
-    weight_grad_kernel<<<chunks, 256, 0, s>>>(t.a1, kH, t.h0, kIn, true, b, grad + kOffW1,
-                                              grad + kOffB1);
-    weight_grad_kernel<<<chunks, 256, 0, s>>>(t.a2, kH, t.h1, kH, false, b, grad + kOffW2,
-                                              grad + kOffB2);
-    weight_grad_kernel<<<chunks, 256, 0, s>>>(t.a3, kH, t.h2, kH, false, b, grad + kOffW3,
-                                              grad + kOffB3);
-    out_grad_kernel<<<chunks, 128, 0, s>>>(t.dz, t.h3, b, grad + kOffW4, grad + kOffB4);
+    if (b <= 0) return cudaSuccess;
+    (void)t;   // the tensor-core step keeps its intermediates in shared memory
+    const unsigned blocks = (unsigned)((b + kTS - 1) / kTS);
+    train_mma_kernel<<<blocks, 256, sizeof(TrainSmem), s>>>(w16, norm, x, y, index, b, grad, loss);
     return cudaGetLastError();
 }
 

@@ -22,13 +22,21 @@ def test_forward_and_gradient_match_oracle():
     m.set_params(params, norm)
     x = rng.normal(size=(5000, 8)).astype(np.float32)
     z = m.forward(x)
-    zr = mo.forward(params, norm.astype(np.float64), x)
-    np.testing.assert_allclose(z, zr, rtol=1e-4, atol=1e-4)
+    # the tensor-core kernels round inputs, activations and deltas to BF16
+    # (FP32 accumulation); the oracle restates that rounding in float64
+    zr = mo.forward(params, norm.astype(np.float64), x, round_act=True)
+    np.testing.assert_allclose(z, zr, rtol=2e-3, atol=2e-3)
+    # and against the unrounded network: BF16 operand error only
+    z64 = mo.forward(params, norm.astype(np.float64), x)
+    assert np.abs(z - z64).max() < 0.05 * max(1.0, np.abs(z64).max())
     y = (rng.random(5000) < 0.2).astype(np.float32)
     loss, g = m.loss_grad(x, y)
-    lr, gr = mo.loss_grad(params, norm.astype(np.float64), x, y)
-    assert abs(loss - lr) < 1e-4 * max(1.0, abs(lr))
-    np.testing.assert_allclose(g, gr, rtol=2e-3, atol=2e-3 * np.abs(gr).max())
+    lr, gr = mo.loss_grad(params, norm.astype(np.float64), x, y, round_act=True)
+    assert abs(loss - lr) < 1e-3 * max(1.0, abs(lr))
+    np.testing.assert_allclose(g, gr, rtol=1e-2, atol=5e-3 * np.abs(gr).max())
+    lr64, gr64 = mo.loss_grad(params, norm.astype(np.float64), x, y)
+    cos = float(g @ gr64 / (np.linalg.norm(g) * np.linalg.norm(gr64)))
+    assert cos > 0.999, cos
     p2, n2 = m.get_params()
     assert np.array_equal(p2, params) and np.array_equal(n2, norm)
     m.close()
