@@ -42,8 +42,13 @@ int device_slots(DeviceSlots **out) {
     DeviceSlots &s = g_slots[dev];
     if (!s.ready) {
         void *scratch = nullptr, *counters = nullptr;
-        if (cudaGetSymbolAddress(&scratch, g_split_scratch) != cudaSuccess) return GPAT_ERR_CUDA;
-        if (cudaGetSymbolAddress(&counters, g_split_counters) != cudaSuccess) return GPAT_ERR_CUDA;
+        // a failed lookup leaves its error pending: clear it, so that the
+        // next call does not pick it up from cudaGetLastError()
+        if (cudaGetSymbolAddress(&scratch, g_split_scratch) != cudaSuccess ||
+            cudaGetSymbolAddress(&counters, g_split_counters) != cudaSuccess) {
+            cudaGetLastError();
+            return GPAT_ERR_CUDA;
+        }
         s.scratch = scratch;
         s.counters = static_cast<DevCounters *>(counters);
         s.ready = true;

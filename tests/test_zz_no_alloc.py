@@ -81,6 +81,55 @@ def test_split_noalloc_matches_split_particle_twice():
     eng.close()
 
 
+def test_split_noalloc_warm_up_call():
+    """The n = 0 call a driver makes on each device before its time loop (it
+    loads the device code and looks up the scratch) returns GPAT_OK."""
+    torch = pytest.importorskip("torch")
+    lib = _abi.load()
+    dev = {name: torch.zeros(16, dtype=getattr(torch, TORCH_DTYPES[t]), device="cuda")
+           for name, t in _abi.PARTICLE_FIELDS}
+    st = _as_struct(dev)
+    n_out, n_split = C.c_int64(-1), C.c_int64(-1)
+    rc = lib.gpat_split_particle_noalloc(C.byref(st), 0, 16, 2.72, 2.0, 0.1, 100.0, None,
+                                         C.byref(n_out), C.byref(n_split))
+    assert rc == _abi.GPAT_OK and n_out.value == 0 and n_split.value == 0
+
+
+def test_split_noalloc_capacity_like_split_particle():
+    """capacity below n + candidates: GPAT_ERR_CAPACITY, n_out = capacity, and
+    the same particles as gpat_split_particle on a handle with that nptl_max."""
+    torch = pytest.importorskip("torch")
+    from gpat.engine import GPATError
+    lib = _abi.load()
+    p0, pmax, ratio, pmin_split = 0.1, 100.0, 2.72, 2.0
+    n0, cap = 3000, 4000
+    cfg = make_mhd_config(32, 32, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.02)
+    eng = Engine(make_params(p0=p0, pmin=p0, pmax=pmax, nptl_max=cap, ndim=2), cfg, 0)
+    eng.set_tstamps([0.0, 0.02])
+    eng.inject_particles_at_x(n0, 0.5, 1e-6, 1, 1.0, 1)
+    start = eng.get_particles()
+    start.arrays["p"][:] = p0 * np.exp(np.random.default_rng(99).uniform(0.0, 3.0, n0))
+    eng.put_particles(start)
+    # split_times is 0 after injection: candidates have p > pmin_split p0
+    wanted = int(np.sum(start.arrays["p"] > pmin_split * p0))
+    assert n0 + wanted > cap
+    with pytest.raises(GPATError):
+        eng.split_particle(ratio, pmin_split, 10)
+    ref = eng.get_particles()
+    assert len(ref) == cap
+    dev = _device_arrays(torch, start, cap)
+    st = _as_struct(dev)
+    torch.cuda.synchronize()
+    n_out, n_split = C.c_int64(), C.c_int64()
+    rc = lib.gpat_split_particle_noalloc(C.byref(st), n0, cap, ratio, pmin_split, p0, pmax, None,
+                                         C.byref(n_out), C.byref(n_split))
+    assert rc == _abi.GPAT_ERR_CAPACITY and n_out.value == cap and n_split.value == cap - n0
+    got = _to_host(dev, cap)
+    for name, _ in _abi.PARTICLE_FIELDS:
+        assert np.array_equal(got[name], ref.arrays[name]), name
+    eng.close()
+
+
 def test_split_noalloc_rejects_sizes_beyond_its_scratch():
     lib = _abi.load()
     st = _abi.Particles()
