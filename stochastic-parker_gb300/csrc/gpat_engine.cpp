@@ -63,6 +63,14 @@ struct gpat_handle {
     int tile_threads = 512;
     int tile_items = 4096;
     bool binned_tiles = false;
+    // chunked split-precision launches: paused flag per index, the particles
+    // the last binning put in spatial bins (the rest finished the interval)
+    // and the bins of that binning
+    uint8_t *pause = nullptr;
+    int64_t pause_cap = 0;
+    int64_t n_active = 0;
+    int64_t last_sort_bins = 0;
+    unsigned int n_spatial_host = 0;
     long long *tile_dev = nullptr;   // item prefix (nbricks + 1) and the item counter
     int64_t tile_dev_n = 0;
     void *tile_ovf = nullptr;        // overflow list: indices, pushes done, count
@@ -339,6 +347,7 @@ int mover_args(gpat_handle_t *h, int mhd_tframe, int nsteps_interval, int num_fi
     a.key1 = (uint32_t)(p.seed >> 32);
     a.trk = track_args(h);
     a.cnt = h->dcnt;
+    a.pause = nullptr;
     return GPAT_OK;
 }
 
@@ -379,9 +388,20 @@ EscHist escaped_hist(const gpat_handle_t *h) {
 }
 
 // tiled: brick-major bins for the tile mover (the sort scratch grows to fit).
-int bin_particles(gpat_handle_t *h, bool tiled = false) {
+// n_moved >= 0: the binning after a chunk launch that moved the first n_moved
+// particles.  While some are still paused, those that finished the interval
+// go to the trailing done bin and h->n_active counts the paused ones, which
+// lead the array; once none is paused, every particle is binned spatially
+// again for the next interval.  n_moved < 0: every particle spatially.
+int bin_particles(gpat_handle_t *h, bool tiled = false, int64_t n_moved = -1) {
     const int nxt = 1 - h->cur;
-    const CellGrid g = cell_grid(h, tiled);
+    CellGrid g = cell_grid(h, tiled);
+    if (n_moved >= 0 && h->pause) {
+        g.done_bin = 1;
+        g.pause = h->pause;
+        g.n_moved = n_moved;
+        g.nactive = &h->dcnt->nactive;
+    }
     const int64_t nbins = cell_grid_bins(g);
     if (nbins > h->sort_bins) {
         CK(cudaStreamSynchronize(h->stream));
@@ -396,12 +416,31 @@ int bin_particles(gpat_handle_t *h, bool tiled = false) {
     }
     CK(launch_cell_sort(h->P[h->cur], h->P[nxt], h->n, g, h->sort_scratch, h->dcnt,
                         escaped_hist(h), h->stream));
+    if (g.done_bin && h->n > 0)   // particles in spatial bins: the prefix before the done bin
+        CK(cudaMemcpyAsync(&h->n_spatial_host, cell_sort_counts(h->sort_scratch, nbins) + nbins - 2,
+                           sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
     int rc = pull_counters(h);
     if (rc) return rc;
     h->cur = nxt;
     h->n = (int64_t)h->hcnt.nkept;
+    h->n_active = (g.done_bin && h->n > 0) ? (int64_t)h->n_spatial_host : h->n;
+    h->last_sort_bins = nbins;
     h->unsorted = false;
     h->binned_tiles = tiled;
+    return GPAT_OK;
+}
+
+int ensure_pause(gpat_handle_t *h) {
+    if (h->pause_cap >= h->cap) return GPAT_OK;
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->pause) CK(cudaFree(h->pause));
+    h->pause = nullptr;
+    h->pause_cap = 0;
+    if (cudaMalloc(&h->pause, (size_t)h->cap) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, GPAT_ERR_OOM, "pause flags");
+    }
+    h->pause_cap = h->cap;
     return GPAT_OK;
 }
 
@@ -684,6 +723,7 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->scratch) cudaFree(h->scratch);
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->tile_dev) cudaFree(h->tile_dev);
+    if (h->pause) cudaFree(h->pause);
     if (h->tile_ovf) cudaFree(h->tile_ovf);
     for (int s = 0; s < 2; ++s)
         if (h->planes[s]) cudaFree(h->planes[s]);
@@ -1335,7 +1375,12 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     rc = ensure_scratch(h, h->n);
     if (rc) return rc;
     const bool tiled = mixed && tiles_on(h);
-    if (mixed && (h->unsorted || (tiled && !h->binned_tiles))) {
+    if (mixed) {
+        rc = ensure_pause(h);
+        if (rc) return rc;
+        a.pause = h->pause;
+    }
+    if (mixed && (h->unsorted || (tiled && !h->binned_tiles) || h->n_active != h->n)) {
         // New particles since the last binning (or a binning for another
         // brick shape): bin them before moving.
         rc = bin_particles(h, tiled);
@@ -1421,8 +1466,8 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
             CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
             CK(cudaMemsetAsync(s.ovf_count, 0, sizeof(unsigned long long), h->stream));
             a.P = h->P[h->cur];
-            a.n = h->n;
-            s.incl = cell_sort_counts(h->sort_scratch, cell_grid_bins(g));
+            a.n = h->n_active;   // paused particles lead the array; finished ones trail
+            s.incl = cell_sort_counts(h->sort_scratch, h->last_sort_bins);
             CK(cudaEventRecord(h->ev0, h->stream));
             CK(launch_mover_tile(a, k, s, tm1, tm2, h->tile_threads, h->sm_count, h->stream));
             CK(cudaEventRecord(h->ev1, h->stream));
@@ -1431,7 +1476,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
                 rc = collect_escaped(h);
                 if (rc) return rc;
             }
-            rc = bin_particles(h, true);
+            rc = bin_particles(h, true, a.n);
             if (rc) return rc;
             float ms = 0.0f;
             CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
@@ -1452,7 +1497,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         for (;;) {
             CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
             a.P = h->P[h->cur];
-            a.n = h->n;
+            a.n = h->n_active;   // paused particles lead the array; finished ones trail
             CK(cudaEventRecord(h->ev0, h->stream));
             CK(launch_mover_mixed(a, k, h->sm_count, h->stream));
             CK(cudaEventRecord(h->ev1, h->stream));
@@ -1461,7 +1506,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
                 rc = collect_escaped(h);
                 if (rc) return rc;
             }
-            rc = bin_particles(h);   // remove_particles as a binning by cell
+            rc = bin_particles(h, false, a.n);   // remove_particles as a binning by cell
             if (rc) return rc;
             float ms = 0.0f;
             CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));

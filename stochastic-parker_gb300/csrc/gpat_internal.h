@@ -86,6 +86,7 @@ struct MoverArgs {
     int check_drift_2d, pbcx, pbcy, pbcz, noise;
     uint32_t key0, key1;
     uint32_t max_pushes;        // per particle per call, guards runaway loops
+    uint8_t *pause;             // split-precision chunk launches: paused (1) / finished (0) per index
     uint32_t chunk_pushes;      // split-precision mover: stop a particle after this many
                                 // pushes (between pushes) so the set can be re-binned; 0 = off
     // particle_mover's focused_transport / nlgc / kperp_kpara and duu0.
@@ -146,6 +147,10 @@ struct MixedRunArgs {
     int nxg, nyg, nzg, time_interp, nsteps_interval, acc_region_flag, mag_dependency;
     int momentum_dependency, check_drift_2d, pbcx, pbcy, pbcz, noise;
     uint32_t key0, key1, max_pushes, chunk_pushes;
+    // Chunked launches: one byte per particle index set to 1 when the particle
+    // paused with pushes left in the interval, 0 when it finished (null: not
+    // recorded).  The next binning moves finished particles out of the way.
+    uint8_t *pause;
 };
 
 // One run of a batched launch: its arguments, constants and both particle
@@ -383,9 +388,18 @@ struct CellGrid {
     int tile;
     double dx, dy, dz;
     int bx, by, bz, nbx, nby, nbz;
+    // done_bin: one more bin after the spatial ones collects the in-box
+    // particles that finished the interval, so the next chunk launch covers
+    // the paused ones only.  A particle is binned spatially when every
+    // particle is (*nactive == 0 after the launch, or all_active), or when it
+    // was moved by the launch (index below n_moved) and paused (pause[i]).
+    int done_bin, all_active;
+    const uint8_t *pause;
+    int64_t n_moved;
+    const unsigned long long *nactive;
 };
-// Bins of a grid: cells, or bricks x cells per brick.
-int64_t cell_grid_bins(const CellGrid &g);
+// Bins of a grid: cells, or bricks x cells per brick; plus the done bin.
+__host__ __device__ int64_t cell_grid_bins(const CellGrid &g);
 // The per-bin counts inside the sort scratch; after a sort they hold the
 // inclusive prefix (the end of every bin's particle range).
 const unsigned int *cell_sort_counts(const void *scratch, int64_t nbins);

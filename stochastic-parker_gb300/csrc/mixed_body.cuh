@@ -49,7 +49,12 @@ __device__ __forceinline__ void bc_axis(int &c, float f, int n, bool ext, int op
         flag = lo ? flo : fhi;
     } else {
         const int per = ext ? n + 1 : n;
-        c += lo ? per : -per;
+        c += lo ? per : -per;   // the reference's wrap by one period
+        // A push longer than a period (a drift near a magnetic null at dt_min)
+        // leaves the particle outside even so; the reference would then index
+        // outside its arrays.  Whole periods more bring it back into the box.
+        if (c < -1) c += per * ((-1 - c + per - 1) / per);
+        else if (c > n) c -= per * ((c - n + per - 1) / per);
     }
 }
 

@@ -59,7 +59,11 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool active = false, exited = false;
     uint32_t pushes = 0;
-    if (i < n) pushes = move_particle<NDIM, NLGC>(a, k, P, i, active, GlobalGather{}, a.chunk_pushes, exited);
+    if (i < n) {
+        pushes = move_particle<NDIM, NLGC>(a, k, P, i, active, GlobalGather{}, a.chunk_pushes,
+                                           exited);
+        if (a.pause) a.pause[i] = active ? 1 : 0;
+    }
     add_warp_counters(a.cnt, pushes, active, nullptr);
 }
 
@@ -135,6 +139,7 @@ MixedRunArgs mixed_run_args(const MoverArgs &a) {
     r.pbcx = a.pbcx; r.pbcy = a.pbcy; r.pbcz = a.pbcz; r.noise = a.noise;
     r.key0 = a.key0; r.key1 = a.key1; r.max_pushes = a.max_pushes;
     r.chunk_pushes = a.chunk_pushes;
+    r.pause = a.pause;
     return r;
 }
 

@@ -170,8 +170,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int64_t i = beg + (long long)grp + lane;
             bool active = false, exited = false;
             uint32_t pushes = 0;
-            if (i < end)
+            if (i < end) {
                 pushes = move_particle<NDIM, NLGC>(a, k, P, i, active, g, a.chunk_pushes, exited);
+                if (a.pause) a.pause[i] = active ? 1 : 0;   // exited: set by the overflow kernel
+            }
             // particles that left the staged region go to the overflow list
             const unsigned m = __ballot_sync(0xffffffffu, exited);
             if (m) {
@@ -208,6 +210,7 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
             const uint32_t left = a.chunk_pushes ? a.chunk_pushes - done[t] : 0u;
             pushes = move_particle<NDIM, NLGC>(a, k, P, idx[t], active, GlobalGather{}, left,
                                                exited);
+            if (a.pause) a.pause[idx[t]] = active ? 1 : 0;
         }
         add_warp_counters(a.cnt, pushes, active, nullptr);
     }

@@ -656,7 +656,13 @@ __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int
     if (i < n) {
         const int flag = P.count_flag[i];
         int32_t key = -1;
-        if (flag == 1 && g.tile) {
+        const bool spatial = !g.done_bin || g.all_active || *g.nactive == 0ull ||
+                             (i < g.n_moved && g.pause[i] != 0);
+        if (flag == 1 && !spatial) {
+            // finished the interval: the trailing done bin
+            key = (int32_t)(cell_grid_bins(g) - 1);
+            atomicAdd(&counts[key], 1u);
+        } else if (flag == 1 && g.tile) {
             // the mover's own cell (cell_of), so the particle lands in the
             // brick whose records are staged for it; clamped into the grid
             int cx, cy, cz = 0;
@@ -778,9 +784,10 @@ __global__ void __launch_bounds__(256) cell_scatter_kernel(const DevParticles S,
 
 }  // namespace
 
-int64_t cell_grid_bins(const CellGrid &g) {
-    if (g.tile) return (int64_t)g.nbx * g.nby * g.nbz * ((int64_t)g.bx * g.by * g.bz);
-    return (int64_t)g.nxg * g.nyg * g.nzg;
+__host__ __device__ int64_t cell_grid_bins(const CellGrid &g) {
+    const int64_t spatial = g.tile ? (int64_t)g.nbx * g.nby * g.nbz * ((int64_t)g.bx * g.by * g.bz)
+                                   : (int64_t)g.nxg * g.nyg * g.nzg;
+    return spatial + (g.done_bin ? 1 : 0);
 }
 
 const unsigned int *cell_sort_counts(const void *scratch, int64_t nbins) {
