@@ -38,12 +38,15 @@ def _spectrum(eng, edges):
 
 
 def compare(workload: configs.Workload, intervals: int, split=(2.72, 2.0),
-            device: int = 0) -> dict:
-    """Runs the workload in FP64 and split precision; returns the tail error."""
+            device: int = 0, tiles=None) -> dict:
+    """Runs the workload in FP64 and split precision; returns the tail error.
+    tiles: gpat_set_mover_tiles arguments for the split-precision run."""
     out = {}
     for prec in (0, 1):
         eng = configs.build_engine(workload, device=device, precision=prec,
                                    nptl_max=int(workload.nptl * 8))
+        if prec == 1 and tiles:
+            eng.set_mover_tiles(*tiles)
         configs.inject(eng, workload)
         for k in range(intervals):
             eng.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=1)
@@ -64,6 +67,57 @@ def spectrum(eng) -> dict:
     f_dev, _ = eng.calc_particle_distributions()
     f, f2, c = _spectrum(eng, edges)
     return dict(f=f, f2=f2, c=c, f_dev=f_dev, n=eng.nptl_current, steps=eng.counters().steps)
+
+
+def subset_spectrum(eng, max_tag: int) -> dict:
+    """f(p) of the particles injected with tag_injected <= max_tag (split
+    children share their parent's injection tag); a tracked particle's tag
+    is negated, hence the absolute value."""
+    edges = eng.pbins_edges()
+    ps = eng.get_particles()
+    keep = np.abs(ps["tag_injected"].astype(np.int64)) <= max_tag
+    p, w = ps["p"][keep], ps["weight"][keep]
+    npp = len(edges) - 1
+    lo = math.log10(edges[0])
+    d = (math.log10(edges[-1]) - lo) / npp
+    ok = (p > edges[0]) & (p <= edges[-1])
+    ib = np.floor((np.log10(p[ok]) - lo) / d).astype(np.int64)
+    sel = (ib >= 0) & (ib < npp)
+    ib, ww = ib[sel], w[ok][sel]
+    f = np.bincount(ib, weights=ww, minlength=npp)
+    f2 = np.bincount(ib, weights=ww * ww, minlength=npp)
+    c = np.bincount(ib, minlength=npp)
+    return dict(f=f, f2=f2, c=c, f_dev=f, n=int(keep.sum()), steps=0)
+
+
+def batched_runs_check(runs, engines, intervals: int, sample: int = 20000,
+                       device: int = 0) -> list:
+    """Per-run tail error of batched split-precision runs against FP64 runs
+    of the same injected particles.  Injection draws are keyed by particle
+    tag, so an FP64 run that injects the first `sample` particles starts
+    from exactly the first `sample` particles of the batched run; each run's
+    f(p) of those particles (children included) after `intervals` intervals
+    with splitting is compared with the FP64 run's."""
+    out = []
+    for w, e in zip(runs, engines):
+        s = min(sample, w.nptl)
+        mixed = subset_spectrum(e, s)
+        e64 = configs.build_engine(w, device=device, precision=0, nptl_max=16 * s + 64)
+        configs.inject(e64, w, nptl=s)
+        for k in range(intervals):
+            e64.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=1)
+            if w.split:
+                e64.split_particle(w.split["ratio"], w.split["pmin"], 10)
+        ref = spectrum(e64)
+        e64.close()
+        try:
+            t = tail_stats(ref, mixed, w.params["pmin"], w.params["pmax"])
+        except RuntimeError:
+            continue
+        out.append({"run": w.name, "particles": w.nptl, "sample": s, "tail_err": t["tail_err"],
+                    "tail_err_sigma": t["tail_err_sigma"], "top_decade_p": t["top_decade_p"],
+                    "chi2": t["chi2"], "chi2_dof": t["chi2_dof"]})
+    return out
 
 
 def tail_stats(a: dict, b: dict, pmin: float, pmax: float) -> dict:
@@ -98,4 +152,18 @@ def planar_shock_check(scale: float = 1.0, t_end: float = 2.0, device: int = 0) 
     w = configs.planar_shock(scale=scale, t_end=t_end)
     r = compare(w, w.nframes, split=(2.72, 2.0), device=device)
     r["workload"] = f"{w.name}, {w.nptl} particles injected, t = {t_end}, split 2.72 / 2.0"
+    return r
+
+
+def turbulent_shock_check(scale: float = 0.1, intervals: int = 25, device: int = 0,
+                          tiles=None) -> dict:
+    """The benchmarked 2048^2 turbulent shock (r = 3.5, dB/B0 = 0.5, 1000
+    pushes per particle per interval) on a sample of scale x 1e7 particles,
+    both precisions from the same injection, with splitting."""
+    w = configs.turbulent_shock_2d(scale=scale, nframes=intervals + 1)
+    r = compare(w, intervals, split=(w.split["ratio"], w.split["pmin"]), device=device,
+                tiles=tiles)
+    r["workload"] = (f"{w.name}, {w.nptl} particles injected, {intervals} intervals "
+                     f"(t = {intervals * (w.tstamps[1] - w.tstamps[0]):g}), split "
+                     f"{w.split['ratio']} / {w.split['pmin']}")
     return r

@@ -2,10 +2,12 @@
 
 - The FP64 mover recovers the diffusive-shock-acceleration spectrum: for
   r = 4 the weighted number per log-p bin falls as p^(3 - 3r/(r-1)) = p^-1
-  above injection (a softer slope is expected where the diffusion step per
-  push exceeds the shock width).
-- The split-precision mover's f(p) tail agrees with the FP64 mover's within
-  2 % plus three Monte Carlo standard errors.
+  above injection, within two standard errors of eight independent runs
+  plus a stated bias of the finite shock width.
+- The split-precision mover's f(p) tail agrees with the FP64 mover's: the
+  one-sided 95 % bound on the tail error is within 2 %, with a Monte Carlo
+  standard error of at most 0.5 %, on the planar shock and on the
+  benchmarked turbulent-shock field.
 """
 import math
 
@@ -17,28 +19,63 @@ from gpat import accuracy, configs
 pytestmark = pytest.mark.gpu
 
 
-def test_planar_shock_spectral_index_fp64():
-    w = configs.planar_shock(scale=0.5, t_end=2.0)
-    eng = configs.build_engine(w, precision=0, nptl_max=w.nptl * 8)
+def _shock_slope(precision, seed, scale=0.5):
+    """dN/dln p slope of one planar-shock run over 1.5 p0 .. 6 p0 (p0 = 0.1):
+    above injection, below the escape-limited cut-off."""
+    w = configs.planar_shock(scale=scale, t_end=2.0, seed=seed)
+    eng = configs.build_engine(w, precision=precision, nptl_max=w.nptl * 8)
     configs.inject(eng, w)
     for k in range(w.nframes):
         eng.particle_mover(mhd_tframe=k + 1)
         eng.split_particle(2.72, 2.0, 10)
     f, c = eng.calc_particle_distributions()
     edges = eng.pbins_edges()
+    eng.close()
     centers = np.sqrt(edges[:-1] * edges[1:])
-    # fit dN/dlnp over 1.5 p0 .. 6 p0 (p0 = 0.1): above injection, below the
-    # escape-limited cut-off
     m = (centers > 0.15) & (centers < 0.6) & (c > 50)
     assert m.sum() >= 6
-    slope = np.polyfit(np.log(centers[m]), np.log(f[m]), 1)[0]
-    assert -1.6 < slope < -0.8, slope
-    eng.close()
+    return np.polyfit(np.log(centers[m]), np.log(f[m]), 1)[0]
+
+
+# Finite shock width: w = 0.002 against diffusion lengths kappa(p)/u1 of 0.017
+# to 0.1 in the fitted window (kappa = 0.01 (p/p0)^(4/3)), which flattens the
+# test-particle slope of -1 by a few hundredths.
+SHOCK_WIDTH_BIAS = 0.08
+
+
+def test_planar_shock_spectral_index():
+    """r = 4: dN/dln p ~ p^(3 - 3r/(r-1)) = p^-1.  Eight independent FP64 runs
+    give the slope and its standard error (the spread of the runs, which
+    includes the correlation that splitting brings); the FP64 mean must lie
+    within 2 standard errors plus the shock-width bias of -1, and the
+    split-precision runs' mean within 3 combined standard errors of it."""
+    seeds = range(11, 19)
+    s64 = np.array([_shock_slope(0, s) for s in seeds])
+    smx = np.array([_shock_slope(1, s) for s in seeds])
+    m64, e64 = s64.mean(), s64.std(ddof=1) / math.sqrt(len(s64))
+    mmx, emx = smx.mean(), smx.std(ddof=1) / math.sqrt(len(smx))
+    assert abs(m64 + 1.0) < 2 * e64 + SHOCK_WIDTH_BIAS, (m64, e64, s64)
+    assert e64 < 0.05, e64
+    assert abs(mmx - m64) < 3 * math.hypot(e64, emx), (mmx, m64, e64, emx)
 
 
 def test_mixed_tail_error_planar_shock():
-    r = accuracy.planar_shock_check(scale=0.5)
-    assert r["top_decade_particles_fp64"] > 1000
-    assert abs(r["tail_err"]) <= 0.02 + 3 * r["tail_err_sigma"], r
+    """Tail error of the split-precision mover against the FP64 mover with a
+    Monte Carlo standard error of at most 0.5 %, and the one-sided 95 % upper
+    bound on its size, |e| + 1.645 sigma, within 2 %."""
+    r = accuracy.planar_shock_check(scale=5.0)
+    assert r["top_decade_particles_fp64"] > 50000
+    assert r["tail_err_sigma"] <= 0.005, r
+    assert abs(r["tail_err"]) + 1.645 * r["tail_err_sigma"] <= 0.02, r
+    dof = max(1, r["chi2_dof"])
+    assert r["chi2"] < dof + 4 * math.sqrt(2 * dof) + 10, r
+
+
+def test_mixed_tail_error_turbulent_shock_2048():
+    """The same gate on the benchmarked 2048^2 turbulent-shock field: 1e6
+    particles, 25 intervals of 1000 pushes, splitting after each."""
+    r = accuracy.turbulent_shock_check(scale=0.1, intervals=25)
+    assert r["tail_err_sigma"] <= 0.005, r
+    assert abs(r["tail_err"]) + 1.645 * r["tail_err_sigma"] <= 0.02, r
     dof = max(1, r["chi2_dof"])
     assert r["chi2"] < dof + 4 * math.sqrt(2 * dof) + 10, r
