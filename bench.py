@@ -87,6 +87,10 @@ def parse_args(argv=None):
                     help="pushes between re-binnings (0: engine default, <0: once per call)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 sample and the f(p) tail-error check")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only (no 3D and batched keys in its line)")
+    ap.add_argument("--tiles-3d", default="off",
+                    help="--tiles for the 3D measurement inside the headline line")
     ap.add_argument("--tiles", default="off",
                     help="split-precision mover field bricks: 'off' (global gathers) or "
                          "'bx,by,bz[,hx,hy,hz[,threads[,items]]]': cells per brick and halo "
@@ -233,18 +237,53 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profiled_traffic(name: str):
-    """DRAM bytes per push recorded in profiles/<name>.md ('traffic_bytes_per_push: N')."""
-    p = REPO / "profiles" / f"{name}.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_push:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+# From the ncu captures summarised in profiles/ (commands there): DRAM bytes
+# (read + write) per push of the mover kernel at the bench's particle
+# density, and the L1TEX throughput (percent of peak, active cycles) of the
+# full capture, which ncu names as the binding unit of the gather movers.
+NCU_MOVER = {
+    ("global", 2): {"dram_bytes_per_push": 0.934, "l1tex_pct": 94.2,
+                    "profile": "profiles/mover_mixed_turbulent_shock_2d.md"},
+    ("global", 3): {"dram_bytes_per_push": 6.7, "l1tex_pct": 79.4,
+                    "profile": "profiles/mover_mixed_turbulence_3d.md"},
+}
+# Bytes one SM's L1TEX/shared-memory data path returns per clock.
+L1_BYTES_PER_CLK_SM = 128
+# Field bytes the movers read through L1 per push: the global-gather kernel
+# loads whole 32-byte halves of the 64-byte (2D) or 96-byte (3D) records of
+# every corner; the tile kernel reads 16-byte chunks from shared memory
+# (3D: 5 chunks and one 4-byte value per corner).
+L1_GATHER_BYTES_PER_PUSH = {("global", 2): 4 * 64, ("global", 3): 8 * 96,
+                            ("tile", 2): 4 * 64, ("tile", 3): 8 * (5 * 16 + 4)}
+
+
+def roofline_of(kind, ndim, avg_ms, avg_steps, avg_n, sm_count, sm_mhz, peaks) -> dict:
+    """Roofline of one mover launch: the L1TEX data path is the bound (ncu),
+    HBM is reported beside it on the algorithmic bytes."""
+    secs = avg_ms / 1e3
+    l1_bytes = avg_steps * L1_GATHER_BYTES_PER_PUSH[(kind, ndim)]
+    l1_peak = sm_count * L1_BYTES_PER_CLK_SM * (sm_mhz or 2070.0) * 1e6 / 1e9
+    alg = avg_steps * GATHER_BYTES_PER_STEP[ndim] + avg_n * STATE_BYTES_PER_PARTICLE
+    ncu = NCU_MOVER.get((kind, ndim), {})
+    dram = ncu.get("dram_bytes_per_push")
+    return {"bound": "l1", "achieved": l1_bytes / secs / 1e9, "peak": l1_peak, "unit": "GB/s",
+            "frac": l1_bytes / secs / 1e9 / l1_peak,
+            "peak_source": f"nominal: {L1_BYTES_PER_CLK_SM} B/clk per SM x {sm_count} SMs x "
+                           f"median sampled SM clock {sm_mhz} MHz (no measured L1 figure)",
+            "traffic": dram * avg_steps if dram is not None else None,
+            "traffic_source": ncu.get("profile"),
+            "ncu_l1tex_throughput_pct": ncu.get("l1tex_pct"),
+            "l1_bytes_per_push": L1_GATHER_BYTES_PER_PUSH[(kind, ndim)],
+            "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
+            "kernel_steps_per_s": avg_steps / secs,
+            "hbm": {"achieved": alg / secs / 1e9, "peak": peaks["hbm_gbs"],
+                    "frac": alg / secs / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                    "algorithmic_bytes_per_push": GATHER_BYTES_PER_STEP[ndim],
+                    "state_bytes_per_particle": STATE_BYTES_PER_PARTICLE},
+            "note": "achieved = field bytes read through L1/shared memory per push x pushes / "
+                    "launch time; ncu_l1tex_throughput_pct is the unit's measured busy share "
+                    "(per-request work, not bytes, saturates it); hbm = algorithmic bytes "
+                    "(corners x stored field arrays x 4 B + FP64 state) over measured HBM"}
 
 
 # ---------------------------------------------------------------------------
@@ -378,12 +417,12 @@ def run_ours(args, world, rank, local):
     n_cap = int(w.nptl * 1.6)
     pinned = {}
     from gpat import _abi
-    for name, t in _abi.PARTICLE_FIELDS:
+    for name, t in (_abi.PARTICLE_FIELDS if args.e2e_steps > 0 else []):
         tt = torch.empty(n_cap, dtype=getattr(torch, {"f8": "float64", "i1": "int8", "i4": "int32",
                                                         "u4": "uint32"}[t]), pin_memory=True)
         pinned[name] = tt.numpy()
-    host = ParticleSet(pinned)
-    cur = eng.get_particles(out=host)
+    host = ParticleSet(pinned) if pinned else None
+    cur = eng.get_particles(out=host) if host is not None else None
     e2e_steps, e2e_h2d, e2e_d2h = 0, 0, 0
     bytes_per_ptl = sum(np.dtype(t).itemsize for _, t in _abi.PARTICLE_FIELDS)
     barrier(world)
@@ -408,7 +447,7 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         eng.close()
-        return
+        return None
     peaks = measured_peaks()
     launches = statistics.mean(kernel_launches)
     avg_ms = statistics.mean(kernel_ms) / launches          # per mover launch
@@ -418,39 +457,26 @@ def run_ours(args, world, rank, local):
     ncells = (w.mhd_config.nx + 4) * (w.mhd_config.ny + 4) * ((w.mhd_config.nz + 4) if ndim == 3 else 1)
     rec_mb = ncells * (64 if ndim == 2 else 96) / 1e6
     state_mb = avg_n * 98 / 1e6
-    bytes_launch = avg_steps * GATHER_BYTES_PER_STEP[ndim] + avg_n * STATE_BYTES_PER_PARTICLE
-    achieved = bytes_launch / (avg_ms / 1e3) / 1e9
-    impl_launch = avg_steps * IMPL_GATHER_BYTES_PER_STEP[ndim] + avg_n * STATE_BYTES_PER_PARTICLE
-    achieved_impl = impl_launch / (avg_ms / 1e3) / 1e9
-    kname = f"mover_{args.precision}_{args.workload}"
-    traffic = profiled_traffic(kname)
-    l2 = l2_read_gbs(torch, dev)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"],
-                "traffic": traffic * avg_steps if traffic is not None else None,
-                "kernel": f"mover_{args.precision}_kernel<{ndim}>",
-                "peak_source": peaks["source"],
-                "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
-                "mover_launches_per_interval": launches,
-                "kernel_steps_per_s": avg_steps / (avg_ms / 1e3),
-                "algorithmic_bytes_per_launch": bytes_launch,
-                "algorithmic_bytes_per_push": GATHER_BYTES_PER_STEP[ndim],
-                "implemented_gather_bytes_per_push": IMPL_GATHER_BYTES_PER_STEP[ndim],
-                "achieved_implemented_gbs": achieved_impl,
-                "frac_implemented": achieved_impl / peaks["hbm_gbs"],
-                "note": "achieved = algorithmic bytes (corners x stored field arrays x 4 B per "
-                        "push + 90 B of particle state per particle and launch) / launch time; "
-                        "the packed records gather more per push (implemented_*), served from "
-                        "L1/L2; traffic = ncu DRAM bytes per push x pushes",
-                "l2_read_gbs_measured": l2, "frac_of_l2_read": achieved / l2}
+    kind = "tile" if tiles else "global"
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    roofline = roofline_of(kind, ndim, avg_ms, avg_steps, avg_n, sm_count, clk.get("sm_mhz"),
+                           peaks)
+    roofline["kernel"] = (f"mover_tile_kernel<{ndim}> + mover_overflow_kernel<{ndim}>" if tiles
+                          else f"mover_{args.precision}_kernel<{ndim}>")
+    roofline["mover_launches_per_interval"] = launches
+    if tiles:
+        roofline["tiles"] = eng.mover_tiles()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+ff" if prec else "f64", "data": "synthetic",
+            "dtype": "f32" if prec else "f64", "data": "synthetic",
             "config": {"workload": w.name, "particles_per_rank": w.nptl,
                        "pushes_per_particle_per_interval":
                            round(statistics.mean(kernel_steps) / max(1.0, avg_n), 1),
-                       "precision": args.precision,
+                       "precision": args.precision + (" (FP32 fields, kappa, drift and dt; "
+                                                      "Kahan-compensated FP32 momentum and clock; "
+                                                      "integer cell + FP32 offset positions)"
+                                                      if prec else ""),
                        "step": "particle_mover" + (" + split_particle" if w.split else "") +
                                " + f(p) over one MHD interval",
                        "l2": f"inputs exceed L2 (packed field records {rec_mb:.0f} MB, "
@@ -473,14 +499,18 @@ def run_ours(args, world, rank, local):
         line["fp64_gpu"] = {"value": v64, "unit": UNIT, "sample": f"{n64} particles, one interval, "
                                                                   f"{s64} particle-steps",
                             "mixed_over_fp64": value / v64}
-        line["accuracy"] = accuracy.planar_shock_check(scale=1.0, device=local)
+        if args.workload == "turbulent_shock_2d":
+            line["accuracy"] = accuracy.turbulent_shock_check(scale=0.1, intervals=25,
+                                                              device=local, tiles=tiles)
+        else:
+            line["accuracy"] = accuracy.planar_shock_check(scale=1.0, device=local)
     if world == 1 and not args.no_cpu_baseline:
         v, cores, n, steps, dt, _ = cpu_sample(w, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{n} particles of {w.name} injected as the workload "
                                           f"does, one MHD interval of FP64 pushes ({steps} "
                                           f"particle-steps in {dt:.2f} s)"}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_batch(args, world, rank, local):
@@ -540,33 +570,18 @@ def run_batch(args, world, rank, local):
     value = sum_over_ranks(world, float(psteps), dev) / t_max
     intervals_done = frame[0] - 1
 
-    # f(p) of the runs nearest 1e5 particles against FP64 runs of the same runs
+    # f(p) of every run's first injected particles against an FP64 run of the
+    # same particles
     acc = []
     if not args.no_accuracy:
-        order = sorted(range(len(runs)), key=lambda r: abs(math.log10(runs[r].nptl) - 5.0))[:4]
-        for r in order:
-            w = runs[r]
-            mixed = accuracy.spectrum(engines[r])
-            e64 = configs.build_engine(w, device=local, precision=0, nptl_max=int(w.nptl * 8))
-            configs.inject(e64, w)
-            for k in range(intervals_done):
-                e64.particle_mover(nsteps_interval=10, mhd_tframe=k + 1, num_fine_steps=1)
-                e64.split_particle(w.split["ratio"], w.split["pmin"], 10)
-            ref = accuracy.spectrum(e64)
-            e64.close()
-            try:
-                t = accuracy.tail_stats(ref, mixed, w.params["pmin"], w.params["pmax"])
-            except RuntimeError:
-                continue
-            acc.append({"run": w.name, "particles": w.nptl, "tail_err": t["tail_err"],
-                        "tail_err_sigma": t["tail_err_sigma"], "chi2": t["chi2"],
-                        "chi2_dof": t["chi2_dof"]})
+        acc = accuracy.batched_runs_check(runs, engines, intervals_done, sample=20000,
+                                          device=local)
 
     # end to end: every run's particles host -> device, the batched frame,
     # f(p) and particles back
     bytes_per_ptl = sum(np.dtype(t).itemsize for _, t in _abi.PARTICLE_FIELDS)
     hosts = []
-    for e in engines:
+    for e in (engines if args.e2e_steps > 0 else []):
         cap = e.params.nptl_max
         arrs = {name: torch.empty(cap, dtype=getattr(torch, {"f8": "float64", "i1": "int8",
                                                              "i4": "int32", "u4": "uint32"}[t]),
@@ -599,19 +614,24 @@ def run_batch(args, world, rank, local):
         batch.close()
         for e in engines:
             e.close()
-        return
+        return None
     peaks = measured_peaks()
     chunks = statistics.mean(graph_launches)
     ms_chunk = statistics.mean(graph_ms) / chunks
     pushes_chunk = statistics.mean(chunk_pushes) / chunks
-    bytes_chunk = pushes_chunk * GATHER_BYTES_PER_STEP[2] + n_timed * STATE_BYTES_PER_PARTICLE
-    achieved = bytes_chunk / (ms_chunk / 1e3) / 1e9
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    batch_roofline = roofline_of("global", 2, ms_chunk, pushes_chunk, n_timed, sm_count,
+                                 clk.get("sm_mhz"), peaks)
+    batch_roofline.update({"kernel": "mover_mixed_batch_kernel<2> chunk graph (mover + binning)",
+                           "ms_per_chunk": ms_chunk, "pushes_per_chunk": pushes_chunk,
+                           "chunks_per_interval": chunks,
+                           "timing": "whole chunk graph (the binning kernels included)"})
     nruns = len(runs)
     sizes = sorted({w.mhd_config.nx for w in runs})
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+ff", "data": "synthetic",
+            "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"batched_shock_2d_{nruns}_runs",
                        "runs": nruns,
                        "particles_total": int(sum(w.nptl for w in runs)),
@@ -633,13 +653,7 @@ def run_batch(args, world, rank, local):
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": e2e_h2d // max(1, args.e2e_steps),
                     "d2h_bytes_per_step": e2e_d2h // max(1, args.e2e_steps)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                         "kernel": "mover_mixed_batch_kernel<2> chunk graph (mover + binning)",
-                         "peak_source": peaks["source"], "ms_per_chunk": ms_chunk,
-                         "pushes_per_chunk": pushes_chunk, "chunks_per_interval": chunks,
-                         "note": "achieved = algorithmic bytes of the chunk's pushes and particle "
-                                 "state over the whole chunk graph time (binning included)"},
+            "roofline": batch_roofline,
             "per_run_fp_error": acc}
     batch.close()
     for e in engines:
@@ -651,7 +665,7 @@ def run_batch(args, world, rank, local):
                                 "sample": f"{n} particles of {w.name} injected on the shock, one "
                                           f"MHD interval of FP64 pushes ({steps} particle-steps "
                                           f"in {dt:.2f} s)"}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_learned(args, world, rank, local):
@@ -745,7 +759,7 @@ def run_learned(args, world, rank, local):
             "n_gpus": world, "steps": 1, "warmup": 0,
             "ms_per_step": 1e3 * learned["seconds"] / nint,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+ff", "data": "synthetic",
+            "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"learned_splitting_{w.name}", "particles": n_cmp,
                        "intervals": nint,
                        "step": "one MHD interval of the learned-splitting arm (weighted split + "
@@ -770,17 +784,46 @@ def run_learned(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# Keys of a workload's own line kept when it is reported inside the headline.
+EXTRA_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "clocks",
+              "roofline", "per_run_fp_error", "accuracy")
+
+
+def other_configs(args, local) -> dict:
+    """The 3D compressible turbulence (256^3, 1e8 particles) and the batch of
+    64 turbulent-shock runs, each measured for one timed MHD interval after
+    one warm-up interval with the same mover options, for the headline line."""
+    out = {}
+    common = dict(steps=1, warmup=1, e2e_steps=0, no_cpu_baseline=True, scale=1.0, grid=2048)
+    a3 = argparse.Namespace(**{**vars(args), **common, "workload": "turbulence_3d",
+                               "no_accuracy": True, "tiles": args.tiles_3d})
+    l3 = run_ours(a3, 1, 0, local)
+    out["turbulence_3d_256"] = {k: l3[k] for k in EXTRA_KEYS if k in l3}
+    ab = argparse.Namespace(**{**vars(args), **common, "workload": "batched_shock_2d",
+                               "no_accuracy": False})
+    lb = run_batch(ab, 1, 0, local)
+    out["batched_shock_2d_64"] = {k: lb[k] for k in EXTRA_KEYS if k in lb}
+    return out
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
     elif args.workload == "batched_shock_2d":
-        run_batch(args, world, rank, local)
+        line = run_batch(args, world, rank, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
     elif args.workload == "learned_3d":
         run_learned(args, world, rank, local)
     else:
-        run_ours(args, world, rank, local)
+        line = run_ours(args, world, rank, local)
+        if line is not None and args.workload == "turbulent_shock_2d" and not args.no_extras \
+                and world == 1:
+            line["configs"] = other_configs(args, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
