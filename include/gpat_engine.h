@@ -466,10 +466,14 @@ void *gpat_stream(gpat_handle_t *h);
 typedef struct gpat_batch gpat_batch_t;
 /* Launch shape picked by gpat_batch_autotune: minb = resident 128-thread
  * blocks per SM of the kernel variant (its register target), grab = tiles a
- * block takes per scheduler step; pushes_per_s = the measured rate. */
+ * block takes per scheduler step; pushes_per_s = the measured rate;
+ * chunk_pushes = pushes per particle between re-binnings for every run (0:
+ * each run's own bin_interval).  minb and grab do not change results;
+ * chunk_pushes moves the pause points, so results agree statistically. */
 typedef struct gpat_batch_tuning {
     int32_t minb, grab;
     double pushes_per_s;
+    int32_t chunk_pushes, reserved;
 } gpat_batch_tuning_t;
 int gpat_batch_create(gpat_handle_t *const *runs, int nruns, gpat_batch_t **out);
 int gpat_batch_destroy(gpat_batch_t *b);
@@ -477,9 +481,10 @@ const char *gpat_batch_last_error(const gpat_batch_t *b);
 /* particle_mover for every run; mhd_tframe holds one frame index per run. */
 int gpat_batch_particle_mover(gpat_batch_t *b, const int *mhd_tframe, int nlgc,
                               double kperp_kpara, int nsteps_interval, int num_fine_steps);
-/* Times one chunk of every launch-shape candidate from a snapshot of the
- * runs (restored afterwards, so the runs are unchanged) and keeps the
- * fastest for later calls.  Launch shapes do not change results. */
+/* Times one chunk of every candidate (register-target variant x tile grab x
+ * chunk length 64 / 128 / 256) from a snapshot of the runs (restored
+ * afterwards, so the runs are unchanged) and keeps the fastest for later
+ * calls. */
 int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double kperp_kpara,
                         int nsteps_interval, int num_fine_steps, gpat_batch_tuning_t *best);
 int gpat_batch_get_tuning(const gpat_batch_t *b, gpat_batch_tuning_t *t);
@@ -542,6 +547,22 @@ int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_
  * keyed by the particle's tags and push counter). */
 int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
                         double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled);
+/* No counterpart in the reference.  Learned splitting inside the mover:
+ * while set, gpat_particle_mover's split-precision chunk launches score every
+ * particle that finishes the interval in the box with the network m (tensor
+ * cores, in the same launch) at features of normalised time t_norm, and apply
+ * gpat_weighted_split's weight window around w_t = w_ref exp(-(z - z_ref)):
+ * children are appended after the set (up to nptl_max), roulette losers are
+ * removed.  The brick mover is not used while this is set.  m = NULL turns it
+ * off.  The network must outlive the setting. */
+int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref,
+                           double z_ref, double window_ratio, int max_level);
+/* After a mover call with learned splitting: log of the sum of w exp(z) over
+ * the judged particles (before their split; the next call's z_ref is this
+ * minus log of the target population), their number, children created and
+ * particles removed by roulette. */
+int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, int64_t *judged,
+                           int64_t *nsplit, int64_t *nkilled);
 /* Count, sum of weights and of squared weights of live particles with
  * p > p_threshold: (sum w)^2 / sum w^2 is their effective sample size. */
 int gpat_tail_weights(gpat_handle_t *h, double p_threshold, int64_t *count, double *wsum,

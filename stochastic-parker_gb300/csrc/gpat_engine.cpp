@@ -68,6 +68,14 @@ struct gpat_handle {
     // and the bins of that binning
     uint8_t *pause = nullptr;
     int64_t pause_cap = 0;
+    // learned splitting inside the mover (gpat_set_mover_learned): the
+    // launch arguments, and on the device the particle count with children,
+    // the judged count and the fixed-point sum of w exp(z - z_shift)
+    bool learn_on = false;
+    FusedLearn learn{};
+    unsigned long long *learn_dev = nullptr;
+    unsigned long long learn_host[4] = {};
+    int64_t learn_split = 0, learn_killed = 0;
     int64_t n_active = 0;
     int64_t last_sort_bins = 0;
     unsigned int n_spatial_host = 0;
@@ -724,6 +732,7 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->sort_scratch) cudaFree(h->sort_scratch);
     if (h->tile_dev) cudaFree(h->tile_dev);
     if (h->pause) cudaFree(h->pause);
+    if (h->learn_dev) cudaFree(h->learn_dev);
     if (h->tile_ovf) cudaFree(h->tile_ovf);
     for (int s = 0; s < 2; ++s)
         if (h->planes[s]) cudaFree(h->planes[s]);
@@ -1374,7 +1383,8 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
     CK(cudaSetDevice(h->device));
     rc = ensure_scratch(h, h->n);
     if (rc) return rc;
-    const bool tiled = mixed && tiles_on(h);
+    const bool learned = mixed && h->learn_on;
+    const bool tiled = mixed && tiles_on(h) && !learned;
     if (mixed) {
         rc = ensure_pause(h);
         if (rc) return rc;
@@ -1494,13 +1504,34 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         a.chunk_pushes = bi == 0 ? 128u : (bi > 0 ? (uint32_t)bi : 0u);
         const MixedConsts k = make_mixed_consts(a);
         const int64_t max_chunks = (int64_t)a.max_pushes / (a.chunk_pushes ? a.chunk_pushes : 1) + 4;
+        const unsigned long long split0 = h->hcnt.nsplit, kill0 = h->hcnt.nkilled;
+        if (learned)
+            CK(cudaMemsetAsync(h->learn_dev + 1, 0, 3 * sizeof(unsigned long long), h->stream));
         for (;;) {
             CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
             a.P = h->P[h->cur];
             a.n = h->n_active;   // paused particles lead the array; finished ones trail
-            CK(cudaEventRecord(h->ev0, h->stream));
-            CK(launch_mover_mixed(a, k, h->sm_count, h->stream));
-            CK(cudaEventRecord(h->ev1, h->stream));
+            if (learned) {
+                // children are appended after every particle of the set
+                h->learn_host[0] = (unsigned long long)h->n;
+                CK(cudaMemcpyAsync(h->learn_dev, h->learn_host, sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, h->stream));
+                FusedLearn L = h->learn;
+                L.cap = h->cap;
+                L.count = h->learn_dev;
+                L.zsum = h->learn_dev + 1;
+                CK(cudaEventRecord(h->ev0, h->stream));
+                CK(launch_mover_learned(a, k, L, h->stream));
+                CK(cudaEventRecord(h->ev1, h->stream));
+                CK(cudaMemcpyAsync(h->learn_host, h->learn_dev, 4 * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, h->stream));
+                CK(cudaStreamSynchronize(h->stream));
+                h->n = (int64_t)h->learn_host[0];
+            } else {
+                CK(cudaEventRecord(h->ev0, h->stream));
+                CK(launch_mover_mixed(a, k, h->sm_count, h->stream));
+                CK(cudaEventRecord(h->ev1, h->stream));
+            }
             ++launches;
             if (keep_escaped) {
                 rc = collect_escaped(h);
@@ -1514,6 +1545,11 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
             if (h->hcnt.nactive == 0) break;
             if (launches > max_chunks)
                 return fail(h, GPAT_ERR_DEVICE, "mover chunks did not finish the interval");
+        }
+        if (learned) {
+            h->learn_split = (int64_t)(h->hcnt.nsplit - split0);
+            h->learn_killed = (int64_t)(h->hcnt.nkilled - kill0);
+            h->nptl_split += h->learn_split;
         }
     } else {
         CK(cudaEventRecord(h->ev0, h->stream));
@@ -2077,6 +2113,7 @@ int batch_prepare(gpat_batch_t *b, const int *tframes, int nlgc, double kperp_kp
         a.kperp_kpara = kperp_kpara;
         const int bi = h->prm.bin_interval;
         a.chunk_pushes = bi == 0 ? 128u : (bi > 0 ? (uint32_t)bi : 0u);
+        if (b->tuning.chunk_pushes > 0) a.chunk_pushes = (uint32_t)b->tuning.chunk_pushes;
         for (int k = 0; k < 2 && (h->unsorted || h->cur != 0); ++k) {
             rc = bin_particles(h);
             if (rc) return bfail(b, rc, "run " + std::to_string(r) + ": " + h->err);
@@ -2262,8 +2299,12 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
     int variants[4];
     const int nv = batch_minb_variants(b->ndim, variants);
     const int grabs[2] = {1, 4};
+    const int chunks[3] = {64, 128, 256};
     gpat_batch_tuning_t top{};
     top.pushes_per_s = -1.0;
+    for (int ci = 0; ci < 3; ++ci) {
+        for (size_t r = 0; r < nr; ++r) b->desc[r].a.chunk_pushes = (uint32_t)chunks[ci];
+        BCK(upload_batch_runs(b->desc.data(), (int)nr, b->stream));
     for (int v = 0; v < nv; ++v)
         for (int gi = 0; gi < 2; ++gi) {
             rc = capture_graphs(b, nlgc ? 1 : 0, variants[v], grabs[gi]);
@@ -2296,6 +2337,7 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
                 top.minb = variants[v];
                 top.grab = grabs[gi];
                 top.pushes_per_s = rate;
+                top.chunk_pushes = chunks[ci];
             }
             // restore the snapshot
             for (size_t r = 0; r < nr; ++r) {
@@ -2311,6 +2353,7 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
             }
             BCK(cudaStreamSynchronize(b->stream));
         }
+    }
     release();
     for (size_t r = 0; r < nr; ++r) {
         gpat_handle_t *h = b->runs[r];
@@ -2337,6 +2380,9 @@ int gpat_batch_set_tuning(gpat_batch_t *b, const gpat_batch_tuning_t *t) {
     bool ok = false;
     for (int v = 0; v < nv; ++v) ok = ok || variants[v] == t->minb;
     if (!ok || t->grab < 1 || t->grab > 64) return bfail(b, GPAT_ERR_ARG, "tuning outside the variants");
+    if (t->chunk_pushes < 0 || (t->chunk_pushes > 0 && t->chunk_pushes < 8) ||
+        t->chunk_pushes > 1 << 20)
+        return bfail(b, GPAT_ERR_ARG, "chunk_pushes: 0 or 8 .. 2^20");
     b->tuning = *t;
     return GPAT_OK;
 }
@@ -2776,6 +2822,55 @@ int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w
     if (nsplit) *nsplit = created;
     if (nkilled) *nkilled = (int64_t)(h->hcnt.nkilled - kill0);
     return check_status(h);
+}
+
+int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref,
+                           double z_ref, double window_ratio, int max_level) {
+    if (!h) return GPAT_ERR_ARG;
+    if (!m) {
+        h->learn_on = false;
+        return GPAT_OK;
+    }
+    if (!(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8)
+        return fail(h, GPAT_ERR_ARG, "w_ref > 0, window_ratio > 1, max_level in 1..8");
+    if (h->prm.precision != GPAT_PREC_MIXED || h->prm.ndim < 2)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "learned splitting runs in the split-precision mover");
+    if (h->dtags)
+        return fail(h, GPAT_ERR_UNSUPPORTED, "weighted splitting keeps no particle tracks");
+    CK(cudaSetDevice(h->device));
+    if (!h->learn_dev) {
+        if (cudaMalloc(&h->learn_dev, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, GPAT_ERR_OOM, "learned splitting counters");
+        }
+    }
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess)
+        return fail(h, GPAT_ERR_CUDA, "network stream");
+    FusedLearn L{};
+    L.w16 = m->w16;
+    L.norm = m->norm;
+    L.f = feature_args(h, t_norm);
+    L.s.w_ref = w_ref;
+    L.s.z_ref = z_ref;
+    L.s.sqrt_ratio = std::sqrt(window_ratio);
+    L.s.max_level = max_level;
+    L.s.key0 = (uint32_t)h->prm.seed;
+    L.s.key1 = (uint32_t)(h->prm.seed >> 32) + 2u;
+    L.z_shift = z_ref;
+    h->learn = L;
+    h->learn_on = true;
+    return GPAT_OK;
+}
+
+int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, int64_t *judged,
+                           int64_t *nsplit, int64_t *nkilled) {
+    if (!h) return GPAT_ERR_ARG;
+    const double s = fixed_to_double(h->learn_host[2], h->learn_host[3]);
+    if (log_sum_wexpz) *log_sum_wexpz = s > 0.0 ? h->learn.z_shift + std::log(s) : -INFINITY;
+    if (judged) *judged = (int64_t)h->learn_host[1];
+    if (nsplit) *nsplit = h->learn_split;
+    if (nkilled) *nkilled = h->learn_killed;
+    return GPAT_OK;
 }
 
 int gpat_tail_weights(gpat_handle_t *h, double p_threshold, int64_t *count, double *wsum,

@@ -180,6 +180,19 @@ struct WSplitArgs {
     int max_level;
     uint32_t key0, key1;
 };
+// Learned splitting inside the split-precision mover: particles that finish
+// the interval in the box are scored by the network and split or played
+// roulette in the same launch.
+struct FusedLearn {
+    const __nv_bfloat16 *w16;
+    const float *norm;
+    FeatureArgs f;
+    WSplitArgs s;
+    int64_t cap;
+    unsigned long long *count;   // particles including children (starts at the launch's total)
+    unsigned long long *zsum;    // {judged, sum of w exp(z - z_shift) as hi, lo}
+    double z_shift;
+};
 // Per-minibatch activations ([64][b] except h0: [b][8]) and output deltas.
 struct MlpTrainBuffers {
     float *h0, *a1, *a2, *a3, *h1, *h2, *h3, *dz;
@@ -211,6 +224,9 @@ cudaError_t launch_mover_fp64(const MoverArgs &a, int sm_count, cudaStream_t s);
 cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_count,
                                cudaStream_t s);
 MixedConsts make_mixed_consts(const MoverArgs &a);
+// The global-gather chunk launch with learned splitting of finished particles.
+cudaError_t launch_mover_learned(const MoverArgs &a, const MixedConsts &c, const FusedLearn &L,
+                                 cudaStream_t s);
 MixedRunArgs mixed_run_args(const MoverArgs &a);
 // Batched split-precision mover (see mover_mixed.cu).
 cudaError_t upload_batch_runs(const BatchRun *runs, int nruns, cudaStream_t s);

@@ -17,79 +17,16 @@
 #include <cfloat>
 
 #include "device_common.cuh"
+#include "learned_dev.cuh"
 #include "mlp_mma.cuh"
 
 namespace gpat {
 namespace {
 
-constexpr int kIn = kMlpFeatures, kH = kMlpHidden;
 constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kIn, kOffW2 = kOffB1 + kH;
 constexpr int kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH, kOffB3 = kOffW3 + kH * kH;
 constexpr int kOffW4 = kOffB3 + kH, kOffB4 = kOffW4 + kH;
 static_assert(kOffB4 + 1 == kMlpParams, "parameter layout");
-
-__device__ __forceinline__ void clone_particle(const DevParticles &P, int64_t i, int64_t j) {
-    P.x[j] = P.x[i]; P.y[j] = P.y[i]; P.z[j] = P.z[i]; P.p[j] = P.p[i];
-    P.v[j] = P.v[i]; P.mu[j] = P.mu[i]; P.weight[j] = P.weight[i];
-    P.t[j] = P.t[i]; P.dt[j] = P.dt[i];
-    P.split_times[j] = P.split_times[i]; P.count_flag[j] = P.count_flag[i];
-    P.origin[j] = P.origin[i]; P.nsteps_tracked[j] = P.nsteps_tracked[i];
-    P.nsteps_pushed[j] = P.nsteps_pushed[i]; P.tag_injected[j] = P.tag_injected[i];
-    P.tag_splitted[j] = P.tag_splitted[i]; P.rng_ctr[j] = P.rng_ctr[i];
-}
-
-__device__ __forceinline__ void standardise(const float *x, const float *mean, const float *istd,
-                                            float h0[kIn]) {
-#pragma unroll
-    for (int j = 0; j < kIn; ++j) h0[j] = (x[j] - mean[j]) * istd[j];
-}
-
-// ---------------------------------------------------------------------------
-// Features of particles, from the packed field records (FP32, trilinear).
-// ---------------------------------------------------------------------------
-template <int NDIM>
-__device__ void particle_features(const FeatureArgs &g, const DevParticles &P, int64_t i,
-                                  float f[kIn]) {
-    constexpr int R = (NDIM == 2) ? kRec2D : kRec3D;
-    const double px = (P.x[i] - g.xmin) * g.idx, py = (P.y[i] - g.ymin) * g.idy;
-    const double pz = (NDIM == 3) ? (P.z[i] - g.zmin) * g.idz : 0.0;
-    int cx = (int)floor(px), cy = (int)floor(py), cz = (NDIM == 3) ? (int)floor(pz) : 0;
-    float fx = (float)(px - cx), fy = (float)(py - cy), fz = (float)(pz - cz);
-    // clamp into the ghost-padded grid (a particle about to leave keeps the
-    // edge values)
-    const int ix = min(max(cx + 2, 0), g.nxg - 2), iy = min(max(cy + 2, 0), g.nyg - 2);
-    const int iz = (NDIM == 3) ? min(max(cz + 2, 0), g.nzg - 2) : 0;
-    fx = fminf(fmaxf(fx, 0.0f), 1.0f); fy = fminf(fmaxf(fy, 0.0f), 1.0f);
-    fz = fminf(fmaxf(fz, 0.0f), 1.0f);
-    float v[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = 0.0f;
-    for (int kk = 0; kk < (NDIM == 3 ? 2 : 1); ++kk)
-        for (int j = 0; j < 2; ++j)
-            for (int ii = 0; ii < 2; ++ii) {
-                float w = (ii ? fx : 1.0f - fx) * (j ? fy : 1.0f - fy);
-                if (NDIM == 3) w *= (kk ? fz : 1.0f - fz);
-                const size_t cell = (size_t)(ix + ii) +
-                                    (size_t)g.nxg * ((size_t)(iy + j) + (size_t)g.nyg * (iz + kk));
-                const float *r = g.rec + (size_t)R * cell;
-#pragma unroll
-                for (int k = 0; k < R; ++k) v[k] = fmaf(__ldg(r + k), w, v[k]);
-            }
-    f[0] = (float)((P.x[i] - g.xmin) * g.ilx);
-    f[1] = (float)((P.y[i] - g.ymin) * g.ily);
-    f[2] = (NDIM == 3) ? (float)((P.z[i] - g.zmin) * g.ilz) : 0.0f;
-    f[3] = (float)log10(P.p[i] * g.ip0);
-    if (NDIM == 2) {   // slots: vx vy bx by bz dvx/dx dvy/dy ... db/dx(13) db/dy(14)
-        f[4] = v[5] + v[6];
-        f[5] = sqrtf(v[2] * v[2] + v[3] * v[3] + v[4] * v[4]);
-        f[6] = sqrtf(v[13] * v[13] + v[14] * v[14]);
-    } else {           // slots: vx vy vz bx by bz dvx/dx dvy/dy dvz/dz ... db/dx(18..20)
-        f[4] = v[6] + v[7] + v[8];
-        f[5] = sqrtf(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
-        f[6] = sqrtf(v[18] * v[18] + v[19] * v[19] + v[20] * v[20]);
-    }
-    f[7] = g.t_norm;
-}
 
 // Appends (features, tag_injected) of every live particle to the records.
 template <int NDIM>
@@ -408,65 +345,7 @@ __global__ void __launch_bounds__(128) weighted_split_kernel(
         for (int k = 0; k < kIn; ++k) h0[k] = 0.0f;
     }
     const float z = mma_mlp::warp_forward(S, h0);   // every lane of the warp takes part
-    int j = 0;
-    double w = 0.0;
-    if (live) {
-        const double wt = a.w_ref * exp(-((double)fminf(fmaxf(z, -60.0f), 60.0f) - a.z_ref));
-        w = P.weight[i];
-        if (w > wt * a.sqrt_ratio) {
-            const int split_times = P.split_times[i];
-            j = (int)ceil(log2(w / (wt * a.sqrt_ratio)));
-            j = max(1, min(j, a.max_level));
-            j = min(j, 30 - split_times);          // int32 lineage tags
-            if (j < 1) j = 0;
-        } else if (w < wt / a.sqrt_ratio) {
-            const uint4 r = philox4x32_10(
-                make_uint4(P.rng_ctr[i], 0x524C5454u, (uint32_t)P.tag_injected[i],
-                           (uint32_t)P.tag_splitted[i]),
-                a.key0, a.key1);
-            const double u = u01_53(r.x, r.y);
-            if (u < w / wt) {
-                P.weight[i] = wt;
-            } else {
-                P.count_flag[i] = 0;               // removed at the next removal
-                atomicAdd(&cnt->nkilled, 1ull);
-            }
-        }
-    }
-    // Warp-aggregated reservation of the children slots.
-    const int lane = threadIdx.x & 31;
-    const unsigned m = (j > 0) ? ((1u << j) - 1u) : 0u;
-    unsigned inc = m;
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
-    unsigned long long base = 0;
-    int ok = 0;
-    if (lane == 31 && total > 0) {
-        unsigned long long old = *(volatile unsigned long long *)count;
-        for (int t = 0; t < 1024; ++t) {       // bounded compare-and-swap
-            if (old + total > (unsigned long long)cap) break;
-            const unsigned long long prev = atomicCAS(count, old, old + total);
-            if (prev == old) { ok = 1; base = old; break; }
-            old = prev;
-        }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 31);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    if (!ok || j == 0) return;
-    const int64_t first = (int64_t)(base + inc - m);
-    const int s = P.split_times[i];
-    const double wc = w / (double)(1u << j);
-    P.weight[i] = wc;
-    P.split_times[i] = (int8_t)(s + j);
-    for (unsigned c = 1; c <= m; ++c) {
-        const int64_t d = first + (int64_t)(c - 1);
-        clone_particle(P, i, d);
-        P.tag_splitted[d] = (int32_t)((uint32_t)P.tag_splitted[i] + (c << s));
-    }
-    atomicAdd(&cnt->nsplit, (unsigned long long)m);
+    window_split(a, P, i, live, z, cap, count, cnt);
 }
 
 // Network output of every live particle (z[i], index-aligned) and the

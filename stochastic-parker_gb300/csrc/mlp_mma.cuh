@@ -42,9 +42,21 @@ struct Smem {
     float b1[kH], b2[kH], b3[kH], w4f[kH], b4;
 };
 
-// Fills the shared image from the BF16 parameter vector (the block's threads
-// share the work; the caller synchronises).  transposed: also W2t / W3t.
-__device__ __forceinline__ void load_smem(const __nv_bfloat16 *w16, Smem &s, bool transposed) {
+// Inference-only image (no transposed copies, about 24 KB) for kernels whose
+// shared memory competes with L1 for the field gathers.
+struct SmemInf {
+    __nv_bfloat16 w1[kH * kS1];
+    __nv_bfloat16 w2[kH * kS];
+    __nv_bfloat16 w3[kH * kS];
+    __nv_bfloat16 w4[8 * kS];
+    float b1[kH], b2[kH], b3[kH], w4f[kH], b4;
+};
+
+// Fills a shared image from the BF16 parameter vector (the block's threads
+// share the work; the caller synchronises).  transposed: also W2t / W3t
+// (Smem only).
+template <class SM>
+__device__ __forceinline__ void load_smem(const __nv_bfloat16 *w16, SM &s, bool transposed) {
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
     for (int e = threadIdx.x; e < kH * kS1; e += blockDim.x) {
         const int n = e / kS1, k = e % kS1;
@@ -55,9 +67,11 @@ __device__ __forceinline__ void load_smem(const __nv_bfloat16 *w16, Smem &s, boo
         const bool in = k < kH;
         s.w2[e] = in ? w16[kOffW2 + n * kH + k] : zero;
         s.w3[e] = in ? w16[kOffW3 + n * kH + k] : zero;
-        if (transposed) {
-            s.w2t[e] = in ? w16[kOffW2 + k * kH + n] : zero;
-            s.w3t[e] = in ? w16[kOffW3 + k * kH + n] : zero;
+        if constexpr (sizeof(SM) == sizeof(Smem)) {
+            if (transposed) {
+                s.w2t[e] = in ? w16[kOffW2 + k * kH + n] : zero;
+                s.w3t[e] = in ? w16[kOffW3 + k * kH + n] : zero;
+            }
         }
     }
     for (int e = threadIdx.x; e < 8 * kS; e += blockDim.x) {
@@ -161,8 +175,8 @@ struct Stash {
 
 // Forward pass of one 16-sample tile.  Returns z of row g (zr[0]) and row g+8
 // (zr[1]) in the lanes with t == 0.
-template <bool KEEP>
-__device__ __forceinline__ void forward_tile(const Smem &s, const uint32_t (&a1)[4], int g, int t,
+template <bool KEEP, class SM>
+__device__ __forceinline__ void forward_tile(const SM &s, const uint32_t (&a1)[4], int g, int t,
                                              float (&zr)[2], Stash *st) {
     float c[8][4];
 #pragma unroll
@@ -199,7 +213,8 @@ __device__ __forceinline__ void forward_tile(const Smem &s, const uint32_t (&a1)
 
 // z of every lane's own sample: each lane holds 8 standardised inputs; lanes
 // 0..15 form tile 0, lanes 16..31 tile 1.  All 32 lanes must call.
-__device__ __forceinline__ float warp_forward(const Smem &s, const float (&x)[kIn]) {
+template <class SM>
+__device__ __forceinline__ float warp_forward(const SM &s, const float (&x)[kIn]) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     uint32_t p[4];
 #pragma unroll

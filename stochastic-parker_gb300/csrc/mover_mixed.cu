@@ -21,6 +21,9 @@
 // global memory (one particle per thread, and the batched persistent form).
 #include "mixed_body.cuh"
 
+#include "learned_dev.cuh"
+#include "mlp_mma.cuh"
+
 namespace gpat {
 
 MixedConsts make_mixed_consts(const MoverArgs &a) {
@@ -65,6 +68,49 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
         if (a.pause) a.pause[i] = active ? 1 : 0;
     }
     add_warp_counters(a.cnt, pushes, active, nullptr);
+}
+
+// The global-gather chunk kernel with learned splitting: as a particle
+// finishes its interval in the box, the warp scores it with the network
+// (tensor cores, weights staged in shared memory), adds w exp(z - z_shift)
+// to the normalisation of the next interval and applies the weight window
+// (split into lineage-tagged copies appended after the set, or roulette) in
+// the same launch.  Warps with no finished particle skip the network.
+template <int NDIM, bool NLGC>
+__global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIXED_MINB_3D)
+    mover_learned_kernel(const MixedRunArgs a, const MixedConsts k, const DevParticles P,
+                         const int64_t n, const FusedLearn L) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    mma_mlp::SmemInf &S = *reinterpret_cast<mma_mlp::SmemInf *>(smem_raw);
+    mma_mlp::load_smem(L.w16, S, false);
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = false, exited = false;
+    uint32_t pushes = 0;
+    if (i < n) {
+        pushes = move_particle<NDIM, NLGC>(a, k, P, i, active, GlobalGather{}, a.chunk_pushes,
+                                           exited);
+        if (a.pause) a.pause[i] = active ? 1 : 0;
+    }
+    add_warp_counters(a.cnt, pushes, active, nullptr);
+    const bool fin = i < n && !active && P.count_flag[i] == 1;
+    if (!__any_sync(0xffffffffu, fin)) return;
+    float h0[kMlpFeatures];
+    if (fin) {
+        float f[kMlpFeatures];
+        particle_features<NDIM>(L.f, P, i, f);
+        standardise(f, L.norm, L.norm + kMlpFeatures, h0);
+    } else {
+#pragma unroll
+        for (int q = 0; q < kMlpFeatures; ++q) h0[q] = 0.0f;
+    }
+    const float z = mma_mlp::warp_forward(S, h0);
+    if (fin) {
+        const double e = fmin(fmax((double)z - L.z_shift, -60.0), 60.0);
+        atomicAdd(&L.zsum[0], 1ull);
+        atomic_add_fixed(&L.zsum[1], &L.zsum[2], P.weight[i] * exp(e));
+    }
+    window_split(L.s, P, i, fin, z, L.cap, L.count, a.cnt);
 }
 
 // ---------------------------------------------------------------------------
@@ -157,6 +203,22 @@ cudaError_t launch_mover_mixed(const MoverArgs &a, const MixedConsts &c, int sm_
     } else {
         if (a.nlgc) mover_mixed_kernel<3, true><<<g, threads, 0, s>>>(r, c, a.P, a.n);
         else mover_mixed_kernel<3, false><<<g, threads, 0, s>>>(r, c, a.P, a.n);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mover_learned(const MoverArgs &a, const MixedConsts &c, const FusedLearn &L,
+                                 cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    const unsigned g = (unsigned)((a.n + 127) / 128);
+    const size_t smem = sizeof(mma_mlp::SmemInf);
+    const MixedRunArgs r = mixed_run_args(a);
+    if (a.ndim == 2) {
+        if (a.nlgc) mover_learned_kernel<2, true><<<g, 128, smem, s>>>(r, c, a.P, a.n, L);
+        else mover_learned_kernel<2, false><<<g, 128, smem, s>>>(r, c, a.P, a.n, L);
+    } else {
+        if (a.nlgc) mover_learned_kernel<3, true><<<g, 128, smem, s>>>(r, c, a.P, a.n, L);
+        else mover_learned_kernel<3, false><<<g, 128, smem, s>>>(r, c, a.P, a.n, L);
     }
     return cudaGetLastError();
 }

@@ -106,7 +106,8 @@ MLP_PARAMS = 8961
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("minb", i32), ("grab", i32), ("pushes_per_s", d)]
+    _fields_ = [("minb", i32), ("grab", i32), ("pushes_per_s", d), ("chunk_pushes", i32),
+                ("reserved", i32)]
 
 
 # name -> (restype, argtypes); every symbol include/gpat_engine.h declares.
@@ -173,6 +174,9 @@ SIGNATURES = {
     "gpat_particle_mover": (C.c_int, [Handle, C.c_int, C.c_int, d, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
     "gpat_split_particle": (C.c_int, [Handle, d, d, C.c_int]),
+    "gpat_set_mover_learned": (C.c_int, [Handle, C.c_void_p, d, d, d, d, C.c_int]),
+    "gpat_get_mover_learned": (C.c_int, [Handle, C.POINTER(d), C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gpat_set_mover_tiles": (C.c_int, [Handle] + [C.c_int] * 8),
     "gpat_get_mover_tiles": (C.c_int, [Handle, C.POINTER(C.c_int)]),
     "gpat_split_particle_noalloc": (C.c_int, [P(Particles), i64, i64, d, d, d, d, C.c_void_p,

@@ -75,7 +75,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines: dict | None
                                           CSRC / "gpat_internal.h", CSRC / "device_common.cuh",
                                           CSRC / "grid_common.cuh", CSRC / "track_common.cuh",
                                           CSRC / "mixed_body.cuh", CSRC / "cell_index.cuh",
-                                          CSRC / "mlp_mma.cuh"]
+                                          CSRC / "mlp_mma.cuh", CSRC / "learned_dev.cuh"]
     if out_path.exists() and not force and not defines:
         lib_mtime = out_path.stat().st_mtime
         if all(s.stat().st_mtime <= lib_mtime for s in srcs):

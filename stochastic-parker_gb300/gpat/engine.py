@@ -169,6 +169,7 @@ class Engine:
         self.lib = _abi.load()
         self.params = params
         self.cfg = mhd_config
+        self.device = device
         self.h = _abi.Handle()
         rc = self.lib.gpat_create(C.byref(params), C.byref(mhd_config), device, C.byref(self.h))
         if rc != _abi.GPAT_OK:
@@ -590,20 +591,45 @@ class Batch:
             num_fine_steps))
 
     def autotune(self, mhd_tframe=1, nlgc=False, kperp_kpara=0.01, nsteps_interval=10,
-                 num_fine_steps=1) -> dict:
+                 num_fine_steps=1, cache=None) -> dict:
+        """gpat_batch_autotune.  cache: a JSON file of earlier choices keyed by
+        the GPU and a hash of the runs' grids, sizes and parameters; a hit
+        applies the stored choice without timing."""
+        key = self._cache_key(nlgc) if cache else None
+        if cache:
+            table = _read_cache(cache)
+            if key in table:
+                c = table[key]
+                self.set_tuning(c["minb"], c["grab"], c["chunk_pushes"])
+                return dict(c, cached=True)
         t = _abi.BatchTuning()
         self._check(self.lib.gpat_batch_autotune(
             self.b, self._frames(mhd_tframe), int(nlgc), kperp_kpara, nsteps_interval,
             num_fine_steps, C.byref(t)))
-        return dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s)
+        out = dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s,
+                   chunk_pushes=t.chunk_pushes)
+        if cache:
+            table = _read_cache(cache)
+            table[key] = out
+            _write_cache(cache, table)
+        return out
+
+    def _cache_key(self, nlgc) -> str:
+        import hashlib
+        import torch
+        gpu = torch.cuda.get_device_name(self.engines[0].device) if torch.cuda.is_available() else "?"
+        desc = [(e.cfg.nx, e.cfg.ny, e.cfg.nz, e.nptl_current, e.params.kpara0, e.params.kret,
+                 e.params.ndim, e.params.bin_interval) for e in self.engines]
+        return gpu + ":" + hashlib.sha1(repr((desc, bool(nlgc))).encode()).hexdigest()[:16]
 
     def tuning(self) -> dict:
         t = _abi.BatchTuning()
         self._check(self.lib.gpat_batch_get_tuning(self.b, C.byref(t)))
-        return dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s)
+        return dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s,
+                    chunk_pushes=t.chunk_pushes)
 
-    def set_tuning(self, minb, grab):
-        t = _abi.BatchTuning(minb, grab, 0.0)
+    def set_tuning(self, minb, grab, chunk_pushes=0):
+        t = _abi.BatchTuning(minb, grab, 0.0, chunk_pushes, 0)
         self._check(self.lib.gpat_batch_set_tuning(self.b, C.byref(t)))
 
     def stats(self) -> dict:
@@ -707,6 +733,35 @@ def weighted_split(eng, mlp: Mlp, t_norm, w_ref, z_ref, window_ratio=4.0, max_le
     eng._check(eng.lib.gpat_weighted_split(eng.h, mlp.m, t_norm, w_ref, z_ref, window_ratio,
                                            max_level, C.byref(ns), C.byref(nk)))
     return ns.value, nk.value
+
+
+def set_mover_learned(eng, mlp, t_norm=0.0, w_ref=1.0, z_ref=0.0, window_ratio=4.0,
+                      max_level=3):
+    """gpat_set_mover_learned: learned splitting of particles as they finish
+    an interval, inside the mover launch; mlp = None turns it off."""
+    eng._check(eng.lib.gpat_set_mover_learned(eng.h, mlp.m if mlp is not None else None, t_norm,
+                                              w_ref, z_ref, window_ratio, max_level))
+
+
+def mover_learned_stats(eng) -> dict:
+    """gpat_get_mover_learned after a mover call."""
+    lse, j, ns, nk = C.c_double(), C.c_int64(), C.c_int64(), C.c_int64()
+    eng._check(eng.lib.gpat_get_mover_learned(eng.h, C.byref(lse), C.byref(j), C.byref(ns),
+                                              C.byref(nk)))
+    return dict(log_sum_wexpz=lse.value, judged=j.value, nsplit=ns.value, nkilled=nk.value)
+
+
+def _read_cache(path) -> dict:
+    import json
+    try:
+        return json.loads(Path(path).read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _write_cache(path, table: dict):
+    import json
+    Path(path).write_text(json.dumps(table, indent=1, sort_keys=True))
 
 
 def tail_weights(eng, p_threshold):

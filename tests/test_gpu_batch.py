@@ -82,7 +82,10 @@ def test_batch_autotune_leaves_runs_unchanged():
     batch = Batch(batched)
     best = batch.autotune(mhd_tframe=1)
     assert best["minb"] in (5, 6, 8) and best["grab"] in (1, 4) and best["pushes_per_s"] > 0
+    assert best["chunk_pushes"] in (64, 128, 256)
     assert batch.tuning()["minb"] == best["minb"]
+    # the chunk length moves the pause points: compare with the runs' own (64)
+    batch.set_tuning(best["minb"], best["grab"], 0)
     for k in range(2):
         for e in solo:
             e.particle_mover(mhd_tframe=k + 1)

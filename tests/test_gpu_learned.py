@@ -102,3 +102,57 @@ def test_learned_splitting_3d_unbiased_and_more_samples():
     for e in (plain, eng_l):
         e.close()
     net.close()
+
+
+def test_learned_splitting_fused_in_the_mover():
+    """The same method with the network evaluated inside the mover launch as
+    particles finish each interval (gpat_set_mover_learned): the tail weight
+    agrees with a plain run within Monte Carlo error, every finished particle
+    is judged, the tail gets more effective samples per push, and lineage
+    tags stay unique."""
+    from gpat.engine import mover_learned_stats, set_mover_learned
+    n_grid, nptl, nint = 32, 20000, 8
+    w = configs.turbulence_3d(scale=nptl / 1e8, n=n_grid, nframes=nint)
+    net = Mlp(seed=9, record_capacity=nptl * nint)
+    plain = configs.build_engine(w, nptl_max=nptl * 40)
+    configs.inject(plain, w)
+    pushes_plain = 0
+    for k in range(nint):
+        net.record(plain, k / nint)
+        plain.particle_mover(mhd_tframe=k + 1)
+        pushes_plain += plain.counters().last_mover_steps
+    pthr = float(np.quantile(plain.get_particles()["p"], 0.98))
+    net.label(plain, pthr)
+    net.train(epochs=4, batch=4096, lr=3e-3, seed=3)
+
+    target = 2 * nptl
+    eng = configs.build_engine(w, nptl_max=nptl * 40)
+    configs.inject(eng, w)
+    _, lse = net.score(eng, 0.0)
+    pushes = 0
+    for k in range(nint):
+        set_mover_learned(eng, net, (k + 1) / nint, 1.0, lse - math.log(target), 4.0, 3)
+        n_before = eng.nptl_current
+        eng.particle_mover(mhd_tframe=k + 1)
+        pushes += eng.counters().last_mover_steps
+        st = mover_learned_stats(eng)
+        # a periodic box: every particle finishes the interval and is judged once
+        assert st["judged"] == n_before, (st, n_before)
+        assert eng.nptl_current == n_before + st["nsplit"] - st["nkilled"]
+        lse = st["log_sum_wexpz"]
+    set_mover_learned(eng, None)
+    c0, w0, w20 = tail_weights(plain, pthr)
+    c1, w1, w21 = tail_weights(eng, pthr)
+    assert abs(w1 - w0) < 4.0 * math.sqrt(w20 + w21), (w0, w1, w20, w21)
+    ess0, ess1 = w0 * w0 / w20, w1 * w1 / w21
+    assert ess1 / pushes > 1.5 * ess0 / pushes_plain, (ess0, ess1, pushes_plain, pushes)
+    ps = eng.get_particles()
+    key = (ps["tag_injected"].astype(np.int64) << 32) | (ps["tag_splitted"].astype(np.int64) &
+                                                         0xFFFFFFFF)
+    assert len(np.unique(key)) == len(key)
+    # the total weight is kept in expectation only: roulette survivors carry
+    # w_t >> w, so the sum fluctuates widely; a sanity range
+    assert 0.3 * nptl < ps["weight"].sum() < 3.0 * nptl
+    for e in (plain, eng):
+        e.close()
+    net.close()
