@@ -87,6 +87,16 @@ def parse_args(argv=None):
                     help="pushes between re-binnings (0: engine default, <0: once per call)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 sample and the f(p) tail-error check")
+    ap.add_argument("--intervals", type=int, default=0,
+                    help="learned_3d: MHD intervals of every arm (0: the first interval count "
+                         "at which a pilot plain run has 0.1 %% of its particles above 100 p0)")
+    ap.add_argument("--train-trajectories", type=float, default=1e7,
+                    help="learned_3d: plain trajectories generating the training records")
+    ap.add_argument("--record-every", type=int, default=0,
+                    help="learned_3d: intervals between training records of a trajectory "
+                         "(0: ten records over the run)")
+    ap.add_argument("--fp64-particles", type=float, default=2e5,
+                    help="learned_3d: particles of the FP64 judge")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline workload only (no 3D and batched keys in its line)")
     ap.add_argument("--tiles-3d", default="off",
@@ -668,54 +678,107 @@ def run_batch(args, world, rank, local):
     return line
 
 
+# Fraction of the weighted mean importance added to every particle's in the
+# learned arm (defensive importance sampling, Hesterberg 1995).
+DEFENSIVE = 0.1
+
+
 def run_learned(args, world, rank, local):
-    """Learned splitting on the 3D compressible-turbulence field: a plain run
-    generates training records, the network is trained on the GPU, then
-    plain, fixed-threshold and learned splitting runs of the same size are
-    timed and their effective samples in the momentum tail compared."""
+    """Learned splitting on the 256^3 compressible-turbulence field (the 3D
+    workload's field and transport, f(p) up to 1e4 p0).  A plain run of
+    n_train trajectories over the whole run length generates the training
+    records (every record_every intervals) and labels them by whether the
+    trajectory ends above p_label; the network is trained on the GPU.  Then,
+    on fresh particles, four arms run the same intervals:
+      plain      split-precision, no splitting (4x the particles);
+      fixed      split-precision with split_particle's fixed thresholds;
+      learned    split-precision with the network applied inside the mover
+                 as particles finish each interval (weight window 4, the
+                 particle cap of 4e8, importance exp(z) floored at DEFENSIVE
+                 times its weighted mean so roulette weights stay bounded);
+      fp64       the FP64 mover with fixed-threshold splitting: the judge.
+    Each reports the weighted count above 100 p0 and its effective samples
+    (sum w)^2 / sum w^2 per second."""
     import numpy as np
     import torch
     from gpat import configs
-    from gpat.engine import GPATCapacityError, Mlp, tail_weights, weighted_split
+    from gpat.engine import (FusedWindow, GPATCapacityError, Mlp, mover_learned_stats,
+                             set_mover_learned, tail_weights)
 
     torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    nint = 16
-    n_train = max(1000, int(2e6 * args.scale))
+    n_train = max(1000, int(args.train_trajectories * args.scale))
     n_cmp = max(1000, int(1e6 * args.scale))
-    w = make_workload(args, 1, seed=3 + rank, nframes=nint, scale=n_train / 1e8)
+    n_fp64 = max(1000, int(args.fp64_particles * args.scale))
+    max_intervals = args.intervals if args.intervals > 0 else 100
+    w = make_workload(args, 1, seed=3 + rank, nframes=max_intervals, scale=n_train / 1e8)
     p0 = w.params["p0"]
+    pyield = 100.0 * p0
+    if args.intervals > 0:
+        nint, pilot = args.intervals, None
+    else:
+        # run length: the first interval count at which 0.1 % of a plain
+        # run's particles are above 100 p0 (100 p0 is then a tail)
+        n_pilot = max(20000, int(2e5 * args.scale))
+        eng = configs.build_engine(w, device=local, nptl_max=n_pilot, seed=50 + rank,
+                                   pmax=1.0e4 * p0)
+        configs.inject(eng, w, nptl=n_pilot)
+        nint, frac = max_intervals, 0.0
+        for k in range(max_intervals):
+            eng.particle_mover(mhd_tframe=k + 1)
+            frac = tail_weights(eng, pyield)[1] / n_pilot
+            if frac >= 1e-3:
+                nint = k + 1
+                break
+        eng.close()
+        pilot = {"particles": n_pilot, "intervals": nint, "fraction_above_100p0": frac}
+        print(f"learned_3d: run length {nint} intervals ({frac:.2e} of {n_pilot} pilot "
+              f"particles above 100 p0)", file=sys.stderr, flush=True)
     fixed_ratio, fixed_pmin = 1.5, 6.0
+    every = args.record_every if args.record_every > 0 else max(1, nint // 10)
 
-    def arm(kind, n, seed, recorder=None, net=None, target=None, cap=None):
-        eng = configs.build_engine(w, device=local, nptl_max=cap or 2 * n, seed=seed)
+    def arm(kind, n, seed, recorder=None, net=None, target=None, cap=None, precision=1):
+        eng = configs.build_engine(w, device=local, nptl_max=cap or 2 * n, seed=seed,
+                                   precision=precision, pmax=1.0e4 * p0)
         configs.inject(eng, w, nptl=n)
-        pushes, capped = 0, False
+        pushes, capped, judged = 0, False, 0
+        win = FusedWindow(target, DEFENSIVE) if kind == "learned" else None
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        if kind == "learned":
+            win.start(*net.score(eng, 0.0)[1:])
         for k in range(nint):
-            if kind == "learned":
-                _, lse = net.score(eng, k / nint)
-                weighted_split(eng, net, k / nint, 1.0, lse - math.log(target), window_ratio=4.0,
-                               max_level=3)
-            if recorder is not None:
+            if recorder is not None and k % every == 0:
                 recorder.record(eng, k / nint)
+            if kind == "learned":
+                z_ref, z_floor = win.params()
+                set_mover_learned(eng, net, (k + 1) / nint, 1.0, z_ref, 4.0, 3, z_floor=z_floor)
             eng.particle_mover(mhd_tframe=k + 1)
             pushes += eng.counters().last_mover_steps
-            if kind == "fixed" and not capped:
+            if kind == "learned":
+                st = mover_learned_stats(eng)
+                judged += st["judged"]
+                win.update(st)
+            if kind in ("fixed", "fp64") and not capped:
                 try:
                     eng.split_particle(fixed_ratio, fixed_pmin, 10)
                 except GPATCapacityError:
                     capped = True
         torch.cuda.synchronize()
-        return eng, pushes, time.perf_counter() - t0
+        secs = time.perf_counter() - t0
+        if kind == "learned":
+            set_mover_learned(eng, None)
+        return eng, pushes, secs, capped
 
-    # 1. plain run generating the training records
-    net = Mlp(device=local, seed=7 + rank, record_capacity=n_train * nint)
-    eng, train_pushes, train_s = arm("plain", n_train, 100 + rank, recorder=net)
+    # 1. plain run generating the training records; labels from its final momenta
+    net = Mlp(device=local, seed=7 + rank,
+              record_capacity=n_train * ((nint + every - 1) // every))
+    eng, train_pushes, train_s, _ = arm("plain", n_train, 100 + rank, recorder=net)
+    print(f"learned_3d: training run {n_train} trajectories, {train_pushes} pushes in "
+          f"{train_s:.1f} s", file=sys.stderr, flush=True)
     p_end = eng.get_particles()["p"]
-    pthr = float(np.quantile(p_end, 0.999))
-    npos, nrec = net.label(eng, pthr)
+    p_label = float(min(pyield, np.quantile(p_end, 0.999)))
+    reached = int(np.sum(p_end > pyield))
+    npos, nrec = net.label(eng, p_label)
     eng.close()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -723,64 +786,70 @@ def run_learned(args, world, rank, local):
     torch.cuda.synchronize()
     fit_s = time.perf_counter() - t0
 
-    # 2. the three arms on fresh particles (another injection seed)
+    # 2. the arms on fresh particles (another injection seed)
     out = {}
     clocks = ClockSampler(local)
     clocks.start()
-    # the plain arm runs 4x the particles: it is the tail reference
-    for kind, n, kw in (("plain", 4 * n_cmp, {}), ("fixed", n_cmp, dict(cap=16 * n_cmp)),
-                        ("learned", n_cmp, dict(net=net, target=2 * n_cmp, cap=16 * n_cmp))):
-        e, pushes, secs = arm(kind, n, 200 + rank, **kw)
-        c, ws, w2 = tail_weights(e, pthr)
+    for kind, n, kw in (("plain", 2 * n_cmp, {}),
+                        ("fixed", n_cmp, dict(cap=4 * n_cmp)),
+                        ("learned", n_cmp, dict(net=net, target=2 * n_cmp, cap=int(4e8))),
+                        ("fp64", n_fp64, dict(cap=4 * n_fp64, precision=0))):
+        e, pushes, secs, capped = arm(kind, n, 200 + rank, **kw)
+        c, ws, w2 = tail_weights(e, pyield)
+        _, wall, _ = tail_weights(e, 0.0)
         ess = ws * ws / w2 if w2 > 0 else 0.0
         out[kind] = {"particles": n, "pushes": pushes, "seconds": secs,
-                     "particle_steps_per_s": pushes / secs,
-                     "tail_particles": c, "tail_weight": ws,
-                     "tail_weight_sigma": math.sqrt(w2), "ess": ess,
-                     "ess_per_s": ess / secs, "final_particles": e.nptl_current}
+                     "particle_steps_per_s": pushes / secs, "capped": capped,
+                     "tail_particles": c, "tail_fraction": ws / n,
+                     "tail_fraction_sigma": math.sqrt(w2) / n, "ess": ess,
+                     "ess_per_s": ess / secs, "final_particles": e.nptl_current,
+                     "total_weight_over_injected": wall / n}
+        print(f"learned_3d: {kind} " + json.dumps(out[kind]), file=sys.stderr, flush=True)
         e.close()
     clk = clocks.stop()
     net.close()
-    # tail fractions (weight above the threshold per injected weight)
-    for d in out.values():
-        d["tail_fraction"] = d["tail_weight"] / d["particles"]
-        d["tail_fraction_sigma"] = d["tail_weight_sigma"] / d["particles"]
-    ref = out["plain"]
-    learned = out["learned"]
-    for kind in ("fixed", "learned"):
+    judge = out["fp64"]
+    for kind in ("plain", "fixed", "learned"):
         d = out[kind]
-        if ref["tail_fraction"] > 0:
-            d["tail_err_vs_plain"] = d["tail_fraction"] / ref["tail_fraction"] - 1.0
+        if judge["tail_fraction"] > 0:
+            d["tail_err_vs_fp64"] = d["tail_fraction"] / judge["tail_fraction"] - 1.0
             d["tail_err_sigma"] = math.hypot(d["tail_fraction_sigma"],
-                                             ref["tail_fraction_sigma"]) / ref["tail_fraction"]
+                                             judge["tail_fraction_sigma"]) / judge["tail_fraction"]
     if rank != 0:
         return
+    learned = out["learned"]
     line = {"metric": METRIC, "value": learned["particle_steps_per_s"], "unit": UNIT,
             "n_gpus": world, "steps": 1, "warmup": 0,
             "ms_per_step": 1e3 * learned["seconds"] / nint,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"learned_splitting_{w.name}", "particles": n_cmp,
-                       "intervals": nint,
-                       "step": "one MHD interval of the learned-splitting arm (weighted split + "
-                               "particle_mover)",
-                       "threshold_p_over_p0": pthr / p0,
-                       "threshold_rule": "99.9th percentile of the plain run's final momenta "
-                                         "(no particle of this field reaches 100 p0 in the run)",
+                       "intervals": nint, "run_length_pilot": pilot,
+                       "yield_threshold_p_over_p0": pyield / p0,
+                       "label_threshold_p_over_p0": p_label / p0,
+                       "label_rule": "trajectory ends above min(100 p0, 99.9th percentile of "
+                                     "the plain run's final momenta)",
+                       "training_particles_above_100p0": reached,
+                       "step": "one MHD interval of the learned arm (mover with the network "
+                               "applied to particles finishing the interval)",
                        "l2": "inputs exceed L2 (256^3 field records 1.7 GB)",
                        "parallelism": f"replicas x{world}"},
-            "clocks": clk,
-            "gpu_launches": None,
-            "e2e": None,
+            "clocks": clk, "gpu_launches": None, "e2e": None,
             "learned_splitting": {
-                "network": "8-64-64-64-1 SiLU, BF16 weights, FP32 accumulation",
+                "network": "8-64-64-64-1 SiLU, BF16 weights and activations, FP32 accumulation "
+                           "(mma.sync m16n8k16)",
+                "importance": f"exp(z) + {DEFENSIVE} x weighted mean of exp(z) (defensive mixture)",
+                "weight_window_ratio": 4.0, "max_split_level": 3,
                 "training": {"trajectories": n_train, "records": nrec, "positives": npos,
-                             "plain_run_seconds": train_s, "fit_seconds": fit_s,
-                             "final_loss": loss, "epochs": 3, "negatives_kept": 0.25},
+                             "record_every_intervals": every, "plain_run_seconds": train_s,
+                             "fit_seconds": fit_s, "final_loss": loss, "epochs": 3},
                 "fixed_threshold": {"split_ratio": fixed_ratio, "pmin_split": fixed_pmin},
+                "judge": "FP64 mover with fixed-threshold splitting",
                 "arms": out,
-                "ess_per_s_learned_over_fixed": learned["ess_per_s"] / max(out["fixed"]["ess_per_s"], 1e-30),
-                "ess_per_s_learned_over_plain": learned["ess_per_s"] / max(out["plain"]["ess_per_s"], 1e-30)}}
+                "ess_per_s_learned_over_fixed":
+                    learned["ess_per_s"] / max(out["fixed"]["ess_per_s"], 1e-30),
+                "ess_per_s_learned_over_plain":
+                    learned["ess_per_s"] / max(out["plain"]["ess_per_s"], 1e-30)}}
     print(json.dumps(line), flush=True)
 
 

@@ -469,11 +469,15 @@ typedef struct gpat_batch gpat_batch_t;
  * block takes per scheduler step; pushes_per_s = the measured rate;
  * chunk_pushes = pushes per particle between re-binnings for every run (0:
  * each run's own bin_interval).  minb and grab do not change results;
- * chunk_pushes moves the pause points, so results agree statistically. */
+ * chunk_pushes moves the pause points, so results agree statistically.
+ * default_pushes_per_s: gpat_batch_autotune's measured rate of the untuned
+ * launch (the single-run kernel's register target, one tile per grab, the
+ * first run's own chunk length); 0 where not measured. */
 typedef struct gpat_batch_tuning {
     int32_t minb, grab;
     double pushes_per_s;
     int32_t chunk_pushes, reserved;
+    double default_pushes_per_s;
 } gpat_batch_tuning_t;
 int gpat_batch_create(gpat_handle_t *const *runs, int nruns, gpat_batch_t **out);
 int gpat_batch_destroy(gpat_batch_t *b);
@@ -533,36 +537,44 @@ int gpat_mlp_label(gpat_mlp_t *m, gpat_handle_t *h, double p_threshold, int64_t 
  * bias is corrected by log(neg_keep) afterwards). */
 int gpat_mlp_train(gpat_mlp_t *m, int epochs, int64_t batch, double lr, double neg_keep,
                    uint64_t seed, double *final_loss);
-/* Over a run's live particles at time t_norm: the mean output and
- * log(sum_i w_i exp(z_i)).  With z_ref = log_sum_wexpz - log(N) and
- * w_ref = 1, gpat_weighted_split aims the population at N particles
- * (sum_i w_i / w_t,i = N). */
+/* Over a run's live particles at time t_norm: the mean output,
+ * L = log(sum_i w_i exp(z_i)) and log(sum_i w_i).  Defensive importance
+ * (a fraction alpha of the weighted mean importance added to every
+ * particle's): z_floor = log(alpha) + L - log(sum w) and
+ * z_ref = L + log(1 + alpha) - log(N); with w_ref = 1 gpat_weighted_split
+ * then aims the population at N particles (sum_i w_i / w_t,i = N) and no
+ * roulette survivor weighs more than about (1 + alpha) / alpha times the
+ * mean weight per target particle. */
 int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_z,
-                   double *log_sum_wexpz);
-/* Weighted split / roulette of a run's particles: target weight
- * w_t = w_ref exp(z_ref - z), window [w_t / sqrt(window_ratio),
+                   double *log_sum_wexpz, double *log_sum_w);
+/* Weighted split / roulette of a run's particles: floored log-importance
+ * z' = log(exp(z) + exp(z_floor)) (z_floor = -INFINITY: none), target
+ * weight w_t = w_ref exp(z_ref - z'), window [w_t / sqrt(window_ratio),
  * w_t sqrt(window_ratio)]; above it a particle splits into 2^j copies
  * (j <= max_level, children appended up to nptl_max), below it survives
  * with probability w / w_t at weight w_t (roulette draws are Philox,
- * keyed by the particle's tags and push counter). */
+ * keyed by the particle's tags and push counter).  Both keep the expected
+ * weight of every particle. */
 int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
-                        double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled);
+                        double z_floor, double window_ratio, int max_level, int64_t *nsplit,
+                        int64_t *nkilled);
 /* No counterpart in the reference.  Learned splitting inside the mover:
  * while set, gpat_particle_mover's split-precision chunk launches score every
  * particle that finishes the interval in the box with the network m (tensor
  * cores, in the same launch) at features of normalised time t_norm, and apply
- * gpat_weighted_split's weight window around w_t = w_ref exp(-(z - z_ref)):
- * children are appended after the set (up to nptl_max), roulette losers are
- * removed.  The brick mover is not used while this is set.  m = NULL turns it
- * off.  The network must outlive the setting. */
+ * gpat_weighted_split's weight window (same z_ref, z_floor, window_ratio,
+ * max_level): children are appended after the set (up to nptl_max), roulette
+ * losers are removed.  The brick mover is not used while this is set.
+ * m = NULL turns it off.  The network must outlive the setting. */
 int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref,
-                           double z_ref, double window_ratio, int max_level);
-/* After a mover call with learned splitting: log of the sum of w exp(z) over
- * the judged particles (before their split; the next call's z_ref is this
- * minus log of the target population), their number, children created and
- * particles removed by roulette. */
-int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, int64_t *judged,
-                           int64_t *nsplit, int64_t *nkilled);
+                           double z_ref, double z_floor, double window_ratio, int max_level);
+/* After a mover call with learned splitting, over the judged particles
+ * (before their split): log of the sum of w exp(z) and log of the sum of w
+ * (the next call's z_ref and z_floor follow from them as for
+ * gpat_mlp_score's), their number, children created and particles removed
+ * by roulette. */
+int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, double *log_sum_w,
+                           int64_t *judged, int64_t *nsplit, int64_t *nkilled);
 /* Count, sum of weights and of squared weights of live particles with
  * p > p_threshold: (sum w)^2 / sum w^2 is their effective sample size. */
 int gpat_tail_weights(gpat_handle_t *h, double p_threshold, int64_t *count, double *wsum,

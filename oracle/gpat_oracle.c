@@ -1796,34 +1796,46 @@ static void push_1d_ft(const mover_ctx *c, ptl_state *s, const double *f, const 
 /* particle_boundary_condition on a single rank: particle_module.f90:1984-2129.
  * A periodic direction has itself as neighbour and wraps by the box passed
  * in; an open direction escapes with count_flag -1..-6 and adds to leak. */
+/* After particle_boundary_condition's one-period wrap (particle_module.f90
+ * :1984-2129): a push longer than a period leaves the particle outside, where
+ * the reference indexes outside its arrays (undefined).  The engine wraps by
+ * whole periods more; inside the box this is the identity. */
+static double wrap_rest(double x, double lo, double hi)
+{
+    const double per = hi - lo;
+    if (x < lo) x += per * ceil((lo - x) / per);
+    else if (x > hi) x -= per * ceil((x - hi) / per);
+    return x;
+}
+
 static void boundary(const mover_ctx *c, ptl_state *s, double xlo, double xhi, double ylo,
                      double yhi, double zlo, double zhi, thread_acc *acc)
 {
     const orc_params *pr = c->pr;
     if (s->x < xlo && s->flag == 1) {
         if (pr->pbcx) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -1; }
-        else s->x = s->x - xlo + xhi;
+        else s->x = wrap_rest(s->x - xlo + xhi, xlo, xhi);
     } else if (s->x > xhi && s->flag == 1) {
         if (pr->pbcx) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -2; }
-        else s->x = s->x - xhi + xlo;
+        else s->x = wrap_rest(s->x - xhi + xlo, xlo, xhi);
     }
     if (c->ndim > 1) {
         if (s->y < ylo && s->flag == 1) {
             if (pr->pbcy) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -3; }
-            else s->y = s->y - ylo + yhi;
+            else s->y = wrap_rest(s->y - ylo + yhi, ylo, yhi);
         } else if (s->y > yhi && s->flag == 1) {
             if (pr->pbcy) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -4; }
-            else s->y = s->y - yhi + ylo;
+            else s->y = wrap_rest(s->y - yhi + ylo, ylo, yhi);
         }
     }
     /* z too for include_3rd_dim runs (:2084) */
     if (c->ndim == 3 || c->i3) {
         if (s->z < zlo && s->flag == 1) {
             if (pr->pbcz) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -5; }
-            else s->z = s->z - zlo + zhi;
+            else s->z = wrap_rest(s->z - zlo + zhi, zlo, zhi);
         } else if (s->z > zhi && s->flag == 1) {
             if (pr->pbcz) { orc_fixed_add(&acc->leak_hi, &acc->leak_lo, s->weight); s->flag = -6; }
-            else s->z = s->z - zhi + zlo;
+            else s->z = wrap_rest(s->z - zhi + zlo, zlo, zhi);
         }
     }
 }

@@ -74,7 +74,7 @@ struct gpat_handle {
     bool learn_on = false;
     FusedLearn learn{};
     unsigned long long *learn_dev = nullptr;
-    unsigned long long learn_host[4] = {};
+    unsigned long long learn_host[6] = {};
     int64_t learn_split = 0, learn_killed = 0;
     int64_t n_active = 0;
     int64_t last_sort_bins = 0;
@@ -1506,7 +1506,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
         const int64_t max_chunks = (int64_t)a.max_pushes / (a.chunk_pushes ? a.chunk_pushes : 1) + 4;
         const unsigned long long split0 = h->hcnt.nsplit, kill0 = h->hcnt.nkilled;
         if (learned)
-            CK(cudaMemsetAsync(h->learn_dev + 1, 0, 3 * sizeof(unsigned long long), h->stream));
+            CK(cudaMemsetAsync(h->learn_dev + 1, 0, 5 * sizeof(unsigned long long), h->stream));
         for (;;) {
             CK(cudaMemsetAsync(&h->dcnt->nactive, 0, sizeof(unsigned long long), h->stream));
             a.P = h->P[h->cur];
@@ -1523,7 +1523,7 @@ int gpat_particle_mover(gpat_handle_t *h, int focused_transport, int nlgc, doubl
                 CK(cudaEventRecord(h->ev0, h->stream));
                 CK(launch_mover_learned(a, k, L, h->stream));
                 CK(cudaEventRecord(h->ev1, h->stream));
-                CK(cudaMemcpyAsync(h->learn_host, h->learn_dev, 4 * sizeof(unsigned long long),
+                CK(cudaMemcpyAsync(h->learn_host, h->learn_dev, 6 * sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, h->stream));
                 CK(cudaStreamSynchronize(h->stream));
                 h->n = (int64_t)h->learn_host[0];
@@ -2302,6 +2302,10 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
     const int chunks[3] = {64, 128, 256};
     gpat_batch_tuning_t top{};
     top.pushes_per_s = -1.0;
+    const int def_minb = b->ndim == 2 ? 6 : 5;
+    const int bi0 = b->runs[0]->prm.bin_interval;
+    const int def_chunk = bi0 == 0 ? 128 : (bi0 > 0 ? bi0 : 0);
+    double def_rate = 0.0;
     for (int ci = 0; ci < 3; ++ci) {
         for (size_t r = 0; r < nr; ++r) b->desc[r].a.chunk_pushes = (uint32_t)chunks[ci];
         BCK(upload_batch_runs(b->desc.data(), (int)nr, b->stream));
@@ -2333,6 +2337,8 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
                 pushes += c.steps - before[r];
             }
             const double rate = ms > 0.0f ? (double)pushes / (ms * 1e-3) : 0.0;
+            if (variants[v] == def_minb && grabs[gi] == 1 && chunks[ci] == def_chunk)
+                def_rate = rate;
             if (rate > top.pushes_per_s) {
                 top.minb = variants[v];
                 top.grab = grabs[gi];
@@ -2362,6 +2368,7 @@ int gpat_batch_autotune(gpat_batch_t *b, const int *mhd_tframe, int nlgc, double
         h->cur = 0;
         h->unsorted = false;
     }
+    top.default_pushes_per_s = def_rate;
     b->tuning = top;
     if (best) *best = top;
     return GPAT_OK;
@@ -2756,7 +2763,7 @@ int gpat_mlp_train(gpat_mlp_t *m, int epochs, int64_t batch, double lr, double n
 }
 
 int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_z,
-                   double *log_sum_wexpz) {
+                   double *log_sum_wexpz, double *log_sum_w) {
     if (!m || !h) return GPAT_ERR_ARG;
     MCK(cudaSetDevice(m->device));
     const int64_t n = h->n;
@@ -2764,13 +2771,13 @@ int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_
     int rc = mlp_xbuf(m, n);
     if (rc) return rc;
     unsigned long long *out = nullptr;
-    MCK(cudaMalloc(&out, 5 * sizeof(unsigned long long) + sizeof(int)));
-    int *zmax_key = reinterpret_cast<int *>(out + 5);
+    MCK(cudaMalloc(&out, 7 * sizeof(unsigned long long) + sizeof(int)));
+    int *zmax_key = reinterpret_cast<int *>(out + 7);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
         cudaFree(out);
         return mfail(m, GPAT_ERR_CUDA, "run stream");
     }
-    unsigned long long r[5] = {};
+    unsigned long long r[7] = {};
     int key = 0;
     cudaError_t e = launch_score(m->w16, m->norm, feature_args(h, t_norm), h->prm.ndim, h->P[h->cur],
                                  n, m->zbuf, zmax_key, out, m->stream);
@@ -2786,12 +2793,15 @@ int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_
     std::memcpy(&zmax, &kb, sizeof zmax);
     if (mean_z) *mean_z = fixed_to_double(r[1], r[2]) / (double)r[0] - 64.0;
     if (log_sum_wexpz) *log_sum_wexpz = (double)zmax + std::log(fixed_to_double(r[3], r[4]));
+    if (log_sum_w) *log_sum_w = std::log(fixed_to_double(r[5], r[6]));
     return GPAT_OK;
 }
 
 int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
-                        double window_ratio, int max_level, int64_t *nsplit, int64_t *nkilled) {
-    if (!h || !m || !(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8)
+                        double z_floor, double window_ratio, int max_level, int64_t *nsplit,
+                        int64_t *nkilled) {
+    if (!h || !m || !(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8 ||
+        std::isnan(z_ref) || std::isnan(z_floor) || z_floor == INFINITY)
         return GPAT_ERR_ARG;
     if (h->dtags)
         return fail(h, GPAT_ERR_UNSUPPORTED, "weighted splitting keeps no particle tracks");
@@ -2804,6 +2814,7 @@ int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w
     WSplitArgs a{};
     a.w_ref = w_ref;
     a.z_ref = z_ref;
+    a.z_floor = z_floor;
     a.sqrt_ratio = std::sqrt(window_ratio);
     a.max_level = max_level;
     a.key0 = (uint32_t)h->prm.seed;
@@ -2825,21 +2836,23 @@ int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w
 }
 
 int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref,
-                           double z_ref, double window_ratio, int max_level) {
+                           double z_ref, double z_floor, double window_ratio, int max_level) {
     if (!h) return GPAT_ERR_ARG;
     if (!m) {
         h->learn_on = false;
         return GPAT_OK;
     }
-    if (!(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8)
-        return fail(h, GPAT_ERR_ARG, "w_ref > 0, window_ratio > 1, max_level in 1..8");
+    if (!(w_ref > 0.0) || !(window_ratio > 1.0) || max_level < 1 || max_level > 8 ||
+        !std::isfinite(z_ref) || std::isnan(z_floor) || z_floor == INFINITY)
+        return fail(h, GPAT_ERR_ARG,
+                    "w_ref > 0, window_ratio > 1, max_level in 1..8, z_ref finite, z_floor < inf");
     if (h->prm.precision != GPAT_PREC_MIXED || h->prm.ndim < 2)
         return fail(h, GPAT_ERR_UNSUPPORTED, "learned splitting runs in the split-precision mover");
     if (h->dtags)
         return fail(h, GPAT_ERR_UNSUPPORTED, "weighted splitting keeps no particle tracks");
     CK(cudaSetDevice(h->device));
     if (!h->learn_dev) {
-        if (cudaMalloc(&h->learn_dev, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        if (cudaMalloc(&h->learn_dev, 6 * sizeof(unsigned long long)) != cudaSuccess) {
             cudaGetLastError();
             return fail(h, GPAT_ERR_OOM, "learned splitting counters");
         }
@@ -2852,6 +2865,7 @@ int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, doubl
     L.f = feature_args(h, t_norm);
     L.s.w_ref = w_ref;
     L.s.z_ref = z_ref;
+    L.s.z_floor = z_floor;
     L.s.sqrt_ratio = std::sqrt(window_ratio);
     L.s.max_level = max_level;
     L.s.key0 = (uint32_t)h->prm.seed;
@@ -2862,11 +2876,13 @@ int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, doubl
     return GPAT_OK;
 }
 
-int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, int64_t *judged,
-                           int64_t *nsplit, int64_t *nkilled) {
+int gpat_get_mover_learned(const gpat_handle_t *h, double *log_sum_wexpz, double *log_sum_w,
+                           int64_t *judged, int64_t *nsplit, int64_t *nkilled) {
     if (!h) return GPAT_ERR_ARG;
     const double s = fixed_to_double(h->learn_host[2], h->learn_host[3]);
+    const double sw = fixed_to_double(h->learn_host[4], h->learn_host[5]);
     if (log_sum_wexpz) *log_sum_wexpz = s > 0.0 ? h->learn.z_shift + std::log(s) : -INFINITY;
+    if (log_sum_w) *log_sum_w = sw > 0.0 ? std::log(sw) : -INFINITY;
     if (judged) *judged = (int64_t)h->learn_host[1];
     if (nsplit) *nsplit = h->learn_split;
     if (nkilled) *nkilled = h->learn_killed;

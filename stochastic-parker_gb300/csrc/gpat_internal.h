@@ -175,8 +175,11 @@ struct FeatureArgs {
     int nxg, nyg, nzg;
     float t_norm;
 };
+// Importance exp(z') with z' = log(exp(z) + exp(z_floor)): the floor (a
+// fraction of the weighted mean importance, -inf for none) bounds the
+// weights roulette can create.
 struct WSplitArgs {
-    double w_ref, z_ref, sqrt_ratio;
+    double w_ref, z_ref, z_floor, sqrt_ratio;
     int max_level;
     uint32_t key0, key1;
 };
@@ -190,7 +193,7 @@ struct FusedLearn {
     WSplitArgs s;
     int64_t cap;
     unsigned long long *count;   // particles including children (starts at the launch's total)
-    unsigned long long *zsum;    // {judged, sum of w exp(z - z_shift) as hi, lo}
+    unsigned long long *zsum;    // {judged, sum of w exp(z - z_shift) as hi, lo, sum of w as hi, lo}
     double z_shift;
 };
 // Per-minibatch activations ([64][b] except h0: [b][8]) and output deltas.

@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(128) score_kernel(const __nv_bfloat16 *w16, co
     atomicMax(zmax_key, b >= 0 ? b : b ^ 0x7FFFFFFF);
 }
 
-// Exact sums over live particles of z + 64 and of w exp(z - zmax).
+// Exact sums over live particles of z + 64, of w exp(z - zmax) and of w.
 __global__ void score_sum_kernel(const DevParticles P, int64_t n, const float *z,
                                  const int *zmax_key, unsigned long long *out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -387,6 +387,7 @@ __global__ void score_sum_kernel(const DevParticles P, int64_t n, const float *z
     atomicAdd(&out[0], 1ull);
     atomic_add_fixed(&out[1], &out[2], (double)z[i] + 64.0);
     atomic_add_fixed(&out[3], &out[4], P.weight[i] * exp((double)z[i] - (double)zmax));
+    atomic_add_fixed(&out[5], &out[6], P.weight[i]);
 }
 
 // Sum of weights and squared weights of live particles above a momentum.
@@ -499,7 +500,7 @@ cudaError_t launch_weighted_split(const __nv_bfloat16 *w16, const float *norm,
 cudaError_t launch_score(const __nv_bfloat16 *w16, const float *norm, const FeatureArgs &g,
                          int ndim, const DevParticles &P, int64_t n, float *z, int *zmax_key,
                          unsigned long long *out, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(out, 0, 5 * sizeof(unsigned long long), s);
+    cudaError_t e = cudaMemsetAsync(out, 0, 7 * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(zmax_key, 0x80, sizeof(int), s);   // most negative
     if (e != cudaSuccess || n <= 0) return e;
     const unsigned blocks = (unsigned)((n + 127) / 128);

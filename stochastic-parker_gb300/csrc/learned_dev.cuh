@@ -75,16 +75,25 @@ __device__ void particle_features(const FeatureArgs &g, const DevParticles &P, i
 }
 
 
-// The weight window around w_t = w_ref exp(-(z - z_ref)) for the particle of
-// this lane (live: in the box and to be judged), then the warp-aggregated
-// reservation of the children's slots.  All 32 lanes of the warp must call.
+// Floored log-importance log(exp(z) + exp(z_floor)) of a network output.
+__device__ __forceinline__ double floored_importance(double z, double z_floor) {
+    z = fmin(fmax(z, -60.0), 60.0);
+    if (!(z_floor > -1e300)) return z;
+    const double hi = fmax(z, z_floor), lo = fmin(z, z_floor);
+    return hi + log1p(exp(lo - hi));
+}
+
+// The weight window around w_t = w_ref exp(-(z' - z_ref)), z' the floored
+// log-importance, for the particle of this lane (live: in the box and to be
+// judged), then the warp-aggregated reservation of the children's slots.
+// All 32 lanes of the warp must call.
 __device__ __forceinline__ void window_split(const WSplitArgs &a, const DevParticles &P, int64_t i,
                                              bool live, float z, int64_t cap,
                                              unsigned long long *count, DevCounters *cnt) {
     int j = 0;
     double w = 0.0;
     if (live) {
-        const double wt = a.w_ref * exp(-((double)fminf(fmaxf(z, -60.0f), 60.0f) - a.z_ref));
+        const double wt = a.w_ref * exp(-(floored_importance((double)z, a.z_floor) - a.z_ref));
         w = P.weight[i];
         if (w > wt * a.sqrt_ratio) {
             const int split_times = P.split_times[i];

@@ -1100,32 +1100,44 @@ __device__ __forceinline__ void push_ft(const MoverArgs &a, State &s, const Fld 
     push_ft_tail<NDIM, I3 ? 2 : NDIM>(a, s, dX, dY, dZ, dp_dt, dpp, dmu_dt, duu, sdt, r, d);
 }
 
+// After the reference's one-period wrap: a push longer than a period (a
+// drift at dt_min where kappa's gradient is steep) leaves the particle
+// outside even so, where the reference would index outside its arrays.
+// Whole periods more bring it back; inside the box this is the identity, so
+// every case the reference defines is unchanged.
+__device__ __forceinline__ double wrap_rest(double x, double lo, double hi) {
+    const double per = hi - lo;
+    if (x < lo) x += per * ceil((lo - x) / per);
+    else if (x > hi) x -= per * ceil((x - hi) / per);
+    return x;
+}
+
 template <int NDIM>
 __device__ __forceinline__ void boundary(const MoverArgs &a, State &s, double xlo, double xhi,
                                          double ylo, double yhi, double zlo, double zhi, Acc &acc) {
     if (s.x < xlo && s.flag == 1) {
         if (a.pbcx) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -1; }
-        else s.x = s.x - xlo + xhi;
+        else s.x = wrap_rest(s.x - xlo + xhi, xlo, xhi);
     } else if (s.x > xhi && s.flag == 1) {
         if (a.pbcx) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -2; }
-        else s.x = s.x - xhi + xlo;
+        else s.x = wrap_rest(s.x - xhi + xlo, xlo, xhi);
     }
     if (NDIM > 1) {
         if (s.y < ylo && s.flag == 1) {
             if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -3; }
-            else s.y = s.y - ylo + yhi;
+            else s.y = wrap_rest(s.y - ylo + yhi, ylo, yhi);
         } else if (s.y > yhi && s.flag == 1) {
             if (a.pbcy) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -4; }
-            else s.y = s.y - yhi + ylo;
+            else s.y = wrap_rest(s.y - yhi + ylo, ylo, yhi);
         }
     }
     if (NDIM == 3 || a.include_3rd) {   // z too for include_3rd_dim runs (:2084)
         if (s.z < zlo && s.flag == 1) {
             if (a.pbcz) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -5; }
-            else s.z = s.z - zlo + zhi;
+            else s.z = wrap_rest(s.z - zlo + zhi, zlo, zhi);
         } else if (s.z > zhi && s.flag == 1) {
             if (a.pbcz) { acc_add(acc.leak_h, acc.leak_l, s.w); s.flag = -6; }
-            else s.z = s.z - zhi + zlo;
+            else s.z = wrap_rest(s.z - zhi + zlo, zlo, zhi);
         }
     }
 }

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(128, NDIM == 2 ? GPAT_MIXED_MINB_2D : GPAT_MIX
         const double e = fmin(fmax((double)z - L.z_shift, -60.0), 60.0);
         atomicAdd(&L.zsum[0], 1ull);
         atomic_add_fixed(&L.zsum[1], &L.zsum[2], P.weight[i] * exp(e));
+        atomic_add_fixed(&L.zsum[3], &L.zsum[4], P.weight[i]);
     }
     window_split(L.s, P, i, fin, z, L.cap, L.count, a.cnt);
 }

@@ -107,7 +107,7 @@ MLP_PARAMS = 8961
 
 class BatchTuning(C.Structure):
     _fields_ = [("minb", i32), ("grab", i32), ("pushes_per_s", d), ("chunk_pushes", i32),
-                ("reserved", i32)]
+                ("reserved", i32), ("default_pushes_per_s", d)]
 
 
 # name -> (restype, argtypes); every symbol include/gpat_engine.h declares.
@@ -151,8 +151,8 @@ SIGNATURES = {
     "gpat_mlp_record": (C.c_int, [Mlp, Handle, d, P(i64)]),
     "gpat_mlp_label": (C.c_int, [Mlp, Handle, d, P(i64), P(i64)]),
     "gpat_mlp_train": (C.c_int, [Mlp, C.c_int, i64, d, d, u64, P(d)]),
-    "gpat_mlp_score": (C.c_int, [Mlp, Handle, d, P(d), P(d)]),
-    "gpat_weighted_split": (C.c_int, [Handle, Mlp, d, d, d, d, C.c_int, P(i64), P(i64)]),
+    "gpat_mlp_score": (C.c_int, [Mlp, Handle, d, P(d), P(d), P(d)]),
+    "gpat_weighted_split": (C.c_int, [Handle, Mlp, d, d, d, d, d, C.c_int, P(i64), P(i64)]),
     "gpat_tail_weights": (C.c_int, [Handle, d, P(i64), P(d), P(d)]),
     "gpat_set_fluctuations": (C.c_int, [Handle, C.c_int, P(C.c_float), P(C.c_float),
                                         P(C.c_float), P(C.c_float)]),
@@ -174,8 +174,8 @@ SIGNATURES = {
     "gpat_particle_mover": (C.c_int, [Handle, C.c_int, C.c_int, d, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
     "gpat_split_particle": (C.c_int, [Handle, d, d, C.c_int]),
-    "gpat_set_mover_learned": (C.c_int, [Handle, C.c_void_p, d, d, d, d, C.c_int]),
-    "gpat_get_mover_learned": (C.c_int, [Handle, C.POINTER(d), C.POINTER(C.c_int64),
+    "gpat_set_mover_learned": (C.c_int, [Handle, C.c_void_p, d, d, d, d, d, C.c_int]),
+    "gpat_get_mover_learned": (C.c_int, [Handle, C.POINTER(d), C.POINTER(d), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gpat_set_mover_tiles": (C.c_int, [Handle] + [C.c_int] * 8),
     "gpat_get_mover_tiles": (C.c_int, [Handle, C.POINTER(C.c_int)]),

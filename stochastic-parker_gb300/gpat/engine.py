@@ -12,6 +12,7 @@ implementation.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -607,7 +608,7 @@ class Batch:
             self.b, self._frames(mhd_tframe), int(nlgc), kperp_kpara, nsteps_interval,
             num_fine_steps, C.byref(t)))
         out = dict(minb=t.minb, grab=t.grab, pushes_per_s=t.pushes_per_s,
-                   chunk_pushes=t.chunk_pushes)
+                   chunk_pushes=t.chunk_pushes, default_pushes_per_s=t.default_pushes_per_s)
         if cache:
             table = _read_cache(cache)
             table[key] = out
@@ -629,7 +630,7 @@ class Batch:
                     chunk_pushes=t.chunk_pushes)
 
     def set_tuning(self, minb, grab, chunk_pushes=0):
-        t = _abi.BatchTuning(minb, grab, 0.0, chunk_pushes, 0)
+        t = _abi.BatchTuning(minb, grab, 0.0, chunk_pushes, 0, 0.0)
         self._check(self.lib.gpat_batch_set_tuning(self.b, C.byref(t)))
 
     def stats(self) -> dict:
@@ -716,10 +717,11 @@ class Mlp:
         return loss.value
 
     def score(self, eng, t_norm):
-        """(mean z, log sum w exp(z)) over the run's live particles."""
-        z, lse = C.c_double(), C.c_double()
-        self._check(self.lib.gpat_mlp_score(self.m, eng.h, t_norm, C.byref(z), C.byref(lse)))
-        return z.value, lse.value
+        """(mean z, log sum w exp(z), log sum w) over the run's live particles."""
+        z, lse, lsw = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.gpat_mlp_score(self.m, eng.h, t_norm, C.byref(z), C.byref(lse),
+                                            C.byref(lsw)))
+        return z.value, lse.value, lsw.value
 
     def close(self):
         if self.m:
@@ -727,28 +729,74 @@ class Mlp:
             self.m = _abi.Mlp()
 
 
-def weighted_split(eng, mlp: Mlp, t_norm, w_ref, z_ref, window_ratio=4.0, max_level=4):
+def window_params(log_sum_wexpz, log_sum_w, target, defensive=0.1):
+    """(z_ref, z_floor) that aim weighted splitting at `target` particles with
+    defensive importance exp(z) + defensive * (weighted mean of exp(z)):
+    no roulette survivor then weighs more than about
+    (1 + defensive) / defensive * sum(w) / target.  defensive = 0 gives the
+    bare importance exp(z) (z_floor = -inf)."""
+    if defensive <= 0.0:
+        return log_sum_wexpz - math.log(target), -math.inf
+    z_floor = math.log(defensive) + log_sum_wexpz - log_sum_w
+    return log_sum_wexpz + math.log1p(defensive) - math.log(target), z_floor
+
+
+class FusedWindow:
+    """z_ref and z_floor for learned splitting inside the mover
+    (set_mover_learned), interval after interval.  The mover judges the
+    particles that finish an interval with sums taken in the interval
+    before (the judged particles' sums are only complete at its end), and
+    the network's outputs drift as time advances and particles move: the
+    log-sum of w exp(z) is therefore carried one interval ahead by its last
+    change (at most `max_step` in magnitude), which keeps the population
+    near `target`.  Usage: start() with Mlp.score's sums before the first
+    interval, params() before each mover call, update() with
+    mover_learned_stats after it."""
+
+    def __init__(self, target, defensive=0.1, max_step=2.0):
+        self.target, self.defensive, self.max_step = target, defensive, max_step
+        self.lse = self.lsw = self.prev = None
+
+    def start(self, log_sum_wexpz, log_sum_w):
+        self.lse, self.lsw, self.prev = log_sum_wexpz, log_sum_w, None
+
+    def update(self, stats: dict):
+        if stats["judged"] > 0 and math.isfinite(stats["log_sum_wexpz"]):
+            self.prev = self.lse
+            self.lse, self.lsw = stats["log_sum_wexpz"], stats["log_sum_w"]
+
+    def params(self):
+        lse = self.lse
+        if self.prev is not None:
+            lse += max(-self.max_step, min(self.max_step, self.lse - self.prev))
+        return window_params(lse, self.lsw, self.target, self.defensive)
+
+
+def weighted_split(eng, mlp: Mlp, t_norm, w_ref, z_ref, window_ratio=4.0, max_level=4,
+                   z_floor=-math.inf):
     """gpat_weighted_split; returns (children created, particles killed)."""
     ns, nk = C.c_int64(), C.c_int64()
-    eng._check(eng.lib.gpat_weighted_split(eng.h, mlp.m, t_norm, w_ref, z_ref, window_ratio,
-                                           max_level, C.byref(ns), C.byref(nk)))
+    eng._check(eng.lib.gpat_weighted_split(eng.h, mlp.m, t_norm, w_ref, z_ref, z_floor,
+                                           window_ratio, max_level, C.byref(ns), C.byref(nk)))
     return ns.value, nk.value
 
 
 def set_mover_learned(eng, mlp, t_norm=0.0, w_ref=1.0, z_ref=0.0, window_ratio=4.0,
-                      max_level=3):
+                      max_level=3, z_floor=-math.inf):
     """gpat_set_mover_learned: learned splitting of particles as they finish
     an interval, inside the mover launch; mlp = None turns it off."""
     eng._check(eng.lib.gpat_set_mover_learned(eng.h, mlp.m if mlp is not None else None, t_norm,
-                                              w_ref, z_ref, window_ratio, max_level))
+                                              w_ref, z_ref, z_floor, window_ratio, max_level))
 
 
 def mover_learned_stats(eng) -> dict:
     """gpat_get_mover_learned after a mover call."""
-    lse, j, ns, nk = C.c_double(), C.c_int64(), C.c_int64(), C.c_int64()
-    eng._check(eng.lib.gpat_get_mover_learned(eng.h, C.byref(lse), C.byref(j), C.byref(ns),
-                                              C.byref(nk)))
-    return dict(log_sum_wexpz=lse.value, judged=j.value, nsplit=ns.value, nkilled=nk.value)
+    lse, lsw = C.c_double(), C.c_double()
+    j, ns, nk = C.c_int64(), C.c_int64(), C.c_int64()
+    eng._check(eng.lib.gpat_get_mover_learned(eng.h, C.byref(lse), C.byref(lsw), C.byref(j),
+                                              C.byref(ns), C.byref(nk)))
+    return dict(log_sum_wexpz=lse.value, log_sum_w=lsw.value, judged=j.value, nsplit=ns.value,
+                nkilled=nk.value)
 
 
 def _read_cache(path) -> dict:

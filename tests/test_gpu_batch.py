@@ -83,6 +83,9 @@ def test_batch_autotune_leaves_runs_unchanged():
     best = batch.autotune(mhd_tframe=1)
     assert best["minb"] in (5, 6, 8) and best["grab"] in (1, 4) and best["pushes_per_s"] > 0
     assert best["chunk_pushes"] in (64, 128, 256)
+    # the untuned launch (6 blocks per SM, single grabs, the runs' chunk of
+    # 64) is one of the candidates: timed, and never faster than the choice
+    assert 0 < best["default_pushes_per_s"] <= best["pushes_per_s"]
     assert batch.tuning()["minb"] == best["minb"]
     # the chunk length moves the pause points: compare with the runs' own (64)
     batch.set_tuning(best["minb"], best["grab"], 0)

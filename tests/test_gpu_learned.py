@@ -1,7 +1,9 @@
 """Learned splitting: the network's GPU forward and gradient against the CPU
 oracle (oracle/mlp_oracle.py), training, and weighted splitting / roulette
 driven by the trained network on a 3D run (unbiased tail, more effective
-samples, unique lineage tags)."""
+samples, unique lineage tags, bounded weights: the importance is floored at
+a tenth of its weighted mean, so the total weight stays within Monte Carlo
+error of the injected weight)."""
 import math
 
 import numpy as np
@@ -9,7 +11,10 @@ import pytest
 
 import mlp_oracle as mo
 from gpat import configs
-from gpat.engine import Mlp, tail_weights, weighted_split
+from gpat.engine import Mlp, tail_weights, weighted_split, window_params
+
+# defensive fraction of the weighted mean importance added to every particle's
+DEFENSIVE = 0.1
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +63,22 @@ def test_training_learns_a_rule():
     m.close()
 
 
+def check_total_weight(eng, nptl, target):
+    """The live particles' total weight is the injected nptl within Monte
+    Carlo error, and no weight exceeds the floor's bound.  A roulette survivor
+    weighs at most (1 + a) / a * W / target (a = DEFENSIVE, W the total
+    weight at the judgement), 5.5 here; every roulette adds at most
+    w * 5.5 to the variance of the total, so after 8 judgements of at most
+    40000 particles of weight <= 1 its standard deviation is below
+    sqrt(8 * 20000 * 5.5) ~ 940, 4.7 % of nptl: 15 % is over 3 sigma."""
+    c, wsum, _ = tail_weights(eng, 0.0)
+    bound = (1.0 + DEFENSIVE) / DEFENSIVE * nptl / target
+    assert abs(wsum - nptl) < 0.15 * nptl, (wsum, nptl)
+    ps = eng.get_particles()
+    live = ps["count_flag"] == 1
+    assert ps["weight"][live].max() < 2.0 * bound, (ps["weight"][live].max(), bound)
+
+
 def test_learned_splitting_3d_unbiased_and_more_samples():
     n_grid, nptl, nint = 32, 20000, 8
     w = configs.turbulence_3d(scale=nptl / 1e8, n=n_grid, nframes=nint)
@@ -69,9 +90,10 @@ def test_learned_splitting_3d_unbiased_and_more_samples():
         for k in range(nint):
             if learned is not None:
                 # importance-weighted population of about `target` particles
-                _, lse = learned.score(eng, k / nint)
-                weighted_split(eng, learned, k / nint, 1.0, lse - math.log(target),
-                               window_ratio=4.0, max_level=3)
+                _, lse, lsw = learned.score(eng, k / nint)
+                z_ref, z_floor = window_params(lse, lsw, target, DEFENSIVE)
+                weighted_split(eng, learned, k / nint, 1.0, z_ref, window_ratio=4.0, max_level=3,
+                               z_floor=z_floor)
             if recorder is not None:
                 recorder.record(eng, k / nint)
             eng.particle_mover(mhd_tframe=k + 1)
@@ -99,6 +121,7 @@ def test_learned_splitting_3d_unbiased_and_more_samples():
     key = (ps["tag_injected"].astype(np.int64) << 32) | (ps["tag_splitted"].astype(np.int64) &
                                                          0xFFFFFFFF)
     assert len(np.unique(key)) == len(key)
+    check_total_weight(eng_l, nptl, 2 * nptl)
     for e in (plain, eng_l):
         e.close()
     net.close()
@@ -110,7 +133,7 @@ def test_learned_splitting_fused_in_the_mover():
     agrees with a plain run within Monte Carlo error, every finished particle
     is judged, the tail gets more effective samples per push, and lineage
     tags stay unique."""
-    from gpat.engine import mover_learned_stats, set_mover_learned
+    from gpat.engine import FusedWindow, mover_learned_stats, set_mover_learned
     n_grid, nptl, nint = 32, 20000, 8
     w = configs.turbulence_3d(scale=nptl / 1e8, n=n_grid, nframes=nint)
     net = Mlp(seed=9, record_capacity=nptl * nint)
@@ -128,10 +151,12 @@ def test_learned_splitting_fused_in_the_mover():
     target = 2 * nptl
     eng = configs.build_engine(w, nptl_max=nptl * 40)
     configs.inject(eng, w)
-    _, lse = net.score(eng, 0.0)
+    win = FusedWindow(target, DEFENSIVE)
+    win.start(*net.score(eng, 0.0)[1:])
     pushes = 0
     for k in range(nint):
-        set_mover_learned(eng, net, (k + 1) / nint, 1.0, lse - math.log(target), 4.0, 3)
+        z_ref, z_floor = win.params()
+        set_mover_learned(eng, net, (k + 1) / nint, 1.0, z_ref, 4.0, 3, z_floor=z_floor)
         n_before = eng.nptl_current
         eng.particle_mover(mhd_tframe=k + 1)
         pushes += eng.counters().last_mover_steps
@@ -139,8 +164,10 @@ def test_learned_splitting_fused_in_the_mover():
         # a periodic box: every particle finishes the interval and is judged once
         assert st["judged"] == n_before, (st, n_before)
         assert eng.nptl_current == n_before + st["nsplit"] - st["nkilled"]
-        lse = st["log_sum_wexpz"]
+        win.update(st)
     set_mover_learned(eng, None)
+    # the lagged, extrapolated normalisation keeps the population near target
+    assert 0.7 * target < eng.nptl_current < 1.3 * target, eng.nptl_current
     c0, w0, w20 = tail_weights(plain, pthr)
     c1, w1, w21 = tail_weights(eng, pthr)
     assert abs(w1 - w0) < 4.0 * math.sqrt(w20 + w21), (w0, w1, w20, w21)
@@ -150,9 +177,7 @@ def test_learned_splitting_fused_in_the_mover():
     key = (ps["tag_injected"].astype(np.int64) << 32) | (ps["tag_splitted"].astype(np.int64) &
                                                          0xFFFFFFFF)
     assert len(np.unique(key)) == len(key)
-    # the total weight is kept in expectation only: roulette survivors carry
-    # w_t >> w, so the sum fluctuates widely; a sanity range
-    assert 0.3 * nptl < ps["weight"].sum() < 3.0 * nptl
+    check_total_weight(eng, nptl, target)
     for e in (plain, eng):
         e.close()
     net.close()

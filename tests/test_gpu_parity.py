@@ -329,3 +329,38 @@ def test_status_and_errors():
     with pytest.raises(GPATCapacityError):
         eng.inject_particles_at_x(params["nptl_max"] + 5, 0.5, 1e-6, 1, 1.0, 1)
     assert eng.counters().nptl_current == params["nptl_max"]
+
+
+def test_pushes_longer_than_a_period_match_oracle():
+    """kappa 1000 at a fixed dt of dt_out / 20 on the unit periodic box: most
+    pushes land more than one period away, and the one-period wrap of
+    particle_boundary_condition is followed by whole periods more (where the
+    reference would index outside its arrays).  The FP64 mover matches the
+    oracle bit for bit; the split-precision mover keeps every particle in
+    the box too."""
+    n = 32
+    cfg = make_mhd_config(n, n, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.02)
+    kw = dict(ndim=2, p0=0.1, pmin=0.1, pmax=100.0, kpara0=1000.0, kret=0.1, dt_min_rel=0.05,
+              dt_max_rel=0.05, pbcx=0, pbcy=0, momentum_dependency=0, nptl_max=2000, seed=3)
+    frame = fields.planar_shock_2d(n, n, 0.0, 1.0, 0.0, 1.0, u1=1.0, r=3.0, w=0.05)
+    box = (0.0, 0.0, 0.0, 1.0, 1.0, 1.0)
+
+    def inject(e):
+        e.inject_particles_spatial_uniform(1000, 1e-3, 1, 1.0, 1, box)
+
+    eng, gpu, ref, cnt, _ = run_pair(kw, cfg, frame, [0.0, 0.02, 0.04], inject, intervals=2)
+    assert_same_set(gpu, ref)
+    assert len(gpu) == 1000 and (gpu["count_flag"] == 1).all()
+    eng.close()
+    mixed = Engine(make_params(**dict(kw, precision=1)), cfg, 0)
+    mixed.set_tstamps([0.0, 0.02, 0.04])
+    mixed.set_fields(frame, 0)
+    mixed.calc_fields_gradients(0)
+    inject(mixed)
+    for k in range(2):
+        mixed.particle_mover(nsteps_interval=10, mhd_tframe=k + 1)
+    ps = mixed.get_particles()
+    assert len(ps) == 1000 and (ps["count_flag"] == 1).all()
+    assert 0.0 <= ps["x"].min() and ps["x"].max() <= 1.0
+    assert 0.0 <= ps["y"].min() and ps["y"].max() <= 1.0
+    mixed.close()

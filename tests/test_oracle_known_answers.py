@@ -248,3 +248,37 @@ def test_histogram_bins_and_strict_lower_edge():
     # 775-780 writes out of bounds there); it is dropped here.
     assert list(c) == [1, 1, 1, 1]
     assert list(f) == [0.5, 0.25, 1.0, 1.0]
+
+
+def _long_push_case():
+    """kappa 1000 at a fixed dt of dt_out / 20 on the unit periodic box:
+    the diffusion steps are about 1.4 box lengths (rms per axis), so most
+    pushes land more than one period away."""
+    n = 32
+    cfg = make_mhd_config(n, n, 1, 0.0, 1.0, 0.0, 1.0, dt_out=0.02)
+    prm = make_params(ndim=2, p0=0.1, pmin=0.1, pmax=100.0, kpara0=1000.0, kret=0.1,
+                      dt_min_rel=0.05, dt_max_rel=0.05, pbcx=0, pbcy=0, momentum_dependency=0,
+                      nptl_max=2000, seed=3)
+    frame = fields.planar_shock_2d(n, n, 0.0, 1.0, 0.0, 1.0, u1=1.0, r=3.0, w=0.05)
+    return prm, cfg, frame
+
+
+def test_pushes_longer_than_a_period_stay_in_the_box():
+    """particle_boundary_condition wraps by one period; a longer push then
+    leaves the particle outside, where the reference indexes outside its
+    arrays.  The oracle (and the engine) wrap by whole periods more: every
+    particle stays in the periodic box with its flag, and each moved its 20
+    pushes (one interval at dt = dt_out / 20)."""
+    prm, cfg, frame = _long_push_case()
+    oprm = oracle.params_from(prm)
+    parts = oracle.Particles(2000)
+    cnt = oracle.OrcCounters()
+    oracle.inject_spatial_uniform(oprm, parts, 1000, 1e-3, 1, 1.0, 0.0, 0.0,
+                                  (0.0, 0.0, 0.0, 1.0, 1.0, 1.0), cnt)
+    oracle.mover(oprm, oracle.config_from(cfg), oracle.full_fields(frame, 2, cfg), parts, 0.0,
+                 0.02, counters=cnt)
+    v = parts.view()
+    assert parts.n == 1000 and (v["count_flag"] == 1).all()
+    assert v["x"].min() >= 0.0 and v["x"].max() <= 1.0
+    assert v["y"].min() >= 0.0 and v["y"].max() <= 1.0
+    assert 20 * 1000 <= cnt.steps <= 21 * 1000
