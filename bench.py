@@ -254,46 +254,56 @@ def measured_peaks() -> dict:
 NCU_MOVER = {
     ("global", 2): {"dram_bytes_per_push": 0.934, "l1tex_pct": 94.2,
                     "profile": "profiles/mover_mixed_turbulent_shock_2d.md"},
-    ("global", 3): {"dram_bytes_per_push": 6.7, "l1tex_pct": 79.4,
+    ("global", 3): {"dram_bytes_per_push": 6.7, "l1tex_pct": 91.7,
                     "profile": "profiles/mover_mixed_turbulence_3d.md"},
 }
-# Bytes one SM's L1TEX/shared-memory data path returns per clock.
-L1_BYTES_PER_CLK_SM = 128
-# Field bytes the movers read through L1 per push: the global-gather kernel
-# loads whole 32-byte halves of the 64-byte (2D) or 96-byte (3D) records of
-# every corner; the tile kernel reads 16-byte chunks from shared memory
-# (3D: 5 chunks and one 4-byte value per corner).
-L1_GATHER_BYTES_PER_PUSH = {("global", 2): 4 * 64, ("global", 3): 8 * 96,
-                            ("tile", 2): 4 * 64, ("tile", 3): 8 * (5 * 16 + 4)}
+# The L1TEX data path per push and per clock.  Global-gather movers: the
+# 32-byte loads of scattered records cost one data-pipe wavefront per
+# 32-byte sector (3D capture: 1.51e9 wavefronts for 1.53e9 sectors; the pipe
+# at 88 % of its wavefronts), one wavefront per clock per SM, so the rate is
+# sectors: 7.3 per push in 2D (8 loads, neighbouring lanes share some), 24
+# in 3D (8 corners x 3 loads; 23.0 distinct sectors per 32-lane request).
+# Brick movers read 16-byte chunks from shared memory, up to 128 bytes per
+# wavefront (nominal; bank conflicts cost more).
+L1_MODEL = {("global", 2): {"bytes_per_push": 7.3 * 32, "bytes_per_clk_sm": 32},
+            ("global", 3): {"bytes_per_push": 24 * 32, "bytes_per_clk_sm": 32},
+            ("tile", 2): {"bytes_per_push": 4 * 64, "bytes_per_clk_sm": 128},
+            ("tile", 3): {"bytes_per_push": 8 * (5 * 16 + 4), "bytes_per_clk_sm": 128}}
 
 
 def roofline_of(kind, ndim, avg_ms, avg_steps, avg_n, sm_count, sm_mhz, peaks) -> dict:
     """Roofline of one mover launch: the L1TEX data path is the bound (ncu),
     HBM is reported beside it on the algorithmic bytes."""
     secs = avg_ms / 1e3
-    l1_bytes = avg_steps * L1_GATHER_BYTES_PER_PUSH[(kind, ndim)]
-    l1_peak = sm_count * L1_BYTES_PER_CLK_SM * (sm_mhz or 2070.0) * 1e6 / 1e9
+    m = L1_MODEL[(kind, ndim)]
+    l1_bytes = avg_steps * m["bytes_per_push"]
+    l1_peak = sm_count * m["bytes_per_clk_sm"] * (sm_mhz or 2070.0) * 1e6 / 1e9
     alg = avg_steps * GATHER_BYTES_PER_STEP[ndim] + avg_n * STATE_BYTES_PER_PARTICLE
     ncu = NCU_MOVER.get((kind, ndim), {})
     dram = ncu.get("dram_bytes_per_push")
+    if m["bytes_per_clk_sm"] == 32:
+        peak_source = (f"L1TEX data pipe: one 32-byte sector per clock per SM for scattered "
+                       f"32-byte loads (ncu: wavefronts = sectors) x {sm_count} SMs x median "
+                       f"sampled SM clock {sm_mhz} MHz")
+    else:
+        peak_source = (f"nominal shared-memory rate: 128 B/clk per SM x {sm_count} SMs x "
+                       f"median sampled SM clock {sm_mhz} MHz")
     return {"bound": "l1", "achieved": l1_bytes / secs / 1e9, "peak": l1_peak, "unit": "GB/s",
-            "frac": l1_bytes / secs / 1e9 / l1_peak,
-            "peak_source": f"nominal: {L1_BYTES_PER_CLK_SM} B/clk per SM x {sm_count} SMs x "
-                           f"median sampled SM clock {sm_mhz} MHz (no measured L1 figure)",
+            "frac": l1_bytes / secs / 1e9 / l1_peak, "peak_source": peak_source,
             "traffic": dram * avg_steps if dram is not None else None,
             "traffic_source": ncu.get("profile"),
             "ncu_l1tex_throughput_pct": ncu.get("l1tex_pct"),
-            "l1_bytes_per_push": L1_GATHER_BYTES_PER_PUSH[(kind, ndim)],
+            "l1_bytes_per_push": m["bytes_per_push"],
             "kernel_ms_per_launch": avg_ms, "steps_per_launch": avg_steps,
             "kernel_steps_per_s": avg_steps / secs,
             "hbm": {"achieved": alg / secs / 1e9, "peak": peaks["hbm_gbs"],
                     "frac": alg / secs / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
                     "algorithmic_bytes_per_push": GATHER_BYTES_PER_STEP[ndim],
                     "state_bytes_per_particle": STATE_BYTES_PER_PARTICLE},
-            "note": "achieved = field bytes read through L1/shared memory per push x pushes / "
-                    "launch time; ncu_l1tex_throughput_pct is the unit's measured busy share "
-                    "(per-request work, not bytes, saturates it); hbm = algorithmic bytes "
-                    "(corners x stored field arrays x 4 B + FP64 state) over measured HBM"}
+            "note": "achieved = L1 sectors (32 B) the gathers move per push x pushes / launch "
+                    "time, against the data pipe's sector rate; ncu_l1tex_throughput_pct is the "
+                    "unit's measured busy share; hbm = algorithmic bytes (corners x stored field "
+                    "arrays x 4 B + FP64 state) over measured HBM"}
 
 
 # ---------------------------------------------------------------------------
@@ -713,15 +723,28 @@ def run_learned(args, world, rank, local):
     w = make_workload(args, 1, seed=3 + rank, nframes=max_intervals, scale=n_train / 1e8)
     p0 = w.params["p0"]
     pyield = 100.0 * p0
+
+    def fresh(n, seed, cap, precision=1):
+        """An engine holding n particles injected as the workload does
+        (log-uniform in [p0, 10 p0]: the injection draws up to the workload's
+        pmax) in an engine whose pmax is 1e4 p0, so split_particle's p <= pmax
+        rule does not stop the splitting of the tail."""
+        inj = configs.build_engine(w, device=local, nptl_max=n, seed=seed)
+        configs.inject(inj, w, nptl=n)
+        ps = inj.get_particles()
+        inj.close()
+        eng = configs.build_engine(w, device=local, nptl_max=cap, seed=seed,
+                                   precision=precision, pmax=1.0e4 * p0)
+        eng.put_particles(ps)
+        return eng
+
     if args.intervals > 0:
         nint, pilot = args.intervals, None
     else:
         # run length: the first interval count at which 0.1 % of a plain
         # run's particles are above 100 p0 (100 p0 is then a tail)
         n_pilot = max(20000, int(2e5 * args.scale))
-        eng = configs.build_engine(w, device=local, nptl_max=n_pilot, seed=50 + rank,
-                                   pmax=1.0e4 * p0)
-        configs.inject(eng, w, nptl=n_pilot)
+        eng = fresh(n_pilot, 50 + rank, n_pilot)
         nint, frac = max_intervals, 0.0
         for k in range(max_intervals):
             eng.particle_mover(mhd_tframe=k + 1)
@@ -737,9 +760,7 @@ def run_learned(args, world, rank, local):
     every = args.record_every if args.record_every > 0 else max(1, nint // 10)
 
     def arm(kind, n, seed, recorder=None, net=None, target=None, cap=None, precision=1):
-        eng = configs.build_engine(w, device=local, nptl_max=cap or 2 * n, seed=seed,
-                                   precision=precision, pmax=1.0e4 * p0)
-        configs.inject(eng, w, nptl=n)
+        eng = fresh(n, seed, cap or 2 * n, precision)
         pushes, capped, judged = 0, False, 0
         win = FusedWindow(target, DEFENSIVE) if kind == "learned" else None
         torch.cuda.synchronize()
