@@ -698,22 +698,27 @@ def run_learned(args, world, rank, local):
     workload's field and transport, f(p) up to 1e4 p0).  A plain run of
     n_train trajectories over the whole run length generates the training
     records (every record_every intervals) and labels them by whether the
-    trajectory ends above p_label; the network is trained on the GPU.  Then,
-    on fresh particles, four arms run the same intervals:
-      plain      split-precision, no splitting (4x the particles);
-      fixed      split-precision with split_particle's fixed thresholds;
-      learned    split-precision with the network applied inside the mover
-                 as particles finish each interval (weight window 4, the
-                 particle cap of 4e8, importance exp(z) floored at DEFENSIVE
-                 times its weighted mean so roulette weights stay bounded);
-      fp64       the FP64 mover with fixed-threshold splitting: the judge.
-    Each reports the weighted count above 100 p0 and its effective samples
-    (sum w)^2 / sum w^2 per second."""
+    trajectory ends above p_label (the 99.9th percentile of its final
+    momenta, or 100 p0 if lower); the network is trained on the GPU.  Then,
+    on fresh particles, five arms run the same intervals:
+      plain        split-precision, no splitting (2x the particles);
+      fixed        split-precision with split_particle's fixed thresholds;
+      learned      split-precision with the network applied inside the mover
+                   as particles finish each interval (weight window 4, the
+                   particle cap of 4e8, importance exp(z) floored at
+                   DEFENSIVE times its weighted mean);
+      fp64         the FP64 mover, no splitting: the independent judge;
+      fp64_learned the FP64 mover with the same network applied by the
+                   separate split kernel after each interval: the FP64 judge
+                   with samples in the tail.
+    Each reports, above 100 p0 and above p_label, the weighted fraction, its
+    Monte Carlo error and the effective samples (sum w)^2 / sum w^2 per
+    second."""
     import numpy as np
     import torch
     from gpat import configs
     from gpat.engine import (FusedWindow, GPATCapacityError, Mlp, mover_learned_stats,
-                             set_mover_learned, tail_weights)
+                             set_mover_learned, tail_weights, weighted_split, window_params)
 
     torch.cuda.set_device(local)
     n_train = max(1000, int(args.train_trajectories * args.scale))
@@ -761,7 +766,7 @@ def run_learned(args, world, rank, local):
 
     def arm(kind, n, seed, recorder=None, net=None, target=None, cap=None, precision=1):
         eng = fresh(n, seed, cap or 2 * n, precision)
-        pushes, capped, judged = 0, False, 0
+        pushes, capped, judged, pop = 0, False, 0, []
         win = FusedWindow(target, DEFENSIVE) if kind == "learned" else None
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -779,21 +784,26 @@ def run_learned(args, world, rank, local):
                 st = mover_learned_stats(eng)
                 judged += st["judged"]
                 win.update(st)
-            if kind in ("fixed", "fp64") and not capped:
+            if kind == "fp64_learned":
+                _, lse, lsw = net.score(eng, (k + 1) / nint)
+                z_ref, z_floor = window_params(lse, lsw, target, DEFENSIVE)
+                weighted_split(eng, net, (k + 1) / nint, 1.0, z_ref, 4.0, 3, z_floor=z_floor)
+            if kind == "fixed" and not capped:
                 try:
                     eng.split_particle(fixed_ratio, fixed_pmin, 10)
                 except GPATCapacityError:
                     capped = True
+            pop.append(eng.nptl_current)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         if kind == "learned":
             set_mover_learned(eng, None)
-        return eng, pushes, secs, capped
+        return eng, pushes, secs, capped, pop
 
     # 1. plain run generating the training records; labels from its final momenta
     net = Mlp(device=local, seed=7 + rank,
               record_capacity=n_train * ((nint + every - 1) // every))
-    eng, train_pushes, train_s, _ = arm("plain", n_train, 100 + rank, recorder=net)
+    eng, train_pushes, train_s, _, _ = arm("plain", n_train, 100 + rank, recorder=net)
     print(f"learned_3d: training run {n_train} trajectories, {train_pushes} pushes in "
           f"{train_s:.1f} s", file=sys.stderr, flush=True)
     p_end = eng.get_particles()["p"]
@@ -807,6 +817,9 @@ def run_learned(args, world, rank, local):
     torch.cuda.synchronize()
     fit_s = time.perf_counter() - t0
 
+    print(f"learned_3d: labels {npos} positive of {nrec} records at p > {p_label / p0:.1f} p0, "
+          f"fit {fit_s:.1f} s", file=sys.stderr, flush=True)
+
     # 2. the arms on fresh particles (another injection seed)
     out = {}
     clocks = ClockSampler(local)
@@ -814,28 +827,36 @@ def run_learned(args, world, rank, local):
     for kind, n, kw in (("plain", 2 * n_cmp, {}),
                         ("fixed", n_cmp, dict(cap=4 * n_cmp)),
                         ("learned", n_cmp, dict(net=net, target=2 * n_cmp, cap=int(4e8))),
-                        ("fp64", n_fp64, dict(cap=4 * n_fp64, precision=0))):
-        e, pushes, secs, capped = arm(kind, n, 200 + rank, **kw)
-        c, ws, w2 = tail_weights(e, pyield)
+                        ("fp64", n_fp64, dict(precision=0)),
+                        ("fp64_learned", n_fp64, dict(net=net, target=2 * n_fp64,
+                                                      cap=16 * n_fp64, precision=0))):
+        e, pushes, secs, capped, pop = arm(kind, n, 200 + rank, **kw)
+        d = {"particles": n, "pushes": pushes, "seconds": secs,
+             "particle_steps_per_s": pushes / secs, "capped": capped,
+             "final_particles": e.nptl_current,
+             "population_min_max": [min(pop), max(pop)],
+             "max_split_level": int(e.get_particles()["split_times"].max())}
         _, wall, _ = tail_weights(e, 0.0)
-        ess = ws * ws / w2 if w2 > 0 else 0.0
-        out[kind] = {"particles": n, "pushes": pushes, "seconds": secs,
-                     "particle_steps_per_s": pushes / secs, "capped": capped,
-                     "tail_particles": c, "tail_fraction": ws / n,
-                     "tail_fraction_sigma": math.sqrt(w2) / n, "ess": ess,
-                     "ess_per_s": ess / secs, "final_particles": e.nptl_current,
-                     "total_weight_over_injected": wall / n}
-        print(f"learned_3d: {kind} " + json.dumps(out[kind]), file=sys.stderr, flush=True)
+        d["total_weight_over_injected"] = wall / n
+        for name, thr in (("above_100p0", pyield), ("above_p_label", p_label)):
+            c, ws, w2 = tail_weights(e, thr)
+            ess = ws * ws / w2 if w2 > 0 else 0.0
+            d[name] = {"particles": c, "fraction": ws / n, "sigma": math.sqrt(w2) / n,
+                       "ess": ess, "ess_per_s": ess / secs}
+        out[kind] = d
+        print(f"learned_3d: {kind} " + json.dumps(d), file=sys.stderr, flush=True)
         e.close()
     clk = clocks.stop()
     net.close()
-    judge = out["fp64"]
-    for kind in ("plain", "fixed", "learned"):
-        d = out[kind]
-        if judge["tail_fraction"] > 0:
-            d["tail_err_vs_fp64"] = d["tail_fraction"] / judge["tail_fraction"] - 1.0
-            d["tail_err_sigma"] = math.hypot(d["tail_fraction_sigma"],
-                                             judge["tail_fraction_sigma"]) / judge["tail_fraction"]
+    for name in ("above_100p0", "above_p_label"):
+        for judge in ("fp64", "fp64_learned"):
+            j = out[judge][name]
+            for kind in ("plain", "fixed", "learned", "fp64_learned"):
+                if kind == judge or j["fraction"] <= 0:
+                    continue
+                d = out[kind][name]
+                d[f"err_vs_{judge}"] = d["fraction"] / j["fraction"] - 1.0
+                d[f"err_sigma_vs_{judge}"] = math.hypot(d["sigma"], j["sigma"]) / j["fraction"]
     if rank != 0:
         return
     learned = out["learned"]
@@ -865,12 +886,16 @@ def run_learned(args, world, rank, local):
                              "record_every_intervals": every, "plain_run_seconds": train_s,
                              "fit_seconds": fit_s, "final_loss": loss, "epochs": 3},
                 "fixed_threshold": {"split_ratio": fixed_ratio, "pmin_split": fixed_pmin},
-                "judge": "FP64 mover with fixed-threshold splitting",
+                "judges": {"fp64": "FP64 mover, no splitting (independent of the method)",
+                           "fp64_learned": "FP64 mover with the network applied by the "
+                                           "separate split kernel (tail samples)"},
                 "arms": out,
-                "ess_per_s_learned_over_fixed":
-                    learned["ess_per_s"] / max(out["fixed"]["ess_per_s"], 1e-30),
-                "ess_per_s_learned_over_plain":
-                    learned["ess_per_s"] / max(out["plain"]["ess_per_s"], 1e-30)}}
+                "ess_per_s_learned_over_fixed": {
+                    name: learned[name]["ess_per_s"] / max(out["fixed"][name]["ess_per_s"], 1e-30)
+                    for name in ("above_100p0", "above_p_label")},
+                "ess_per_s_learned_over_plain": {
+                    name: learned[name]["ess_per_s"] / max(out["plain"][name]["ess_per_s"], 1e-30)
+                    for name in ("above_100p0", "above_p_label")}}}
     print(json.dumps(line), flush=True)
 
 

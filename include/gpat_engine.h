@@ -286,7 +286,8 @@ int gpat_inject_particles_at_large(gpat_handle_t *h, int quantity, int64_t nptl,
                                    int64_t *ninjected);
 
 /* Particle exchange with the host (e.g. restart files, the Fortran ptls
- * array).  put replaces the whole particle set. */
+ * array).  put replaces the whole particle set and raises the injection
+ * counter (tag_max) past the largest tag_injected it receives. */
 int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n);
 int gpat_get_particles(gpat_handle_t *h, gpat_particles_t *dst, int64_t capacity,
                        int64_t *n);

@@ -1263,6 +1263,12 @@ int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n)
     CK(cudaStreamSynchronize(h->stream));
     h->n = n;
     h->unsorted = true;
+    // the injection counter moves past every tag received, so later
+    // injections do not repeat a tag and per-tag tables (labels of learned
+    // splitting) cover them
+    int64_t top = -1;
+    for (int64_t i = 0; i < n; ++i) top = std::max<int64_t>(top, src->tag_injected[i]);
+    h->tag_max = std::max<int64_t>(h->tag_max, top + 1);
     return GPAT_OK;
 }
 

@@ -653,15 +653,17 @@ __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n = (int64_t)*n_dev;
     int esc = 0;
+    bool done = false;
     if (i < n) {
         const int flag = P.count_flag[i];
         int32_t key = -1;
         const bool spatial = !g.done_bin || g.all_active || *g.nactive == 0ull ||
                              (i < g.n_moved && g.pause[i] != 0);
         if (flag == 1 && !spatial) {
-            // finished the interval: the trailing done bin
+            // finished the interval: the trailing done bin (counted per warp
+            // below: most particles of a late chunk land in this one bin)
             key = (int32_t)(cell_grid_bins(g) - 1);
-            atomicAdd(&counts[key], 1u);
+            done = true;
         } else if (flag == 1 && g.tile) {
             // the mover's own cell (cell_of), so the particle lands in the
             // brick whose records are staged for it; clamped into the grid
@@ -701,6 +703,9 @@ __global__ void __launch_bounds__(256) cell_key_kernel(const DevParticles P, int
         }
         keys[i] = key;
     }
+    const unsigned dm = __ballot_sync(0xffffffffu, done);
+    if ((threadIdx.x & 31) == 0 && dm)
+        atomicAdd(&counts[cell_grid_bins(g) - 1], (unsigned)__popc(dm));
     const unsigned e = __ballot_sync(0xffffffffu, esc);
     if ((threadIdx.x & 31) == 0 && e) atomicAdd(&cnt->nescaped, (unsigned long long)__popc(e));
 }
@@ -768,17 +773,28 @@ __global__ void __launch_bounds__(kBinScanThreads) bin_tile_scan_kernel(unsigned
     }
 }
 
+// done_key: the trailing done bin (-1: none), whose slots are reserved per
+// warp, one atomic for all its lanes that go there.
 __global__ void __launch_bounds__(256) cell_scatter_kernel(const DevParticles S, const DevParticles D,
                                                            int64_t n,
                                                            const unsigned long long *n_dev,
                                                            const int32_t *keys,
-                                                           unsigned int *cursor) {
+                                                           unsigned int *cursor, int32_t done_key) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n_dev) n = (int64_t)*n_dev;
-    if (i >= n) return;
-    const int32_t key = keys[i];
+    const int32_t key = i < n ? keys[i] : -1;
+    const unsigned dm = __ballot_sync(0xffffffffu, key >= 0 && key == done_key);
+    unsigned int pos = 0;
+    if (dm) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(dm) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[done_key], (unsigned)__popc(dm));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        pos = base + (unsigned)__popc(dm & ((1u << lane) - 1u));
+    }
     if (key < 0) return;
-    const unsigned int pos = atomicAdd(&cursor[key], 1u);
+    if (key != done_key) pos = atomicAdd(&cursor[key], 1u);
     copy_particle(S, i, D, (int64_t)pos);
 }
 
@@ -819,7 +835,8 @@ cudaError_t launch_cell_sort(const DevParticles &src, const DevParticles &dst, i
     bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
     tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
     bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
-    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, n, nullptr, keys, counts);
+    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, n, nullptr, keys, counts,
+                                               g.done_bin ? (int32_t)(nbins - 1) : -1);
     return cudaGetLastError();
 }
 
@@ -842,7 +859,8 @@ cudaError_t launch_cell_sort_dev(const DevParticles &src, const DevParticles &ds
     bin_tile_sum_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_sums);
     tile_scan_kernel<<<1, 1024, 0, s>>>(tile_sums, tile_offsets, ntiles, &cnt->nkept);
     bin_tile_scan_kernel<<<(unsigned)ntiles, kBinScanThreads, 0, s>>>(counts, nbins, tile_offsets);
-    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, 0, n_dev, keys, counts);
+    cell_scatter_kernel<<<blocks, 256, 0, s>>>(src, dst, 0, n_dev, keys, counts,
+                                               g.done_bin ? (int32_t)(nbins - 1) : -1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(n_dev, &cnt->nkept, sizeof(unsigned long long),
