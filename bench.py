@@ -896,7 +896,7 @@ def run_learned(args, world, rank, local):
                 "ess_per_s_learned_over_plain": {
                     name: learned[name]["ess_per_s"] / max(out["plain"][name]["ess_per_s"], 1e-30)
                     for name in ("above_100p0", "above_p_label")}}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # Keys of a workload's own line kept when it is reported inside the headline.
@@ -907,7 +907,8 @@ EXTRA_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "cloc
 def other_configs(args, local) -> dict:
     """The 3D compressible turbulence (256^3, 1e8 particles) and the batch of
     64 turbulent-shock runs, each measured for one timed MHD interval after
-    one warm-up interval with the same mover options, for the headline line."""
+    one warm-up interval with the same mover options, and the learned
+    splitting comparison at a tenth of its size, for the headline line."""
     out = {}
     common = dict(steps=1, warmup=1, e2e_steps=0, no_cpu_baseline=True, scale=1.0, grid=2048)
     a3 = argparse.Namespace(**{**vars(args), **common, "workload": "turbulence_3d",
@@ -918,6 +919,14 @@ def other_configs(args, local) -> dict:
                                "no_accuracy": False})
     lb = run_batch(ab, 1, 0, local)
     out["batched_shock_2d_64"] = {k: lb[k] for k in EXTRA_KEYS if k in lb}
+    # learned vs fixed-threshold splitting on the 3D field at a tenth of the
+    # full comparison's particles (1e6 training trajectories, 1e5 particles
+    # per split-precision arm, 2e4 per FP64 judge, 100 intervals)
+    al = argparse.Namespace(**{**vars(args), "workload": "learned_3d", "scale": 0.1,
+                               "grid": 2048, "tiles": "off"})
+    ll = run_learned(al, 1, 0, local)
+    out["learned_3d_scale_0.1"] = {k: ll[k] for k in ("value", "unit", "ms_per_step", "config",
+                                                      "clocks", "learned_splitting")}
     return out
 
 
@@ -931,7 +940,9 @@ def main():
         if line is not None:
             print(json.dumps(line), flush=True)
     elif args.workload == "learned_3d":
-        run_learned(args, world, rank, local)
+        line = run_learned(args, world, rank, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
     else:
         line = run_ours(args, world, rank, local)
         if line is not None and args.workload == "turbulent_shock_2d" and not args.no_extras \
