@@ -712,13 +712,14 @@ def run_learned(args, world, rank, local):
                    separate split kernel after each interval: the FP64 judge
                    with samples in the tail.
     Each reports, above 100 p0 and above p_label, the weighted fraction, its
-    Monte Carlo error and the effective samples (sum w)^2 / sum w^2 per
-    second."""
+    Monte Carlo error and the effective samples per second, with one sample
+    per injected particle (the tail weight of all its descendants)."""
     import numpy as np
     import torch
     from gpat import configs
     from gpat.engine import (FusedWindow, GPATCapacityError, Mlp, mover_learned_stats,
-                             set_mover_learned, tail_weights, weighted_split, window_params)
+                             set_mover_learned, tail_by_ancestor, tail_weights, weighted_split,
+                             window_params)
 
     torch.cuda.set_device(local)
     n_train = max(1000, int(args.train_trajectories * args.scale))
@@ -839,10 +840,15 @@ def run_learned(args, world, rank, local):
         _, wall, _ = tail_weights(e, 0.0)
         d["total_weight_over_injected"] = wall / n
         for name, thr in (("above_100p0", pyield), ("above_p_label", p_label)):
-            c, ws, w2 = tail_weights(e, thr)
-            ess = ws * ws / w2 if w2 > 0 else 0.0
-            d[name] = {"particles": c, "fraction": ws / n, "sigma": math.sqrt(w2) / n,
-                       "ess": ess, "ess_per_s": ess / secs}
+            # one sample per injected particle: split copies share their
+            # parent's history (the per-particle (sum w)^2 / sum w^2 is kept
+            # as ess_particles, which overstates the samples of split runs)
+            a = tail_by_ancestor(e, thr, n)
+            _, ws, w2 = tail_weights(e, thr)
+            d[name] = {"particles": a["particles"], "ancestors": a["ancestors"],
+                       "fraction": a["fraction"], "sigma": a["sigma"], "ess": a["ess"],
+                       "ess_per_s": a["ess"] / secs,
+                       "ess_particles": ws * ws / w2 if w2 > 0 else 0.0}
         out[kind] = d
         print(f"learned_3d: {kind} " + json.dumps(d), file=sys.stderr, flush=True)
         e.close()

@@ -818,3 +818,26 @@ def tail_weights(eng, p_threshold):
     eng._check(eng.lib.gpat_tail_weights(eng.h, p_threshold, C.byref(n), C.byref(w),
                                          C.byref(w2)))
     return n.value, w.value, w2.value
+
+
+def tail_by_ancestor(eng, p_threshold, n_injected):
+    """Tail statistics of a run with splitting, one sample per injected
+    particle.  Copies split from one parent share its history, so the
+    particles of a lineage are not independent samples: the tail weight W_a
+    of all live descendants (same tag_injected) of each of the n_injected
+    ancestors is.  Returns the tail fraction sum(W_a) / n_injected, its Monte
+    Carlo error sqrt(sum W_a^2) / n_injected, the effective sample size
+    (sum W_a)^2 / sum W_a^2, and the numbers of tail particles and of
+    ancestors with descendants in the tail."""
+    ps = eng.get_particles()
+    m = (ps["count_flag"] == 1) & (ps["p"] > p_threshold)
+    tags = ps["tag_injected"][m].astype(np.int64)
+    w = ps["weight"][m]
+    if len(w) == 0:
+        return dict(fraction=0.0, sigma=0.0, ess=0.0, particles=0, ancestors=0)
+    _, inv = np.unique(tags, return_inverse=True)
+    W = np.bincount(inv, weights=w)
+    s1, s2 = float(W.sum()), float((W * W).sum())
+    return dict(fraction=s1 / n_injected, sigma=math.sqrt(s2) / n_injected,
+                ess=s1 * s1 / s2 if s2 > 0 else 0.0, particles=int(m.sum()),
+                ancestors=int(len(W)))
