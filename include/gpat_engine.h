@@ -555,7 +555,9 @@ int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_
  * (j <= max_level, children appended up to nptl_max), below it survives
  * with probability w / w_t at weight w_t (roulette draws are Philox,
  * keyed by the particle's tags and push counter).  Both keep the expected
- * weight of every particle. */
+ * weight of every particle.  Copies split past the 30 binary levels of the
+ * int32 tag take tag_splitted = -id from a per-handle counter (ids past the
+ * most negative tag a gpat_put_particles set holds). */
 int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
                         double z_floor, double window_ratio, int max_level, int64_t *nsplit,
                         int64_t *nkilled);

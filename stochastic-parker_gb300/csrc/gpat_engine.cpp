@@ -75,6 +75,10 @@ struct gpat_handle {
     FusedLearn learn{};
     unsigned long long *learn_dev = nullptr;
     unsigned long long learn_host[6] = {};
+    // weighted splitting's next fresh lineage id (device), and the floor a
+    // received particle set puts under it (the most negative tag_splitted)
+    unsigned long long *fresh_dev = nullptr;
+    unsigned long long fresh_floor = 0;
     int64_t learn_split = 0, learn_killed = 0;
     int64_t n_active = 0;
     int64_t last_sort_bins = 0;
@@ -733,6 +737,7 @@ int gpat_destroy(gpat_handle_t *h) {
     if (h->tile_dev) cudaFree(h->tile_dev);
     if (h->pause) cudaFree(h->pause);
     if (h->learn_dev) cudaFree(h->learn_dev);
+    if (h->fresh_dev) cudaFree(h->fresh_dev);
     if (h->tile_ovf) cudaFree(h->tile_ovf);
     for (int s = 0; s < 2; ++s)
         if (h->planes[s]) cudaFree(h->planes[s]);
@@ -1266,9 +1271,14 @@ int gpat_put_particles(gpat_handle_t *h, const gpat_particles_t *src, int64_t n)
     // the injection counter moves past every tag received, so later
     // injections do not repeat a tag and per-tag tables (labels of learned
     // splitting) cover them
-    int64_t top = -1;
-    for (int64_t i = 0; i < n; ++i) top = std::max<int64_t>(top, src->tag_injected[i]);
+    int64_t top = -1, low = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        top = std::max<int64_t>(top, src->tag_injected[i]);
+        low = std::min<int64_t>(low, src->tag_splitted[i]);
+    }
     h->tag_max = std::max<int64_t>(h->tag_max, top + 1);
+    // weighted splitting hands out lineage ids past the most negative tag
+    h->fresh_floor = std::max<unsigned long long>(h->fresh_floor, (unsigned long long)(-low));
     return GPAT_OK;
 }
 
@@ -2803,6 +2813,35 @@ int gpat_mlp_score(gpat_mlp_t *m, gpat_handle_t *h, double t_norm, double *mean_
     return GPAT_OK;
 }
 
+namespace {
+
+// The device counter of weighted splitting's fresh lineage ids (copies split
+// past the int32 tag's 30 binary levels get tag_splitted = -id), created at
+// first use and raised past the ids of any particle set received since.
+int ensure_fresh(gpat_handle_t *h) {
+    if (!h->fresh_dev) {
+        if (cudaMalloc(&h->fresh_dev, sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, GPAT_ERR_OOM, "lineage id counter");
+        }
+        CK(cudaMemsetAsync(h->fresh_dev, 0, sizeof(unsigned long long), h->stream));
+    }
+    if (h->fresh_floor > 0) {
+        unsigned long long cur = 0;
+        CK(cudaMemcpyAsync(&cur, h->fresh_dev, sizeof cur, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (cur < h->fresh_floor) {
+            cur = h->fresh_floor;
+            CK(cudaMemcpyAsync(h->fresh_dev, &cur, sizeof cur, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        h->fresh_floor = 0;
+    }
+    return GPAT_OK;
+}
+
+}  // namespace
+
 int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w_ref, double z_ref,
                         double z_floor, double window_ratio, int max_level, int64_t *nsplit,
                         int64_t *nkilled) {
@@ -2814,10 +2853,13 @@ int gpat_weighted_split(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, double w
     CK(cudaSetDevice(h->device));
     if (cudaStreamSynchronize(m->stream) != cudaSuccess)
         return fail(h, GPAT_ERR_CUDA, "network stream");
-    int rc = pull_counters(h);
+    int rc = ensure_fresh(h);
+    if (rc) return rc;
+    rc = pull_counters(h);
     if (rc) return rc;
     const unsigned long long split0 = h->hcnt.nsplit, kill0 = h->hcnt.nkilled;
     WSplitArgs a{};
+    a.fresh = h->fresh_dev;
     a.w_ref = w_ref;
     a.z_ref = z_ref;
     a.z_floor = z_floor;
@@ -2865,6 +2907,8 @@ int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, doubl
     }
     if (cudaStreamSynchronize(m->stream) != cudaSuccess)
         return fail(h, GPAT_ERR_CUDA, "network stream");
+    const int rcf = ensure_fresh(h);
+    if (rcf) return rcf;
     FusedLearn L{};
     L.w16 = m->w16;
     L.norm = m->norm;
@@ -2876,6 +2920,7 @@ int gpat_set_mover_learned(gpat_handle_t *h, gpat_mlp_t *m, double t_norm, doubl
     L.s.max_level = max_level;
     L.s.key0 = (uint32_t)h->prm.seed;
     L.s.key1 = (uint32_t)(h->prm.seed >> 32) + 2u;
+    L.s.fresh = h->fresh_dev;
     L.z_shift = z_ref;
     h->learn = L;
     h->learn_on = true;

@@ -182,6 +182,9 @@ struct WSplitArgs {
     double w_ref, z_ref, z_floor, sqrt_ratio;
     int max_level;
     uint32_t key0, key1;
+    // lineage ids handed to copies split past the int32 tag's 30 binary
+    // levels (their tag_splitted is minus the id); null: no split there
+    unsigned long long *fresh;
 };
 // Learned splitting inside the split-precision mover: particles that finish
 // the interval in the box are scored by the network and split or played

@@ -10,6 +10,9 @@ namespace gpat {
 namespace {
 
 constexpr int kIn = kMlpFeatures, kH = kMlpHidden;
+// Fresh lineage ids stop here: the concurrent additions that can pass the
+// check (every resident thread x 255 copies) stay below 2^31.
+constexpr unsigned long long kFreshIdLimit = 2000000000ull;
 
 __device__ __forceinline__ void clone_particle(const DevParticles &P, int64_t i, int64_t j) {
     P.x[j] = P.x[i]; P.y[j] = P.y[i]; P.z[j] = P.z[i]; P.p[j] = P.p[i];
@@ -91,6 +94,7 @@ __device__ __forceinline__ void window_split(const WSplitArgs &a, const DevParti
                                              bool live, float z, int64_t cap,
                                              unsigned long long *count, DevCounters *cnt) {
     int j = 0;
+    bool fresh = false;
     double w = 0.0;
     if (live) {
         const double wt = a.w_ref * exp(-(floored_importance((double)z, a.z_floor) - a.z_ref));
@@ -99,8 +103,13 @@ __device__ __forceinline__ void window_split(const WSplitArgs &a, const DevParti
             const int split_times = P.split_times[i];
             j = (int)ceil(log2(w / (wt * a.sqrt_ratio)));
             j = max(1, min(j, a.max_level));
-            j = min(j, 30 - split_times);          // int32 lineage tags
-            if (j < 1) j = 0;
+            if (split_times + j > 30) {
+                // past the int32 tag's 30 binary levels the copies take fresh
+                // negative ids (every copy keeps a distinct Philox stream);
+                // the ids stop short of the int32 range
+                if (!a.fresh || *(volatile unsigned long long *)a.fresh > kFreshIdLimit) j = 0;
+                else fresh = true;
+            }
         } else if (w < wt / a.sqrt_ratio) {
             const uint4 r = philox4x32_10(
                 make_uint4(P.rng_ctr[i], 0x524C5454u, (uint32_t)P.tag_injected[i],
@@ -142,11 +151,13 @@ __device__ __forceinline__ void window_split(const WSplitArgs &a, const DevParti
     const int s = P.split_times[i];
     const double wc = w / (double)(1u << j);
     P.weight[i] = wc;
-    P.split_times[i] = (int8_t)(s + j);
+    P.split_times[i] = (int8_t)min(s + j, 120);
+    const unsigned long long id0 = fresh ? atomicAdd(a.fresh, (unsigned long long)m) : 0ull;
     for (unsigned c = 1; c <= m; ++c) {
         const int64_t d = first + (int64_t)(c - 1);
         clone_particle(P, i, d);
-        P.tag_splitted[d] = (int32_t)((uint32_t)P.tag_splitted[i] + (c << s));
+        P.tag_splitted[d] = fresh ? -(int32_t)(id0 + c)
+                                  : (int32_t)((uint32_t)P.tag_splitted[i] + (c << s));
     }
     atomicAdd(&cnt->nsplit, (unsigned long long)m);
 }

@@ -187,3 +187,61 @@ def test_learned_splitting_fused_in_the_mover():
     for e in (plain, eng):
         e.close()
     net.close()
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_splits_past_thirty_levels_take_fresh_lineage_ids(fused):
+    """Copies split past the int32 tag's 30 binary levels take fresh negative
+    tag_splitted ids: every (tag_injected, tag_splitted) pair stays unique
+    (so every copy keeps its own Philox stream), the total weight is kept in
+    expectation, and an engine that receives such a set hands out ids past
+    the ones it holds."""
+    from gpat.engine import FusedWindow, mover_learned_stats, set_mover_learned
+    n_grid, nptl, nint = 32, 20000, 2
+    w = configs.turbulence_3d(scale=nptl / 1e8, n=n_grid, nframes=4)
+    net = Mlp(seed=11)   # an untrained network: z varies a little with the features
+
+    def split_run(eng, target):
+        if fused:
+            win = FusedWindow(target, DEFENSIVE)
+            win.start(*net.score(eng, 0.0)[1:])
+        for k in range(nint):
+            if fused:
+                z_ref, z_floor = win.params()
+                set_mover_learned(eng, net, (k + 1) / 4, 1.0, z_ref, 4.0, 3, z_floor=z_floor)
+                eng.particle_mover(mhd_tframe=k + 1)
+                win.update(mover_learned_stats(eng))
+            else:
+                _, lse, lsw = net.score(eng, k / 4)
+                z_ref, z_floor = window_params(lse, lsw, target, DEFENSIVE)
+                weighted_split(eng, net, k / 4, 1.0, z_ref, 4.0, 3, z_floor=z_floor)
+                eng.particle_mover(mhd_tframe=k + 1)
+        set_mover_learned(eng, None)
+        return eng.get_particles()
+
+    def unique_keys(ps):
+        key = (ps["tag_injected"].astype(np.int64) << 32) | \
+              (ps["tag_splitted"].astype(np.int64) & 0xFFFFFFFF)
+        return len(np.unique(key)) == len(key)
+
+    eng = configs.build_engine(w, nptl_max=nptl * 40)
+    configs.inject(eng, w)
+    ps = eng.get_particles()
+    ps.arrays["split_times"][:] = 30   # every split is past the 30 levels
+    eng.put_particles(ps)
+    out = split_run(eng, 4 * nptl)   # w / w_t ~ 4: particles above the window split once
+    neg = out["tag_splitted"] < 0
+    assert neg.sum() > nptl // 4, neg.sum()
+    assert len(np.unique(out["tag_splitted"][neg])) == neg.sum()
+    assert unique_keys(out)
+    assert abs(out["weight"].sum() - nptl) < 0.15 * nptl
+    # a second engine receiving the set continues past its ids
+    eng2 = configs.build_engine(w, nptl_max=nptl * 40)
+    eng2.put_particles(out)
+    lowest = int(out["tag_splitted"].min())
+    out2 = split_run(eng2, 16 * nptl)   # the received weights (~0.5) split again
+    new = out2["tag_splitted"] < lowest
+    assert new.sum() > 0 and unique_keys(out2)
+    for e in (eng, eng2):
+        e.close()
+    net.close()
