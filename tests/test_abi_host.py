@@ -288,3 +288,70 @@ def test_fortran_interface_check_catches_a_mismatch():
     cargs = _c_prototypes(HEADER.read_text())[name][1]
     assert cargs[i] == "i64"
     assert not _same_kind("i32", cargs[i])
+
+
+def _py_kind(t):
+    """The kind of a ctypes argument type, in the notation of _c_kind."""
+    if t is C.c_void_p:
+        return "ptr"
+    if t is C.c_char_p:
+        return "char*"
+    scalars = {C.c_int: "i32", C.c_int32: "i32", C.c_int64: "i64", C.c_uint64: "i64",
+               C.c_int8: "i8", C.c_uint32: "u32", C.c_double: "f64", C.c_float: "f32",
+               C.c_char: "char"}
+    for k, v in scalars.items():
+        if t is k:
+            return v
+    if isinstance(t, type) and issubclass(t, C._Pointer):
+        return _py_kind(t._type_) + "*"
+    if isinstance(t, type) and issubclass(t, C.Structure):
+        return "struct"
+    raise AssertionError(f"unmapped ctypes type {t}")
+
+
+def _py_matches_c(p, c):
+    if p == c:
+        return True
+    c = c.replace("uint32_t", "u32").replace("uint8_t", "i8")
+    if p == c:
+        return True
+    # a structure pointer stands for the header's gpat_*_t pointer of the
+    # same depth; an opaque handle pointer for void *
+    if p.startswith("struct") and c.startswith("gpat_"):
+        return p.count("*") == c.count("*")
+    return p == "ptr" and c.endswith("*") and c.count("*") == 1
+
+
+def _binding_mismatches(signatures):
+    cproto = _c_prototypes(HEADER.read_text())
+    bad = sorted(set(signatures) ^ set(cproto))
+    for name, (_, args) in sorted(signatures.items()):
+        if name not in cproto:
+            continue
+        cargs = cproto[name][1]
+        if len(args) != len(cargs):
+            bad.append((name, len(args), len(cargs)))
+            continue
+        for i, (t, c) in enumerate(zip(args, cargs)):
+            if not _py_matches_c(_py_kind(t), c):
+                bad.append((name, i, _py_kind(t), c))
+    return bad
+
+
+def test_python_bindings_match_c_prototypes():
+    """Every ctypes declaration in gpat/_abi.py has the header prototype's
+    argument count, scalar types and pointer depths, so a changed signature
+    cannot go unnoticed by the Python callers."""
+    assert _binding_mismatches(_abi.SIGNATURES) == []
+
+
+def test_python_binding_check_catches_a_mismatch():
+    """Dropping an argument or narrowing an int64_t to int fails the check."""
+    sigs = dict(_abi.SIGNATURES)
+    res, args = sigs["gpat_weighted_split"]
+    sigs["gpat_weighted_split"] = (res, args[:5] + args[6:])          # no z_floor
+    res, args = sigs["gpat_put_particles"]
+    sigs["gpat_put_particles"] = (res, args[:2] + [C.c_int])           # int64_t n as int
+    bad = _binding_mismatches(sigs)
+    assert any(b[0] == "gpat_weighted_split" for b in bad)
+    assert any(b[0] == "gpat_put_particles" for b in bad)
