@@ -96,7 +96,7 @@ def parse_args(argv=None):
                     help="learned_3d: intervals between training records of a trajectory "
                          "(0: ten records over the run)")
     ap.add_argument("--fp64-particles", type=float, default=2e5,
-                    help="learned_3d: particles of the FP64 judge")
+                    help="learned_3d: particles of the FP64 reference arms")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline workload only (no 3D and batched keys in its line)")
     ap.add_argument("--tiles-3d", default="off",
@@ -707,10 +707,10 @@ def run_learned(args, world, rank, local):
                    as particles finish each interval (weight window 4, the
                    particle cap of 4e8, importance exp(z) floored at
                    DEFENSIVE times its weighted mean);
-      fp64         the FP64 mover, no splitting: the independent judge;
+      fp64         the FP64 mover, no splitting: the independent reference;
       fp64_learned the FP64 mover with the same network applied by the
-                   separate split kernel after each interval: the FP64 judge
-                   with samples in the tail.
+                   separate split kernel after each interval: the FP64
+                   reference with samples in the tail.
     Each reports, above 100 p0 and above p_label, the weighted fraction, its
     Monte Carlo error and the effective samples per second, with one sample
     per injected particle (the tail weight of all its descendants)."""
@@ -855,14 +855,14 @@ def run_learned(args, world, rank, local):
     clk = clocks.stop()
     net.close()
     for name in ("above_100p0", "above_p_label"):
-        for judge in ("fp64", "fp64_learned"):
-            j = out[judge][name]
+        for ref in ("fp64", "fp64_learned"):
+            j = out[ref][name]
             for kind in ("plain", "fixed", "learned", "fp64_learned"):
-                if kind == judge or j["fraction"] <= 0:
+                if kind == ref or j["fraction"] <= 0:
                     continue
                 d = out[kind][name]
-                d[f"err_vs_{judge}"] = d["fraction"] / j["fraction"] - 1.0
-                d[f"err_sigma_vs_{judge}"] = math.hypot(d["sigma"], j["sigma"]) / j["fraction"]
+                d[f"err_vs_{ref}"] = d["fraction"] / j["fraction"] - 1.0
+                d[f"err_sigma_vs_{ref}"] = math.hypot(d["sigma"], j["sigma"]) / j["fraction"]
     if rank != 0:
         return
     learned = out["learned"]
@@ -892,7 +892,7 @@ def run_learned(args, world, rank, local):
                              "record_every_intervals": every, "plain_run_seconds": train_s,
                              "fit_seconds": fit_s, "final_loss": loss, "epochs": 3},
                 "fixed_threshold": {"split_ratio": fixed_ratio, "pmin_split": fixed_pmin},
-                "judges": {"fp64": "FP64 mover, no splitting (independent of the method)",
+                "fp64_references": {"fp64": "FP64 mover, no splitting (independent of the method)",
                            "fp64_learned": "FP64 mover with the network applied by the "
                                            "separate split kernel (tail samples)"},
                 "arms": out,
@@ -927,7 +927,7 @@ def other_configs(args, local) -> dict:
     out["batched_shock_2d_64"] = {k: lb[k] for k in EXTRA_KEYS if k in lb}
     # learned vs fixed-threshold splitting on the 3D field at a tenth of the
     # full comparison's particles (1e6 training trajectories, 1e5 particles
-    # per split-precision arm, 2e4 per FP64 judge, 100 intervals)
+    # per split-precision arm, 2e4 per FP64 reference arm, 100 intervals)
     al = argparse.Namespace(**{**vars(args), "workload": "learned_3d", "scale": 0.1,
                                "grid": 2048, "tiles": "off"})
     ll = run_learned(al, 1, 0, local)
