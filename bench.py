@@ -892,9 +892,10 @@ def run_learned(args, world, rank, local):
                              "record_every_intervals": every, "plain_run_seconds": train_s,
                              "fit_seconds": fit_s, "final_loss": loss, "epochs": 3},
                 "fixed_threshold": {"split_ratio": fixed_ratio, "pmin_split": fixed_pmin},
-                "fp64_references": {"fp64": "FP64 mover, no splitting (independent of the method)",
-                           "fp64_learned": "FP64 mover with the network applied by the "
-                                           "separate split kernel (tail samples)"},
+                "fp64_references": {
+                    "fp64": "FP64 mover, no splitting (independent of the method)",
+                    "fp64_learned": "FP64 mover with the network applied by the separate "
+                                    "split kernel (tail samples)"},
                 "arms": out,
                 "ess_per_s_learned_over_fixed": {
                     name: learned[name]["ess_per_s"] / max(out["fixed"][name]["ess_per_s"], 1e-30)
