@@ -282,3 +282,26 @@ def test_pushes_longer_than_a_period_stay_in_the_box():
     assert v["x"].min() >= 0.0 and v["x"].max() <= 1.0
     assert v["y"].min() >= 0.0 and v["y"].max() <= 1.0
     assert 20 * 1000 <= cnt.steps <= 21 * 1000
+
+
+def test_pushes_longer_than_a_period_stay_in_the_box_3d():
+    """The same in 3D, where the wrap acts on z too: κ 1000 at dt = dt_out / 20
+    on a periodic unit cube with a turbulent frame."""
+    n = 16
+    cfg = make_mhd_config(n, n, n, 0.0, 1.0, 0.0, 1.0, zmin=0.0, zmax=1.0, dt_out=0.02, ndim=3)
+    prm = make_params(ndim=3, p0=0.1, pmin=0.1, pmax=100.0, kpara0=1000.0, kret=0.1,
+                      dt_min_rel=0.05, dt_max_rel=0.05, pbcx=0, pbcy=0, pbcz=0,
+                      momentum_dependency=0, nptl_max=1000, seed=5)
+    frame = fields.turbulence_3d(n, seed=7)
+    oprm = oracle.params_from(prm)
+    parts = oracle.Particles(1000)
+    cnt = oracle.OrcCounters()
+    oracle.inject_spatial_uniform(oprm, parts, 500, 1e-3, 1, 1.0, 0.0, 0.0,
+                                  (0.0, 0.0, 0.0, 1.0, 1.0, 1.0), cnt)
+    oracle.mover(oprm, oracle.config_from(cfg), oracle.full_fields(frame, 3, cfg), parts, 0.0,
+                 0.02, counters=cnt)
+    v = parts.view()
+    assert parts.n == 500 and (v["count_flag"] == 1).all()
+    for k in ("x", "y", "z"):
+        assert v[k].min() >= 0.0 and v[k].max() <= 1.0, k
+    assert 20 * 500 <= cnt.steps <= 21 * 500
