@@ -918,22 +918,41 @@ def other_configs(args, local) -> dict:
     splitting comparison at a tenth of its size, for the headline line."""
     out = {}
     common = dict(steps=1, warmup=1, e2e_steps=0, no_cpu_baseline=True, scale=1.0, grid=2048)
-    a3 = argparse.Namespace(**{**vars(args), **common, "workload": "turbulence_3d",
-                               "no_accuracy": True, "tiles": args.tiles_3d})
-    l3 = run_ours(a3, 1, 0, local)
-    out["turbulence_3d_256"] = {k: l3[k] for k in EXTRA_KEYS if k in l3}
-    ab = argparse.Namespace(**{**vars(args), **common, "workload": "batched_shock_2d",
-                               "no_accuracy": False})
-    lb = run_batch(ab, 1, 0, local)
-    out["batched_shock_2d_64"] = {k: lb[k] for k in EXTRA_KEYS if k in lb}
-    # learned vs fixed-threshold splitting on the 3D field at a tenth of the
-    # full comparison's particles (1e6 training trajectories, 1e5 particles
-    # per split-precision arm, 2e4 per FP64 reference arm, 100 intervals)
-    al = argparse.Namespace(**{**vars(args), "workload": "learned_3d", "scale": 0.1,
-                               "grid": 2048, "tiles": "off"})
-    ll = run_learned(al, 1, 0, local)
-    out["learned_3d_scale_0.1"] = {k: ll[k] for k in ("value", "unit", "ms_per_step", "config",
-                                                      "clocks", "learned_splitting")}
+
+    def extra(key, fn):
+        # a failing extra is recorded in the line, which the headline keeps
+        try:
+            out[key] = fn()
+        except Exception as e:  # noqa: BLE001 - reported, not hidden
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+            print(f"bench: {key} failed: {e}", file=sys.stderr, flush=True)
+
+    def turbulence_3d():
+        a3 = argparse.Namespace(**{**vars(args), **common, "workload": "turbulence_3d",
+                                   "no_accuracy": True, "tiles": args.tiles_3d})
+        l3 = run_ours(a3, 1, 0, local)
+        return {k: l3[k] for k in EXTRA_KEYS if k in l3}
+
+    def batched():
+        ab = argparse.Namespace(**{**vars(args), **common, "workload": "batched_shock_2d",
+                                   "no_accuracy": False})
+        lb = run_batch(ab, 1, 0, local)
+        return {k: lb[k] for k in EXTRA_KEYS if k in lb}
+
+    def learned():
+        # learned vs fixed-threshold splitting on the 3D field at a tenth of
+        # the full comparison's particles (1e6 training trajectories, 1e5
+        # particles per split-precision arm, 2e4 per FP64 reference arm,
+        # 100 intervals)
+        al = argparse.Namespace(**{**vars(args), "workload": "learned_3d", "scale": 0.1,
+                                   "grid": 2048, "tiles": "off"})
+        ll = run_learned(al, 1, 0, local)
+        return {k: ll[k] for k in ("value", "unit", "ms_per_step", "config", "clocks",
+                                   "learned_splitting")}
+
+    extra("turbulence_3d_256", turbulence_3d)
+    extra("batched_shock_2d_64", batched)
+    extra("learned_3d_scale_0.1", learned)
     return out
 
 

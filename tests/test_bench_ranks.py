@@ -64,3 +64,36 @@ def test_replicas_have_distinct_seeds():
     args = bench.parse_args(["--grid", "64", "--scale", "1e-4"])
     seeds = {bench.make_workload(args, 1, seed=2 + r, nframes=1).params["seed"] for r in range(2)}
     assert len(seeds) == 2
+
+
+def test_headline_extras_record_a_failure(monkeypatch):
+    """The headline line's extra configurations: each is measured by its own
+    workload function, a failing one is recorded with its error, and the
+    others (and the headline) are kept."""
+    sys.path[:0] = [str(REPO), str(REPO / "stochastic-parker_gb300")]
+    import bench
+    seen = []
+
+    def fake_ours(a, world, rank, local):
+        seen.append((a.workload, a.steps, a.warmup, a.no_accuracy))
+        return {"value": 1.0, "unit": "particle-steps/s", "config": {"workload": a.workload},
+                "not_kept": 0}
+
+    def fake_batch(a, world, rank, local):
+        raise RuntimeError("out of memory")
+
+    def fake_learned(a, world, rank, local):
+        seen.append((a.workload, a.scale))
+        return {"value": 2.0, "unit": "particle-steps/s", "ms_per_step": 1.0, "config": {},
+                "clocks": {}, "learned_splitting": {"arms": {}}}
+
+    monkeypatch.setattr(bench, "run_ours", fake_ours)
+    monkeypatch.setattr(bench, "run_batch", fake_batch)
+    monkeypatch.setattr(bench, "run_learned", fake_learned)
+    args = bench.parse_args([])
+    out = bench.other_configs(args, 0)
+    assert out["turbulence_3d_256"] == {"value": 1.0, "unit": "particle-steps/s",
+                                        "config": {"workload": "turbulence_3d"}}
+    assert out["batched_shock_2d_64"] == {"error": "RuntimeError: out of memory"}
+    assert out["learned_3d_scale_0.1"]["value"] == 2.0
+    assert ("turbulence_3d", 1, 1, True) in seen and ("learned_3d", 0.1) in seen
